@@ -1,0 +1,390 @@
+#!/usr/bin/env python3
+"""Benchmark of the lossy VarDCT pixel path + SSIMULACRA2 on GB300.
+
+Workload (one "step"): the quality controller's probe — encode transform,
+reconstruct (dequantize, IDCT, Gaborish, 3-step EPF, colour, 8/16-bit depth
+round trip) and SSIMULACRA2 against the precomputed source — over a batch of
+8 distinct 2048x2048 RGB16 synthetic images (seeded; mixed DCT8/16/32 cover;
+CfL; Gaborish; uniform sharpness 7; global_scale 40000).  Source moments for
+the metric are precomputed once per image, outside the timed region, as the
+reference's evaluator does (evaluator.rs:88 -> reference.rs:90).
+
+Prints one JSON line.  `value` is source MPix/s with inputs resident in HBM;
+`e2e` is the same metric through the C ABI with pinned host buffers (the H2D
+copy of each image and the D2H read of each score inside the timed region).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+if str(ROOT) not in sys.path:
+    sys.path.insert(0, str(ROOT))
+
+W, H, BITS = 2048, 2048, 16
+IMAGES_PER_STEP = 8
+GLOBAL_SCALE = 40000
+WORKLOAD = ("2048x2048 RGB16 quality probe: encode transform (XYB, inverse Gaborish, DCT8/16/32, "
+            "CfL, quantize) + reconstruct (Gaborish, 3-step EPF, 16-bit depth) + SSIMULACRA2 "
+            "(6 scales)")
+
+# Algorithmic HBM bytes per source pixel of each stage for this workload
+# (f32 planes, int32 coefficients, RGB16 input); see the design doc.
+STAGE_BYTES_PER_PX = {
+    "xyb": 6 + 12,              # RGB16 in, 3 f32 planes out
+    "precondition": 12 + 12,    # 3 planes in, 3 out
+    "fdct_luma": 12 + 12 + 4 + 4 + 0.5,  # planes in; coeffs, dY, qY out; LF
+    "cfl": 12 + 4,              # coeffs + dY read
+    "quant_chroma": 8 + 4 + 8,  # cX, cB, dY in; qX, qB out
+    "render_varblocks": 12 + 12,  # q in, XYB planes out
+    "gaborish": 12 + 12,
+    "epf": 3 * (12 + 12),       # three steps
+    "colour": 12 + 12,
+    "ssim": (12 + 36) * 4 / 3 + 15,  # candidate + reference moments over the pyramid
+}
+
+
+def shard_units(units: list, rank: int, world: int) -> list:
+    """Replicas: each rank takes a disjoint slice of the images."""
+    return units[rank::world]
+
+
+def max_over_ranks(t: float) -> float:
+    import torch
+    import torch.distributed as dist
+
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return t
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    x = torch.tensor([t], dtype=torch.float64, device=dev)
+    dist.all_reduce(x, op=dist.ReduceOp.MAX)
+    return float(x.item())
+
+
+def barrier() -> None:
+    import torch.distributed as dist
+
+    if dist.is_available() and dist.is_initialized():
+        dist.barrier()
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.proc = None
+        self.lines: list[str] = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            threading.Thread(target=self._read, daemon=True).start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self) -> dict:
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+        mhz, maxes, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                mhz.append(float(parts[1]))
+                maxes.append(float(parts[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(mhz) if mhz else None,
+                "sm_max_mhz": max(maxes) if maxes else None,
+                "reasons": sorted(reasons), "samples": len(mhz)}
+
+
+def measured_peaks() -> tuple[float, str]:
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        return float(json.loads(p.read_text())["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def make_workload(rank: int, world: int):
+    import numpy as np
+
+    from jpxl_gb300 import synth
+
+    seeds = shard_units(list(range(IMAGES_PER_STEP * world)), rank, world)
+    images = []
+    for s in seeds:
+        rgb = synth.synthetic_rgb(W, H, seed=1000 + s, bits=BITS)
+        cover = synth.activity_cover(rgb)
+        images.append((rgb, cover))
+    return images, np
+
+
+def cpu_probe(rgb, cover, np):
+    """The CPU restatement's probe on one image (encode, render at depth, score)."""
+    import jpxl_gb300 as jg
+    from oracle import loader
+
+    h, w = rgb.shape[:2]
+    hf = np.ones(cover.shape, np.uint32)
+    sh = np.full(cover.shape, 7, np.uint8)
+    rc, plan = loader.encode(rgb, cover, hf, global_scale=GLOBAL_SCALE, gaborish=True)
+    assert rc == 0
+    rc, lin = loader.reconstruct(w, h, cover, hf, sh, plan, global_scale=GLOBAL_SCALE,
+                                 gaborish=True, epf_iters=3, out_kind=3, bits=BITS)
+    assert rc == 0
+    src = jg.srgb_to_linear_planes(rgb, BITS)
+    return loader.ssim2(src, lin)[0]
+
+
+CPU_SAMPLE = 512  # crop side of the bounded CPU sample
+
+
+def cpu_sample(images, np):
+    rgb, cover = images[0]
+    crop = np.ascontiguousarray(rgb[:CPU_SAMPLE, :CPU_SAMPLE])
+    from jpxl_gb300 import synth
+
+    return crop, synth.activity_cover(crop)
+
+
+def run_reference(args):
+    """The CPU arm: the restatement of the reference on all host threads."""
+    import concurrent.futures
+
+    import numpy as np
+
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    from oracle import loader
+
+    loader.build()
+    threads = os.cpu_count() or 1
+    images = []
+    from jpxl_gb300 import synth
+
+    for i in range(threads):
+        rgb = synth.synthetic_rgb(CPU_SAMPLE, CPU_SAMPLE, seed=5000 + i, bits=BITS)
+        images.append((rgb, synth.activity_cover(rgb)))
+    pool = concurrent.futures.ThreadPoolExecutor(max_workers=threads)
+
+    def step():
+        list(pool.map(lambda t: cpu_probe(t[0], t[1], np), images))
+
+    for _ in range(args.warmup):
+        step()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        step()
+    dt = time.perf_counter() - t0
+    mpix = CPU_SAMPLE * CPU_SAMPLE * threads * args.steps / 1e6
+    value = mpix / dt
+    sample = (f"{threads} concurrent {CPU_SAMPLE}x{CPU_SAMPLE} RGB16 crops per step, one per "
+              f"host thread, same probe arithmetic as the GPU arm")
+    print(json.dumps({
+        "impl": "reference", "metric": "probe MPix/s (encode+reconstruct+SSIMULACRA2)",
+        "value": round(value, 4), "unit": "MPix/s", "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(dt / args.steps * 1e3, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic", "config": {"workload": WORKLOAD, "images_per_step": threads,
+                                         "image": f"{CPU_SAMPLE}x{CPU_SAMPLE} crops"},
+        "cpu_baseline": {"value": round(value, 4), "unit": "MPix/s", "cores": threads,
+                         "kind": "port", "sample": sample},
+        "e2e": {"value": round(value, 4), "unit": "MPix/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }), flush=True)
+
+
+def run_ours(args):
+    import numpy as np
+    import torch
+    import torch.distributed as dist
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+
+    import jpxl_gb300 as jg
+    from jpxl_gb300 import build
+
+    build.build()
+    images, _ = make_workload(rank, world)
+    ctx = jg.Context(local)
+    stream = torch.cuda.current_stream()
+    ctx.set_stream(stream.cuda_stream)
+    req = jg.EncodeRequest.with_global_scale(GLOBAL_SCALE, gaborish=True, epf_iters=3)
+    layouts, refs, dev_rgb, host_rgb = [], [], [], []
+    for rgb, cover in images:
+        layouts.append(jg.Layout(ctx, W, H, cover, 1, 7))
+        src = torch.from_numpy(jg.srgb_to_linear_planes(rgb, BITS)).cuda()
+        refs.append(jg.PrecomputedReference(ctx, device_ptr=src.data_ptr(), width=W, height=H))
+        torch.cuda.synchronize()
+        del src
+        t = torch.from_numpy(rgb.view(np.int16)).cuda()
+        dev_rgb.append(t)
+        pinned = torch.empty(rgb.shape, dtype=torch.int16, pin_memory=True)
+        pinned.copy_(torch.from_numpy(rgb.view(np.int16)))
+        host_rgb.append(pinned)
+    scores = torch.zeros(len(images), dtype=torch.float64, device="cuda")
+    ctx.synchronize()
+
+    def device_step():
+        for i in range(len(images)):
+            ctx.probe_device(layouts[i], refs[i], dev_rgb[i].data_ptr(), BITS, req,
+                             scores.data_ptr() + 8 * i)
+
+    for _ in range(max(args.warmup, 3)):
+        device_step()
+    ctx.synchronize()
+    ctx.stage_times()  # reset
+    sampler = ClockSampler(local)
+    sampler.start()
+    ctx.stage_timing(True)
+    launches0 = ctx.launches
+    barrier()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        device_step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    barrier()
+    ms = e0.elapsed_time(e1)
+    launches = ctx.launches - launches0
+    ctx.synchronize()
+    stages = ctx.stage_times()
+    ctx.stage_timing(False)
+    clocks = sampler.stop()
+    ms_max = max_over_ranks(ms)
+    px_total = W * H * len(images) * args.steps * world
+    value = px_total / (ms_max / 1e3) / 1e6
+
+    # e2e through the C ABI with pinned host buffers
+    host_scores = []
+
+    def host_step():
+        for i in range(len(images)):
+            host_scores.append(ctx.probe(layouts[i], refs[i], host_rgb[i].numpy().view(np.uint16),
+                                         jg.EncodeRequest.with_global_scale(
+                                             GLOBAL_SCALE, gaborish=True, epf_iters=3), BITS))
+
+    for _ in range(max(args.warmup, 3)):
+        host_step()
+    barrier()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        host_step()
+    torch.cuda.synchronize()
+    e2e_s = max_over_ranks(time.perf_counter() - t0)
+    e2e = px_total / e2e_s / 1e6
+    dev_scores = scores.cpu().numpy()
+    if not np.allclose(dev_scores, host_scores[-len(images):]):
+        raise RuntimeError(f"device and host probes disagree: {dev_scores} {host_scores}")
+
+    if rank != 0:
+        if world > 1:
+            dist.destroy_process_group()
+        return
+    # Roofline of the dominant stage.
+    top = max(stages, key=lambda k: stages[k][0])
+    top_ms, top_launches = stages[top]
+    n_img = len(images) * args.steps
+    bytes_per_launch = STAGE_BYTES_PER_PX[top] * W * H * n_img / max(top_launches, 1)
+    per_launch_s = top_ms / 1e3 / max(top_launches, 1)
+    achieved = bytes_per_launch / per_launch_s / 1e9
+    peak, peak_kind = measured_peaks()
+    traffic = None
+    tf = ROOT / "profiles" / "traffic.json"
+    if tf.exists():
+        traffic = json.loads(tf.read_text()).get(top)
+
+    # CPU baseline: the restatement on a bounded sample, one thread.
+    crop, ccover = cpu_sample(images, np)
+    t0 = time.perf_counter()
+    cpu_probe(crop, ccover, np)
+    cpu_s = time.perf_counter() - t0
+    cpu_value = CPU_SAMPLE * CPU_SAMPLE / cpu_s / 1e6
+
+    line = {
+        "metric": "probe MPix/s (encode+reconstruct+SSIMULACRA2)",
+        "value": round(value, 2), "unit": "MPix/s", "n_gpus": world, "steps": args.steps,
+        "warmup": max(args.warmup, 3), "ms_per_step": round(ms_max / args.steps, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic",
+        "config": {"workload": WORKLOAD, "images_per_step": IMAGES_PER_STEP, "width": W,
+                   "height": H, "bits": BITS, "global_scale": GLOBAL_SCALE,
+                   "cover": "activity DCT8/16/32 (stand-in for select_blocks)",
+                   "l2": "inputs larger than L2: 8 distinct images, 201 MB of RGB16 per step",
+                   "parallelism": f"replicas x{world}"},
+        "stages_ms": {k: round(v[0] / args.steps, 4) for k, v in stages.items()},
+        "roofline": {"kernel": top, "bound": "hbm", "achieved": round(achieved, 1),
+                     "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4),
+                     "peak_kind": peak_kind, "traffic": traffic},
+        "cpu_baseline": {"value": round(cpu_value, 4), "unit": "MPix/s", "cores": 1,
+                         "kind": "port",
+                         "sample": f"one {CPU_SAMPLE}x{CPU_SAMPLE} RGB16 crop of image 0, full "
+                                   "probe, single thread"},
+        "e2e": {"value": round(e2e, 2), "unit": "MPix/s",
+                "h2d_bytes_per_step": int(sum(r.nbytes for r, _ in images)),
+                "d2h_bytes_per_step": 8 * len(images)},
+        "gpu_launches": int(launches),
+        "clocks": clocks,
+        "scores": [round(float(s), 6) for s in dev_scores],
+    }
+    print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

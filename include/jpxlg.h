@@ -1,0 +1,198 @@
+/*
+ * jpxlg.h — C ABI of the GB300 (sm_103a) lossy VarDCT pixel path and
+ * SSIMULACRA2 metric of JPXL.
+ *
+ * The library replaces, behind plain pointers and sizes, the data-parallel
+ * stages that the reference (the JPXL Rust workspace) runs on CPU threads:
+ *
+ *   jpxlg_encode_transform  replaces jpxl-encode-policy's per-frame transform
+ *                           and quantization: PreparedFrame::from_srgb8_with /
+ *                           from_srgb16_with (crates/jpxl-encode-policy/src/
+ *                           source.rs:226, :355), prepare_gaborish_frame
+ *                           (lib.rs:2256 -> jpxl-encode vardct/gaborish.rs:218),
+ *                           the forward cache (lib.rs:2683), estimate_cfl
+ *                           (lib.rs:3437) and quantize_square_varblock
+ *                           (lib.rs:3237), for a cover the caller supplies.
+ *   jpxlg_reconstruct       replaces PlanRenderer::render / render_linear_at_
+ *                           depth_with (crates/jpxl-plan-render/src/lib.rs:
+ *                           680, :749) and the decoder's VarDCT tail
+ *                           (crates/jpxl-decode/src/decode.rs:2955-3061,
+ *                           vardct/render.rs:427, :563, :880).
+ *   jpxlg_ssim2_ref_create  replaces PrecomputedReference::new
+ *                           (crates/jpxl-perceptual/src/reference.rs:90).
+ *   jpxlg_ssim2_score       replaces Ssimulacra2::score (ssimulacra2.rs:79).
+ *   jpxlg_score_pair        replaces jpxl_perceptual::score_pair (lib.rs:195).
+ *   jpxlg_probe             replaces one PlanRenderEvaluator::evaluate_with
+ *                           (crates/jpxl-perceptual/src/evaluator.rs:243):
+ *                           plan, render at depth, score against the source.
+ *
+ * Conventions.  Every function returns 0 on success and a negative
+ * jpxlg_status on failure and never aborts; jpxlg_last_error() describes the
+ * last failure of a context.  Buffers are owned by the caller.  With
+ * JPXLG_MEM_HOST the pointers are host memory (pinned or pageable) and the
+ * call returns after the results are in place; with JPXLG_MEM_DEVICE they
+ * are device pointers on the context's device, work is queued on the
+ * context's stream and device-side errors are reported by the next
+ * jpxlg_ctx_synchronize().  A context serves one host thread at a time.
+ *
+ * Layouts.
+ *   planes      float, row-major width x height, three planes back to back
+ *               ([X,Y,B] or [R,G,B]).
+ *   RGB input   interleaved 8-bit (bits == 8) or 16-bit (bits 9..16) samples.
+ *   block map   one byte per 8x8 block of the ceil(w/8) x ceil(h/8) grid:
+ *               bits 0..4 the Table I.1 DctSelect (0 DCT8, 4 DCT16,
+ *               5 DCT32, 6 DCT16x8, 7 DCT8x16, 8 DCT32x8, 9 DCT8x32,
+ *               10 DCT32x16, 11 DCT16x32), bit 7 set on the top-left block of
+ *               each varblock.  Varblocks are naturally aligned.
+ *   coeff image int32, three planes of (8*bh) x (8*bw): a varblock at block
+ *               (bx,by) of R x C blocks stores its landscape coefficient
+ *               matrix (min(R,C)*8 rows, max(R,C)*8 cols, row-major as the
+ *               reference's CoeffMatrix) at row by*8.., column bx*8.. when
+ *               R <= C, transposed when R > C.
+ *   lf          int32, three planes of bw x bh quantized LF samples.
+ *   cfl tiles   int8 per 64x64 tile, ceil(bw/8) x ceil(bh/8), X then B.
+ */
+#ifndef JPXLG_H
+#define JPXLG_H
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+  JPXLG_OK = 0,
+  JPXLG_ERR_ARGUMENT = -1,     /* null pointer, bad size or parameter */
+  JPXLG_ERR_BLOCK_MAP = -2,    /* block map does not tile the frame */
+  JPXLG_ERR_QUANT = -3,        /* quantization out of range (PolicyError::Unsupported) */
+  JPXLG_ERR_CUDA = -4,         /* CUDA runtime failure */
+  JPXLG_ERR_NO_DEVICE = -5,    /* no usable sm_103 device */
+  JPXLG_ERR_TOO_SMALL = -6,    /* SSIMULACRA2 needs 8x8 (MetricError::TooSmall) */
+  JPXLG_ERR_MISMATCH = -7      /* dimensions differ (MetricError::DimensionMismatch) */
+} jpxlg_status;
+
+enum { JPXLG_MEM_HOST = 0, JPXLG_MEM_DEVICE = 1 };
+
+/* Output kinds of jpxlg_reconstruct. */
+enum {
+  JPXLG_OUT_XYB = 0,          /* three float planes after restoration */
+  JPXLG_OUT_LINEAR = 1,       /* three float linear-sRGB planes */
+  JPXLG_OUT_SRGB8 = 2,        /* interleaved 8-bit sRGB, as the decoder writes it */
+  JPXLG_OUT_LINEAR_DEPTH = 3  /* linear planes after a round trip through `bits` */
+};
+
+typedef struct jpxlg_ctx jpxlg_ctx;
+typedef struct jpxlg_layout jpxlg_layout;
+typedef struct jpxlg_ref jpxlg_ref;
+
+/* The request fields of jpxl-encode-policy EncodeRequest (request.rs:855)
+ * that the transform path reads. */
+typedef struct {
+  uint32_t global_scale;  /* I.2.1 global_scale */
+  uint32_t quant_lf;      /* I.2.1 quant_lf */
+  uint32_t x_qm_scale;    /* I.2.4 x_qm_scale (2 = neutral) */
+  uint32_t b_qm_scale;    /* I.2.4 b_qm_scale (2 = neutral) */
+  uint32_t gaborish;      /* RestorationDecision::gaborish */
+  uint32_t epf_iters;     /* RestorationDecision::epf_iters, 0..3 */
+  uint32_t cfl;           /* chroma-from-luma estimation on */
+} jpxlg_params;
+
+/* The quantized half of a plan (jpxl-encode vardct/plan.rs:434 LfQuantPlanes,
+ * :519 VarblockCoefficients, :251 CflGrid, LfCorrelationDecision). */
+typedef struct {
+  int32_t* qcoeff;        /* 3 * (8*bh) * (8*bw) */
+  int32_t* lf;            /* 3 * bw * bh */
+  int8_t* cfl_x;          /* tw * th */
+  int8_t* cfl_b;          /* tw * th */
+  int32_t lf_factors[2];  /* x_factor_lf, b_factor_lf, biased by +128 */
+} jpxlg_plan;
+
+/* Context: owns device tables, workspace and a stream. device < 0 picks the
+ * current device. flags: reserved, pass 0. */
+int jpxlg_ctx_create(int device, uint32_t flags, jpxlg_ctx** out);
+int jpxlg_ctx_destroy(jpxlg_ctx* ctx);
+/* Queue work on an external cudaStream_t (NULL restores the context's own). */
+int jpxlg_ctx_set_stream(jpxlg_ctx* ctx, void* cuda_stream);
+void* jpxlg_ctx_stream(jpxlg_ctx* ctx);
+/* Waits for queued work; returns the first device-side error since the last
+ * synchronize (quantization range, block map) or a CUDA error. */
+int jpxlg_ctx_synchronize(jpxlg_ctx* ctx);
+const char* jpxlg_last_error(const jpxlg_ctx* ctx);
+/* Kernel launches the context issued since creation (for accounting). */
+uint64_t jpxlg_ctx_launches(const jpxlg_ctx* ctx);
+
+/* Stage timers (the GPU counterpart of plan-render lib.rs:472 RenderTimings
+ * and the policy's stage diagnostics): when enabled, CUDA events recorded on
+ * the context's stream at stage boundaries accumulate device time per
+ * stage.  jpxlg_stage_times() synchronizes, writes up to `n` entries of
+ * milliseconds and launch counts in JPXLG_STAGE_* order, returns the number
+ * of stages, and resets the accumulators. */
+enum {
+  JPXLG_STAGE_XYB = 0,          /* K1 RGB -> XYB */
+  JPXLG_STAGE_PRECONDITION,     /* K2 inverse Gaborish, 12 steps */
+  JPXLG_STAGE_FDCT_LUMA,        /* K3 forward DCT, LF, luma quantization */
+  JPXLG_STAGE_CFL,              /* K4 CfL estimation */
+  JPXLG_STAGE_QUANT_CHROMA,     /* K5 chroma quantization */
+  JPXLG_STAGE_RENDER_VARBLOCKS, /* R1 dequant, CfL, LLF, IDCT */
+  JPXLG_STAGE_GABORISH,         /* R2 */
+  JPXLG_STAGE_EPF,              /* R3, all steps */
+  JPXLG_STAGE_COLOUR,           /* R4 */
+  JPXLG_STAGE_SSIM,             /* S1-S5 candidate side */
+  JPXLG_STAGE_COUNT
+};
+int jpxlg_stage_timing(jpxlg_ctx* ctx, int enable);
+int jpxlg_stage_times(jpxlg_ctx* ctx, double* ms, uint64_t* launches, int n);
+
+/* Frame structure of a plan (jpxl-encode vardct/plan.rs:239 varblocks with
+ * hf_mul, :318 SharpnessGrid): validated once, reused by every call on
+ * frames of this shape.  hf_mul and sharpness are per 8x8 block (hf_mul read
+ * at varblock origins); sharpness may be NULL (all zero). Host memory. */
+int jpxlg_layout_create(jpxlg_ctx* ctx, int width, int height, const uint8_t* block_map,
+                        const uint32_t* hf_mul, const uint8_t* sharpness, jpxlg_layout** out);
+int jpxlg_layout_destroy(jpxlg_layout* layout);
+int jpxlg_layout_dims(const jpxlg_layout* layout, int* bw, int* bh, int* tw, int* th);
+
+/* RGB -> quantized plan.  `rgb`, `plan->*` follow `mem`. */
+int jpxlg_encode_transform(jpxlg_ctx* ctx, const jpxlg_layout* layout, const void* rgb,
+                           int bits, const jpxlg_params* params, jpxlg_plan* plan,
+                           uint32_t mem);
+
+/* Diagnostic: the intermediate planes of jpxlg_encode_transform for one
+ * frame, in host memory (any may be NULL): the XYB planes
+ * (PreparedFrame::xyb, 3*w*h floats), the Gaborish-preconditioned planes
+ * (3*w*h) and the forward coefficient image before quantization (3 planes
+ * of (8*bh) x (8*bw) floats). */
+int jpxlg_encode_stages(jpxlg_ctx* ctx, const jpxlg_layout* layout, const void* rgb, int bits,
+                        const jpxlg_params* params, float* xyb, float* pre, float* coeff);
+
+/* Quantized plan -> pixels.  `out` sizes: JPXLG_OUT_SRGB8 w*h*3 bytes, other
+ * kinds 3*w*h floats.  `bits` is the depth of JPXLG_OUT_LINEAR_DEPTH. */
+int jpxlg_reconstruct(jpxlg_ctx* ctx, const jpxlg_layout* layout, const jpxlg_plan* plan,
+                      const jpxlg_params* params, int out_kind, int bits, void* out,
+                      uint32_t mem);
+
+/* SSIMULACRA2 reference moments of a linear-sRGB image (planes follow mem). */
+int jpxlg_ssim2_ref_create(jpxlg_ctx* ctx, const float* linear_rgb, int width, int height,
+                           uint32_t mem, jpxlg_ref** out);
+int jpxlg_ssim2_ref_destroy(jpxlg_ref* ref);
+/* Score a candidate against a reference.  terms (optional, host) receives
+ * up to 6 scales x 3 channels x 6 norms. */
+int jpxlg_ssim2_score(jpxlg_ctx* ctx, const jpxlg_ref* ref, const float* linear_rgb,
+                      uint32_t mem, double* score, double* raw_error, double* terms);
+/* One-shot pair score (reference moments are built and dropped). */
+int jpxlg_score_pair(jpxlg_ctx* ctx, const float* ref_rgb, const float* cand_rgb, int width,
+                     int height, uint32_t mem, double* score);
+
+/* One quality-controller probe: encode `rgb` with `params`, render the plan
+ * at 8-bit depth and score it against `ref` (built from the same source).
+ * With JPXLG_MEM_DEVICE the score is written to the device pointer
+ * `score_dev` (a double) and the call does not synchronize. */
+int jpxlg_probe(jpxlg_ctx* ctx, const jpxlg_layout* layout, const jpxlg_ref* ref,
+                const void* rgb, int bits, const jpxlg_params* params, uint32_t mem,
+                double* score);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

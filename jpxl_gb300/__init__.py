@@ -1,0 +1,361 @@
+"""jpxl_gb300 — the lossy VarDCT pixel path and SSIMULACRA2 of JPXL on GB300.
+
+Host-side mirror of the reference's entry points for this path, over the C
+ABI of ``libjpxlg.so`` (include/jpxlg.h):
+
+=============================  ==================================================
+this package                   reference (JPXL, crates/...)
+=============================  ==================================================
+``EncodeRequest``              jpxl-encode-policy request.rs:855 EncodeRequest
+``Layout``                     a validated cover: plan.rs:239 varblocks + hf_mul,
+                               :318 SharpnessGrid
+``encode_transform``           policy lib.rs:555 build_pixel_plan's transform and
+                               quantization (source.rs:226/:355, gaborish.rs:218,
+                               lib.rs:3437 estimate_cfl, :3237 quantize)
+``PlanRenderer.render``        jpxl-plan-render lib.rs:680 render /
+                               render_linear_at_depth_with
+``PrecomputedReference``       jpxl-perceptual reference.rs:90
+``Ssimulacra2.score``          jpxl-perceptual ssimulacra2.rs:79
+``score_pair``                 jpxl-perceptual lib.rs:195
+``Context.probe``              jpxl-perceptual evaluator.rs:243 evaluate_with
+=============================  ==================================================
+
+Arrays are numpy (host memory) unless stated; the ``*_device`` variants take
+integer device pointers (e.g. ``torch.Tensor.data_ptr()``) and queue work on
+the context's stream without synchronizing.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import _lib
+from ._lib import Params, PlanStruct
+
+MEM_HOST = 0
+MEM_DEVICE = 1
+OUT_XYB = 0
+OUT_LINEAR = 1
+OUT_SRGB8 = 2
+OUT_LINEAR_DEPTH = 3
+
+# Table I.1 DctSelect values of the plain DCT shapes this path carries.
+DCT8, DCT16, DCT32 = 0, 4, 5
+DCT16X8, DCT8X16, DCT32X8, DCT8X32, DCT32X16, DCT16X32 = 6, 7, 8, 9, 10, 11
+SHAPES = {
+    DCT8: (1, 1), DCT16: (2, 2), DCT32: (4, 4), DCT16X8: (2, 1), DCT8X16: (1, 2),
+    DCT32X8: (4, 1), DCT8X32: (1, 4), DCT32X16: (4, 2), DCT16X32: (2, 4),
+}
+ORIGIN = 0x80
+
+# JPXLG_STAGE_* order (include/jpxlg.h).
+STAGES = ("xyb", "precondition", "fdct_luma", "cfl", "quant_chroma", "render_varblocks",
+          "gaborish", "epf", "colour", "ssim")
+
+
+class JpxlError(RuntimeError):
+    """A non-zero jpxlg_status; ``code`` is the status."""
+
+    def __init__(self, code: int, message: str):
+        super().__init__(f"jpxlg status {code}: {message}")
+        self.code = code
+
+
+@dataclass
+class EncodeRequest:
+    """The request fields the transform path reads (request.rs:855)."""
+
+    global_scale: int = 32768
+    quant_lf: int = 16
+    x_qm_scale: int = 2
+    b_qm_scale: int = 2
+    gaborish: bool = False
+    epf_iters: int = 0
+    cfl: bool = True
+
+    @classmethod
+    def with_global_scale(cls, gs: int, **kw) -> "EncodeRequest":
+        """jpxl lib.rs:561 Encoder::with_global_scale (fixed quantizer)."""
+        return cls(global_scale=gs, **kw)
+
+    def _struct(self) -> Params:
+        return Params(self.global_scale, self.quant_lf, self.x_qm_scale, self.b_qm_scale,
+                      int(bool(self.gaborish)), self.epf_iters, int(bool(self.cfl)))
+
+
+@dataclass
+class Plan:
+    """The quantized half of a plan (plan.rs:434/:519/:251, LF correlation)."""
+
+    qcoeff: np.ndarray          # int32 [3, 8*bh, 8*bw] coefficient image
+    lf: np.ndarray              # int32 [3, bh, bw]
+    cfl_x: np.ndarray           # int8 [th, tw]
+    cfl_b: np.ndarray           # int8 [th, tw]
+    lf_factors: tuple = (128, 128)
+
+    def _struct(self) -> PlanStruct:
+        s = PlanStruct()
+        s.qcoeff = self.qcoeff.ctypes.data
+        s.lf = self.lf.ctypes.data
+        s.cfl_x = self.cfl_x.ctypes.data
+        s.cfl_b = self.cfl_b.ctypes.data
+        s.lf_factors[0] = int(self.lf_factors[0])
+        s.lf_factors[1] = int(self.lf_factors[1])
+        return s
+
+
+class Context:
+    """A device context: tables, workspace and a CUDA stream (jpxlg_ctx)."""
+
+    def __init__(self, device: int = 0):
+        self.lib = _lib.load()
+        h = C.c_void_p()
+        rc = self.lib.jpxlg_ctx_create(device, 0, C.byref(h))
+        if rc:
+            raise JpxlError(rc, "jpxlg_ctx_create failed (no sm_103 device?)")
+        self.handle = h
+
+    def check(self, rc: int) -> None:
+        if rc:
+            raise JpxlError(rc, self.lib.jpxlg_last_error(self.handle).decode())
+
+    def close(self) -> None:
+        if self.handle:
+            self.lib.jpxlg_ctx_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def stream(self) -> int:
+        return int(self.lib.jpxlg_ctx_stream(self.handle) or 0)
+
+    def set_stream(self, stream: int | None) -> None:
+        self.check(self.lib.jpxlg_ctx_set_stream(self.handle, C.c_void_p(stream or 0)))
+
+    def synchronize(self) -> None:
+        self.check(self.lib.jpxlg_ctx_synchronize(self.handle))
+
+    @property
+    def launches(self) -> int:
+        return int(self.lib.jpxlg_ctx_launches(self.handle))
+
+    def stage_timing(self, enable: bool) -> None:
+        self.check(self.lib.jpxlg_stage_timing(self.handle, int(enable)))
+
+    def stage_times(self) -> dict:
+        """Device milliseconds and kernel launches per stage since the last
+        call (synchronizes)."""
+        ms = np.zeros(len(STAGES), np.float64)
+        ln = np.zeros(len(STAGES), np.uint64)
+        n = self.lib.jpxlg_stage_times(self.handle, ms.ctypes.data, ln.ctypes.data, len(STAGES))
+        if n < 0:
+            self.check(n)
+        return {name: (float(ms[i]), int(ln[i])) for i, name in enumerate(STAGES)}
+
+    # -- encode ---------------------------------------------------------------
+    def encode_transform(self, layout: "Layout", rgb: np.ndarray, req: EncodeRequest,
+                         bits: int | None = None) -> Plan:
+        rgb = np.ascontiguousarray(rgb)
+        if bits is None:
+            bits = 8 if rgb.dtype == np.uint8 else 16
+        want = np.uint8 if bits == 8 else np.uint16
+        if rgb.dtype != want or rgb.shape != (layout.height, layout.width, 3):
+            raise ValueError(f"rgb must be {want.__name__} [{layout.height}, {layout.width}, 3]")
+        plan = layout.empty_plan()
+        s = plan._struct()
+        p = req._struct()
+        self.check(self.lib.jpxlg_encode_transform(self.handle, layout.handle,
+                                                   rgb.ctypes.data, bits, C.byref(p),
+                                                   C.byref(s), MEM_HOST))
+        plan.lf_factors = (s.lf_factors[0], s.lf_factors[1])
+        return plan
+
+    def encode_stages(self, layout: "Layout", rgb: np.ndarray, req: EncodeRequest,
+                      bits: int | None = None) -> dict:
+        """Diagnostic: XYB, preconditioned planes and forward coefficients."""
+        rgb = np.ascontiguousarray(rgb)
+        if bits is None:
+            bits = 8 if rgb.dtype == np.uint8 else 16
+        h, w = layout.height, layout.width
+        out = {"xyb": np.zeros((3, h, w), np.float32), "pre": np.zeros((3, h, w), np.float32),
+               "coeff": np.zeros((3, 8 * layout.bh, 8 * layout.bw), np.float32)}
+        p = req._struct()
+        self.check(self.lib.jpxlg_encode_stages(self.handle, layout.handle, rgb.ctypes.data, bits,
+                                                C.byref(p), out["xyb"].ctypes.data,
+                                                out["pre"].ctypes.data, out["coeff"].ctypes.data))
+        return out
+
+    def probe(self, layout: "Layout", ref: "PrecomputedReference", rgb: np.ndarray,
+              req: EncodeRequest, bits: int | None = None) -> float:
+        """Encode, render at the source depth and score against ``ref``."""
+        rgb = np.ascontiguousarray(rgb)
+        if bits is None:
+            bits = 8 if rgb.dtype == np.uint8 else 16
+        out = C.c_double()
+        p = req._struct()
+        self.check(self.lib.jpxlg_probe(self.handle, layout.handle, ref.handle, rgb.ctypes.data,
+                                        bits, C.byref(p), MEM_HOST, C.byref(out)))
+        return out.value
+
+    def probe_device(self, layout, ref, rgb_ptr: int, bits: int, req: EncodeRequest,
+                     score_ptr: int) -> None:
+        p = req._struct()
+        self.check(self.lib.jpxlg_probe(self.handle, layout.handle, ref.handle,
+                                        C.c_void_p(rgb_ptr), bits, C.byref(p), MEM_DEVICE,
+                                        C.c_void_p(score_ptr)))
+
+
+class Layout:
+    """A validated cover and its per-block hf_mul / sharpness (jpxlg_layout)."""
+
+    def __init__(self, ctx: Context, width: int, height: int, block_map: np.ndarray,
+                 hf_mul: np.ndarray | int = 1, sharpness: np.ndarray | int | None = None):
+        self.ctx = ctx
+        self.width, self.height = width, height
+        bw, bh = (width + 7) // 8, (height + 7) // 8
+        self.block_map = np.ascontiguousarray(block_map, dtype=np.uint8).reshape(bh, bw)
+        if np.isscalar(hf_mul):
+            hf_mul = np.full((bh, bw), hf_mul, np.uint32)
+        self.hf_mul = np.ascontiguousarray(hf_mul, dtype=np.uint32).reshape(bh, bw)
+        if sharpness is None:
+            sharpness = 0
+        if np.isscalar(sharpness):
+            sharpness = np.full((bh, bw), sharpness, np.uint8)
+        self.sharpness = np.ascontiguousarray(sharpness, dtype=np.uint8).reshape(bh, bw)
+        h = C.c_void_p()
+        ctx.check(ctx.lib.jpxlg_layout_create(ctx.handle, width, height,
+                                              self.block_map.ctypes.data,
+                                              self.hf_mul.ctypes.data,
+                                              self.sharpness.ctypes.data, C.byref(h)))
+        self.handle = h
+        self.bw, self.bh = bw, bh
+        self.tw, self.th = (bw + 7) // 8, (bh + 7) // 8
+
+    def empty_plan(self) -> Plan:
+        return Plan(np.zeros((3, 8 * self.bh, 8 * self.bw), np.int32),
+                    np.zeros((3, self.bh, self.bw), np.int32),
+                    np.zeros((self.th, self.tw), np.int8),
+                    np.zeros((self.th, self.tw), np.int8))
+
+    def close(self):
+        if self.handle:
+            self.ctx.lib.jpxlg_layout_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class PlanRenderer:
+    """jpxl-plan-render lib.rs:560 PlanRenderer over the CUDA path."""
+
+    def __init__(self, ctx: Context):
+        self.ctx = ctx
+
+    def render(self, layout: Layout, plan: Plan, req: EncodeRequest, out: str = "srgb8",
+               bits: int = 8) -> np.ndarray:
+        kind = {"xyb": OUT_XYB, "linear": OUT_LINEAR, "srgb8": OUT_SRGB8,
+                "linear_at_depth": OUT_LINEAR_DEPTH}[out]
+        h, w = layout.height, layout.width
+        res = (np.zeros((h, w, 3), np.uint8) if kind == OUT_SRGB8
+               else np.zeros((3, h, w), np.float32))
+        s = plan._struct()
+        p = req._struct()
+        self.ctx.check(self.ctx.lib.jpxlg_reconstruct(self.ctx.handle, layout.handle, C.byref(s),
+                                                      C.byref(p), kind, bits, res.ctypes.data,
+                                                      MEM_HOST))
+        return res
+
+
+class PrecomputedReference:
+    """reference.rs:90 PrecomputedReference (Moments retention) on the device."""
+
+    def __init__(self, ctx: Context, linear_rgb: np.ndarray | None = None, *,
+                 device_ptr: int | None = None, width: int = 0, height: int = 0):
+        self.ctx = ctx
+        h = C.c_void_p()
+        if device_ptr is not None:
+            self.width, self.height = width, height
+            rc = ctx.lib.jpxlg_ssim2_ref_create(ctx.handle, C.c_void_p(device_ptr), width,
+                                                height, MEM_DEVICE, C.byref(h))
+        else:
+            planes = np.ascontiguousarray(linear_rgb, dtype=np.float32)
+            if planes.ndim != 3 or planes.shape[0] != 3:
+                raise ValueError("linear_rgb must be float32 [3, H, W]")
+            self.height, self.width = planes.shape[1], planes.shape[2]
+            rc = ctx.lib.jpxlg_ssim2_ref_create(ctx.handle, planes.ctypes.data, self.width,
+                                                self.height, MEM_HOST, C.byref(h))
+        ctx.check(rc)
+        self.handle = h
+
+    def close(self):
+        if self.handle:
+            self.ctx.lib.jpxlg_ssim2_ref_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+@dataclass
+class Ssimulacra2Result:
+    score: float
+    raw_error: float
+    terms: np.ndarray = field(default_factory=lambda: np.zeros(0))
+
+
+class Ssimulacra2:
+    """ssimulacra2.rs Ssimulacra2::score over the CUDA path."""
+
+    def __init__(self, ctx: Context):
+        self.ctx = ctx
+
+    def score(self, ref: PrecomputedReference, linear_rgb: np.ndarray) -> Ssimulacra2Result:
+        planes = np.ascontiguousarray(linear_rgb, dtype=np.float32)
+        if planes.shape != (3, ref.height, ref.width):
+            raise JpxlError(-7, "candidate dimensions differ from the reference")
+        sc, raw = C.c_double(), C.c_double()
+        terms = np.zeros(6 * 18, np.float64)
+        self.ctx.check(self.ctx.lib.jpxlg_ssim2_score(self.ctx.handle, ref.handle,
+                                                      planes.ctypes.data, MEM_HOST,
+                                                      C.byref(sc), C.byref(raw),
+                                                      terms.ctypes.data))
+        return Ssimulacra2Result(sc.value, raw.value, terms)
+
+
+def score_pair(ctx: Context, ref_rgb: np.ndarray, cand_rgb: np.ndarray) -> float:
+    """jpxl-perceptual lib.rs:195 score_pair on linear [3, H, W] planes."""
+    a = np.ascontiguousarray(ref_rgb, dtype=np.float32)
+    b = np.ascontiguousarray(cand_rgb, dtype=np.float32)
+    if a.shape != b.shape:
+        raise JpxlError(-7, "dimension mismatch")
+    out = C.c_double()
+    ctx.check(ctx.lib.jpxlg_score_pair(ctx.handle, a.ctypes.data, b.ctypes.data, a.shape[2],
+                                       a.shape[1], MEM_HOST, C.byref(out)))
+    return out.value
+
+
+def srgb_to_linear_planes(rgb: np.ndarray, bits: int = 8) -> np.ndarray:
+    """Source code points -> linear planes through the reference's per-code-point
+    curve (source.rs:226/:355, evaluator.rs:88), as float32 [3, H, W]."""
+    maxv = 255.0 if bits == 8 else float(min(65535, (1 << bits) - 1))
+    lut = np.empty(256 if bits == 8 else 65536, np.float32)
+    v = (np.arange(lut.size, dtype=np.float32) / np.float32(maxv)).astype(np.float32)
+    a = np.abs(v)
+    lin = np.where(a <= np.float32(12.92) * np.float32(0.0031308), a / np.float32(12.92),
+                   np.power((a + np.float32(0.055)) / np.float32(1.055), np.float32(2.4)))
+    lut[:] = lin.astype(np.float32)
+    return np.ascontiguousarray(lut[rgb].transpose(2, 0, 1))

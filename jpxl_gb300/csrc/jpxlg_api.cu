@@ -1,0 +1,928 @@
+// jpxlg_api.cu — the C ABI (include/jpxlg.h): contexts, layouts, workspace
+// and the host orchestration of the sm_103a kernels.  Host code only; the
+// kernels live in k_encode.cu, k_render.cu and k_ssim.cu.
+#include <algorithm>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "../../include/jpxlg.h"
+#include "jpxlg_common.cuh"
+#include "jpxlg_internal.h"
+#include "jpxlg_kernels.h"
+
+using namespace jpxlg;
+
+namespace {
+
+// A grow-only device buffer.
+struct DevBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+  cudaError_t ensure(size_t n) {
+    if (n <= bytes) return cudaSuccess;
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+    cudaError_t e = cudaMalloc(&p, n);
+    if (e == cudaSuccess) bytes = n;
+    return e;
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+  }
+  template <typename T>
+  T* as() const { return (T*)p; }
+};
+
+struct DepthTable {
+  float* thr = nullptr;
+  float* lev = nullptr;
+  int levels = 0;
+};
+
+}  // namespace
+
+struct jpxlg_ctx {
+  int device = 0;
+  int num_sms = 0;
+  cudaStream_t own_stream = nullptr;
+  cudaStream_t stream = nullptr;
+  std::string last_error;
+  uint64_t launches = 0;
+  // tables
+  float* d_dq = nullptr;
+  std::map<int, float*> lut;          // sRGB -> linear per source depth
+  std::map<int, DepthTable> depth;    // output depth classifiers
+  // small device words
+  uint32_t* d_words = nullptr;  // [0] err, [1] not_gray, [2] cfl fallbacks
+  int* d_lf = nullptr;          // [0..1] unbiased LF factors, [2..3] biased
+  uint32_t* h_words = nullptr;  // pinned mirror
+  double* h_score = nullptr;    // pinned score out (2 + 108)
+  // workspace
+  DevBuf rgb, xyb, pre, coeff, dyhf, qcoeff, lfs, dylf, lfq, cflx, cflb;
+  DevBuf planes, aux, sigma, out;
+  DevBuf lf_part, lf_cost, lf_seed;
+  DevBuf pyr, partial, score;
+  // stage timers
+  struct Mark {
+    int stage;
+    cudaEvent_t a, b;
+    uint64_t launches;
+  };
+  bool timing = false;
+  std::vector<Mark> marks;
+  std::vector<cudaEvent_t> event_pool;
+  int open_stage = -1;
+  cudaEvent_t open_event = nullptr;
+  uint64_t open_launches = 0;
+  double stage_ms[JPXLG_STAGE_COUNT] = {};
+  uint64_t stage_launches[JPXLG_STAGE_COUNT] = {};
+};
+
+struct jpxlg_layout {
+  jpxlg_ctx* ctx = nullptr;
+  Geo geo;
+  uint8_t* d_map = nullptr;
+  uint32_t* d_hf_mul = nullptr;
+  uint8_t* d_sharp = nullptr;
+  uint32_t* d_lists = nullptr;
+  const uint32_t* lists[kNumShapes] = {};
+  int counts[kNumShapes] = {};
+  uint32_t base_hf_mul = 1;
+  bool all_square = true;
+};
+
+struct jpxlg_ref {
+  jpxlg_ctx* ctx = nullptr;
+  int w = 0, h = 0, nscales = 0;
+  SsimScale scales[6];
+  void* block = nullptr;  // one allocation holding every scale's planes
+};
+
+namespace {
+
+int fail(jpxlg_ctx* ctx, int code, const char* fmt, ...) {
+  if (ctx) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    ctx->last_error = buf;
+  }
+  return code;
+}
+
+#define CK(call)                                                                     \
+  do {                                                                               \
+    cudaError_t e_ = (call);                                                         \
+    if (e_ != cudaSuccess)                                                           \
+      return fail(ctx, JPXLG_ERR_CUDA, "%s: %s", #call, cudaGetErrorString(e_));     \
+  } while (0)
+
+cudaEvent_t pool_event(jpxlg_ctx* ctx) {
+  if (!ctx->event_pool.empty()) {
+    cudaEvent_t e = ctx->event_pool.back();
+    ctx->event_pool.pop_back();
+    return e;
+  }
+  cudaEvent_t e = nullptr;
+  cudaEventCreate(&e);
+  return e;
+}
+
+// Stage boundaries: an event before the stage's first launch and one after
+// its last, on the context's stream.
+void stage_begin(jpxlg_ctx* ctx, int stage) {
+  if (!ctx->timing) return;
+  ctx->open_stage = stage;
+  ctx->open_event = pool_event(ctx);
+  ctx->open_launches = ctx->launches;
+  cudaEventRecord(ctx->open_event, ctx->stream);
+}
+
+void stage_end(jpxlg_ctx* ctx) {
+  if (!ctx->timing || ctx->open_stage < 0) return;
+  cudaEvent_t b = pool_event(ctx);
+  cudaEventRecord(b, ctx->stream);
+  ctx->marks.push_back({ctx->open_stage, ctx->open_event, b, ctx->launches - ctx->open_launches});
+  ctx->open_stage = -1;
+}
+
+int after_launch(jpxlg_ctx* ctx, uint64_t n) {
+  ctx->launches += n;
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return fail(ctx, JPXLG_ERR_CUDA, "kernel launch: %s", cudaGetErrorString(e));
+  return JPXLG_OK;
+}
+
+// Reads and clears the device error word after the stream drains.
+int sync_and_check(jpxlg_ctx* ctx) {
+  CK(cudaMemcpyAsync(ctx->h_words, ctx->d_words, 3 * sizeof(uint32_t), cudaMemcpyDeviceToHost,
+                     ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  uint32_t err = ctx->h_words[0];
+  if (err) {
+    CK(cudaMemsetAsync(ctx->d_words, 0, sizeof(uint32_t), ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    if (err & kDevQuantRange)
+      return fail(ctx, JPXLG_ERR_QUANT, "a quantization target outside the working range");
+    if (err & kDevBadStep) return fail(ctx, JPXLG_ERR_QUANT, "a degenerate quantization step");
+    return fail(ctx, JPXLG_ERR_BLOCK_MAP, "a block-map entry the kernels cannot place");
+  }
+  return JPXLG_OK;
+}
+
+const float* get_lut(jpxlg_ctx* ctx, int bits) {
+  auto it = ctx->lut.find(bits);
+  if (it != ctx->lut.end()) return it->second;
+  int n = bits == 8 ? 256 : 65536;
+  std::vector<float> h(n);
+  build_srgb_lut(bits, h.data());
+  float* d = nullptr;
+  if (cudaMalloc(&d, n * sizeof(float)) != cudaSuccess) return nullptr;
+  cudaMemcpy(d, h.data(), n * sizeof(float), cudaMemcpyHostToDevice);
+  ctx->lut[bits] = d;
+  return d;
+}
+
+const DepthTable* get_depth(jpxlg_ctx* ctx, int bits) {
+  auto it = ctx->depth.find(bits);
+  if (it != ctx->depth.end()) return &it->second;
+  int levels = bits >= 32 ? 65536 : (1 << std::min(std::max(bits, 1), 16));
+  std::vector<float> thr(levels), lev(levels);
+  build_depth_thresholds(bits, thr.data(), lev.data());
+  DepthTable t;
+  t.levels = levels;
+  if (cudaMalloc(&t.thr, levels * sizeof(float)) != cudaSuccess) return nullptr;
+  if (cudaMalloc(&t.lev, levels * sizeof(float)) != cudaSuccess) return nullptr;
+  cudaMemcpy(t.thr, thr.data(), levels * sizeof(float), cudaMemcpyHostToDevice);
+  cudaMemcpy(t.lev, lev.data(), levels * sizeof(float), cudaMemcpyHostToDevice);
+  ctx->depth[bits] = t;
+  return &ctx->depth[bits];
+}
+
+QuantScalars scalars_of(const jpxlg_params* p) {
+  QuantScalars q;
+  q.global_scale = p->global_scale;
+  host_lf_multipliers(p->global_scale, p->quant_lf, q.m_dc);
+  q.qm[0] = host_qm_multiplier(p->x_qm_scale);
+  q.qm[1] = 1.0f;
+  q.qm[2] = host_qm_multiplier(p->b_qm_scale);
+  return q;
+}
+
+int check_params(jpxlg_ctx* ctx, const jpxlg_params* p) {
+  if (!p) return fail(ctx, JPXLG_ERR_ARGUMENT, "null params");
+  if (p->global_scale == 0 || p->quant_lf == 0)
+    return fail(ctx, JPXLG_ERR_ARGUMENT, "global_scale and quant_lf must be positive");
+  if (p->x_qm_scale > 7 || p->b_qm_scale > 7)
+    return fail(ctx, JPXLG_ERR_ARGUMENT, "qm scales are u(3)");
+  if (p->epf_iters > 3) return fail(ctx, JPXLG_ERR_ARGUMENT, "epf_iters outside 0..=3");
+  return JPXLG_OK;
+}
+
+// Encode into plan buffers that live on the device.
+int encode_device(jpxlg_ctx* ctx, const jpxlg_layout* L, const void* rgb_dev, int bits,
+                  const jpxlg_params* p, int32_t* qcoeff, int32_t* lfq, int8_t* cflx,
+                  int8_t* cflb, int32_t* lf_factors_biased) {
+  const Geo& g = L->geo;
+  if (!L->all_square)
+    return fail(ctx, JPXLG_ERR_BLOCK_MAP, "the encoder covers frames with square varblocks only");
+  const size_t n = (size_t)g.w * g.h, n8 = (size_t)g.W8 * g.H8, nb = (size_t)g.bw * g.bh;
+  CK(ctx->xyb.ensure(3 * n * sizeof(float)));
+  CK(ctx->coeff.ensure(3 * n8 * sizeof(float)));
+  CK(ctx->dyhf.ensure(n8 * sizeof(float)));
+  CK(ctx->lfs.ensure(3 * nb * sizeof(float)));
+  CK(ctx->dylf.ensure(nb * sizeof(float)));
+  const int nparts = std::max(1, std::min(ctx->num_sms * 2, (int)((nb + 255) / 256)));
+  CK(ctx->lf_part.ensure((size_t)nparts * 8 * sizeof(double)));
+  CK(ctx->lf_cost.ensure((size_t)nparts * 8 * sizeof(unsigned long long)));
+  CK(ctx->lf_seed.ensure(4 * sizeof(int)));
+  const float* lut = get_lut(ctx, bits);
+  if (!lut) return fail(ctx, JPXLG_ERR_CUDA, "transfer table allocation failed");
+  CK(cudaMemsetAsync(ctx->d_words + 1, 0, sizeof(uint32_t), ctx->stream));
+  float* xyb = ctx->xyb.as<float>();
+  stage_begin(ctx, JPXLG_STAGE_XYB);
+  launch_srgb_to_xyb(rgb_dev, bits, n, lut, xyb, xyb + n, xyb + 2 * n, ctx->d_words + 1,
+                     ctx->num_sms, ctx->stream);
+  int rc = after_launch(ctx, 1);
+  stage_end(ctx);
+  if (rc) return rc;
+  const float* pre = xyb;
+  if (p->gaborish) {
+    CK(ctx->pre.ensure(3 * n * sizeof(float)));
+    stage_begin(ctx, JPXLG_STAGE_PRECONDITION);
+    launch_precondition(xyb, ctx->pre.as<float>(), g.w, g.h, ctx->stream);
+    rc = after_launch(ctx, 1);
+    stage_end(ctx);
+    if (rc) return rc;
+    pre = ctx->pre.as<float>();
+  }
+  EncArgs a;
+  a.geo = g;
+  a.qs = scalars_of(p);
+  a.pre = pre;
+  a.dq = ctx->d_dq;
+  a.hf_mul = L->d_hf_mul;
+  a.block_map = L->d_map;
+  a.coeff = ctx->coeff.as<float>();
+  a.dyhf = ctx->dyhf.as<float>();
+  a.qcoeff = qcoeff;
+  a.lfs = ctx->lfs.as<float>();
+  a.dylf = ctx->dylf.as<float>();
+  a.lfq = lfq;
+  a.cfl_x = cflx;
+  a.cfl_b = cflb;
+  a.lf_factors = ctx->d_lf;
+  a.not_gray = ctx->d_words + 1;
+  a.cfl_enabled = p->cfl;
+  a.base_mul = host_hf_multiplier(p->global_scale, L->base_hf_mul);
+  a.err = ctx->d_words;
+  a.cfl_fallbacks = ctx->d_words + 2;
+  // square classes only: DCT8, DCT16, DCT32 are shape classes 0..2
+  stage_begin(ctx, JPXLG_STAGE_FDCT_LUMA);
+  rc = after_launch(ctx, launch_fdct_luma(a, L->lists, L->counts, ctx->stream));
+  stage_end(ctx);
+  if (rc) return rc;
+  stage_begin(ctx, JPXLG_STAGE_CFL);
+  rc = after_launch(ctx, launch_cfl(a, ctx->lf_part.as<double>(),
+                                    ctx->lf_cost.as<unsigned long long>(), ctx->lf_seed.as<int>(),
+                                    nparts, ctx->stream));
+  stage_end(ctx);
+  if (rc) return rc;
+  stage_begin(ctx, JPXLG_STAGE_QUANT_CHROMA);
+  rc = after_launch(ctx, launch_quant_chroma(a, L->lists, L->counts, ctx->stream));
+  stage_end(ctx);
+  if (rc) return rc;
+  // biased copy of the LF factors for the plan
+  if (lf_factors_biased) {
+    // d_lf[0..1] unbiased; the plan stores factor + 128.
+    CK(cudaMemcpyAsync(ctx->h_words + 4, ctx->d_lf, 2 * sizeof(int), cudaMemcpyDeviceToHost,
+                       ctx->stream));
+  }
+  return JPXLG_OK;
+}
+
+int render_device(jpxlg_ctx* ctx, const jpxlg_layout* L, const int32_t* qcoeff,
+                  const int32_t* lfq, const int8_t* cflx, const int8_t* cflb, int fx_biased,
+                  int fb_biased, const int* lf_dev_unbiased, const jpxlg_params* p, int out_kind,
+                  int bits, void* out_dev) {
+  const Geo& g = L->geo;
+  const size_t n = (size_t)g.w * g.h, nb = (size_t)g.bw * g.bh;
+  CK(ctx->planes.ensure(3 * n * sizeof(float)));
+  CK(ctx->aux.ensure(3 * n * sizeof(float)));
+  CK(ctx->sigma.ensure(nb * sizeof(float)));
+  RenderArgs a;
+  a.geo = g;
+  a.qs = scalars_of(p);
+  a.dq = ctx->d_dq;
+  a.hf_mul = L->d_hf_mul;
+  a.sharpness = L->d_sharp;
+  a.qcoeff = qcoeff;
+  a.lfq = lfq;
+  a.cfl_x = cflx;
+  a.cfl_b = cflb;
+  a.k_x_lf = 0.0f + (float)(fx_biased - 128) / 84.0f;
+  a.k_b_lf = 1.0f + (float)(fb_biased - 128) / 84.0f;
+  a.lf_factors_dev = lf_dev_unbiased;
+  a.planes = ctx->planes.as<float>();
+  a.sigma = ctx->sigma.as<float>();
+  stage_begin(ctx, JPXLG_STAGE_RENDER_VARBLOCKS);
+  launch_render_varblocks(a, L->lists, L->counts, ctx->stream);
+  uint64_t k = 0;
+  for (int i = 0; i < kNumShapes; ++i) k += L->counts[i] ? 1 : 0;
+  int rc = after_launch(ctx, k);
+  stage_end(ctx);
+  if (rc) return rc;
+  float* cur = ctx->planes.as<float>();
+  float* nxt = ctx->aux.as<float>();
+  if (p->gaborish) {
+    stage_begin(ctx, JPXLG_STAGE_GABORISH);
+    launch_gaborish(cur, nxt, g.w, g.h, ctx->stream);
+    std::swap(cur, nxt);
+    rc = after_launch(ctx, 1);
+    stage_end(ctx);
+    if (rc) return rc;
+  }
+  static const int steps_for[4][3] = {{-1, -1, -1}, {1, -1, -1}, {1, 2, -1}, {0, 1, 2}};
+  if (p->epf_iters) stage_begin(ctx, JPXLG_STAGE_EPF);
+  for (int s = 0; s < 3; ++s) {
+    int step = steps_for[p->epf_iters][s];
+    if (step < 0) break;
+    launch_epf_step(step, cur, nxt, ctx->sigma.as<float>(), g.w, g.h, ctx->stream);
+    std::swap(cur, nxt);
+    if ((rc = after_launch(ctx, 1))) return rc;
+  }
+  if (p->epf_iters) stage_end(ctx);
+  if (out_kind == JPXLG_OUT_XYB) {
+    CK(cudaMemcpyAsync(out_dev, cur, 3 * n * sizeof(float), cudaMemcpyDeviceToDevice, ctx->stream));
+    return JPXLG_OK;
+  }
+  int b = out_kind == JPXLG_OUT_SRGB8 ? 8 : bits;
+  const DepthTable* dt = nullptr;
+  if (out_kind != JPXLG_OUT_LINEAR) {
+    dt = get_depth(ctx, b);
+    if (!dt) return fail(ctx, JPXLG_ERR_CUDA, "depth table allocation failed");
+  }
+  stage_begin(ctx, JPXLG_STAGE_COLOUR);
+  launch_colour_out(cur, g.w, g.h, out_kind, dt ? dt->thr : nullptr, dt ? dt->lev : nullptr,
+                    dt ? dt->levels : 0, out_dev, ctx->num_sms, ctx->stream);
+  rc = after_launch(ctx, 1);
+  stage_end(ctx);
+  return rc;
+}
+
+int score_device(jpxlg_ctx* ctx, const jpxlg_ref* ref, const float* cand_dev, double* out_dev) {
+  const int w = ref->w, h = ref->h;
+  // candidate pyramid (scales 1..): sum of quarter-ish planes
+  size_t pyr = 0;
+  int cw = w, ch = h;
+  for (int s = 1; s < ref->nscales; ++s) {
+    cw = (cw + 1) / 2;
+    ch = (ch + 1) / 2;
+    pyr += 3 * (size_t)cw * ch;
+  }
+  CK(ctx->pyr.ensure(std::max<size_t>(pyr, 1) * sizeof(float)));
+  size_t ctas_total = 0;
+  for (int s = 0; s < ref->nscales; ++s)
+    ctas_total += (size_t)((ref->scales[s].w + 31) / 32) * ((ref->scales[s].h + 31) / 32);
+  CK(ctx->partial.ensure(ctas_total * 18 * sizeof(double)));
+  int ctas[6], pixels[6];
+  stage_begin(ctx, JPXLG_STAGE_SSIM);
+  const float* cur = cand_dev;
+  float* next = ctx->pyr.as<float>();
+  double* part = ctx->partial.as<double>();
+  uint64_t k = 0;
+  for (int s = 0; s < ref->nscales; ++s) {
+    const SsimScale& rs = ref->scales[s];
+    if (s > 0) {
+      launch_downscale3(cur, ref->scales[s - 1].w, ref->scales[s - 1].h, next, ctx->stream);
+      ++k;
+      cur = next;
+      next += 3 * (size_t)rs.w * rs.h;
+    }
+    ctas[s] = launch_score_scale(cur, rs, part, ctx->stream);
+    ++k;
+    pixels[s] = rs.w * rs.h;
+    part += (size_t)ctas[s] * 18;
+  }
+  launch_score_finish(ctx->partial.as<double>(), ctas, ref->nscales, pixels, out_dev, ctx->stream);
+  int rc = after_launch(ctx, k + 1);
+  stage_end(ctx);
+  return rc;
+}
+
+}  // namespace
+
+extern "C" {
+
+int jpxlg_ctx_create(int device, uint32_t flags, jpxlg_ctx** out) {
+  (void)flags;
+  if (!out) return JPXLG_ERR_ARGUMENT;
+  *out = nullptr;
+  int count = 0;
+  if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0) return JPXLG_ERR_NO_DEVICE;
+  if (device < 0) cudaGetDevice(&device);
+  if (device >= count) return JPXLG_ERR_NO_DEVICE;
+  cudaDeviceProp prop;
+  if (cudaGetDeviceProperties(&prop, device) != cudaSuccess) return JPXLG_ERR_NO_DEVICE;
+  if (prop.major != 10 || prop.minor != 3) return JPXLG_ERR_NO_DEVICE;  // built for sm_103a only
+  std::unique_ptr<jpxlg_ctx> ctx(new jpxlg_ctx);
+  ctx->device = device;
+  ctx->num_sms = prop.multiProcessorCount;
+  jpxlg_ctx* c = ctx.get();
+#define CKC(call)                                 \
+  do {                                            \
+    if ((call) != cudaSuccess) return JPXLG_ERR_CUDA; \
+  } while (0)
+  CKC(cudaSetDevice(device));
+  CKC(cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking));
+  c->stream = c->own_stream;
+  CKC(cudaMalloc(&c->d_words, 8 * sizeof(uint32_t)));
+  CKC(cudaMemset(c->d_words, 0, 8 * sizeof(uint32_t)));
+  CKC(cudaMalloc(&c->d_lf, 4 * sizeof(int)));
+  CKC(cudaMemset(c->d_lf, 0, 4 * sizeof(int)));
+  CKC(cudaMallocHost(&c->h_words, 16 * sizeof(uint32_t)));
+  CKC(cudaMallocHost(&c->h_score, 128 * sizeof(double)));
+  std::vector<float> dq(3 * kDequantTableFloats);
+  build_dequant_tables(dq.data());
+  CKC(cudaMalloc(&c->d_dq, dq.size() * sizeof(float)));
+  CKC(cudaMemcpy(c->d_dq, dq.data(), dq.size() * sizeof(float), cudaMemcpyHostToDevice));
+  float iv4[16], iv8[64], iv16[256], sf[12], taps[5], om[9], ob[3], oc[3];
+  build_iv_tables(iv4, iv8, iv16);
+  build_scale_f(sf);
+  build_blur_taps(taps);
+  build_opsin_inverse(om, ob, oc);
+  upload_dct_constants(iv4, iv8, iv16, sf, c->stream);
+  upload_blur_taps(taps, c->stream);
+  upload_render_constants(om, ob, oc, c->stream);
+  CKC(cudaStreamSynchronize(c->stream));
+#undef CKC
+  *out = ctx.release();
+  return JPXLG_OK;
+}
+
+int jpxlg_ctx_destroy(jpxlg_ctx* ctx) {
+  if (!ctx) return JPXLG_ERR_ARGUMENT;
+  cudaSetDevice(ctx->device);
+  cudaStreamSynchronize(ctx->stream);
+  for (auto& kv : ctx->lut) cudaFree(kv.second);
+  for (auto& kv : ctx->depth) {
+    cudaFree(kv.second.thr);
+    cudaFree(kv.second.lev);
+  }
+  DevBuf* bufs[] = {&ctx->rgb,    &ctx->xyb,   &ctx->pre,     &ctx->coeff,   &ctx->dyhf,
+                    &ctx->qcoeff, &ctx->lfs,   &ctx->dylf,    &ctx->lfq,     &ctx->cflx,
+                    &ctx->cflb,   &ctx->planes, &ctx->aux,    &ctx->sigma,   &ctx->out,
+                    &ctx->lf_part, &ctx->lf_cost, &ctx->lf_seed, &ctx->pyr,  &ctx->partial,
+                    &ctx->score};
+  for (DevBuf* b : bufs) b->release();
+  for (auto& m : ctx->marks) {
+    cudaEventDestroy(m.a);
+    cudaEventDestroy(m.b);
+  }
+  for (cudaEvent_t e : ctx->event_pool) cudaEventDestroy(e);
+  cudaFree(ctx->d_dq);
+  cudaFree(ctx->d_words);
+  cudaFree(ctx->d_lf);
+  cudaFreeHost(ctx->h_words);
+  cudaFreeHost(ctx->h_score);
+  cudaStreamDestroy(ctx->own_stream);
+  delete ctx;
+  return JPXLG_OK;
+}
+
+int jpxlg_ctx_set_stream(jpxlg_ctx* ctx, void* stream) {
+  if (!ctx) return JPXLG_ERR_ARGUMENT;
+  ctx->stream = stream ? (cudaStream_t)stream : ctx->own_stream;
+  return JPXLG_OK;
+}
+
+void* jpxlg_ctx_stream(jpxlg_ctx* ctx) { return ctx ? (void*)ctx->stream : nullptr; }
+
+int jpxlg_ctx_synchronize(jpxlg_ctx* ctx) {
+  if (!ctx) return JPXLG_ERR_ARGUMENT;
+  cudaSetDevice(ctx->device);
+  return sync_and_check(ctx);
+}
+
+const char* jpxlg_last_error(const jpxlg_ctx* ctx) {
+  return ctx ? ctx->last_error.c_str() : "null context";
+}
+
+uint64_t jpxlg_ctx_launches(const jpxlg_ctx* ctx) { return ctx ? ctx->launches : 0; }
+
+int jpxlg_stage_timing(jpxlg_ctx* ctx, int enable) {
+  if (!ctx) return JPXLG_ERR_ARGUMENT;
+  ctx->timing = enable != 0;
+  return JPXLG_OK;
+}
+
+int jpxlg_stage_times(jpxlg_ctx* ctx, double* ms, uint64_t* launches, int n) {
+  if (!ctx) return JPXLG_ERR_ARGUMENT;
+  cudaSetDevice(ctx->device);
+  CK(cudaStreamSynchronize(ctx->stream));
+  for (auto& m : ctx->marks) {
+    float t = 0.0f;
+    if (cudaEventElapsedTime(&t, m.a, m.b) == cudaSuccess) ctx->stage_ms[m.stage] += t;
+    ctx->stage_launches[m.stage] += m.launches;
+    ctx->event_pool.push_back(m.a);
+    ctx->event_pool.push_back(m.b);
+  }
+  ctx->marks.clear();
+  for (int i = 0; i < JPXLG_STAGE_COUNT && i < n; ++i) {
+    if (ms) ms[i] = ctx->stage_ms[i];
+    if (launches) launches[i] = ctx->stage_launches[i];
+    ctx->stage_ms[i] = 0.0;
+    ctx->stage_launches[i] = 0;
+  }
+  return JPXLG_STAGE_COUNT;
+}
+
+int jpxlg_layout_create(jpxlg_ctx* ctx, int width, int height, const uint8_t* block_map,
+                        const uint32_t* hf_mul, const uint8_t* sharpness, jpxlg_layout** out) {
+  if (!ctx || !out || !block_map || !hf_mul) return fail(ctx, JPXLG_ERR_ARGUMENT, "null argument");
+  *out = nullptr;
+  if (width <= 0 || height <= 0 || width > 65535 * 8 || height > 65535 * 8)
+    return fail(ctx, JPXLG_ERR_ARGUMENT, "frame %dx%d outside 1..524280", width, height);
+  cudaSetDevice(ctx->device);
+  std::unique_ptr<jpxlg_layout> L(new jpxlg_layout);
+  L->ctx = ctx;
+  L->geo = make_geo(width, height);
+  const Geo& g = L->geo;
+  const size_t nb = (size_t)g.bw * g.bh;
+  // Validate the cover (every block covered exactly once by naturally
+  // aligned varblocks of the nine plain DCT shapes) and bucket origins.
+  std::vector<uint8_t> covered(nb, 0);
+  std::vector<uint32_t> bucket[kNumShapes];
+  for (int by = 0; by < g.bh; ++by)
+    for (int bx = 0; bx < g.bw; ++bx) {
+      uint8_t e = block_map[(size_t)by * g.bw + bx];
+      if (!(e & 0x80)) continue;
+      int sel = e & 0x1f;
+      Shape sh;
+      if (!shape_of(sel, &sh))
+        return fail(ctx, JPXLG_ERR_BLOCK_MAP, "block (%d,%d): DctSelect %d is not a plain DCT", bx,
+                    by, sel);
+      if (bx % sh.bcols || by % sh.brows || bx + sh.bcols > g.bw || by + sh.brows > g.bh)
+        return fail(ctx, JPXLG_ERR_BLOCK_MAP, "block (%d,%d): varblock misaligned or outside", bx,
+                    by);
+      for (int dy = 0; dy < sh.brows; ++dy)
+        for (int dx = 0; dx < sh.bcols; ++dx) {
+          size_t i = (size_t)(by + dy) * g.bw + bx + dx;
+          if (covered[i] || (block_map[i] & 0x1f) != sel)
+            return fail(ctx, JPXLG_ERR_BLOCK_MAP, "block (%d,%d): overlapping varblocks", bx + dx,
+                        by + dy);
+          covered[i] = 1;
+        }
+      int cls = 0;
+      while (kShapeSel[cls] != sel) ++cls;
+      bucket[cls].push_back(((uint32_t)by << 16) | (uint32_t)bx);
+      if (sh.brows != sh.bcols) L->all_square = false;
+      if (hf_mul[(size_t)by * g.bw + bx] == 0)
+        return fail(ctx, JPXLG_ERR_ARGUMENT, "block (%d,%d): hf_mul must be positive", bx, by);
+    }
+  for (size_t i = 0; i < nb; ++i)
+    if (!covered[i])
+      return fail(ctx, JPXLG_ERR_BLOCK_MAP, "block (%zu,%zu) is not covered", i % g.bw, i / g.bw);
+  L->base_hf_mul = hf_mul[0];
+  size_t total = 0;
+  for (auto& b : bucket) total += b.size();
+  CK(cudaMalloc(&L->d_map, nb));
+  CK(cudaMalloc(&L->d_hf_mul, nb * sizeof(uint32_t)));
+  CK(cudaMalloc(&L->d_sharp, nb));
+  CK(cudaMalloc(&L->d_lists, std::max<size_t>(total, 1) * sizeof(uint32_t)));
+  CK(cudaMemcpy(L->d_map, block_map, nb, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(L->d_hf_mul, hf_mul, nb * sizeof(uint32_t), cudaMemcpyHostToDevice));
+  if (sharpness) CK(cudaMemcpy(L->d_sharp, sharpness, nb, cudaMemcpyHostToDevice));
+  else CK(cudaMemset(L->d_sharp, 0, nb));
+  size_t off = 0;
+  for (int c = 0; c < kNumShapes; ++c) {
+    L->counts[c] = (int)bucket[c].size();
+    L->lists[c] = L->d_lists + off;
+    if (!bucket[c].empty())
+      CK(cudaMemcpy(L->d_lists + off, bucket[c].data(), bucket[c].size() * sizeof(uint32_t),
+                    cudaMemcpyHostToDevice));
+    off += bucket[c].size();
+  }
+  *out = L.release();
+  return JPXLG_OK;
+}
+
+int jpxlg_layout_destroy(jpxlg_layout* L) {
+  if (!L) return JPXLG_ERR_ARGUMENT;
+  cudaSetDevice(L->ctx->device);
+  cudaStreamSynchronize(L->ctx->stream);
+  cudaFree(L->d_map);
+  cudaFree(L->d_hf_mul);
+  cudaFree(L->d_sharp);
+  cudaFree(L->d_lists);
+  delete L;
+  return JPXLG_OK;
+}
+
+int jpxlg_layout_dims(const jpxlg_layout* L, int* bw, int* bh, int* tw, int* th) {
+  if (!L) return JPXLG_ERR_ARGUMENT;
+  if (bw) *bw = L->geo.bw;
+  if (bh) *bh = L->geo.bh;
+  if (tw) *tw = L->geo.tw;
+  if (th) *th = L->geo.th;
+  return JPXLG_OK;
+}
+
+int jpxlg_encode_transform(jpxlg_ctx* ctx, const jpxlg_layout* L, const void* rgb, int bits,
+                           const jpxlg_params* p, jpxlg_plan* plan, uint32_t mem) {
+  if (!ctx || !L || !rgb || !plan) return fail(ctx, JPXLG_ERR_ARGUMENT, "null argument");
+  if (!(bits == 8 || (bits >= 9 && bits <= 16)))
+    return fail(ctx, JPXLG_ERR_ARGUMENT, "bits must be 8 or 9..16");
+  int rc = check_params(ctx, p);
+  if (rc) return rc;
+  cudaSetDevice(ctx->device);
+  const Geo& g = L->geo;
+  const size_t n = (size_t)g.w * g.h, n8 = (size_t)g.W8 * g.H8, nb = (size_t)g.bw * g.bh;
+  const size_t nt = (size_t)g.tw * g.th;
+  const size_t rgb_bytes = 3 * n * (bits == 8 ? 1 : 2);
+  if (mem == JPXLG_MEM_DEVICE) {
+    if (!plan->qcoeff || !plan->lf || !plan->cfl_x || !plan->cfl_b)
+      return fail(ctx, JPXLG_ERR_ARGUMENT, "null plan buffer");
+    rc = encode_device(ctx, L, rgb, bits, p, plan->qcoeff, plan->lf, plan->cfl_x, plan->cfl_b,
+                       plan->lf_factors);
+    if (rc) return rc;
+    // The two LF factors are plan scalars the caller needs on the host: the
+    // call waits for them (8 bytes) and reports device-side errors.
+    rc = sync_and_check(ctx);
+    if (rc) return rc;
+    const int* f = (const int*)(ctx->h_words + 4);
+    plan->lf_factors[0] = f[0] + 128;
+    plan->lf_factors[1] = f[1] + 128;
+    return JPXLG_OK;
+  }
+  CK(ctx->rgb.ensure(rgb_bytes));
+  CK(ctx->qcoeff.ensure(3 * n8 * sizeof(int32_t)));
+  CK(ctx->lfq.ensure(3 * nb * sizeof(int32_t)));
+  CK(ctx->cflx.ensure(nt));
+  CK(ctx->cflb.ensure(nt));
+  CK(cudaMemcpyAsync(ctx->rgb.p, rgb, rgb_bytes, cudaMemcpyHostToDevice, ctx->stream));
+  rc = encode_device(ctx, L, ctx->rgb.p, bits, p, ctx->qcoeff.as<int32_t>(), ctx->lfq.as<int32_t>(),
+                     ctx->cflx.as<int8_t>(), ctx->cflb.as<int8_t>(), plan->lf_factors);
+  if (rc) return rc;
+  if (plan->qcoeff)
+    CK(cudaMemcpyAsync(plan->qcoeff, ctx->qcoeff.p, 3 * n8 * sizeof(int32_t),
+                       cudaMemcpyDeviceToHost, ctx->stream));
+  if (plan->lf)
+    CK(cudaMemcpyAsync(plan->lf, ctx->lfq.p, 3 * nb * sizeof(int32_t), cudaMemcpyDeviceToHost,
+                       ctx->stream));
+  if (plan->cfl_x) CK(cudaMemcpyAsync(plan->cfl_x, ctx->cflx.p, nt, cudaMemcpyDeviceToHost, ctx->stream));
+  if (plan->cfl_b) CK(cudaMemcpyAsync(plan->cfl_b, ctx->cflb.p, nt, cudaMemcpyDeviceToHost, ctx->stream));
+  rc = sync_and_check(ctx);
+  if (rc) return rc;
+  const int* f = (const int*)(ctx->h_words + 4);
+  plan->lf_factors[0] = f[0] + 128;
+  plan->lf_factors[1] = f[1] + 128;
+  return JPXLG_OK;
+}
+
+int jpxlg_encode_stages(jpxlg_ctx* ctx, const jpxlg_layout* L, const void* rgb, int bits,
+                        const jpxlg_params* p, float* xyb, float* pre, float* coeff) {
+  if (!ctx || !L || !rgb) return fail(ctx, JPXLG_ERR_ARGUMENT, "null argument");
+  if (!(bits == 8 || (bits >= 9 && bits <= 16)))
+    return fail(ctx, JPXLG_ERR_ARGUMENT, "bits must be 8 or 9..16");
+  int rc = check_params(ctx, p);
+  if (rc) return rc;
+  cudaSetDevice(ctx->device);
+  const Geo& g = L->geo;
+  const size_t n = (size_t)g.w * g.h, n8 = (size_t)g.W8 * g.H8, nb = (size_t)g.bw * g.bh;
+  const size_t nt = (size_t)g.tw * g.th;
+  const size_t rgb_bytes = 3 * n * (bits == 8 ? 1 : 2);
+  CK(ctx->rgb.ensure(rgb_bytes));
+  CK(ctx->qcoeff.ensure(3 * n8 * sizeof(int32_t)));
+  CK(ctx->lfq.ensure(3 * nb * sizeof(int32_t)));
+  CK(ctx->cflx.ensure(nt));
+  CK(ctx->cflb.ensure(nt));
+  CK(cudaMemcpyAsync(ctx->rgb.p, rgb, rgb_bytes, cudaMemcpyHostToDevice, ctx->stream));
+  rc = encode_device(ctx, L, ctx->rgb.p, bits, p, ctx->qcoeff.as<int32_t>(), ctx->lfq.as<int32_t>(),
+                     ctx->cflx.as<int8_t>(), ctx->cflb.as<int8_t>(), nullptr);
+  if (rc) return rc;
+  if (xyb) CK(cudaMemcpyAsync(xyb, ctx->xyb.p, 3 * n * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream));
+  if (pre)
+    CK(cudaMemcpyAsync(pre, p->gaborish ? ctx->pre.p : ctx->xyb.p, 3 * n * sizeof(float),
+                       cudaMemcpyDeviceToHost, ctx->stream));
+  if (coeff)
+    CK(cudaMemcpyAsync(coeff, ctx->coeff.p, 3 * n8 * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream));
+  return sync_and_check(ctx);
+}
+
+int jpxlg_reconstruct(jpxlg_ctx* ctx, const jpxlg_layout* L, const jpxlg_plan* plan,
+                      const jpxlg_params* p, int out_kind, int bits, void* out, uint32_t mem) {
+  if (!ctx || !L || !plan || !out) return fail(ctx, JPXLG_ERR_ARGUMENT, "null argument");
+  if (!plan->qcoeff || !plan->lf || !plan->cfl_x || !plan->cfl_b)
+    return fail(ctx, JPXLG_ERR_ARGUMENT, "null plan buffer");
+  int rc = check_params(ctx, p);
+  if (rc) return rc;
+  if (out_kind < 0 || out_kind > 3) return fail(ctx, JPXLG_ERR_ARGUMENT, "bad out_kind");
+  if (out_kind == JPXLG_OUT_LINEAR_DEPTH && (bits < 1 || bits > 16))
+    return fail(ctx, JPXLG_ERR_ARGUMENT, "depth must be 1..16 bits");
+  for (int i = 0; i < 2; ++i)
+    if (plan->lf_factors[i] < 0 || plan->lf_factors[i] > 255)
+      return fail(ctx, JPXLG_ERR_ARGUMENT, "LF factor outside u8");
+  cudaSetDevice(ctx->device);
+  const Geo& g = L->geo;
+  const size_t n = (size_t)g.w * g.h, n8 = (size_t)g.W8 * g.H8, nb = (size_t)g.bw * g.bh;
+  const size_t nt = (size_t)g.tw * g.th;
+  const size_t out_bytes = out_kind == JPXLG_OUT_SRGB8 ? 3 * n : 3 * n * sizeof(float);
+  if (mem == JPXLG_MEM_DEVICE)
+    return render_device(ctx, L, plan->qcoeff, plan->lf, plan->cfl_x, plan->cfl_b,
+                         plan->lf_factors[0], plan->lf_factors[1], nullptr, p, out_kind, bits, out);
+  CK(ctx->qcoeff.ensure(3 * n8 * sizeof(int32_t)));
+  CK(ctx->lfq.ensure(3 * nb * sizeof(int32_t)));
+  CK(ctx->cflx.ensure(nt));
+  CK(ctx->cflb.ensure(nt));
+  CK(ctx->out.ensure(out_bytes));
+  CK(cudaMemcpyAsync(ctx->qcoeff.p, plan->qcoeff, 3 * n8 * sizeof(int32_t), cudaMemcpyHostToDevice,
+                     ctx->stream));
+  CK(cudaMemcpyAsync(ctx->lfq.p, plan->lf, 3 * nb * sizeof(int32_t), cudaMemcpyHostToDevice,
+                     ctx->stream));
+  CK(cudaMemcpyAsync(ctx->cflx.p, plan->cfl_x, nt, cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(ctx->cflb.p, plan->cfl_b, nt, cudaMemcpyHostToDevice, ctx->stream));
+  rc = render_device(ctx, L, ctx->qcoeff.as<int32_t>(), ctx->lfq.as<int32_t>(), ctx->cflx.as<int8_t>(),
+                     ctx->cflb.as<int8_t>(), plan->lf_factors[0], plan->lf_factors[1], nullptr, p,
+                     out_kind, bits, ctx->out.p);
+  if (rc) return rc;
+  CK(cudaMemcpyAsync(out, ctx->out.p, out_bytes, cudaMemcpyDeviceToHost, ctx->stream));
+  return sync_and_check(ctx);
+}
+
+int jpxlg_ssim2_ref_create(jpxlg_ctx* ctx, const float* rgb, int w, int h, uint32_t mem,
+                           jpxlg_ref** out) {
+  if (!ctx || !rgb || !out) return fail(ctx, JPXLG_ERR_ARGUMENT, "null argument");
+  *out = nullptr;
+  if (w < 8 || h < 8) return fail(ctx, JPXLG_ERR_TOO_SMALL, "SSIMULACRA2 needs at least 8x8");
+  cudaSetDevice(ctx->device);
+  std::unique_ptr<jpxlg_ref> R(new jpxlg_ref);
+  R->ctx = ctx;
+  R->w = w;
+  R->h = h;
+  // reference.rs:90 — keep halving while the current scale is at least 8x8.
+  int cw = w, ch = h, ns = 0;
+  size_t total = 0;
+  int dims[6][2];
+  for (int s = 0; s < 6; ++s) {
+    if (s > 0) {
+      if (cw < 8 || ch < 8) break;
+      cw = (cw + 1) / 2;
+      ch = (ch + 1) / 2;
+    }
+    dims[s][0] = cw;
+    dims[s][1] = ch;
+    total += 9 * (size_t)cw * ch + 3 * (size_t)cw * ch;  // xyb, mu, s11 + rgb level
+    ++ns;
+  }
+  R->nscales = ns;
+  CK(cudaMalloc(&R->block, total * sizeof(float)));
+  float* cursor = (float*)R->block;
+  const size_t n0 = (size_t)w * h;
+  CK(ctx->aux.ensure(n0 * sizeof(float)));
+  CK(ctx->out.ensure(3 * n0 * sizeof(float)));
+  const float* src = rgb;
+  if (mem == JPXLG_MEM_HOST) {
+    CK(cudaMemcpyAsync(ctx->out.p, rgb, 3 * n0 * sizeof(float), cudaMemcpyHostToDevice, ctx->stream));
+    src = ctx->out.as<float>();
+  }
+  uint64_t k = 0;
+  const float* level = src;
+  for (int s = 0; s < ns; ++s) {
+    SsimScale& sc = R->scales[s];
+    sc.w = dims[s][0];
+    sc.h = dims[s][1];
+    const size_t n = (size_t)sc.w * sc.h;
+    float* rgb_s = cursor;
+    cursor += 3 * n;
+    if (s > 0) {
+      launch_downscale3(level, dims[s - 1][0], dims[s - 1][1], rgb_s, ctx->stream);
+      ++k;
+      level = rgb_s;
+    }
+    sc.xyb = cursor;
+    cursor += 3 * n;
+    sc.mu = cursor;
+    cursor += 3 * n;
+    sc.s11 = cursor;
+    cursor += 3 * n;
+    launch_positive_xyb(level, sc.xyb, n, ctx->num_sms, ctx->stream);
+    launch_ref_moments(sc.xyb, sc.mu, sc.s11, ctx->aux.as<float>(), sc.w, sc.h, ctx->stream);
+    k += 1 + 12;
+  }
+  int rc = after_launch(ctx, k);
+  if (rc) {
+    cudaFree(R->block);
+    return rc;
+  }
+  if (mem == JPXLG_MEM_HOST) {
+    rc = sync_and_check(ctx);
+    if (rc) {
+      cudaFree(R->block);
+      return rc;
+    }
+  }
+  *out = R.release();
+  return JPXLG_OK;
+}
+
+int jpxlg_ssim2_ref_destroy(jpxlg_ref* R) {
+  if (!R) return JPXLG_ERR_ARGUMENT;
+  cudaSetDevice(R->ctx->device);
+  cudaStreamSynchronize(R->ctx->stream);
+  cudaFree(R->block);
+  delete R;
+  return JPXLG_OK;
+}
+
+int jpxlg_ssim2_score(jpxlg_ctx* ctx, const jpxlg_ref* R, const float* rgb, uint32_t mem,
+                      double* score, double* raw_error, double* terms) {
+  if (!ctx || !R || !rgb) return fail(ctx, JPXLG_ERR_ARGUMENT, "null argument");
+  cudaSetDevice(ctx->device);
+  const size_t n = (size_t)R->w * R->h;
+  CK(ctx->score.ensure(128 * sizeof(double)));
+  const float* cand = rgb;
+  if (mem == JPXLG_MEM_HOST) {
+    CK(ctx->out.ensure(3 * n * sizeof(float)));
+    CK(cudaMemcpyAsync(ctx->out.p, rgb, 3 * n * sizeof(float), cudaMemcpyHostToDevice, ctx->stream));
+    cand = ctx->out.as<float>();
+  }
+  int rc = score_device(ctx, R, cand, mem == JPXLG_MEM_DEVICE && score ? score : ctx->score.as<double>());
+  if (rc) return rc;
+  if (mem == JPXLG_MEM_DEVICE) return JPXLG_OK;
+  CK(cudaMemcpyAsync(ctx->h_score, ctx->score.p, (2 + 108) * sizeof(double), cudaMemcpyDeviceToHost,
+                     ctx->stream));
+  rc = sync_and_check(ctx);
+  if (rc) return rc;
+  if (score) *score = ctx->h_score[0];
+  if (raw_error) *raw_error = ctx->h_score[1];
+  if (terms)
+    for (int i = 0; i < R->nscales * 18; ++i) terms[i] = ctx->h_score[2 + i];
+  return JPXLG_OK;
+}
+
+int jpxlg_score_pair(jpxlg_ctx* ctx, const float* ref_rgb, const float* cand_rgb, int w, int h,
+                     uint32_t mem, double* score) {
+  jpxlg_ref* R = nullptr;
+  int rc = jpxlg_ssim2_ref_create(ctx, ref_rgb, w, h, mem, &R);
+  if (rc) return rc;
+  rc = jpxlg_ssim2_score(ctx, R, cand_rgb, mem, score, nullptr, nullptr);
+  if (mem == JPXLG_MEM_DEVICE && rc == JPXLG_OK) rc = sync_and_check(ctx);
+  jpxlg_ssim2_ref_destroy(R);
+  return rc;
+}
+
+int jpxlg_probe(jpxlg_ctx* ctx, const jpxlg_layout* L, const jpxlg_ref* R, const void* rgb,
+                int bits, const jpxlg_params* p, uint32_t mem, double* score) {
+  if (!ctx || !L || !R || !rgb || !score) return fail(ctx, JPXLG_ERR_ARGUMENT, "null argument");
+  if (R->w != L->geo.w || R->h != L->geo.h)
+    return fail(ctx, JPXLG_ERR_MISMATCH, "reference and layout dimensions differ");
+  int rc = check_params(ctx, p);
+  if (rc) return rc;
+  cudaSetDevice(ctx->device);
+  const Geo& g = L->geo;
+  const size_t n = (size_t)g.w * g.h, n8 = (size_t)g.W8 * g.H8, nb = (size_t)g.bw * g.bh;
+  const size_t nt = (size_t)g.tw * g.th;
+  CK(ctx->qcoeff.ensure(3 * n8 * sizeof(int32_t)));
+  CK(ctx->lfq.ensure(3 * nb * sizeof(int32_t)));
+  CK(ctx->cflx.ensure(nt));
+  CK(ctx->cflb.ensure(nt));
+  CK(ctx->out.ensure(3 * n * sizeof(float)));
+  CK(ctx->score.ensure(128 * sizeof(double)));
+  const void* src = rgb;
+  if (mem == JPXLG_MEM_HOST) {
+    const size_t rgb_bytes = 3 * n * (bits == 8 ? 1 : 2);
+    CK(ctx->rgb.ensure(rgb_bytes));
+    CK(cudaMemcpyAsync(ctx->rgb.p, rgb, rgb_bytes, cudaMemcpyHostToDevice, ctx->stream));
+    src = ctx->rgb.p;
+  }
+  rc = encode_device(ctx, L, src, bits, p, ctx->qcoeff.as<int32_t>(), ctx->lfq.as<int32_t>(),
+                     ctx->cflx.as<int8_t>(), ctx->cflb.as<int8_t>(), nullptr);
+  if (rc) return rc;
+  rc = render_device(ctx, L, ctx->qcoeff.as<int32_t>(), ctx->lfq.as<int32_t>(),
+                     ctx->cflx.as<int8_t>(), ctx->cflb.as<int8_t>(), 128, 128, ctx->d_lf, p,
+                     JPXLG_OUT_LINEAR_DEPTH, bits, ctx->out.p);
+  if (rc) return rc;
+  double* dst = mem == JPXLG_MEM_DEVICE ? score : ctx->score.as<double>();
+  rc = score_device(ctx, R, ctx->out.as<float>(), dst);
+  if (rc) return rc;
+  if (mem == JPXLG_MEM_DEVICE) return JPXLG_OK;
+  CK(cudaMemcpyAsync(ctx->h_score, ctx->score.p, sizeof(double), cudaMemcpyDeviceToHost,
+                     ctx->stream));
+  rc = sync_and_check(ctx);
+  if (rc) return rc;
+  *score = ctx->h_score[0];
+  return JPXLG_OK;
+}
+
+}  // extern "C"

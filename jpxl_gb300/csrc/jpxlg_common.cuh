@@ -1,0 +1,283 @@
+// jpxlg_common.cuh — device helpers shared by the sm_103a kernels of the
+// lossy VarDCT pixel path: exact-parity cube roots, mirroring, the transform
+// table, the DCT butterflies and the error word.
+//
+// Everything here is compiled with -fmad=false: a*b+c always rounds twice,
+// exactly as the Rust reference (which never contracts), and __fmaf_rn is
+// written out exactly where the reference calls mul_add.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace jpxlg {
+
+// ---- error word (device -> host) -------------------------------------------
+// A kernel that meets a condition for which the reference returns an Err
+// records it with atomicOr into the context's error word instead of
+// trapping; the host reads the word after the stage and returns a status.
+enum DevError : uint32_t {
+  kDevQuantRange = 1u << 0,   // clamp_round saw a non-finite or |q| > 2^20 target
+  kDevBadStep = 1u << 1,      // degenerate quantization step
+  kDevBlockMap = 1u << 2,     // a block-map entry the kernel cannot place
+};
+
+__device__ __forceinline__ void raise_error(uint32_t* err, uint32_t bit) {
+  if (err) atomicOr(err, bit);
+}
+
+// ---- mirroring (18181-1 5.2 Mirror1D) ---------------------------------------
+__device__ __forceinline__ int mirror1d(int c, int size) {
+  // Bounded: a coordinate at most a few samples outside needs at most a few
+  // reflections even for a one-sample plane.
+  for (int i = 0; i < 64; ++i) {
+    if (c < 0) c = -c - 1;
+    else if (c >= size) c = 2 * size - 1 - c;
+    else return c;
+  }
+  return 0;
+}
+
+// ---- transforms -------------------------------------------------------------
+// The nine plain DCTRxC types (Table I.1): DctSelect, footprint rows/cols in
+// blocks, dequant matrix slot (0..5 in the library's compact table).
+struct Shape {
+  int brows, bcols;
+};
+__host__ __device__ __forceinline__ bool shape_of(int sel, Shape* s) {
+  switch (sel) {
+    case 0: *s = {1, 1}; return true;
+    case 4: *s = {2, 2}; return true;
+    case 5: *s = {4, 4}; return true;
+    case 6: *s = {2, 1}; return true;
+    case 7: *s = {1, 2}; return true;
+    case 8: *s = {4, 1}; return true;
+    case 9: *s = {1, 4}; return true;
+    case 10: *s = {4, 2}; return true;
+    case 11: *s = {2, 4}; return true;
+    default: return false;
+  }
+}
+// compact dequant slot: 0 DCT8, 1 DCT16x16, 2 DCT32x32, 3 DCT16x8/8x16,
+// 4 DCT32x8/8x32, 5 DCT32x16/16x32 (Table I.4 indices 0,4,5,6,7,8).
+__host__ __device__ __forceinline__ int dq_slot(int sel) {
+  switch (sel) {
+    case 0: return 0;
+    case 4: return 1;
+    case 5: return 2;
+    case 6: case 7: return 3;
+    case 8: case 9: return 4;
+    default: return 5;
+  }
+}
+// Offsets of each slot's landscape matrix in the packed dequant table.
+__host__ __device__ __forceinline__ int dq_offset(int slot) {
+  // sizes: 64, 256, 1024, 128, 256, 512
+  const int off[6] = {0, 64, 320, 1344, 1472, 1728};
+  return off[slot];
+}
+constexpr int kDequantTableFloats = 2240;  // per channel
+
+// ---- exact-parity cube roots -----------------------------------------------
+// The reference has two cube roots, each f64 iteration rounded once to f32:
+// jpxl-core simd.rs:36 (estimate + 2 Halley steps) and jpxl-perceptual
+// color.rs:46 (estimate + 4 Newton steps).  Both land within ~2^-24 ulp of the
+// exact cube root, i.e. they return the correctly rounded cube root unless
+// the exact root lies within that distance of a rounding midpoint.  The fast
+// path below finds the correctly rounded root in f32 arithmetic (CUDA's
+// cbrtf, then a double-float residual that places the exact root to within
+// 2^-21 ulp); where the root lies within 2^-17 ulp of a midpoint, or the input
+// is outside the verified range, it runs the reference's own f64 iteration,
+// so the result is the reference's bit for bit either way.
+
+static __device__ __noinline__ float cbrt_core_f64(float value) {
+  const uint32_t B1 = 709958130u, B2 = 642849266u;
+  uint32_t bits = __float_as_uint(value);
+  uint32_t magnitude = bits & 0x7fffffffu;
+  if (magnitude == 0 || magnitude >= 0x7f800000u) return value;
+  uint32_t estimate;
+  if (magnitude < 0x00800000u) {
+    float scaled = value * 16777216.0f;
+    estimate = (__float_as_uint(scaled) & 0x7fffffffu) / 3u + B2;
+  } else {
+    estimate = magnitude / 3u + B1;
+  }
+  double x = (double)value;
+  double t = (double)__uint_as_float((bits & 0x80000000u) | estimate);
+  for (int i = 0; i < 2; ++i) {
+    double r = (t * t) * t;
+    t = (t * ((x + x) + r)) / ((x + r) + r);
+  }
+  return (float)t;
+}
+
+static __device__ __noinline__ float cbrt_perceptual_f64(float value) {
+  double x = (double)value;
+  double a = fabs(x);
+  unsigned long long ab = (unsigned long long)__double_as_longlong(a);
+  double y = __longlong_as_double((long long)(ab / 3ull + (0x2A9F7893ull << 32)));
+  for (int i = 0; i < 4; ++i) y -= (((y * y) * y) - a) / ((3.0 * y) * y);
+  float root = (float)y;
+  float signed_root = x < 0.0 ? -root : root;
+  if (value == 0.0f || !isfinite(value)) return value;
+  return signed_root;
+}
+
+// Correctly rounded cbrt of a > 0 in [2^-90, 2^90]; sets *ok = false where
+// the decision is not certain to 2^-17 ulp.
+__device__ __forceinline__ float cbrt_cr_fast(float a, bool* ok) {
+  float y = cbrtf(a);
+  uint32_t yb = __float_as_uint(y);
+  float p = y * y;
+  float e1 = __fmaf_rn(y, y, -p);   // y*y = p + e1 exactly
+  float q = p * y;
+  float e2 = __fmaf_rn(p, y, -q);   // p*y = q + e2 exactly
+  float e3 = e1 * y;                // e1*y, rounded (relative 2^-48 of y^3)
+  float d = (q - a) + (e2 + e3);    // y^3 - a; q - a is exact (Sterbenz)
+  int e = (int)((yb >> 23) & 0xffu) - 127;
+  float inv_ulp = __uint_as_float((uint32_t)(127 + 23 - e) << 23);  // 2^(23-e)
+  float delta = (-d / (3.0f * p)) * inv_ulp;  // (cbrt(a) - y) in ulps of y
+  float k = rintf(delta);
+  float frac = fabsf(delta - k);
+  *ok = frac < 0.5f - 7.62939453125e-06f && fabsf(delta) < 2.5f;  // 2^-17
+  int ki = (int)k;
+  uint32_t mant = yb & 0x7fffffu;
+  if ((ki < 0 && mant < (uint32_t)(-ki)) || (ki > 0 && mant + (uint32_t)ki > 0x7fffffu))
+    *ok = false;  // the step would cross a binade, where the ulp changes
+  return __uint_as_float(yb + ki);
+}
+
+// jpxl-core simd.rs:36 reproducible_cbrt, bit for bit.
+__device__ __forceinline__ float cbrt_core(float v) {
+  float a = fabsf(v);
+  if (a >= 8.0e-28f && a <= 1.2e27f) {
+    bool ok;
+    float r = cbrt_cr_fast(a, &ok);
+    if (ok) return copysignf(r, v);
+  }
+  return cbrt_core_f64(v);
+}
+
+// jpxl-perceptual color.rs:46 reproducible_cbrt, bit for bit.
+__device__ __forceinline__ float cbrt_perceptual(float v) {
+  float a = fabsf(v);
+  if (a >= 8.0e-28f && a <= 1.2e27f) {
+    bool ok;
+    float r = cbrt_cr_fast(a, &ok);
+    if (ok) return copysignf(r, v);
+  }
+  return cbrt_perceptual_f64(v);
+}
+
+// ---- DCT butterflies (jpxl-core dct.rs:235-465) -----------------------------
+// Orthonormal DCT-IV leaves live in constant memory (filled by the host from
+// the reference's first-row magnitudes); loops over them are unrolled, so
+// every coefficient is a constant-bank operand.
+extern __constant__ float c_iv4[16];
+extern __constant__ float c_iv8[64];
+extern __constant__ float c_iv16[256];
+
+constexpr float kSqrtHalf = 0.707106769f;
+constexpr float kCosPi8 = 0.9238795f;
+constexpr float kSinPi8 = 0.38268343f;
+
+template <int M>
+__device__ __forceinline__ float iv_coef(int u, int n) {
+  if constexpr (M == 4) return c_iv4[u * 4 + n];
+  else if constexpr (M == 8) return c_iv8[u * 8 + n];
+  else return c_iv16[u * 16 + n];
+}
+
+template <int M>
+__device__ __forceinline__ void dct_iv(float* v) {
+  if constexpr (M == 2) {
+    float x0 = v[0], x1 = v[1];
+    v[0] = kCosPi8 * x0 + kSinPi8 * x1;
+    v[1] = kSinPi8 * x0 - kCosPi8 * x1;
+  } else {
+    float x[M];
+#pragma unroll
+    for (int i = 0; i < M; ++i) x[i] = v[i];
+#pragma unroll
+    for (int u = 0; u < M; ++u) {
+      float acc = 0.0f;
+#pragma unroll
+      for (int n = 0; n < M; ++n) acc = acc + iv_coef<M>(u, n) * x[n];
+      v[u] = acc;
+    }
+  }
+}
+
+__device__ __forceinline__ void dct_ii_2(float* v) {
+  float x0 = v[0], x1 = v[1];
+  v[0] = (x0 + x1) * kSqrtHalf;
+  v[1] = (x0 - x1) * kSqrtHalf;
+}
+
+template <int N>
+__device__ __forceinline__ void dct_ii(float* v) {
+  if constexpr (N == 1) {
+  } else if constexpr (N == 2) {
+    dct_ii_2(v);
+  } else {
+    constexpr int H = N / 2;
+    float even[H], odd[H];
+#pragma unroll
+    for (int k = 0; k < H; ++k) {
+      even[k] = v[k] + v[N - 1 - k];
+      odd[k] = v[k] - v[N - 1 - k];
+    }
+    dct_ii<H>(even);
+    dct_iv<H>(odd);
+#pragma unroll
+    for (int k = 0; k < H; ++k) {
+      v[2 * k] = even[k] * kSqrtHalf;
+      v[2 * k + 1] = odd[k] * kSqrtHalf;
+    }
+  }
+}
+
+template <int N>
+__device__ __forceinline__ void dct_iii(float* v) {
+  if constexpr (N == 1) {
+  } else if constexpr (N == 2) {
+    dct_ii_2(v);
+  } else {
+    constexpr int H = N / 2;
+    float even[H], odd[H];
+#pragma unroll
+    for (int k = 0; k < H; ++k) {
+      even[k] = v[2 * k] * kSqrtHalf;
+      odd[k] = v[2 * k + 1] * kSqrtHalf;
+    }
+    dct_iii<H>(even);
+    dct_iv<H>(odd);
+#pragma unroll
+    for (int k = 0; k < H; ++k) {
+      v[k] = even[k] + odd[k];
+      v[N - 1 - k] = even[k] - odd[k];
+    }
+  }
+}
+
+// dct.rs:731/749: normative scaling after the butterfly.  The factors are
+// 1/sqrtf(N) and sqrtf(N) in f32, as the reference computes them.
+template <int N>
+__device__ __forceinline__ float fwd_factor() {
+  return 1.0f / sqrtf((float)N);
+}
+template <int N>
+__device__ __forceinline__ void dct_1d(float* v) {
+  dct_ii<N>(v);
+  const float f = 1.0f / __fsqrt_rn((float)N);
+#pragma unroll
+  for (int i = 0; i < N; ++i) v[i] *= f;
+}
+template <int N>
+__device__ __forceinline__ void idct_1d(float* v) {
+  dct_iii<N>(v);
+  const float f = __fsqrt_rn((float)N);
+#pragma unroll
+  for (int i = 0; i < N; ++i) v[i] *= f;
+}
+
+}  // namespace jpxlg

@@ -1,0 +1,57 @@
+// jpxlg_internal.h — host-side declarations shared by the library's
+// translation units: frame geometry, the per-call parameter blocks passed to
+// kernels, the host table builders and the kernel launchers.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace jpxlg {
+
+struct Geo {
+  int w, h;    // pixels
+  int bw, bh;  // 8x8 blocks
+  int W8, H8;  // coefficient image = 8*bw x 8*bh
+  int tw, th;  // 64x64 CfL tiles
+};
+
+inline Geo make_geo(int w, int h) {
+  Geo g;
+  g.w = w;
+  g.h = h;
+  g.bw = (w + 7) / 8;
+  g.bh = (h + 7) / 8;
+  g.W8 = g.bw * 8;
+  g.H8 = g.bh * 8;
+  g.tw = (g.bw + 7) / 8;
+  g.th = (g.bh + 7) / 8;
+  return g;
+}
+
+// Quantizer scalars shared by encode and render (formed on the host exactly
+// as the reference forms them; see tables.cu).
+struct QuantScalars {
+  uint32_t global_scale;
+  float m_dc[3];       // LF multipliers (reconstruct.rs:67 / quantize.rs:150)
+  float qm[3];         // {qm_multiplier(x), 1, qm_multiplier(b)}
+};
+
+// Nine shape classes of the plain DCTRxC types, in this order.
+constexpr int kNumShapes = 9;
+constexpr int kShapeSel[kNumShapes] = {0, 4, 5, 6, 7, 8, 9, 10, 11};
+
+// ---- host tables (tables.cu) -------------------------------------------------
+void build_dequant_tables(float* out /* 3 * kDequantTableFloats */);
+void build_iv_tables(float* iv4, float* iv8, float* iv16);
+void build_scale_f(float* out /* [3][4]: lf counts 1,2,4 x c<4 */);
+float host_hf_multiplier(uint32_t gs, uint32_t hf_mul);
+float host_qm_multiplier(uint32_t qm_scale);
+void host_lf_multipliers(uint32_t gs, uint32_t quant_lf, float out[3]);
+float host_srgb_to_linear(float v);
+float host_linear_to_srgb(float v);
+void build_srgb_lut(int bits, float* out /* 256 or 65536 */);
+int build_depth_thresholds(int bits, float* thresholds, float* levels_linear);
+void build_blur_taps(float* taps /* 5: centre, +-1 .. +-4 */);
+void build_opsin_inverse(float* matrix9, float* bias3, float* bias_cbrt3);
+float host_cbrt_core(float v);
+
+}  // namespace jpxlg

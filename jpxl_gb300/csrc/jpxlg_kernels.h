@@ -1,0 +1,96 @@
+// jpxlg_kernels.h — argument blocks and launchers of the sm_103a kernels.
+#pragma once
+#include <cstddef>
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "jpxlg_internal.h"
+
+namespace jpxlg {
+
+// Everything the encoder kernels read and write (device pointers).
+struct EncArgs {
+  Geo geo;
+  QuantScalars qs;
+  const float* pre;          // 3 planes w*h: XYB after the optional precondition
+  const float* dq;           // [3][kDequantTableFloats] dequant multipliers
+  const uint32_t* hf_mul;    // per 8x8 block (read at varblock origins)
+  const uint8_t* block_map;  // per 8x8 block
+  float* coeff;              // [3][W8*H8] forward coefficients (f32)
+  float* dyhf;               // [W8*H8] reconstructed luma HF
+  int32_t* qcoeff;           // [3][W8*H8] quantized coefficients
+  float* lfs;                // [3][bw*bh] LF samples
+  float* dylf;               // [bw*bh] reconstructed luma LF
+  int32_t* lfq;              // [3][bw*bh] quantized LF
+  int8_t* cfl_x;             // [tw*th]
+  int8_t* cfl_b;             // [tw*th]
+  int* lf_factors;           // [2] frame LF factors, unbiased
+  const uint32_t* not_gray;  // set by the colour kernel when any pixel is not grey
+  uint32_t cfl_enabled;
+  float base_mul;            // hf multiplier of the frame's baseline hf_mul
+  uint32_t* err;
+  uint32_t* cfl_fallbacks;   // count of sequential-order fallbacks taken
+};
+
+// Everything the render kernels read and write.
+struct RenderArgs {
+  Geo geo;
+  QuantScalars qs;
+  const float* dq;
+  const uint32_t* hf_mul;
+  const uint8_t* sharpness;
+  const int32_t* qcoeff;     // [3][W8*H8]
+  const int32_t* lfq;        // [3][bw*bh]
+  const int8_t* cfl_x;
+  const int8_t* cfl_b;
+  float k_x_lf, k_b_lf;      // frame LF CfL multipliers
+  const int* lf_factors_dev; // when non-null, read the LF factors from here
+  float* planes;             // [3][w*h] XYB out
+  float* sigma;              // [bw*bh]
+};
+
+void upload_dct_constants(const float* iv4, const float* iv8, const float* iv16,
+                          const float* scale_f, cudaStream_t s);
+void launch_srgb_to_xyb(const void* rgb, int bits, size_t n, const float* lut, float* x, float* y,
+                        float* b, uint32_t* not_gray, int num_sms, cudaStream_t s);
+void launch_precondition(const float* in, float* out, int w, int h, cudaStream_t s);
+// Each returns the number of kernels it launched.
+int launch_fdct_luma(const EncArgs& a, const uint32_t* const* lists, const int* counts,
+                     cudaStream_t s);
+int launch_cfl(const EncArgs& a, double* lf_part, unsigned long long* lf_cost_part, int* lf_seeds,
+               int nparts, cudaStream_t s);
+int launch_quant_chroma(const EncArgs& a, const uint32_t* const* lists, const int* counts,
+                        cudaStream_t s);
+
+void launch_render_varblocks(const RenderArgs& a, const uint32_t* const* lists,
+                             const int* counts, cudaStream_t s);
+void launch_gaborish(const float* in, float* out, int w, int h, cudaStream_t s);
+void launch_epf_step(int step, const float* in, float* out, const float* sigma, int w, int h,
+                     cudaStream_t s);
+// out_kind: 1 linear f32 planes, 2 sRGB8 interleaved, 3 linear at depth
+void launch_colour_out(const float* xyb, int w, int h, int out_kind, const float* thresholds,
+                       const float* levels, int nlevels, void* out, int num_sms, cudaStream_t s);
+void upload_render_constants(const float* opsin_m, const float* opsin_bias,
+                             const float* opsin_bias_cbrt, cudaStream_t s);
+
+// SSIMULACRA2
+struct SsimScale {
+  int w, h;
+  float* xyb;   // [3][w*h]  (reference side)
+  float* mu;    // [3][w*h]
+  float* s11;   // [3][w*h]
+};
+void upload_blur_taps(const float* taps, cudaStream_t s);
+void launch_downscale3(const float* in, int w, int h, float* out, cudaStream_t s);
+void launch_positive_xyb(const float* rgb, float* xyb, size_t n, int num_sms, cudaStream_t s);
+void launch_ref_moments(const float* xyb, float* mu, float* s11, float* tmp, int w, int h,
+                        cudaStream_t s);
+// Candidate side of one scale: cand is linear RGB [3][w*h]; partial receives
+// per-CTA f64 sums [ctas][18].
+int launch_score_scale(const float* cand_rgb, const SsimScale& ref, double* partial,
+                       cudaStream_t s);
+void launch_score_finish(const double* partials, const int* ctas_per_scale, int nscales,
+                         const int* pixels_per_scale, double* out /* score, raw, terms[108] */,
+                         cudaStream_t s);
+
+}  // namespace jpxlg

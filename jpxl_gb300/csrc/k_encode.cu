@@ -1,0 +1,960 @@
+// k_encode.cu — sm_103a kernels of the encoder's transform path:
+//   K1 k_srgb_to_xyb       RGB8/RGB16 -> LUT -> linear -> XYB planes
+//   K2 k_precondition      12 fused Jacobi steps of the inverse Gaborish
+//   K3 k_fdct_luma<N>      gather + DCT_2D + LF samples + luma quantization
+//   K4 k_cfl_*             chroma-from-luma factor estimation
+//   K5 k_quant_chroma<N>   X/B quantization against reconstructed luma
+// Each kernel restates the reference arithmetic it replaces (cited per
+// kernel) in the reference's operation order; the build uses -fmad=false.
+#include <cstdint>
+
+#include "jpxlg_common.cuh"
+#include "jpxlg_internal.h"
+#include "jpxlg_kernels.h"
+
+namespace jpxlg {
+
+__constant__ float c_iv4[16];
+__constant__ float c_iv8[64];
+__constant__ float c_iv16[256];
+__constant__ float c_scale_f[12];  // [lf count 1,2,4][c < 4]
+
+// ---------------------------------------------------------------------------
+// K1 — jpxl-encode-policy source.rs:226 (RGB8) / :355 (RGB16): code point ->
+// linear through the host-built table, then jpxl-core color.rs:84 opsin mix
+// (no FMA), reproducible cube root, opponent rotation.
+// ---------------------------------------------------------------------------
+
+__device__ __forceinline__ void xyb_of(float r, float g, float b, float* x, float* y, float* s) {
+  float lm = 0.3f * r + 0.622f * g + 0.078f * b + 0.0037930734f;
+  float mm = 0.23f * r + 0.692f * g + 0.078f * b + 0.0037930734f;
+  float sm = 0.2434227f * r + 0.2047674f * g + 0.5518099f * b + 0.0037930734f;
+  float lg = cbrt_core(lm) - 0.1559542f;
+  float mg = cbrt_core(mm) - 0.1559542f;
+  float sg = cbrt_core(sm) - 0.1559542f;
+  *x = 0.5f * (lg - mg);
+  *y = 0.5f * (lg + mg);
+  *s = sg;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_srgb_to_xyb(const T* __restrict__ rgb, size_t n,
+                                                     const float* __restrict__ lut,
+                                                     float* __restrict__ px,
+                                                     float* __restrict__ py,
+                                                     float* __restrict__ pb,
+                                                     uint32_t* __restrict__ not_gray) {
+  size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  bool color = false;
+  for (; i < n; i += stride) {
+    uint32_t cr = rgb[3 * i], cg = rgb[3 * i + 1], cb = rgb[3 * i + 2];
+    color |= (cr != cg) || (cg != cb);
+    float x, y, b;
+    xyb_of(__ldg(&lut[cr]), __ldg(&lut[cg]), __ldg(&lut[cb]), &x, &y, &b);
+    px[i] = x;
+    py[i] = y;
+    pb[i] = b;
+  }
+  if (__any_sync(0xffffffffu, color) && (threadIdx.x & 31) == 0) atomicOr(not_gray, 1u);
+}
+
+void launch_srgb_to_xyb(const void* rgb, int bits, size_t n, const float* lut, float* x, float* y,
+                        float* b, uint32_t* not_gray, int num_sms, cudaStream_t s) {
+  int blocks = (int)std::min<size_t>((n + 255) / 256, (size_t)num_sms * 8);
+  if (blocks < 1) blocks = 1;
+  if (bits == 8)
+    k_srgb_to_xyb<uint8_t><<<blocks, 256, 0, s>>>((const uint8_t*)rgb, n, lut, x, y, b, not_gray);
+  else
+    k_srgb_to_xyb<uint16_t><<<blocks, 256, 0, s>>>((const uint16_t*)rgb, n, lut, x, y, b,
+                                                   not_gray);
+}
+
+// ---------------------------------------------------------------------------
+// K2 — jpxl-encode vardct/gaborish.rs:218 precondition_xyb_planes: twelve
+// Jacobi steps x <- x + (f - Kx) * (1/centre) (tail: / centre) against the
+// encoder's non-FMA J.1 kernel.  All twelve steps run on one shared-memory
+// tile with a 12-sample halo, so the plane is read once and written once.
+//
+// Bit parity with the reference's position-dependent arithmetic:
+//   * a pixel on the frame border sums its nine mirrored taps sequentially
+//     (dy outer, dx inner), acc += w*s;
+//   * an interior pixel in the SIMD groups of four that start at x = 1
+//     (x - 1 < 4*floor((w-2)/4)) evaluates mid*c + (N+S+W+E)*e + (NW+NE+SW+SE)*k;
+//   * remaining interior pixels sum the nine taps sequentially;
+//   * the update multiplies by 1/centre for flat indices below 4*floor(n/4)
+//     and divides by centre above.
+// Halo cells outside the frame hold copies of their mirror images, refreshed
+// after every step, so border taps read exactly the mirrored samples.
+// ---------------------------------------------------------------------------
+
+constexpr int kPreTile = 32;
+constexpr int kPreHalo = 12;
+constexpr int kPreS = kPreTile + 2 * kPreHalo;  // 56
+
+struct EncKernel {
+  float centre, edge, corner, inv_c;
+};
+
+__global__ void __launch_bounds__(256) k_precondition(const float* __restrict__ in,
+                                                      float* __restrict__ out, int w, int h,
+                                                      EncKernel k) {
+  __shared__ float F[kPreS * kPreS];
+  __shared__ float X[2][kPreS * kPreS];
+  const size_t plane = (size_t)w * h;
+  in += plane * blockIdx.z;
+  out += plane * blockIdx.z;
+  const int tx0 = blockIdx.x * kPreTile, ty0 = blockIdx.y * kPreTile;
+  const int gx0 = tx0 - kPreHalo, gy0 = ty0 - kPreHalo;
+  for (int i = threadIdx.x; i < kPreS * kPreS; i += blockDim.x) {
+    int lx = i % kPreS, ly = i / kPreS;
+    int gx = mirror1d(gx0 + lx, w), gy = mirror1d(gy0 + ly, h);
+    float v = in[(size_t)gy * w + gx];
+    F[i] = v;
+    X[0][i] = v;
+  }
+  __syncthreads();
+  const size_t n = plane;
+  const size_t bulk = n - n % 4;
+  const int groups = (w >= 3 && h >= 3) ? (w - 2) / 4 : 0;
+  int cur = 0;
+  for (int it = 0; it < 12; ++it) {
+    const int r = kPreHalo - 1 - it;  // cells within r of the tile are updated
+    const int lo = kPreHalo - r, hi = kPreHalo + kPreTile + r;  // local [lo, hi)
+    const int span = hi - lo;
+    const float* xs = X[cur];
+    float* xn = X[cur ^ 1];
+    for (int i = threadIdx.x; i < span * span; i += blockDim.x) {
+      int lx = lo + i % span, ly = lo + i / span;
+      int gx = gx0 + lx, gy = gy0 + ly;
+      if (gx < 0 || gy < 0 || gx >= w || gy >= h) continue;
+      const int c = ly * kPreS + lx;
+      float kx;
+      bool border = gx == 0 || gy == 0 || gx == w - 1 || gy == h - 1;
+      if (!border && gx - 1 < 4 * groups) {
+        float mid = xs[c], north = xs[c - kPreS], south = xs[c + kPreS];
+        float west = xs[c - 1], east = xs[c + 1];
+        float nw = xs[c - kPreS - 1], ne = xs[c - kPreS + 1];
+        float sw = xs[c + kPreS - 1], se = xs[c + kPreS + 1];
+        kx = mid * k.centre + (north + south + west + east) * k.edge +
+             (nw + ne + sw + se) * k.corner;
+      } else {
+        float acc = 0.0f;
+#pragma unroll
+        for (int dy = -1; dy <= 1; ++dy)
+#pragma unroll
+          for (int dx = -1; dx <= 1; ++dx) {
+            float wt = (dx == 0 && dy == 0) ? k.centre : ((dx == 0 || dy == 0) ? k.edge : k.corner);
+            acc += wt * xs[c + dy * kPreS + dx];
+          }
+        kx = acc;
+      }
+      size_t flat = (size_t)gy * w + gx;
+      float xv = xs[c], fv = F[c];
+      xn[c] = flat < bulk ? xv + (fv - kx) * k.inv_c : xv + (fv - kx) / k.centre;
+    }
+    __syncthreads();
+    // Out-of-frame halo cells take their mirror's new value.
+    for (int i = threadIdx.x; i < span * span; i += blockDim.x) {
+      int lx = lo + i % span, ly = lo + i / span;
+      int gx = gx0 + lx, gy = gy0 + ly;
+      if (gx >= 0 && gy >= 0 && gx < w && gy < h) continue;
+      int mx = mirror1d(gx, w) - gx0, my = mirror1d(gy, h) - gy0;
+      xn[ly * kPreS + lx] = xn[my * kPreS + mx];
+    }
+    __syncthreads();
+    cur ^= 1;
+  }
+  for (int i = threadIdx.x; i < kPreTile * kPreTile; i += blockDim.x) {
+    int lx = i % kPreTile, ly = i / kPreTile;
+    int gx = tx0 + lx, gy = ty0 + ly;
+    if (gx < w && gy < h) out[(size_t)gy * w + gx] = X[cur][(ly + kPreHalo) * kPreS + lx + kPreHalo];
+  }
+}
+
+void launch_precondition(const float* in, float* out, int w, int h, cudaStream_t s) {
+  const float w1 = 0.115169525f, w2 = 0.061248592f;
+  // gaborish.rs:31 GaborKernel::new, normalised without FMA.
+  float unnorm = 1.0f + 4.0f * w1 + 4.0f * w2;
+  float scale = 1.0f / unnorm;
+  EncKernel k{scale, w1 * scale, w2 * scale, 1.0f / scale};
+  dim3 grid((w + kPreTile - 1) / kPreTile, (h + kPreTile - 1) / kPreTile, 3);
+  k_precondition<<<grid, 256, 0, s>>>(in, out, w, h, k);
+}
+
+// ---------------------------------------------------------------------------
+// Shared quantization rules (jpxl-encode-policy quantize.rs)
+// ---------------------------------------------------------------------------
+
+__constant__ float c_quant_bias[3] = {1.0f - 0.054650073f, 1.0f - 0.0700545f,
+                                      1.0f - 0.049935103f};
+
+// quantize.rs:1720 clamp_round: v +- 0.5 then truncate; false = Err.
+__device__ __forceinline__ bool clamp_round(float v, int32_t* out) {
+  if (!isfinite(v)) return false;
+  float adjusted = signbit(v) ? v - 0.5f : v + 0.5f;
+  if (!(fabsf(adjusted) < 2147483648.0f)) return false;
+  int32_t q = (int32_t)adjusted;
+  if ((q < 0 ? -q : q) > (1 << 20)) return false;
+  *out = q;
+  return true;
+}
+
+// reconstruct.rs:50 bias_adjust.
+__device__ __forceinline__ float bias_adjust(int32_t q, float bias) {
+  float f = (float)q;
+  if (q >= -1 && q <= 1) return f * bias;
+  return f - 0.145f / f;
+}
+
+// quantize.rs:1400 HfQuantizer::choose (nearest reconstruction, ties to the
+// smaller magnitude) with step = scale * matrix and the zero threshold
+// 0.5 * bias * step, both formed as quantize.rs:334 forms them.
+__device__ __forceinline__ int32_t choose(float target, float step, float bias, uint32_t* err,
+                                          float* recon) {
+  if (!(isfinite(step) && step > 0.0f)) {
+    raise_error(err, kDevBadStep);
+    *recon = 0.0f;
+    return 0;
+  }
+  float thr = 0.5f * bias * step;
+  if (fabsf(target) <= thr) {
+    *recon = bias_adjust(0, bias) * step;
+    return 0;
+  }
+  int32_t e;
+  if (!clamp_round(target / step, &e)) {
+    raise_error(err, kDevQuantRange);
+    *recon = 0.0f;
+    return 0;
+  }
+  int32_t best = 0;
+  float best_err = __int_as_float(0x7f800000);
+  float best_recon = 0.0f;
+  const int32_t cand[4] = {0, e - 1, e, e + 1};
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    int32_t q = cand[i];
+    if ((q < 0 ? -q : q) > (1 << 20)) continue;
+    float r = bias_adjust(q, bias) * step;
+    float er = fabsf(r - target);
+    int32_t aq = q < 0 ? -q : q, ab = best < 0 ? -best : best;
+    if (er < best_err || (er == best_err && aq < ab)) {
+      best = q;
+      best_err = er;
+      best_recon = r;
+    }
+  }
+  *recon = best_recon;
+  return best;
+}
+
+// quantize.rs:199 LfQuantizer::quantize with extra_precision 0.
+__device__ __forceinline__ int32_t lf_quantize(float target, float m, uint32_t* err) {
+  if (!(isfinite(m) && m > 0.0f)) {
+    raise_error(err, kDevBadStep);
+    return 0;
+  }
+  float scaled = target * 1.0f / m;
+  int32_t q;
+  if (!clamp_round(scaled, &q)) {
+    raise_error(err, kDevQuantRange);
+    return 0;
+  }
+  return q;
+}
+
+// forward.rs:779 lf_from_llf_into for an n x n (n = 1, 2, 4) LLF corner:
+// divide by scale_f(y)*scale_f(x), then IDCT_2D.
+__device__ __forceinline__ void lf_from_llf(const float* llf, int n, float* lf) {
+  const float* sf = &c_scale_f[(n == 1 ? 0 : (n == 2 ? 1 : 2)) * 4];
+  float work[16];
+  for (int y = 0; y < n; ++y)
+    for (int x = 0; x < n; ++x) work[y * n + x] = llf[y * n + x] / (sf[y] * sf[x]);
+  if (n == 1) {
+    lf[0] = work[0];  // a 1x1 IDCT_2D multiplies by sqrt(1) twice
+    lf[0] = lf[0] * 1.0f * 1.0f;
+    return;
+  }
+  // dct.rs:982 idct_2d_in_place on an n x n square: scratch = work;
+  // column pass; transpose; column pass.
+  float col[4], t[16];
+  for (int c = 0; c < n; ++c) {
+    for (int r = 0; r < n; ++r) col[r] = work[r * n + c];
+    if (n == 2) idct_1d<2>(col); else idct_1d<4>(col);
+    for (int r = 0; r < n; ++r) work[r * n + c] = col[r];
+  }
+  for (int r = 0; r < n; ++r)
+    for (int c = 0; c < n; ++c) t[c * n + r] = work[r * n + c];
+  for (int c = 0; c < n; ++c) {
+    for (int r = 0; r < n; ++r) col[r] = t[r * n + c];
+    if (n == 2) idct_1d<2>(col); else idct_1d<4>(col);
+    for (int r = 0; r < n; ++r) lf[r * n + c] = col[r];
+  }
+}
+
+// ---------------------------------------------------------------------------
+// K3 — forward transform of every square varblock of size N (policy
+// lib.rs:3008 gather_square with edge replication; forward.rs:451
+// forward_dct_rc = dct.rs:956 DCT_2D), LF samples (lib.rs:3100
+// lf_samples_of), and the luma half of lib.rs:3237 quantize_square_varblock:
+// LF quantize + reconstruct, HF choose + reconstruct.
+//
+// N threads per varblock: thread j transforms column j, then (after a shared
+// memory transpose) row j, ending with column j of the coefficient matrix,
+// which it writes to column bx*8+j of the coefficient image (coalesced).
+// ---------------------------------------------------------------------------
+
+template <int N>
+__global__ void __launch_bounds__(128) k_fdct_luma(EncArgs a, const uint32_t* __restrict__ list,
+                                                   int count) {
+  constexpr int VPB = 128 / N;  // varblocks per CTA
+  constexpr int n = N / 8;
+  __shared__ float T[VPB][N][N + 1];
+  __shared__ float LL[VPB][3][16];
+  const int g = threadIdx.x / N, j = threadIdx.x % N;
+  const int vi = blockIdx.x * VPB + g;
+  const bool active = vi < count;
+  uint32_t packed = active ? list[vi] : 0u;
+  const int bx = packed & 0xffff, by = packed >> 16;
+  const int x0 = bx * 8, y0 = by * 8;
+  const Geo& geo = a.geo;
+  const size_t plane = (size_t)geo.w * geo.h;
+  const size_t cplane = (size_t)geo.W8 * geo.H8;
+  float ycoef[N];
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    float v[N];
+    if (active) {
+      const float* p = a.pre + plane * c;
+      const int xx = min(x0 + j, geo.w - 1);
+#pragma unroll
+      for (int r = 0; r < N; ++r) v[r] = p[(size_t)min(y0 + r, geo.h - 1) * geo.w + xx];
+      dct_1d<N>(v);
+#pragma unroll
+      for (int r = 0; r < N; ++r) T[g][r][j] = v[r];
+    }
+    __syncthreads();
+    if (active) {
+#pragma unroll
+      for (int k = 0; k < N; ++k) v[k] = T[g][j][k];
+      dct_1d<N>(v);
+#pragma unroll
+      for (int k = 0; k < N; ++k) {
+        if (c == 1) ycoef[k] = v[k];
+        a.coeff[cplane * c + (size_t)(y0 + k) * geo.W8 + x0 + j] = v[k];
+      }
+      if (j < n) {
+#pragma unroll
+        for (int k = 0; k < n; ++k) LL[g][c][k * n + j] = v[k];
+      }
+    }
+    __syncthreads();
+  }
+  if (!active) return;
+  // LF samples of all three channels and the luma LF quantization.
+  const size_t bplane = (size_t)geo.bw * geo.bh;
+  if (j < 3) {
+    float lf[16];
+    lf_from_llf(LL[g][j], n, lf);
+    for (int i = 0; i < n * n; ++i) {
+      size_t bi = (size_t)(by + i / n) * geo.bw + bx + i % n;
+      a.lfs[bplane * j + bi] = lf[i];
+      if (j == 1) {
+        int32_t q = lf_quantize(lf[i], a.qs.m_dc[1], a.err);
+        a.lfq[bplane + bi] = q;
+        a.dylf[bi] = a.qs.m_dc[1] * (float)q / 1.0f;
+      }
+    }
+  }
+  // Luma HF: cells (k, j) of column j; the n x n LLF corner stays zero.
+  const uint32_t hf_mul = a.hf_mul[(size_t)by * geo.bw + bx];
+  const double denom = (double)a.qs.global_scale * (double)hf_mul;
+  const float mul = denom <= 0.0 ? 0.0f : (float)(65536.0 / denom);
+  const float scale = mul * a.qs.qm[1];
+  const float* m = a.dq + kDequantTableFloats + dq_offset(dq_slot(N == 8 ? 0 : (N == 16 ? 4 : 5)));
+  const float bias = c_quant_bias[1];
+#pragma unroll
+  for (int k = 0; k < N; ++k) {
+    const int cell = k * N + j;
+    const size_t ci = (size_t)(y0 + k) * geo.W8 + x0 + j;
+    int32_t q = 0;
+    float recon;
+    const float step = scale * __ldg(&m[cell]);
+    if (k < n && j < n) {
+      recon = bias_adjust(0, bias) * step;
+    } else {
+      q = choose(ycoef[k], step, bias, a.err, &recon);
+    }
+    a.qcoeff[cplane + ci] = q;
+    a.dyhf[ci] = recon;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// K4 — chroma-from-luma estimation (policy lib.rs:3437 estimate_cfl).
+//
+// Decisions depend on f64 regression sums that the reference accumulates in
+// one fixed sequential order.  The kernels sum in a fixed tree order instead
+// and bound the difference: both orders lie within n*u*sum|t| of the exact
+// sum (u = 2^-53), which bounds how far the least-squares seed
+// round((s_yc/s_yy - base)*84) and the energy comparisons that confirm it
+// can move.  Where the seed is more than that bound away from a decision
+// boundary the tree result is the reference's; otherwise the tile (or the
+// frame-wide LF pair) is recomputed sequentially in the reference's own
+// order.  Residual bit costs are integer sums, exact in any order.
+// ---------------------------------------------------------------------------
+
+struct RegSums {
+  double s_yy, s_yc, s_cc, a_yc;
+  double n;
+};
+
+// quantize.rs:1640 best_factor on given sums; *robust = the result is
+// certainly the one the reference's sequential sums give (bound `slack` on
+// the absolute error of each sum, relative to its magnitude sum).
+__device__ int best_factor(const RegSums& s, float base, double slack_yy, double slack_yc,
+                           double slack_cc, bool* robust) {
+  *robust = true;
+  if (s.s_yy <= 0.0) {
+    // s_yy is a sum of squares: the reference's is <= 0 only when every term
+    // is zero, which the tree sum sees identically.
+    return 0;
+  }
+  const double cf = 84.0;
+  double k_ls = s.s_yc / s.s_yy;
+  double star = (k_ls - (double)base) * cf;
+  double centre_d = round(star);
+  // Error of star from the sum differences (first order), with margin.
+  double dk = (slack_yc + fabs(k_ls) * slack_yy) / s.s_yy;
+  double dstar = cf * dk * 1.01 + 1e-12 * (1.0 + fabs(star));
+  // Energy comparisons between neighbouring candidates are decided by
+  // |j + 0.5 - star| * 2 s_yy / 84^2 against the f64 rounding of the
+  // energies themselves (a few ulps of s_cc + 2|k s_yc| + k^2 s_yy).
+  double kk = fabs(k_ls) + 2.0;
+  double e_round = 8.0 * 1.1102230246251565e-16 *
+                   (s.s_cc + slack_cc + 2.0 * kk * (fabs(s.s_yc) + slack_yc) + kk * kk * (s.s_yy + slack_yy));
+  double tie = e_round * cf * cf / (2.0 * s.s_yy);
+  double frac = star - floor(star);
+  double dist = fabs(frac - 0.5);
+  if (dist <= dstar + tie || !isfinite(star)) *robust = false;
+  long long centre = (long long)centre_d;
+  // candidates centre-2..centre+2 clamped to [-128,127], then 0; with a
+  // robust star the nearest candidate wins outright.
+  int best = 0;
+  double best_e = 0.0;
+  bool have = false;
+  auto consider = [&](int cand) {
+    double k = (double)((float)base + (float)cand / 84.0f);
+    double e = s.s_cc - 2.0 * k * s.s_yc + k * k * s.s_yy;
+    int ac = cand < 0 ? -cand : cand, ab = best < 0 ? -best : best;
+    if (!have || e < best_e || (e == best_e && ac < ab)) {
+      have = true;
+      best = cand;
+      best_e = e;
+    }
+  };
+  for (int d = -2; d <= 2; ++d) {
+    long long c = centre + d;
+    c = c < -128 ? -128 : (c > 127 ? 127 : c);
+    consider((int)c);
+  }
+  consider(0);
+  return best;
+}
+
+__device__ __forceinline__ uint32_t residual_bits(int32_t q) {
+  if (q == 0) return 0;
+  uint32_t aq = (uint32_t)(q < 0 ? -q : q);
+  return (32u - __clz(aq)) + 1u;
+}
+__device__ __forceinline__ uint32_t factor_bits(int32_t f) {
+  if (f == 0) return 0;
+  uint32_t af = (uint32_t)(f < 0 ? -f : f);
+  return (32u - __clz(af)) + 2u;
+}
+
+// Block-wide fixed-order sum of doubles (warp shuffles, then warp order).
+template <int NT>
+__device__ double block_sum(double v, double* scratch) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  const int wid = threadIdx.x / 32, lane = threadIdx.x % 32;
+  __syncthreads();
+  if (lane == 0) scratch[wid] = v;
+  __syncthreads();
+  double t = 0.0;
+  if (threadIdx.x == 0)
+    for (int i = 0; i < NT / 32; ++i) t += scratch[i];
+  __syncthreads();
+  return t;  // valid in thread 0
+}
+template <int NT>
+__device__ unsigned long long block_sum_u64(unsigned long long v, unsigned long long* scratch) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  const int wid = threadIdx.x / 32, lane = threadIdx.x % 32;
+  __syncthreads();
+  if (lane == 0) scratch[wid] = v;
+  __syncthreads();
+  unsigned long long t = 0;
+  if (threadIdx.x == 0)
+    for (int i = 0; i < NT / 32; ++i) t += scratch[i];
+  __syncthreads();
+  return t;
+}
+
+// The varblock containing block (bx, by) and whether coefficient-image cell
+// (px, py) is in its n x n LLF corner.  Square varblocks only (the encoder's
+// cover); origins are naturally aligned.
+__device__ __forceinline__ bool cell_is_llf(const uint8_t* map, int bw, int px, int py, int* side) {
+  int bx = px >> 3, by = py >> 3;
+  int sel = map[(size_t)by * bw + bx] & 0x1f;
+  int nb = sel == 0 ? 1 : (sel == 4 ? 2 : 4);
+  *side = nb * 8;
+  int ox = (bx / nb) * nb * 8, oy = (by / nb) * nb * 8;
+  return (px - ox) < nb && (py - oy) < nb;
+}
+
+constexpr int kCflThreads = 256;
+
+// Per 64x64 tile: HF regression sums (X and B against source Y), the seed,
+// and the residual bit costs of the candidate window.  One CTA per tile.
+__global__ void __launch_bounds__(kCflThreads) k_cfl_tiles(EncArgs a) {
+  __shared__ double sd[kCflThreads / 32];
+  __shared__ unsigned long long su[kCflThreads / 32];
+  __shared__ int s_seed[2];
+  __shared__ int s_robust[2];
+  __shared__ int s_cands[2][4];
+  __shared__ int s_ncand[2];
+  const Geo& geo = a.geo;
+  const int tx = blockIdx.x, ty = blockIdx.y;
+  const int tile = ty * geo.tw + tx;
+  if (*a.not_gray == 0u || !a.cfl_enabled) {
+    if (threadIdx.x == 0) {
+      a.cfl_x[tile] = 0;
+      a.cfl_b[tile] = 0;
+    }
+    return;
+  }
+  const size_t cplane = (size_t)geo.W8 * geo.H8;
+  const int px0 = tx * 64, py0 = ty * 64;
+  const int pw = min(64, geo.W8 - px0), ph = min(64, geo.H8 - py0);
+  // Phase A: tree sums.
+  double syy = 0, syx = 0, sxx = 0, syb = 0, sbb = 0, ayx = 0, ayb = 0, cnt = 0;
+  for (int i = threadIdx.x; i < pw * ph; i += kCflThreads) {
+    int px = px0 + i % pw, py = py0 + i / pw;
+    int side;
+    if (cell_is_llf(a.block_map, geo.bw, px, py, &side)) continue;
+    size_t ci = (size_t)py * geo.W8 + px;
+    double y = (double)a.coeff[cplane + ci];
+    double x = (double)a.coeff[ci];
+    double b = (double)a.coeff[2 * cplane + ci];
+    syy += y * y;
+    syx += y * x;
+    sxx += x * x;
+    syb += y * b;
+    sbb += b * b;
+    ayx += fabs(y * x);
+    ayb += fabs(y * b);
+    cnt += 1.0;
+  }
+  double t_syy = block_sum<kCflThreads>(syy, sd);
+  double t_syx = block_sum<kCflThreads>(syx, sd);
+  double t_sxx = block_sum<kCflThreads>(sxx, sd);
+  double t_syb = block_sum<kCflThreads>(syb, sd);
+  double t_sbb = block_sum<kCflThreads>(sbb, sd);
+  double t_ayx = block_sum<kCflThreads>(ayx, sd);
+  double t_ayb = block_sum<kCflThreads>(ayb, sd);
+  double t_cnt = block_sum<kCflThreads>(cnt, sd);
+  if (threadIdx.x == 0) {
+    const double u = 1.1102230246251565e-16;
+    const double gam = 2.0 * (t_cnt + 2.0) * u;  // both orders vs exact
+    for (int ch = 0; ch < 2; ++ch) {
+      RegSums s;
+      s.s_yy = t_syy;
+      s.s_yc = ch == 0 ? t_syx : t_syb;
+      s.s_cc = ch == 0 ? t_sxx : t_sbb;
+      s.a_yc = ch == 0 ? t_ayx : t_ayb;
+      s.n = t_cnt;
+      bool robust = true;
+      int seed = 0;
+      if (t_cnt > 0.0) {
+        seed = best_factor(s, ch == 0 ? 0.0f : 1.0f, gam * s.s_yy, gam * s.a_yc, gam * s.s_cc,
+                           &robust);
+      }
+      s_seed[ch] = seed;
+      s_robust[ch] = robust ? 1 : 0;
+    }
+  }
+  __syncthreads();
+  // Sequential fallback in the reference's order (varblocks in raster order
+  // of their origins within the tile, then coefficient rows and columns).
+  if ((!s_robust[0] || !s_robust[1]) && threadIdx.x == 0) {
+    atomicAdd(a.cfl_fallbacks, 1u);
+    RegSums sx{0, 0, 0, 0, 0}, sb{0, 0, 0, 0, 0};
+    for (int by = py0 / 8; by < (py0 + ph) / 8; ++by)
+      for (int bx = px0 / 8; bx < (px0 + pw) / 8; ++bx) {
+        uint8_t e = a.block_map[(size_t)by * geo.bw + bx];
+        if (!(e & 0x80)) continue;
+        int sel = e & 0x1f;
+        int nb = sel == 0 ? 1 : (sel == 4 ? 2 : 4), side = nb * 8;
+        for (int row = 0; row < side; ++row)
+          for (int col = (row < nb ? nb : 0); col < side; ++col) {
+            size_t ci = (size_t)(by * 8 + row) * geo.W8 + bx * 8 + col;
+            double y = (double)a.coeff[cplane + ci];
+            double x = (double)a.coeff[ci];
+            double b = (double)a.coeff[2 * cplane + ci];
+            sx.s_yy += y * y; sx.s_yc += y * x; sx.s_cc += x * x;
+            sb.s_yy += y * y; sb.s_yc += y * b; sb.s_cc += b * b;
+            sx.n += 1.0;
+          }
+      }
+    sb.n = sx.n;
+    bool r;
+    s_seed[0] = sx.n > 0 ? best_factor(sx, 0.0f, 0, 0, 0, &r) : 0;
+    s_seed[1] = sb.n > 0 ? best_factor(sb, 1.0f, 0, 0, 0, &r) : 0;
+  }
+  __syncthreads();
+  // lib.rs:3735 factor_candidates(seed, -128, 127): seed-1, seed, seed+1
+  // clamped and de-duplicated, then 0 if absent.
+  if (threadIdx.x < 2) {
+    int ch = threadIdx.x, seed = s_seed[ch], nc = 0;
+    int* c = s_cands[ch];
+    for (int d = -1; d <= 1; ++d) {
+      int v = min(max(seed + d, -128), 127);
+      bool dup = false;
+      for (int i = 0; i < nc; ++i) dup |= c[i] == v;
+      if (!dup) c[nc++] = v;
+    }
+    bool has0 = false;
+    for (int i = 0; i < nc; ++i) has0 |= c[i] == 0;
+    if (!has0) c[nc++] = 0;
+    s_ncand[ch] = nc;
+  }
+  __syncthreads();
+  // Phase C: residual bits of every candidate through the DCT8x8 baseline
+  // quantizer (cells folded onto the 8x8 grid, lib.rs:3585).
+  const float scale_x = a.base_mul * a.qs.qm[0], scale_b = a.base_mul * a.qs.qm[2];
+  const float* m_x = a.dq;
+  const float* m_b = a.dq + 2 * kDequantTableFloats;
+  unsigned long long bits[2][4] = {{0, 0, 0, 0}, {0, 0, 0, 0}};
+  float kx[4], kb[4];
+  for (int i = 0; i < 4; ++i) {
+    kx[i] = 0.0f + (float)s_cands[0][i < s_ncand[0] ? i : 0] / 84.0f;
+    kb[i] = 1.0f + (float)s_cands[1][i < s_ncand[1] ? i : 0] / 84.0f;
+  }
+  const bool need_x = s_seed[0] != 0, need_b = s_seed[1] != 0;
+  if (need_x || need_b) {
+    for (int i = threadIdx.x; i < pw * ph; i += kCflThreads) {
+      int px = px0 + i % pw, py = py0 + i / pw;
+      int side;
+      if (cell_is_llf(a.block_map, geo.bw, px, py, &side)) continue;
+      int fold = side / 8;
+      int lrow = (py % side), lcol = (px % side);
+      int cell8 = (lrow / fold) * 8 + (lcol / fold);
+      size_t ci = (size_t)py * geo.W8 + px;
+      float dy = a.dyhf[ci];
+      float x = a.coeff[ci], b = a.coeff[2 * cplane + ci];
+      float step_x = scale_x * __ldg(&m_x[cell8]);
+      float step_b = scale_b * __ldg(&m_b[cell8]);
+      float rc;
+      for (int c = 0; c < 4; ++c) {
+        if (need_x && c < s_ncand[0])
+          bits[0][c] += residual_bits(choose(x - kx[c] * dy, step_x, c_quant_bias[0], a.err, &rc));
+        if (need_b && c < s_ncand[1])
+          bits[1][c] += residual_bits(choose(b - kb[c] * dy, step_b, c_quant_bias[2], a.err, &rc));
+      }
+    }
+  }
+  unsigned long long tot[2][4];
+  for (int ch = 0; ch < 2; ++ch)
+    for (int c = 0; c < 4; ++c) tot[ch][c] = block_sum_u64<kCflThreads>(bits[ch][c], su);
+  if (threadIdx.x == 0) {
+    for (int ch = 0; ch < 2; ++ch) {
+      int result = 0;
+      if (s_seed[ch] != 0) {
+        // lib.rs:3966 refine_hf_factor: cost(0) first, then each non-zero
+        // candidate needs residual + factor bits strictly below (ties to
+        // the smaller magnitude).
+        unsigned long long best_cost = 0;
+        for (int c = 0; c < s_ncand[ch]; ++c)
+          if (s_cands[ch][c] == 0) best_cost = tot[ch][c];
+        int best_f = 0;
+        for (int c = 0; c < s_ncand[ch]; ++c) {
+          int f = s_cands[ch][c];
+          if (f == 0) continue;
+          unsigned long long fb = factor_bits(f);
+          unsigned long long cutoff = best_cost > fb ? best_cost - fb : 0;
+          if (tot[ch][c] > cutoff) continue;
+          unsigned long long cost = tot[ch][c] + fb;
+          int af = f < 0 ? -f : f, ab = best_f < 0 ? -best_f : best_f;
+          if (cost < best_cost || (cost == best_cost && af < ab)) {
+            best_cost = cost;
+            best_f = f;
+          }
+        }
+        result = best_f;
+      }
+      if (ch == 0) a.cfl_x[tile] = (int8_t)result;
+      else a.cfl_b[tile] = (int8_t)result;
+    }
+  }
+}
+
+// Frame-wide LF pair (lib.rs:3831 refine_lf_factors).  Pass 1: per-CTA
+// regression partial sums over the LF samples (one per 8x8 block).
+constexpr int kLfThreads = 256;
+__global__ void __launch_bounds__(kLfThreads) k_cfl_lf_sums(EncArgs a, double* partial) {
+  __shared__ double sd[kLfThreads / 32];
+  const Geo& geo = a.geo;
+  const size_t nb = (size_t)geo.bw * geo.bh;
+  double v[7] = {0, 0, 0, 0, 0, 0, 0};  // yy, yx, xx, yb, bb, |yx|, |yb|
+  for (size_t i = (size_t)blockIdx.x * kLfThreads + threadIdx.x; i < nb;
+       i += (size_t)gridDim.x * kLfThreads) {
+    double y = a.lfs[nb + i], x = a.lfs[i], b = a.lfs[2 * nb + i];
+    v[0] += y * y; v[1] += y * x; v[2] += x * x; v[3] += y * b; v[4] += b * b;
+    v[5] += fabs(y * x); v[6] += fabs(y * b);
+  }
+  for (int k = 0; k < 7; ++k) {
+    double t = block_sum<kLfThreads>(v[k], sd);
+    if (threadIdx.x == 0) partial[blockIdx.x * 8 + k] = t;
+  }
+}
+
+// Pass 2 (one thread): reduce the partials in block order, decide the seeds
+// (with the sequential fallback in the reference's LF-group / band /
+// varblock / cell order when a seed is not robust), write the candidate
+// windows.
+__global__ void k_cfl_lf_seed(EncArgs a, const double* partial, int nparts, int* cand) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  if (*a.not_gray == 0u || !a.cfl_enabled) {
+    cand[0] = 0;
+    cand[1] = 0;
+    return;
+  }
+  const Geo& geo = a.geo;
+  double t[7] = {0, 0, 0, 0, 0, 0, 0};
+  for (int p = 0; p < nparts; ++p)
+    for (int k = 0; k < 7; ++k) t[k] += partial[p * 8 + k];
+  const double n = (double)geo.bw * geo.bh;
+  const double gam = 2.0 * (n + 2.0) * 1.1102230246251565e-16;
+  bool rx, rb;
+  RegSums sx{t[0], t[1], t[2], t[5], n}, sb{t[0], t[3], t[4], t[6], n};
+  int seed_x = best_factor(sx, 0.0f, gam * t[0], gam * t[5], gam * t[2], &rx);
+  int seed_b = best_factor(sb, 1.0f, gam * t[0], gam * t[6], gam * t[4], &rb);
+  if (!rx || !rb) {
+    atomicAdd(a.cfl_fallbacks, 1u);
+    const size_t nb = (size_t)geo.bw * geo.bh;
+    RegSums qx{0, 0, 0, 0, n}, qb{0, 0, 0, 0, n};
+    const int G = 256;
+    const int gw = (geo.bw + G - 1) / G, gh = (geo.bh + G - 1) / G;
+    for (int gy = 0; gy < gh; ++gy)
+      for (int gx = 0; gx < gw; ++gx) {
+        int by0 = gy * G, bx0 = gx * G;
+        int gbh = min(G, geo.bh - by0), gbw = min(G, geo.bw - bx0);
+        for (int trow = 0; trow < (gbh + 7) / 8; ++trow)
+          for (int by = by0 + trow * 8; by < min(by0 + trow * 8 + 8, by0 + gbh); ++by)
+            for (int bx = bx0; bx < bx0 + gbw; ++bx) {
+              uint8_t e = a.block_map[(size_t)by * geo.bw + bx];
+              if (!(e & 0x80)) continue;
+              int sel = e & 0x1f, nbk = sel == 0 ? 1 : (sel == 4 ? 2 : 4);
+              for (int i = 0; i < nbk * nbk; ++i) {
+                size_t bi = (size_t)(by + i / nbk) * geo.bw + bx + i % nbk;
+                double y = a.lfs[nb + bi], x = a.lfs[bi], b = a.lfs[2 * nb + bi];
+                qx.s_yy += y * y; qx.s_yc += y * x; qx.s_cc += x * x;
+                qb.s_yy += y * y; qb.s_yc += y * b; qb.s_cc += b * b;
+              }
+            }
+      }
+    bool r;
+    seed_x = best_factor(qx, 0.0f, 0, 0, 0, &r);
+    seed_b = best_factor(qb, 1.0f, 0, 0, 0, &r);
+  }
+  cand[0] = seed_x;
+  cand[1] = seed_b;
+}
+
+// Pass 3: residual bits of every candidate, per-CTA partials.
+__global__ void __launch_bounds__(kLfThreads) k_cfl_lf_costs(EncArgs a, const int* seeds,
+                                                             unsigned long long* partial) {
+  __shared__ unsigned long long su[kLfThreads / 32];
+  const Geo& geo = a.geo;
+  const size_t nb = (size_t)geo.bw * geo.bh;
+  int cand[2][4];
+  int ncand[2];
+  for (int ch = 0; ch < 2; ++ch) {
+    int seed = seeds[ch], nc = 0;
+    for (int d = -1; d <= 1; ++d) {
+      int v = min(max(seed + d, -128), 127);
+      bool dup = false;
+      for (int i = 0; i < nc; ++i) dup |= cand[ch][i] == v;
+      if (!dup) cand[ch][nc++] = v;
+    }
+    bool has0 = false;
+    for (int i = 0; i < nc; ++i) has0 |= cand[ch][i] == 0;
+    if (!has0) cand[ch][nc++] = 0;
+    ncand[ch] = nc;
+  }
+  unsigned long long bits[2][4] = {{0, 0, 0, 0}, {0, 0, 0, 0}};
+  float k[2][4];
+  for (int c = 0; c < 4; ++c) {
+    k[0][c] = 0.0f + (float)cand[0][c < ncand[0] ? c : 0] / 84.0f;
+    k[1][c] = 1.0f + (float)cand[1][c < ncand[1] ? c : 0] / 84.0f;
+  }
+  for (size_t i = (size_t)blockIdx.x * kLfThreads + threadIdx.x; i < nb;
+       i += (size_t)gridDim.x * kLfThreads) {
+    float dy = a.dylf[i], x = a.lfs[i], b = a.lfs[2 * nb + i];
+    for (int c = 0; c < 4; ++c) {
+      if (c < ncand[0]) bits[0][c] += residual_bits(lf_quantize(x - k[0][c] * dy, a.qs.m_dc[0], a.err));
+      if (c < ncand[1]) bits[1][c] += residual_bits(lf_quantize(b - k[1][c] * dy, a.qs.m_dc[2], a.err));
+    }
+  }
+  for (int ch = 0; ch < 2; ++ch)
+    for (int c = 0; c < 4; ++c) {
+      unsigned long long t = block_sum_u64<kLfThreads>(bits[ch][c], su);
+      if (threadIdx.x == 0) partial[blockIdx.x * 8 + ch * 4 + c] = t;
+    }
+}
+
+// Pass 4 (one thread): lib.rs:3831 joint choice with the 50-bit bundle cost.
+__global__ void k_cfl_lf_pick(EncArgs a, const int* seeds, const unsigned long long* partial,
+                              int nparts) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  int* out = a.lf_factors;
+  if (*a.not_gray == 0u || !a.cfl_enabled) {
+    out[0] = 0;
+    out[1] = 0;
+    return;
+  }
+  int cand[2][4], ncand[2];
+  for (int ch = 0; ch < 2; ++ch) {
+    int seed = seeds[ch], nc = 0;
+    for (int d = -1; d <= 1; ++d) {
+      int v = min(max(seed + d, -128), 127);
+      bool dup = false;
+      for (int i = 0; i < nc; ++i) dup |= cand[ch][i] == v;
+      if (!dup) cand[ch][nc++] = v;
+    }
+    bool has0 = false;
+    for (int i = 0; i < nc; ++i) has0 |= cand[ch][i] == 0;
+    if (!has0) cand[ch][nc++] = 0;
+    ncand[ch] = nc;
+  }
+  unsigned long long cost[2][4] = {{0, 0, 0, 0}, {0, 0, 0, 0}};
+  for (int p = 0; p < nparts; ++p)
+    for (int ch = 0; ch < 2; ++ch)
+      for (int c = 0; c < 4; ++c) cost[ch][c] += partial[p * 8 + ch * 4 + c];
+  unsigned long long nx = 0, nbb = 0;
+  for (int c = 0; c < ncand[0]; ++c) if (cand[0][c] == 0) { nx = cost[0][c]; break; }
+  for (int c = 0; c < ncand[1]; ++c) if (cand[1][c] == 0) { nbb = cost[1][c]; break; }
+  int bx = 0, bb = 0;
+  unsigned long long best = nx + nbb;
+  for (int i = 0; i < ncand[0]; ++i)
+    for (int j = 0; j < ncand[1]; ++j) {
+      int fx = cand[0][i], fb = cand[1][j];
+      unsigned long long c = cost[0][i] + cost[1][j];
+      if (fx != 0 || fb != 0) c += 50ull + factor_bits(fx) + factor_bits(fb);
+      int mag = abs(fx) + abs(fb), bmag = abs(bx) + abs(bb);
+      if (c < best || (c == best && mag < bmag)) {
+        bx = fx;
+        bb = fb;
+        best = c;
+      }
+    }
+  out[0] = bx;
+  out[1] = bb;
+}
+
+// ---------------------------------------------------------------------------
+// K5 — chroma half of lib.rs:3237 quantize_square_varblock: LF targets
+// c - k_lf*dY_lf, HF targets c - k_hf*dY_hf (no FMA), nearest choice.
+// ---------------------------------------------------------------------------
+
+template <int N>
+__global__ void __launch_bounds__(128) k_quant_chroma(EncArgs a, const uint32_t* __restrict__ list,
+                                                      int count) {
+  constexpr int VPB = 128 / N;
+  constexpr int n = N / 8;
+  const int g = threadIdx.x / N, j = threadIdx.x % N;
+  const int vi = blockIdx.x * VPB + g;
+  if (vi >= count) return;
+  const uint32_t packed = list[vi];
+  const int bx = packed & 0xffff, by = packed >> 16;
+  const int x0 = bx * 8, y0 = by * 8;
+  const Geo& geo = a.geo;
+  const size_t cplane = (size_t)geo.W8 * geo.H8;
+  const size_t bplane = (size_t)geo.bw * geo.bh;
+  const int tile = (by / 8) * geo.tw + bx / 8;
+  const int fx = a.lf_factors[0], fb = a.lf_factors[1];
+  const float k_lf[3] = {0.0f + (float)fx / 84.0f, 0.0f, 1.0f + (float)fb / 84.0f};
+  const float k_hf[3] = {0.0f + (float)a.cfl_x[tile] / 84.0f, 0.0f,
+                         1.0f + (float)a.cfl_b[tile] / 84.0f};
+  // LF: n*n samples, thread j < n*n takes sample j.
+  if (j < n * n) {
+    size_t bi = (size_t)(by + j / n) * geo.bw + bx + j % n;
+    float dy = a.dylf[bi];
+    for (int c = 0; c <= 2; c += 2) {
+      float target = a.lfs[bplane * c + bi] - k_lf[c] * dy;
+      a.lfq[bplane * c + bi] = lf_quantize(target, a.qs.m_dc[c], a.err);
+    }
+  }
+  const uint32_t hf_mul = a.hf_mul[(size_t)by * geo.bw + bx];
+  const double denom = (double)a.qs.global_scale * (double)hf_mul;
+  const float mul = denom <= 0.0 ? 0.0f : (float)(65536.0 / denom);
+  const int off = dq_offset(dq_slot(N == 8 ? 0 : (N == 16 ? 4 : 5)));
+  for (int c = 0; c <= 2; c += 2) {
+    const float scale = mul * a.qs.qm[c];
+    const float* m = a.dq + c * kDequantTableFloats + off;
+    const float bias = c_quant_bias[c];
+#pragma unroll 4
+    for (int k = 0; k < N; ++k) {
+      const size_t ci = (size_t)(y0 + k) * geo.W8 + x0 + j;
+      int32_t q = 0;
+      if (!(k < n && j < n)) {
+        float target = a.coeff[cplane * c + ci] - k_hf[c] * a.dyhf[ci];
+        float rc;
+        q = choose(target, scale * __ldg(&m[k * N + j]), bias, a.err, &rc);
+      }
+      a.qcoeff[cplane * c + ci] = q;
+    }
+  }
+}
+
+int launch_fdct_luma(const EncArgs& a, const uint32_t* const* lists, const int* counts,
+                     cudaStream_t s) {
+  // square classes: 0 -> DCT8, 1 -> DCT16, 2 -> DCT32
+  int k = 0;
+  if (counts[0]) { k_fdct_luma<8><<<(counts[0] + 15) / 16, 128, 0, s>>>(a, lists[0], counts[0]); ++k; }
+  if (counts[1]) { k_fdct_luma<16><<<(counts[1] + 7) / 8, 128, 0, s>>>(a, lists[1], counts[1]); ++k; }
+  if (counts[2]) { k_fdct_luma<32><<<(counts[2] + 3) / 4, 128, 0, s>>>(a, lists[2], counts[2]); ++k; }
+  return k;
+}
+
+int launch_cfl(const EncArgs& a, double* lf_part, unsigned long long* lf_cost_part, int* lf_seeds,
+               int nparts, cudaStream_t s) {
+  dim3 tiles(a.geo.tw, a.geo.th);
+  k_cfl_tiles<<<tiles, kCflThreads, 0, s>>>(a);
+  k_cfl_lf_sums<<<nparts, kLfThreads, 0, s>>>(a, lf_part);
+  k_cfl_lf_seed<<<1, 32, 0, s>>>(a, lf_part, nparts, lf_seeds);
+  k_cfl_lf_costs<<<nparts, kLfThreads, 0, s>>>(a, lf_seeds, lf_cost_part);
+  k_cfl_lf_pick<<<1, 32, 0, s>>>(a, lf_seeds, lf_cost_part, nparts);
+  return 5;
+}
+
+int launch_quant_chroma(const EncArgs& a, const uint32_t* const* lists, const int* counts,
+                        cudaStream_t s) {
+  int k = 0;
+  if (counts[0]) { k_quant_chroma<8><<<(counts[0] + 15) / 16, 128, 0, s>>>(a, lists[0], counts[0]); ++k; }
+  if (counts[1]) { k_quant_chroma<16><<<(counts[1] + 7) / 8, 128, 0, s>>>(a, lists[1], counts[1]); ++k; }
+  if (counts[2]) { k_quant_chroma<32><<<(counts[2] + 3) / 4, 128, 0, s>>>(a, lists[2], counts[2]); ++k; }
+  return k;
+}
+
+void upload_dct_constants(const float* iv4, const float* iv8, const float* iv16,
+                          const float* scale_f, cudaStream_t s) {
+  cudaMemcpyToSymbolAsync(c_iv4, iv4, sizeof(float) * 16, 0, cudaMemcpyHostToDevice, s);
+  cudaMemcpyToSymbolAsync(c_iv8, iv8, sizeof(float) * 64, 0, cudaMemcpyHostToDevice, s);
+  cudaMemcpyToSymbolAsync(c_iv16, iv16, sizeof(float) * 256, 0, cudaMemcpyHostToDevice, s);
+  cudaMemcpyToSymbolAsync(c_scale_f, scale_f, sizeof(float) * 12, 0, cudaMemcpyHostToDevice, s);
+}
+
+}  // namespace jpxlg

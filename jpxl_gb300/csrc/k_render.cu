@@ -1,0 +1,461 @@
+// k_render.cu — sm_103a kernels of the plan renderer / decoder tail:
+//   R1 k_render_vb<R,C>  dequantize, HF CfL, LLF from the LF planes, IDCT_2D,
+//                        in-frame scatter and the per-block EPF sigma
+//   R2 k_gaborish        J.3 3x3 with FMA, mirrored borders
+//   R3 k_epf<step>       J.4 steps 0/1/2
+//   R4 k_colour_out      L.2.2 opsin inverse and the output encoding
+// Operation order follows jpxl-plan-render lib.rs:749 render_inner and the
+// jpxl-core kernels it calls; -fmad=false keeps every unfused product.
+#include <algorithm>
+#include <cstdint>
+
+#include "jpxlg_common.cuh"
+#include "jpxlg_internal.h"
+#include "jpxlg_kernels.h"
+
+namespace jpxlg {
+
+extern __constant__ float c_scale_f[12];
+extern __constant__ float c_quant_bias[3];
+
+__constant__ float c_opsin_m[9];
+__constant__ float c_opsin_bias[3];
+__constant__ float c_opsin_bias_cbrt[3];
+
+__device__ __forceinline__ float rbias_adjust(int32_t q, float bias) {
+  float f = (float)q;
+  if (q >= -1 && q <= 1) return f * bias;
+  return f - 0.145f / f;
+}
+
+template <int N>
+__device__ __forceinline__ void idct_n(float* v) {
+  idct_1d<N>(v);
+}
+
+// dct.rs:956 DCT_2D of an LF rectangle cy x cx (cy <= cx, both <= 4) in place.
+__device__ __forceinline__ void dct2d_small(float* m, int rows, int cols) {
+  float col[4], s[16];
+  // column pass (length rows) on rows x cols
+  for (int c = 0; c < cols; ++c) {
+    for (int r = 0; r < rows; ++r) col[r] = m[r * cols + c];
+    if (rows == 2) dct_1d<2>(col);
+    else if (rows == 4) dct_1d<4>(col);
+    for (int r = 0; r < rows; ++r) m[r * cols + c] = col[r];
+  }
+  // transpose to cols x rows, column pass (length cols)
+  for (int r = 0; r < rows; ++r)
+    for (int c = 0; c < cols; ++c) s[c * rows + r] = m[r * cols + c];
+  for (int r = 0; r < rows; ++r) {
+    for (int c = 0; c < cols; ++c) col[c] = s[c * rows + r];
+    if (cols == 2) dct_1d<2>(col);
+    else if (cols == 4) dct_1d<4>(col);
+    for (int c = 0; c < cols; ++c) s[c * rows + r] = col[c];
+  }
+  // cols x rows result; landscape => transpose back when cols > rows
+  if (cols <= rows) {
+    for (int i = 0; i < rows * cols; ++i) m[i] = s[i];
+  } else {
+    for (int c = 0; c < cols; ++c)
+      for (int r = 0; r < rows; ++r) m[r * cols + c] = s[c * rows + r];
+  }
+}
+
+// ---------------------------------------------------------------------------
+// R1 — one varblock of R x C samples per group of T = max(R, C) threads.
+// Landscape coefficients are crows = min x ccols = max.  IDCT_2D
+// (dct.rs:982): scratch S (C x R) is L transposed when C > R, else L; step A
+// runs length-C IDCTs down S's R columns; step B runs length-R IDCTs along
+// the C rows of the result, producing sample column i in thread i.
+// ---------------------------------------------------------------------------
+
+template <int R, int C>
+__global__ void __launch_bounds__(128) k_render_vb(RenderArgs a, const uint32_t* __restrict__ list,
+                                                   int count) {
+  constexpr int T = R > C ? R : C;
+  constexpr int CR = R < C ? R : C;   // landscape rows
+  constexpr int CC = T;               // landscape cols
+  constexpr bool portrait = R > C;
+  constexpr int BR = R / 8, BC = C / 8;
+  constexpr int LY = CR / 8, LX = CC / 8;  // LLF corner
+  constexpr int VPB = 128 / T;
+  __shared__ float L[VPB][CR][CC + 1];
+  __shared__ float LLF[VPB][3][16];
+  const int g = threadIdx.x / T, j = threadIdx.x % T;
+  const int vi = blockIdx.x * VPB + g;
+  const bool active = vi < count;
+  const uint32_t packed = active ? list[vi] : 0u;
+  const int bx = packed & 0xffff, by = packed >> 16;
+  const int x0 = bx * 8, y0 = by * 8;
+  const Geo& geo = a.geo;
+  const size_t cplane = (size_t)geo.W8 * geo.H8;
+  const size_t bplane = (size_t)geo.bw * geo.bh;
+  const size_t plane = (size_t)geo.w * geo.h;
+
+  float mul = 0.0f, kx = 0.0f, kb = 0.0f;
+  if (active) {
+    const uint32_t hf_mul = a.hf_mul[(size_t)by * geo.bw + bx];
+    const double denom = (double)a.qs.global_scale * (double)hf_mul;
+    mul = denom <= 0.0 ? 0.0f : (float)(65536.0 / denom);  // reconstruct.rs:27
+    const int tile = (by / 8) * geo.tw + bx / 8;
+    kx = 0.0f + (float)a.cfl_x[tile] / 84.0f;  // reconstruct.rs:96 cfl_factors
+    kb = 1.0f + (float)a.cfl_b[tile] / 84.0f;
+    // LLF rectangles (varblock.rs:817 llf_from_lf) of the three channels:
+    // LF dequantized (reconstruct.rs:84) with the LF CfL (plan-render
+    // lib.rs:1314), laid out landscape, DCT_2D, times scale_f(y)*scale_f(x).
+    if (j < 3) {
+      const int c = j;
+      float k_x_lf = a.k_x_lf, k_b_lf = a.k_b_lf;
+      if (a.lf_factors_dev) {
+        k_x_lf = 0.0f + (float)a.lf_factors_dev[0] / 84.0f;
+        k_b_lf = 1.0f + (float)a.lf_factors_dev[1] / 84.0f;
+      }
+      float rect[16];
+      for (int dy = 0; dy < BR; ++dy)
+        for (int dx = 0; dx < BC; ++dx) {
+          size_t bi = (size_t)(by + dy) * geo.bw + bx + dx;
+          float dY = a.qs.m_dc[1] * (float)a.lfq[bplane + bi] / 1.0f;
+          float v;
+          if (c == 1) v = dY;
+          else {
+            float d = a.qs.m_dc[c] * (float)a.lfq[bplane * c + bi] / 1.0f;
+            v = d + (c == 0 ? k_x_lf : k_b_lf) * dY;
+          }
+          if (portrait) rect[dx * BR + dy] = v; else rect[dy * BC + dx] = v;
+        }
+      if (LY * LX > 1) dct2d_small(rect, LY, LX);
+      const float* sfy = &c_scale_f[(LY == 1 ? 0 : (LY == 2 ? 1 : 2)) * 4];
+      const float* sfx = &c_scale_f[(LX == 1 ? 0 : (LX == 2 ? 1 : 2)) * 4];
+      for (int y = 0; y < LY; ++y)
+        for (int x = 0; x < LX; ++x) LLF[g][c][y * LX + x] = rect[y * LX + x] * sfy[y] * sfx[x];
+    }
+  }
+  __syncthreads();
+
+  // Dequantize landscape column x = j of each channel (plan-render
+  // lib.rs:913: adjusted * (mul*qm) * matrix, left to right).
+  float dY[CR];
+  // compact dequant slot of this shape (Table I.4 indices 0,4,5,6,7,8)
+  constexpr int slot = (R == C) ? (R == 8 ? 0 : (R == 16 ? 1 : 2))
+                                : (CC == 16 ? 3 : (CR == 8 ? 4 : 5));
+  const int off = dq_offset(slot);
+#pragma unroll
+  for (int ci = 0; ci < 3; ++ci) {
+    const int c = ci == 0 ? 1 : (ci == 1 ? 0 : 2);  // luma first: CfL needs it
+    if (active) {
+      const float scale = mul * a.qs.qm[c];
+      const float bias = c_quant_bias[c];
+      const float* m = a.dq + c * kDequantTableFloats + off;
+#pragma unroll
+      for (int y = 0; y < CR; ++y) {
+        const int x = j;
+        size_t pos = portrait ? (size_t)(y0 + x) * geo.W8 + x0 + y : (size_t)(y0 + y) * geo.W8 + x0 + x;
+        int32_t q = a.qcoeff[cplane * c + pos];
+        float d = rbias_adjust(q, bias) * scale * __ldg(&m[y * CC + x]);
+        if (c == 1) dY[y] = d;
+        else d = d + (c == 0 ? kx : kb) * dY[y];  // lib.rs:1344 apply_hf_cfl
+        if (y < LY && x < LX) d = LLF[g][c][y * LX + x];
+        L[g][y][x] = d;
+      }
+    }
+    __syncthreads();
+    // Step A: thread jj < R transforms column jj of S (length C).
+    float v[T];
+    if (active && j < R) {
+#pragma unroll
+      for (int i = 0; i < C; ++i) v[i] = (C > R) ? L[g][j][i] : L[g][i][j];
+      idct_n<C>(v);
+    }
+    __syncthreads();
+    if (active && j < R) {
+#pragma unroll
+      for (int i = 0; i < C; ++i) {
+        if (C > R) L[g][j][i] = v[i]; else L[g][i][j] = v[i];
+      }
+    }
+    __syncthreads();
+    // Step B: thread i < C transforms row i of the step-A result (length R)
+    // into sample column i and scatters it inside the frame.
+    if (active && j < C) {
+#pragma unroll
+      for (int r = 0; r < R; ++r) v[r] = (C > R) ? L[g][r][j] : L[g][j][r];
+      idct_n<R>(v);
+      const int fx = x0 + j;
+      if (fx < geo.w) {
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+          const int fy = y0 + r;
+          if (fy < geo.h) a.planes[plane * c + (size_t)fy * geo.w + fx] = v[r];
+        }
+      }
+    }
+    __syncthreads();
+  }
+  // J.4.3 sigma per block (restoration.rs:338 vardct_sigma).
+  if (active && j < BR * BC) {
+    const int dy = j / BC, dx = j % BC;
+    size_t bi = (size_t)(by + dy) * geo.bw + bx + dx;
+    int s = a.sharpness[bi];
+    s = s > 7 ? 7 : s;
+    const float lut = s == 7 ? 1.0f : (float)s / 7.0f;
+    a.sigma[bi] = mul * 0.46f * lut;
+  }
+}
+
+void launch_render_varblocks(const RenderArgs& a, const uint32_t* const* lists, const int* counts,
+                             cudaStream_t s) {
+#define JPXLG_RV(IDX, R, C)                                                              \
+  if (counts[IDX])                                                                       \
+    k_render_vb<R, C><<<(counts[IDX] + (128 / ((R) > (C) ? (R) : (C))) - 1) /            \
+                            (128 / ((R) > (C) ? (R) : (C))),                             \
+                        128, 0, s>>>(a, lists[IDX], counts[IDX]);
+  // shape classes in kShapeSel order: DCT8, 16x16, 32x32, 16x8, 8x16, 32x8,
+  // 8x32, 32x16, 16x32 (rows x cols of samples)
+  JPXLG_RV(0, 8, 8)
+  JPXLG_RV(1, 16, 16)
+  JPXLG_RV(2, 32, 32)
+  JPXLG_RV(3, 16, 8)
+  JPXLG_RV(4, 8, 16)
+  JPXLG_RV(5, 32, 8)
+  JPXLG_RV(6, 8, 32)
+  JPXLG_RV(7, 32, 16)
+  JPXLG_RV(8, 16, 32)
+#undef JPXLG_RV
+}
+
+// ---------------------------------------------------------------------------
+// R2 — restoration.rs:148 gaborish_into: acc = fma(w, s, acc) over (dy, dx)
+// in row-major order from 0, kernel from GaborKernel::new (:111, with FMA).
+// ---------------------------------------------------------------------------
+
+constexpr int kGT = 32;
+__global__ void __launch_bounds__(256) k_gaborish(const float* __restrict__ in,
+                                                  float* __restrict__ out, int w, int h,
+                                                  float centre, float edge, float corner) {
+  __shared__ float t[kGT + 2][kGT + 3];
+  const size_t plane = (size_t)w * h;
+  in += plane * blockIdx.z;
+  out += plane * blockIdx.z;
+  const int x0 = blockIdx.x * kGT, y0 = blockIdx.y * kGT;
+  for (int i = threadIdx.x; i < (kGT + 2) * (kGT + 2); i += blockDim.x) {
+    int lx = i % (kGT + 2), ly = i / (kGT + 2);
+    int gx = mirror1d(x0 + lx - 1, w), gy = mirror1d(y0 + ly - 1, h);
+    t[ly][lx] = in[(size_t)gy * w + gx];
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < kGT * kGT; i += blockDim.x) {
+    int lx = i % kGT, ly = i / kGT;
+    int gx = x0 + lx, gy = y0 + ly;
+    if (gx >= w || gy >= h) continue;
+    float acc = 0.0f;
+#pragma unroll
+    for (int dy = -1; dy <= 1; ++dy)
+#pragma unroll
+      for (int dx = -1; dx <= 1; ++dx) {
+        float wt = (dx == 0 && dy == 0) ? centre : ((dx == 0 || dy == 0) ? edge : corner);
+        acc = __fmaf_rn(wt, t[ly + 1 + dy][lx + 1 + dx], acc);
+      }
+    out[(size_t)gy * w + gx] = acc;
+  }
+}
+
+void launch_gaborish(const float* in, float* out, int w, int h, cudaStream_t s) {
+  const float w1 = 0.115169525f, w2 = 0.061248592f;
+  float unnorm = fmaf(4.0f, w2, fmaf(4.0f, w1, 1.0f));
+  float scale = 1.0f / unnorm;
+  dim3 grid((w + kGT - 1) / kGT, (h + kGT - 1) / kGT, 3);
+  k_gaborish<<<grid, 256, 0, s>>>(in, out, w, h, scale, w1 * scale, w2 * scale);
+}
+
+// ---------------------------------------------------------------------------
+// R3 — restoration.rs:619 epf_step_rows_impl.  Distances: per tap,
+// d = fma(|a-b|, channel_scale[c], d) over channels then the cross (step 2:
+// the pixel alone); weight max(0, fma(pos_mul*d, -inv_sigma, 1)) (exactly 1
+// for zero distance); output sum_t fma(v, w, acc) / sum_t w.  Blocks with
+// sigma < 0.3 are copied.  pos_mul = 2/3 on the 8x8 border of the reference
+// pixel.  Mirrored padding of 3.
+// ---------------------------------------------------------------------------
+
+constexpr int kET = 32;
+constexpr int kEP = 3;
+constexpr int kES = kET + 2 * kEP;
+
+template <int STEP>
+__global__ void __launch_bounds__(256) k_epf(const float* __restrict__ in, float* __restrict__ out,
+                                             const float* __restrict__ sigma, int w, int h,
+                                             float step_mul4) {
+  __shared__ float t[3][kES][kES + 1];
+  const size_t plane = (size_t)w * h;
+  const int x0 = blockIdx.x * kET, y0 = blockIdx.y * kET;
+  for (int i = threadIdx.x; i < kES * kES; i += blockDim.x) {
+    int lx = i % kES, ly = i / kES;
+    int gx = mirror1d(x0 + lx - kEP, w), gy = mirror1d(y0 + ly - kEP, h);
+    size_t p = (size_t)gy * w + gx;
+    t[0][ly][lx] = in[p];
+    t[1][ly][lx] = in[plane + p];
+    t[2][ly][lx] = in[2 * plane + p];
+  }
+  __syncthreads();
+  const int bw = (w + 7) / 8;
+  const float scale[3] = {40.0f, 5.0f, 3.5f};
+  for (int i = threadIdx.x; i < kET * kET; i += blockDim.x) {
+    int lx = i % kET, ly = i / kET;
+    int gx = x0 + lx, gy = y0 + ly;
+    if (gx >= w || gy >= h) continue;
+    const int cx = lx + kEP, cy = ly + kEP;
+    size_t p = (size_t)gy * w + gx;
+    float bs = sigma[(size_t)(gy / 8) * bw + gx / 8];
+    if (bs < 0.3f) {
+      out[p] = t[0][cy][cx];
+      out[plane + p] = t[1][cy][cx];
+      out[2 * plane + p] = t[2][cy][cx];
+      continue;
+    }
+    const float inv_sigma = step_mul4 / bs;
+    const int rx = gx % 8, ry = gy % 8;
+    const bool at_border = ry == 0 || ry == 7 || rx == 0 || rx == 7;
+    const float pos_mul = at_border ? 2.0f / 3.0f : 1.0f;
+    float sum_w = 0.0f, acc0 = 0.0f, acc1 = 0.0f, acc2 = 0.0f;
+    constexpr int NT = STEP == 0 ? 13 : 5;
+#pragma unroll
+    for (int tp = 0; tp < NT; ++tp) {
+      // J.4.4 kernels: the 5-pixel cross, plus the diagonals and +-2 for step 0.
+      const int tkx[13] = {0, -1, 1, 0, 0, 1, 1, -1, -1, -2, 2, 0, 0};
+      const int tky[13] = {0, 0, 0, -1, 1, -1, 1, 1, -1, 0, 0, 2, -2};
+      const int kx = tkx[tp], ky = tky[tp];
+      float d = 0.0f;
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        if (STEP == 2) {
+          d = __fmaf_rn(fabsf(t[c][cy][cx] - t[c][cy + ky][cx + kx]), scale[c], d);
+        } else {
+          const int ix[5] = {0, -1, 1, 0, 0}, iy[5] = {0, 0, 0, -1, 1};
+#pragma unroll
+          for (int q = 0; q < 5; ++q) {
+            float av = t[c][cy + iy[q]][cx + ix[q]];
+            float bv = t[c][cy + ky + iy[q]][cx + kx + ix[q]];
+            d = __fmaf_rn(fabsf(av - bv), scale[c], d);
+          }
+        }
+      }
+      float sd = pos_mul * d;
+      float wt;
+      if (sd == 0.0f) {
+        wt = 1.0f;
+      } else {
+        float v = __fmaf_rn(sd, -inv_sigma, 1.0f);
+        wt = v > 0.0f ? v : 0.0f;
+      }
+      sum_w += wt;
+      acc0 = __fmaf_rn(t[0][cy + ky][cx + kx], wt, acc0);
+      acc1 = __fmaf_rn(t[1][cy + ky][cx + kx], wt, acc1);
+      acc2 = __fmaf_rn(t[2][cy + ky][cx + kx], wt, acc2);
+    }
+    out[p] = acc0 / sum_w;
+    out[plane + p] = acc1 / sum_w;
+    out[2 * plane + p] = acc2 / sum_w;
+  }
+}
+
+void launch_epf_step(int step, const float* in, float* out, const float* sigma, int w, int h,
+                     cudaStream_t s) {
+  // restoration.rs:356 epf_inv_sigma: step_multiplier * 4 * (1 - sqrt(0.5)) / sigma,
+  // evaluated left to right; the numerator is formed here once.
+  float sc = step == 0 ? 0.9f : (step == 1 ? 1.0f : 6.5f);
+  float sm = 1.65f * sc;
+  float num = sm * 4.0f * (1.0f - sqrtf(0.5f));
+  dim3 grid((w + kET - 1) / kET, (h + kET - 1) / kET);
+  if (step == 0) k_epf<0><<<grid, 256, 0, s>>>(in, out, sigma, w, h, num);
+  else if (step == 1) k_epf<1><<<grid, 256, 0, s>>>(in, out, sigma, w, h, num);
+  else k_epf<2><<<grid, 256, 0, s>>>(in, out, sigma, w, h, num);
+}
+
+// ---------------------------------------------------------------------------
+// R4 — color.rs:673 OpsinInverse::convert (cube without pow, FMA matrix),
+// then the output: linear planes; 8-bit sRGB as the decoder writes it
+// (decode.rs:3498 round(linear_to_srgb(v)*255) clamped) found by binary
+// search in the host-bisected level thresholds (plan-render lib.rs:333,
+// identical by construction); or the level's linear value (lib.rs:437).
+// ---------------------------------------------------------------------------
+
+__device__ __forceinline__ int level_of(float x, const float* thr, int n) {
+  if (!isfinite(x)) return 0;
+  int lo = 0, hi = n;  // count of thresholds <= x
+  while (lo < hi) {
+    int mid = (lo + hi) >> 1;
+    if (thr[mid] <= x) lo = mid + 1;
+    else hi = mid;
+  }
+  return lo;
+}
+
+template <int KIND>
+__global__ void __launch_bounds__(256) k_colour_out(const float* __restrict__ xyb, size_t n,
+                                                    const float* __restrict__ thr,
+                                                    const float* __restrict__ levels, int nlev,
+                                                    void* __restrict__ out) {
+  __shared__ float s_thr[255];
+  __shared__ float s_lev[256];
+  if (KIND == 2 || (KIND == 3 && nlev <= 256)) {
+    for (int i = threadIdx.x; i < nlev - 1; i += blockDim.x) s_thr[i] = thr[i];
+    for (int i = threadIdx.x; i < nlev; i += blockDim.x) s_lev[i] = levels[i];
+    __syncthreads();
+  }
+  const float* T = (nlev <= 256) ? s_thr : thr;
+  const float* LV = (nlev <= 256) ? s_lev : levels;
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (size_t)gridDim.x * blockDim.x) {
+    float x = xyb[i], y = xyb[n + i], b = xyb[2 * n + i];
+    float gm[3] = {y + x, y - x, b};
+    float mix[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      float v = gm[c] - c_opsin_bias_cbrt[c];
+      mix[c] = ((v * v) * v + c_opsin_bias[c]) * 1.0f;
+    }
+    float rgb[3];
+#pragma unroll
+    for (int r = 0; r < 3; ++r) {
+      float acc = 0.0f;
+#pragma unroll
+      for (int c = 0; c < 3; ++c) acc = __fmaf_rn(c_opsin_m[r * 3 + c], mix[c], acc);
+      rgb[r] = acc;
+    }
+    if (KIND == 1) {
+      float* o = (float*)out;
+      o[i] = rgb[0];
+      o[n + i] = rgb[1];
+      o[2 * n + i] = rgb[2];
+    } else if (KIND == 2) {
+      uint8_t* o = (uint8_t*)out;
+      o[3 * i] = (uint8_t)level_of(rgb[0], T, nlev - 1);
+      o[3 * i + 1] = (uint8_t)level_of(rgb[1], T, nlev - 1);
+      o[3 * i + 2] = (uint8_t)level_of(rgb[2], T, nlev - 1);
+    } else {
+      float* o = (float*)out;
+      o[i] = LV[level_of(rgb[0], T, nlev - 1)];
+      o[n + i] = LV[level_of(rgb[1], T, nlev - 1)];
+      o[2 * n + i] = LV[level_of(rgb[2], T, nlev - 1)];
+    }
+  }
+}
+
+void launch_colour_out(const float* xyb, int w, int h, int out_kind, const float* thresholds,
+                       const float* levels, int nlevels, void* out, int num_sms, cudaStream_t s) {
+  size_t n = (size_t)w * h;
+  int blocks = (int)std::min<size_t>((n + 255) / 256, (size_t)num_sms * 8);
+  if (blocks < 1) blocks = 1;
+  if (out_kind == 1) k_colour_out<1><<<blocks, 256, 0, s>>>(xyb, n, thresholds, levels, nlevels, out);
+  else if (out_kind == 2) k_colour_out<2><<<blocks, 256, 0, s>>>(xyb, n, thresholds, levels, nlevels, out);
+  else k_colour_out<3><<<blocks, 256, 0, s>>>(xyb, n, thresholds, levels, nlevels, out);
+}
+
+void upload_render_constants(const float* opsin_m, const float* opsin_bias,
+                             const float* opsin_bias_cbrt, cudaStream_t s) {
+  cudaMemcpyToSymbolAsync(c_opsin_m, opsin_m, sizeof(float) * 9, 0, cudaMemcpyHostToDevice, s);
+  cudaMemcpyToSymbolAsync(c_opsin_bias, opsin_bias, sizeof(float) * 3, 0, cudaMemcpyHostToDevice, s);
+  cudaMemcpyToSymbolAsync(c_opsin_bias_cbrt, opsin_bias_cbrt, sizeof(float) * 3, 0,
+                          cudaMemcpyHostToDevice, s);
+}
+
+}  // namespace jpxlg

@@ -1,0 +1,153 @@
+"""ctypes loader of the CPU restatement (oracle/_build/liboracle.so).
+
+TEST INFRASTRUCTURE ONLY: tests/, __graft_entry__.smoke() and bench.py's CPU
+baseline leg use it as the checker; the product never imports it.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+LIB = HERE / "_build" / "liboracle.so"
+
+
+class EncodeParams(C.Structure):
+    _fields_ = [("global_scale", C.c_uint32), ("quant_lf", C.c_uint32),
+                ("x_qm_scale", C.c_uint32), ("b_qm_scale", C.c_uint32),
+                ("gaborish", C.c_uint32), ("cfl", C.c_uint32)]
+
+
+class LfCfl(C.Structure):
+    _fields_ = [("x_factor_lf", C.c_int32), ("b_factor_lf", C.c_int32)]
+
+
+class RenderParams(C.Structure):
+    _fields_ = [("global_scale", C.c_uint32), ("quant_lf", C.c_uint32),
+                ("x_qm_scale", C.c_uint32), ("b_qm_scale", C.c_uint32),
+                ("gaborish", C.c_uint32), ("epf_iters", C.c_uint32),
+                ("x_factor_lf", C.c_int32), ("b_factor_lf", C.c_int32)]
+
+
+def build() -> Path:
+    """Builds liboracle.so with the committed Makefile (gcc, no GPU)."""
+    res = subprocess.run(["make", "-s", "-C", str(HERE)], capture_output=True, text=True)
+    if res.returncode != 0:
+        raise RuntimeError(f"oracle build failed:\n{res.stdout}\n{res.stderr}")
+    return LIB
+
+
+_lib = None
+
+
+def load() -> C.CDLL:
+    global _lib
+    if _lib is None:
+        if not LIB.exists():
+            build()
+        lib = C.CDLL(str(LIB))
+        f, i, p = C.c_float, C.c_int, C.c_void_p
+        for name in ("orc_cbrt_core", "orc_cbrt_perceptual", "orc_srgb_to_linear",
+                     "orc_linear_to_srgb"):
+            getattr(lib, name).restype = f
+            getattr(lib, name).argtypes = [f]
+        lib.orc_hf_multiplier.restype = f
+        lib.orc_hf_multiplier.argtypes = [C.c_uint32, C.c_uint32]
+        lib.orc_bias_adjust.restype = f
+        lib.orc_bias_adjust.argtypes = [C.c_int32, f, f]
+        lib.orc_scale_f.restype = f
+        lib.orc_scale_f.argtypes = [i, i]
+        lib.orc_gaborish_w.argtypes = [p, i, i, f, f, p]
+        lib.orc_encode.restype = i
+        lib.orc_encode.argtypes = [p, i, i, i, p, p, p, p, p, p, p, p, p, p, p]
+        lib.orc_reconstruct.restype = i
+        lib.orc_reconstruct.argtypes = [i, i, p, p, p, p, p, p, p, p, i, i, p]
+        lib.orc_ssim2.restype = i
+        lib.orc_ssim2.argtypes = [p, p, i, i, p, p, p]
+        lib.orc_perceptual_add_noise.argtypes = [p, p, p, i, f, C.c_uint32]
+        lib.orc_perceptual_synthetic.argtypes = [i, i, C.c_uint32, p, p, p]
+        _lib = lib
+    return _lib
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data
+
+
+def encode(rgb: np.ndarray, block_map: np.ndarray, hf_mul: np.ndarray, *, global_scale: int,
+           quant_lf: int = 16, x_qm_scale: int = 2, b_qm_scale: int = 2, gaborish: bool = False,
+           cfl: bool = True, bits: int | None = None, stages: bool = False):
+    """orc_encode: returns (rc, dict of outputs)."""
+    lib = load()
+    h, w = rgb.shape[:2]
+    bw, bh = (w + 7) // 8, (h + 7) // 8
+    tw, th = (bw + 7) // 8, (bh + 7) // 8
+    if bits is None:
+        bits = 8 if rgb.dtype == np.uint8 else 16
+    rgb = np.ascontiguousarray(rgb)
+    out = {
+        "qcoeff": np.zeros((3, bh * 8, bw * 8), np.int32),
+        "lf": np.zeros((3, bh, bw), np.int32),
+        "cfl_x": np.zeros((th, tw), np.int8),
+        "cfl_b": np.zeros((th, tw), np.int8),
+    }
+    if stages:
+        out["xyb"] = np.zeros((3, h, w), np.float32)
+        out["pre"] = np.zeros((3, h, w), np.float32)
+        out["coeff"] = np.zeros((3, bh * 8, bw * 8), np.float32)
+    lfc = LfCfl()
+    p = EncodeParams(global_scale, quant_lf, x_qm_scale, b_qm_scale, int(gaborish), int(cfl))
+    bm = np.ascontiguousarray(block_map, np.uint8)
+    hm = np.ascontiguousarray(hf_mul, np.uint32)
+    rc = lib.orc_encode(rgb.ctypes.data, w, h, bits, bm.ctypes.data, hm.ctypes.data, C.byref(p),
+                        _ptr(out.get("xyb")), _ptr(out.get("pre")), _ptr(out.get("coeff")),
+                        out["qcoeff"].ctypes.data, out["lf"].ctypes.data,
+                        out["cfl_x"].ctypes.data, out["cfl_b"].ctypes.data, C.byref(lfc))
+    out["lf_factors"] = (lfc.x_factor_lf, lfc.b_factor_lf)
+    return rc, out
+
+
+def reconstruct(w: int, h: int, block_map, hf_mul, sharpness, plan: dict, *, global_scale: int,
+                quant_lf: int = 16, x_qm_scale: int = 2, b_qm_scale: int = 2,
+                gaborish: bool = False, epf_iters: int = 0, out_kind: int = 2, bits: int = 8):
+    lib = load()
+    p = RenderParams(global_scale, quant_lf, x_qm_scale, b_qm_scale, int(gaborish), epf_iters,
+                     int(plan["lf_factors"][0]), int(plan["lf_factors"][1]))
+    out = (np.zeros((h, w, 3), np.uint8) if out_kind == 2 else np.zeros((3, h, w), np.float32))
+    arrs = [np.ascontiguousarray(block_map, np.uint8), np.ascontiguousarray(hf_mul, np.uint32),
+            np.ascontiguousarray(sharpness, np.uint8),
+            np.ascontiguousarray(plan["qcoeff"], np.int32),
+            np.ascontiguousarray(plan["lf"], np.int32),
+            np.ascontiguousarray(plan["cfl_x"], np.int8),
+            np.ascontiguousarray(plan["cfl_b"], np.int8)]
+    rc = lib.orc_reconstruct(w, h, *[a.ctypes.data for a in arrs], C.byref(p), out_kind, bits,
+                             out.ctypes.data)
+    return rc, out
+
+
+def ssim2(ref: np.ndarray, cand: np.ndarray):
+    """orc_ssim2 on linear float32 [3, H, W] planes: (score, raw_error, terms)."""
+    lib = load()
+    ref = np.ascontiguousarray(ref, np.float32)
+    cand = np.ascontiguousarray(cand, np.float32)
+    _, h, w = ref.shape
+    ra = (C.c_void_p * 3)(*[ref[c].ctypes.data for c in range(3)])
+    ca = (C.c_void_p * 3)(*[cand[c].ctypes.data for c in range(3)])
+    sc, raw = C.c_double(), C.c_double()
+    terms = np.zeros(6 * 18, np.float64)
+    n = lib.orc_ssim2(ra, ca, w, h, C.byref(sc), C.byref(raw), terms.ctypes.data)
+    return sc.value, raw.value, terms[: max(n, 0) * 18]
+
+
+def perceptual_pair(w: int, h: int, seed: int, amp: float, noise_seed: int):
+    """The reference's perceptual test fixtures (synthetic + add_noise)."""
+    lib = load()
+    a = np.zeros((3, h, w), np.float32)
+    lib.orc_perceptual_synthetic(w, h, seed, a[0].ctypes.data, a[1].ctypes.data, a[2].ctypes.data)
+    b = a.copy()
+    lib.orc_perceptual_add_noise(b[0].ctypes.data, b[1].ctypes.data, b[2].ctypes.data, w * h,
+                                 C.c_float(amp), noise_seed)
+    return a, b
