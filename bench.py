@@ -245,8 +245,13 @@ def run_ours(args):
     build.build()
     images, _ = make_workload(rank, world)
     ctx = jg.Context(local)
-    stream = torch.cuda.current_stream()
+    # A dedicated stream shared by the library and the timing events (the
+    # default stream's handle is 0, which the library reads as "own stream").
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
     ctx.set_stream(stream.cuda_stream)
+    if ctx.stream != stream.cuda_stream:
+        raise RuntimeError("the library did not adopt the timing stream")
     req = jg.EncodeRequest.with_global_scale(GLOBAL_SCALE, gaborish=True, epf_iters=3)
     layouts, refs, dev_rgb, host_rgb = [], [], [], []
     for rgb, cover in images:
@@ -365,6 +370,7 @@ def run_ours(args):
                 "h2d_bytes_per_step": int(sum(r.nbytes for r, _ in images)),
                 "d2h_bytes_per_step": 8 * len(images)},
         "gpu_launches": int(launches),
+        "cfl_sequential_fallbacks": ctx.cfl_fallbacks,
         "clocks": clocks,
         "scores": [round(float(s), 6) for s in dev_scores],
     }

@@ -121,6 +121,10 @@ int jpxlg_ctx_synchronize(jpxlg_ctx* ctx);
 const char* jpxlg_last_error(const jpxlg_ctx* ctx);
 /* Kernel launches the context issued since creation (for accounting). */
 uint64_t jpxlg_ctx_launches(const jpxlg_ctx* ctx);
+/* CfL decisions (per tile, or the frame's LF pair) that the tree-ordered f64
+ * sums could not settle and that were recomputed in the reference's
+ * sequential order, since creation (synchronizes). */
+uint32_t jpxlg_ctx_cfl_fallbacks(jpxlg_ctx* ctx);
 
 /* Stage timers (the GPU counterpart of plan-render lib.rs:472 RenderTimings
  * and the policy's stage diagnostics): when enabled, CUDA events recorded on

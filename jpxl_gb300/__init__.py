@@ -146,6 +146,10 @@ class Context:
     def launches(self) -> int:
         return int(self.lib.jpxlg_ctx_launches(self.handle))
 
+    @property
+    def cfl_fallbacks(self) -> int:
+        return int(self.lib.jpxlg_ctx_cfl_fallbacks(self.handle))
+
     def stage_timing(self, enable: bool) -> None:
         self.check(self.lib.jpxlg_stage_timing(self.handle, int(enable)))
 

@@ -24,6 +24,7 @@ SIGNATURES: dict[str, tuple] = {
     "jpxlg_ctx_synchronize": (_I, [_P]),
     "jpxlg_last_error": (C.c_char_p, [_P]),
     "jpxlg_ctx_launches": (C.c_uint64, [_P]),
+    "jpxlg_ctx_cfl_fallbacks": (_U32, [_P]),
     "jpxlg_stage_timing": (_I, [_P, _I]),
     "jpxlg_stage_times": (_I, [_P, _P, _P, _I]),
     "jpxlg_layout_create": (_I, [_P, _I, _I, _P, _P, _P, C.POINTER(_P)]),

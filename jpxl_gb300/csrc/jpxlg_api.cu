@@ -242,9 +242,6 @@ int encode_device(jpxlg_ctx* ctx, const jpxlg_layout* L, const void* rgb_dev, in
   CK(ctx->dyhf.ensure(n8 * sizeof(float)));
   CK(ctx->lfs.ensure(3 * nb * sizeof(float)));
   CK(ctx->dylf.ensure(nb * sizeof(float)));
-  const int nparts = std::max(1, std::min(ctx->num_sms * 2, (int)((nb + 255) / 256)));
-  CK(ctx->lf_part.ensure((size_t)nparts * 8 * sizeof(double)));
-  CK(ctx->lf_cost.ensure((size_t)nparts * 8 * sizeof(unsigned long long)));
   CK(ctx->lf_seed.ensure(4 * sizeof(int)));
   const float* lut = get_lut(ctx, bits);
   if (!lut) return fail(ctx, JPXLG_ERR_CUDA, "transfer table allocation failed");
@@ -293,9 +290,7 @@ int encode_device(jpxlg_ctx* ctx, const jpxlg_layout* L, const void* rgb_dev, in
   stage_end(ctx);
   if (rc) return rc;
   stage_begin(ctx, JPXLG_STAGE_CFL);
-  rc = after_launch(ctx, launch_cfl(a, ctx->lf_part.as<double>(),
-                                    ctx->lf_cost.as<unsigned long long>(), ctx->lf_seed.as<int>(),
-                                    nparts, ctx->stream));
+  rc = after_launch(ctx, launch_cfl(a, ctx->lf_seed.as<int>(), ctx->stream));
   stage_end(ctx);
   if (rc) return rc;
   stage_begin(ctx, JPXLG_STAGE_QUANT_CHROMA);
@@ -409,7 +404,7 @@ int score_device(jpxlg_ctx* ctx, const jpxlg_ref* ref, const float* cand_dev, do
       cur = next;
       next += 3 * (size_t)rs.w * rs.h;
     }
-    ctas[s] = launch_score_scale(cur, rs, part, ctx->stream);
+    ctas[s] = launch_score_scale(cur, rs, part, ctx->num_sms, ctx->stream);
     ++k;
     pixels[s] = rs.w * rs.h;
     part += (size_t)ctas[s] * 18;
@@ -519,6 +514,15 @@ const char* jpxlg_last_error(const jpxlg_ctx* ctx) {
 }
 
 uint64_t jpxlg_ctx_launches(const jpxlg_ctx* ctx) { return ctx ? ctx->launches : 0; }
+
+uint32_t jpxlg_ctx_cfl_fallbacks(jpxlg_ctx* ctx) {
+  if (!ctx) return 0;
+  cudaSetDevice(ctx->device);
+  uint32_t v = 0;
+  cudaStreamSynchronize(ctx->stream);
+  cudaMemcpy(&v, ctx->d_words + 2, sizeof(uint32_t), cudaMemcpyDeviceToHost);
+  return v;
+}
 
 int jpxlg_stage_timing(jpxlg_ctx* ctx, int enable) {
   if (!ctx) return JPXLG_ERR_ARGUMENT;

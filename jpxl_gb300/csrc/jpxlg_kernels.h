@@ -57,8 +57,7 @@ void launch_precondition(const float* in, float* out, int w, int h, cudaStream_t
 // Each returns the number of kernels it launched.
 int launch_fdct_luma(const EncArgs& a, const uint32_t* const* lists, const int* counts,
                      cudaStream_t s);
-int launch_cfl(const EncArgs& a, double* lf_part, unsigned long long* lf_cost_part, int* lf_seeds,
-               int nparts, cudaStream_t s);
+int launch_cfl(const EncArgs& a, int* lf_seeds, cudaStream_t s);
 int launch_quant_chroma(const EncArgs& a, const uint32_t* const* lists, const int* counts,
                         cudaStream_t s);
 
@@ -88,7 +87,7 @@ void launch_ref_moments(const float* xyb, float* mu, float* s11, float* tmp, int
 // Candidate side of one scale: cand is linear RGB [3][w*h]; partial receives
 // per-CTA f64 sums [ctas][18].
 int launch_score_scale(const float* cand_rgb, const SsimScale& ref, double* partial,
-                       cudaStream_t s);
+                       int num_sms, cudaStream_t s);
 void launch_score_finish(const double* partials, const int* ctas_per_scale, int nscales,
                          const int* pixels_per_scale, double* out /* score, raw, terms[108] */,
                          cudaStream_t s);

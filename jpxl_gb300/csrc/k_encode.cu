@@ -88,88 +88,119 @@ void launch_srgb_to_xyb(const void* rgb, int bits, size_t n, const float* lut, f
 // after every step, so border taps read exactly the mirrored samples.
 // ---------------------------------------------------------------------------
 
-constexpr int kPreTile = 32;
+constexpr int kPreTile = 64;
 constexpr int kPreHalo = 12;
-constexpr int kPreS = kPreTile + 2 * kPreHalo;  // 56
+constexpr int kPreS = kPreTile + 2 * kPreHalo;  // 88
+constexpr int kPreThreads = 512;
+constexpr size_t kPreSmem = 3 * kPreS * kPreS * sizeof(float);
 
 struct EncKernel {
   float centre, edge, corner, inv_c;
 };
 
-__global__ void __launch_bounds__(256) k_precondition(const float* __restrict__ in,
-                                                      float* __restrict__ out, int w, int h,
-                                                      EncKernel k) {
-  __shared__ float F[kPreS * kPreS];
-  __shared__ float X[2][kPreS * kPreS];
+__global__ void __launch_bounds__(kPreThreads) k_precondition(const float* __restrict__ in,
+                                                              float* __restrict__ out, int w,
+                                                              int h, EncKernel k) {
+  extern __shared__ float pre_smem[];
+  float* F = pre_smem;
+  float* const X0 = pre_smem + kPreS * kPreS;
+  float* const X1 = pre_smem + 2 * kPreS * kPreS;
   const size_t plane = (size_t)w * h;
   in += plane * blockIdx.z;
   out += plane * blockIdx.z;
   const int tx0 = blockIdx.x * kPreTile, ty0 = blockIdx.y * kPreTile;
   const int gx0 = tx0 - kPreHalo, gy0 = ty0 - kPreHalo;
-  for (int i = threadIdx.x; i < kPreS * kPreS; i += blockDim.x) {
-    int lx = i % kPreS, ly = i / kPreS;
-    int gx = mirror1d(gx0 + lx, w), gy = mirror1d(gy0 + ly, h);
-    float v = in[(size_t)gy * w + gx];
-    F[i] = v;
-    X[0][i] = v;
+  const int lane = threadIdx.x % 32, warp = threadIdx.x / 32;
+  constexpr int kWarps = kPreThreads / 32;
+  for (int ly = warp; ly < kPreS; ly += kWarps) {
+    const int gy = mirror1d(gy0 + ly, h);
+    for (int lx = lane; lx < kPreS; lx += 32) {
+      int gx = mirror1d(gx0 + lx, w);
+      float v = in[(size_t)gy * w + gx];
+      F[ly * kPreS + lx] = v;
+      X0[ly * kPreS + lx] = v;
+    }
   }
   __syncthreads();
   const size_t n = plane;
   const size_t bulk = n - n % 4;
+  // flat < bulk  <=>  (gy, gx) < (bulk_row, bulk_col) lexicographically
+  const int bulk_row = (int)(bulk / (size_t)w), bulk_col = (int)(bulk % (size_t)w);
   const int groups = (w >= 3 && h >= 3) ? (w - 2) / 4 : 0;
+  // Whether any cell of the tile lies outside the frame (block-uniform).
+  const bool has_halo_out = gx0 < 0 || gy0 < 0 || gx0 + kPreS > w || gy0 + kPreS > h;
   int cur = 0;
   for (int it = 0; it < 12; ++it) {
     const int r = kPreHalo - 1 - it;  // cells within r of the tile are updated
     const int lo = kPreHalo - r, hi = kPreHalo + kPreTile + r;  // local [lo, hi)
-    const int span = hi - lo;
-    const float* xs = X[cur];
-    float* xn = X[cur ^ 1];
-    for (int i = threadIdx.x; i < span * span; i += blockDim.x) {
-      int lx = lo + i % span, ly = lo + i / span;
-      int gx = gx0 + lx, gy = gy0 + ly;
-      if (gx < 0 || gy < 0 || gx >= w || gy >= h) continue;
-      const int c = ly * kPreS + lx;
-      float kx;
-      bool border = gx == 0 || gy == 0 || gx == w - 1 || gy == h - 1;
-      if (!border && gx - 1 < 4 * groups) {
-        float mid = xs[c], north = xs[c - kPreS], south = xs[c + kPreS];
-        float west = xs[c - 1], east = xs[c + 1];
-        float nw = xs[c - kPreS - 1], ne = xs[c - kPreS + 1];
-        float sw = xs[c + kPreS - 1], se = xs[c + kPreS + 1];
-        kx = mid * k.centre + (north + south + west + east) * k.edge +
-             (nw + ne + sw + se) * k.corner;
-      } else {
-        float acc = 0.0f;
-#pragma unroll
-        for (int dy = -1; dy <= 1; ++dy)
-#pragma unroll
-          for (int dx = -1; dx <= 1; ++dx) {
-            float wt = (dx == 0 && dy == 0) ? k.centre : ((dx == 0 || dy == 0) ? k.edge : k.corner);
-            acc += wt * xs[c + dy * kPreS + dx];
+    const float* xs = cur ? X1 : X0;
+    float* xn = cur ? X0 : X1;
+    // Each warp sweeps a band of rows; each lane a column, with the 3x3
+    // neighbourhood rolling down in registers.
+    const int band = (hi - lo + kWarps - 1) / kWarps;
+    const int ly0 = lo + warp * band, ly1 = min(ly0 + band, hi);
+    for (int lx = lo + lane; lx < hi; lx += 32) {
+      if (ly0 >= ly1) break;
+      const int gx = gx0 + lx;
+      const bool in_x = gx >= 0 && gx < w;
+      const bool edge_x = gx == 0 || gx == w - 1;
+      const bool simd_x = gx - 1 < 4 * groups;
+      const float* p = xs + (ly0 - 1) * kPreS + lx;
+      float nw = p[-1], nn = p[0], ne = p[1];
+      p += kPreS;
+      float ww = p[-1], mm = p[0], ee = p[1];
+      for (int ly = ly0; ly < ly1; ++ly) {
+        p += kPreS;
+        const float sw = p[-1], ss = p[0], se = p[1];
+        const int gy = gy0 + ly;
+        if (in_x && gy >= 0 && gy < h) {
+          const bool border = edge_x || gy == 0 || gy == h - 1;
+          float kx;
+          if (!border && simd_x) {
+            kx = mm * k.centre + (nn + ss + ww + ee) * k.edge + (nw + ne + sw + se) * k.corner;
+          } else {
+            // nine taps in order: dy = -1, 0, 1 outer, dx inner
+            float acc = 0.0f;
+            acc += k.corner * nw;
+            acc += k.edge * nn;
+            acc += k.corner * ne;
+            acc += k.edge * ww;
+            acc += k.centre * mm;
+            acc += k.edge * ee;
+            acc += k.corner * sw;
+            acc += k.edge * ss;
+            acc += k.corner * se;
+            kx = acc;
           }
-        kx = acc;
+          const int c = ly * kPreS + lx;
+          const float fv = F[c];
+          const bool in_bulk = gy < bulk_row || (gy == bulk_row && gx < bulk_col);
+          xn[c] = in_bulk ? mm + (fv - kx) * k.inv_c : mm + (fv - kx) / k.centre;
+        }
+        nw = ww; nn = mm; ne = ee;
+        ww = sw; mm = ss; ee = se;
       }
-      size_t flat = (size_t)gy * w + gx;
-      float xv = xs[c], fv = F[c];
-      xn[c] = flat < bulk ? xv + (fv - kx) * k.inv_c : xv + (fv - kx) / k.centre;
     }
     __syncthreads();
     // Out-of-frame halo cells take their mirror's new value.
-    for (int i = threadIdx.x; i < span * span; i += blockDim.x) {
-      int lx = lo + i % span, ly = lo + i / span;
-      int gx = gx0 + lx, gy = gy0 + ly;
-      if (gx >= 0 && gy >= 0 && gx < w && gy < h) continue;
-      int mx = mirror1d(gx, w) - gx0, my = mirror1d(gy, h) - gy0;
-      xn[ly * kPreS + lx] = xn[my * kPreS + mx];
+    if (has_halo_out) {
+      for (int ly = lo + warp; ly < hi; ly += kWarps)
+        for (int lx = lo + lane; lx < hi; lx += 32) {
+          int gx = gx0 + lx, gy = gy0 + ly;
+          if (gx >= 0 && gy >= 0 && gx < w && gy < h) continue;
+          int mx = mirror1d(gx, w) - gx0, my = mirror1d(gy, h) - gy0;
+          xn[ly * kPreS + lx] = xn[my * kPreS + mx];
+        }
+      __syncthreads();
     }
-    __syncthreads();
     cur ^= 1;
   }
-  for (int i = threadIdx.x; i < kPreTile * kPreTile; i += blockDim.x) {
-    int lx = i % kPreTile, ly = i / kPreTile;
-    int gx = tx0 + lx, gy = ty0 + ly;
-    if (gx < w && gy < h) out[(size_t)gy * w + gx] = X[cur][(ly + kPreHalo) * kPreS + lx + kPreHalo];
-  }
+  for (int ly = warp; ly < kPreTile; ly += kWarps)
+    for (int lx = lane; lx < kPreTile; lx += 32) {
+      int gx = tx0 + lx, gy = ty0 + ly;
+      if (gx < w && gy < h)
+        out[(size_t)gy * w + gx] = (cur ? X1 : X0)[(ly + kPreHalo) * kPreS + lx + kPreHalo];
+    }
 }
 
 void launch_precondition(const float* in, float* out, int w, int h, cudaStream_t s) {
@@ -178,8 +209,14 @@ void launch_precondition(const float* in, float* out, int w, int h, cudaStream_t
   float unnorm = 1.0f + 4.0f * w1 + 4.0f * w2;
   float scale = 1.0f / unnorm;
   EncKernel k{scale, w1 * scale, w2 * scale, 1.0f / scale};
+  static bool configured = false;
+  if (!configured) {
+    cudaFuncSetAttribute(k_precondition, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)kPreSmem);
+    configured = true;
+  }
   dim3 grid((w + kPreTile - 1) / kPreTile, (h + kPreTile - 1) / kPreTile, 3);
-  k_precondition<<<grid, 256, 0, s>>>(in, out, w, h, k);
+  k_precondition<<<grid, kPreThreads, kPreSmem, s>>>(in, out, w, h, k);
 }
 
 // ---------------------------------------------------------------------------
@@ -474,6 +511,45 @@ __device__ __forceinline__ uint32_t factor_bits(int32_t f) {
   return (32u - __clz(af)) + 2u;
 }
 
+// Double-float (f32 pair) accumulation for the regression sums: products of
+// two f32 are split exactly (two_prod), sums keep hi+lo to ~2^-46 per
+// addition, so a sum over n terms lies within n*2^-46*sum|t| of the exact sum
+// at f32 issue rates (GB300's FP64 rate is 1/64 of its FP32 rate).
+struct DF {
+  float hi, lo;
+};
+__device__ __forceinline__ DF df_two_prod(float a, float b) {
+  float p = a * b;
+  return {p, __fmaf_rn(a, b, -p)};
+}
+__device__ __forceinline__ DF df_add(DF a, DF b) {
+  float s = a.hi + b.hi;
+  float bb = s - a.hi;
+  float e = (a.hi - (s - bb)) + (b.hi - bb);
+  e = e + (a.lo + b.lo);
+  float h = s + e;
+  return {h, e - (h - s)};
+}
+// Block sum of a DF in fixed order (warp butterfly, then warps in order);
+// returned as f64 in thread 0.
+template <int NT>
+__device__ double block_sum_df(DF v, double* scratch) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    DF w{__shfl_xor_sync(0xffffffffu, v.hi, o), __shfl_xor_sync(0xffffffffu, v.lo, o)};
+    v = df_add(v, w);
+  }
+  const int wid = threadIdx.x / 32, lane = threadIdx.x % 32;
+  __syncthreads();
+  if (lane == 0) scratch[wid] = (double)v.hi + (double)v.lo;
+  __syncthreads();
+  double t = 0.0;
+  if (threadIdx.x == 0)
+    for (int i = 0; i < NT / 32; ++i) t += scratch[i];
+  __syncthreads();
+  return t;
+}
+
 // Block-wide fixed-order sum of doubles (warp shuffles, then warp order).
 template <int NT>
 __device__ double block_sum(double v, double* scratch) {
@@ -538,36 +614,46 @@ __global__ void __launch_bounds__(kCflThreads) k_cfl_tiles(EncArgs a) {
   const size_t cplane = (size_t)geo.W8 * geo.H8;
   const int px0 = tx * 64, py0 = ty * 64;
   const int pw = min(64, geo.W8 - px0), ph = min(64, geo.H8 - py0);
-  // Phase A: tree sums.
-  double syy = 0, syx = 0, sxx = 0, syb = 0, sbb = 0, ayx = 0, ayb = 0, cnt = 0;
-  for (int i = threadIdx.x; i < pw * ph; i += kCflThreads) {
-    int px = px0 + i % pw, py = py0 + i / pw;
-    int side;
-    if (cell_is_llf(a.block_map, geo.bw, px, py, &side)) continue;
-    size_t ci = (size_t)py * geo.W8 + px;
-    double y = (double)a.coeff[cplane + ci];
-    double x = (double)a.coeff[ci];
-    double b = (double)a.coeff[2 * cplane + ci];
-    syy += y * y;
-    syx += y * x;
-    sxx += x * x;
-    syb += y * b;
-    sbb += b * b;
-    ayx += fabs(y * x);
-    ayb += fabs(y * b);
-    cnt += 1.0;
+  // Phase A: tree sums in double-float.  Thread t covers column (t % 64) of
+  // rows t/64, t/64 + 4, ... of the tile: coalesced rows, no divisions.
+  DF syy{0, 0}, syx{0, 0}, sxx{0, 0}, syb{0, 0}, sbb{0, 0};
+  float ayx = 0.0f, ayb = 0.0f, cnt = 0.0f;
+  {
+    const int col = threadIdx.x % 64;
+    if (col < pw) {
+      const int px = px0 + col;
+      for (int row = threadIdx.x / 64; row < ph; row += kCflThreads / 64) {
+        const int py = py0 + row;
+        int side;
+        if (cell_is_llf(a.block_map, geo.bw, px, py, &side)) continue;
+        size_t ci = (size_t)py * geo.W8 + px;
+        float y = a.coeff[cplane + ci];
+        float x = a.coeff[ci];
+        float b = a.coeff[2 * cplane + ci];
+        syy = df_add(syy, df_two_prod(y, y));
+        syx = df_add(syx, df_two_prod(y, x));
+        sxx = df_add(sxx, df_two_prod(x, x));
+        syb = df_add(syb, df_two_prod(y, b));
+        sbb = df_add(sbb, df_two_prod(b, b));
+        ayx += fabsf(y * x);
+        ayb += fabsf(y * b);
+        cnt += 1.0f;
+      }
+    }
   }
-  double t_syy = block_sum<kCflThreads>(syy, sd);
-  double t_syx = block_sum<kCflThreads>(syx, sd);
-  double t_sxx = block_sum<kCflThreads>(sxx, sd);
-  double t_syb = block_sum<kCflThreads>(syb, sd);
-  double t_sbb = block_sum<kCflThreads>(sbb, sd);
-  double t_ayx = block_sum<kCflThreads>(ayx, sd);
-  double t_ayb = block_sum<kCflThreads>(ayb, sd);
-  double t_cnt = block_sum<kCflThreads>(cnt, sd);
+  double t_syy = block_sum_df<kCflThreads>(syy, sd);
+  double t_syx = block_sum_df<kCflThreads>(syx, sd);
+  double t_sxx = block_sum_df<kCflThreads>(sxx, sd);
+  double t_syb = block_sum_df<kCflThreads>(syb, sd);
+  double t_sbb = block_sum_df<kCflThreads>(sbb, sd);
+  double t_ayx = block_sum_df<kCflThreads>(DF{ayx, 0.0f}, sd);
+  double t_ayb = block_sum_df<kCflThreads>(DF{ayb, 0.0f}, sd);
+  double t_cnt = block_sum_df<kCflThreads>(DF{cnt, 0.0f}, sd);
   if (threadIdx.x == 0) {
-    const double u = 1.1102230246251565e-16;
-    const double gam = 2.0 * (t_cnt + 2.0) * u;  // both orders vs exact
+    // Distance of the double-float tree sum and of the reference's
+    // sequential f64 sum from the exact sum, relative to sum|t| (the |t|
+    // sums above are f32 estimates; the factor 2 covers their error).
+    const double gam = 2.0 * (t_cnt + 64.0) * (2.2737367544323206e-13 + 1.1102230246251565e-16);
     for (int ch = 0; ch < 2; ++ch) {
       RegSums s;
       s.s_yy = t_syy;
@@ -638,30 +724,36 @@ __global__ void __launch_bounds__(kCflThreads) k_cfl_tiles(EncArgs a) {
   const float* m_b = a.dq + 2 * kDequantTableFloats;
   unsigned long long bits[2][4] = {{0, 0, 0, 0}, {0, 0, 0, 0}};
   float kx[4], kb[4];
+#pragma unroll
   for (int i = 0; i < 4; ++i) {
     kx[i] = 0.0f + (float)s_cands[0][i < s_ncand[0] ? i : 0] / 84.0f;
     kb[i] = 1.0f + (float)s_cands[1][i < s_ncand[1] ? i : 0] / 84.0f;
   }
   const bool need_x = s_seed[0] != 0, need_b = s_seed[1] != 0;
+  const int ncx = need_x ? s_ncand[0] : 0, ncb = need_b ? s_ncand[1] : 0;
   if (need_x || need_b) {
-    for (int i = threadIdx.x; i < pw * ph; i += kCflThreads) {
-      int px = px0 + i % pw, py = py0 + i / pw;
-      int side;
-      if (cell_is_llf(a.block_map, geo.bw, px, py, &side)) continue;
-      int fold = side / 8;
-      int lrow = (py % side), lcol = (px % side);
-      int cell8 = (lrow / fold) * 8 + (lcol / fold);
-      size_t ci = (size_t)py * geo.W8 + px;
-      float dy = a.dyhf[ci];
-      float x = a.coeff[ci], b = a.coeff[2 * cplane + ci];
-      float step_x = scale_x * __ldg(&m_x[cell8]);
-      float step_b = scale_b * __ldg(&m_b[cell8]);
-      float rc;
-      for (int c = 0; c < 4; ++c) {
-        if (need_x && c < s_ncand[0])
-          bits[0][c] += residual_bits(choose(x - kx[c] * dy, step_x, c_quant_bias[0], a.err, &rc));
-        if (need_b && c < s_ncand[1])
-          bits[1][c] += residual_bits(choose(b - kb[c] * dy, step_b, c_quant_bias[2], a.err, &rc));
+    const int col = threadIdx.x % 64;
+    if (col < pw) {
+      const int px = px0 + col;
+      for (int row = threadIdx.x / 64; row < ph; row += kCflThreads / 64) {
+        const int py = py0 + row;
+        int side;
+        if (cell_is_llf(a.block_map, geo.bw, px, py, &side)) continue;
+        const int fold = side / 8;
+        const int cell8 = ((py & (side - 1)) / fold) * 8 + ((px & (side - 1)) / fold);
+        size_t ci = (size_t)py * geo.W8 + px;
+        float dy = a.dyhf[ci];
+        float x = a.coeff[ci], b = a.coeff[2 * cplane + ci];
+        float step_x = scale_x * __ldg(&m_x[cell8]);
+        float step_b = scale_b * __ldg(&m_b[cell8]);
+        float rc;
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+          if (c < ncx)
+            bits[0][c] += residual_bits(choose(x - kx[c] * dy, step_x, c_quant_bias[0], a.err, &rc));
+          if (c < ncb)
+            bits[1][c] += residual_bits(choose(b - kb[c] * dy, step_b, c_quant_bias[2], a.err, &rc));
+        }
       }
     }
   }
@@ -700,50 +792,67 @@ __global__ void __launch_bounds__(kCflThreads) k_cfl_tiles(EncArgs a) {
   }
 }
 
-// Frame-wide LF pair (lib.rs:3831 refine_lf_factors).  Pass 1: per-CTA
-// regression partial sums over the LF samples (one per 8x8 block).
-constexpr int kLfThreads = 256;
-__global__ void __launch_bounds__(kLfThreads) k_cfl_lf_sums(EncArgs a, double* partial) {
-  __shared__ double sd[kLfThreads / 32];
-  const Geo& geo = a.geo;
-  const size_t nb = (size_t)geo.bw * geo.bh;
-  double v[7] = {0, 0, 0, 0, 0, 0, 0};  // yy, yx, xx, yb, bb, |yx|, |yb|
-  for (size_t i = (size_t)blockIdx.x * kLfThreads + threadIdx.x; i < nb;
-       i += (size_t)gridDim.x * kLfThreads) {
-    double y = a.lfs[nb + i], x = a.lfs[i], b = a.lfs[2 * nb + i];
-    v[0] += y * y; v[1] += y * x; v[2] += x * x; v[3] += y * b; v[4] += b * b;
-    v[5] += fabs(y * x); v[6] += fabs(y * b);
+// Frame-wide LF pair (lib.rs:3831 refine_lf_factors), in two single-CTA
+// kernels: the regression sums over every LF sample and the seeds (with the
+// sequential fallback in the reference's LF-group / band / varblock / cell
+// order when a seed is not robust); then the residual bit costs of both
+// candidate windows and the joint choice.
+constexpr int kLfThreads = 1024;
+
+__device__ void lf_candidates(int seed, int* c, int* nc_out) {
+  int nc = 0;
+  for (int d = -1; d <= 1; ++d) {
+    int v = min(max(seed + d, -128), 127);
+    bool dup = false;
+    for (int i = 0; i < nc; ++i) dup |= c[i] == v;
+    if (!dup) c[nc++] = v;
   }
-  for (int k = 0; k < 7; ++k) {
-    double t = block_sum<kLfThreads>(v[k], sd);
-    if (threadIdx.x == 0) partial[blockIdx.x * 8 + k] = t;
-  }
+  bool has0 = false;
+  for (int i = 0; i < nc; ++i) has0 |= c[i] == 0;
+  if (!has0) c[nc++] = 0;
+  *nc_out = nc;
 }
 
-// Pass 2 (one thread): reduce the partials in block order, decide the seeds
-// (with the sequential fallback in the reference's LF-group / band /
-// varblock / cell order when a seed is not robust), write the candidate
-// windows.
-__global__ void k_cfl_lf_seed(EncArgs a, const double* partial, int nparts, int* cand) {
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+__global__ void __launch_bounds__(kLfThreads) k_cfl_lf_seed(EncArgs a, int* seeds) {
+  __shared__ double sd[kLfThreads / 32];
+  const Geo& geo = a.geo;
   if (*a.not_gray == 0u || !a.cfl_enabled) {
-    cand[0] = 0;
-    cand[1] = 0;
+    if (threadIdx.x == 0) {
+      seeds[0] = 0;
+      seeds[1] = 0;
+    }
     return;
   }
-  const Geo& geo = a.geo;
-  double t[7] = {0, 0, 0, 0, 0, 0, 0};
-  for (int p = 0; p < nparts; ++p)
-    for (int k = 0; k < 7; ++k) t[k] += partial[p * 8 + k];
-  const double n = (double)geo.bw * geo.bh;
-  const double gam = 2.0 * (n + 2.0) * 1.1102230246251565e-16;
+  const size_t nb = (size_t)geo.bw * geo.bh;
+  DF yy{0, 0}, yx{0, 0}, xx{0, 0}, yb{0, 0}, bb{0, 0};
+  float ayx = 0.0f, ayb = 0.0f;
+  for (size_t i = threadIdx.x; i < nb; i += kLfThreads) {
+    float y = a.lfs[nb + i], x = a.lfs[i], b = a.lfs[2 * nb + i];
+    yy = df_add(yy, df_two_prod(y, y));
+    yx = df_add(yx, df_two_prod(y, x));
+    xx = df_add(xx, df_two_prod(x, x));
+    yb = df_add(yb, df_two_prod(y, b));
+    bb = df_add(bb, df_two_prod(b, b));
+    ayx += fabsf(y * x);
+    ayb += fabsf(y * b);
+  }
+  double t[7];
+  t[0] = block_sum_df<kLfThreads>(yy, sd);
+  t[1] = block_sum_df<kLfThreads>(yx, sd);
+  t[2] = block_sum_df<kLfThreads>(xx, sd);
+  t[3] = block_sum_df<kLfThreads>(yb, sd);
+  t[4] = block_sum_df<kLfThreads>(bb, sd);
+  t[5] = block_sum_df<kLfThreads>(DF{ayx, 0.0f}, sd);
+  t[6] = block_sum_df<kLfThreads>(DF{ayb, 0.0f}, sd);
+  if (threadIdx.x != 0) return;
+  const double n = (double)nb;
+  const double gam = 2.0 * (n + 64.0) * (2.2737367544323206e-13 + 1.1102230246251565e-16);
   bool rx, rb;
   RegSums sx{t[0], t[1], t[2], t[5], n}, sb{t[0], t[3], t[4], t[6], n};
   int seed_x = best_factor(sx, 0.0f, gam * t[0], gam * t[5], gam * t[2], &rx);
   int seed_b = best_factor(sb, 1.0f, gam * t[0], gam * t[6], gam * t[4], &rb);
   if (!rx || !rb) {
     atomicAdd(a.cfl_fallbacks, 1u);
-    const size_t nb = (size_t)geo.bw * geo.bh;
     RegSums qx{0, 0, 0, 0, n}, qb{0, 0, 0, 0, n};
     const int G = 256;
     const int gw = (geo.bw + G - 1) / G, gh = (geo.bh + G - 1) / G;
@@ -769,99 +878,65 @@ __global__ void k_cfl_lf_seed(EncArgs a, const double* partial, int nparts, int*
     seed_x = best_factor(qx, 0.0f, 0, 0, 0, &r);
     seed_b = best_factor(qb, 1.0f, 0, 0, 0, &r);
   }
-  cand[0] = seed_x;
-  cand[1] = seed_b;
+  seeds[0] = seed_x;
+  seeds[1] = seed_b;
 }
 
-// Pass 3: residual bits of every candidate, per-CTA partials.
-__global__ void __launch_bounds__(kLfThreads) k_cfl_lf_costs(EncArgs a, const int* seeds,
-                                                             unsigned long long* partial) {
+__global__ void __launch_bounds__(kLfThreads) k_cfl_lf_pick(EncArgs a, const int* seeds) {
   __shared__ unsigned long long su[kLfThreads / 32];
   const Geo& geo = a.geo;
-  const size_t nb = (size_t)geo.bw * geo.bh;
-  int cand[2][4];
-  int ncand[2];
-  for (int ch = 0; ch < 2; ++ch) {
-    int seed = seeds[ch], nc = 0;
-    for (int d = -1; d <= 1; ++d) {
-      int v = min(max(seed + d, -128), 127);
-      bool dup = false;
-      for (int i = 0; i < nc; ++i) dup |= cand[ch][i] == v;
-      if (!dup) cand[ch][nc++] = v;
+  int* out = a.lf_factors;
+  if (*a.not_gray == 0u || !a.cfl_enabled) {
+    if (threadIdx.x == 0) {
+      out[0] = 0;
+      out[1] = 0;
     }
-    bool has0 = false;
-    for (int i = 0; i < nc; ++i) has0 |= cand[ch][i] == 0;
-    if (!has0) cand[ch][nc++] = 0;
-    ncand[ch] = nc;
+    return;
   }
-  unsigned long long bits[2][4] = {{0, 0, 0, 0}, {0, 0, 0, 0}};
+  const size_t nb = (size_t)geo.bw * geo.bh;
+  int cand[2][4], ncand[2];
+  lf_candidates(seeds[0], cand[0], &ncand[0]);
+  lf_candidates(seeds[1], cand[1], &ncand[1]);
+  uint32_t bits[2][4] = {{0, 0, 0, 0}, {0, 0, 0, 0}};
   float k[2][4];
+#pragma unroll
   for (int c = 0; c < 4; ++c) {
     k[0][c] = 0.0f + (float)cand[0][c < ncand[0] ? c : 0] / 84.0f;
     k[1][c] = 1.0f + (float)cand[1][c < ncand[1] ? c : 0] / 84.0f;
   }
-  for (size_t i = (size_t)blockIdx.x * kLfThreads + threadIdx.x; i < nb;
-       i += (size_t)gridDim.x * kLfThreads) {
+  for (size_t i = threadIdx.x; i < nb; i += kLfThreads) {
     float dy = a.dylf[i], x = a.lfs[i], b = a.lfs[2 * nb + i];
+#pragma unroll
     for (int c = 0; c < 4; ++c) {
       if (c < ncand[0]) bits[0][c] += residual_bits(lf_quantize(x - k[0][c] * dy, a.qs.m_dc[0], a.err));
       if (c < ncand[1]) bits[1][c] += residual_bits(lf_quantize(b - k[1][c] * dy, a.qs.m_dc[2], a.err));
     }
   }
+  unsigned long long cost[2][4];
+#pragma unroll
   for (int ch = 0; ch < 2; ++ch)
-    for (int c = 0; c < 4; ++c) {
-      unsigned long long t = block_sum_u64<kLfThreads>(bits[ch][c], su);
-      if (threadIdx.x == 0) partial[blockIdx.x * 8 + ch * 4 + c] = t;
-    }
-}
-
-// Pass 4 (one thread): lib.rs:3831 joint choice with the 50-bit bundle cost.
-__global__ void k_cfl_lf_pick(EncArgs a, const int* seeds, const unsigned long long* partial,
-                              int nparts) {
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
-  int* out = a.lf_factors;
-  if (*a.not_gray == 0u || !a.cfl_enabled) {
-    out[0] = 0;
-    out[1] = 0;
-    return;
-  }
-  int cand[2][4], ncand[2];
-  for (int ch = 0; ch < 2; ++ch) {
-    int seed = seeds[ch], nc = 0;
-    for (int d = -1; d <= 1; ++d) {
-      int v = min(max(seed + d, -128), 127);
-      bool dup = false;
-      for (int i = 0; i < nc; ++i) dup |= cand[ch][i] == v;
-      if (!dup) cand[ch][nc++] = v;
-    }
-    bool has0 = false;
-    for (int i = 0; i < nc; ++i) has0 |= cand[ch][i] == 0;
-    if (!has0) cand[ch][nc++] = 0;
-    ncand[ch] = nc;
-  }
-  unsigned long long cost[2][4] = {{0, 0, 0, 0}, {0, 0, 0, 0}};
-  for (int p = 0; p < nparts; ++p)
-    for (int ch = 0; ch < 2; ++ch)
-      for (int c = 0; c < 4; ++c) cost[ch][c] += partial[p * 8 + ch * 4 + c];
+#pragma unroll
+    for (int c = 0; c < 4; ++c) cost[ch][c] = block_sum_u64<kLfThreads>(bits[ch][c], su);
+  if (threadIdx.x != 0) return;
   unsigned long long nx = 0, nbb = 0;
   for (int c = 0; c < ncand[0]; ++c) if (cand[0][c] == 0) { nx = cost[0][c]; break; }
   for (int c = 0; c < ncand[1]; ++c) if (cand[1][c] == 0) { nbb = cost[1][c]; break; }
-  int bx = 0, bb = 0;
+  int bx = 0, bbf = 0;
   unsigned long long best = nx + nbb;
   for (int i = 0; i < ncand[0]; ++i)
     for (int j = 0; j < ncand[1]; ++j) {
       int fx = cand[0][i], fb = cand[1][j];
       unsigned long long c = cost[0][i] + cost[1][j];
       if (fx != 0 || fb != 0) c += 50ull + factor_bits(fx) + factor_bits(fb);
-      int mag = abs(fx) + abs(fb), bmag = abs(bx) + abs(bb);
+      int mag = abs(fx) + abs(fb), bmag = abs(bx) + abs(bbf);
       if (c < best || (c == best && mag < bmag)) {
         bx = fx;
-        bb = fb;
+        bbf = fb;
         best = c;
       }
     }
   out[0] = bx;
-  out[1] = bb;
+  out[1] = bbf;
 }
 
 // ---------------------------------------------------------------------------
@@ -929,15 +1004,12 @@ int launch_fdct_luma(const EncArgs& a, const uint32_t* const* lists, const int* 
   return k;
 }
 
-int launch_cfl(const EncArgs& a, double* lf_part, unsigned long long* lf_cost_part, int* lf_seeds,
-               int nparts, cudaStream_t s) {
+int launch_cfl(const EncArgs& a, int* lf_seeds, cudaStream_t s) {
   dim3 tiles(a.geo.tw, a.geo.th);
   k_cfl_tiles<<<tiles, kCflThreads, 0, s>>>(a);
-  k_cfl_lf_sums<<<nparts, kLfThreads, 0, s>>>(a, lf_part);
-  k_cfl_lf_seed<<<1, 32, 0, s>>>(a, lf_part, nparts, lf_seeds);
-  k_cfl_lf_costs<<<nparts, kLfThreads, 0, s>>>(a, lf_seeds, lf_cost_part);
-  k_cfl_lf_pick<<<1, 32, 0, s>>>(a, lf_seeds, lf_cost_part, nparts);
-  return 5;
+  k_cfl_lf_seed<<<1, kLfThreads, 0, s>>>(a, lf_seeds);
+  k_cfl_lf_pick<<<1, kLfThreads, 0, s>>>(a, lf_seeds);
+  return 3;
 }
 
 int launch_quant_chroma(const EncArgs& a, const uint32_t* const* lists, const int* counts,

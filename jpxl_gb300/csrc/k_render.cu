@@ -389,6 +389,28 @@ __device__ __forceinline__ int level_of(float x, const float* thr, int n) {
   return lo;
 }
 
+// For deep outputs (65535 thresholds in global memory) the level is first
+// estimated from the transfer curve with CUDA's powf and then confirmed
+// against the exact thresholds (two loads), stepping by one where the
+// estimate sits on the wrong side; the binary search remains the fallback.
+// The thresholds decide, so the result is exactly the bisected level.
+__device__ __forceinline__ int level_guided(float x, const float* __restrict__ thr, int n,
+                                            float maxv) {
+  if (!isfinite(x)) return 0;
+  float a = fabsf(x);
+  float e = a <= 0.0031308f ? 12.92f * a : 1.055f * powf(a, 1.0f / 2.4f) - 0.055f;
+  float s = rintf((x < 0.0f ? -e : e) * maxv);
+  int est = (int)fminf(fmaxf(s, 0.0f), maxv);
+#pragma unroll 1
+  for (int it = 0; it < 4; ++it) {
+    bool lo_ok = est == 0 || __ldg(&thr[est - 1]) <= x;
+    bool hi_ok = est == n || x < __ldg(&thr[est]);
+    if (lo_ok && hi_ok) return est;
+    est += lo_ok ? 1 : -1;
+  }
+  return level_of(x, thr, n);
+}
+
 template <int KIND>
 __global__ void __launch_bounds__(256) k_colour_out(const float* __restrict__ xyb, size_t n,
                                                     const float* __restrict__ thr,
@@ -431,11 +453,17 @@ __global__ void __launch_bounds__(256) k_colour_out(const float* __restrict__ xy
       o[3 * i] = (uint8_t)level_of(rgb[0], T, nlev - 1);
       o[3 * i + 1] = (uint8_t)level_of(rgb[1], T, nlev - 1);
       o[3 * i + 2] = (uint8_t)level_of(rgb[2], T, nlev - 1);
-    } else {
+    } else if (nlev <= 256) {
       float* o = (float*)out;
       o[i] = LV[level_of(rgb[0], T, nlev - 1)];
       o[n + i] = LV[level_of(rgb[1], T, nlev - 1)];
       o[2 * n + i] = LV[level_of(rgb[2], T, nlev - 1)];
+    } else {
+      float* o = (float*)out;
+      const float maxv = (float)(nlev - 1);
+      o[i] = __ldg(&LV[level_guided(rgb[0], T, nlev - 1, maxv)]);
+      o[n + i] = __ldg(&LV[level_guided(rgb[1], T, nlev - 1, maxv)]);
+      o[2 * n + i] = __ldg(&LV[level_guided(rgb[2], T, nlev - 1, maxv)]);
     }
   }
 }

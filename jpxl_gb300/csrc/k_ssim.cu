@@ -26,14 +26,21 @@ namespace jpxlg {
 
 __constant__ float c_taps[5];
 
+// The 9-tap FIR on nine values in registers, outer pairs first.
+__device__ __forceinline__ float fir9v(float m4, float m3, float m2, float m1, float c0, float p1,
+                                       float p2, float p3, float p4) {
+  float acc = c_taps[4] * (m4 + p4);
+  acc = __fmaf_rn(c_taps[3], m3 + p3, acc);
+  acc = __fmaf_rn(c_taps[2], m2 + p2, acc);
+  acc = __fmaf_rn(c_taps[1], m1 + p1, acc);
+  acc = __fmaf_rn(c_taps[0], c0, acc);
+  return acc;
+}
+
 __device__ __forceinline__ float fir9(const float* p, int stride) {
   // p points at the centre sample; taps symmetric.
-  float acc = c_taps[4] * (p[-4 * stride] + p[4 * stride]);
-  acc = __fmaf_rn(c_taps[3], p[-3 * stride] + p[3 * stride], acc);
-  acc = __fmaf_rn(c_taps[2], p[-2 * stride] + p[2 * stride], acc);
-  acc = __fmaf_rn(c_taps[1], p[-stride] + p[stride], acc);
-  acc = __fmaf_rn(c_taps[0], p[0], acc);
-  return acc;
+  return fir9v(p[-4 * stride], p[-3 * stride], p[-2 * stride], p[-stride], p[0], p[stride],
+               p[2 * stride], p[3 * stride], p[4 * stride]);
 }
 
 // S1
@@ -165,6 +172,12 @@ constexpr int kSH = 4;
 constexpr int kSS = kST + 2 * kSH;  // 40
 constexpr int kScoreThreads = 256;
 
+// Persistent: CTA b scores tiles b, b + gridDim.x, ...  Per tile, each
+// thread sums its pixels' terms in f32, each warp folds its lanes in f32
+// (butterfly, so every lane holds the warp's totals) and lane k adds total k
+// into an f64 accumulator; the CTA writes its 18 f64 sums in warp order.
+// With the grid fixed by the device's SM count, the summation order is
+// fixed.
 __global__ void __launch_bounds__(kScoreThreads) k_score_tile(const float* __restrict__ cand,
                                                               const float* __restrict__ rxyb,
                                                               const float* __restrict__ rmu,
@@ -176,7 +189,12 @@ __global__ void __launch_bounds__(kScoreThreads) k_score_tile(const float* __res
   __shared__ float hp[3][kSS][kST + 1];
   __shared__ double red[kScoreThreads / 32][18];
   const size_t n = (size_t)w * h;
-  const int x0 = blockIdx.x * kST - kSH, y0 = blockIdx.y * kST - kSH;
+  const int tiles_x = (w + kST - 1) / kST, tiles_y = (h + kST - 1) / kST;
+  const int lane = threadIdx.x % 32, warp = threadIdx.x / 32;
+  double acc64 = 0.0;  // lane k < 18 owns term k
+  for (int tile = blockIdx.x; tile < tiles_x * tiles_y; tile += gridDim.x) {
+  const int x0 = (tile % tiles_x) * kST - kSH, y0 = (tile / tiles_x) * kST - kSH;
+  __syncthreads();
   for (int i = threadIdx.x; i < kSS * kSS; i += kScoreThreads) {
     int lx = i % kSS, ly = i / kSS;
     int gx = x0 + lx, gy = y0 + ly;
@@ -193,6 +211,7 @@ __global__ void __launch_bounds__(kScoreThreads) k_score_tile(const float* __res
 #pragma unroll
   for (int k = 0; k < 18; ++k) sums[k] = 0.0f;
   const float C2 = 0.0009f;
+#pragma unroll
   for (int c = 0; c < 3; ++c) {
     __syncthreads();
     for (int i = threadIdx.x; i < kSS * kSS; i += kScoreThreads) {
@@ -201,24 +220,22 @@ __global__ void __launch_bounds__(kScoreThreads) k_score_tile(const float* __res
       rx[ly][lx] = (gx >= 0 && gy >= 0 && gx < w && gy < h) ? rxyb[n * c + (size_t)gy * w + gx] : 0.0f;
     }
     __syncthreads();
-    // horizontal: rows 0..39, output columns 0..31
-    for (int i = threadIdx.x; i < kSS * kST; i += kScoreThreads) {
-      int ox = i % kST, ly = i / kST;
-      const float* pc = &cx[c][ly][ox + kSH];
-      const float* pr = &rx[ly][ox + kSH];
-      float q[9], pp[9];
-#pragma unroll
-      for (int t = 0; t < 9; ++t) {
-        q[t] = pc[t - 4] * pc[t - 4];
-        pp[t] = pr[t - 4] * pc[t - 4];
-      }
-      hp[0][ly][ox] = fir9(pc, 1);
-      hp[1][ly][ox] = fir9(&q[4], 1);
-      hp[2][ly][ox] = fir9(&pp[4], 1);
+    // horizontal: rows 0..39, output columns 0..31 (lane = column)
+    for (int ly = warp; ly < kSS; ly += kScoreThreads / 32) {
+      const int ox = lane;
+      const float* pc = &cx[c][ly][ox];
+      const float* pr = &rx[ly][ox];
+      float c0 = pc[0], c1 = pc[1], c2 = pc[2], c3 = pc[3], c4 = pc[4], c5 = pc[5], c6 = pc[6],
+            c7 = pc[7], c8 = pc[8];
+      hp[0][ly][ox] = fir9v(c0, c1, c2, c3, c4, c5, c6, c7, c8);
+      hp[1][ly][ox] = fir9v(c0 * c0, c1 * c1, c2 * c2, c3 * c3, c4 * c4, c5 * c5, c6 * c6,
+                            c7 * c7, c8 * c8);
+      hp[2][ly][ox] = fir9v(pr[0] * c0, pr[1] * c1, pr[2] * c2, pr[3] * c3, pr[4] * c4,
+                            pr[5] * c5, pr[6] * c6, pr[7] * c7, pr[8] * c8);
     }
     __syncthreads();
-    for (int i = threadIdx.x; i < kST * kST; i += kScoreThreads) {
-      int ox = i % kST, oy = i / kST;
+    for (int oy = warp; oy < kST; oy += kScoreThreads / 32) {
+      const int ox = lane;
       int gx = x0 + kSH + ox, gy = y0 + kSH + oy;
       if (gx >= w || gy >= h) continue;
       float m2 = fir9(&hp[0][oy + kSH][ox], kST + 1);
@@ -248,28 +265,31 @@ __global__ void __launch_bounds__(kScoreThreads) k_score_tile(const float* __res
       sums[c * 6 + 5] += lost2 * lost2;
     }
   }
-  // fixed-order reduction: warp shuffles, then warps in order
-  const int wid = threadIdx.x / 32, lane = threadIdx.x % 32;
+  // warp fold in f32 (butterfly: all lanes receive the totals)
 #pragma unroll
   for (int k = 0; k < 18; ++k) {
-    double v = (double)sums[k];
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-    if (lane == 0) red[wid][k] = v;
+    float v = sums[k];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if (lane == k) acc64 += (double)v;
   }
+  }  // tiles
+  if (lane < 18) red[warp][lane] = acc64;
   __syncthreads();
   if (threadIdx.x < 18) {
     double t = 0.0;
     for (int i = 0; i < kScoreThreads / 32; ++i) t += red[i][threadIdx.x];
-    partial[(size_t)(blockIdx.y * gridDim.x + blockIdx.x) * 18 + threadIdx.x] = t;
+    partial[(size_t)blockIdx.x * 18 + threadIdx.x] = t;
   }
 }
 
 int launch_score_scale(const float* cand_rgb, const SsimScale& ref, double* partial,
-                       cudaStream_t s) {
-  dim3 grid((ref.w + kST - 1) / kST, (ref.h + kST - 1) / kST);
+                       int num_sms, cudaStream_t s) {
+  const int tiles = ((ref.w + kST - 1) / kST) * ((ref.h + kST - 1) / kST);
+  const int grid = std::max(1, std::min(tiles, num_sms * 4));
   k_score_tile<<<grid, kScoreThreads, 0, s>>>(cand_rgb, ref.xyb, ref.mu, ref.s11, ref.w, ref.h,
                                               partial);
-  return (int)(grid.x * grid.y);
+  return grid;
 }
 
 // S5 — ssimulacra2.rs:391 WEIGHTS (the metric's data table), :509
@@ -299,17 +319,40 @@ struct FinishArgs {
   long long pixels[6];
 };
 
-__global__ void k_score_finish(const double* __restrict__ partials, FinishArgs fa,
-                               double* __restrict__ out) {
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
-  double terms[6][3][6];
+constexpr int kFinishThreads = 256;
+
+__global__ void __launch_bounds__(kFinishThreads) k_score_finish(const double* __restrict__ partials,
+                                                                 FinishArgs fa,
+                                                                 double* __restrict__ out) {
+  // Per scale, thread t sums CTAs t, t+256, ... in order; the 256 partial
+  // sums are then folded pairwise in a fixed tree.  Deterministic.
+  __shared__ double tree[kFinishThreads][18];
+  __shared__ double scale_sums[6][18];
   size_t base = 0;
   for (int s = 0; s < fa.nscales; ++s) {
-    double sum[18];
-    for (int k = 0; k < 18; ++k) sum[k] = 0.0;
-    for (int i = 0; i < fa.ctas[s]; ++i)
-      for (int k = 0; k < 18; ++k) sum[k] += partials[(base + i) * 18 + k];
+    double acc[18];
+#pragma unroll
+    for (int k = 0; k < 18; ++k) acc[k] = 0.0;
+    for (int i = threadIdx.x; i < fa.ctas[s]; i += kFinishThreads)
+#pragma unroll
+      for (int k = 0; k < 18; ++k) acc[k] += partials[(base + i) * 18 + k];
+#pragma unroll
+    for (int k = 0; k < 18; ++k) tree[threadIdx.x][k] = acc[k];
+    __syncthreads();
+    for (int half = kFinishThreads / 2; half > 0; half >>= 1) {
+      if (threadIdx.x < half)
+#pragma unroll
+        for (int k = 0; k < 18; ++k) tree[threadIdx.x][k] += tree[threadIdx.x + half][k];
+      __syncthreads();
+    }
+    if (threadIdx.x < 18) scale_sums[s][threadIdx.x] = tree[0][threadIdx.x];
+    __syncthreads();
     base += fa.ctas[s];
+  }
+  if (threadIdx.x != 0) return;
+  double terms[6][3][6];
+  for (int s = 0; s < fa.nscales; ++s) {
+    const double* sum = scale_sums[s];
     double inv = 1.0 / (double)(fa.pixels[s] > 0 ? fa.pixels[s] : 1);
     for (int c = 0; c < 3; ++c) {
       const double* q = &sum[c * 6];
@@ -350,7 +393,7 @@ void launch_score_finish(const double* partials, const int* ctas_per_scale, int 
     fa.ctas[i] = i < nscales ? ctas_per_scale[i] : 0;
     fa.pixels[i] = i < nscales ? pixels_per_scale[i] : 0;
   }
-  k_score_finish<<<1, 32, 0, s>>>(partials, fa, out);
+  k_score_finish<<<1, kFinishThreads, 0, s>>>(partials, fa, out);
 }
 
 void upload_blur_taps(const float* taps, cudaStream_t s) {
