@@ -162,101 +162,124 @@ void launch_ref_moments(const float* xyb, float* mu, float* s11, float* tmp, int
   }
 }
 
-// S4 — candidate side of one scale, fused.  A CTA owns a 32x32 output tile;
-// it converts the candidate's linear RGB to positive XYB over the tile plus a
-// 4-sample halo (zero outside the frame: the blur's zero padding), runs the
-// horizontal then vertical FIR of c, c*c and r*c for each channel in shared
-// memory, and pools pool.rs:248's per-pixel terms.
+// S4 — candidate side of one scale, fused.  One CTA per 32x32 output tile:
+// the candidate's linear RGB becomes positive XYB over the tile plus a
+// 4-sample halo (zero outside the frame: the blur's zero padding), the
+// horizontal then vertical FIR of c, c*c and r*c run per channel in shared
+// memory, and pool.rs:248's per-pixel terms are pooled.  Every global load a
+// phase needs is issued before any of them is used, so a CTA's latency
+// chain is a handful of round trips; per-thread sums are f32, folded per
+// warp in f32 and across warps in f64 into one row of 18 sums per tile.
 constexpr int kST = 32;
 constexpr int kSH = 4;
 constexpr int kSS = kST + 2 * kSH;  // 40
+constexpr int kSP = kSS + 1;        // padded row
 constexpr int kScoreThreads = 256;
+constexpr int kScoreLoads = (kSS * kSS + kScoreThreads - 1) / kScoreThreads;  // 7
+constexpr size_t kScoreSmem = (6 * kSS * kSP + 3 * kSS * (kST + 1)) * sizeof(float);
 
-// Persistent: CTA b scores tiles b, b + gridDim.x, ...  Per tile, each
-// thread sums its pixels' terms in f32, each warp folds its lanes in f32
-// (butterfly, so every lane holds the warp's totals) and lane k adds total k
-// into an f64 accumulator; the CTA writes its 18 f64 sums in warp order.
-// With the grid fixed by the device's SM count, the summation order is
-// fixed.
-__global__ void __launch_bounds__(kScoreThreads) k_score_tile(const float* __restrict__ cand,
+__global__ void __launch_bounds__(kScoreThreads, 3) k_score_tile(const float* __restrict__ cand,
                                                               const float* __restrict__ rxyb,
                                                               const float* __restrict__ rmu,
                                                               const float* __restrict__ rs11,
                                                               int w, int h,
                                                               double* __restrict__ partial) {
-  __shared__ float cx[3][kSS][kSS + 1];
-  __shared__ float rx[kSS][kSS + 1];
-  __shared__ float hp[3][kSS][kST + 1];
+  extern __shared__ float ssm[];
+  float* cx = ssm;                      // [3][kSS][kSP]
+  float* rx = ssm + 3 * kSS * kSP;      // [3][kSS][kSP]
+  float* hp = ssm + 6 * kSS * kSP;      // [3][kSS][kST + 1]
   __shared__ double red[kScoreThreads / 32][18];
   const size_t n = (size_t)w * h;
-  const int tiles_x = (w + kST - 1) / kST, tiles_y = (h + kST - 1) / kST;
   const int lane = threadIdx.x % 32, warp = threadIdx.x / 32;
-  double acc64 = 0.0;  // lane k < 18 owns term k
-  for (int tile = blockIdx.x; tile < tiles_x * tiles_y; tile += gridDim.x) {
-  const int x0 = (tile % tiles_x) * kST - kSH, y0 = (tile / tiles_x) * kST - kSH;
-  __syncthreads();
-  for (int i = threadIdx.x; i < kSS * kSS; i += kScoreThreads) {
-    int lx = i % kSS, ly = i / kSS;
-    int gx = x0 + lx, gy = y0 + ly;
-    float o[3] = {0.0f, 0.0f, 0.0f};
-    if (gx >= 0 && gy >= 0 && gx < w && gy < h) {
-      size_t p = (size_t)gy * w + gx;
-      positive_xyb(cand[p], cand[n + p], cand[2 * n + p], o);
+  const int x0 = blockIdx.x * kST - kSH, y0 = blockIdx.y * kST - kSH;
+  // Phase 1: all candidate and reference samples of the haloed tile.
+  {
+    float v[kScoreLoads][6];
+#pragma unroll
+    for (int k = 0; k < kScoreLoads; ++k) {
+      const int i = threadIdx.x + k * kScoreThreads;
+      const int lx = i % kSS, ly = i / kSS;
+      const int gx = x0 + lx, gy = y0 + ly;
+      const bool ok = i < kSS * kSS && gx >= 0 && gy >= 0 && gx < w && gy < h;
+      const size_t p = ok ? (size_t)gy * w + gx : 0;
+#pragma unroll
+      for (int q = 0; q < 3; ++q) {
+        v[k][q] = ok ? cand[n * q + p] : 0.0f;
+        v[k][3 + q] = ok ? rxyb[n * q + p] : 0.0f;
+      }
     }
-    cx[0][ly][lx] = o[0];
-    cx[1][ly][lx] = o[1];
-    cx[2][ly][lx] = o[2];
+#pragma unroll
+    for (int k = 0; k < kScoreLoads; ++k) {
+      const int i = threadIdx.x + k * kScoreThreads;
+      if (i >= kSS * kSS) continue;
+      const int lx = i % kSS, ly = i / kSS;
+      const int gx = x0 + lx, gy = y0 + ly;
+      float o[3] = {0.0f, 0.0f, 0.0f};
+      if (gx >= 0 && gy >= 0 && gx < w && gy < h) positive_xyb(v[k][0], v[k][1], v[k][2], o);
+#pragma unroll
+      for (int q = 0; q < 3; ++q) {
+        cx[(q * kSS + ly) * kSP + lx] = o[q];
+        rx[(q * kSS + ly) * kSP + lx] = v[k][3 + q];
+      }
+    }
   }
   float sums[18];
 #pragma unroll
   for (int k = 0; k < 18; ++k) sums[k] = 0.0f;
   const float C2 = 0.0009f;
+  constexpr int kRowsPerWarp = kST / (kScoreThreads / 32);  // 4 output rows per warp
 #pragma unroll
   for (int c = 0; c < 3; ++c) {
-    __syncthreads();
-    for (int i = threadIdx.x; i < kSS * kSS; i += kScoreThreads) {
-      int lx = i % kSS, ly = i / kSS;
-      int gx = x0 + lx, gy = y0 + ly;
-      rx[ly][lx] = (gx >= 0 && gy >= 0 && gx < w && gy < h) ? rxyb[n * c + (size_t)gy * w + gx] : 0.0f;
+    // this thread's pooled pixels: rows warp + 8j, column lane
+    float m1[kRowsPerWarp], v11[kRowsPerWarp];
+#pragma unroll
+    for (int j = 0; j < kRowsPerWarp; ++j) {
+      const int gx = x0 + kSH + lane, gy = y0 + kSH + warp + 8 * j;
+      const bool ok = gx < w && gy < h;
+      const size_t p = n * c + (ok ? (size_t)gy * w + gx : 0);
+      m1[j] = ok ? rmu[p] : 0.0f;
+      v11[j] = ok ? rs11[p] : 0.0f;
     }
     __syncthreads();
+    const float* cc = cx + c * kSS * kSP;
+    const float* rr = rx + c * kSS * kSP;
     // horizontal: rows 0..39, output columns 0..31 (lane = column)
     for (int ly = warp; ly < kSS; ly += kScoreThreads / 32) {
-      const int ox = lane;
-      const float* pc = &cx[c][ly][ox];
-      const float* pr = &rx[ly][ox];
+      const float* pc = cc + ly * kSP + lane;
+      const float* pr = rr + ly * kSP + lane;
       float c0 = pc[0], c1 = pc[1], c2 = pc[2], c3 = pc[3], c4 = pc[4], c5 = pc[5], c6 = pc[6],
             c7 = pc[7], c8 = pc[8];
-      hp[0][ly][ox] = fir9v(c0, c1, c2, c3, c4, c5, c6, c7, c8);
-      hp[1][ly][ox] = fir9v(c0 * c0, c1 * c1, c2 * c2, c3 * c3, c4 * c4, c5 * c5, c6 * c6,
-                            c7 * c7, c8 * c8);
-      hp[2][ly][ox] = fir9v(pr[0] * c0, pr[1] * c1, pr[2] * c2, pr[3] * c3, pr[4] * c4,
-                            pr[5] * c5, pr[6] * c6, pr[7] * c7, pr[8] * c8);
+      hp[(0 * kSS + ly) * (kST + 1) + lane] = fir9v(c0, c1, c2, c3, c4, c5, c6, c7, c8);
+      hp[(1 * kSS + ly) * (kST + 1) + lane] =
+          fir9v(c0 * c0, c1 * c1, c2 * c2, c3 * c3, c4 * c4, c5 * c5, c6 * c6, c7 * c7, c8 * c8);
+      hp[(2 * kSS + ly) * (kST + 1) + lane] =
+          fir9v(pr[0] * c0, pr[1] * c1, pr[2] * c2, pr[3] * c3, pr[4] * c4, pr[5] * c5,
+                pr[6] * c6, pr[7] * c7, pr[8] * c8);
     }
     __syncthreads();
-    for (int oy = warp; oy < kST; oy += kScoreThreads / 32) {
-      const int ox = lane;
-      int gx = x0 + kSH + ox, gy = y0 + kSH + oy;
+#pragma unroll
+    for (int j = 0; j < kRowsPerWarp; ++j) {
+      const int oy = warp + 8 * j, ox = lane;
+      const int gx = x0 + kSH + ox, gy = y0 + kSH + oy;
       if (gx >= w || gy >= h) continue;
-      float m2 = fir9(&hp[0][oy + kSH][ox], kST + 1);
-      float s22 = fir9(&hp[1][oy + kSH][ox], kST + 1);
-      float s12 = fir9(&hp[2][oy + kSH][ox], kST + 1);
-      size_t p = n * c + (size_t)gy * w + gx;
-      float m1 = rmu[p], s11 = rs11[p];
-      float i1 = rx[oy + kSH][ox + kSH], i2 = cx[c][oy + kSH][ox + kSH];
-      float mu11 = m1 * m1, mu22 = m2 * m2, mu12 = m1 * m2;
-      float md = m1 - m2;
-      float num_m = 1.0f - md * md;
-      float num_s = 2.0f * (s12 - mu12) + C2;
-      float den_s = (s11 - mu11) + (s22 - mu22) + C2;
-      float d = fmaxf(1.0f - (num_m * num_s) / den_s, 0.0f);
-      float d2 = d * d;
+      const int r = (oy + kSH) * (kST + 1) + ox;
+      const float m2 = fir9(&hp[0 * kSS * (kST + 1) + r], kST + 1);
+      const float s22 = fir9(&hp[1 * kSS * (kST + 1) + r], kST + 1);
+      const float s12 = fir9(&hp[2 * kSS * (kST + 1) + r], kST + 1);
+      const float i1 = rr[(oy + kSH) * kSP + ox + kSH], i2 = cc[(oy + kSH) * kSP + ox + kSH];
+      const float mu11 = m1[j] * m1[j], mu22 = m2 * m2, mu12 = m1[j] * m2;
+      const float md = m1[j] - m2;
+      const float num_m = 1.0f - md * md;
+      const float num_s = 2.0f * (s12 - mu12) + C2;
+      const float den_s = (v11[j] - mu11) + (s22 - mu22) + C2;
+      const float d = fmaxf(1.0f - (num_m * num_s) / den_s, 0.0f);
+      const float d2 = d * d;
       // (1 + |i2-m2|) / (1 + |i1-m1|) - 1, written as a difference over the
       // denominator so that the result keeps its relative precision.
-      float a1 = fabsf(i1 - m1), a2 = fabsf(i2 - m2);
-      float d1 = (a2 - a1) / (1.0f + a1);
-      float art = fmaxf(d1, 0.0f), lost = fmaxf(-d1, 0.0f);
-      float art2 = art * art, lost2 = lost * lost;
+      const float a1 = fabsf(i1 - m1[j]), a2 = fabsf(i2 - m2);
+      const float d1 = (a2 - a1) / (1.0f + a1);
+      const float art = fmaxf(d1, 0.0f), lost = fmaxf(-d1, 0.0f);
+      const float art2 = art * art, lost2 = lost * lost;
       sums[c * 6 + 0] += d;
       sums[c * 6 + 1] += d2 * d2;
       sums[c * 6 + 2] += art;
@@ -265,31 +288,31 @@ __global__ void __launch_bounds__(kScoreThreads) k_score_tile(const float* __res
       sums[c * 6 + 5] += lost2 * lost2;
     }
   }
-  // warp fold in f32 (butterfly: all lanes receive the totals)
+  // warp fold in f32, then the 8 warps in order in f64
 #pragma unroll
   for (int k = 0; k < 18; ++k) {
     float v = sums[k];
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    if (lane == k) acc64 += (double)v;
+    if (lane == k) red[warp][k] = (double)v;
   }
-  }  // tiles
-  if (lane < 18) red[warp][lane] = acc64;
   __syncthreads();
   if (threadIdx.x < 18) {
     double t = 0.0;
     for (int i = 0; i < kScoreThreads / 32; ++i) t += red[i][threadIdx.x];
-    partial[(size_t)blockIdx.x * 18 + threadIdx.x] = t;
+    partial[(size_t)(blockIdx.y * gridDim.x + blockIdx.x) * 18 + threadIdx.x] = t;
   }
 }
 
 int launch_score_scale(const float* cand_rgb, const SsimScale& ref, double* partial,
                        int num_sms, cudaStream_t s) {
-  const int tiles = ((ref.w + kST - 1) / kST) * ((ref.h + kST - 1) / kST);
-  const int grid = std::max(1, std::min(tiles, num_sms * 4));
-  k_score_tile<<<grid, kScoreThreads, 0, s>>>(cand_rgb, ref.xyb, ref.mu, ref.s11, ref.w, ref.h,
-                                              partial);
-  return grid;
+  (void)num_sms;
+  cudaFuncSetAttribute(k_score_tile, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)kScoreSmem);
+  dim3 grid((ref.w + kST - 1) / kST, (ref.h + kST - 1) / kST);
+  k_score_tile<<<grid, kScoreThreads, kScoreSmem, s>>>(cand_rgb, ref.xyb, ref.mu, ref.s11, ref.w,
+                                                       ref.h, partial);
+  return (int)(grid.x * grid.y);
 }
 
 // S5 — ssimulacra2.rs:391 WEIGHTS (the metric's data table), :509
@@ -319,15 +342,18 @@ struct FinishArgs {
   long long pixels[6];
 };
 
-constexpr int kFinishThreads = 256;
+constexpr int kFinishThreads = 1024;
 
 __global__ void __launch_bounds__(kFinishThreads) k_score_finish(const double* __restrict__ partials,
                                                                  FinishArgs fa,
                                                                  double* __restrict__ out) {
-  // Per scale, thread t sums CTAs t, t+256, ... in order; the 256 partial
-  // sums are then folded pairwise in a fixed tree.  Deterministic.
-  __shared__ double tree[kFinishThreads][18];
+  // Per scale: thread t sums tile rows t, t+1024, ... in order; warps fold
+  // their lanes with shuffles (fixed tree); the 32 warp results are summed
+  // in warp order.  Deterministic for a given frame size.
+  __shared__ double wsum[kFinishThreads / 32][18];
   __shared__ double scale_sums[6][18];
+  __shared__ double terms[6][3][6];
+  const int lane = threadIdx.x % 32, warp = threadIdx.x / 32;
   size_t base = 0;
   for (int s = 0; s < fa.nscales; ++s) {
     double acc[18];
@@ -337,33 +363,35 @@ __global__ void __launch_bounds__(kFinishThreads) k_score_finish(const double* _
 #pragma unroll
       for (int k = 0; k < 18; ++k) acc[k] += partials[(base + i) * 18 + k];
 #pragma unroll
-    for (int k = 0; k < 18; ++k) tree[threadIdx.x][k] = acc[k];
-    __syncthreads();
-    for (int half = kFinishThreads / 2; half > 0; half >>= 1) {
-      if (threadIdx.x < half)
+    for (int k = 0; k < 18; ++k) {
+      double v = acc[k];
 #pragma unroll
-        for (int k = 0; k < 18; ++k) tree[threadIdx.x][k] += tree[threadIdx.x + half][k];
-      __syncthreads();
+      for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+      if (lane == 0) wsum[warp][k] = v;
     }
-    if (threadIdx.x < 18) scale_sums[s][threadIdx.x] = tree[0][threadIdx.x];
+    __syncthreads();
+    if (threadIdx.x < 18) {
+      double t = 0.0;
+      for (int i = 0; i < kFinishThreads / 32; ++i) t += wsum[i][threadIdx.x];
+      scale_sums[s][threadIdx.x] = t;
+    }
     __syncthreads();
     base += fa.ctas[s];
   }
-  if (threadIdx.x != 0) return;
-  double terms[6][3][6];
-  for (int s = 0; s < fa.nscales; ++s) {
-    const double* sum = scale_sums[s];
-    double inv = 1.0 / (double)(fa.pixels[s] > 0 ? fa.pixels[s] : 1);
-    for (int c = 0; c < 3; ++c) {
-      const double* q = &sum[c * 6];
-      terms[s][c][0] = inv * q[0];
-      terms[s][c][1] = inv * q[2];
-      terms[s][c][2] = inv * q[4];
-      terms[s][c][3] = sqrt(sqrt(inv * q[1]));
-      terms[s][c][4] = sqrt(sqrt(inv * q[3]));
-      terms[s][c][5] = sqrt(sqrt(inv * q[5]));
-    }
+  // pool.rs:60 norms, one (scale, channel) per thread.
+  if (threadIdx.x < fa.nscales * 3) {
+    const int s = threadIdx.x / 3, c = threadIdx.x % 3;
+    const double inv = 1.0 / (double)(fa.pixels[s] > 0 ? fa.pixels[s] : 1);
+    const double* q = &scale_sums[s][c * 6];
+    terms[s][c][0] = inv * q[0];
+    terms[s][c][1] = inv * q[2];
+    terms[s][c][2] = inv * q[4];
+    terms[s][c][3] = sqrt(sqrt(inv * q[1]));
+    terms[s][c][4] = sqrt(sqrt(inv * q[3]));
+    terms[s][c][5] = sqrt(sqrt(inv * q[5]));
   }
+  __syncthreads();
+  if (threadIdx.x != 0) return;
   double err = 0.0;
   int wi = 0;
   for (int c = 0; c < 3; ++c)
