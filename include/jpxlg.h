@@ -196,6 +196,22 @@ int jpxlg_probe(jpxlg_ctx* ctx, const jpxlg_layout* layout, const jpxlg_ref* ref
                 const void* rgb, int bits, const jpxlg_params* params, uint32_t mem,
                 double* score);
 
+/* Allocation-free variant of jpxlg_ssim2_score; it has no counterpart in the
+ * reference.  The candidate (device planes) is scored against `ref` using a
+ * fixed device scratch inside the library instead of the context's
+ * workspace, so the call never allocates or frees device memory: for callers
+ * that score between launches of their own and cannot take cudaFree's
+ * device-wide synchronisation, or that run beside a caching allocator which
+ * already holds the free device memory.  `out_dev` (device, 2 + 18 * scales
+ * doubles, at most 110) receives the score, the raw error and the terms.
+ * Work is queued on the context's stream and the call does not synchronize.
+ * Limits: reference frames up to 2048 x 2048 (larger ones return
+ * JPXLG_ERR_ARGUMENT); the first call on a device resolves the scratch
+ * address and should come before any stream capture; there is one scratch
+ * per device, so calls in flight at the same time on one device race. */
+int jpxlg_ssim2_score_static(jpxlg_ctx* ctx, const jpxlg_ref* ref,
+                             const float* linear_rgb_dev, double* out_dev);
+
 #ifdef __cplusplus
 }
 #endif

@@ -339,6 +339,14 @@ class Ssimulacra2:
                                                       terms.ctypes.data))
         return Ssimulacra2Result(sc.value, raw.value, terms)
 
+    def score_static_device(self, ref: PrecomputedReference, cand_ptr: int, out_ptr: int) -> None:
+        """Queue an allocation-free score of device planes at `cand_ptr`
+        ([3, H, W] float32) on the context's stream; `out_ptr` (device, 110
+        float64) receives [score, raw error, terms...].  Frames up to
+        2048 x 2048; calls in flight together on one device share scratch."""
+        self.ctx.check(self.ctx.lib.jpxlg_ssim2_score_static(
+            self.ctx.handle, ref.handle, C.c_void_p(cand_ptr), C.c_void_p(out_ptr)))
+
 
 def score_pair(ctx: Context, ref_rgb: np.ndarray, cand_rgb: np.ndarray) -> float:
     """jpxl-perceptual lib.rs:195 score_pair on linear [3, H, W] planes."""

@@ -38,6 +38,7 @@ SIGNATURES: dict[str, tuple] = {
     "jpxlg_ssim2_score": (_I, [_P, _P, _P, _U32, _P, _P, _P]),
     "jpxlg_score_pair": (_I, [_P, _P, _P, _I, _I, _U32, _P]),
     "jpxlg_probe": (_I, [_P, _P, _P, _P, _I, _P, _U32, _P]),
+    "jpxlg_ssim2_score_static": (_I, [_P, _P, _P, _P]),
 }
 
 

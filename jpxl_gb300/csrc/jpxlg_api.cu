@@ -7,6 +7,7 @@
 #include <cstring>
 #include <map>
 #include <memory>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -930,3 +931,99 @@ int jpxlg_probe(jpxlg_ctx* ctx, const jpxlg_layout* L, const jpxlg_ref* R, const
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Allocation-free scoring.  jpxlg_ssim2_score_static runs the same kernels as
+// jpxlg_ssim2_score but keeps the candidate pyramid and the per-tile partial
+// sums in one file-scope device array instead of the context's workspace, so
+// no call ever reaches cudaMalloc or cudaFree.
+//
+// Capacity: reference frames up to kStaticMaxSide x kStaticMaxSide.  The
+// pyramid of scales 1..5 of a 2048 x 2048 frame holds
+// 3 * (1024^2 + 512^2 + 256^2 + 128^2 + 64^2) = 4,190,208 floats, and its six
+// scales cover 64^2 + 32^2 + 16^2 + 8^2 + 4^2 + 2^2 = 5,460 tiles of 32 x 32,
+// each with 18 double sums: 17.5 MB in all.  Both counts grow with width and
+// height, so any frame within the side limit fits.
+//
+// Nothing in the scratch has to start at zero: each call writes every pyramid
+// level and every partial row before reading it.  There is one scratch per
+// device, so calls whose work overlaps on a device (two streams, two
+// contexts, or two host threads) race on it; callers serialise them.
+namespace {
+
+constexpr int kStaticMaxSide = 2048;
+constexpr size_t kStaticPyrFloats = 4190208;
+constexpr size_t kStaticPartialRows = 5460;
+constexpr size_t kStaticPyrBytes = kStaticPyrFloats * sizeof(float);  // a multiple of 256
+constexpr size_t kStaticScratchBytes = kStaticPyrBytes + kStaticPartialRows * 18 * sizeof(double);
+constexpr int kStaticMaxDevices = 64;
+
+static __device__ __align__(256) unsigned char g_score_scratch[kStaticScratchBytes];
+
+std::mutex g_scratch_mu;
+void* g_scratch_ptr[kStaticMaxDevices] = {};
+
+// Resolves the scratch address on the current device, once per device.  The
+// first resolution can load the module's device globals, so the first call
+// on a device should come before any stream capture that includes it.
+int static_scratch(jpxlg_ctx* ctx, unsigned char** out) {
+  if (ctx->device < 0 || ctx->device >= kStaticMaxDevices)
+    return fail(ctx, JPXLG_ERR_ARGUMENT, "device ordinal %d beyond %d", ctx->device,
+                kStaticMaxDevices);
+  std::lock_guard<std::mutex> lock(g_scratch_mu);
+  if (!g_scratch_ptr[ctx->device]) {
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_score_scratch);
+    if (e != cudaSuccess || !p)
+      return fail(ctx, JPXLG_ERR_CUDA, "static scratch address: %s", cudaGetErrorString(e));
+    g_scratch_ptr[ctx->device] = p;
+  }
+  *out = (unsigned char*)g_scratch_ptr[ctx->device];
+  return JPXLG_OK;
+}
+
+}  // namespace
+
+extern "C" int jpxlg_ssim2_score_static(jpxlg_ctx* ctx, const jpxlg_ref* ref,
+                                        const float* linear_rgb_dev, double* out_dev) {
+  if (!ctx || !ref || !linear_rgb_dev || !out_dev)
+    return fail(ctx, JPXLG_ERR_ARGUMENT, "null argument");
+  if (ref->w > kStaticMaxSide || ref->h > kStaticMaxSide)
+    return fail(ctx, JPXLG_ERR_ARGUMENT,
+                "%dx%d exceeds the static scoring scratch limit of %dx%d; use jpxlg_ssim2_score",
+                ref->w, ref->h, kStaticMaxSide, kStaticMaxSide);
+  CK(cudaSetDevice(ctx->device));
+  unsigned char* scratch = nullptr;
+  int rc = static_scratch(ctx, &scratch);
+  if (rc) return rc;
+  size_t pyr = 0, rows = 0;
+  for (int s = 0; s < ref->nscales; ++s) {
+    const SsimScale& rs = ref->scales[s];
+    if (s > 0) pyr += 3 * (size_t)rs.w * rs.h;
+    rows += (size_t)((rs.w + 31) / 32) * ((rs.h + 31) / 32);
+  }
+  if (pyr > kStaticPyrFloats || rows > kStaticPartialRows)
+    return fail(ctx, JPXLG_ERR_ARGUMENT, "static scoring scratch too small for %dx%d", ref->w,
+                ref->h);
+  float* next = (float*)scratch;
+  double* part0 = (double*)(scratch + kStaticPyrBytes);
+  double* part = part0;
+  const float* cur = linear_rgb_dev;
+  int ctas[6], pixels[6];
+  uint64_t k = 0;
+  for (int s = 0; s < ref->nscales; ++s) {
+    const SsimScale& rs = ref->scales[s];
+    if (s > 0) {
+      launch_downscale3(cur, ref->scales[s - 1].w, ref->scales[s - 1].h, next, ctx->stream);
+      ++k;
+      cur = next;
+      next += 3 * (size_t)rs.w * rs.h;
+    }
+    ctas[s] = launch_score_scale(cur, rs, part, ctx->num_sms, ctx->stream);
+    ++k;
+    pixels[s] = rs.w * rs.h;
+    part += (size_t)ctas[s] * 18;
+  }
+  launch_score_finish(part0, ctas, ref->nscales, pixels, out_dev, ctx->stream);
+  return after_launch(ctx, k + 1);
+}
