@@ -69,7 +69,7 @@ struct jpxlg_ctx {
   // workspace
   DevBuf rgb, xyb, pre, coeff, dyhf, qcoeff, lfs, dylf, lfq, cflx, cflb;
   DevBuf planes, aux, sigma, out;
-  DevBuf lf_part, lf_cost, lf_seed;
+  DevBuf lf_part, lf_seed;
   DevBuf pyr, partial, score;
   // stage timers
   struct Mark {
@@ -244,6 +244,7 @@ int encode_device(jpxlg_ctx* ctx, const jpxlg_layout* L, const void* rgb_dev, in
   CK(ctx->lfs.ensure(3 * nb * sizeof(float)));
   CK(ctx->dylf.ensure(nb * sizeof(float)));
   CK(ctx->lf_seed.ensure(4 * sizeof(int)));
+  CK(ctx->lf_part.ensure(kCflScratchBytes));
   const float* lut = get_lut(ctx, bits);
   if (!lut) return fail(ctx, JPXLG_ERR_CUDA, "transfer table allocation failed");
   CK(cudaMemsetAsync(ctx->d_words + 1, 0, sizeof(uint32_t), ctx->stream));
@@ -291,7 +292,7 @@ int encode_device(jpxlg_ctx* ctx, const jpxlg_layout* L, const void* rgb_dev, in
   stage_end(ctx);
   if (rc) return rc;
   stage_begin(ctx, JPXLG_STAGE_CFL);
-  rc = after_launch(ctx, launch_cfl(a, ctx->lf_seed.as<int>(), ctx->stream));
+  rc = after_launch(ctx, launch_cfl(a, ctx->lf_seed.as<int>(), ctx->lf_part.p, ctx->stream));
   stage_end(ctx);
   if (rc) return rc;
   stage_begin(ctx, JPXLG_STAGE_QUANT_CHROMA);
@@ -390,12 +391,12 @@ int score_device(jpxlg_ctx* ctx, const jpxlg_ref* ref, const float* cand_dev, do
   size_t ctas_total = 0;
   for (int s = 0; s < ref->nscales; ++s)
     ctas_total += (size_t)((ref->scales[s].w + 31) / 32) * ((ref->scales[s].h + 31) / 32);
-  CK(ctx->partial.ensure(ctas_total * 18 * sizeof(double)));
+  CK(ctx->partial.ensure(ctas_total * 18 * sizeof(DF)));
   int ctas[6], pixels[6];
   stage_begin(ctx, JPXLG_STAGE_SSIM);
   const float* cur = cand_dev;
   float* next = ctx->pyr.as<float>();
-  double* part = ctx->partial.as<double>();
+  DF* part = ctx->partial.as<DF>();
   uint64_t k = 0;
   for (int s = 0; s < ref->nscales; ++s) {
     const SsimScale& rs = ref->scales[s];
@@ -410,7 +411,7 @@ int score_device(jpxlg_ctx* ctx, const jpxlg_ref* ref, const float* cand_dev, do
     pixels[s] = rs.w * rs.h;
     part += (size_t)ctas[s] * 18;
   }
-  launch_score_finish(ctx->partial.as<double>(), ctas, ref->nscales, pixels, out_dev, ctx->stream);
+  launch_score_finish(ctx->partial.as<DF>(), ctas, ref->nscales, pixels, out_dev, ctx->stream);
   int rc = after_launch(ctx, k + 1);
   stage_end(ctx);
   return rc;
@@ -478,7 +479,7 @@ int jpxlg_ctx_destroy(jpxlg_ctx* ctx) {
   DevBuf* bufs[] = {&ctx->rgb,    &ctx->xyb,   &ctx->pre,     &ctx->coeff,   &ctx->dyhf,
                     &ctx->qcoeff, &ctx->lfs,   &ctx->dylf,    &ctx->lfq,     &ctx->cflx,
                     &ctx->cflb,   &ctx->planes, &ctx->aux,    &ctx->sigma,   &ctx->out,
-                    &ctx->lf_part, &ctx->lf_cost, &ctx->lf_seed, &ctx->pyr,  &ctx->partial,
+                    &ctx->lf_part, &ctx->lf_seed, &ctx->pyr,  &ctx->partial,
                     &ctx->score};
   for (DevBuf* b : bufs) b->release();
   for (auto& m : ctx->marks) {
@@ -942,8 +943,8 @@ int jpxlg_probe(jpxlg_ctx* ctx, const jpxlg_layout* L, const jpxlg_ref* R, const
 // pyramid of scales 1..5 of a 2048 x 2048 frame holds
 // 3 * (1024^2 + 512^2 + 256^2 + 128^2 + 64^2) = 4,190,208 floats, and its six
 // scales cover 64^2 + 32^2 + 16^2 + 8^2 + 4^2 + 2^2 = 5,460 tiles of 32 x 32,
-// each with 18 double sums: 17.5 MB in all.  Both counts grow with width and
-// height, so any frame within the side limit fits.
+// each with 18 double-float sums of 8 bytes: 17.5 MB in all.  Both counts
+// grow with width and height, so any frame within the side limit fits.
 //
 // Nothing in the scratch has to start at zero: each call writes every pyramid
 // level and every partial row before reading it.  There is one scratch per
@@ -955,7 +956,7 @@ constexpr int kStaticMaxSide = 2048;
 constexpr size_t kStaticPyrFloats = 4190208;
 constexpr size_t kStaticPartialRows = 5460;
 constexpr size_t kStaticPyrBytes = kStaticPyrFloats * sizeof(float);  // a multiple of 256
-constexpr size_t kStaticScratchBytes = kStaticPyrBytes + kStaticPartialRows * 18 * sizeof(double);
+constexpr size_t kStaticScratchBytes = kStaticPyrBytes + kStaticPartialRows * 18 * sizeof(DF);
 constexpr int kStaticMaxDevices = 64;
 
 static __device__ __align__(256) unsigned char g_score_scratch[kStaticScratchBytes];
@@ -1006,8 +1007,8 @@ extern "C" int jpxlg_ssim2_score_static(jpxlg_ctx* ctx, const jpxlg_ref* ref,
     return fail(ctx, JPXLG_ERR_ARGUMENT, "static scoring scratch too small for %dx%d", ref->w,
                 ref->h);
   float* next = (float*)scratch;
-  double* part0 = (double*)(scratch + kStaticPyrBytes);
-  double* part = part0;
+  DF* part0 = (DF*)(scratch + kStaticPyrBytes);
+  DF* part = part0;
   const float* cur = linear_rgb_dev;
   int ctas[6], pixels[6];
   uint64_t k = 0;

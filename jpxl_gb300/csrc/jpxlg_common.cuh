@@ -168,6 +168,56 @@ __device__ __forceinline__ float cbrt_perceptual(float v) {
   return cbrt_perceptual_f64(v);
 }
 
+// ---- double-float (f32 pair) sums --------------------------------------------
+// Products of two f32 are split exactly (two_prod); sums keep hi + lo to
+// about 2^-46 per addition, so a sum over n terms lies within
+// n * 2^-46 * sum|t| of the exact sum, at f32 issue rates (GB300's FP64
+// rate is a small fraction of its FP32 rate).  hi + lo converts to f64
+// exactly.
+struct DF {
+  float hi, lo;
+};
+__device__ __forceinline__ DF df_two_prod(float a, float b) {
+  float p = a * b;
+  return {p, __fmaf_rn(a, b, -p)};
+}
+__device__ __forceinline__ DF df_add(DF a, DF b) {
+  float s = a.hi + b.hi;
+  float bb = s - a.hi;
+  float e = (a.hi - (s - bb)) + (b.hi - bb);
+  e = e + (a.lo + b.lo);
+  float h = s + e;
+  return {h, e - (h - s)};
+}
+// Fixed-order butterfly over a warp; every lane ends with the same sum.
+__device__ __forceinline__ DF df_warp_sum(DF v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    DF w{__shfl_xor_sync(0xffffffffu, v.hi, o), __shfl_xor_sync(0xffffffffu, v.lo, o)};
+    v = df_add(v, w);
+  }
+  return v;
+}
+__device__ __forceinline__ double df_value(DF v) { return (double)v.hi + (double)v.lo; }
+
+// ---- reconstruct.rs:50 bias_adjust ------------------------------------------
+// q -> q * bias for |q| <= 1, else q - 0.145 / q.  The expression is odd in q
+// under round-to-nearest, so |q| < kBiasQuotN reads 0.145f / |q| from a table
+// that the host fills with the same IEEE division, and the sign is applied
+// last; larger |q| divide.
+constexpr int kBiasQuotN = 256;
+extern __device__ float g_bias_quot[kBiasQuotN];
+
+__device__ __forceinline__ float bias_adjust_q(int32_t q, float bias) {
+  const float f = (float)q;
+  if (q >= -1 && q <= 1) return f * bias;
+  const int32_t aq = q < 0 ? -q : q;
+  const float af = (float)aq;
+  const float t = aq < kBiasQuotN ? __ldg(&g_bias_quot[aq]) : 0.145f / af;
+  const float r = af - t;
+  return q < 0 ? -r : r;
+}
+
 // ---- DCT butterflies (jpxl-core dct.rs:235-465) -----------------------------
 // Orthonormal DCT-IV leaves live in constant memory (filled by the host from
 // the reference's first-row magnitudes); loops over them are unrolled, so

@@ -57,7 +57,10 @@ void launch_precondition(const float* in, float* out, int w, int h, cudaStream_t
 // Each returns the number of kernels it launched.
 int launch_fdct_luma(const EncArgs& a, const uint32_t* const* lists, const int* counts,
                      cudaStream_t s);
-int launch_cfl(const EncArgs& a, int* lf_seeds, cudaStream_t s);
+// LF CfL partials: kLfCtas CTAs, each 7 double-float sums and 8 bit counts.
+constexpr int kLfCtas = 128;
+constexpr size_t kCflScratchBytes = (size_t)kLfCtas * (7 * 8 + 8 * 4);
+int launch_cfl(const EncArgs& a, int* lf_seeds, void* lf_scratch, cudaStream_t s);
 int launch_quant_chroma(const EncArgs& a, const uint32_t* const* lists, const int* counts,
                         cudaStream_t s);
 
@@ -85,10 +88,11 @@ void launch_positive_xyb(const float* rgb, float* xyb, size_t n, int num_sms, cu
 void launch_ref_moments(const float* xyb, float* mu, float* s11, float* tmp, int w, int h,
                         cudaStream_t s);
 // Candidate side of one scale: cand is linear RGB [3][w*h]; partial receives
-// per-CTA f64 sums [ctas][18].
-int launch_score_scale(const float* cand_rgb, const SsimScale& ref, double* partial,
+// per-CTA double-float sums [ctas][18] (8 bytes each).
+struct DF;
+int launch_score_scale(const float* cand_rgb, const SsimScale& ref, DF* partial,
                        int num_sms, cudaStream_t s);
-void launch_score_finish(const double* partials, const int* ctas_per_scale, int nscales,
+void launch_score_finish(const DF* partials, const int* ctas_per_scale, int nscales,
                          const int* pixels_per_scale, double* out /* score, raw, terms[108] */,
                          cudaStream_t s);
 

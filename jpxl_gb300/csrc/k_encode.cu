@@ -129,8 +129,51 @@ __global__ void __launch_bounds__(kPreThreads) k_precondition(const float* __res
   const int groups = (w >= 3 && h >= 3) ? (w - 2) / 4 : 0;
   // Whether any cell of the tile lies outside the frame (block-uniform).
   const bool has_halo_out = gx0 < 0 || gy0 < 0 || gx0 + kPreS > w || gy0 + kPreS > h;
+  // Interior tiles: every updated cell (local 1..86 on both axes) is an
+  // interior pixel inside the SIMD groups and below the division tail, and
+  // no cell of the haloed tile lies outside the frame, so each step is one
+  // formula with no per-cell tests.  Other tiles take the general loop.
+  const bool fast = !has_halo_out && gx0 + kPreS - 2 <= 4 * groups &&
+                    (bulk == n || gy0 + kPreS - 2 < bulk_row);
   int cur = 0;
-  for (int it = 0; it < 12; ++it) {
+  if (fast) {
+    for (int it = 0; it < 12; ++it) {
+      const int lo = 1 + it, hi = kPreS - 1 - it;
+      const float* xs = cur ? X1 : X0;
+      float* xn = cur ? X0 : X1;
+      // Column chunks of 32 (lane = column); the warps sharing a chunk
+      // split its rows into bands.
+      const int wd = hi - lo;
+      const int nch = (wd + 31) >> 5;
+      const int chunk = warp % nch;
+      const int nb = (kWarps - chunk + nch - 1) / nch;
+      const int rows = (wd + nb - 1) / nb;
+      const int ly0 = lo + (warp / nch) * rows, ly1 = min(ly0 + rows, hi);
+      const int lx = lo + chunk * 32 + lane;
+      if (lx < hi && ly0 < ly1) {
+        const float* p = xs + (ly0 - 1) * kPreS + lx;
+        float nw = p[-1], nn = p[0], ne = p[1];
+        p += kPreS;
+        float ww = p[-1], mm = p[0], ee = p[1];
+        const float* f = F + ly0 * kPreS + lx;
+        float* o = xn + ly0 * kPreS + lx;
+        for (int ly = ly0; ly < ly1; ++ly) {
+          p += kPreS;
+          const float sw = p[-1], ss = p[0], se = p[1];
+          const float kx =
+              mm * k.centre + (nn + ss + ww + ee) * k.edge + (nw + ne + sw + se) * k.corner;
+          *o = mm + (*f - kx) * k.inv_c;
+          f += kPreS;
+          o += kPreS;
+          nw = ww; nn = mm; ne = ee;
+          ww = sw; mm = ss; ee = se;
+        }
+      }
+      __syncthreads();
+      cur ^= 1;
+    }
+  }
+  for (int it = 0; it < (fast ? 0 : 12); ++it) {
     const int r = kPreHalo - 1 - it;  // cells within r of the tile are updated
     const int lo = kPreHalo - r, hi = kPreHalo + kPreTile + r;  // local [lo, hi)
     const float* xs = cur ? X1 : X0;
@@ -237,18 +280,25 @@ __device__ __forceinline__ bool clamp_round(float v, int32_t* out) {
   return true;
 }
 
-// reconstruct.rs:50 bias_adjust.
-__device__ __forceinline__ float bias_adjust(int32_t q, float bias) {
-  float f = (float)q;
-  if (q >= -1 && q <= 1) return f * bias;
-  return f - 0.145f / f;
-}
+__device__ float g_bias_quot[kBiasQuotN];
+
+__device__ __forceinline__ float bias_adjust(int32_t q, float bias) { return bias_adjust_q(q, bias); }
 
 // quantize.rs:1400 HfQuantizer::choose (nearest reconstruction, ties to the
 // smaller magnitude) with step = scale * matrix and the zero threshold
 // 0.5 * bias * step, both formed as quantize.rs:334 forms them.
-__device__ __forceinline__ int32_t choose(float target, float step, float bias, uint32_t* err,
-                                          float* recon) {
+//
+// The reference centres its candidates {0, e-1, e, e+1} on
+// e = clamp_round(target / step).  The winner is always within one of
+// target / step (a reconstruction bias_adjust(q) * step lies within 0.08
+// steps of q * step), so a centre taken from target * (1 / step), which can
+// differ from e by one only next to a half-integer, yields a candidate set
+// holding the same winner, and the exact error comparison below picks it.
+// `rstep` is 1.0f / step, formed once per cell by the caller.  Quotients
+// near the 2^20 range limit, where the reference's error condition is
+// decided, take the exact division.
+__device__ __forceinline__ int32_t choose(float target, float step, float rstep, float bias,
+                                          uint32_t* err, float* recon) {
   if (!(isfinite(step) && step > 0.0f)) {
     raise_error(err, kDevBadStep);
     *recon = 0.0f;
@@ -260,7 +310,10 @@ __device__ __forceinline__ int32_t choose(float target, float step, float bias, 
     return 0;
   }
   int32_t e;
-  if (!clamp_round(target / step, &e)) {
+  const float va = target * rstep;
+  if (fabsf(va) < 1048000.0f) {
+    e = (int32_t)(signbit(va) ? va - 0.5f : va + 0.5f);
+  } else if (!clamp_round(target / step, &e)) {
     raise_error(err, kDevQuantRange);
     *recon = 0.0f;
     return 0;
@@ -421,7 +474,7 @@ __global__ void __launch_bounds__(128) k_fdct_luma(EncArgs a, const uint32_t* __
     if (k < n && j < n) {
       recon = bias_adjust(0, bias) * step;
     } else {
-      q = choose(ycoef[k], step, bias, a.err, &recon);
+      q = choose(ycoef[k], step, 1.0f / step, bias, a.err, &recon);
     }
     a.qcoeff[cplane + ci] = q;
     a.dyhf[ci] = recon;
@@ -511,73 +564,6 @@ __device__ __forceinline__ uint32_t factor_bits(int32_t f) {
   return (32u - __clz(af)) + 2u;
 }
 
-// Double-float (f32 pair) accumulation for the regression sums: products of
-// two f32 are split exactly (two_prod), sums keep hi+lo to ~2^-46 per
-// addition, so a sum over n terms lies within n*2^-46*sum|t| of the exact sum
-// at f32 issue rates (GB300's FP64 rate is 1/64 of its FP32 rate).
-struct DF {
-  float hi, lo;
-};
-__device__ __forceinline__ DF df_two_prod(float a, float b) {
-  float p = a * b;
-  return {p, __fmaf_rn(a, b, -p)};
-}
-__device__ __forceinline__ DF df_add(DF a, DF b) {
-  float s = a.hi + b.hi;
-  float bb = s - a.hi;
-  float e = (a.hi - (s - bb)) + (b.hi - bb);
-  e = e + (a.lo + b.lo);
-  float h = s + e;
-  return {h, e - (h - s)};
-}
-// Block sum of a DF in fixed order (warp butterfly, then warps in order);
-// returned as f64 in thread 0.
-template <int NT>
-__device__ double block_sum_df(DF v, double* scratch) {
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) {
-    DF w{__shfl_xor_sync(0xffffffffu, v.hi, o), __shfl_xor_sync(0xffffffffu, v.lo, o)};
-    v = df_add(v, w);
-  }
-  const int wid = threadIdx.x / 32, lane = threadIdx.x % 32;
-  __syncthreads();
-  if (lane == 0) scratch[wid] = (double)v.hi + (double)v.lo;
-  __syncthreads();
-  double t = 0.0;
-  if (threadIdx.x == 0)
-    for (int i = 0; i < NT / 32; ++i) t += scratch[i];
-  __syncthreads();
-  return t;
-}
-
-// Block-wide fixed-order sum of doubles (warp shuffles, then warp order).
-template <int NT>
-__device__ double block_sum(double v, double* scratch) {
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-  const int wid = threadIdx.x / 32, lane = threadIdx.x % 32;
-  __syncthreads();
-  if (lane == 0) scratch[wid] = v;
-  __syncthreads();
-  double t = 0.0;
-  if (threadIdx.x == 0)
-    for (int i = 0; i < NT / 32; ++i) t += scratch[i];
-  __syncthreads();
-  return t;  // valid in thread 0
-}
-template <int NT>
-__device__ unsigned long long block_sum_u64(unsigned long long v, unsigned long long* scratch) {
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-  const int wid = threadIdx.x / 32, lane = threadIdx.x % 32;
-  __syncthreads();
-  if (lane == 0) scratch[wid] = v;
-  __syncthreads();
-  unsigned long long t = 0;
-  if (threadIdx.x == 0)
-    for (int i = 0; i < NT / 32; ++i) t += scratch[i];
-  __syncthreads();
-  return t;
-}
-
 // The varblock containing block (bx, by) and whether coefficient-image cell
 // (px, py) is in its n x n LLF corner.  Square varblocks only (the encoder's
 // cover); origins are naturally aligned.
@@ -595,8 +581,9 @@ constexpr int kCflThreads = 256;
 // Per 64x64 tile: HF regression sums (X and B against source Y), the seed,
 // and the residual bit costs of the candidate window.  One CTA per tile.
 __global__ void __launch_bounds__(kCflThreads) k_cfl_tiles(EncArgs a) {
-  __shared__ double sd[kCflThreads / 32];
-  __shared__ unsigned long long su[kCflThreads / 32];
+  __shared__ double s_part[kCflThreads / 32][8];
+  __shared__ double s_tot[8];
+  __shared__ uint32_t s_bits[kCflThreads / 32][8];
   __shared__ int s_seed[2];
   __shared__ int s_robust[2];
   __shared__ int s_cands[2][4];
@@ -641,20 +628,40 @@ __global__ void __launch_bounds__(kCflThreads) k_cfl_tiles(EncArgs a) {
       }
     }
   }
-  double t_syy = block_sum_df<kCflThreads>(syy, sd);
-  double t_syx = block_sum_df<kCflThreads>(syx, sd);
-  double t_sxx = block_sum_df<kCflThreads>(sxx, sd);
-  double t_syb = block_sum_df<kCflThreads>(syb, sd);
-  double t_sbb = block_sum_df<kCflThreads>(sbb, sd);
-  double t_ayx = block_sum_df<kCflThreads>(DF{ayx, 0.0f}, sd);
-  double t_ayb = block_sum_df<kCflThreads>(DF{ayb, 0.0f}, sd);
-  double t_cnt = block_sum_df<kCflThreads>(DF{cnt, 0.0f}, sd);
-  if (threadIdx.x == 0) {
+  // One fixed-order reduction of all eight sums: a butterfly per warp, then
+  // the warps in order in f64 by eight threads of warp 0.
+  {
+    DF v[8] = {syy, syx, sxx, syb, sbb, DF{ayx, 0.0f}, DF{ayb, 0.0f}, DF{cnt, 0.0f}};
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        DF u{__shfl_xor_sync(0xffffffffu, v[q].hi, o), __shfl_xor_sync(0xffffffffu, v[q].lo, o)};
+        v[q] = df_add(v[q], u);
+      }
+    }
+    const int lane = threadIdx.x % 32, wid = threadIdx.x / 32;
+    if (lane == 0)
+#pragma unroll
+      for (int q = 0; q < 8; ++q) s_part[wid][q] = (double)v[q].hi + (double)v[q].lo;
+    __syncthreads();
+    if (threadIdx.x < 8) {
+      double t = 0.0;
+      for (int i = 0; i < kCflThreads / 32; ++i) t += s_part[i][threadIdx.x];
+      s_tot[threadIdx.x] = t;
+    }
+    __syncthreads();
+  }
+  const double t_syy = s_tot[0], t_syx = s_tot[1], t_sxx = s_tot[2], t_syb = s_tot[3],
+               t_sbb = s_tot[4], t_ayx = s_tot[5], t_ayb = s_tot[6], t_cnt = s_tot[7];
+  // Channel X in thread 0, B in thread 32 (separate warps, in parallel).
+  if (threadIdx.x % 32 == 0 && threadIdx.x < 64) {
     // Distance of the double-float tree sum and of the reference's
     // sequential f64 sum from the exact sum, relative to sum|t| (the |t|
     // sums above are f32 estimates; the factor 2 covers their error).
     const double gam = 2.0 * (t_cnt + 64.0) * (2.2737367544323206e-13 + 1.1102230246251565e-16);
-    for (int ch = 0; ch < 2; ++ch) {
+    {
+      const int ch = threadIdx.x / 32;
       RegSums s;
       s.s_yy = t_syy;
       s.s_yc = ch == 0 ? t_syx : t_syb;
@@ -744,24 +751,47 @@ __global__ void __launch_bounds__(kCflThreads) k_cfl_tiles(EncArgs a) {
         size_t ci = (size_t)py * geo.W8 + px;
         float dy = a.dyhf[ci];
         float x = a.coeff[ci], b = a.coeff[2 * cplane + ci];
-        float step_x = scale_x * __ldg(&m_x[cell8]);
-        float step_b = scale_b * __ldg(&m_b[cell8]);
+        const float step_x = scale_x * __ldg(&m_x[cell8]);
+        const float step_b = scale_b * __ldg(&m_b[cell8]);
+        const float rstep_x = 1.0f / step_x, rstep_b = 1.0f / step_b;
         float rc;
 #pragma unroll
         for (int c = 0; c < 4; ++c) {
           if (c < ncx)
-            bits[0][c] += residual_bits(choose(x - kx[c] * dy, step_x, c_quant_bias[0], a.err, &rc));
+            bits[0][c] += residual_bits(
+                choose(x - kx[c] * dy, step_x, rstep_x, c_quant_bias[0], a.err, &rc));
           if (c < ncb)
-            bits[1][c] += residual_bits(choose(b - kb[c] * dy, step_b, c_quant_bias[2], a.err, &rc));
+            bits[1][c] += residual_bits(
+                choose(b - kb[c] * dy, step_b, rstep_b, c_quant_bias[2], a.err, &rc));
         }
       }
     }
   }
-  unsigned long long tot[2][4];
-  for (int ch = 0; ch < 2; ++ch)
-    for (int c = 0; c < 4; ++c) tot[ch][c] = block_sum_u64<kCflThreads>(bits[ch][c], su);
-  if (threadIdx.x == 0) {
-    for (int ch = 0; ch < 2; ++ch) {
+  // Integer sums (exact in any order): butterflies, then warps in order.
+  // A tile holds at most 4096 cells of at most 22 bits, so 32 bits suffice.
+  {
+    uint32_t v[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      v[q] = (uint32_t)bits[q / 4][q % 4];
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) v[q] += __shfl_xor_sync(0xffffffffu, v[q], o);
+    }
+    const int lane = threadIdx.x % 32, wid = threadIdx.x / 32;
+    if (lane == 0)
+#pragma unroll
+      for (int q = 0; q < 8; ++q) s_bits[wid][q] = v[q];
+    __syncthreads();
+  }
+  if (threadIdx.x % 32 == 0 && threadIdx.x < 64) {
+    unsigned long long tot[2][4];
+    for (int q = 0; q < 8; ++q) {
+      unsigned long long t = 0;
+      for (int i = 0; i < kCflThreads / 32; ++i) t += s_bits[i][q];
+      tot[q / 4][q % 4] = t;
+    }
+    {
+      const int ch = threadIdx.x / 32;
       int result = 0;
       if (s_seed[ch] != 0) {
         // lib.rs:3966 refine_hf_factor: cost(0) first, then each non-zero
@@ -792,12 +822,14 @@ __global__ void __launch_bounds__(kCflThreads) k_cfl_tiles(EncArgs a) {
   }
 }
 
-// Frame-wide LF pair (lib.rs:3831 refine_lf_factors), in two single-CTA
-// kernels: the regression sums over every LF sample and the seeds (with the
+// Frame-wide LF pair (lib.rs:3831 refine_lf_factors) in four kernels: the
+// regression sums of every LF sample as per-CTA double-float partials across
+// the GPU; one CTA folding them in a fixed order into the two seeds (with the
 // sequential fallback in the reference's LF-group / band / varblock / cell
-// order when a seed is not robust); then the residual bit costs of both
-// candidate windows and the joint choice.
-constexpr int kLfThreads = 1024;
+// order when a seed is not robust); the residual bit costs of both candidate
+// windows as per-CTA partials; one CTA folding those and making the joint
+// choice.
+constexpr int kLfThreads = 256;
 
 __device__ void lf_candidates(int seed, int* c, int* nc_out) {
   int nc = 0;
@@ -813,38 +845,60 @@ __device__ void lf_candidates(int seed, int* c, int* nc_out) {
   *nc_out = nc;
 }
 
-__global__ void __launch_bounds__(kLfThreads) k_cfl_lf_seed(EncArgs a, int* seeds) {
-  __shared__ double sd[kLfThreads / 32];
+__device__ __forceinline__ bool cfl_off(const EncArgs& a) {
+  return *a.not_gray == 0u || !a.cfl_enabled;
+}
+
+// Partial sums per CTA: [kLfCtas][7] double-float (yy, yx, xx, yb, bb, |yx|, |yb|).
+__global__ void __launch_bounds__(kLfThreads) k_cfl_lf_sums(EncArgs a, DF* part) {
+  __shared__ DF s_w[kLfThreads / 32][7];
+  if (cfl_off(a)) return;
+  const size_t nb = (size_t)a.geo.bw * a.geo.bh;
+  DF v[7] = {};
+  for (size_t i = (size_t)blockIdx.x * kLfThreads + threadIdx.x; i < nb;
+       i += (size_t)kLfCtas * kLfThreads) {
+    const float y = a.lfs[nb + i], x = a.lfs[i], b = a.lfs[2 * nb + i];
+    v[0] = df_add(v[0], df_two_prod(y, y));
+    v[1] = df_add(v[1], df_two_prod(y, x));
+    v[2] = df_add(v[2], df_two_prod(x, x));
+    v[3] = df_add(v[3], df_two_prod(y, b));
+    v[4] = df_add(v[4], df_two_prod(b, b));
+    v[5].hi += fabsf(y * x);
+    v[6].hi += fabsf(y * b);
+  }
+  const int lane = threadIdx.x % 32, wid = threadIdx.x / 32;
+#pragma unroll
+  for (int q = 0; q < 7; ++q) {
+    DF t = df_warp_sum(v[q]);
+    if (lane == 0) s_w[wid][q] = t;
+  }
+  __syncthreads();
+  if (threadIdx.x < 7) {
+    DF t = s_w[0][threadIdx.x];
+    for (int i = 1; i < kLfThreads / 32; ++i) t = df_add(t, s_w[i][threadIdx.x]);
+    part[blockIdx.x * 7 + threadIdx.x] = t;
+  }
+}
+
+__global__ void __launch_bounds__(64) k_cfl_lf_seed(EncArgs a, const DF* part, int* seeds) {
+  __shared__ double s_t[7];
   const Geo& geo = a.geo;
-  if (*a.not_gray == 0u || !a.cfl_enabled) {
+  if (cfl_off(a)) {
     if (threadIdx.x == 0) {
       seeds[0] = 0;
       seeds[1] = 0;
     }
     return;
   }
-  const size_t nb = (size_t)geo.bw * geo.bh;
-  DF yy{0, 0}, yx{0, 0}, xx{0, 0}, yb{0, 0}, bb{0, 0};
-  float ayx = 0.0f, ayb = 0.0f;
-  for (size_t i = threadIdx.x; i < nb; i += kLfThreads) {
-    float y = a.lfs[nb + i], x = a.lfs[i], b = a.lfs[2 * nb + i];
-    yy = df_add(yy, df_two_prod(y, y));
-    yx = df_add(yx, df_two_prod(y, x));
-    xx = df_add(xx, df_two_prod(x, x));
-    yb = df_add(yb, df_two_prod(y, b));
-    bb = df_add(bb, df_two_prod(b, b));
-    ayx += fabsf(y * x);
-    ayb += fabsf(y * b);
+  if (threadIdx.x < 7) {
+    DF t = part[threadIdx.x];
+    for (int c = 1; c < kLfCtas; ++c) t = df_add(t, part[c * 7 + threadIdx.x]);
+    s_t[threadIdx.x] = df_value(t);
   }
-  double t[7];
-  t[0] = block_sum_df<kLfThreads>(yy, sd);
-  t[1] = block_sum_df<kLfThreads>(yx, sd);
-  t[2] = block_sum_df<kLfThreads>(xx, sd);
-  t[3] = block_sum_df<kLfThreads>(yb, sd);
-  t[4] = block_sum_df<kLfThreads>(bb, sd);
-  t[5] = block_sum_df<kLfThreads>(DF{ayx, 0.0f}, sd);
-  t[6] = block_sum_df<kLfThreads>(DF{ayb, 0.0f}, sd);
+  __syncthreads();
   if (threadIdx.x != 0) return;
+  const size_t nb = (size_t)geo.bw * geo.bh;
+  const double* t = s_t;
   const double n = (double)nb;
   const double gam = 2.0 * (n + 64.0) * (2.2737367544323206e-13 + 1.1102230246251565e-16);
   bool rx, rb;
@@ -882,51 +936,81 @@ __global__ void __launch_bounds__(kLfThreads) k_cfl_lf_seed(EncArgs a, int* seed
   seeds[1] = seed_b;
 }
 
-__global__ void __launch_bounds__(kLfThreads) k_cfl_lf_pick(EncArgs a, const int* seeds) {
-  __shared__ unsigned long long su[kLfThreads / 32];
-  const Geo& geo = a.geo;
-  int* out = a.lf_factors;
-  if (*a.not_gray == 0u || !a.cfl_enabled) {
-    if (threadIdx.x == 0) {
-      out[0] = 0;
-      out[1] = 0;
-    }
-    return;
-  }
-  const size_t nb = (size_t)geo.bw * geo.bh;
+// Residual bits of every candidate per CTA: [kLfCtas][8] (X candidates 0..3,
+// B candidates 0..3).  At most 2^16 * 22 bits per CTA fit in 32 bits for
+// frames up to 2^28 LF samples.
+__global__ void __launch_bounds__(kLfThreads) k_cfl_lf_bits(EncArgs a, const int* seeds,
+                                                            uint32_t* part) {
+  __shared__ uint32_t s_w[kLfThreads / 32][8];
+  if (cfl_off(a)) return;
+  const size_t nb = (size_t)a.geo.bw * a.geo.bh;
   int cand[2][4], ncand[2];
   lf_candidates(seeds[0], cand[0], &ncand[0]);
   lf_candidates(seeds[1], cand[1], &ncand[1]);
-  uint32_t bits[2][4] = {{0, 0, 0, 0}, {0, 0, 0, 0}};
+  uint32_t bits[8] = {};
   float k[2][4];
 #pragma unroll
   for (int c = 0; c < 4; ++c) {
     k[0][c] = 0.0f + (float)cand[0][c < ncand[0] ? c : 0] / 84.0f;
     k[1][c] = 1.0f + (float)cand[1][c < ncand[1] ? c : 0] / 84.0f;
   }
-  for (size_t i = threadIdx.x; i < nb; i += kLfThreads) {
-    float dy = a.dylf[i], x = a.lfs[i], b = a.lfs[2 * nb + i];
+  for (size_t i = (size_t)blockIdx.x * kLfThreads + threadIdx.x; i < nb;
+       i += (size_t)kLfCtas * kLfThreads) {
+    const float dy = a.dylf[i], x = a.lfs[i], b = a.lfs[2 * nb + i];
 #pragma unroll
     for (int c = 0; c < 4; ++c) {
-      if (c < ncand[0]) bits[0][c] += residual_bits(lf_quantize(x - k[0][c] * dy, a.qs.m_dc[0], a.err));
-      if (c < ncand[1]) bits[1][c] += residual_bits(lf_quantize(b - k[1][c] * dy, a.qs.m_dc[2], a.err));
+      if (c < ncand[0]) bits[c] += residual_bits(lf_quantize(x - k[0][c] * dy, a.qs.m_dc[0], a.err));
+      if (c < ncand[1]) bits[4 + c] += residual_bits(lf_quantize(b - k[1][c] * dy, a.qs.m_dc[2], a.err));
     }
   }
-  unsigned long long cost[2][4];
+  const int lane = threadIdx.x % 32, wid = threadIdx.x / 32;
 #pragma unroll
-  for (int ch = 0; ch < 2; ++ch)
+  for (int q = 0; q < 8; ++q) {
+    uint32_t t = bits[q];
 #pragma unroll
-    for (int c = 0; c < 4; ++c) cost[ch][c] = block_sum_u64<kLfThreads>(bits[ch][c], su);
+    for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+    if (lane == 0) s_w[wid][q] = t;
+  }
+  __syncthreads();
+  if (threadIdx.x < 8) {
+    uint32_t t = 0;
+    for (int i = 0; i < kLfThreads / 32; ++i) t += s_w[i][threadIdx.x];
+    part[blockIdx.x * 8 + threadIdx.x] = t;
+  }
+}
+
+__global__ void __launch_bounds__(32) k_cfl_lf_pick(EncArgs a, const int* seeds,
+                                                    const uint32_t* part) {
+  __shared__ unsigned long long s_cost[8];
+  int* out = a.lf_factors;
+  if (cfl_off(a)) {
+    if (threadIdx.x == 0) {
+      out[0] = 0;
+      out[1] = 0;
+    }
+    return;
+  }
+  if (threadIdx.x < 8) {
+    unsigned long long t = 0;
+    for (int c = 0; c < kLfCtas; ++c) t += part[c * 8 + threadIdx.x];
+    s_cost[threadIdx.x] = t;
+  }
+  __syncwarp();
   if (threadIdx.x != 0) return;
+  int cand[2][4], ncand[2];
+  lf_candidates(seeds[0], cand[0], &ncand[0]);
+  lf_candidates(seeds[1], cand[1], &ncand[1]);
+  const unsigned long long* cost0 = s_cost;
+  const unsigned long long* cost1 = s_cost + 4;
   unsigned long long nx = 0, nbb = 0;
-  for (int c = 0; c < ncand[0]; ++c) if (cand[0][c] == 0) { nx = cost[0][c]; break; }
-  for (int c = 0; c < ncand[1]; ++c) if (cand[1][c] == 0) { nbb = cost[1][c]; break; }
+  for (int c = 0; c < ncand[0]; ++c) if (cand[0][c] == 0) { nx = cost0[c]; break; }
+  for (int c = 0; c < ncand[1]; ++c) if (cand[1][c] == 0) { nbb = cost1[c]; break; }
   int bx = 0, bbf = 0;
   unsigned long long best = nx + nbb;
   for (int i = 0; i < ncand[0]; ++i)
     for (int j = 0; j < ncand[1]; ++j) {
       int fx = cand[0][i], fb = cand[1][j];
-      unsigned long long c = cost[0][i] + cost[1][j];
+      unsigned long long c = cost0[i] + cost1[j];
       if (fx != 0 || fb != 0) c += 50ull + factor_bits(fx) + factor_bits(fb);
       int mag = abs(fx) + abs(fb), bmag = abs(bx) + abs(bbf);
       if (c < best || (c == best && mag < bmag)) {
@@ -987,7 +1071,8 @@ __global__ void __launch_bounds__(128) k_quant_chroma(EncArgs a, const uint32_t*
       if (!(k < n && j < n)) {
         float target = a.coeff[cplane * c + ci] - k_hf[c] * a.dyhf[ci];
         float rc;
-        q = choose(target, scale * __ldg(&m[k * N + j]), bias, a.err, &rc);
+        const float step = scale * __ldg(&m[k * N + j]);
+        q = choose(target, step, 1.0f / step, bias, a.err, &rc);
       }
       a.qcoeff[cplane * c + ci] = q;
     }
@@ -1004,12 +1089,16 @@ int launch_fdct_luma(const EncArgs& a, const uint32_t* const* lists, const int* 
   return k;
 }
 
-int launch_cfl(const EncArgs& a, int* lf_seeds, cudaStream_t s) {
+int launch_cfl(const EncArgs& a, int* lf_seeds, void* lf_scratch, cudaStream_t s) {
   dim3 tiles(a.geo.tw, a.geo.th);
   k_cfl_tiles<<<tiles, kCflThreads, 0, s>>>(a);
-  k_cfl_lf_seed<<<1, kLfThreads, 0, s>>>(a, lf_seeds);
-  k_cfl_lf_pick<<<1, kLfThreads, 0, s>>>(a, lf_seeds);
-  return 3;
+  DF* sums = (DF*)lf_scratch;
+  uint32_t* bits = (uint32_t*)((char*)lf_scratch + kLfCtas * 7 * sizeof(DF));
+  k_cfl_lf_sums<<<kLfCtas, kLfThreads, 0, s>>>(a, sums);
+  k_cfl_lf_seed<<<1, 64, 0, s>>>(a, sums, lf_seeds);
+  k_cfl_lf_bits<<<kLfCtas, kLfThreads, 0, s>>>(a, lf_seeds, bits);
+  k_cfl_lf_pick<<<1, 32, 0, s>>>(a, lf_seeds, bits);
+  return 5;
 }
 
 int launch_quant_chroma(const EncArgs& a, const uint32_t* const* lists, const int* counts,
@@ -1027,6 +1116,11 @@ void upload_dct_constants(const float* iv4, const float* iv8, const float* iv16,
   cudaMemcpyToSymbolAsync(c_iv8, iv8, sizeof(float) * 64, 0, cudaMemcpyHostToDevice, s);
   cudaMemcpyToSymbolAsync(c_iv16, iv16, sizeof(float) * 256, 0, cudaMemcpyHostToDevice, s);
   cudaMemcpyToSymbolAsync(c_scale_f, scale_f, sizeof(float) * 12, 0, cudaMemcpyHostToDevice, s);
+  // 0.145f / q in IEEE single precision, as bias_adjust divides on the device.
+  static float quot[kBiasQuotN];
+  quot[0] = 0.0f;
+  for (int q = 1; q < kBiasQuotN; ++q) quot[q] = 0.145f / (float)q;
+  cudaMemcpyToSymbolAsync(g_bias_quot, quot, sizeof quot, 0, cudaMemcpyHostToDevice, s);
 }
 
 }  // namespace jpxlg

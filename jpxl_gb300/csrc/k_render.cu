@@ -22,12 +22,6 @@ __constant__ float c_opsin_m[9];
 __constant__ float c_opsin_bias[3];
 __constant__ float c_opsin_bias_cbrt[3];
 
-__device__ __forceinline__ float rbias_adjust(int32_t q, float bias) {
-  float f = (float)q;
-  if (q >= -1 && q <= 1) return f * bias;
-  return f - 0.145f / f;
-}
-
 template <int N>
 __device__ __forceinline__ void idct_n(float* v) {
   idct_1d<N>(v);
@@ -151,7 +145,7 @@ __global__ void __launch_bounds__(128) k_render_vb(RenderArgs a, const uint32_t*
         const int x = j;
         size_t pos = portrait ? (size_t)(y0 + x) * geo.W8 + x0 + y : (size_t)(y0 + y) * geo.W8 + x0 + x;
         int32_t q = a.qcoeff[cplane * c + pos];
-        float d = rbias_adjust(q, bias) * scale * __ldg(&m[y * CC + x]);
+        float d = bias_adjust_q(q, bias) * scale * __ldg(&m[y * CC + x]);
         if (c == 1) dY[y] = d;
         else d = d + (c == 0 ? kx : kb) * dY[y];  // lib.rs:1344 apply_hf_cfl
         if (y < LY && x < LX) d = LLF[g][c][y * LX + x];

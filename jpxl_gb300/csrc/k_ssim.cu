@@ -183,12 +183,12 @@ __global__ void __launch_bounds__(kScoreThreads, 3) k_score_tile(const float* __
                                                               const float* __restrict__ rmu,
                                                               const float* __restrict__ rs11,
                                                               int w, int h,
-                                                              double* __restrict__ partial) {
+                                                              DF* __restrict__ partial) {
   extern __shared__ float ssm[];
   float* cx = ssm;                      // [3][kSS][kSP]
   float* rx = ssm + 3 * kSS * kSP;      // [3][kSS][kSP]
   float* hp = ssm + 6 * kSS * kSP;      // [3][kSS][kST + 1]
-  __shared__ double red[kScoreThreads / 32][18];
+  __shared__ float red[kScoreThreads / 32][18];
   const size_t n = (size_t)w * h;
   const int lane = threadIdx.x % 32, warp = threadIdx.x / 32;
   const int x0 = blockIdx.x * kST - kSH, y0 = blockIdx.y * kST - kSH;
@@ -288,23 +288,23 @@ __global__ void __launch_bounds__(kScoreThreads, 3) k_score_tile(const float* __
       sums[c * 6 + 5] += lost2 * lost2;
     }
   }
-  // warp fold in f32, then the 8 warps in order in f64
+  // warp fold in f32, then the 8 warps in order in double-float
 #pragma unroll
   for (int k = 0; k < 18; ++k) {
     float v = sums[k];
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    if (lane == k) red[warp][k] = (double)v;
+    if (lane == k) red[warp][k] = v;
   }
   __syncthreads();
   if (threadIdx.x < 18) {
-    double t = 0.0;
-    for (int i = 0; i < kScoreThreads / 32; ++i) t += red[i][threadIdx.x];
+    DF t{red[0][threadIdx.x], 0.0f};
+    for (int i = 1; i < kScoreThreads / 32; ++i) t = df_add(t, DF{red[i][threadIdx.x], 0.0f});
     partial[(size_t)(blockIdx.y * gridDim.x + blockIdx.x) * 18 + threadIdx.x] = t;
   }
 }
 
-int launch_score_scale(const float* cand_rgb, const SsimScale& ref, double* partial,
+int launch_score_scale(const float* cand_rgb, const SsimScale& ref, DF* partial,
                        int num_sms, cudaStream_t s) {
   (void)num_sms;
   cudaFuncSetAttribute(k_score_tile, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -343,37 +343,32 @@ struct FinishArgs {
 };
 
 constexpr int kFinishThreads = 1024;
+constexpr int kFinishGroups = kFinishThreads / 18;  // 56 groups of 18 threads
 
-__global__ void __launch_bounds__(kFinishThreads) k_score_finish(const double* __restrict__ partials,
+__global__ void __launch_bounds__(kFinishThreads) k_score_finish(const DF* __restrict__ partials,
                                                                  FinishArgs fa,
                                                                  double* __restrict__ out) {
-  // Per scale: thread t sums tile rows t, t+1024, ... in order; warps fold
-  // their lanes with shuffles (fixed tree); the 32 warp results are summed
-  // in warp order.  Deterministic for a given frame size.
-  __shared__ double wsum[kFinishThreads / 32][18];
+  // Per scale: thread (g, k) sums quantity k of tile rows g, g + 56, ... in
+  // order in double-float; the 56 group sums of each quantity are added in
+  // group order.  Deterministic for a given frame size, f32 issue rates.
+  __shared__ DF gsum[kFinishGroups][18];
   __shared__ double scale_sums[6][18];
   __shared__ double terms[6][3][6];
-  const int lane = threadIdx.x % 32, warp = threadIdx.x / 32;
+  __shared__ double wterm[108];
+  const int g = threadIdx.x / 18, k = threadIdx.x % 18;
   size_t base = 0;
   for (int s = 0; s < fa.nscales; ++s) {
-    double acc[18];
-#pragma unroll
-    for (int k = 0; k < 18; ++k) acc[k] = 0.0;
-    for (int i = threadIdx.x; i < fa.ctas[s]; i += kFinishThreads)
-#pragma unroll
-      for (int k = 0; k < 18; ++k) acc[k] += partials[(base + i) * 18 + k];
-#pragma unroll
-    for (int k = 0; k < 18; ++k) {
-      double v = acc[k];
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-      if (lane == 0) wsum[warp][k] = v;
+    if (g < kFinishGroups) {
+      DF acc{0.0f, 0.0f};
+      for (int i = g; i < fa.ctas[s]; i += kFinishGroups)
+        acc = df_add(acc, partials[(base + i) * 18 + k]);
+      gsum[g][k] = acc;
     }
     __syncthreads();
     if (threadIdx.x < 18) {
-      double t = 0.0;
-      for (int i = 0; i < kFinishThreads / 32; ++i) t += wsum[i][threadIdx.x];
-      scale_sums[s][threadIdx.x] = t;
+      DF t = gsum[0][threadIdx.x];
+      for (int i = 1; i < kFinishGroups; ++i) t = df_add(t, gsum[i][threadIdx.x]);
+      scale_sums[s][threadIdx.x] = df_value(t);
     }
     __syncthreads();
     base += fa.ctas[s];
@@ -391,18 +386,22 @@ __global__ void __launch_bounds__(kFinishThreads) k_score_finish(const double* _
     terms[s][c][5] = sqrt(sqrt(inv * q[5]));
   }
   __syncthreads();
+  // ssimulacra2.rs:509 weighted error: weight i belongs to channel c, scale
+  // s, norm nn, map m with i = ((c * scales + s) * 2 + nn) * 3 + m.
+  if (threadIdx.x < 108) {
+    const int i = threadIdx.x;
+    const int m = i % 3, nn = (i / 3) % 2, cs = i / 6;
+    const int c = cs / fa.nscales, s = cs % fa.nscales;
+    wterm[i] = c < 3 ? c_weights[i] * fabs(terms[s][c][nn * 3 + m]) : 0.0;
+  }
+  __syncthreads();
+  if (threadIdx.x >= 32) return;
+  double part = 0.0;
+  for (int i = threadIdx.x; i < 3 * fa.nscales * 6; i += 32) part += wterm[i];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
   if (threadIdx.x != 0) return;
-  double err = 0.0;
-  int wi = 0;
-  for (int c = 0; c < 3; ++c)
-    for (int s = 0; s < fa.nscales; ++s)
-      for (int nn = 0; nn < 2; ++nn)
-        for (int m = 0; m < 3; ++m) {
-          double v = terms[s][c][nn * 3 + m];
-          double wgt = wi < 108 ? c_weights[wi] : 0.0;
-          ++wi;
-          err += wgt * fabs(v);
-        }
+  const double err = part;
   double sc = err * 0.9562382616834844;
   sc = 6.248496625763138e-5 * sc * sc * sc + 2.326765642916932 * sc -
        0.020884521182843837 * sc * sc;
@@ -413,7 +412,7 @@ __global__ void __launch_bounds__(kFinishThreads) k_score_finish(const double* _
       for (int m = 0; m < 6; ++m) out[2 + (s * 3 + c) * 6 + m] = terms[s][c][m];
 }
 
-void launch_score_finish(const double* partials, const int* ctas_per_scale, int nscales,
+void launch_score_finish(const DF* partials, const int* ctas_per_scale, int nscales,
                          const int* pixels_per_scale, double* out, cudaStream_t s) {
   FinishArgs fa;
   fa.nscales = nscales;
