@@ -318,21 +318,34 @@ __device__ __forceinline__ int32_t choose(float target, float step, float rstep,
     *recon = 0.0f;
     return 0;
   }
+  // Reconstruction levels increase with q, so of {e-1, e, e+1} only e and
+  // its neighbour on the target's side can be nearest; the third is strictly
+  // farther.  Candidates in the reference's update rule: q = 0 first (its
+  // level is 0, error |target|), then the pair in increasing q.
+  const float re = bias_adjust(e, bias) * step;
+  const int32_t nb = re < target ? e + 1 : e - 1;
+  const float rn = bias_adjust(nb, bias) * step;
   int32_t best = 0;
-  float best_err = __int_as_float(0x7f800000);
+  float best_err = fabsf(target);
   float best_recon = 0.0f;
-  const int32_t cand[4] = {0, e - 1, e, e + 1};
-#pragma unroll
-  for (int i = 0; i < 4; ++i) {
-    int32_t q = cand[i];
-    if ((q < 0 ? -q : q) > (1 << 20)) continue;
-    float r = bias_adjust(q, bias) * step;
-    float er = fabsf(r - target);
-    int32_t aq = q < 0 ? -q : q, ab = best < 0 ? -best : best;
-    if (er < best_err || (er == best_err && aq < ab)) {
-      best = q;
+  const int32_t q_lo = min(e, nb), q_hi = max(e, nb);
+  const float r_lo = e < nb ? re : rn, r_hi = e < nb ? rn : re;
+  // (|q| > 2^20 is outside the reference's candidate range; only the exact
+  // path near the limit can reach it.)
+  if (abs(q_lo) <= (1 << 20)) {
+    const float er = fabsf(r_lo - target);
+    if (er < best_err || (er == best_err && abs(q_lo) < abs(best))) {
+      best = q_lo;
       best_err = er;
-      best_recon = r;
+      best_recon = r_lo;
+    }
+  }
+  if (abs(q_hi) <= (1 << 20)) {
+    const float er = fabsf(r_hi - target);
+    if (er < best_err || (er == best_err && abs(q_hi) < abs(best))) {
+      best = q_hi;
+      best_err = er;
+      best_recon = r_hi;
     }
   }
   *recon = best_recon;
@@ -564,16 +577,16 @@ __device__ __forceinline__ uint32_t factor_bits(int32_t f) {
   return (32u - __clz(af)) + 2u;
 }
 
-// The varblock containing block (bx, by) and whether coefficient-image cell
-// (px, py) is in its n x n LLF corner.  Square varblocks only (the encoder's
-// cover); origins are naturally aligned.
-__device__ __forceinline__ bool cell_is_llf(const uint8_t* map, int bw, int px, int py, int* side) {
-  int bx = px >> 3, by = py >> 3;
-  int sel = map[(size_t)by * bw + bx] & 0x1f;
-  int nb = sel == 0 ? 1 : (sel == 4 ? 2 : 4);
-  *side = nb * 8;
-  int ox = (bx / nb) * nb * 8, oy = (by / nb) * nb * 8;
-  return (px - ox) < nb && (py - oy) < nb;
+// Whether coefficient-image cell (px, py) is in the n x n LLF corner of its
+// varblock; *lg = log2 of the varblock side in blocks (DCT8 0, DCT16 1,
+// DCT32 2).  Square varblocks only (the encoder's cover); origins are
+// naturally aligned, so positions within the varblock are masks.
+__device__ __forceinline__ bool cell_is_llf(const uint8_t* map, int bw, int px, int py, int* lg) {
+  const int sel = map[(size_t)(py >> 3) * bw + (px >> 3)] & 0x1f;
+  const int l = sel == 0 ? 0 : (sel == 4 ? 1 : 2);
+  *lg = l;
+  const int mask = (8 << l) - 1;
+  return (px & mask) < (1 << l) && (py & mask) < (1 << l);
 }
 
 constexpr int kCflThreads = 256;
@@ -611,8 +624,8 @@ __global__ void __launch_bounds__(kCflThreads) k_cfl_tiles(EncArgs a) {
       const int px = px0 + col;
       for (int row = threadIdx.x / 64; row < ph; row += kCflThreads / 64) {
         const int py = py0 + row;
-        int side;
-        if (cell_is_llf(a.block_map, geo.bw, px, py, &side)) continue;
+        int lg;
+        if (cell_is_llf(a.block_map, geo.bw, px, py, &lg)) continue;
         size_t ci = (size_t)py * geo.W8 + px;
         float y = a.coeff[cplane + ci];
         float x = a.coeff[ci];
@@ -726,9 +739,16 @@ __global__ void __launch_bounds__(kCflThreads) k_cfl_tiles(EncArgs a) {
   __syncthreads();
   // Phase C: residual bits of every candidate through the DCT8x8 baseline
   // quantizer (cells folded onto the 8x8 grid, lib.rs:3585).
-  const float scale_x = a.base_mul * a.qs.qm[0], scale_b = a.base_mul * a.qs.qm[2];
-  const float* m_x = a.dq;
-  const float* m_b = a.dq + 2 * kDequantTableFloats;
+  // Steps of the 64 folded cells and their reciprocals, per channel.
+  __shared__ float s_step[2][64], s_rstep[2][64];
+  if (threadIdx.x < 128) {
+    const int ch = threadIdx.x / 64, cell = threadIdx.x % 64;
+    const float scale = a.base_mul * a.qs.qm[ch == 0 ? 0 : 2];
+    const float st = scale * a.dq[(ch == 0 ? 0 : 2) * kDequantTableFloats + cell];
+    s_step[ch][cell] = st;
+    s_rstep[ch][cell] = 1.0f / st;
+  }
+  __syncthreads();
   unsigned long long bits[2][4] = {{0, 0, 0, 0}, {0, 0, 0, 0}};
   float kx[4], kb[4];
 #pragma unroll
@@ -744,16 +764,15 @@ __global__ void __launch_bounds__(kCflThreads) k_cfl_tiles(EncArgs a) {
       const int px = px0 + col;
       for (int row = threadIdx.x / 64; row < ph; row += kCflThreads / 64) {
         const int py = py0 + row;
-        int side;
-        if (cell_is_llf(a.block_map, geo.bw, px, py, &side)) continue;
-        const int fold = side / 8;
-        const int cell8 = ((py & (side - 1)) / fold) * 8 + ((px & (side - 1)) / fold);
+        int lg;
+        if (cell_is_llf(a.block_map, geo.bw, px, py, &lg)) continue;
+        const int mask = (8 << lg) - 1;
+        const int cell8 = ((py & mask) >> lg) * 8 + ((px & mask) >> lg);
         size_t ci = (size_t)py * geo.W8 + px;
         float dy = a.dyhf[ci];
         float x = a.coeff[ci], b = a.coeff[2 * cplane + ci];
-        const float step_x = scale_x * __ldg(&m_x[cell8]);
-        const float step_b = scale_b * __ldg(&m_b[cell8]);
-        const float rstep_x = 1.0f / step_x, rstep_b = 1.0f / step_b;
+        const float step_x = s_step[0][cell8], rstep_x = s_rstep[0][cell8];
+        const float step_b = s_step[1][cell8], rstep_b = s_rstep[1][cell8];
         float rc;
 #pragma unroll
         for (int c = 0; c < 4; ++c) {
