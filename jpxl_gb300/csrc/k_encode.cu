@@ -98,6 +98,12 @@ struct EncKernel {
   float centre, edge, corner, inv_c;
 };
 
+// The update of the last n % 4 samples of the plane divides by the centre
+// weight; out of line so that the division is not evaluated for every cell.
+static __device__ __noinline__ float precondition_tail(float mm, float fv, float kx, float centre) {
+  return mm + (fv - kx) / centre;
+}
+
 __global__ void __launch_bounds__(kPreThreads) k_precondition(const float* __restrict__ in,
                                                               float* __restrict__ out, int w,
                                                               int h, EncKernel k) {
@@ -178,12 +184,15 @@ __global__ void __launch_bounds__(kPreThreads) k_precondition(const float* __res
     const int lo = kPreHalo - r, hi = kPreHalo + kPreTile + r;  // local [lo, hi)
     const float* xs = cur ? X1 : X0;
     float* xn = cur ? X0 : X1;
-    // Each warp sweeps a band of rows; each lane a column, with the 3x3
-    // neighbourhood rolling down in registers.
-    const int band = (hi - lo + kWarps - 1) / kWarps;
-    const int ly0 = lo + warp * band, ly1 = min(ly0 + band, hi);
-    for (int lx = lo + lane; lx < hi; lx += 32) {
-      if (ly0 >= ly1) break;
+    // Same chunk / band mapping as the interior loop.
+    const int wd = hi - lo;
+    const int nch = (wd + 31) >> 5;
+    const int chunk = warp % nch;
+    const int nb = (kWarps - chunk + nch - 1) / nch;
+    const int rows = (wd + nb - 1) / nb;
+    const int ly0 = lo + (warp / nch) * rows, ly1 = min(ly0 + rows, hi);
+    const int lx = lo + chunk * 32 + lane;
+    if (lx < hi && ly0 < ly1) {
       const int gx = gx0 + lx;
       const bool in_x = gx >= 0 && gx < w;
       const bool edge_x = gx == 0 || gx == w - 1;
@@ -218,22 +227,34 @@ __global__ void __launch_bounds__(kPreThreads) k_precondition(const float* __res
           const int c = ly * kPreS + lx;
           const float fv = F[c];
           const bool in_bulk = gy < bulk_row || (gy == bulk_row && gx < bulk_col);
-          xn[c] = in_bulk ? mm + (fv - kx) * k.inv_c : mm + (fv - kx) / k.centre;
+          if (in_bulk) xn[c] = mm + (fv - kx) * k.inv_c;
+          else xn[c] = precondition_tail(mm, fv, kx, k.centre);
         }
         nw = ww; nn = mm; ne = ee;
         ww = sw; mm = ss; ee = se;
       }
     }
     __syncthreads();
-    // Out-of-frame halo cells take their mirror's new value.
+    // Out-of-frame halo cells take their mirror's new value: whole rows
+    // above or below the frame, and the bands left [lo, xl) and right
+    // [xr, hi) of it on the rows inside.
     if (has_halo_out) {
-      for (int ly = lo + warp; ly < hi; ly += kWarps)
-        for (int lx = lo + lane; lx < hi; lx += 32) {
-          int gx = gx0 + lx, gy = gy0 + ly;
-          if (gx >= 0 && gy >= 0 && gx < w && gy < h) continue;
-          int mx = mirror1d(gx, w) - gx0, my = mirror1d(gy, h) - gy0;
-          xn[ly * kPreS + lx] = xn[my * kPreS + mx];
+      const int xl = min(hi, max(lo, -gx0));
+      const int xr = max(lo, min(hi, w - gx0));
+      const int nl = xl - lo, nr = hi - xr;
+      for (int ly = lo + warp; ly < hi; ly += kWarps) {
+        const int gy = gy0 + ly;
+        const int my = mirror1d(gy, h) - gy0;
+        if (gy < 0 || gy >= h) {
+          for (int cx = lo + lane; cx < hi; cx += 32)
+            xn[ly * kPreS + cx] = xn[my * kPreS + mirror1d(gx0 + cx, w) - gx0];
+        } else {
+          for (int i = lane; i < nl + nr; i += 32) {
+            const int cx = i < nl ? lo + i : xr + (i - nl);
+            xn[ly * kPreS + cx] = xn[ly * kPreS + mirror1d(gx0 + cx, w) - gx0];
+          }
         }
+      }
       __syncthreads();
     }
     cur ^= 1;
@@ -424,32 +445,35 @@ __global__ void __launch_bounds__(128) k_fdct_luma(EncArgs a, const uint32_t* __
   const Geo& geo = a.geo;
   const size_t plane = (size_t)geo.w * geo.h;
   const size_t cplane = (size_t)geo.W8 * geo.H8;
-  float ycoef[N];
-#pragma unroll
-  for (int c = 0; c < 3; ++c) {
-    float v[N];
+  // Six passes (three channels x column and row transforms) through one copy
+  // of the transform: the loop stays rolled so that a 32-point transform is
+  // not inlined six times past the instruction cache.  Luma runs last, so
+  // its coefficients are in v when the loop ends.
+  float v[N];
+#pragma unroll 1
+  for (int pass = 0; pass < 6; ++pass) {
+    const int c = pass < 2 ? 0 : (pass < 4 ? 2 : 1);
     if (active) {
-      const float* p = a.pre + plane * c;
-      const int xx = min(x0 + j, geo.w - 1);
+      if ((pass & 1) == 0) {
+        const float* p = a.pre + plane * c;
+        const int xx = min(x0 + j, geo.w - 1);
 #pragma unroll
-      for (int r = 0; r < N; ++r) v[r] = p[(size_t)min(y0 + r, geo.h - 1) * geo.w + xx];
-      dct_1d<N>(v);
+        for (int r = 0; r < N; ++r) v[r] = p[(size_t)min(y0 + r, geo.h - 1) * geo.w + xx];
+      } else {
 #pragma unroll
-      for (int r = 0; r < N; ++r) T[g][r][j] = v[r];
-    }
-    __syncthreads();
-    if (active) {
-#pragma unroll
-      for (int k = 0; k < N; ++k) v[k] = T[g][j][k];
-      dct_1d<N>(v);
-#pragma unroll
-      for (int k = 0; k < N; ++k) {
-        if (c == 1) ycoef[k] = v[k];
-        a.coeff[cplane * c + (size_t)(y0 + k) * geo.W8 + x0 + j] = v[k];
+        for (int k = 0; k < N; ++k) v[k] = T[g][j][k];
       }
-      if (j < n) {
+      dct_1d<N>(v);
+      if ((pass & 1) == 0) {
 #pragma unroll
-        for (int k = 0; k < n; ++k) LL[g][c][k * n + j] = v[k];
+        for (int r = 0; r < N; ++r) T[g][r][j] = v[r];
+      } else {
+#pragma unroll
+        for (int k = 0; k < N; ++k) a.coeff[cplane * c + (size_t)(y0 + k) * geo.W8 + x0 + j] = v[k];
+        if (j < n) {
+#pragma unroll
+          for (int k = 0; k < n; ++k) LL[g][c][k * n + j] = v[k];
+        }
       }
     }
     __syncthreads();
@@ -477,7 +501,11 @@ __global__ void __launch_bounds__(128) k_fdct_luma(EncArgs a, const uint32_t* __
   const float scale = mul * a.qs.qm[1];
   const float* m = a.dq + kDequantTableFloats + dq_offset(dq_slot(N == 8 ? 0 : (N == 16 ? 4 : 5)));
   const float bias = c_quant_bias[1];
+  // The luma coefficients go through this thread's own row of T so that the
+  // quantization loop need not be unrolled N times.
 #pragma unroll
+  for (int k = 0; k < N; ++k) T[g][j][k] = v[k];
+#pragma unroll 2
   for (int k = 0; k < N; ++k) {
     const int cell = k * N + j;
     const size_t ci = (size_t)(y0 + k) * geo.W8 + x0 + j;
@@ -487,7 +515,7 @@ __global__ void __launch_bounds__(128) k_fdct_luma(EncArgs a, const uint32_t* __
     if (k < n && j < n) {
       recon = bias_adjust(0, bias) * step;
     } else {
-      q = choose(ycoef[k], step, 1.0f / step, bias, a.err, &recon);
+      q = choose(T[g][j][k], step, 1.0f / step, bias, a.err, &recon);
     }
     a.qcoeff[cplane + ci] = q;
     a.dyhf[ci] = recon;

@@ -133,13 +133,17 @@ __global__ void __launch_bounds__(128) k_render_vb(RenderArgs a, const uint32_t*
   constexpr int slot = (R == C) ? (R == 8 ? 0 : (R == 16 ? 1 : 2))
                                 : (CC == 16 ? 3 : (CR == 8 ? 4 : 5));
   const int off = dq_offset(slot);
-#pragma unroll
+  // The channel loop stays rolled, and for square shapes both IDCT passes
+  // run through one copy of the transform: a 32-point transform inlined six
+  // times does not fit the instruction cache.
+#pragma unroll 1
   for (int ci = 0; ci < 3; ++ci) {
     const int c = ci == 0 ? 1 : (ci == 1 ? 0 : 2);  // luma first: CfL needs it
     if (active) {
       const float scale = mul * a.qs.qm[c];
       const float bias = c_quant_bias[c];
       const float* m = a.dq + c * kDequantTableFloats + off;
+      const float kc = c == 0 ? kx : kb;
 #pragma unroll
       for (int y = 0; y < CR; ++y) {
         const int x = j;
@@ -147,43 +151,74 @@ __global__ void __launch_bounds__(128) k_render_vb(RenderArgs a, const uint32_t*
         int32_t q = a.qcoeff[cplane * c + pos];
         float d = bias_adjust_q(q, bias) * scale * __ldg(&m[y * CC + x]);
         if (c == 1) dY[y] = d;
-        else d = d + (c == 0 ? kx : kb) * dY[y];  // lib.rs:1344 apply_hf_cfl
+        else d = d + kc * dY[y];  // lib.rs:1344 apply_hf_cfl
         if (y < LY && x < LX) d = LLF[g][c][y * LX + x];
         L[g][y][x] = d;
       }
     }
     __syncthreads();
-    // Step A: thread jj < R transforms column jj of S (length C).
     float v[T];
-    if (active && j < R) {
+    if constexpr (R == C) {
+      // Step A (st = 0): thread j transforms column j of L in place.
+      // Step B (st = 1): thread j transforms row j of the result into sample
+      // column j and scatters it inside the frame.
+#pragma unroll 1
+      for (int st = 0; st < 2; ++st) {
+        if (active) {
 #pragma unroll
-      for (int i = 0; i < C; ++i) v[i] = (C > R) ? L[g][j][i] : L[g][i][j];
-      idct_n<C>(v);
-    }
-    __syncthreads();
-    if (active && j < R) {
+          for (int i = 0; i < T; ++i) v[i] = st == 0 ? L[g][i][j] : L[g][j][i];
+          idct_n<T>(v);
+        }
+        if (st == 0) {
+          __syncthreads();
+          if (active) {
 #pragma unroll
-      for (int i = 0; i < C; ++i) {
-        if (C > R) L[g][j][i] = v[i]; else L[g][i][j] = v[i];
+            for (int i = 0; i < T; ++i) L[g][i][j] = v[i];
+          }
+        } else if (active) {
+          const int fx = x0 + j;
+          if (fx < geo.w) {
+#pragma unroll
+            for (int r = 0; r < T; ++r) {
+              const int fy = y0 + r;
+              if (fy < geo.h) a.planes[plane * c + (size_t)fy * geo.w + fx] = v[r];
+            }
+          }
+        }
+        __syncthreads();
       }
-    }
-    __syncthreads();
-    // Step B: thread i < C transforms row i of the step-A result (length R)
-    // into sample column i and scatters it inside the frame.
-    if (active && j < C) {
+    } else {
+      // Step A: thread jj < R transforms column jj of S (length C).
+      if (active && j < R) {
 #pragma unroll
-      for (int r = 0; r < R; ++r) v[r] = (C > R) ? L[g][r][j] : L[g][j][r];
-      idct_n<R>(v);
-      const int fx = x0 + j;
-      if (fx < geo.w) {
+        for (int i = 0; i < C; ++i) v[i] = (C > R) ? L[g][j][i] : L[g][i][j];
+        idct_n<C>(v);
+      }
+      __syncthreads();
+      if (active && j < R) {
 #pragma unroll
-        for (int r = 0; r < R; ++r) {
-          const int fy = y0 + r;
-          if (fy < geo.h) a.planes[plane * c + (size_t)fy * geo.w + fx] = v[r];
+        for (int i = 0; i < C; ++i) {
+          if (C > R) L[g][j][i] = v[i]; else L[g][i][j] = v[i];
         }
       }
+      __syncthreads();
+      // Step B: thread i < C transforms row i of the step-A result (length R)
+      // into sample column i and scatters it inside the frame.
+      if (active && j < C) {
+#pragma unroll
+        for (int r = 0; r < R; ++r) v[r] = (C > R) ? L[g][r][j] : L[g][j][r];
+        idct_n<R>(v);
+        const int fx = x0 + j;
+        if (fx < geo.w) {
+#pragma unroll
+          for (int r = 0; r < R; ++r) {
+            const int fy = y0 + r;
+            if (fy < geo.h) a.planes[plane * c + (size_t)fy * geo.w + fx] = v[r];
+          }
+        }
+      }
+      __syncthreads();
     }
-    __syncthreads();
   }
   // J.4.3 sigma per block (restoration.rs:338 vardct_sigma).
   if (active && j < BR * BC) {
