@@ -39,7 +39,7 @@ WORKLOAD = ("2048x2048 RGB16 quality probe: encode transform (XYB, inverse Gabor
             "(6 scales)")
 
 # Algorithmic HBM bytes per source pixel of each stage for this workload
-# (f32 planes, int32 coefficients, RGB16 input); see the design doc.
+# (f32 planes, int32 coefficients, RGB16 input).
 STAGE_BYTES_PER_PX = {
     "xyb": 6 + 12,              # RGB16 in, 3 f32 planes out
     "precondition": 12 + 12,    # 3 planes in, 3 out
@@ -244,14 +244,22 @@ def run_ours(args):
 
     build.build()
     images, _ = make_workload(rank, world)
-    ctx = jg.Context(local)
-    # A dedicated stream shared by the library and the timing events (the
+    # One context per stream: images alternate over the streams so that the
+    # small launches of one probe overlap the work of another.  Dedicated
+    # torch streams carry both the library's work and the timing events (the
     # default stream's handle is 0, which the library reads as "own stream").
-    stream = torch.cuda.Stream()
-    torch.cuda.set_stream(stream)
-    ctx.set_stream(stream.cuda_stream)
-    if ctx.stream != stream.cuda_stream:
-        raise RuntimeError("the library did not adopt the timing stream")
+    nstreams = max(1, args.streams)
+    ctxs, streams = [], []
+    for _ in range(nstreams):
+        c = jg.Context(local)
+        st = torch.cuda.Stream()
+        c.set_stream(st.cuda_stream)
+        if c.stream != st.cuda_stream:
+            raise RuntimeError("the library did not adopt the timing stream")
+        ctxs.append(c)
+        streams.append(st)
+    ctx = ctxs[0]
+    torch.cuda.set_stream(streams[0])
     req = jg.EncodeRequest.with_global_scale(GLOBAL_SCALE, gaborish=True, epf_iters=3)
     layouts, refs, dev_rgb, host_rgb = [], [], [], []
     for rgb, cover in images:
@@ -266,61 +274,81 @@ def run_ours(args):
         pinned.copy_(torch.from_numpy(rgb.view(np.int16)))
         host_rgb.append(pinned)
     scores = torch.zeros(len(images), dtype=torch.float64, device="cuda")
-    ctx.synchronize()
+    torch.cuda.synchronize()
+    for c in ctxs:
+        c.synchronize()
 
-    def device_step():
+    def device_step(contexts):
         for i in range(len(images)):
-            ctx.probe_device(layouts[i], refs[i], dev_rgb[i].data_ptr(), BITS, req,
-                             scores.data_ptr() + 8 * i)
+            contexts[i % len(contexts)].probe_device(layouts[i], refs[i], dev_rgb[i].data_ptr(),
+                                                     BITS, req, scores.data_ptr() + 8 * i)
 
     for _ in range(max(args.warmup, 3)):
-        device_step()
-    ctx.synchronize()
-    ctx.stage_times()  # reset
+        device_step(ctxs)
+    torch.cuda.synchronize()
     sampler = ClockSampler(local)
     sampler.start()
-    ctx.stage_timing(True)
-    launches0 = ctx.launches
+    launches0 = sum(c.launches for c in ctxs)
     barrier()
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
+    e0.record(streams[0])
+    for st in streams[1:]:
+        st.wait_event(e0)
     for _ in range(args.steps):
-        device_step()
-    e1.record(stream)
+        device_step(ctxs)
+    for st in streams[1:]:
+        done = torch.cuda.Event()
+        done.record(st)
+        streams[0].wait_event(done)
+    e1.record(streams[0])
     torch.cuda.synchronize()
     barrier()
     ms = e0.elapsed_time(e1)
-    launches = ctx.launches - launches0
-    ctx.synchronize()
-    stages = ctx.stage_times()
-    ctx.stage_timing(False)
+    launches = sum(c.launches for c in ctxs) - launches0
     clocks = sampler.stop()
     ms_max = max_over_ranks(ms)
     px_total = W * H * len(images) * args.steps * world
     value = px_total / (ms_max / 1e3) / 1e6
 
-    # e2e through the C ABI with pinned host buffers
-    host_scores = []
+    # Stage breakdown: the same steps on one stream with stage timers.
+    ctx.stage_times()  # reset
+    ctx.stage_timing(True)
+    for _ in range(args.steps):
+        device_step([ctx])
+    ctx.synchronize()
+    stages = ctx.stage_times()
+    ctx.stage_timing(False)
 
-    def host_step():
-        for i in range(len(images)):
-            host_scores.append(ctx.probe(layouts[i], refs[i], host_rgb[i].numpy().view(np.uint16),
-                                         jg.EncodeRequest.with_global_scale(
-                                             GLOBAL_SCALE, gaborish=True, epf_iters=3), BITS))
+    # e2e through the C ABI with pinned host buffers: one host thread per
+    # context, each probing its share of the images (host mode copies the
+    # image in and the score out, and returns when the score is in place).
+    host_scores = [None] * len(images)
 
-    for _ in range(max(args.warmup, 3)):
-        host_step()
+    def host_worker(t, steps):
+        c = ctxs[t]
+        for _ in range(steps):
+            for i in range(t, len(images), nstreams):
+                host_scores[i] = c.probe(layouts[i], refs[i], host_rgb[i].numpy().view(np.uint16),
+                                         req, BITS)
+
+    def host_step(steps):
+        threads = [threading.Thread(target=host_worker, args=(t, steps)) for t in range(nstreams)]
+        for th in threads:
+            th.start()
+        for th in threads:
+            th.join()
+
+    host_step(max(args.warmup, 3))
     barrier()
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    for _ in range(args.steps):
-        host_step()
+    host_step(args.steps)
     torch.cuda.synchronize()
     e2e_s = max_over_ranks(time.perf_counter() - t0)
     e2e = px_total / e2e_s / 1e6
     dev_scores = scores.cpu().numpy()
-    if not np.allclose(dev_scores, host_scores[-len(images):]):
+    if not np.allclose(dev_scores, host_scores):
         raise RuntimeError(f"device and host probes disagree: {dev_scores} {host_scores}")
 
     if rank != 0:
@@ -360,7 +388,7 @@ def run_ours(args):
                    "cover": "activity DCT8/16/32 (stand-in for select_blocks)",
                    "l2": (f"inputs larger than L2: {IMAGES_PER_STEP} distinct images, "
                           f"{W * H * 6 * IMAGES_PER_STEP / 1e6:.0f} MB of RGB16 per step"),
-                   "parallelism": f"replicas x{world}"},
+                   "parallelism": f"replicas x{world}", "streams": nstreams},
         "stages_ms": {k: round(v[0] / args.steps, 4) for k, v in stages.items()},
         "roofline": {"kernel": top, "bound": "hbm", "achieved": round(achieved, 1),
                      "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4),
@@ -373,7 +401,7 @@ def run_ours(args):
                 "h2d_bytes_per_step": int(sum(r.nbytes for r, _ in images)),
                 "d2h_bytes_per_step": 8 * len(images)},
         "gpu_launches": int(launches),
-        "cfl_sequential_fallbacks": ctx.cfl_fallbacks,
+        "cfl_sequential_fallbacks": sum(c.cfl_fallbacks for c in ctxs),
         "clocks": clocks,
         "scores": [round(float(s), 6) for s in dev_scores],
     }
@@ -392,6 +420,8 @@ def main():
     ap.add_argument("--size", type=int, default=None, help="square image side (profiling)")
     ap.add_argument("--images", type=int, default=None, help="images per step (profiling)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--streams", type=int, default=4,
+                    help="contexts (each with its own stream) that images alternate over")
     args = ap.parse_args()
     global W, H, IMAGES_PER_STEP
     if args.size:

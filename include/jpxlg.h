@@ -34,6 +34,11 @@
  * are device pointers on the context's device, work is queued on the
  * context's stream and device-side errors are reported by the next
  * jpxlg_ctx_synchronize().  A context serves one host thread at a time.
+ * Layouts and references are read-only device data of their device: any
+ * context on that device may use them, so several contexts (streams, host
+ * threads) can probe the same frame concurrently.  Destroying one waits for
+ * its creating context's stream only; synchronize the other contexts that
+ * used it first.
  *
  * Layouts.
  *   planes      float, row-major width x height, three planes back to back

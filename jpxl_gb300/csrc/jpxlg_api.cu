@@ -647,6 +647,7 @@ int jpxlg_layout_dims(const jpxlg_layout* L, int* bw, int* bh, int* tw, int* th)
 int jpxlg_encode_transform(jpxlg_ctx* ctx, const jpxlg_layout* L, const void* rgb, int bits,
                            const jpxlg_params* p, jpxlg_plan* plan, uint32_t mem) {
   if (!ctx || !L || !rgb || !plan) return fail(ctx, JPXLG_ERR_ARGUMENT, "null argument");
+  if (L->ctx->device != ctx->device) return fail(ctx, JPXLG_ERR_ARGUMENT, "layout on another device");
   if (!(bits == 8 || (bits >= 9 && bits <= 16)))
     return fail(ctx, JPXLG_ERR_ARGUMENT, "bits must be 8 or 9..16");
   int rc = check_params(ctx, p);
@@ -699,6 +700,7 @@ int jpxlg_encode_transform(jpxlg_ctx* ctx, const jpxlg_layout* L, const void* rg
 int jpxlg_encode_stages(jpxlg_ctx* ctx, const jpxlg_layout* L, const void* rgb, int bits,
                         const jpxlg_params* p, float* xyb, float* pre, float* coeff) {
   if (!ctx || !L || !rgb) return fail(ctx, JPXLG_ERR_ARGUMENT, "null argument");
+  if (L->ctx->device != ctx->device) return fail(ctx, JPXLG_ERR_ARGUMENT, "layout on another device");
   if (!(bits == 8 || (bits >= 9 && bits <= 16)))
     return fail(ctx, JPXLG_ERR_ARGUMENT, "bits must be 8 or 9..16");
   int rc = check_params(ctx, p);
@@ -729,6 +731,7 @@ int jpxlg_encode_stages(jpxlg_ctx* ctx, const jpxlg_layout* L, const void* rgb, 
 int jpxlg_reconstruct(jpxlg_ctx* ctx, const jpxlg_layout* L, const jpxlg_plan* plan,
                       const jpxlg_params* p, int out_kind, int bits, void* out, uint32_t mem) {
   if (!ctx || !L || !plan || !out) return fail(ctx, JPXLG_ERR_ARGUMENT, "null argument");
+  if (L->ctx->device != ctx->device) return fail(ctx, JPXLG_ERR_ARGUMENT, "layout on another device");
   if (!plan->qcoeff || !plan->lf || !plan->cfl_x || !plan->cfl_b)
     return fail(ctx, JPXLG_ERR_ARGUMENT, "null plan buffer");
   int rc = check_params(ctx, p);
@@ -854,6 +857,8 @@ int jpxlg_ssim2_ref_destroy(jpxlg_ref* R) {
 int jpxlg_ssim2_score(jpxlg_ctx* ctx, const jpxlg_ref* R, const float* rgb, uint32_t mem,
                       double* score, double* raw_error, double* terms) {
   if (!ctx || !R || !rgb) return fail(ctx, JPXLG_ERR_ARGUMENT, "null argument");
+  if (R->ctx->device != ctx->device)
+    return fail(ctx, JPXLG_ERR_ARGUMENT, "reference on another device");
   cudaSetDevice(ctx->device);
   const size_t n = (size_t)R->w * R->h;
   CK(ctx->score.ensure(128 * sizeof(double)));
@@ -891,6 +896,8 @@ int jpxlg_score_pair(jpxlg_ctx* ctx, const float* ref_rgb, const float* cand_rgb
 int jpxlg_probe(jpxlg_ctx* ctx, const jpxlg_layout* L, const jpxlg_ref* R, const void* rgb,
                 int bits, const jpxlg_params* p, uint32_t mem, double* score) {
   if (!ctx || !L || !R || !rgb || !score) return fail(ctx, JPXLG_ERR_ARGUMENT, "null argument");
+  if (L->ctx->device != ctx->device || R->ctx->device != ctx->device)
+    return fail(ctx, JPXLG_ERR_ARGUMENT, "layout or reference on another device");
   if (R->w != L->geo.w || R->h != L->geo.h)
     return fail(ctx, JPXLG_ERR_MISMATCH, "reference and layout dimensions differ");
   int rc = check_params(ctx, p);

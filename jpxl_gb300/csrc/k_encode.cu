@@ -145,8 +145,8 @@ __global__ void __launch_bounds__(kPreThreads) k_precondition(const float* __res
   if (fast) {
     for (int it = 0; it < 12; ++it) {
       const int lo = 1 + it, hi = kPreS - 1 - it;
-      const float* xs = cur ? X1 : X0;
-      float* xn = cur ? X0 : X1;
+      // Offsets of the source and destination planes in pre_smem (F at 0).
+      const int xs = (cur ? 2 : 1) * kPreS * kPreS, xd = (cur ? 1 : 2) * kPreS * kPreS;
       // Column chunks of 32 (lane = column); the warps sharing a chunk
       // split its rows into bands.
       const int wd = hi - lo;
@@ -157,20 +157,18 @@ __global__ void __launch_bounds__(kPreThreads) k_precondition(const float* __res
       const int ly0 = lo + (warp / nch) * rows, ly1 = min(ly0 + rows, hi);
       const int lx = lo + chunk * 32 + lane;
       if (lx < hi && ly0 < ly1) {
-        const float* p = xs + (ly0 - 1) * kPreS + lx;
-        float nw = p[-1], nn = p[0], ne = p[1];
-        p += kPreS;
-        float ww = p[-1], mm = p[0], ee = p[1];
-        const float* f = F + ly0 * kPreS + lx;
-        float* o = xn + ly0 * kPreS + lx;
-        for (int ly = ly0; ly < ly1; ++ly) {
-          p += kPreS;
-          const float sw = p[-1], ss = p[0], se = p[1];
+        int c = ly0 * kPreS + lx;
+        float nw = pre_smem[xs + c - kPreS - 1], nn = pre_smem[xs + c - kPreS],
+              ne = pre_smem[xs + c - kPreS + 1];
+        float ww = pre_smem[xs + c - 1], mm = pre_smem[xs + c], ee = pre_smem[xs + c + 1];
+        const int end = ly1 * kPreS + lx;
+#pragma unroll 3
+        for (; c < end; c += kPreS) {
+          const float sw = pre_smem[xs + c + kPreS - 1], ss = pre_smem[xs + c + kPreS],
+                      se = pre_smem[xs + c + kPreS + 1];
           const float kx =
               mm * k.centre + (nn + ss + ww + ee) * k.edge + (nw + ne + sw + se) * k.corner;
-          *o = mm + (*f - kx) * k.inv_c;
-          f += kPreS;
-          o += kPreS;
+          pre_smem[xd + c] = mm + (pre_smem[c] - kx) * k.inv_c;
           nw = ww; nn = mm; ne = ee;
           ww = sw; mm = ss; ee = se;
         }
