@@ -168,6 +168,53 @@ __device__ __forceinline__ float cbrt_perceptual(float v) {
   return cbrt_perceptual_f64(v);
 }
 
+// ---- paired f32 arithmetic (sm_100 family) ----------------------------------
+// Two f32 lanes in one 64-bit register (lane 0 in the low word).  Each lane
+// of add/sub.rn.f32x2 rounds exactly as the scalar f32 operation.
+//
+// Products need care: the assembler fuses a paired multiply with a following
+// paired add into one rounding, whatever the rounding modifier or -fmad
+// setting (measured on sm_103a: mul.rn.f32x2 then add.rn.f32x2 differed
+// from the scalar mul-then-add in about one result in nine, and so did
+// fma.rn.f32x2(a, b, -0.0) with the -0.0 as an immediate).  f2_mul is
+// therefore fma.rn.f32x2(a, b, z) with z = (-0.0, -0.0) supplied at run time
+// (a kernel argument), which the assembler cannot see through: one rounding
+// of a*b, signed zeros included, exactly the scalar product.
+typedef unsigned long long f2;
+__device__ __forceinline__ f2 f2_pack(float lo, float hi) {
+  f2 r;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
+  return r;
+}
+__device__ __forceinline__ float f2_lo(f2 v) {
+  float a, b;
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(v));
+  (void)b;
+  return a;
+}
+__device__ __forceinline__ float f2_hi(f2 v) {
+  float a, b;
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(v));
+  (void)a;
+  return b;
+}
+__device__ __forceinline__ f2 f2_add(f2 a, f2 b) {
+  f2 d;
+  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+__device__ __forceinline__ f2 f2_sub(f2 a, f2 b) {
+  f2 d;
+  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+// a * b per lane; nz must be the run-time pair (-0.0f, -0.0f).
+__device__ __forceinline__ f2 f2_mul(f2 a, f2 b, f2 nz) {
+  f2 d;
+  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(nz));
+  return d;
+}
+
 // ---- double-float (f32 pair) sums --------------------------------------------
 // Products of two f32 are split exactly (two_prod); sums keep hi + lo to
 // about 2^-46 per addition, so a sum over n terms lies within

@@ -92,10 +92,41 @@ constexpr int kPreTile = 64;
 constexpr int kPreHalo = 12;
 constexpr int kPreS = kPreTile + 2 * kPreHalo;  // 88
 constexpr int kPreThreads = 512;
-constexpr size_t kPreSmem = 3 * kPreS * kPreS * sizeof(float);
+// Three planes (source F and the ping-pong pair) with a 4-float pad on both
+// sides, so that the paired loop's edge lanes may read one column past the
+// region; the base stays 16-byte aligned.
+constexpr int kPrePad = 4;
+constexpr size_t kPreSmem = (3 * kPreS * kPreS + 2 * kPrePad) * sizeof(float);
+
+// Interior-tile mapping of step `it`: lane t updates the column pair
+// p_lo + t % np (columns 2p, 2p+1) over the rows of band t / np; the band
+// is (t * mg) >> 16, exact for t < kPreThreads (checked below).
+struct PreStep {
+  int p_lo, np, mg, bands, rows;
+};
+constexpr PreStep pre_step(int it) {
+  const int lo = 1 + it, hi = kPreS - 1 - it, wd = hi - lo;
+  const int p_lo = lo >> 1, p_hi = (hi - 1) >> 1, np = p_hi - p_lo + 1;
+  const int bands = kPreThreads / np;
+  return {p_lo, np, (65536 + np - 1) / np, bands, (wd + bands - 1) / bands};
+}
+constexpr bool pre_steps_exact() {
+  for (int it = 0; it < 12; ++it) {
+    const PreStep s = pre_step(it);
+    for (int t = 0; t < kPreThreads; ++t)
+      if (((t * s.mg) >> 16) != t / s.np) return false;
+    if (s.bands * s.rows < (kPreS - 2 - 2 * it)) return false;
+  }
+  return true;
+}
+static_assert(pre_steps_exact(), "interior mapping of the inverse Gaborish");
+__constant__ PreStep c_pre_steps[12] = {pre_step(0), pre_step(1), pre_step(2),  pre_step(3),
+                                        pre_step(4), pre_step(5), pre_step(6),  pre_step(7),
+                                        pre_step(8), pre_step(9), pre_step(10), pre_step(11)};
 
 struct EncKernel {
   float centre, edge, corner, inv_c;
+  float neg_zero;  // -0.0f, the run-time addend of the paired products
 };
 
 // The update of the last n % 4 samples of the plane divides by the centre
@@ -107,10 +138,11 @@ static __device__ __noinline__ float precondition_tail(float mm, float fv, float
 __global__ void __launch_bounds__(kPreThreads) k_precondition(const float* __restrict__ in,
                                                               float* __restrict__ out, int w,
                                                               int h, EncKernel k) {
-  extern __shared__ float pre_smem[];
-  float* F = pre_smem;
-  float* const X0 = pre_smem + kPreS * kPreS;
-  float* const X1 = pre_smem + 2 * kPreS * kPreS;
+  extern __shared__ __align__(16) float pre_smem[];
+  float* const base = pre_smem + kPrePad;
+  float* F = base;
+  float* const X0 = base + kPreS * kPreS;
+  float* const X1 = base + 2 * kPreS * kPreS;
   const size_t plane = (size_t)w * h;
   in += plane * blockIdx.z;
   out += plane * blockIdx.z;
@@ -143,34 +175,45 @@ __global__ void __launch_bounds__(kPreThreads) k_precondition(const float* __res
                     (bulk == n || gy0 + kPreS - 2 < bulk_row);
   int cur = 0;
   if (fast) {
+    // Paired lanes: each thread updates two adjacent columns with f32x2
+    // arithmetic; the formula and its operation order are the scalar ones.
+    const f2 c2 = f2_pack(k.centre, k.centre), e2 = f2_pack(k.edge, k.edge);
+    const f2 k2 = f2_pack(k.corner, k.corner), i2 = f2_pack(k.inv_c, k.inv_c);
+    const f2 nz = f2_pack(k.neg_zero, k.neg_zero);
+    const int t = threadIdx.x;
     for (int it = 0; it < 12; ++it) {
+      const PreStep ps = c_pre_steps[it];
       const int lo = 1 + it, hi = kPreS - 1 - it;
-      // Offsets of the source and destination planes in pre_smem (F at 0).
-      const int xs = (cur ? 2 : 1) * kPreS * kPreS, xd = (cur ? 1 : 2) * kPreS * kPreS;
-      // Column chunks of 32 (lane = column); the warps sharing a chunk
-      // split its rows into bands.
-      const int wd = hi - lo;
-      const int nch = (wd + 31) >> 5;
-      const int chunk = warp % nch;
-      const int nb = (kWarps - chunk + nch - 1) / nch;
-      const int rows = (wd + nb - 1) / nb;
-      const int ly0 = lo + (warp / nch) * rows, ly1 = min(ly0 + rows, hi);
-      const int lx = lo + chunk * 32 + lane;
-      if (lx < hi && ly0 < ly1) {
-        int c = ly0 * kPreS + lx;
-        float nw = pre_smem[xs + c - kPreS - 1], nn = pre_smem[xs + c - kPreS],
-              ne = pre_smem[xs + c - kPreS + 1];
-        float ww = pre_smem[xs + c - 1], mm = pre_smem[xs + c], ee = pre_smem[xs + c + 1];
-        const int end = ly1 * kPreS + lx;
+      const float* X = cur ? X1 : X0;
+      float* Y = cur ? X0 : X1;
+      const int band = (int)(((unsigned)t * (unsigned)ps.mg) >> 16);
+      const int c0 = 2 * (ps.p_lo + t - band * ps.np);
+      const int ly0 = lo + band * ps.rows, ly1 = min(ly0 + ps.rows, hi);
+      if (band < ps.bands && ly0 < ly1) {
+        const bool st_lo = c0 >= lo, st_hi = c0 + 1 < hi;
+        int c = ly0 * kPreS + c0;
+        f2 Mn = *reinterpret_cast<const f2*>(X + c - kPreS);
+        f2 Wn = f2_pack(X[c - kPreS - 1], f2_lo(Mn)), En = f2_pack(f2_hi(Mn), X[c - kPreS + 2]);
+        f2 Mm = *reinterpret_cast<const f2*>(X + c);
+        f2 Wm = f2_pack(X[c - 1], f2_lo(Mm)), Em = f2_pack(f2_hi(Mm), X[c + 2]);
+        const int end = ly1 * kPreS + c0;
 #pragma unroll 3
         for (; c < end; c += kPreS) {
-          const float sw = pre_smem[xs + c + kPreS - 1], ss = pre_smem[xs + c + kPreS],
-                      se = pre_smem[xs + c + kPreS + 1];
-          const float kx =
-              mm * k.centre + (nn + ss + ww + ee) * k.edge + (nw + ne + sw + se) * k.corner;
-          pre_smem[xd + c] = mm + (pre_smem[c] - kx) * k.inv_c;
-          nw = ww; nn = mm; ne = ee;
-          ww = sw; mm = ss; ee = se;
+          const f2 Ms = *reinterpret_cast<const f2*>(X + c + kPreS);
+          const f2 Ws = f2_pack(X[c + kPreS - 1], f2_lo(Ms));
+          const f2 Es = f2_pack(f2_hi(Ms), X[c + kPreS + 2]);
+          // mm*c + (nn + ss + ww + ee)*e + (nw + ne + sw + se)*k
+          const f2 s1 = f2_add(f2_add(f2_add(Mn, Ms), Wm), Em);
+          const f2 s2 = f2_add(f2_add(f2_add(Wn, En), Ws), Es);
+          const f2 kx =
+              f2_add(f2_add(f2_mul(Mm, c2, nz), f2_mul(s1, e2, nz)), f2_mul(s2, k2, nz));
+          const f2 u =
+              f2_add(Mm, f2_mul(f2_sub(*reinterpret_cast<const f2*>(F + c), kx), i2, nz));
+          if (st_lo && st_hi) *reinterpret_cast<f2*>(Y + c) = u;
+          else if (st_lo) Y[c] = f2_lo(u);
+          else if (st_hi) Y[c + 1] = f2_hi(u);
+          Mn = Mm; Wn = Wm; En = Em;
+          Mm = Ms; Wm = Ws; Em = Es;
         }
       }
       __syncthreads();
@@ -270,7 +313,7 @@ void launch_precondition(const float* in, float* out, int w, int h, cudaStream_t
   // gaborish.rs:31 GaborKernel::new, normalised without FMA.
   float unnorm = 1.0f + 4.0f * w1 + 4.0f * w2;
   float scale = 1.0f / unnorm;
-  EncKernel k{scale, w1 * scale, w2 * scale, 1.0f / scale};
+  EncKernel k{scale, w1 * scale, w2 * scale, 1.0f / scale, -0.0f};
   static bool configured = false;
   if (!configured) {
     cudaFuncSetAttribute(k_precondition, cudaFuncAttributeMaxDynamicSharedMemorySize,

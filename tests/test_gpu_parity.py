@@ -56,6 +56,24 @@ def test_stages_are_bit_identical(ctx, oracle):
     assert np.array_equal(st["coeff"].view(np.uint32), ref["coeff"].view(np.uint32))
 
 
+@pytest.mark.parametrize("w,h", [(520, 330), (517, 331)])
+def test_precondition_interior_and_edge_tiles(ctx, oracle, w, h):
+    """Frames with many interior 64x64 tiles (the paired-lane loop) around
+    edge tiles (mirrored halo, border taps); 517 x 331 also has the n % 4
+    division tail on its last row."""
+    rgb = synth.synthetic_rgb(w, h, seed=w + h, bits=16)
+    bmap = synth.fixed_dct8_map(w, h)
+    req = jg.EncodeRequest(global_scale=30000, gaborish=True)
+    layout = jg.Layout(ctx, w, h, bmap)
+    st = ctx.encode_stages(layout, rgb, req, bits=16)
+    rc, ref = oracle.encode(rgb, bmap, np.ones(bmap.shape, np.uint32), bits=16,
+                            global_scale=30000, gaborish=True, stages=True)
+    assert rc == 0
+    assert np.array_equal(st["xyb"].view(np.uint32), ref["xyb"].view(np.uint32))
+    diff = np.argwhere(st["pre"].view(np.uint32) != ref["pre"].view(np.uint32))
+    assert diff.size == 0, (len(diff), diff[:5])
+
+
 def test_xyb_of_every_16bit_code_point(ctx, oracle):
     """All 65536 code points per channel pass the exact-parity cube root."""
     w, h = 256, 256
