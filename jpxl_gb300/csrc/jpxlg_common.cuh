@@ -187,15 +187,13 @@ __device__ __forceinline__ f2 f2_pack(float lo, float hi) {
   return r;
 }
 __device__ __forceinline__ float f2_lo(f2 v) {
-  float a, b;
-  asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(v));
-  (void)b;
+  float a;
+  asm("mov.b64 {%0, _}, %1;" : "=f"(a) : "l"(v));
   return a;
 }
 __device__ __forceinline__ float f2_hi(f2 v) {
-  float a, b;
-  asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(v));
-  (void)a;
+  float b;
+  asm("mov.b64 {_, %0}, %1;" : "=f"(b) : "l"(v));
   return b;
 }
 __device__ __forceinline__ f2 f2_add(f2 a, f2 b) {

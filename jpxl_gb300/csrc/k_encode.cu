@@ -135,7 +135,7 @@ static __device__ __noinline__ float precondition_tail(float mm, float fv, float
   return mm + (fv - kx) / centre;
 }
 
-__global__ void __launch_bounds__(kPreThreads) k_precondition(const float* __restrict__ in,
+__global__ void __launch_bounds__(kPreThreads, 2) k_precondition(const float* __restrict__ in,
                                                               float* __restrict__ out, int w,
                                                               int h, EncKernel k) {
   extern __shared__ __align__(16) float pre_smem[];
@@ -173,24 +173,31 @@ __global__ void __launch_bounds__(kPreThreads) k_precondition(const float* __res
   // formula with no per-cell tests.  Other tiles take the general loop.
   const bool fast = !has_halo_out && gx0 + kPreS - 2 <= 4 * groups &&
                     (bulk == n || gy0 + kPreS - 2 < bulk_row);
+  // Every step runs the paired loop over the whole update region.  On edge
+  // tiles that loop also writes cells whose reference arithmetic differs
+  // (frame border, columns past the SIMD groups, the division tail) and
+  // cells outside the frame; a second pass recomputes the former with the
+  // scalar rules and a third copies mirrored values into the latter.
+  const int simd_end = min(w - 1, 4 * groups + 1);  // frame x in [1, simd_end) is SIMD
+  const int row_end = bulk == n ? h - 1 : min(h - 1, bulk_row);  // rows below take the tail rule
+  const f2 c2 = f2_pack(k.centre, k.centre), e2 = f2_pack(k.edge, k.edge);
+  const f2 k2 = f2_pack(k.corner, k.corner), i2 = f2_pack(k.inv_c, k.inv_c);
+  const f2 nz = f2_pack(k.neg_zero, k.neg_zero);
+  const int t = threadIdx.x;
   int cur = 0;
-  if (fast) {
-    // Paired lanes: each thread updates two adjacent columns with f32x2
-    // arithmetic; the formula and its operation order are the scalar ones.
-    const f2 c2 = f2_pack(k.centre, k.centre), e2 = f2_pack(k.edge, k.edge);
-    const f2 k2 = f2_pack(k.corner, k.corner), i2 = f2_pack(k.inv_c, k.inv_c);
-    const f2 nz = f2_pack(k.neg_zero, k.neg_zero);
-    const int t = threadIdx.x;
-    for (int it = 0; it < 12; ++it) {
-      const PreStep ps = c_pre_steps[it];
-      const int lo = 1 + it, hi = kPreS - 1 - it;
-      const float* X = cur ? X1 : X0;
-      float* Y = cur ? X0 : X1;
+  for (int it = 0; it < 12; ++it) {
+    const PreStep ps = c_pre_steps[it];
+    const int lo = 1 + it, hi = kPreS - 1 - it;
+    const float* X = cur ? X1 : X0;
+    float* Y = cur ? X0 : X1;
+    {
       const int band = (int)(((unsigned)t * (unsigned)ps.mg) >> 16);
       const int c0 = 2 * (ps.p_lo + t - band * ps.np);
       const int ly0 = lo + band * ps.rows, ly1 = min(ly0 + ps.rows, hi);
       if (band < ps.bands && ly0 < ly1) {
-        const bool st_lo = c0 >= lo, st_hi = c0 + 1 < hi;
+        // A pair straddling the region's edge also writes the column just
+        // outside it; no later step, fixup, mirror copy or output reads that
+        // column of this plane (each step reads only the previous region).
         int c = ly0 * kPreS + c0;
         f2 Mn = *reinterpret_cast<const f2*>(X + c - kPreS);
         f2 Wn = f2_pack(X[c - kPreS - 1], f2_lo(Mn)), En = f2_pack(f2_hi(Mn), X[c - kPreS + 2]);
@@ -209,47 +216,41 @@ __global__ void __launch_bounds__(kPreThreads) k_precondition(const float* __res
               f2_add(f2_add(f2_mul(Mm, c2, nz), f2_mul(s1, e2, nz)), f2_mul(s2, k2, nz));
           const f2 u =
               f2_add(Mm, f2_mul(f2_sub(*reinterpret_cast<const f2*>(F + c), kx), i2, nz));
-          if (st_lo && st_hi) *reinterpret_cast<f2*>(Y + c) = u;
-          else if (st_lo) Y[c] = f2_lo(u);
-          else if (st_hi) Y[c + 1] = f2_hi(u);
+          *reinterpret_cast<f2*>(Y + c) = u;
           Mn = Mm; Wn = Wm; En = Em;
           Mm = Ms; Wm = Ws; Em = Es;
         }
       }
-      __syncthreads();
-      cur ^= 1;
     }
-  }
-  for (int it = 0; it < (fast ? 0 : 12); ++it) {
-    const int r = kPreHalo - 1 - it;  // cells within r of the tile are updated
-    const int lo = kPreHalo - r, hi = kPreHalo + kPreTile + r;  // local [lo, hi)
-    const float* xs = cur ? X1 : X0;
-    float* xn = cur ? X0 : X1;
-    // Same chunk / band mapping as the interior loop.
-    const int wd = hi - lo;
-    const int nch = (wd + 31) >> 5;
-    const int chunk = warp % nch;
-    const int nb = (kWarps - chunk + nch - 1) / nch;
-    const int rows = (wd + nb - 1) / nb;
-    const int ly0 = lo + (warp / nch) * rows, ly1 = min(ly0 + rows, hi);
-    const int lx = lo + chunk * 32 + lane;
-    if (lx < hi && ly0 < ly1) {
-      const int gx = gx0 + lx;
-      const bool in_x = gx >= 0 && gx < w;
-      const bool edge_x = gx == 0 || gx == w - 1;
-      const bool simd_x = gx - 1 < 4 * groups;
-      const float* p = xs + (ly0 - 1) * kPreS + lx;
-      float nw = p[-1], nn = p[0], ne = p[1];
-      p += kPreS;
-      float ww = p[-1], mm = p[0], ee = p[1];
-      for (int ly = ly0; ly < ly1; ++ly) {
-        p += kPreS;
-        const float sw = p[-1], ss = p[0], se = p[1];
+    __syncthreads();
+    if (!fast) {
+      // Cells whose arithmetic is not the interior formula: whole rows at
+      // the frame's top and bottom (and from the tail row down), and on
+      // the other rows column 0 and the columns from simd_end to w - 1.
+      const int left = -gx0;  // local column of frame x = 0
+      const bool has_left = left >= lo && left < hi;
+      const int r0 = max(max(lo, simd_end - gx0), has_left ? left + 1 : lo);
+      const int r1 = min(hi, w - gx0);
+      const int nright = max(0, r1 - r0);
+      for (int ly = lo + warp; ly < hi; ly += kWarps) {
         const int gy = gy0 + ly;
-        if (in_x && gy >= 0 && gy < h) {
-          const bool border = edge_x || gy == 0 || gy == h - 1;
+        if (gy < 0 || gy >= h) continue;
+        const bool full = gy == 0 || gy >= row_end;
+        const int ncell = full ? hi - lo : (has_left ? 1 : 0) + nright;
+        for (int i = lane; i < ncell; i += 32) {
+          int lx;
+          if (full) lx = lo + i;
+          else if (has_left) lx = i == 0 ? left : r0 + i - 1;
+          else lx = r0 + i;
+          const int gx = gx0 + lx;
+          if (gx < 0 || gx >= w) continue;
+          const float* q = X + ly * kPreS + lx;
+          const float nw = q[-kPreS - 1], nn = q[-kPreS], ne = q[-kPreS + 1];
+          const float ww = q[-1], mm = q[0], ee = q[1];
+          const float sw = q[kPreS - 1], ss = q[kPreS], se = q[kPreS + 1];
+          const bool border = gx == 0 || gx == w - 1 || gy == 0 || gy == h - 1;
           float kx;
-          if (!border && simd_x) {
+          if (!border && gx - 1 < 4 * groups) {
             kx = mm * k.centre + (nn + ss + ww + ee) * k.edge + (nw + ne + sw + se) * k.corner;
           } else {
             // nine taps in order: dy = -1, 0, 1 outer, dx inner
@@ -266,16 +267,13 @@ __global__ void __launch_bounds__(kPreThreads) k_precondition(const float* __res
             kx = acc;
           }
           const int c = ly * kPreS + lx;
-          const float fv = F[c];
           const bool in_bulk = gy < bulk_row || (gy == bulk_row && gx < bulk_col);
-          if (in_bulk) xn[c] = mm + (fv - kx) * k.inv_c;
-          else xn[c] = precondition_tail(mm, fv, kx, k.centre);
+          if (in_bulk) Y[c] = mm + (F[c] - kx) * k.inv_c;
+          else Y[c] = precondition_tail(mm, F[c], kx, k.centre);
         }
-        nw = ww; nn = mm; ne = ee;
-        ww = sw; mm = ss; ee = se;
       }
+      __syncthreads();
     }
-    __syncthreads();
     // Out-of-frame halo cells take their mirror's new value: whole rows
     // above or below the frame, and the bands left [lo, xl) and right
     // [xr, hi) of it on the rows inside.
@@ -288,11 +286,11 @@ __global__ void __launch_bounds__(kPreThreads) k_precondition(const float* __res
         const int my = mirror1d(gy, h) - gy0;
         if (gy < 0 || gy >= h) {
           for (int cx = lo + lane; cx < hi; cx += 32)
-            xn[ly * kPreS + cx] = xn[my * kPreS + mirror1d(gx0 + cx, w) - gx0];
+            Y[ly * kPreS + cx] = Y[my * kPreS + mirror1d(gx0 + cx, w) - gx0];
         } else {
           for (int i = lane; i < nl + nr; i += 32) {
             const int cx = i < nl ? lo + i : xr + (i - nl);
-            xn[ly * kPreS + cx] = xn[ly * kPreS + mirror1d(gx0 + cx, w) - gx0];
+            Y[ly * kPreS + cx] = Y[ly * kPreS + mirror1d(gx0 + cx, w) - gx0];
           }
         }
       }
