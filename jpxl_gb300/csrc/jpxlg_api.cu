@@ -70,7 +70,7 @@ struct jpxlg_ctx {
   DevBuf rgb, xyb, pre, coeff, dyhf, qcoeff, lfs, dylf, lfq, cflx, cflb;
   DevBuf planes, aux, sigma, out;
   DevBuf lf_part, lf_seed;
-  DevBuf pyr, partial, score;
+  DevBuf pyr, partial, score, cxyb;
   // stage timers
   struct Mark {
     int stage;
@@ -311,7 +311,7 @@ int encode_device(jpxlg_ctx* ctx, const jpxlg_layout* L, const void* rgb_dev, in
 int render_device(jpxlg_ctx* ctx, const jpxlg_layout* L, const int32_t* qcoeff,
                   const int32_t* lfq, const int8_t* cflx, const int8_t* cflb, int fx_biased,
                   int fb_biased, const int* lf_dev_unbiased, const jpxlg_params* p, int out_kind,
-                  int bits, void* out_dev) {
+                  int bits, void* out_dev, float* pxyb_dev = nullptr) {
   const Geo& g = L->geo;
   const size_t n = (size_t)g.w * g.h, nb = (size_t)g.bw * g.bh;
   CK(ctx->planes.ensure(3 * n * sizeof(float)));
@@ -371,22 +371,21 @@ int render_device(jpxlg_ctx* ctx, const jpxlg_layout* L, const int32_t* qcoeff,
   }
   stage_begin(ctx, JPXLG_STAGE_COLOUR);
   launch_colour_out(cur, g.w, g.h, out_kind, dt ? dt->thr : nullptr, dt ? dt->lev : nullptr,
-                    dt ? dt->levels : 0, out_dev, ctx->num_sms, ctx->stream);
+                    dt ? dt->levels : 0, out_dev, pxyb_dev, ctx->num_sms, ctx->stream);
   rc = after_launch(ctx, 1);
   stage_end(ctx);
   return rc;
 }
 
-int score_device(jpxlg_ctx* ctx, const jpxlg_ref* ref, const float* cand_dev, double* out_dev) {
+// Candidate side of SSIMULACRA2 against `ref`: cand_dev is the candidate's
+// linear RGB; cand_xyb (optional) its positive XYB, when the producer of the
+// pixels already formed it.  Each pyramid level keeps linear RGB (for the
+// next level) and positive XYB (for the tile kernel).
+int score_device(jpxlg_ctx* ctx, const jpxlg_ref* ref, const float* cand_dev,
+                 const float* cand_xyb, double* out_dev) {
   const int w = ref->w, h = ref->h;
-  // candidate pyramid (scales 1..): sum of quarter-ish planes
   size_t pyr = 0;
-  int cw = w, ch = h;
-  for (int s = 1; s < ref->nscales; ++s) {
-    cw = (cw + 1) / 2;
-    ch = (ch + 1) / 2;
-    pyr += 3 * (size_t)cw * ch;
-  }
+  for (int s = 1; s < ref->nscales; ++s) pyr += 6 * (size_t)ref->scales[s].w * ref->scales[s].h;
   CK(ctx->pyr.ensure(std::max<size_t>(pyr, 1) * sizeof(float)));
   size_t ctas_total = 0;
   for (int s = 0; s < ref->nscales; ++s)
@@ -394,19 +393,29 @@ int score_device(jpxlg_ctx* ctx, const jpxlg_ref* ref, const float* cand_dev, do
   CK(ctx->partial.ensure(ctas_total * 18 * sizeof(DF)));
   int ctas[6], pixels[6];
   stage_begin(ctx, JPXLG_STAGE_SSIM);
+  uint64_t k = 0;
+  if (!cand_xyb) {
+    CK(ctx->cxyb.ensure(3 * (size_t)w * h * sizeof(float)));
+    launch_positive_xyb(cand_dev, ctx->cxyb.as<float>(), (size_t)w * h, ctx->num_sms, ctx->stream);
+    ++k;
+    cand_xyb = ctx->cxyb.as<float>();
+  }
   const float* cur = cand_dev;
+  const float* cur_xyb = cand_xyb;
   float* next = ctx->pyr.as<float>();
   DF* part = ctx->partial.as<DF>();
-  uint64_t k = 0;
   for (int s = 0; s < ref->nscales; ++s) {
     const SsimScale& rs = ref->scales[s];
     if (s > 0) {
-      launch_downscale3(cur, ref->scales[s - 1].w, ref->scales[s - 1].h, next, ctx->stream);
+      const size_t ns = (size_t)rs.w * rs.h;
+      launch_downscale3(cur, ref->scales[s - 1].w, ref->scales[s - 1].h, next, next + 3 * ns,
+                        ctx->stream);
       ++k;
       cur = next;
-      next += 3 * (size_t)rs.w * rs.h;
+      cur_xyb = next + 3 * ns;
+      next += 6 * ns;
     }
-    ctas[s] = launch_score_scale(cur, rs, part, ctx->num_sms, ctx->stream);
+    ctas[s] = launch_score_scale(cur_xyb, false, rs, part, ctx->num_sms, ctx->stream);
     ++k;
     pixels[s] = rs.w * rs.h;
     part += (size_t)ctas[s] * 18;
@@ -480,7 +489,7 @@ int jpxlg_ctx_destroy(jpxlg_ctx* ctx) {
                     &ctx->qcoeff, &ctx->lfs,   &ctx->dylf,    &ctx->lfq,     &ctx->cflx,
                     &ctx->cflb,   &ctx->planes, &ctx->aux,    &ctx->sigma,   &ctx->out,
                     &ctx->lf_part, &ctx->lf_seed, &ctx->pyr,  &ctx->partial,
-                    &ctx->score};
+                    &ctx->score,  &ctx->cxyb};
   for (DevBuf* b : bufs) b->release();
   for (auto& m : ctx->marks) {
     cudaEventDestroy(m.a);
@@ -815,7 +824,7 @@ int jpxlg_ssim2_ref_create(jpxlg_ctx* ctx, const float* rgb, int w, int h, uint3
     float* rgb_s = cursor;
     cursor += 3 * n;
     if (s > 0) {
-      launch_downscale3(level, dims[s - 1][0], dims[s - 1][1], rgb_s, ctx->stream);
+      launch_downscale3(level, dims[s - 1][0], dims[s - 1][1], rgb_s, nullptr, ctx->stream);
       ++k;
       level = rgb_s;
     }
@@ -868,7 +877,8 @@ int jpxlg_ssim2_score(jpxlg_ctx* ctx, const jpxlg_ref* R, const float* rgb, uint
     CK(cudaMemcpyAsync(ctx->out.p, rgb, 3 * n * sizeof(float), cudaMemcpyHostToDevice, ctx->stream));
     cand = ctx->out.as<float>();
   }
-  int rc = score_device(ctx, R, cand, mem == JPXLG_MEM_DEVICE && score ? score : ctx->score.as<double>());
+  int rc = score_device(ctx, R, cand, nullptr,
+                        mem == JPXLG_MEM_DEVICE && score ? score : ctx->score.as<double>());
   if (rc) return rc;
   if (mem == JPXLG_MEM_DEVICE) return JPXLG_OK;
   CK(cudaMemcpyAsync(ctx->h_score, ctx->score.p, (2 + 108) * sizeof(double), cudaMemcpyDeviceToHost,
@@ -911,6 +921,7 @@ int jpxlg_probe(jpxlg_ctx* ctx, const jpxlg_layout* L, const jpxlg_ref* R, const
   CK(ctx->cflx.ensure(nt));
   CK(ctx->cflb.ensure(nt));
   CK(ctx->out.ensure(3 * n * sizeof(float)));
+  CK(ctx->cxyb.ensure(3 * n * sizeof(float)));
   CK(ctx->score.ensure(128 * sizeof(double)));
   const void* src = rgb;
   if (mem == JPXLG_MEM_HOST) {
@@ -924,10 +935,10 @@ int jpxlg_probe(jpxlg_ctx* ctx, const jpxlg_layout* L, const jpxlg_ref* R, const
   if (rc) return rc;
   rc = render_device(ctx, L, ctx->qcoeff.as<int32_t>(), ctx->lfq.as<int32_t>(),
                      ctx->cflx.as<int8_t>(), ctx->cflb.as<int8_t>(), 128, 128, ctx->d_lf, p,
-                     JPXLG_OUT_LINEAR_DEPTH, bits, ctx->out.p);
+                     JPXLG_OUT_LINEAR_DEPTH, bits, ctx->out.p, ctx->cxyb.as<float>());
   if (rc) return rc;
   double* dst = mem == JPXLG_MEM_DEVICE ? score : ctx->score.as<double>();
-  rc = score_device(ctx, R, ctx->out.as<float>(), dst);
+  rc = score_device(ctx, R, ctx->out.as<float>(), ctx->cxyb.as<float>(), dst);
   if (rc) return rc;
   if (mem == JPXLG_MEM_DEVICE) return JPXLG_OK;
   CK(cudaMemcpyAsync(ctx->h_score, ctx->score.p, sizeof(double), cudaMemcpyDeviceToHost,
@@ -1022,12 +1033,13 @@ extern "C" int jpxlg_ssim2_score_static(jpxlg_ctx* ctx, const jpxlg_ref* ref,
   for (int s = 0; s < ref->nscales; ++s) {
     const SsimScale& rs = ref->scales[s];
     if (s > 0) {
-      launch_downscale3(cur, ref->scales[s - 1].w, ref->scales[s - 1].h, next, ctx->stream);
+      launch_downscale3(cur, ref->scales[s - 1].w, ref->scales[s - 1].h, next, nullptr,
+                        ctx->stream);
       ++k;
       cur = next;
       next += 3 * (size_t)rs.w * rs.h;
     }
-    ctas[s] = launch_score_scale(cur, rs, part, ctx->num_sms, ctx->stream);
+    ctas[s] = launch_score_scale(cur, true, rs, part, ctx->num_sms, ctx->stream);
     ++k;
     pixels[s] = rs.w * rs.h;
     part += (size_t)ctas[s] * 18;

@@ -135,7 +135,10 @@ __device__ __forceinline__ float cbrt_cr_fast(float a, bool* ok) {
   float d = (q - a) + (e2 + e3);    // y^3 - a; q - a is exact (Sterbenz)
   int e = (int)((yb >> 23) & 0xffu) - 127;
   float inv_ulp = __uint_as_float((uint32_t)(127 + 23 - e) << 23);  // 2^(23-e)
-  float delta = (-d / (3.0f * p)) * inv_ulp;  // (cbrt(a) - y) in ulps of y
+  // (cbrt(a) - y) in ulps of y.  The quotient needs ~2^-20 relative accuracy
+  // only (|delta| < 2.5 against a 2^-17 decision margin), so the fast
+  // division (at most 2 ulp off) serves.
+  float delta = __fdividef(-d, 3.0f * p) * inv_ulp;
   float k = rintf(delta);
   float frac = fabsf(delta - k);
   *ok = frac < 0.5f - 7.62939453125e-06f && fabsf(delta) < 2.5f;  // 2^-17
@@ -166,6 +169,23 @@ __device__ __forceinline__ float cbrt_perceptual(float v) {
     if (ok) return copysignf(r, v);
   }
   return cbrt_perceptual_f64(v);
+}
+
+// ---- SSIMULACRA2 positive XYB (jpxl-perceptual color.rs:66) ------------------
+// Opsin mix without FMA, the metric's reproducible cube root, then
+// [14x + 0.42, y + 0.01, b - y + 0.55].
+__device__ __forceinline__ void positive_xyb(float r, float g, float b, float* o) {
+  float lm = 0.3f * r + 0.622f * g + 0.078f * b + 0.0037930734f;
+  float mm = 0.23f * r + 0.692f * g + 0.078f * b + 0.0037930734f;
+  float sm = 0.2434227f * r + 0.2047674f * g + 0.5518099f * b + 0.0037930734f;
+  float lg = cbrt_perceptual(lm) - 0.1559542f;
+  float mg = cbrt_perceptual(mm) - 0.1559542f;
+  float sg = cbrt_perceptual(sm) - 0.1559542f;
+  float x = 0.5f * (lg - mg);
+  float y = 0.5f * (lg + mg);
+  o[0] = x * 14.0f + 0.42f;
+  o[1] = y + 0.01f;
+  o[2] = (sg - y) + 0.55f;
 }
 
 // ---- paired f32 arithmetic (sm_100 family) ----------------------------------

@@ -70,8 +70,11 @@ void launch_gaborish(const float* in, float* out, int w, int h, cudaStream_t s);
 void launch_epf_step(int step, const float* in, float* out, const float* sigma, int w, int h,
                      cudaStream_t s);
 // out_kind: 1 linear f32 planes, 2 sRGB8 interleaved, 3 linear at depth
+// pxyb (optional, out_kind 3 only): also the SSIMULACRA2 positive XYB planes
+// of the output pixels.
 void launch_colour_out(const float* xyb, int w, int h, int out_kind, const float* thresholds,
-                       const float* levels, int nlevels, void* out, int num_sms, cudaStream_t s);
+                       const float* levels, int nlevels, void* out, float* pxyb, int num_sms,
+                       cudaStream_t s);
 void upload_render_constants(const float* opsin_m, const float* opsin_bias,
                              const float* opsin_bias_cbrt, cudaStream_t s);
 
@@ -83,14 +86,18 @@ struct SsimScale {
   float* s11;   // [3][w*h]
 };
 void upload_blur_taps(const float* taps, cudaStream_t s);
-void launch_downscale3(const float* in, int w, int h, float* out, cudaStream_t s);
+// 2x2 mean of linear RGB planes; xyb (optional) receives the result's
+// positive XYB planes.
+void launch_downscale3(const float* in, int w, int h, float* out, float* xyb, cudaStream_t s);
 void launch_positive_xyb(const float* rgb, float* xyb, size_t n, int num_sms, cudaStream_t s);
 void launch_ref_moments(const float* xyb, float* mu, float* s11, float* tmp, int w, int h,
                         cudaStream_t s);
 // Candidate side of one scale: cand is linear RGB [3][w*h]; partial receives
 // per-CTA double-float sums [ctas][18] (8 bytes each).
 struct DF;
-int launch_score_scale(const float* cand_rgb, const SsimScale& ref, DF* partial,
+// cand: the scale's candidate as linear RGB (cand_is_linear) or as its
+// positive XYB planes.
+int launch_score_scale(const float* cand, bool cand_is_linear, const SsimScale& ref, DF* partial,
                        int num_sms, cudaStream_t s);
 void launch_score_finish(const DF* partials, const int* ctas_per_scale, int nscales,
                          const int* pixels_per_scale, double* out /* score, raw, terms[108] */,

@@ -444,7 +444,8 @@ template <int KIND>
 __global__ void __launch_bounds__(256) k_colour_out(const float* __restrict__ xyb, size_t n,
                                                     const float* __restrict__ thr,
                                                     const float* __restrict__ levels, int nlev,
-                                                    void* __restrict__ out) {
+                                                    void* __restrict__ out,
+                                                    float* __restrict__ pxyb) {
   __shared__ float s_thr[255];
   __shared__ float s_lev[256];
   if (KIND == 2 || (KIND == 3 && nlev <= 256)) {
@@ -482,29 +483,45 @@ __global__ void __launch_bounds__(256) k_colour_out(const float* __restrict__ xy
       o[3 * i] = (uint8_t)level_of(rgb[0], T, nlev - 1);
       o[3 * i + 1] = (uint8_t)level_of(rgb[1], T, nlev - 1);
       o[3 * i + 2] = (uint8_t)level_of(rgb[2], T, nlev - 1);
-    } else if (nlev <= 256) {
-      float* o = (float*)out;
-      o[i] = LV[level_of(rgb[0], T, nlev - 1)];
-      o[n + i] = LV[level_of(rgb[1], T, nlev - 1)];
-      o[2 * n + i] = LV[level_of(rgb[2], T, nlev - 1)];
     } else {
+      float lin[3];
+      if (nlev <= 256) {
+#pragma unroll
+        for (int q = 0; q < 3; ++q) lin[q] = LV[level_of(rgb[q], T, nlev - 1)];
+      } else {
+        const float maxv = (float)(nlev - 1);
+#pragma unroll
+        for (int q = 0; q < 3; ++q) lin[q] = __ldg(&LV[level_guided(rgb[q], T, nlev - 1, maxv)]);
+      }
       float* o = (float*)out;
-      const float maxv = (float)(nlev - 1);
-      o[i] = __ldg(&LV[level_guided(rgb[0], T, nlev - 1, maxv)]);
-      o[n + i] = __ldg(&LV[level_guided(rgb[1], T, nlev - 1, maxv)]);
-      o[2 * n + i] = __ldg(&LV[level_guided(rgb[2], T, nlev - 1, maxv)]);
+      o[i] = lin[0];
+      o[n + i] = lin[1];
+      o[2 * n + i] = lin[2];
+      // The metric's positive XYB of the rendered pixel (candidate side of
+      // SSIMULACRA2's first scale), when the caller scores it next.
+      if (pxyb) {
+        float px[3];
+        positive_xyb(lin[0], lin[1], lin[2], px);
+        pxyb[i] = px[0];
+        pxyb[n + i] = px[1];
+        pxyb[2 * n + i] = px[2];
+      }
     }
   }
 }
 
 void launch_colour_out(const float* xyb, int w, int h, int out_kind, const float* thresholds,
-                       const float* levels, int nlevels, void* out, int num_sms, cudaStream_t s) {
+                       const float* levels, int nlevels, void* out, float* pxyb, int num_sms,
+                       cudaStream_t s) {
   size_t n = (size_t)w * h;
   int blocks = (int)std::min<size_t>((n + 255) / 256, (size_t)num_sms * 8);
   if (blocks < 1) blocks = 1;
-  if (out_kind == 1) k_colour_out<1><<<blocks, 256, 0, s>>>(xyb, n, thresholds, levels, nlevels, out);
-  else if (out_kind == 2) k_colour_out<2><<<blocks, 256, 0, s>>>(xyb, n, thresholds, levels, nlevels, out);
-  else k_colour_out<3><<<blocks, 256, 0, s>>>(xyb, n, thresholds, levels, nlevels, out);
+  if (out_kind == 1)
+    k_colour_out<1><<<blocks, 256, 0, s>>>(xyb, n, thresholds, levels, nlevels, out, nullptr);
+  else if (out_kind == 2)
+    k_colour_out<2><<<blocks, 256, 0, s>>>(xyb, n, thresholds, levels, nlevels, out, nullptr);
+  else
+    k_colour_out<3><<<blocks, 256, 0, s>>>(xyb, n, thresholds, levels, nlevels, out, pxyb);
 }
 
 void upload_render_constants(const float* opsin_m, const float* opsin_bias,

@@ -43,42 +43,40 @@ __device__ __forceinline__ float fir9(const float* p, int stride) {
                p[2 * stride], p[3 * stride], p[4 * stride]);
 }
 
-// S1
+// S1 — one output pixel per thread, all three channels; with `xyb` set the
+// pixel's positive XYB (S2) is written too, for the scale's candidate side.
 __global__ void __launch_bounds__(256) k_downscale3(const float* __restrict__ in, int w, int h,
-                                                    float* __restrict__ out) {
+                                                    float* __restrict__ out,
+                                                    float* __restrict__ xyb) {
   const int ow = (w + 1) / 2, oh = (h + 1) / 2;
   const size_t ip = (size_t)w * h, op = (size_t)ow * oh;
-  const int c = blockIdx.z;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < ow * oh; i += gridDim.x * blockDim.x) {
     int ox = i % ow, oy = i / ow;
     int x0 = min(2 * ox, w - 1), x1 = min(2 * ox + 1, w - 1);
     int y0 = min(2 * oy, h - 1), y1 = min(2 * oy + 1, h - 1);
-    const float* p = in + ip * c;
-    float a = p[(size_t)y0 * w + x0], b = p[(size_t)y0 * w + x1];
-    float cc = p[(size_t)y1 * w + x0], d = p[(size_t)y1 * w + x1];
-    out[op * c + i] = (a + b + cc + d) * 0.25f;
+    float v[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      const float* p = in + ip * c;
+      float a = p[(size_t)y0 * w + x0], b = p[(size_t)y0 * w + x1];
+      float cc = p[(size_t)y1 * w + x0], d = p[(size_t)y1 * w + x1];
+      v[c] = (a + b + cc + d) * 0.25f;
+      out[op * c + i] = v[c];
+    }
+    if (xyb) {
+      float o[3];
+      positive_xyb(v[0], v[1], v[2], o);
+      xyb[i] = o[0];
+      xyb[op + i] = o[1];
+      xyb[2 * op + i] = o[2];
+    }
   }
 }
 
-void launch_downscale3(const float* in, int w, int h, float* out, cudaStream_t s) {
+void launch_downscale3(const float* in, int w, int h, float* out, float* xyb, cudaStream_t s) {
   int n = ((w + 1) / 2) * ((h + 1) / 2);
-  dim3 grid(std::max(1, std::min((n + 255) / 256, 4096)), 1, 3);
-  k_downscale3<<<grid, 256, 0, s>>>(in, w, h, out);
-}
-
-// S2 — color.rs:66 (opsin mix without FMA, cbrt, [14x+0.42, y+0.01, b-y+0.55]).
-__device__ __forceinline__ void positive_xyb(float r, float g, float b, float* o) {
-  float lm = 0.3f * r + 0.622f * g + 0.078f * b + 0.0037930734f;
-  float mm = 0.23f * r + 0.692f * g + 0.078f * b + 0.0037930734f;
-  float sm = 0.2434227f * r + 0.2047674f * g + 0.5518099f * b + 0.0037930734f;
-  float lg = cbrt_perceptual(lm) - 0.1559542f;
-  float mg = cbrt_perceptual(mm) - 0.1559542f;
-  float sg = cbrt_perceptual(sm) - 0.1559542f;
-  float x = 0.5f * (lg - mg);
-  float y = 0.5f * (lg + mg);
-  o[0] = x * 14.0f + 0.42f;
-  o[1] = y + 0.01f;
-  o[2] = (sg - y) + 0.55f;
+  dim3 grid(std::max(1, std::min((n + 255) / 256, 4096)));
+  k_downscale3<<<grid, 256, 0, s>>>(in, w, h, out, xyb);
 }
 
 __global__ void __launch_bounds__(256) k_positive_xyb(const float* __restrict__ rgb,
@@ -163,31 +161,43 @@ void launch_ref_moments(const float* xyb, float* mu, float* s11, float* tmp, int
 }
 
 // S4 — candidate side of one scale, fused.  One CTA per 32x32 output tile:
-// the candidate's linear RGB becomes positive XYB over the tile plus a
-// 4-sample halo (zero outside the frame: the blur's zero padding), the
-// horizontal then vertical FIR of c, c*c and r*c run per channel in shared
-// memory, and pool.rs:248's per-pixel terms are pooled.  Every global load a
-// phase needs is issued before any of them is used, so a CTA's latency
-// chain is a handful of round trips; per-thread sums are f32, folded per
-// warp in f32 and across warps in f64 into one row of 18 sums per tile.
+// the candidate's positive XYB over the tile plus a 4-sample halo (zero
+// outside the frame: the blur's zero padding) — read from precomputed
+// planes, or converted here from linear RGB when kFromLinear — then per
+// channel the horizontal and vertical FIR of c, c*c and r*c in shared memory
+// and pool.rs:248's per-pixel terms.  Both passes are register-blocked: a
+// thread produces four adjacent outputs from twelve inputs read as float4s
+// (horizontal) or down one column (vertical).  Per-thread sums are f32,
+// folded per warp in f32 and across warps in double-float into one row of 18
+// sums per tile.
 constexpr int kST = 32;
 constexpr int kSH = 4;
-constexpr int kSS = kST + 2 * kSH;  // 40
-constexpr int kSP = kSS + 1;        // padded row
+constexpr int kSS = kST + 2 * kSH;  // 40: haloed side, rows float4-aligned
 constexpr int kScoreThreads = 256;
 constexpr int kScoreLoads = (kSS * kSS + kScoreThreads - 1) / kScoreThreads;  // 7
-constexpr size_t kScoreSmem = (6 * kSS * kSP + 3 * kSS * (kST + 1)) * sizeof(float);
+constexpr int kHItems = kSS * (kST / 4);  // 320 horizontal items: row x 4-column group
+constexpr size_t kScoreSmem = (6 * kSS * kSS + 3 * kSS * kST) * sizeof(float);
 
+// Four symmetric 9-tap FIR outputs from twelve inputs v[0..11]: output k
+// is centred on v[k + 4].
+__device__ __forceinline__ void fir9x4(const float* v, float* o) {
+#pragma unroll
+  for (int k = 0; k < 4; ++k)
+    o[k] = fir9v(v[k], v[k + 1], v[k + 2], v[k + 3], v[k + 4], v[k + 5], v[k + 6], v[k + 7],
+                 v[k + 8]);
+}
+
+template <bool kFromLinear>
 __global__ void __launch_bounds__(kScoreThreads, 3) k_score_tile(const float* __restrict__ cand,
                                                               const float* __restrict__ rxyb,
                                                               const float* __restrict__ rmu,
                                                               const float* __restrict__ rs11,
                                                               int w, int h,
                                                               DF* __restrict__ partial) {
-  extern __shared__ float ssm[];
-  float* cx = ssm;                      // [3][kSS][kSP]
-  float* rx = ssm + 3 * kSS * kSP;      // [3][kSS][kSP]
-  float* hp = ssm + 6 * kSS * kSP;      // [3][kSS][kST + 1]
+  extern __shared__ __align__(16) float ssm[];
+  float* cx = ssm;                      // [3][kSS][kSS] candidate positive XYB
+  float* rx = ssm + 3 * kSS * kSS;      // [3][kSS][kSS] reference positive XYB
+  float* hp = ssm + 6 * kSS * kSS;      // [3][kSS][kST] horizontal pass of c, c*c, r*c
   __shared__ float red[kScoreThreads / 32][18];
   const size_t n = (size_t)w * h;
   const int lane = threadIdx.x % 32, warp = threadIdx.x / 32;
@@ -214,88 +224,111 @@ __global__ void __launch_bounds__(kScoreThreads, 3) k_score_tile(const float* __
       if (i >= kSS * kSS) continue;
       const int lx = i % kSS, ly = i / kSS;
       const int gx = x0 + lx, gy = y0 + ly;
-      float o[3] = {0.0f, 0.0f, 0.0f};
-      if (gx >= 0 && gy >= 0 && gx < w && gy < h) positive_xyb(v[k][0], v[k][1], v[k][2], o);
+      const bool ok = gx >= 0 && gy >= 0 && gx < w && gy < h;
+      float o[3] = {v[k][0], v[k][1], v[k][2]};
+      if (kFromLinear) {
+        o[0] = o[1] = o[2] = 0.0f;
+        if (ok) positive_xyb(v[k][0], v[k][1], v[k][2], o);
+      }
 #pragma unroll
       for (int q = 0; q < 3; ++q) {
-        cx[(q * kSS + ly) * kSP + lx] = o[q];
-        rx[(q * kSS + ly) * kSP + lx] = v[k][3 + q];
+        cx[(q * kSS + ly) * kSS + lx] = o[q];
+        rx[(q * kSS + ly) * kSS + lx] = v[k][3 + q];
       }
     }
   }
-  float sums[18];
-#pragma unroll
-  for (int k = 0; k < 18; ++k) sums[k] = 0.0f;
   const float C2 = 0.0009f;
-  constexpr int kRowsPerWarp = kST / (kScoreThreads / 32);  // 4 output rows per warp
-#pragma unroll
+  // Vertical pass: column j = lane, output rows 4 * warp .. 4 * warp + 3.
+  const int oj = lane, oi0 = 4 * warp;
+  const int gxo = x0 + kSH + oj;
+#pragma unroll 1
   for (int c = 0; c < 3; ++c) {
-    // this thread's pooled pixels: rows warp + 8j, column lane
-    float m1[kRowsPerWarp], v11[kRowsPerWarp];
+    float m1[4], v11[4];
 #pragma unroll
-    for (int j = 0; j < kRowsPerWarp; ++j) {
-      const int gx = x0 + kSH + lane, gy = y0 + kSH + warp + 8 * j;
-      const bool ok = gx < w && gy < h;
-      const size_t p = n * c + (ok ? (size_t)gy * w + gx : 0);
-      m1[j] = ok ? rmu[p] : 0.0f;
-      v11[j] = ok ? rs11[p] : 0.0f;
+    for (int k = 0; k < 4; ++k) {
+      const int gy = y0 + kSH + oi0 + k;
+      const bool ok = gxo < w && gy < h;
+      const size_t p = n * c + (ok ? (size_t)gy * w + gxo : 0);
+      m1[k] = ok ? rmu[p] : 0.0f;
+      v11[k] = ok ? rs11[p] : 0.0f;
     }
     __syncthreads();
-    const float* cc = cx + c * kSS * kSP;
-    const float* rr = rx + c * kSS * kSP;
-    // horizontal: rows 0..39, output columns 0..31 (lane = column)
-    for (int ly = warp; ly < kSS; ly += kScoreThreads / 32) {
-      const float* pc = cc + ly * kSP + lane;
-      const float* pr = rr + ly * kSP + lane;
-      float c0 = pc[0], c1 = pc[1], c2 = pc[2], c3 = pc[3], c4 = pc[4], c5 = pc[5], c6 = pc[6],
-            c7 = pc[7], c8 = pc[8];
-      hp[(0 * kSS + ly) * (kST + 1) + lane] = fir9v(c0, c1, c2, c3, c4, c5, c6, c7, c8);
-      hp[(1 * kSS + ly) * (kST + 1) + lane] =
-          fir9v(c0 * c0, c1 * c1, c2 * c2, c3 * c3, c4 * c4, c5 * c5, c6 * c6, c7 * c7, c8 * c8);
-      hp[(2 * kSS + ly) * (kST + 1) + lane] =
-          fir9v(pr[0] * c0, pr[1] * c1, pr[2] * c2, pr[3] * c3, pr[4] * c4, pr[5] * c5,
-                pr[6] * c6, pr[7] * c7, pr[8] * c8);
+    const float* cc = cx + c * kSS * kSS;
+    const float* rr = rx + c * kSS * kSS;
+    // Horizontal pass: item = (row y, columns 4g .. 4g+3), inputs 4g .. 4g+11.
+    for (int it = threadIdx.x; it < kHItems; it += kScoreThreads) {
+      const int y = it / (kST / 4), g = it % (kST / 4);
+      const float4* pc = reinterpret_cast<const float4*>(cc + y * kSS + 4 * g);
+      const float4* pr = reinterpret_cast<const float4*>(rr + y * kSS + 4 * g);
+      float a[12], sq[12], cr[12];
+#pragma unroll
+      for (int q = 0; q < 3; ++q) {
+        const float4 u = pc[q], r = pr[q];
+        a[4 * q] = u.x; a[4 * q + 1] = u.y; a[4 * q + 2] = u.z; a[4 * q + 3] = u.w;
+        cr[4 * q] = r.x * u.x; cr[4 * q + 1] = r.y * u.y;
+        cr[4 * q + 2] = r.z * u.z; cr[4 * q + 3] = r.w * u.w;
+      }
+#pragma unroll
+      for (int q = 0; q < 12; ++q) sq[q] = a[q] * a[q];
+      float o[4];
+      fir9x4(a, o);
+      *reinterpret_cast<float4*>(hp + (0 * kSS + y) * kST + 4 * g) = make_float4(o[0], o[1], o[2], o[3]);
+      fir9x4(sq, o);
+      *reinterpret_cast<float4*>(hp + (1 * kSS + y) * kST + 4 * g) = make_float4(o[0], o[1], o[2], o[3]);
+      fir9x4(cr, o);
+      *reinterpret_cast<float4*>(hp + (2 * kSS + y) * kST + 4 * g) = make_float4(o[0], o[1], o[2], o[3]);
     }
     __syncthreads();
+    float sums[6] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+    float m2[4], s22[4], s12[4];
+    {
+      float col[12];
 #pragma unroll
-    for (int j = 0; j < kRowsPerWarp; ++j) {
-      const int oy = warp + 8 * j, ox = lane;
-      const int gx = x0 + kSH + ox, gy = y0 + kSH + oy;
-      if (gx >= w || gy >= h) continue;
-      const int r = (oy + kSH) * (kST + 1) + ox;
-      const float m2 = fir9(&hp[0 * kSS * (kST + 1) + r], kST + 1);
-      const float s22 = fir9(&hp[1 * kSS * (kST + 1) + r], kST + 1);
-      const float s12 = fir9(&hp[2 * kSS * (kST + 1) + r], kST + 1);
-      const float i1 = rr[(oy + kSH) * kSP + ox + kSH], i2 = cc[(oy + kSH) * kSP + ox + kSH];
-      const float mu11 = m1[j] * m1[j], mu22 = m2 * m2, mu12 = m1[j] * m2;
-      const float md = m1[j] - m2;
+      for (int q = 0; q < 12; ++q) col[q] = hp[(0 * kSS + oi0 + q) * kST + oj];
+      fir9x4(col, m2);
+#pragma unroll
+      for (int q = 0; q < 12; ++q) col[q] = hp[(1 * kSS + oi0 + q) * kST + oj];
+      fir9x4(col, s22);
+#pragma unroll
+      for (int q = 0; q < 12; ++q) col[q] = hp[(2 * kSS + oi0 + q) * kST + oj];
+      fir9x4(col, s12);
+    }
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const int gy = y0 + kSH + oi0 + k;
+      if (gxo >= w || gy >= h) continue;
+      const int ctr = (oi0 + k + kSH) * kSS + oj + kSH;
+      const float i1 = rr[ctr], i2 = cc[ctr];
+      const float mu11 = m1[k] * m1[k], mu22 = m2[k] * m2[k], mu12 = m1[k] * m2[k];
+      const float md = m1[k] - m2[k];
       const float num_m = 1.0f - md * md;
-      const float num_s = 2.0f * (s12 - mu12) + C2;
-      const float den_s = (v11[j] - mu11) + (s22 - mu22) + C2;
+      const float num_s = 2.0f * (s12[k] - mu12) + C2;
+      const float den_s = (v11[k] - mu11) + (s22[k] - mu22) + C2;
       const float d = fmaxf(1.0f - (num_m * num_s) / den_s, 0.0f);
       const float d2 = d * d;
       // (1 + |i2-m2|) / (1 + |i1-m1|) - 1, written as a difference over the
       // denominator so that the result keeps its relative precision.
-      const float a1 = fabsf(i1 - m1[j]), a2 = fabsf(i2 - m2);
+      const float a1 = fabsf(i1 - m1[k]), a2 = fabsf(i2 - m2[k]);
       const float d1 = (a2 - a1) / (1.0f + a1);
       const float art = fmaxf(d1, 0.0f), lost = fmaxf(-d1, 0.0f);
       const float art2 = art * art, lost2 = lost * lost;
-      sums[c * 6 + 0] += d;
-      sums[c * 6 + 1] += d2 * d2;
-      sums[c * 6 + 2] += art;
-      sums[c * 6 + 3] += art2 * art2;
-      sums[c * 6 + 4] += lost;
-      sums[c * 6 + 5] += lost2 * lost2;
+      sums[0] += d;
+      sums[1] += d2 * d2;
+      sums[2] += art;
+      sums[3] += art2 * art2;
+      sums[4] += lost;
+      sums[5] += lost2 * lost2;
+    }
+    // This channel's sums: warp fold in f32 (the warps are combined below).
+#pragma unroll
+    for (int k = 0; k < 6; ++k) {
+      float v = sums[k];
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+      if (lane == 0) red[warp][c * 6 + k] = v;
     }
   }
-  // warp fold in f32, then the 8 warps in order in double-float
-#pragma unroll
-  for (int k = 0; k < 18; ++k) {
-    float v = sums[k];
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    if (lane == k) red[warp][k] = v;
-  }
+  // the 8 warps in order in double-float
   __syncthreads();
   if (threadIdx.x < 18) {
     DF t{red[0][threadIdx.x], 0.0f};
@@ -304,14 +337,21 @@ __global__ void __launch_bounds__(kScoreThreads, 3) k_score_tile(const float* __
   }
 }
 
-int launch_score_scale(const float* cand_rgb, const SsimScale& ref, DF* partial,
+int launch_score_scale(const float* cand, bool cand_is_linear, const SsimScale& ref, DF* partial,
                        int num_sms, cudaStream_t s) {
   (void)num_sms;
-  cudaFuncSetAttribute(k_score_tile, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                       (int)kScoreSmem);
   dim3 grid((ref.w + kST - 1) / kST, (ref.h + kST - 1) / kST);
-  k_score_tile<<<grid, kScoreThreads, kScoreSmem, s>>>(cand_rgb, ref.xyb, ref.mu, ref.s11, ref.w,
-                                                       ref.h, partial);
+  if (cand_is_linear) {
+    cudaFuncSetAttribute(k_score_tile<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)kScoreSmem);
+    k_score_tile<true><<<grid, kScoreThreads, kScoreSmem, s>>>(cand, ref.xyb, ref.mu, ref.s11,
+                                                                ref.w, ref.h, partial);
+  } else {
+    cudaFuncSetAttribute(k_score_tile<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)kScoreSmem);
+    k_score_tile<false><<<grid, kScoreThreads, kScoreSmem, s>>>(cand, ref.xyb, ref.mu, ref.s11,
+                                                                 ref.w, ref.h, partial);
+  }
   return (int)(grid.x * grid.y);
 }
 
