@@ -363,10 +363,12 @@ def run_ours(args):
     per_launch_s = top_ms / 1e3 / max(top_launches, 1)
     achieved = bytes_per_launch / per_launch_s / 1e9
     peak, peak_kind = measured_peaks()
+    # DRAM bytes per launch of the stage's kernel from the committed ncu capture
+    # of this workload (single-kernel stages only).
     traffic = None
-    tf = ROOT / "profiles" / "traffic.json"
-    if tf.exists():
-        traffic = json.loads(tf.read_text()).get(top)
+    tf = ROOT / "profiles" / "traffic_2048x2048_rgb16.json"
+    if tf.exists() and (W, H) == (2048, 2048) and top in STAGE_KERNEL:
+        traffic = json.loads(tf.read_text()).get(STAGE_KERNEL[top])
 
     # CPU baseline: the restatement on a bounded sample, one thread.
     cpu_value = None
@@ -408,6 +410,11 @@ def run_ours(args):
     print(json.dumps(line), flush=True)
     if world > 1:
         dist.destroy_process_group()
+
+
+# Stages that are one kernel launch per image, and that kernel.
+STAGE_KERNEL = {"precondition": "k_precondition", "gaborish": "k_gaborish", "xyb": "k_srgb_to_xyb",
+                "colour": "k_colour_out"}
 
 
 def main():
