@@ -12,6 +12,9 @@ reference's evaluator does (evaluator.rs:88 -> reference.rs:90).
 Prints one JSON line.  `value` is source MPix/s with inputs resident in HBM;
 `e2e` is the same metric through the C ABI with pinned host buffers (the H2D
 copy of each image and the D2H read of each score inside the timed region).
+`parity` states the CUDA path's errors against the CPU restatement on the CPU
+sample; `search` times the batched quality search (64 uneven RGB8 frames x 8
+candidate quantizers = 512 probes in one CUDA graph launch).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 """
@@ -151,8 +154,9 @@ def make_workload(rank: int, world: int):
     return images, np
 
 
-def cpu_probe(rgb, cover, np):
-    """The CPU restatement's probe on one image (encode, render at depth, score)."""
+def cpu_probe(rgb, cover, np, full=False):
+    """The CPU restatement's probe on one image (encode, render at depth, score);
+    with `full`, also its plan and rendered planes."""
     import jpxl_gb300 as jg
     from oracle import loader
 
@@ -165,7 +169,33 @@ def cpu_probe(rgb, cover, np):
                                  gaborish=True, epf_iters=3, out_kind=3, bits=BITS)
     assert rc == 0
     src = jg.srgb_to_linear_planes(rgb, BITS)
-    return loader.ssim2(src, lin)[0]
+    score = loader.ssim2(src, lin)[0]
+    return (plan, lin, score) if full else score
+
+
+def gpu_parity(ctx, crop, ccover, oracle_out, np):
+    """Errors of the CUDA path against the CPU restatement on the timed CPU sample."""
+    import jpxl_gb300 as jg
+
+    plan_c, lin_c, score_c = oracle_out
+    h, w = crop.shape[:2]
+    req = jg.EncodeRequest.with_global_scale(GLOBAL_SCALE, gaborish=True, epf_iters=3)
+    layout = jg.Layout(ctx, w, h, ccover, 1, 7)
+    plan = ctx.encode_transform(layout, crop, req)
+    lin = jg.PlanRenderer(ctx).render(layout, plan, req, out="linear_at_depth", bits=BITS)
+    ref = jg.PrecomputedReference(ctx, jg.srgb_to_linear_planes(crop, BITS))
+    score = ctx.probe(layout, ref, crop, req, BITS)
+    ref.close()
+    layout.close()
+    return {
+        "sample": f"the CPU sample ({w}x{h} crop); restatement of the reference's arithmetic",
+        "qcoeff_mismatches": int(np.count_nonzero(plan.qcoeff != plan_c["qcoeff"])),
+        "lf_mismatches": int(np.count_nonzero(plan.lf != plan_c["lf"])),
+        "cfl_mismatches": int(np.count_nonzero(plan.cfl_x != plan_c["cfl_x"]) +
+                              np.count_nonzero(plan.cfl_b != plan_c["cfl_b"])),
+        "pixel_max_abs": float(np.max(np.abs(lin.astype(np.float64) - lin_c))),
+        "score_abs_diff": float(abs(score - score_c)),
+    }
 
 
 CPU_SAMPLE = 512  # crop side of the bounded CPU sample
@@ -225,6 +255,81 @@ def run_reference(args):
         "e2e": {"value": round(value, 4), "unit": "MPix/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }), flush=True)
+
+
+SEARCH_IMAGES = 64
+SEARCH_CANDIDATES = (16000, 22000, 30000, 40000, 52000, 68000, 90000, 120000)
+SEARCH_THRESHOLD = 85.0
+
+
+def search_workload(np):
+    """64 RGB8 frames of uneven sizes, w ~ U[256, 3840], h ~ U[256, 2160], cut
+    at seeded offsets from four seeded 3840x2160 generator images."""
+    from jpxl_gb300 import synth
+
+    masters = [synth.synthetic_rgb(3840, 2160, seed=9000 + m, bits=8) for m in range(4)]
+    rng = np.random.default_rng(2024)
+    frames = []
+    for i in range(SEARCH_IMAGES):
+        w, h = int(rng.integers(256, 3841)), int(rng.integers(256, 2161))
+        x0, y0 = int(rng.integers(0, 3840 - w + 1)), int(rng.integers(0, 2160 - h + 1))
+        rgb = np.ascontiguousarray(masters[i % 4][y0:y0 + h, x0:x0 + w])
+        frames.append((rgb, synth.activity_cover(rgb)))
+    return frames
+
+
+def run_search(ctx, torch, np, steps):
+    """The batched quality search: every frame x every candidate quantizer as
+    one graph launch of 512 probes; the chosen quantizer per frame is the
+    coarsest whose score reaches the threshold."""
+    import jpxl_gb300 as jg
+
+    frames = search_workload(np)
+    items, keep = [], []
+    for rgb, cover in frames:
+        h, w = rgb.shape[:2]
+        layout = jg.Layout(ctx, w, h, cover, 1, 7)
+        ref = jg.PrecomputedReference(ctx, jg.srgb_to_linear_planes(rgb, 8))
+        dev = torch.from_numpy(rgb).cuda()
+        keep.append((layout, ref, dev))
+        for gs in SEARCH_CANDIDATES:
+            items.append(jg.BatchItem(layout, ref, dev.data_ptr(), 8,
+                                      jg.EncodeRequest.with_global_scale(gs, gaborish=True,
+                                                                         epf_iters=3)))
+    torch.cuda.synchronize()
+    batch = jg.BatchProbe(ctx, items, lanes=4)
+    scores = torch.zeros(len(items), dtype=torch.float64, device="cuda")
+    stream = torch.cuda.current_stream()
+    for _ in range(2):
+        batch.run_device(scores.data_ptr())
+    ctx.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(steps):
+        batch.run_device(scores.data_ptr())
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / steps
+    px = sum(rgb.shape[0] * rgb.shape[1] for rgb, _ in frames) * len(SEARCH_CANDIDATES)
+    sc = scores.cpu().numpy().reshape(len(frames), len(SEARCH_CANDIDATES))
+    chosen = []
+    for row in sc:
+        ok = [gs for gs, v in zip(SEARCH_CANDIDATES, row) if v >= SEARCH_THRESHOLD]
+        chosen.append(min(ok) if ok else None)
+    batch.close()
+    for layout, ref, _ in keep:
+        ref.close()
+        layout.close()
+    return {
+        "workload": (f"{len(frames)} RGB8 frames of uneven sizes (w 256-3840, h 256-2160) x "
+                     f"{len(SEARCH_CANDIDATES)} candidate global scales = {len(items)} probes "
+                     "(encode, render at depth, SSIMULACRA2) as one CUDA graph launch"),
+        "value": round(px / (ms / 1e3) / 1e6, 2), "unit": "MPix/s (rendered+scored)",
+        "ms_per_batch": round(ms, 2), "steps": steps, "lanes": 4,
+        "threshold": SEARCH_THRESHOLD,
+        "frames_meeting_threshold": sum(c is not None for c in chosen),
+        "chosen_global_scale": {str(gs): chosen.count(gs) for gs in SEARCH_CANDIDATES},
+    }
 
 
 def run_ours(args):
@@ -370,14 +475,18 @@ def run_ours(args):
     if tf.exists() and (W, H) == (2048, 2048) and top in STAGE_KERNEL:
         traffic = json.loads(tf.read_text()).get(STAGE_KERNEL[top])
 
-    # CPU baseline: the restatement on a bounded sample, one thread.
+    # CPU baseline: the restatement on a bounded sample, one thread; the same
+    # sample through the CUDA path gives the errors reported beside the number.
     cpu_value = None
+    parity = None
     if not args.no_cpu:
         crop, ccover = cpu_sample(images, np)
         t0 = time.perf_counter()
-        cpu_probe(crop, ccover, np)
+        oracle_out = cpu_probe(crop, ccover, np, full=True)
         cpu_s = time.perf_counter() - t0
         cpu_value = round(CPU_SAMPLE * CPU_SAMPLE / cpu_s / 1e6, 4)
+        parity = gpu_parity(ctx, crop, ccover, oracle_out, np)
+    search = None if args.no_search else run_search(ctx, torch, np, 3)
 
     line = {
         "metric": "probe MPix/s (encode+reconstruct+SSIMULACRA2)",
@@ -402,6 +511,8 @@ def run_ours(args):
         "e2e": {"value": round(e2e, 2), "unit": "MPix/s",
                 "h2d_bytes_per_step": int(sum(r.nbytes for r, _ in images)),
                 "d2h_bytes_per_step": 8 * len(images)},
+        "parity": parity,
+        "search": search,
         "gpu_launches": int(launches),
         "cfl_sequential_fallbacks": sum(c.cfl_fallbacks for c in ctxs),
         "clocks": clocks,
@@ -427,6 +538,8 @@ def main():
     ap.add_argument("--size", type=int, default=None, help="square image side (profiling)")
     ap.add_argument("--images", type=int, default=None, help="images per step (profiling)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--no-search", action="store_true",
+                    help="skip the batched quality-search leg")
     ap.add_argument("--streams", type=int, default=4,
                     help="contexts (each with its own stream) that images alternate over")
     args = ap.parse_args()

@@ -36,9 +36,9 @@
  * jpxlg_ctx_synchronize().  A context serves one host thread at a time.
  * Layouts and references are read-only device data of their device: any
  * context on that device may use them, so several contexts (streams, host
- * threads) can probe the same frame concurrently.  Destroying one waits for
- * its creating context's stream only; synchronize the other contexts that
- * used it first.
+ * threads) can probe the same frame concurrently.  Destroying a layout,
+ * reference or batch waits for the device's queued work and does not need
+ * the context that created it.
  *
  * Layouts.
  *   planes      float, row-major width x height, three planes back to back
@@ -185,8 +185,9 @@ int jpxlg_reconstruct(jpxlg_ctx* ctx, const jpxlg_layout* layout, const jpxlg_pl
 int jpxlg_ssim2_ref_create(jpxlg_ctx* ctx, const float* linear_rgb, int width, int height,
                            uint32_t mem, jpxlg_ref** out);
 int jpxlg_ssim2_ref_destroy(jpxlg_ref* ref);
-/* Score a candidate against a reference.  terms (optional, host) receives
- * up to 6 scales x 3 channels x 6 norms. */
+/* Score a candidate against a reference.  score, raw_error (one double each)
+ * and terms (scales x 3 channels x 6 norms, at most 108) are optional; they
+ * follow mem like the planes (device pointers with JPXLG_MEM_DEVICE). */
 int jpxlg_ssim2_score(jpxlg_ctx* ctx, const jpxlg_ref* ref, const float* linear_rgb,
                       uint32_t mem, double* score, double* raw_error, double* terms);
 /* One-shot pair score (reference moments are built and dropped). */
@@ -194,12 +195,45 @@ int jpxlg_score_pair(jpxlg_ctx* ctx, const float* ref_rgb, const float* cand_rgb
                      int height, uint32_t mem, double* score);
 
 /* One quality-controller probe: encode `rgb` with `params`, render the plan
- * at 8-bit depth and score it against `ref` (built from the same source).
- * With JPXLG_MEM_DEVICE the score is written to the device pointer
- * `score_dev` (a double) and the call does not synchronize. */
+ * at the source depth `bits` and score it against `ref` (built from the same
+ * source).  With JPXLG_MEM_DEVICE, `rgb` is device memory, exactly one double
+ * is written at the device pointer `score`, and the call does not
+ * synchronize. */
 int jpxlg_probe(jpxlg_ctx* ctx, const jpxlg_layout* layout, const jpxlg_ref* ref,
                 const void* rgb, int bits, const jpxlg_params* params, uint32_t mem,
                 double* score);
+
+/* Batched probes (the quality controller's candidate sweep: many frames, many
+ * quantizers per frame).  Replaces a loop of PlanRenderEvaluator::evaluate
+ * calls (evaluator.rs:295) inside search_frame_perceptual (quality.rs:2405)
+ * with one graph launch.  An item is one probe of a frame: its layout and
+ * reference (created on this context's device), the frame's RGB in device
+ * memory (interleaved, `bits` per sample) and the candidate's parameters.
+ *
+ * jpxlg_batch_create spreads the items over `lanes` internal contexts (each
+ * with its own stream and workspace; 0 picks min(items, 4)), runs every
+ * probe once to size the workspaces, and captures the whole batch — fork,
+ * the lanes' probes, join — as one CUDA graph on `ctx`'s stream.  The items
+ * and the RGB buffers they point to must stay valid while the batch lives;
+ * the buffers' contents may change between runs.
+ * jpxlg_batch_run launches the graph on ctx's stream.  With JPXLG_MEM_HOST,
+ * `scores` (n doubles) is filled and the call returns when the batch is done;
+ * with JPXLG_MEM_DEVICE, `scores` is a device array written on the stream.
+ * jpxlg_batch_probe is create + run + destroy in one call (host scores). */
+typedef struct jpxlg_batch jpxlg_batch;
+typedef struct {
+  const jpxlg_layout* layout;
+  const jpxlg_ref* ref;
+  const void* rgb;   /* device memory */
+  int bits;
+  jpxlg_params params;
+} jpxlg_batch_item;
+int jpxlg_batch_create(jpxlg_ctx* ctx, int n_items, const jpxlg_batch_item* items, int lanes,
+                       jpxlg_batch** out);
+int jpxlg_batch_run(jpxlg_ctx* ctx, jpxlg_batch* batch, double* scores, uint32_t mem);
+int jpxlg_batch_destroy(jpxlg_batch* batch);
+int jpxlg_batch_probe(jpxlg_ctx* ctx, int n_items, const jpxlg_batch_item* items,
+                      double* scores);
 
 /* Allocation-free variant of jpxlg_ssim2_score; it has no counterpart in the
  * reference.  The candidate (device planes) is scored against `ref` using a

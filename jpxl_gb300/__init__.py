@@ -18,6 +18,9 @@ this package                   reference (JPXL, crates/...)
 ``Ssimulacra2.score``          jpxl-perceptual ssimulacra2.rs:79
 ``score_pair``                 jpxl-perceptual lib.rs:195
 ``Context.probe``              jpxl-perceptual evaluator.rs:243 evaluate_with
+``BatchProbe``                 the candidate sweep of search_frame_perceptual
+                               (quality.rs:2405) over evaluate (evaluator.rs:295),
+                               as one CUDA graph
 =============================  ==================================================
 
 Arrays are numpy (host memory) unless stated; the ``*_device`` variants take
@@ -32,7 +35,7 @@ from dataclasses import dataclass, field
 import numpy as np
 
 from . import _lib
-from ._lib import Params, PlanStruct
+from ._lib import BatchItemStruct, Params, PlanStruct
 
 MEM_HOST = 0
 MEM_DEVICE = 1
@@ -346,6 +349,63 @@ class Ssimulacra2:
         2048 x 2048; calls in flight together on one device share scratch."""
         self.ctx.check(self.ctx.lib.jpxlg_ssim2_score_static(
             self.ctx.handle, ref.handle, C.c_void_p(cand_ptr), C.c_void_p(out_ptr)))
+
+
+@dataclass
+class BatchItem:
+    """One probe of a batch: a frame (layout, reference, RGB in device memory)
+    and a candidate's parameters."""
+
+    layout: "Layout"
+    ref: "PrecomputedReference"
+    rgb_ptr: int
+    bits: int
+    req: EncodeRequest
+
+
+class BatchProbe:
+    """Many probes as one CUDA graph (jpxlg_batch_*): the quality controller's
+    candidate sweep of quality.rs:2405 over evaluator.rs:295 probes."""
+
+    def __init__(self, ctx: Context, items: list, lanes: int = 0):
+        self.ctx = ctx
+        self.items = list(items)
+        arr = (BatchItemStruct * len(self.items))()
+        for a, it in zip(arr, self.items):
+            a.layout = it.layout.handle
+            a.ref = it.ref.handle
+            a.rgb = it.rgb_ptr
+            a.bits = it.bits
+            a.params = it.req._struct()
+        self._arr = arr
+        h = C.c_void_p()
+        ctx.check(ctx.lib.jpxlg_batch_create(ctx.handle, len(self.items), arr, lanes,
+                                             C.byref(h)))
+        self.handle = h
+
+    def run(self) -> np.ndarray:
+        """Runs every probe; returns the scores in item order."""
+        out = np.zeros(len(self.items), np.float64)
+        self.ctx.check(self.ctx.lib.jpxlg_batch_run(self.ctx.handle, self.handle,
+                                                    out.ctypes.data, MEM_HOST))
+        return out
+
+    def run_device(self, scores_ptr: int) -> None:
+        """Queues every probe on the context's stream; scores land in the
+        device array at scores_ptr (float64, one per item)."""
+        self.ctx.check(self.ctx.lib.jpxlg_batch_run(self.ctx.handle, self.handle,
+                                                    C.c_void_p(scores_ptr), MEM_DEVICE))
+
+    def close(self):
+        if getattr(self, "handle", None):
+            self.ctx.lib.jpxlg_batch_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def score_pair(ctx: Context, ref_rgb: np.ndarray, cand_rgb: np.ndarray) -> float:

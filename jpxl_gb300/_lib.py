@@ -39,6 +39,10 @@ SIGNATURES: dict[str, tuple] = {
     "jpxlg_score_pair": (_I, [_P, _P, _P, _I, _I, _U32, _P]),
     "jpxlg_probe": (_I, [_P, _P, _P, _P, _I, _P, _U32, _P]),
     "jpxlg_ssim2_score_static": (_I, [_P, _P, _P, _P]),
+    "jpxlg_batch_create": (_I, [_P, _I, _P, _I, C.POINTER(_P)]),
+    "jpxlg_batch_run": (_I, [_P, _P, _P, _U32]),
+    "jpxlg_batch_destroy": (_I, [_P]),
+    "jpxlg_batch_probe": (_I, [_P, _I, _P, _P]),
 }
 
 
@@ -53,6 +57,18 @@ class Params(C.Structure):
         ("gaborish", C.c_uint32),
         ("epf_iters", C.c_uint32),
         ("cfl", C.c_uint32),
+    ]
+
+
+class BatchItemStruct(C.Structure):
+    """jpxlg_batch_item (include/jpxlg.h)."""
+
+    _fields_ = [
+        ("layout", C.c_void_p),
+        ("ref", C.c_void_p),
+        ("rgb", C.c_void_p),
+        ("bits", C.c_int),
+        ("params", Params),
     ]
 
 

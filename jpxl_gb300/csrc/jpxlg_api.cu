@@ -88,7 +88,8 @@ struct jpxlg_ctx {
 };
 
 struct jpxlg_layout {
-  jpxlg_ctx* ctx = nullptr;
+  jpxlg_ctx* ctx = nullptr;  // creating context (device checks at creation time only)
+  int device = 0;
   Geo geo;
   uint8_t* d_map = nullptr;
   uint32_t* d_hf_mul = nullptr;
@@ -102,6 +103,7 @@ struct jpxlg_layout {
 
 struct jpxlg_ref {
   jpxlg_ctx* ctx = nullptr;
+  int device = 0;
   int w = 0, h = 0, nscales = 0;
   SsimScale scales[6];
   void* block = nullptr;  // one allocation holding every scale's planes
@@ -450,6 +452,8 @@ int jpxlg_ctx_create(int device, uint32_t flags, jpxlg_ctx** out) {
     if ((call) != cudaSuccess) return JPXLG_ERR_CUDA; \
   } while (0)
   CKC(cudaSetDevice(device));
+  CKC(configure_encode_kernels());
+  CKC(configure_ssim_kernels());
   CKC(cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking));
   c->stream = c->own_stream;
   CKC(cudaMalloc(&c->d_words, 8 * sizeof(uint32_t)));
@@ -571,6 +575,7 @@ int jpxlg_layout_create(jpxlg_ctx* ctx, int width, int height, const uint8_t* bl
   cudaSetDevice(ctx->device);
   std::unique_ptr<jpxlg_layout> L(new jpxlg_layout);
   L->ctx = ctx;
+  L->device = ctx->device;
   L->geo = make_geo(width, height);
   const Geo& g = L->geo;
   const size_t nb = (size_t)g.bw * g.bh;
@@ -634,8 +639,9 @@ int jpxlg_layout_create(jpxlg_ctx* ctx, int width, int height, const uint8_t* bl
 
 int jpxlg_layout_destroy(jpxlg_layout* L) {
   if (!L) return JPXLG_ERR_ARGUMENT;
-  cudaSetDevice(L->ctx->device);
-  cudaStreamSynchronize(L->ctx->stream);
+  // The creating context may already be gone; cudaFree waits for the
+  // device's queued work itself.
+  cudaSetDevice(L->device);
   cudaFree(L->d_map);
   cudaFree(L->d_hf_mul);
   cudaFree(L->d_sharp);
@@ -656,7 +662,7 @@ int jpxlg_layout_dims(const jpxlg_layout* L, int* bw, int* bh, int* tw, int* th)
 int jpxlg_encode_transform(jpxlg_ctx* ctx, const jpxlg_layout* L, const void* rgb, int bits,
                            const jpxlg_params* p, jpxlg_plan* plan, uint32_t mem) {
   if (!ctx || !L || !rgb || !plan) return fail(ctx, JPXLG_ERR_ARGUMENT, "null argument");
-  if (L->ctx->device != ctx->device) return fail(ctx, JPXLG_ERR_ARGUMENT, "layout on another device");
+  if (L->device != ctx->device) return fail(ctx, JPXLG_ERR_ARGUMENT, "layout on another device");
   if (!(bits == 8 || (bits >= 9 && bits <= 16)))
     return fail(ctx, JPXLG_ERR_ARGUMENT, "bits must be 8 or 9..16");
   int rc = check_params(ctx, p);
@@ -709,7 +715,7 @@ int jpxlg_encode_transform(jpxlg_ctx* ctx, const jpxlg_layout* L, const void* rg
 int jpxlg_encode_stages(jpxlg_ctx* ctx, const jpxlg_layout* L, const void* rgb, int bits,
                         const jpxlg_params* p, float* xyb, float* pre, float* coeff) {
   if (!ctx || !L || !rgb) return fail(ctx, JPXLG_ERR_ARGUMENT, "null argument");
-  if (L->ctx->device != ctx->device) return fail(ctx, JPXLG_ERR_ARGUMENT, "layout on another device");
+  if (L->device != ctx->device) return fail(ctx, JPXLG_ERR_ARGUMENT, "layout on another device");
   if (!(bits == 8 || (bits >= 9 && bits <= 16)))
     return fail(ctx, JPXLG_ERR_ARGUMENT, "bits must be 8 or 9..16");
   int rc = check_params(ctx, p);
@@ -740,7 +746,7 @@ int jpxlg_encode_stages(jpxlg_ctx* ctx, const jpxlg_layout* L, const void* rgb, 
 int jpxlg_reconstruct(jpxlg_ctx* ctx, const jpxlg_layout* L, const jpxlg_plan* plan,
                       const jpxlg_params* p, int out_kind, int bits, void* out, uint32_t mem) {
   if (!ctx || !L || !plan || !out) return fail(ctx, JPXLG_ERR_ARGUMENT, "null argument");
-  if (L->ctx->device != ctx->device) return fail(ctx, JPXLG_ERR_ARGUMENT, "layout on another device");
+  if (L->device != ctx->device) return fail(ctx, JPXLG_ERR_ARGUMENT, "layout on another device");
   if (!plan->qcoeff || !plan->lf || !plan->cfl_x || !plan->cfl_b)
     return fail(ctx, JPXLG_ERR_ARGUMENT, "null plan buffer");
   int rc = check_params(ctx, p);
@@ -786,6 +792,7 @@ int jpxlg_ssim2_ref_create(jpxlg_ctx* ctx, const float* rgb, int w, int h, uint3
   cudaSetDevice(ctx->device);
   std::unique_ptr<jpxlg_ref> R(new jpxlg_ref);
   R->ctx = ctx;
+  R->device = ctx->device;
   R->w = w;
   R->h = h;
   // reference.rs:90 — keep halving while the current scale is at least 8x8.
@@ -856,8 +863,7 @@ int jpxlg_ssim2_ref_create(jpxlg_ctx* ctx, const float* rgb, int w, int h, uint3
 
 int jpxlg_ssim2_ref_destroy(jpxlg_ref* R) {
   if (!R) return JPXLG_ERR_ARGUMENT;
-  cudaSetDevice(R->ctx->device);
-  cudaStreamSynchronize(R->ctx->stream);
+  cudaSetDevice(R->device);
   cudaFree(R->block);
   delete R;
   return JPXLG_OK;
@@ -866,7 +872,7 @@ int jpxlg_ssim2_ref_destroy(jpxlg_ref* R) {
 int jpxlg_ssim2_score(jpxlg_ctx* ctx, const jpxlg_ref* R, const float* rgb, uint32_t mem,
                       double* score, double* raw_error, double* terms) {
   if (!ctx || !R || !rgb) return fail(ctx, JPXLG_ERR_ARGUMENT, "null argument");
-  if (R->ctx->device != ctx->device)
+  if (R->device != ctx->device)
     return fail(ctx, JPXLG_ERR_ARGUMENT, "reference on another device");
   cudaSetDevice(ctx->device);
   const size_t n = (size_t)R->w * R->h;
@@ -877,10 +883,21 @@ int jpxlg_ssim2_score(jpxlg_ctx* ctx, const jpxlg_ref* R, const float* rgb, uint
     CK(cudaMemcpyAsync(ctx->out.p, rgb, 3 * n * sizeof(float), cudaMemcpyHostToDevice, ctx->stream));
     cand = ctx->out.as<float>();
   }
-  int rc = score_device(ctx, R, cand, nullptr,
-                        mem == JPXLG_MEM_DEVICE && score ? score : ctx->score.as<double>());
+  // The finish kernel writes score, raw error and every term into the
+  // context's own buffer; callers receive only the outputs they asked for.
+  int rc = score_device(ctx, R, cand, nullptr, ctx->score.as<double>());
   if (rc) return rc;
-  if (mem == JPXLG_MEM_DEVICE) return JPXLG_OK;
+  if (mem == JPXLG_MEM_DEVICE) {
+    const double* s = ctx->score.as<double>();
+    if (score)
+      CK(cudaMemcpyAsync(score, s, sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream));
+    if (raw_error)
+      CK(cudaMemcpyAsync(raw_error, s + 1, sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream));
+    if (terms)
+      CK(cudaMemcpyAsync(terms, s + 2, R->nscales * 18 * sizeof(double), cudaMemcpyDeviceToDevice,
+                         ctx->stream));
+    return JPXLG_OK;
+  }
   CK(cudaMemcpyAsync(ctx->h_score, ctx->score.p, (2 + 108) * sizeof(double), cudaMemcpyDeviceToHost,
                      ctx->stream));
   rc = sync_and_check(ctx);
@@ -906,7 +923,7 @@ int jpxlg_score_pair(jpxlg_ctx* ctx, const float* ref_rgb, const float* cand_rgb
 int jpxlg_probe(jpxlg_ctx* ctx, const jpxlg_layout* L, const jpxlg_ref* R, const void* rgb,
                 int bits, const jpxlg_params* p, uint32_t mem, double* score) {
   if (!ctx || !L || !R || !rgb || !score) return fail(ctx, JPXLG_ERR_ARGUMENT, "null argument");
-  if (L->ctx->device != ctx->device || R->ctx->device != ctx->device)
+  if (L->device != ctx->device || R->device != ctx->device)
     return fail(ctx, JPXLG_ERR_ARGUMENT, "layout or reference on another device");
   if (R->w != L->geo.w || R->h != L->geo.h)
     return fail(ctx, JPXLG_ERR_MISMATCH, "reference and layout dimensions differ");
@@ -937,10 +954,15 @@ int jpxlg_probe(jpxlg_ctx* ctx, const jpxlg_layout* L, const jpxlg_ref* R, const
                      ctx->cflx.as<int8_t>(), ctx->cflb.as<int8_t>(), 128, 128, ctx->d_lf, p,
                      JPXLG_OUT_LINEAR_DEPTH, bits, ctx->out.p, ctx->cxyb.as<float>());
   if (rc) return rc;
-  double* dst = mem == JPXLG_MEM_DEVICE ? score : ctx->score.as<double>();
-  rc = score_device(ctx, R, ctx->out.as<float>(), ctx->cxyb.as<float>(), dst);
+  // The finish kernel fills the context's 128-double buffer (score, raw
+  // error, terms); the caller's slot receives the score alone.
+  rc = score_device(ctx, R, ctx->out.as<float>(), ctx->cxyb.as<float>(), ctx->score.as<double>());
   if (rc) return rc;
-  if (mem == JPXLG_MEM_DEVICE) return JPXLG_OK;
+  if (mem == JPXLG_MEM_DEVICE) {
+    CK(cudaMemcpyAsync(score, ctx->score.p, sizeof(double), cudaMemcpyDeviceToDevice,
+                       ctx->stream));
+    return JPXLG_OK;
+  }
   CK(cudaMemcpyAsync(ctx->h_score, ctx->score.p, sizeof(double), cudaMemcpyDeviceToHost,
                      ctx->stream));
   rc = sync_and_check(ctx);
@@ -950,6 +972,154 @@ int jpxlg_probe(jpxlg_ctx* ctx, const jpxlg_layout* L, const jpxlg_ref* R, const
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Batched probes as one CUDA graph.  Each lane is a full context (tables,
+// workspace, stream) owned by the batch; item i runs on lane i % lanes.  The
+// warm-up pass sizes every lane's workspace and builds its lookup tables, so
+// the captured pass performs stream work only.
+struct jpxlg_batch {
+  jpxlg_ctx* owner = nullptr;
+  int device = 0;
+  std::vector<jpxlg_ctx*> lanes;
+  std::vector<jpxlg_batch_item> items;
+  double* d_scores = nullptr;
+  double* h_scores = nullptr;  // pinned
+  cudaEvent_t fork = nullptr;
+  std::vector<cudaEvent_t> joins;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+};
+
+namespace {
+
+void batch_free(jpxlg_batch* b) {
+  if (!b) return;
+  if (b->exec) cudaGraphExecDestroy(b->exec);
+  if (b->graph) cudaGraphDestroy(b->graph);
+  if (b->fork) cudaEventDestroy(b->fork);
+  for (cudaEvent_t e : b->joins) cudaEventDestroy(e);
+  for (jpxlg_ctx* l : b->lanes) jpxlg_ctx_destroy(l);
+  cudaFree(b->d_scores);
+  cudaFreeHost(b->h_scores);
+  delete b;
+}
+
+// Queues every item on its lane (device mode, scores into d_scores).
+int batch_enqueue(jpxlg_ctx* ctx, jpxlg_batch* b) {
+  const int L = (int)b->lanes.size();
+  for (size_t i = 0; i < b->items.size(); ++i) {
+    const jpxlg_batch_item& it = b->items[i];
+    jpxlg_ctx* lane = b->lanes[i % L];
+    int rc = jpxlg_probe(lane, it.layout, it.ref, it.rgb, it.bits, &it.params, JPXLG_MEM_DEVICE,
+                         b->d_scores + i);
+    if (rc) return fail(ctx, rc, "batch item %zu: %s", i, lane->last_error.c_str());
+  }
+  return JPXLG_OK;
+}
+
+// Reads and clears each lane's device error word once the batch is done.
+int batch_check(jpxlg_ctx* ctx, jpxlg_batch* b) {
+  for (jpxlg_ctx* lane : b->lanes) {
+    int rc = sync_and_check(lane);
+    if (rc) return fail(ctx, rc, "batch lane: %s", lane->last_error.c_str());
+  }
+  return JPXLG_OK;
+}
+
+}  // namespace
+
+extern "C" int jpxlg_batch_create(jpxlg_ctx* ctx, int n_items, const jpxlg_batch_item* items,
+                                  int lanes, jpxlg_batch** out) {
+  if (!ctx || !items || !out || n_items <= 0) return fail(ctx, JPXLG_ERR_ARGUMENT, "null argument");
+  *out = nullptr;
+  for (int i = 0; i < n_items; ++i) {
+    const jpxlg_batch_item& it = items[i];
+    if (!it.layout || !it.ref || !it.rgb) return fail(ctx, JPXLG_ERR_ARGUMENT, "item %d: null", i);
+    if (!(it.bits == 8 || (it.bits >= 9 && it.bits <= 16)))
+      return fail(ctx, JPXLG_ERR_ARGUMENT, "item %d: bits must be 8 or 9..16", i);
+    int rc = check_params(ctx, &it.params);
+    if (rc) return rc;
+  }
+  if (lanes <= 0) lanes = std::min(n_items, 4);
+  lanes = std::min(lanes, n_items);
+  CK(cudaSetDevice(ctx->device));
+  std::unique_ptr<jpxlg_batch, void (*)(jpxlg_batch*)> b(new jpxlg_batch, batch_free);
+  b->owner = ctx;
+  b->device = ctx->device;
+  b->items.assign(items, items + n_items);
+  for (int l = 0; l < lanes; ++l) {
+    jpxlg_ctx* lane = nullptr;
+    int rc = jpxlg_ctx_create(ctx->device, 0, &lane);
+    if (rc) return fail(ctx, rc, "batch lane %d: context creation failed", l);
+    b->lanes.push_back(lane);
+    cudaEvent_t e = nullptr;
+    CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    b->joins.push_back(e);
+  }
+  CK(cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming));
+  CK(cudaMalloc(&b->d_scores, n_items * sizeof(double)));
+  CK(cudaMallocHost(&b->h_scores, n_items * sizeof(double)));
+  // Warm-up: every allocation and table the probes need happens here.
+  int rc = batch_enqueue(ctx, b.get());
+  if (rc) return rc;
+  rc = batch_check(ctx, b.get());
+  if (rc) return rc;
+  // Capture: fork from ctx's stream, the lanes' probes, join back.
+  CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+  cudaEventRecord(b->fork, ctx->stream);
+  for (jpxlg_ctx* lane : b->lanes) cudaStreamWaitEvent(lane->stream, b->fork, 0);
+  rc = batch_enqueue(ctx, b.get());
+  for (size_t l = 0; l < b->lanes.size(); ++l) {
+    cudaEventRecord(b->joins[l], b->lanes[l]->stream);
+    cudaStreamWaitEvent(ctx->stream, b->joins[l], 0);
+  }
+  cudaError_t ce = cudaStreamEndCapture(ctx->stream, &b->graph);
+  if (rc) return rc;
+  if (ce != cudaSuccess)
+    return fail(ctx, JPXLG_ERR_CUDA, "batch capture: %s", cudaGetErrorString(ce));
+  CK(cudaGraphInstantiate(&b->exec, b->graph, 0));
+  *out = b.release();
+  return JPXLG_OK;
+}
+
+extern "C" int jpxlg_batch_run(jpxlg_ctx* ctx, jpxlg_batch* b, double* scores, uint32_t mem) {
+  if (!ctx || !b || !scores) return fail(ctx, JPXLG_ERR_ARGUMENT, "null argument");
+  if (b->owner != ctx) return fail(ctx, JPXLG_ERR_ARGUMENT, "batch belongs to another context");
+  CK(cudaSetDevice(ctx->device));
+  CK(cudaGraphLaunch(b->exec, ctx->stream));
+  const size_t bytes = b->items.size() * sizeof(double);
+  if (mem == JPXLG_MEM_DEVICE) {
+    CK(cudaMemcpyAsync(scores, b->d_scores, bytes, cudaMemcpyDeviceToDevice, ctx->stream));
+    return JPXLG_OK;
+  }
+  CK(cudaMemcpyAsync(b->h_scores, b->d_scores, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  int rc = batch_check(ctx, b);
+  if (rc) return rc;
+  std::memcpy(scores, b->h_scores, bytes);
+  return JPXLG_OK;
+}
+
+extern "C" int jpxlg_batch_destroy(jpxlg_batch* b) {
+  if (!b) return JPXLG_ERR_ARGUMENT;
+  // The owning context may already be gone: wait for the device instead of
+  // its stream before the graph and the lanes are released.
+  cudaSetDevice(b->device);
+  cudaDeviceSynchronize();
+  batch_free(b);
+  return JPXLG_OK;
+}
+
+extern "C" int jpxlg_batch_probe(jpxlg_ctx* ctx, int n_items, const jpxlg_batch_item* items,
+                                 double* scores) {
+  jpxlg_batch* b = nullptr;
+  int rc = jpxlg_batch_create(ctx, n_items, items, 0, &b);
+  if (rc) return rc;
+  rc = jpxlg_batch_run(ctx, b, scores, JPXLG_MEM_HOST);
+  jpxlg_batch_destroy(b);
+  return rc;
+}
 
 // ---------------------------------------------------------------------------
 // Allocation-free scoring.  jpxlg_ssim2_score_static runs the same kernels as

@@ -49,6 +49,11 @@ struct RenderArgs {
   float* sigma;              // [bw*bh]
 };
 
+// Per-device kernel attributes (dynamic shared memory above 48 KB); call once
+// per device with it current, before any launch or stream capture.
+cudaError_t configure_encode_kernels();
+cudaError_t configure_ssim_kernels();
+
 void upload_dct_constants(const float* iv4, const float* iv8, const float* iv16,
                           const float* scale_f, cudaStream_t s);
 void launch_srgb_to_xyb(const void* rgb, int bits, size_t n, const float* lut, float* x, float* y,

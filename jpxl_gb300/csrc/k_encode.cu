@@ -312,12 +312,6 @@ void launch_precondition(const float* in, float* out, int w, int h, cudaStream_t
   float unnorm = 1.0f + 4.0f * w1 + 4.0f * w2;
   float scale = 1.0f / unnorm;
   EncKernel k{scale, w1 * scale, w2 * scale, 1.0f / scale, -0.0f};
-  static bool configured = false;
-  if (!configured) {
-    cudaFuncSetAttribute(k_precondition, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)kPreSmem);
-    configured = true;
-  }
   dim3 grid((w + kPreTile - 1) / kPreTile, (h + kPreTile - 1) / kPreTile, 3);
   k_precondition<<<grid, kPreThreads, kPreSmem, s>>>(in, out, w, h, k);
 }
@@ -1194,6 +1188,11 @@ int launch_quant_chroma(const EncArgs& a, const uint32_t* const* lists, const in
   if (counts[1]) { k_quant_chroma<16><<<(counts[1] + 7) / 8, 128, 0, s>>>(a, lists[1], counts[1]); ++k; }
   if (counts[2]) { k_quant_chroma<32><<<(counts[2] + 3) / 4, 128, 0, s>>>(a, lists[2], counts[2]); ++k; }
   return k;
+}
+
+cudaError_t configure_encode_kernels() {
+  return cudaFuncSetAttribute(k_precondition, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)kPreSmem);
 }
 
 void upload_dct_constants(const float* iv4, const float* iv8, const float* iv16,

@@ -342,17 +342,21 @@ int launch_score_scale(const float* cand, bool cand_is_linear, const SsimScale& 
   (void)num_sms;
   dim3 grid((ref.w + kST - 1) / kST, (ref.h + kST - 1) / kST);
   if (cand_is_linear) {
-    cudaFuncSetAttribute(k_score_tile<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)kScoreSmem);
     k_score_tile<true><<<grid, kScoreThreads, kScoreSmem, s>>>(cand, ref.xyb, ref.mu, ref.s11,
                                                                 ref.w, ref.h, partial);
   } else {
-    cudaFuncSetAttribute(k_score_tile<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)kScoreSmem);
     k_score_tile<false><<<grid, kScoreThreads, kScoreSmem, s>>>(cand, ref.xyb, ref.mu, ref.s11,
                                                                  ref.w, ref.h, partial);
   }
   return (int)(grid.x * grid.y);
+}
+
+cudaError_t configure_ssim_kernels() {
+  cudaError_t e = cudaFuncSetAttribute(k_score_tile<true>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kScoreSmem);
+  if (e != cudaSuccess) return e;
+  return cudaFuncSetAttribute(k_score_tile<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)kScoreSmem);
 }
 
 // S5 — ssimulacra2.rs:391 WEIGHTS (the metric's data table), :509
