@@ -310,7 +310,7 @@ constexpr int kEP = 3;
 constexpr int kES = kET + 2 * kEP;
 
 template <int STEP>
-__global__ void __launch_bounds__(256) k_epf(const float* __restrict__ in, float* __restrict__ out,
+__global__ void __launch_bounds__(256, 3) k_epf(const float* __restrict__ in, float* __restrict__ out,
                                              const float* __restrict__ sigma, int w, int h,
                                              float step_mul4) {
   __shared__ float t[3][kES][kES + 1];
