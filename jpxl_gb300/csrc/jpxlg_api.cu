@@ -64,12 +64,13 @@ struct jpxlg_ctx {
   // small device words
   uint32_t* d_words = nullptr;  // [0] err, [1] not_gray, [2] cfl fallbacks
   int* d_lf = nullptr;          // [0..1] unbiased LF factors, [2..3] biased
+  float* d_mul = nullptr;       // hf multipliers of the current call's global_scale
   uint32_t* h_words = nullptr;  // pinned mirror
   double* h_score = nullptr;    // pinned score out (2 + 108)
   // workspace
   DevBuf rgb, xyb, pre, coeff, dyhf, qcoeff, lfs, dylf, lfq, cflx, cflb;
   DevBuf planes, aux, sigma, out;
-  DevBuf lf_part, lf_seed;
+  DevBuf lf_part, lf_seed, cfl_tile;
   DevBuf pyr, partial, score, cxyb;
   // stage timers
   struct Mark {
@@ -247,6 +248,7 @@ int encode_device(jpxlg_ctx* ctx, const jpxlg_layout* L, const void* rgb_dev, in
   CK(ctx->dylf.ensure(nb * sizeof(float)));
   CK(ctx->lf_seed.ensure(4 * sizeof(int)));
   CK(ctx->lf_part.ensure(kCflScratchBytes));
+  CK(ctx->cfl_tile.ensure(cfl_tile_scratch_bytes(g.tw * g.th)));
   const float* lut = get_lut(ctx, bits);
   if (!lut) return fail(ctx, JPXLG_ERR_CUDA, "transfer table allocation failed");
   CK(cudaMemsetAsync(ctx->d_words + 1, 0, sizeof(uint32_t), ctx->stream));
@@ -272,6 +274,7 @@ int encode_device(jpxlg_ctx* ctx, const jpxlg_layout* L, const void* rgb_dev, in
   a.qs = scalars_of(p);
   a.pre = pre;
   a.dq = ctx->d_dq;
+  a.mul_table = ctx->d_mul;
   a.hf_mul = L->d_hf_mul;
   a.block_map = L->d_map;
   a.coeff = ctx->coeff.as<float>();
@@ -290,11 +293,13 @@ int encode_device(jpxlg_ctx* ctx, const jpxlg_layout* L, const void* rgb_dev, in
   a.cfl_fallbacks = ctx->d_words + 2;
   // square classes only: DCT8, DCT16, DCT32 are shape classes 0..2
   stage_begin(ctx, JPXLG_STAGE_FDCT_LUMA);
-  rc = after_launch(ctx, launch_fdct_luma(a, L->lists, L->counts, ctx->stream));
+  launch_mul_table(p->global_scale, ctx->d_mul, ctx->stream);
+  rc = after_launch(ctx, 1 + launch_fdct_luma(a, L->lists, L->counts, ctx->stream));
   stage_end(ctx);
   if (rc) return rc;
   stage_begin(ctx, JPXLG_STAGE_CFL);
-  rc = after_launch(ctx, launch_cfl(a, ctx->lf_seed.as<int>(), ctx->lf_part.p, ctx->stream));
+  rc = after_launch(ctx, launch_cfl(a, ctx->lf_seed.as<int>(), ctx->lf_part.p, ctx->cfl_tile.p,
+                                    ctx->stream));
   stage_end(ctx);
   if (rc) return rc;
   stage_begin(ctx, JPXLG_STAGE_QUANT_CHROMA);
@@ -323,6 +328,7 @@ int render_device(jpxlg_ctx* ctx, const jpxlg_layout* L, const int32_t* qcoeff,
   a.geo = g;
   a.qs = scalars_of(p);
   a.dq = ctx->d_dq;
+  a.mul_table = ctx->d_mul;
   a.hf_mul = L->d_hf_mul;
   a.sharpness = L->d_sharp;
   a.qcoeff = qcoeff;
@@ -335,8 +341,9 @@ int render_device(jpxlg_ctx* ctx, const jpxlg_layout* L, const int32_t* qcoeff,
   a.planes = ctx->planes.as<float>();
   a.sigma = ctx->sigma.as<float>();
   stage_begin(ctx, JPXLG_STAGE_RENDER_VARBLOCKS);
+  launch_mul_table(p->global_scale, ctx->d_mul, ctx->stream);
   launch_render_varblocks(a, L->lists, L->counts, ctx->stream);
-  uint64_t k = 0;
+  uint64_t k = 1;
   for (int i = 0; i < kNumShapes; ++i) k += L->counts[i] ? 1 : 0;
   int rc = after_launch(ctx, k);
   stage_end(ctx);
@@ -459,6 +466,7 @@ int jpxlg_ctx_create(int device, uint32_t flags, jpxlg_ctx** out) {
   CKC(cudaMalloc(&c->d_words, 8 * sizeof(uint32_t)));
   CKC(cudaMemset(c->d_words, 0, 8 * sizeof(uint32_t)));
   CKC(cudaMalloc(&c->d_lf, 4 * sizeof(int)));
+  CKC(cudaMalloc(&c->d_mul, kMulTableN * sizeof(float)));
   CKC(cudaMemset(c->d_lf, 0, 4 * sizeof(int)));
   CKC(cudaMallocHost(&c->h_words, 16 * sizeof(uint32_t)));
   CKC(cudaMallocHost(&c->h_score, 128 * sizeof(double)));
@@ -492,7 +500,7 @@ int jpxlg_ctx_destroy(jpxlg_ctx* ctx) {
   DevBuf* bufs[] = {&ctx->rgb,    &ctx->xyb,   &ctx->pre,     &ctx->coeff,   &ctx->dyhf,
                     &ctx->qcoeff, &ctx->lfs,   &ctx->dylf,    &ctx->lfq,     &ctx->cflx,
                     &ctx->cflb,   &ctx->planes, &ctx->aux,    &ctx->sigma,   &ctx->out,
-                    &ctx->lf_part, &ctx->lf_seed, &ctx->pyr,  &ctx->partial,
+                    &ctx->lf_part, &ctx->lf_seed, &ctx->cfl_tile, &ctx->pyr,  &ctx->partial,
                     &ctx->score,  &ctx->cxyb};
   for (DevBuf* b : bufs) b->release();
   for (auto& m : ctx->marks) {
@@ -503,6 +511,7 @@ int jpxlg_ctx_destroy(jpxlg_ctx* ctx) {
   cudaFree(ctx->d_dq);
   cudaFree(ctx->d_words);
   cudaFree(ctx->d_lf);
+  cudaFree(ctx->d_mul);
   cudaFreeHost(ctx->h_words);
   cudaFreeHost(ctx->h_score);
   cudaStreamDestroy(ctx->own_stream);

@@ -265,6 +265,21 @@ __device__ __forceinline__ DF df_warp_sum(DF v) {
 }
 __device__ __forceinline__ double df_value(DF v) { return (double)v.hi + (double)v.lo; }
 
+// ---- reconstruct.rs:27 hf_multiplier -----------------------------------------
+// Mul = 65536 / (global_scale * hf_mul), formed in f64 and narrowed to f32.
+// A context tabulates it for hf_mul < kMulTableN once per call (the same
+// expression, so the same bits); larger hf_mul evaluate it in place.
+constexpr int kMulTableN = 256;
+__device__ __forceinline__ float hf_multiplier_f64(uint32_t global_scale, uint32_t hf_mul) {
+  const double denom = (double)global_scale * (double)hf_mul;
+  return denom <= 0.0 ? 0.0f : (float)(65536.0 / denom);
+}
+__device__ __forceinline__ float hf_multiplier(const float* table, uint32_t global_scale,
+                                               uint32_t hf_mul) {
+  return hf_mul < (uint32_t)kMulTableN ? __ldg(&table[hf_mul])
+                                       : hf_multiplier_f64(global_scale, hf_mul);
+}
+
 // ---- reconstruct.rs:50 bias_adjust ------------------------------------------
 // q -> q * bias for |q| <= 1, else q - 0.145 / q.  The expression is odd in q
 // under round-to-nearest, so |q| < kBiasQuotN reads 0.145f / |q| from a table

@@ -14,6 +14,7 @@ struct EncArgs {
   QuantScalars qs;
   const float* pre;          // 3 planes w*h: XYB after the optional precondition
   const float* dq;           // [3][kDequantTableFloats] dequant multipliers
+  const float* mul_table;    // [kMulTableN] hf multipliers of this call's global_scale
   const uint32_t* hf_mul;    // per 8x8 block (read at varblock origins)
   const uint8_t* block_map;  // per 8x8 block
   float* coeff;              // [3][W8*H8] forward coefficients (f32)
@@ -37,6 +38,7 @@ struct RenderArgs {
   Geo geo;
   QuantScalars qs;
   const float* dq;
+  const float* mul_table;    // [kMulTableN] hf multipliers of this call's global_scale
   const uint32_t* hf_mul;
   const uint8_t* sharpness;
   const int32_t* qcoeff;     // [3][W8*H8]
@@ -48,6 +50,9 @@ struct RenderArgs {
   float* planes;             // [3][w*h] XYB out
   float* sigma;              // [bw*bh]
 };
+
+// Fills table[h] = hf_multiplier_f64(global_scale, h) for h < kMulTableN.
+void launch_mul_table(uint32_t global_scale, float* table, cudaStream_t s);
 
 // Per-device kernel attributes (dynamic shared memory above 48 KB); call once
 // per device with it current, before any launch or stream capture.
@@ -65,7 +70,10 @@ int launch_fdct_luma(const EncArgs& a, const uint32_t* const* lists, const int* 
 // LF CfL partials: kLfCtas CTAs, each 7 double-float sums and 8 bit counts.
 constexpr int kLfCtas = 128;
 constexpr size_t kCflScratchBytes = (size_t)kLfCtas * (7 * 8 + 8 * 4);
-int launch_cfl(const EncArgs& a, int* lf_seeds, void* lf_scratch, cudaStream_t s);
+// Per-tile CfL scratch: 8 double-float sums and 2 seeds per 64x64 tile.
+inline size_t cfl_tile_scratch_bytes(int ntiles) { return (size_t)ntiles * (8 * 8 + 2 * 4); }
+int launch_cfl(const EncArgs& a, int* lf_seeds, void* lf_scratch, void* tile_scratch,
+               cudaStream_t s);
 int launch_quant_chroma(const EncArgs& a, const uint32_t* const* lists, const int* counts,
                         cudaStream_t s);
 

@@ -528,9 +528,8 @@ __global__ void __launch_bounds__(128) k_fdct_luma(EncArgs a, const uint32_t* __
     }
   }
   // Luma HF: cells (k, j) of column j; the n x n LLF corner stays zero.
-  const uint32_t hf_mul = a.hf_mul[(size_t)by * geo.bw + bx];
-  const double denom = (double)a.qs.global_scale * (double)hf_mul;
-  const float mul = denom <= 0.0 ? 0.0f : (float)(65536.0 / denom);
+  const float mul =
+      hf_multiplier(a.mul_table, a.qs.global_scale, a.hf_mul[(size_t)by * geo.bw + bx]);
   const float scale = mul * a.qs.qm[1];
   const float* m = a.dq + kDequantTableFloats + dq_offset(dq_slot(N == 8 ? 0 : (N == 16 ? 4 : 5)));
   const float bias = c_quant_bias[1];
@@ -652,31 +651,25 @@ __device__ __forceinline__ bool cell_is_llf(const uint8_t* map, int bw, int px, 
 
 constexpr int kCflThreads = 256;
 
-// Per 64x64 tile: HF regression sums (X and B against source Y), the seed,
-// and the residual bit costs of the candidate window.  One CTA per tile.
-__global__ void __launch_bounds__(kCflThreads) k_cfl_tiles(EncArgs a) {
-  __shared__ double s_part[kCflThreads / 32][8];
-  __shared__ double s_tot[8];
-  __shared__ uint32_t s_bits[kCflThreads / 32][8];
-  __shared__ int s_seed[2];
-  __shared__ int s_robust[2];
-  __shared__ int s_cands[2][4];
-  __shared__ int s_ncand[2];
+// Per 64x64 tile in three kernels: (1) the HF regression sums (X and B
+// against source Y) in double-float, one CTA per tile; (2) the seeds, one
+// thread per tile and channel, so that the f64 arithmetic of best_factor and
+// its robustness bound overlaps across tiles instead of holding a CTA at a
+// barrier; (3) the residual bit costs of the candidate windows and the
+// choice, one CTA per tile.
+
+// (1) sums[tile][8]: s_yy, s_yx, s_xx, s_yb, s_bb, sum|yx|, sum|yb|, count.
+__global__ void __launch_bounds__(kCflThreads) k_cfl_tile_sums(EncArgs a, DF* __restrict__ sums) {
+  __shared__ DF s_part[kCflThreads / 32][8];
   const Geo& geo = a.geo;
   const int tx = blockIdx.x, ty = blockIdx.y;
   const int tile = ty * geo.tw + tx;
-  if (*a.not_gray == 0u || !a.cfl_enabled) {
-    if (threadIdx.x == 0) {
-      a.cfl_x[tile] = 0;
-      a.cfl_b[tile] = 0;
-    }
-    return;
-  }
+  if (*a.not_gray == 0u || !a.cfl_enabled) return;
   const size_t cplane = (size_t)geo.W8 * geo.H8;
   const int px0 = tx * 64, py0 = ty * 64;
   const int pw = min(64, geo.W8 - px0), ph = min(64, geo.H8 - py0);
-  // Phase A: tree sums in double-float.  Thread t covers column (t % 64) of
-  // rows t/64, t/64 + 4, ... of the tile: coalesced rows, no divisions.
+  // Thread t covers column (t % 64) of rows t/64, t/64 + 4, ... of the tile:
+  // coalesced rows, no divisions.
   DF syy{0, 0}, syx{0, 0}, sxx{0, 0}, syb{0, 0}, sbb{0, 0};
   float ayx = 0.0f, ayb = 0.0f, cnt = 0.0f;
   {
@@ -702,62 +695,60 @@ __global__ void __launch_bounds__(kCflThreads) k_cfl_tiles(EncArgs a) {
       }
     }
   }
-  // One fixed-order reduction of all eight sums: a butterfly per warp, then
-  // the warps in order in f64 by eight threads of warp 0.
-  {
-    DF v[8] = {syy, syx, sxx, syb, sbb, DF{ayx, 0.0f}, DF{ayb, 0.0f}, DF{cnt, 0.0f}};
+  // One fixed-order reduction: a butterfly per warp, then the warps in order.
+  DF v[8] = {syy, syx, sxx, syb, sbb, DF{ayx, 0.0f}, DF{ayb, 0.0f}, DF{cnt, 0.0f}};
+  const int lane = threadIdx.x % 32, wid = threadIdx.x / 32;
 #pragma unroll
-    for (int q = 0; q < 8; ++q) {
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) {
-        DF u{__shfl_xor_sync(0xffffffffu, v[q].hi, o), __shfl_xor_sync(0xffffffffu, v[q].lo, o)};
-        v[q] = df_add(v[q], u);
-      }
-    }
-    const int lane = threadIdx.x % 32, wid = threadIdx.x / 32;
-    if (lane == 0)
-#pragma unroll
-      for (int q = 0; q < 8; ++q) s_part[wid][q] = (double)v[q].hi + (double)v[q].lo;
-    __syncthreads();
-    if (threadIdx.x < 8) {
-      double t = 0.0;
-      for (int i = 0; i < kCflThreads / 32; ++i) t += s_part[i][threadIdx.x];
-      s_tot[threadIdx.x] = t;
-    }
-    __syncthreads();
-  }
-  const double t_syy = s_tot[0], t_syx = s_tot[1], t_sxx = s_tot[2], t_syb = s_tot[3],
-               t_sbb = s_tot[4], t_ayx = s_tot[5], t_ayb = s_tot[6], t_cnt = s_tot[7];
-  // Channel X in thread 0, B in thread 32 (separate warps, in parallel).
-  if (threadIdx.x % 32 == 0 && threadIdx.x < 64) {
-    // Distance of the double-float tree sum and of the reference's
-    // sequential f64 sum from the exact sum, relative to sum|t| (the |t|
-    // sums above are f32 estimates; the factor 2 covers their error).
-    const double gam = 2.0 * (t_cnt + 64.0) * (2.2737367544323206e-13 + 1.1102230246251565e-16);
-    {
-      const int ch = threadIdx.x / 32;
-      RegSums s;
-      s.s_yy = t_syy;
-      s.s_yc = ch == 0 ? t_syx : t_syb;
-      s.s_cc = ch == 0 ? t_sxx : t_sbb;
-      s.a_yc = ch == 0 ? t_ayx : t_ayb;
-      s.n = t_cnt;
-      bool robust = true;
-      int seed = 0;
-      if (t_cnt > 0.0) {
-        seed = best_factor(s, ch == 0 ? 0.0f : 1.0f, gam * s.s_yy, gam * s.a_yc, gam * s.s_cc,
-                           &robust);
-      }
-      s_seed[ch] = seed;
-      s_robust[ch] = robust ? 1 : 0;
-    }
+  for (int q = 0; q < 8; ++q) {
+    const DF t = df_warp_sum(v[q]);
+    if (lane == 0) s_part[wid][q] = t;
   }
   __syncthreads();
-  // Sequential fallback in the reference's order (varblocks in raster order
-  // of their origins within the tile, then coefficient rows and columns).
-  if ((!s_robust[0] || !s_robust[1]) && threadIdx.x == 0) {
+  if (threadIdx.x < 8) {
+    DF t = s_part[0][threadIdx.x];
+    for (int i = 1; i < kCflThreads / 32; ++i) t = df_add(t, s_part[i][threadIdx.x]);
+    sums[(size_t)tile * 8 + threadIdx.x] = t;
+  }
+}
+
+// (2) seeds[tile][2] from the sums; a seed the bound cannot settle is
+// recomputed from the tile's coefficients in the reference's order
+// (varblocks in raster order of their origins within the tile, then
+// coefficient rows and columns).
+__global__ void __launch_bounds__(128) k_cfl_tile_seeds(EncArgs a, const DF* __restrict__ sums,
+                                                        int* __restrict__ seeds) {
+  const Geo& geo = a.geo;
+  const int ntiles = geo.tw * geo.th;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= 2 * ntiles) return;
+  const int tile = i >> 1, ch = i & 1;
+  if (*a.not_gray == 0u || !a.cfl_enabled) {
+    seeds[i] = 0;
+    return;
+  }
+  const DF* t = sums + (size_t)tile * 8;
+  const double t_syy = df_value(t[0]), t_syc = df_value(t[ch == 0 ? 1 : 3]);
+  const double t_scc = df_value(t[ch == 0 ? 2 : 4]), t_ayc = df_value(t[ch == 0 ? 5 : 6]);
+  const double t_cnt = df_value(t[7]);
+  // Distance of the double-float tree sum and of the reference's sequential
+  // f64 sum from the exact sum, relative to sum|t| (the |t| sums are f32
+  // estimates; the factor 2 covers their error).
+  const double gam = 2.0 * (t_cnt + 64.0) * (2.2737367544323206e-13 + 1.1102230246251565e-16);
+  const float base = ch == 0 ? 0.0f : 1.0f;
+  int seed = 0;
+  bool robust = true;
+  if (t_cnt > 0.0) {
+    RegSums r{t_syy, t_syc, t_scc, t_ayc, t_cnt};
+    seed = best_factor(r, base, gam * t_syy, gam * t_ayc, gam * t_scc, &robust);
+  }
+  if (!robust) {
     atomicAdd(a.cfl_fallbacks, 1u);
-    RegSums sx{0, 0, 0, 0, 0}, sb{0, 0, 0, 0, 0};
+    const size_t cplane = (size_t)geo.W8 * geo.H8;
+    const int tx = tile % geo.tw, ty = tile / geo.tw;
+    const int px0 = tx * 64, py0 = ty * 64;
+    const int pw = min(64, geo.W8 - px0), ph = min(64, geo.H8 - py0);
+    const float* cc = a.coeff + (ch == 0 ? 0 : 2 * cplane);
+    RegSums r{0, 0, 0, 0, 0};
     for (int by = py0 / 8; by < (py0 + ph) / 8; ++by)
       for (int bx = px0 / 8; bx < (px0 + pw) / 8; ++bx) {
         uint8_t e = a.block_map[(size_t)by * geo.bw + bx];
@@ -768,40 +759,57 @@ __global__ void __launch_bounds__(kCflThreads) k_cfl_tiles(EncArgs a) {
           for (int col = (row < nb ? nb : 0); col < side; ++col) {
             size_t ci = (size_t)(by * 8 + row) * geo.W8 + bx * 8 + col;
             double y = (double)a.coeff[cplane + ci];
-            double x = (double)a.coeff[ci];
-            double b = (double)a.coeff[2 * cplane + ci];
-            sx.s_yy += y * y; sx.s_yc += y * x; sx.s_cc += x * x;
-            sb.s_yy += y * y; sb.s_yc += y * b; sb.s_cc += b * b;
-            sx.n += 1.0;
+            double c = (double)cc[ci];
+            r.s_yy += y * y;
+            r.s_yc += y * c;
+            r.s_cc += c * c;
+            r.n += 1.0;
           }
       }
-    sb.n = sx.n;
-    bool r;
-    s_seed[0] = sx.n > 0 ? best_factor(sx, 0.0f, 0, 0, 0, &r) : 0;
-    s_seed[1] = sb.n > 0 ? best_factor(sb, 1.0f, 0, 0, 0, &r) : 0;
+    bool unused;
+    seed = r.n > 0 ? best_factor(r, base, 0, 0, 0, &unused) : 0;
   }
-  __syncthreads();
+  seeds[i] = seed;
+}
+
+// (3) Residual bits of every candidate through the DCT8x8 baseline quantizer
+// (cells folded onto the 8x8 grid, lib.rs:3585), then the choice.
+__global__ void __launch_bounds__(kCflThreads) k_cfl_tile_bits(EncArgs a,
+                                                               const int* __restrict__ seeds) {
+  __shared__ uint32_t s_bits[kCflThreads / 32][8];
+  __shared__ float s_step[2][64], s_rstep[2][64];
+  const Geo& geo = a.geo;
+  const int tx = blockIdx.x, ty = blockIdx.y;
+  const int tile = ty * geo.tw + tx;
+  if (*a.not_gray == 0u || !a.cfl_enabled) {
+    if (threadIdx.x == 0) {
+      a.cfl_x[tile] = 0;
+      a.cfl_b[tile] = 0;
+    }
+    return;
+  }
+  const size_t cplane = (size_t)geo.W8 * geo.H8;
+  const int px0 = tx * 64, py0 = ty * 64;
+  const int pw = min(64, geo.W8 - px0), ph = min(64, geo.H8 - py0);
   // lib.rs:3735 factor_candidates(seed, -128, 127): seed-1, seed, seed+1
-  // clamped and de-duplicated, then 0 if absent.
-  if (threadIdx.x < 2) {
-    int ch = threadIdx.x, seed = s_seed[ch], nc = 0;
-    int* c = s_cands[ch];
+  // clamped and de-duplicated, then 0 if absent (every thread forms both).
+  int cands[2][4], ncand[2];
+  const int seed[2] = {seeds[2 * tile], seeds[2 * tile + 1]};
+#pragma unroll
+  for (int ch = 0; ch < 2; ++ch) {
+    int nc = 0;
     for (int d = -1; d <= 1; ++d) {
-      int v = min(max(seed + d, -128), 127);
+      int v = min(max(seed[ch] + d, -128), 127);
       bool dup = false;
-      for (int i = 0; i < nc; ++i) dup |= c[i] == v;
-      if (!dup) c[nc++] = v;
+      for (int i = 0; i < nc; ++i) dup |= cands[ch][i] == v;
+      if (!dup) cands[ch][nc++] = v;
     }
     bool has0 = false;
-    for (int i = 0; i < nc; ++i) has0 |= c[i] == 0;
-    if (!has0) c[nc++] = 0;
-    s_ncand[ch] = nc;
+    for (int i = 0; i < nc; ++i) has0 |= cands[ch][i] == 0;
+    if (!has0) cands[ch][nc++] = 0;
+    ncand[ch] = nc;
   }
-  __syncthreads();
-  // Phase C: residual bits of every candidate through the DCT8x8 baseline
-  // quantizer (cells folded onto the 8x8 grid, lib.rs:3585).
   // Steps of the 64 folded cells and their reciprocals, per channel.
-  __shared__ float s_step[2][64], s_rstep[2][64];
   if (threadIdx.x < 128) {
     const int ch = threadIdx.x / 64, cell = threadIdx.x % 64;
     const float scale = a.base_mul * a.qs.qm[ch == 0 ? 0 : 2];
@@ -814,11 +822,11 @@ __global__ void __launch_bounds__(kCflThreads) k_cfl_tiles(EncArgs a) {
   float kx[4], kb[4];
 #pragma unroll
   for (int i = 0; i < 4; ++i) {
-    kx[i] = 0.0f + (float)s_cands[0][i < s_ncand[0] ? i : 0] / 84.0f;
-    kb[i] = 1.0f + (float)s_cands[1][i < s_ncand[1] ? i : 0] / 84.0f;
+    kx[i] = 0.0f + (float)cands[0][i < ncand[0] ? i : 0] / 84.0f;
+    kb[i] = 1.0f + (float)cands[1][i < ncand[1] ? i : 0] / 84.0f;
   }
-  const bool need_x = s_seed[0] != 0, need_b = s_seed[1] != 0;
-  const int ncx = need_x ? s_ncand[0] : 0, ncb = need_b ? s_ncand[1] : 0;
+  const bool need_x = seed[0] != 0, need_b = seed[1] != 0;
+  const int ncx = need_x ? ncand[0] : 0, ncb = need_b ? ncand[1] : 0;
   if (need_x || need_b) {
     const int col = threadIdx.x % 64;
     if (col < pw) {
@@ -864,41 +872,39 @@ __global__ void __launch_bounds__(kCflThreads) k_cfl_tiles(EncArgs a) {
     __syncthreads();
   }
   if (threadIdx.x % 32 == 0 && threadIdx.x < 64) {
-    unsigned long long tot[2][4];
-    for (int q = 0; q < 8; ++q) {
+    const int ch = threadIdx.x / 32;
+    unsigned long long tot[4];
+    for (int c = 0; c < 4; ++c) {
       unsigned long long t = 0;
-      for (int i = 0; i < kCflThreads / 32; ++i) t += s_bits[i][q];
-      tot[q / 4][q % 4] = t;
+      for (int i = 0; i < kCflThreads / 32; ++i) t += s_bits[i][ch * 4 + c];
+      tot[c] = t;
     }
-    {
-      const int ch = threadIdx.x / 32;
-      int result = 0;
-      if (s_seed[ch] != 0) {
-        // lib.rs:3966 refine_hf_factor: cost(0) first, then each non-zero
-        // candidate needs residual + factor bits strictly below (ties to
-        // the smaller magnitude).
-        unsigned long long best_cost = 0;
-        for (int c = 0; c < s_ncand[ch]; ++c)
-          if (s_cands[ch][c] == 0) best_cost = tot[ch][c];
-        int best_f = 0;
-        for (int c = 0; c < s_ncand[ch]; ++c) {
-          int f = s_cands[ch][c];
-          if (f == 0) continue;
-          unsigned long long fb = factor_bits(f);
-          unsigned long long cutoff = best_cost > fb ? best_cost - fb : 0;
-          if (tot[ch][c] > cutoff) continue;
-          unsigned long long cost = tot[ch][c] + fb;
-          int af = f < 0 ? -f : f, ab = best_f < 0 ? -best_f : best_f;
-          if (cost < best_cost || (cost == best_cost && af < ab)) {
-            best_cost = cost;
-            best_f = f;
-          }
+    int result = 0;
+    if (seed[ch] != 0) {
+      // lib.rs:3966 refine_hf_factor: cost(0) first, then each non-zero
+      // candidate needs residual + factor bits strictly below (ties to the
+      // smaller magnitude).
+      unsigned long long best_cost = 0;
+      for (int c = 0; c < ncand[ch]; ++c)
+        if (cands[ch][c] == 0) best_cost = tot[c];
+      int best_f = 0;
+      for (int c = 0; c < ncand[ch]; ++c) {
+        int f = cands[ch][c];
+        if (f == 0) continue;
+        unsigned long long fb = factor_bits(f);
+        unsigned long long cutoff = best_cost > fb ? best_cost - fb : 0;
+        if (tot[c] > cutoff) continue;
+        unsigned long long cost = tot[c] + fb;
+        int af = f < 0 ? -f : f, ab = best_f < 0 ? -best_f : best_f;
+        if (cost < best_cost || (cost == best_cost && af < ab)) {
+          best_cost = cost;
+          best_f = f;
         }
-        result = best_f;
       }
-      if (ch == 0) a.cfl_x[tile] = (int8_t)result;
-      else a.cfl_b[tile] = (int8_t)result;
+      result = best_f;
     }
+    if (ch == 0) a.cfl_x[tile] = (int8_t)result;
+    else a.cfl_b[tile] = (int8_t)result;
   }
 }
 
@@ -1136,9 +1142,8 @@ __global__ void __launch_bounds__(128) k_quant_chroma(EncArgs a, const uint32_t*
       a.lfq[bplane * c + bi] = lf_quantize(target, a.qs.m_dc[c], a.err);
     }
   }
-  const uint32_t hf_mul = a.hf_mul[(size_t)by * geo.bw + bx];
-  const double denom = (double)a.qs.global_scale * (double)hf_mul;
-  const float mul = denom <= 0.0 ? 0.0f : (float)(65536.0 / denom);
+  const float mul =
+      hf_multiplier(a.mul_table, a.qs.global_scale, a.hf_mul[(size_t)by * geo.bw + bx]);
   const int off = dq_offset(dq_slot(N == 8 ? 0 : (N == 16 ? 4 : 5)));
   for (int c = 0; c <= 2; c += 2) {
     const float scale = mul * a.qs.qm[c];
@@ -1169,16 +1174,22 @@ int launch_fdct_luma(const EncArgs& a, const uint32_t* const* lists, const int* 
   return k;
 }
 
-int launch_cfl(const EncArgs& a, int* lf_seeds, void* lf_scratch, cudaStream_t s) {
+int launch_cfl(const EncArgs& a, int* lf_seeds, void* lf_scratch, void* tile_scratch,
+               cudaStream_t s) {
   dim3 tiles(a.geo.tw, a.geo.th);
-  k_cfl_tiles<<<tiles, kCflThreads, 0, s>>>(a);
+  const int ntiles = a.geo.tw * a.geo.th;
+  DF* tile_sums = (DF*)tile_scratch;
+  int* tile_seeds = (int*)((char*)tile_scratch + (size_t)ntiles * 8 * sizeof(DF));
+  k_cfl_tile_sums<<<tiles, kCflThreads, 0, s>>>(a, tile_sums);
+  k_cfl_tile_seeds<<<(2 * ntiles + 127) / 128, 128, 0, s>>>(a, tile_sums, tile_seeds);
+  k_cfl_tile_bits<<<tiles, kCflThreads, 0, s>>>(a, tile_seeds);
   DF* sums = (DF*)lf_scratch;
   uint32_t* bits = (uint32_t*)((char*)lf_scratch + kLfCtas * 7 * sizeof(DF));
   k_cfl_lf_sums<<<kLfCtas, kLfThreads, 0, s>>>(a, sums);
   k_cfl_lf_seed<<<1, 64, 0, s>>>(a, sums, lf_seeds);
   k_cfl_lf_bits<<<kLfCtas, kLfThreads, 0, s>>>(a, lf_seeds, bits);
   k_cfl_lf_pick<<<1, 32, 0, s>>>(a, lf_seeds, bits);
-  return 5;
+  return 7;
 }
 
 int launch_quant_chroma(const EncArgs& a, const uint32_t* const* lists, const int* counts,
@@ -1188,6 +1199,15 @@ int launch_quant_chroma(const EncArgs& a, const uint32_t* const* lists, const in
   if (counts[1]) { k_quant_chroma<16><<<(counts[1] + 7) / 8, 128, 0, s>>>(a, lists[1], counts[1]); ++k; }
   if (counts[2]) { k_quant_chroma<32><<<(counts[2] + 3) / 4, 128, 0, s>>>(a, lists[2], counts[2]); ++k; }
   return k;
+}
+
+__global__ void k_mul_table(uint32_t global_scale, float* table) {
+  const int h = threadIdx.x;
+  if (h < kMulTableN) table[h] = hf_multiplier_f64(global_scale, (uint32_t)h);
+}
+
+void launch_mul_table(uint32_t global_scale, float* table, cudaStream_t s) {
+  k_mul_table<<<1, kMulTableN, 0, s>>>(global_scale, table);
 }
 
 cudaError_t configure_encode_kernels() {

@@ -88,9 +88,8 @@ __global__ void __launch_bounds__(128) k_render_vb(RenderArgs a, const uint32_t*
 
   float mul = 0.0f, kx = 0.0f, kb = 0.0f;
   if (active) {
-    const uint32_t hf_mul = a.hf_mul[(size_t)by * geo.bw + bx];
-    const double denom = (double)a.qs.global_scale * (double)hf_mul;
-    mul = denom <= 0.0 ? 0.0f : (float)(65536.0 / denom);  // reconstruct.rs:27
+    mul = hf_multiplier(a.mul_table, a.qs.global_scale,
+                        a.hf_mul[(size_t)by * geo.bw + bx]);  // reconstruct.rs:27
     const int tile = (by / 8) * geo.tw + bx / 8;
     kx = 0.0f + (float)a.cfl_x[tile] / 84.0f;  // reconstruct.rs:96 cfl_factors
     kb = 1.0f + (float)a.cfl_b[tile] / 84.0f;
