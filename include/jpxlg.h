@@ -13,6 +13,8 @@
  *                           the forward cache (lib.rs:2683), estimate_cfl
  *                           (lib.rs:3437) and quantize_square_varblock
  *                           (lib.rs:3237), for a cover the caller supplies.
+ *   jpxlg_select_blocks     replaces select_blocks (jpxl-encode-policy
+ *                           lib.rs:5260), the hierarchical cover.
  *   jpxlg_reconstruct       replaces PlanRenderer::render / render_linear_at_
  *                           depth_with (crates/jpxl-plan-render/src/lib.rs:
  *                           680, :749) and the decoder's VarDCT tail
@@ -202,6 +204,22 @@ int jpxlg_score_pair(jpxlg_ctx* ctx, const float* ref_rgb, const float* cand_rgb
 int jpxlg_probe(jpxlg_ctx* ctx, const jpxlg_layout* layout, const jpxlg_ref* ref,
                 const void* rgb, int bits, const jpxlg_params* params, uint32_t mem,
                 double* score);
+
+/* The encoder's cover: replaces jpxl-encode-policy's select_blocks
+ * (crates/jpxl-encode-policy/src/lib.rs:5260, with tile_region_with :5115 and
+ * block_cost_bounded :4909) for a fixed quantizer with adaptive quantization
+ * off: per aligned 32x32 region, DCT32 or four DCT16 / DCT8 quadrants by the
+ * rate-distortion objective (residual bits + lambda * sample-domain squared
+ * error, fixed bits 2 / 34), ties keeping the split.  Fills `block_map`
+ * (ceil(w/8) x ceil(h/8) bytes in the layout format above; host or device
+ * per `mem`, like `rgb`).  params: global_scale, x/b_qm_scale and gaborish
+ * are read. */
+int jpxlg_select_blocks(jpxlg_ctx* ctx, int width, int height, const void* rgb, int bits,
+                        const jpxlg_params* params, uint8_t* block_map, uint32_t mem);
+/* Regions whose decisions the GPU's tree-ordered error sums could not settle
+ * and that were recomputed in the reference's sequential order, since
+ * creation (synchronizes). */
+uint32_t jpxlg_ctx_cover_fallbacks(jpxlg_ctx* ctx);
 
 /* Batched probes (the quality controller's candidate sweep: many frames, many
  * quantizers per frame).  Replaces a loop of PlanRenderEvaluator::evaluate

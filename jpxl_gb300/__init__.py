@@ -12,6 +12,8 @@ this package                   reference (JPXL, crates/...)
 ``encode_transform``           policy lib.rs:555 build_pixel_plan's transform and
                                quantization (source.rs:226/:355, gaborish.rs:218,
                                lib.rs:3437 estimate_cfl, :3237 quantize)
+``select_blocks``              jpxl-encode-policy lib.rs:5260 select_blocks (the
+                               hierarchical cover, fixed quantizer, AQ off)
 ``PlanRenderer.render``        jpxl-plan-render lib.rs:680 render /
                                render_linear_at_depth_with
 ``PrecomputedReference``       jpxl-perceptual reference.rs:90
@@ -152,6 +154,10 @@ class Context:
     @property
     def cfl_fallbacks(self) -> int:
         return int(self.lib.jpxlg_ctx_cfl_fallbacks(self.handle))
+
+    @property
+    def cover_fallbacks(self) -> int:
+        return int(self.lib.jpxlg_ctx_cover_fallbacks(self.handle))
 
     def stage_timing(self, enable: bool) -> None:
         self.check(self.lib.jpxlg_stage_timing(self.handle, int(enable)))
@@ -349,6 +355,31 @@ class Ssimulacra2:
         2048 x 2048; calls in flight together on one device share scratch."""
         self.ctx.check(self.ctx.lib.jpxlg_ssim2_score_static(
             self.ctx.handle, ref.handle, C.c_void_p(cand_ptr), C.c_void_p(out_ptr)))
+
+
+def select_blocks(ctx: Context, rgb: np.ndarray, req: EncodeRequest,
+                  bits: int | None = None) -> np.ndarray:
+    """The encoder's cover for a fixed quantizer (policy lib.rs:5260
+    select_blocks): a uint8 [bh, bw] block map (DctSelect | ORIGIN on
+    varblock origins) from interleaved RGB in host memory."""
+    rgb = np.ascontiguousarray(rgb)
+    if bits is None:
+        bits = 8 if rgb.dtype == np.uint8 else 16
+    h, w = rgb.shape[:2]
+    out = np.zeros(((h + 7) // 8, (w + 7) // 8), np.uint8)
+    p = req._struct()
+    ctx.check(ctx.lib.jpxlg_select_blocks(ctx.handle, w, h, rgb.ctypes.data, bits, C.byref(p),
+                                          out.ctypes.data, MEM_HOST))
+    return out
+
+
+def select_blocks_device(ctx: Context, width: int, height: int, rgb_ptr: int, bits: int,
+                         req: EncodeRequest, map_ptr: int) -> None:
+    """select_blocks on device RGB; the block map lands in device memory at
+    map_ptr (ceil(w/8) * ceil(h/8) bytes), queued on the context's stream."""
+    p = req._struct()
+    ctx.check(ctx.lib.jpxlg_select_blocks(ctx.handle, width, height, C.c_void_p(rgb_ptr), bits,
+                                          C.byref(p), C.c_void_p(map_ptr), MEM_DEVICE))
 
 
 @dataclass

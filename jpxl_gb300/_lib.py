@@ -39,6 +39,8 @@ SIGNATURES: dict[str, tuple] = {
     "jpxlg_score_pair": (_I, [_P, _P, _P, _I, _I, _U32, _P]),
     "jpxlg_probe": (_I, [_P, _P, _P, _P, _I, _P, _U32, _P]),
     "jpxlg_ssim2_score_static": (_I, [_P, _P, _P, _P]),
+    "jpxlg_select_blocks": (_I, [_P, _I, _I, _P, _I, _P, _P, _U32]),
+    "jpxlg_ctx_cover_fallbacks": (_U32, [_P]),
     "jpxlg_batch_create": (_I, [_P, _I, _P, _I, C.POINTER(_P)]),
     "jpxlg_batch_run": (_I, [_P, _P, _P, _U32]),
     "jpxlg_batch_destroy": (_I, [_P]),

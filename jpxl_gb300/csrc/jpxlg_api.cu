@@ -70,7 +70,7 @@ struct jpxlg_ctx {
   // workspace
   DevBuf rgb, xyb, pre, coeff, dyhf, qcoeff, lfs, dylf, lfq, cflx, cflb;
   DevBuf planes, aux, sigma, out;
-  DevBuf lf_part, lf_seed, cfl_tile;
+  DevBuf lf_part, lf_seed, cfl_tile, cover, cover_map;
   DevBuf pyr, partial, score, cxyb;
   // stage timers
   struct Mark {
@@ -233,22 +233,13 @@ int check_params(jpxlg_ctx* ctx, const jpxlg_params* p) {
   return JPXLG_OK;
 }
 
-// Encode into plan buffers that live on the device.
-int encode_device(jpxlg_ctx* ctx, const jpxlg_layout* L, const void* rgb_dev, int bits,
-                  const jpxlg_params* p, int32_t* qcoeff, int32_t* lfq, int8_t* cflx,
-                  int8_t* cflb, int32_t* lf_factors_biased) {
-  const Geo& g = L->geo;
-  if (!L->all_square)
-    return fail(ctx, JPXLG_ERR_BLOCK_MAP, "the encoder covers frames with square varblocks only");
-  const size_t n = (size_t)g.w * g.h, n8 = (size_t)g.W8 * g.H8, nb = (size_t)g.bw * g.bh;
+// The transform frame of policy lib.rs:605: XYB planes of the source
+// (K1), preconditioned by the inverse Gaborish (K2) when the decoder will
+// run Gaborish.  Also resets and sets the context's not-grey word.
+int transform_frame(jpxlg_ctx* ctx, const Geo& g, const void* rgb_dev, int bits,
+                    const jpxlg_params* p, const float** pre_out) {
+  const size_t n = (size_t)g.w * g.h;
   CK(ctx->xyb.ensure(3 * n * sizeof(float)));
-  CK(ctx->coeff.ensure(3 * n8 * sizeof(float)));
-  CK(ctx->dyhf.ensure(n8 * sizeof(float)));
-  CK(ctx->lfs.ensure(3 * nb * sizeof(float)));
-  CK(ctx->dylf.ensure(nb * sizeof(float)));
-  CK(ctx->lf_seed.ensure(4 * sizeof(int)));
-  CK(ctx->lf_part.ensure(kCflScratchBytes));
-  CK(ctx->cfl_tile.ensure(cfl_tile_scratch_bytes(g.tw * g.th)));
   const float* lut = get_lut(ctx, bits);
   if (!lut) return fail(ctx, JPXLG_ERR_CUDA, "transfer table allocation failed");
   CK(cudaMemsetAsync(ctx->d_words + 1, 0, sizeof(uint32_t), ctx->stream));
@@ -269,6 +260,29 @@ int encode_device(jpxlg_ctx* ctx, const jpxlg_layout* L, const void* rgb_dev, in
     if (rc) return rc;
     pre = ctx->pre.as<float>();
   }
+  *pre_out = pre;
+  return JPXLG_OK;
+}
+
+// Encode into plan buffers that live on the device.
+int encode_device(jpxlg_ctx* ctx, const jpxlg_layout* L, const void* rgb_dev, int bits,
+                  const jpxlg_params* p, int32_t* qcoeff, int32_t* lfq, int8_t* cflx,
+                  int8_t* cflb, int32_t* lf_factors_biased) {
+  const Geo& g = L->geo;
+  if (!L->all_square)
+    return fail(ctx, JPXLG_ERR_BLOCK_MAP, "the encoder covers frames with square varblocks only");
+  const size_t n = (size_t)g.w * g.h, n8 = (size_t)g.W8 * g.H8, nb = (size_t)g.bw * g.bh;
+  CK(ctx->xyb.ensure(3 * n * sizeof(float)));
+  CK(ctx->coeff.ensure(3 * n8 * sizeof(float)));
+  CK(ctx->dyhf.ensure(n8 * sizeof(float)));
+  CK(ctx->lfs.ensure(3 * nb * sizeof(float)));
+  CK(ctx->dylf.ensure(nb * sizeof(float)));
+  CK(ctx->lf_seed.ensure(4 * sizeof(int)));
+  CK(ctx->lf_part.ensure(kCflScratchBytes));
+  CK(ctx->cfl_tile.ensure(cfl_tile_scratch_bytes(g.tw * g.th)));
+  const float* pre = nullptr;
+  int rc = transform_frame(ctx, g, rgb_dev, bits, p, &pre);
+  if (rc) return rc;
   EncArgs a;
   a.geo = g;
   a.qs = scalars_of(p);
@@ -500,7 +514,8 @@ int jpxlg_ctx_destroy(jpxlg_ctx* ctx) {
   DevBuf* bufs[] = {&ctx->rgb,    &ctx->xyb,   &ctx->pre,     &ctx->coeff,   &ctx->dyhf,
                     &ctx->qcoeff, &ctx->lfs,   &ctx->dylf,    &ctx->lfq,     &ctx->cflx,
                     &ctx->cflb,   &ctx->planes, &ctx->aux,    &ctx->sigma,   &ctx->out,
-                    &ctx->lf_part, &ctx->lf_seed, &ctx->cfl_tile, &ctx->pyr,  &ctx->partial,
+                    &ctx->lf_part, &ctx->lf_seed, &ctx->cfl_tile, &ctx->cover,
+                    &ctx->cover_map, &ctx->pyr,  &ctx->partial,
                     &ctx->score,  &ctx->cxyb};
   for (DevBuf* b : bufs) b->release();
   for (auto& m : ctx->marks) {
@@ -981,6 +996,85 @@ int jpxlg_probe(jpxlg_ctx* ctx, const jpxlg_layout* L, const jpxlg_ref* R, const
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Cover selection (policy lib.rs:5260 select_blocks) on the GPU.
+extern "C" int jpxlg_select_blocks(jpxlg_ctx* ctx, int width, int height, const void* rgb,
+                                   int bits, const jpxlg_params* p, uint8_t* block_map,
+                                   uint32_t mem) {
+  if (!ctx || !rgb || !block_map) return fail(ctx, JPXLG_ERR_ARGUMENT, "null argument");
+  if (width <= 0 || height <= 0) return fail(ctx, JPXLG_ERR_ARGUMENT, "empty frame");
+  if (!(bits == 8 || (bits >= 9 && bits <= 16)))
+    return fail(ctx, JPXLG_ERR_ARGUMENT, "bits must be 8 or 9..16");
+  int rc = check_params(ctx, p);
+  if (rc) return rc;
+  CK(cudaSetDevice(ctx->device));
+  const Geo g = make_geo(width, height);
+  const size_t n = (size_t)g.w * g.h, nb = (size_t)g.bw * g.bh;
+  const void* src = rgb;
+  if (mem == JPXLG_MEM_HOST) {
+    const size_t rgb_bytes = 3 * n * (bits == 8 ? 1 : 2);
+    CK(ctx->rgb.ensure(rgb_bytes));
+    CK(cudaMemcpyAsync(ctx->rgb.p, rgb, rgb_bytes, cudaMemcpyHostToDevice, ctx->stream));
+    src = ctx->rgb.p;
+  }
+  const float* pre = nullptr;
+  rc = transform_frame(ctx, g, src, bits, p, &pre);
+  if (rc) return rc;
+  CK(ctx->cover.ensure(cover_scratch_bytes(g)));
+  uint8_t* map = block_map;
+  if (mem == JPXLG_MEM_HOST) {
+    CK(ctx->cover_map.ensure(nb));
+    map = ctx->cover_map.as<uint8_t>();
+  }
+  CoverArgs a;
+  a.geo = g;
+  a.pre = pre;
+  a.dq = ctx->d_dq;
+  // The quantizers of the three square transforms at the baseline HfMul
+  // (adaptive quantization off), as HfQuantizer::new_with_matrices forms
+  // them, and lib.rs:2094's lambda from the DCT8x8 steps.
+  const float mul = host_hf_multiplier(p->global_scale, 1);
+  a.scale[0] = mul * host_qm_multiplier(p->x_qm_scale);
+  a.scale[1] = mul;
+  a.scale[2] = mul * host_qm_multiplier(p->b_qm_scale);
+  std::vector<float> dq(3 * kDequantTableFloats);
+  build_dequant_tables(dq.data());
+  for (int c = 0; c < 3; ++c) {
+    double sum = 0.0;
+    uint32_t count = 0;
+    for (int cell = 1; cell < 64; ++cell) {
+      const float step = a.scale[c] * dq[c * kDequantTableFloats + dq_offset(0) + cell];
+      const double s8 = 8.0 * (double)step;
+      sum += s8 * s8;
+      ++count;
+    }
+    const double mean = sum / (double)std::max(count, 1u);
+    a.lambda[c] = mean > 0.0 ? 1.0 * 16.0 / mean : 0.0;
+    for (int s = 0; s < 3; ++s) {
+      const int side = 8 << s;
+      a.w[s][c] = a.lambda[c] * ((double)(side * side) * 1.0);
+    }
+  }
+  cover_bind_scratch(&a, ctx->cover.p);
+  a.map = map;
+  a.fallbacks = ctx->d_words + 3;
+  a.err = ctx->d_words;
+  rc = after_launch(ctx, launch_cover(a, ctx->stream));
+  if (rc) return rc;
+  if (mem == JPXLG_MEM_DEVICE) return JPXLG_OK;
+  CK(cudaMemcpyAsync(block_map, map, nb, cudaMemcpyDeviceToHost, ctx->stream));
+  return sync_and_check(ctx);
+}
+
+extern "C" uint32_t jpxlg_ctx_cover_fallbacks(jpxlg_ctx* ctx) {
+  if (!ctx) return 0;
+  cudaSetDevice(ctx->device);
+  uint32_t v = 0;
+  cudaStreamSynchronize(ctx->stream);
+  cudaMemcpy(&v, ctx->d_words + 3, sizeof(uint32_t), cudaMemcpyDeviceToHost);
+  return v;
+}
 
 // ---------------------------------------------------------------------------
 // Batched probes as one CUDA graph.  Each lane is a full context (tables,

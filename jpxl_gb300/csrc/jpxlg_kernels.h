@@ -91,6 +91,28 @@ void launch_colour_out(const float* xyb, int w, int h, int out_kind, const float
 void upload_render_constants(const float* opsin_m, const float* opsin_bias,
                              const float* opsin_bias_cbrt, cudaStream_t s);
 
+// Cover selection (k_cover.cu).  Shape s: 0 DCT8, 1 DCT16, 2 DCT32;
+// candidates of shape s sit at every (1 << s)-aligned block position that
+// fits the grid, indexed row-major over (bw >> s) x (bh >> s).
+struct CoverArgs {
+  Geo geo;
+  const float* pre;        // 3 planes w*h: the transform frame
+  const float* dq;         // [3][kDequantTableFloats]
+  float scale[3];          // Mul * qm[c] at the baseline HfMul
+  double lambda[3];        // lib.rs:2094 per-channel Lagrange multipliers
+  double w[3][3];          // [shape][channel] lambda[c] * side^2
+  uint32_t* bits[3];       // [shape][candidate] residual bits, three channels
+  DF* sse[3];              // [shape][candidate][channel] sum of squared error
+  float* coef[3];          // [shape] 3 coefficient planes of W8*H8
+  uint8_t* map;            // block map out (bw*bh)
+  uint32_t* fallbacks;     // regions replayed in the reference's order
+  uint32_t* err;
+};
+size_t cover_scratch_bytes(const Geo& g);
+// Points a's scratch arrays into `scratch` (cover_scratch_bytes(g) bytes).
+void cover_bind_scratch(CoverArgs* a, void* scratch);
+int launch_cover(const CoverArgs& a, cudaStream_t s);
+
 // SSIMULACRA2
 struct SsimScale {
   int w, h;

@@ -418,7 +418,8 @@ __device__ __forceinline__ int level_of(float x, const float* thr, int n) {
 }
 
 // For deep outputs (65535 thresholds in global memory) the level is first
-// estimated from the transfer curve with CUDA's powf and then confirmed
+// estimated from the transfer curve with the fast powf (its error, a few
+// ulp, moves the estimate by well under one level) and then confirmed
 // against the exact thresholds (two loads), stepping by one where the
 // estimate sits on the wrong side; the binary search remains the fallback.
 // The thresholds decide, so the result is exactly the bisected level.
@@ -426,7 +427,7 @@ __device__ __forceinline__ int level_guided(float x, const float* __restrict__ t
                                             float maxv) {
   if (!isfinite(x)) return 0;
   float a = fabsf(x);
-  float e = a <= 0.0031308f ? 12.92f * a : 1.055f * powf(a, 1.0f / 2.4f) - 0.055f;
+  float e = a <= 0.0031308f ? 12.92f * a : 1.055f * __powf(a, 1.0f / 2.4f) - 0.055f;
   float s = rintf((x < 0.0f ? -e : e) * maxv);
   int est = (int)fminf(fmaxf(s, 0.0f), maxv);
 #pragma unroll 1

@@ -65,6 +65,8 @@ def load() -> C.CDLL:
         lib.orc_encode.argtypes = [p, i, i, i, p, p, p, p, p, p, p, p, p, p, p]
         lib.orc_reconstruct.restype = i
         lib.orc_reconstruct.argtypes = [i, i, p, p, p, p, p, p, p, p, i, i, p]
+        lib.orc_select_blocks.restype = i
+        lib.orc_select_blocks.argtypes = [p, i, i, i, p, p, p]
         lib.orc_ssim2.restype = i
         lib.orc_ssim2.argtypes = [p, p, i, i, p, p, p]
         lib.orc_perceptual_add_noise.argtypes = [p, p, p, i, f, C.c_uint32]
@@ -75,6 +77,23 @@ def load() -> C.CDLL:
 
 def _ptr(a):
     return None if a is None else a.ctypes.data
+
+
+def select_blocks(rgb: np.ndarray, *, global_scale: int, quant_lf: int = 16,
+                  x_qm_scale: int = 2, b_qm_scale: int = 2, gaborish: bool = False,
+                  bits: int | None = None):
+    """orc_select_blocks: returns (rc, block map uint8 [bh, bw], candidates scored)."""
+    lib = load()
+    h, w = rgb.shape[:2]
+    if bits is None:
+        bits = 8 if rgb.dtype == np.uint8 else 16
+    rgb = np.ascontiguousarray(rgb)
+    out = np.zeros(((h + 7) // 8, (w + 7) // 8), np.uint8)
+    prm = EncodeParams(global_scale, quant_lf, x_qm_scale, b_qm_scale, int(gaborish), 1)
+    scored = C.c_int64()
+    rc = lib.orc_select_blocks(rgb.ctypes.data, w, h, bits, C.byref(prm), out.ctypes.data,
+                               C.byref(scored))
+    return rc, out, scored.value
 
 
 def encode(rgb: np.ndarray, block_map: np.ndarray, hf_mul: np.ndarray, *, global_scale: int,

@@ -112,6 +112,13 @@ int orc_encode(const void* rgb, int w, int h, int bits, const uint8_t* block_map
                float* coeff_out /* 3*H8*W8 or NULL */, int32_t* qcoeff_out,
                int32_t* lf_out, int8_t* cfl_x, int8_t* cfl_b, orc_lf_cfl* lf_cfl);
 
+/* The encoder's cover (policy lib.rs:5260 select_blocks) for a fixed
+ * quantizer with adaptive quantization off: fills the block map (one byte
+ * per 8x8 block, DctSelect | 0x80 on varblock origins). candidates_scored
+ * (optional) receives the number of candidate costs evaluated. */
+int orc_select_blocks(const void* rgb, int w, int h, int bits, const orc_encode_params* p,
+                      uint8_t* block_map, int64_t* candidates_scored);
+
 /* out_kind: 0 = XYB after restoration (3 planes), 1 = linear sRGB planes,
  * 2 = 8-bit sRGB interleaved (u8, w*h*3), 3 = linear at depth `bits`
  * (3 planes), 4 = XYB before restoration (3 planes). */

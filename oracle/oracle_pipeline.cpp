@@ -6,6 +6,7 @@
 // TEST INFRASTRUCTURE ONLY (the checker, never the product).
 #include <algorithm>
 #include <cstdlib>
+#include <memory>
 #include <thread>
 
 #include "oracle.h"
@@ -625,4 +626,180 @@ extern "C" int orc_reconstruct(int w, int h, const uint8_t* block_map,
     return kOk;
   }
   return kErrParam;
+}
+
+// ---------------------------------------------------------------------------
+// Cover selection (jpxl-encode-policy lib.rs:5260 select_blocks, :5115
+// tile_region_with, :4909 block_cost_bounded, :4685 score_channel_lanes) for
+// the fixed-quantizer request: adaptive quantization off (every HfMul is the
+// baseline, its signal bits 0), the Legacy rate model (residual-bit scale 1,
+// fixed bits 2 for DCT8x8 and 34 otherwise, request.rs:614), neutral size
+// penalty, flat frequency weights and lambda scale 1.
+// ---------------------------------------------------------------------------
+
+namespace orc {
+
+struct CoverCtx {
+  const float* pre;  // 3 planes, w x h (the transform frame)
+  int w, h;
+  const HfQuant* quant[3];  // DCT8, DCT16, DCT32 at the baseline HfMul
+  TransformInfo info[3];
+  double lambda[3];
+  std::vector<float> d_y;  // 32 x 32 luma reconstruction of the current candidate
+  int64_t candidates = 0, pruned = 0;
+};
+
+// One channel of a candidate in the reference's order: rows, then the
+// non-LLF columns; bits and the weighted error accumulate cell by cell and
+// the cutoff is tested at the end of each row (lib.rs:4724-4800).
+static bool score_channel(CoverCtx& cc, int ti, int c, const float* plane, float k,
+                          bool luma_sink, double cutoff, bool has_cutoff, uint64_t* bits,
+                          double* sse) {
+  const TransformInfo& t = cc.info[ti];
+  const int side = t.ccols, n = t.brows;
+  const double flat_weight = cc.lambda[c] * ((double)(side * side) * 1.0);
+  for (int row = 0; row < side; ++row) {
+    for (int col = row < n ? n : 0; col < side; ++col) {
+      const int cell = row * side + col;
+      float target = luma_sink ? plane[cell] : plane[cell] - k * cc.d_y[cell];
+      int32_t q;
+      if (!cc.quant[ti]->choose(target, c, cell, &q)) return false;
+      float recon = cc.quant[ti]->reconstruct(q, c, cell);
+      if (luma_sink) cc.d_y[cell] = recon;
+      *bits += residual_bits(q);
+      double d = (double)(recon - target);
+      *sse += flat_weight * (d * d);
+    }
+    if (has_cutoff && (double)*bits * 1.0 + *sse >= cutoff) return false;
+  }
+  return true;
+}
+
+// Returns false when pruned (or a cell fails, which the reference reports as
+// an error; the encoder's covers never reach it).
+static bool block_cost(CoverCtx& cc, int ti, int px, int py, double cutoff, bool has_cutoff,
+                       double* cost) {
+  const TransformInfo& t = cc.info[ti];
+  const int side = t.ccols;
+  Varblock vb{px / 8, py / 8, t};
+  const size_t n = (size_t)cc.w * cc.h;
+  std::vector<float> cf[3];
+  for (int c = 0; c < 3; ++c) {
+    cf[c].resize((size_t)side * side);
+    forward_varblock(cc.pre + c * n, cc.w, cc.h, vb, cf[c].data());
+  }
+  ++cc.candidates;
+  uint64_t bits = 0;
+  double sse = 0.0;
+  if (!score_channel(cc, ti, 1, cf[1].data(), 0.0f, true, cutoff, has_cutoff, &bits, &sse)) {
+    ++cc.pruned;
+    return false;
+  }
+  if (!score_channel(cc, ti, 0, cf[0].data(), 0.0f, false, cutoff, has_cutoff, &bits, &sse) ||
+      !score_channel(cc, ti, 2, cf[2].data(), 1.0f, false, cutoff, has_cutoff, &bits, &sse)) {
+    ++cc.pruned;
+    return false;
+  }
+  *cost = (double)bits * 1.0 + sse;
+  return true;
+}
+
+struct CoverBlock { int bx, by, ti; };
+
+static double tile_region(CoverCtx& cc, int gbw, int gbh, int bx, int by, int size, int x0,
+                          int y0, std::vector<CoverBlock>* out) {
+  if (bx >= gbw || by >= gbh) return 0.0;
+  if (size == 1) {
+    double rd = 0.0;
+    block_cost(cc, 0, x0 + bx * 8, y0 + by * 8, 0.0, false, &rd);
+    out->push_back({bx, by, 0});
+    return rd + 2.0 + 0.0;
+  }
+  const int half = size / 2;
+  double split = 0.0;
+  std::vector<CoverBlock> split_blocks;
+  const int qx[4] = {bx, bx + half, bx, bx + half}, qy[4] = {by, by, by + half, by + half};
+  for (int i = 0; i < 4; ++i) split += tile_region(cc, gbw, gbh, qx[i], qy[i], half, x0, y0,
+                                                   &split_blocks);
+  const bool fits = bx + size <= gbw && by + size <= gbh;
+  if (fits) {
+    const int ti = size == 2 ? 1 : 2;
+    const double fixed = 34.0 + 0.0;
+    if (!(fixed >= split)) {
+      const double cutoff = split - fixed;
+      double rd;
+      if (block_cost(cc, ti, x0 + bx * 8, y0 + by * 8, cutoff, true, &rd)) {
+        const double single = rd + fixed;
+        if (single < split) {
+          out->push_back({bx, by, ti});
+          return single;
+        }
+      }
+    }
+  }
+  out->insert(out->end(), split_blocks.begin(), split_blocks.end());
+  return split;
+}
+
+}  // namespace orc
+
+extern "C" int orc_select_blocks(const void* rgb, int w, int h, int bits,
+                                 const orc_encode_params* p, uint8_t* block_map,
+                                 int64_t* candidates_scored) {
+  using namespace orc;
+  if (w <= 0 || h <= 0 || !(bits == 8 || (bits >= 1 && bits <= 16))) return kErrShape;
+  const int bw = (w + 7) / 8, bh = (h + 7) / 8;
+  const size_t n = (size_t)w * h;
+  std::vector<float> xyb(3 * n);
+  source_to_xyb(rgb, w, h, bits, &xyb[0], &xyb[n], &xyb[2 * n]);
+  std::vector<float> pre = xyb;
+  if (p->gaborish)
+    for (int c = 0; c < 3; ++c) gab_precondition(&xyb[c * n], w, h, &pre[c * n]);
+  CoverCtx cc;
+  cc.pre = pre.data();
+  cc.w = w;
+  cc.h = h;
+  const int sels[3] = {0, 4, 5};
+  std::vector<std::unique_ptr<HfQuant>> quants;
+  for (int i = 0; i < 3; ++i) {
+    transform_info(sels[i], &cc.info[i]);
+    quants.emplace_back(new HfQuant(cc.info[i], p->global_scale, 1, p->x_qm_scale, p->b_qm_scale));
+    cc.quant[i] = quants.back().get();
+  }
+  // lib.rs:2094: lambda = 16 / mean((8 * step)^2) over the DCT8x8 cells but
+  // the DC, per channel.
+  for (int c = 0; c < 3; ++c) {
+    double sum = 0.0;
+    uint32_t count = 0;
+    for (int cell = 1; cell < 64; ++cell) {
+      double step = 8.0 * (double)cc.quant[0]->steps[c][cell];
+      sum += step * step;
+      ++count;
+    }
+    double mean = sum / (double)std::max(count, 1u);
+    cc.lambda[c] = mean > 0.0 ? 1.0 * 16.0 / mean : 0.0;
+  }
+  cc.d_y.assign(1024, 0.0f);
+  std::memset(block_map, 0, (size_t)bw * bh);
+  const int G = 256;  // LF group side in blocks
+  for (int gy = 0; gy < (bh + G - 1) / G; ++gy)
+    for (int gx = 0; gx < (bw + G - 1) / G; ++gx) {
+      const int gbw = std::min(G, bw - gx * G), gbh = std::min(G, bh - gy * G);
+      const int x0 = gx * G * 8, y0 = gy * G * 8;
+      for (int sby = 0; sby < gbh; sby += 4)
+        for (int sbx = 0; sbx < gbw; sbx += 4) {
+          std::vector<CoverBlock> blocks;
+          tile_region(cc, gbw, gbh, sbx, sby, 4, x0, y0, &blocks);
+          for (const CoverBlock& b : blocks) {
+            const TransformInfo& t = cc.info[b.ti];
+            const int obx = gx * G + b.bx, oby = gy * G + b.by;
+            for (int dy = 0; dy < t.brows; ++dy)
+              for (int dx = 0; dx < t.bcols; ++dx)
+                block_map[(size_t)(oby + dy) * bw + obx + dx] =
+                    (uint8_t)(t.sel | ((dx == 0 && dy == 0) ? 0x80 : 0));
+          }
+        }
+    }
+  if (candidates_scored) *candidates_scored = cc.candidates;
+  return kOk;
 }

@@ -193,3 +193,28 @@ def test_oracle_rejects_bad_block_maps(oracle):
     bad = bm.copy()
     bad[1, 1] = 0  # uncovered block
     assert oracle.encode(rgb, bad, hf, global_scale=20000)[0] == -4
+
+
+def test_cover_restatement_properties(oracle):
+    """select_blocks (policy lib.rs:5260) restated: a flat frame stays DCT8 (a
+    merge pays 34 fixed bits that zero residuals never earn back), covers tile
+    the grid, and coarse quantizers merge more than fine ones."""
+    from jpxl_gb300 import synth
+
+    flat = np.full((96, 128, 3), 77, np.uint8)
+    rc, m, n = oracle.select_blocks(flat, global_scale=20000, gaborish=True)
+    assert rc == 0 and np.all(m == 0x80) and n > 0
+    rgb = synth.synthetic_rgb(320, 256, seed=5, bits=16)
+    merged = []
+    for gs in (4000, 60000):
+        rc, m, _ = oracle.select_blocks(rgb, global_scale=gs, gaborish=True)
+        assert rc == 0
+        covered = np.zeros(m.shape, np.int32)
+        side = {0: 1, 4: 2, 5: 4}
+        for by, bx in np.argwhere(m & 0x80):
+            s = side[int(m[by, bx] & 0x1F)]
+            assert np.all((m[by:by + s, bx:bx + s] & 0x1F) == (m[by, bx] & 0x1F))
+            covered[by:by + s, bx:bx + s] += 1
+        assert np.all(covered == 1)
+        merged.append(int(np.count_nonzero((m & 0x1F) != 0)))
+    assert merged[0] > merged[1]
