@@ -92,20 +92,28 @@ class ClockSampler:
         self.gpu = gpu
         self.proc = None
         self.lines: list[str] = []
+        self.first = threading.Event()
+        self.skip = 0
 
     def start(self):
+        """Starts sampling every 100 ms and returns once the first sample is
+        in (nvidia-smi takes a moment to start), so that the timed region
+        that follows is covered from its beginning."""
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
-                 "--format=csv,noheader,nounits", "-lms", "200"],
+                 "--format=csv,noheader,nounits", "-lms", "100"],
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             threading.Thread(target=self._read, daemon=True).start()
+            self.first.wait(timeout=5.0)
+            self.skip = len(self.lines)  # samples before the timed region
         except OSError:
             self.proc = None
 
     def _read(self):
         for line in self.proc.stdout:
             self.lines.append(line.strip())
+            self.first.set()
 
     def stop(self) -> dict:
         if self.proc:
@@ -116,7 +124,8 @@ class ClockSampler:
                 self.proc.kill()
         mhz, maxes, reasons = [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for ln in self.lines:
+        lines = self.lines[self.skip:] or self.lines
+        for ln in lines:
             parts = [p.strip() for p in ln.split(",")]
             if len(parts) < 9:
                 continue
@@ -141,17 +150,23 @@ def measured_peaks() -> tuple[float, str]:
 
 
 def make_workload(rank: int, world: int):
+    """This rank's share of the step's images (RGB only; covers are chosen
+    by select_blocks at the probe's quantizer)."""
     import numpy as np
 
     from jpxl_gb300 import synth
 
     seeds = shard_units(list(range(IMAGES_PER_STEP * world)), rank, world)
-    images = []
-    for s in seeds:
-        rgb = synth.synthetic_rgb(W, H, seed=1000 + s, bits=BITS)
-        cover = synth.activity_cover(rgb)
-        images.append((rgb, cover))
-    return images, np
+    return [synth.synthetic_rgb(W, H, seed=1000 + s, bits=BITS) for s in seeds], np
+
+
+def oracle_cover(rgb, gs):
+    """The restatement's select_blocks (CPU arm and parity sample)."""
+    from oracle import loader
+
+    rc, cover, _ = loader.select_blocks(rgb, global_scale=gs, gaborish=True)
+    assert rc == 0
+    return cover
 
 
 def cpu_probe(rgb, cover, np, full=False):
@@ -202,11 +217,8 @@ CPU_SAMPLE = 512  # crop side of the bounded CPU sample
 
 
 def cpu_sample(images, np):
-    rgb, cover = images[0]
-    crop = np.ascontiguousarray(rgb[:CPU_SAMPLE, :CPU_SAMPLE])
-    from jpxl_gb300 import synth
-
-    return crop, synth.activity_cover(crop)
+    crop = np.ascontiguousarray(images[0][:CPU_SAMPLE, :CPU_SAMPLE])
+    return crop, oracle_cover(crop, GLOBAL_SCALE)
 
 
 def run_reference(args):
@@ -227,7 +239,7 @@ def run_reference(args):
 
     for i in range(threads):
         rgb = synth.synthetic_rgb(CPU_SAMPLE, CPU_SAMPLE, seed=5000 + i, bits=BITS)
-        images.append((rgb, synth.activity_cover(rgb)))
+        images.append((rgb, oracle_cover(rgb, GLOBAL_SCALE)))
     pool = concurrent.futures.ThreadPoolExecutor(max_workers=threads)
 
     def step():
@@ -274,7 +286,7 @@ def search_workload(np):
         w, h = int(rng.integers(256, 3841)), int(rng.integers(256, 2161))
         x0, y0 = int(rng.integers(0, 3840 - w + 1)), int(rng.integers(0, 2160 - h + 1))
         rgb = np.ascontiguousarray(masters[i % 4][y0:y0 + h, x0:x0 + w])
-        frames.append((rgb, synth.activity_cover(rgb)))
+        frames.append(rgb)
     return frames
 
 
@@ -286,16 +298,18 @@ def run_search(ctx, torch, np, steps):
 
     frames = search_workload(np)
     items, keep = [], []
-    for rgb, cover in frames:
+    for rgb in frames:
         h, w = rgb.shape[:2]
-        layout = jg.Layout(ctx, w, h, cover, 1, 7)
         ref = jg.PrecomputedReference(ctx, jg.srgb_to_linear_planes(rgb, 8))
         dev = torch.from_numpy(rgb).cuda()
-        keep.append((layout, ref, dev))
+        keep.append((None, ref, dev))
         for gs in SEARCH_CANDIDATES:
-            items.append(jg.BatchItem(layout, ref, dev.data_ptr(), 8,
-                                      jg.EncodeRequest.with_global_scale(gs, gaborish=True,
-                                                                         epf_iters=3)))
+            # Each candidate quantizer gets its own cover, as the reference's
+            # plan build selects one per probe (lib.rs:555 -> :804).
+            req = jg.EncodeRequest.with_global_scale(gs, gaborish=True, epf_iters=3)
+            layout = jg.Layout(ctx, w, h, jg.select_blocks(ctx, rgb, req), 1, 7)
+            keep.append((layout, None, None))
+            items.append(jg.BatchItem(layout, ref, dev.data_ptr(), 8, req))
     torch.cuda.synchronize()
     batch = jg.BatchProbe(ctx, items, lanes=4)
     scores = torch.zeros(len(items), dtype=torch.float64, device="cuda")
@@ -310,7 +324,7 @@ def run_search(ctx, torch, np, steps):
     e1.record(stream)
     torch.cuda.synchronize()
     ms = e0.elapsed_time(e1) / steps
-    px = sum(rgb.shape[0] * rgb.shape[1] for rgb, _ in frames) * len(SEARCH_CANDIDATES)
+    px = sum(rgb.shape[0] * rgb.shape[1] for rgb in frames) * len(SEARCH_CANDIDATES)
     sc = scores.cpu().numpy().reshape(len(frames), len(SEARCH_CANDIDATES))
     chosen = []
     for row in sc:
@@ -318,12 +332,15 @@ def run_search(ctx, torch, np, steps):
         chosen.append(min(ok) if ok else None)
     batch.close()
     for layout, ref, _ in keep:
-        ref.close()
-        layout.close()
+        if ref is not None:
+            ref.close()
+        if layout is not None:
+            layout.close()
     return {
         "workload": (f"{len(frames)} RGB8 frames of uneven sizes (w 256-3840, h 256-2160) x "
                      f"{len(SEARCH_CANDIDATES)} candidate global scales = {len(items)} probes "
-                     "(encode, render at depth, SSIMULACRA2) as one CUDA graph launch"),
+                     "(encode, render at depth, SSIMULACRA2) as one CUDA graph launch; each "
+                     "probe's cover from select_blocks at its quantizer"),
         "value": round(px / (ms / 1e3) / 1e6, 2), "unit": "MPix/s (rendered+scored)",
         "ms_per_batch": round(ms, 2), "steps": steps, "lanes": 4,
         "threshold": SEARCH_THRESHOLD,
@@ -366,9 +383,11 @@ def run_ours(args):
     ctx = ctxs[0]
     torch.cuda.set_stream(streams[0])
     req = jg.EncodeRequest.with_global_scale(GLOBAL_SCALE, gaborish=True, epf_iters=3)
-    layouts, refs, dev_rgb, host_rgb = [], [], [], []
-    for rgb, cover in images:
-        layouts.append(jg.Layout(ctx, W, H, cover, 1, 7))
+    layouts, refs, dev_rgb, host_rgb, covers = [], [], [], [], []
+    for rgb in images:
+        # The probe's cover is the encoder's own choice at this quantizer.
+        covers.append(jg.select_blocks(ctx, rgb, req, BITS))
+        layouts.append(jg.Layout(ctx, W, H, covers[-1], 1, 7))
         src = torch.from_numpy(jg.srgb_to_linear_planes(rgb, BITS)).cuda()
         refs.append(jg.PrecomputedReference(ctx, device_ptr=src.data_ptr(), width=W, height=H))
         torch.cuda.synchronize()
@@ -415,6 +434,36 @@ def run_ours(args):
     ms_max = max_over_ranks(ms)
     px_total = W * H * len(images) * args.steps * world
     value = px_total / (ms_max / 1e3) / 1e6
+
+    # Block selection (the plan build's first stage) over the same images,
+    # device-resident, one context per stream as above.
+    maps = torch.empty((len(images), (H + 7) // 8, (W + 7) // 8), dtype=torch.uint8,
+                       device="cuda")
+
+    def select_step(contexts):
+        for i in range(len(images)):
+            jg.select_blocks_device(contexts[i % len(contexts)], W, H, dev_rgb[i].data_ptr(),
+                                    BITS, req, maps[i].data_ptr())
+
+    for _ in range(3):
+        select_step(ctxs)
+    torch.cuda.synchronize()
+    s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    s0.record(streams[0])
+    for st in streams[1:]:
+        st.wait_event(s0)
+    for _ in range(args.steps):
+        select_step(ctxs)
+    for st in streams[1:]:
+        done = torch.cuda.Event()
+        done.record(st)
+        streams[0].wait_event(done)
+    s1.record(streams[0])
+    torch.cuda.synchronize()
+    select_ms = max_over_ranks(s0.elapsed_time(s1))
+    select_value = px_total / (select_ms / 1e3) / 1e6
+    if not np.array_equal(maps.cpu().numpy(), np.stack(covers)):
+        raise RuntimeError("device and host block selection disagree")
 
     # Stage breakdown: the same steps on one stream with stage timers.
     ctx.stage_times()  # reset
@@ -486,6 +535,9 @@ def run_ours(args):
         cpu_s = time.perf_counter() - t0
         cpu_value = round(CPU_SAMPLE * CPU_SAMPLE / cpu_s / 1e6, 4)
         parity = gpu_parity(ctx, crop, ccover, oracle_out, np)
+        req_c = jg.EncodeRequest.with_global_scale(GLOBAL_SCALE, gaborish=True, epf_iters=3)
+        parity["cover_mismatches"] = int(np.count_nonzero(
+            jg.select_blocks(ctx, crop, req_c, BITS) != ccover))
     search = None if args.no_search else run_search(ctx, torch, np, 3)
 
     line = {
@@ -496,7 +548,8 @@ def run_ours(args):
         "data": "synthetic",
         "config": {"workload": WORKLOAD, "images_per_step": IMAGES_PER_STEP, "width": W,
                    "height": H, "bits": BITS, "global_scale": GLOBAL_SCALE,
-                   "cover": "activity DCT8/16/32 (stand-in for select_blocks)",
+                   "cover": ("select_blocks at global_scale 40000 (DCT8/16/32 quadtree "
+                             "rate-distortion), chosen on the GPU before the timed region"),
                    "l2": (f"inputs larger than L2: {IMAGES_PER_STEP} distinct images, "
                           f"{W * H * 6 * IMAGES_PER_STEP / 1e6:.0f} MB of RGB16 per step"),
                    "parallelism": f"replicas x{world}", "streams": nstreams},
@@ -509,10 +562,15 @@ def run_ours(args):
                          "sample": f"one {CPU_SAMPLE}x{CPU_SAMPLE} RGB16 crop of image 0, full "
                                    "probe, single thread"},
         "e2e": {"value": round(e2e, 2), "unit": "MPix/s",
-                "h2d_bytes_per_step": int(sum(r.nbytes for r, _ in images)),
+                "h2d_bytes_per_step": int(sum(r.nbytes for r in images)),
                 "d2h_bytes_per_step": 8 * len(images)},
         "parity": parity,
         "search": search,
+        "select": {"value": round(select_value, 2), "unit": "MPix/s",
+                   "ms_per_step": round(select_ms / args.steps, 3),
+                   "what": ("select_blocks (XYB, inverse Gaborish, DCT8/16/32 scoring, "
+                            "quadtree decision) over the step's images, device-resident"),
+                   "sequential_fallbacks": sum(c.cover_fallbacks for c in ctxs)},
         "gpu_launches": int(launches),
         "cfl_sequential_fallbacks": sum(c.cfl_fallbacks for c in ctxs),
         "clocks": clocks,
@@ -531,7 +589,7 @@ STAGE_KERNEL = {"precondition": "k_precondition", "gaborish": "k_gaborish", "xyb
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=40)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     # Smaller cases for profiler captures (the headline workload is the default).

@@ -1,5 +1,6 @@
 """Size-independent properties of the CUDA path at the bench's full size
-(2048 x 2048 RGB16, activity cover with DCT8/16/32), where a complete CPU
+(2048 x 2048 RGB16, DCT8/16/32 cover from select_blocks at global scale
+40000), where a complete CPU
 probe would take too long: determinism, the probe being exactly encode ->
 render -> score, scores rising with the quantizer, a fine-quantizer round
 trip, and one full-size plan checked bit for bit against the restatement."""
@@ -17,7 +18,8 @@ W = H = 2048
 @pytest.fixture(scope="module")
 def frame(ctx):
     rgb = synth.synthetic_rgb(W, H, seed=1003, bits=16)
-    cover = synth.activity_cover(rgb)
+    cover = jg.select_blocks(ctx, rgb, _req(40000))
+    assert len(np.unique(cover & 0x7F)) == 3  # DCT8, DCT16 and DCT32 all chosen
     layout = jg.Layout(ctx, W, H, cover, 1, 7)
     ref = jg.PrecomputedReference(ctx, jg.srgb_to_linear_planes(rgb, 16))
     yield rgb, cover, layout, ref
