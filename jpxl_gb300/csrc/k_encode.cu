@@ -85,8 +85,8 @@ void launch_srgb_to_xyb(const void* rgb, int bits, size_t n, const float* lut, f
 //   * remaining interior pixels sum the nine taps sequentially;
 //   * the update multiplies by 1/centre for flat indices below 4*floor(n/4)
 //     and divides by centre above.
-// Halo cells outside the frame hold copies of their mirror images, refreshed
-// after every step, so border taps read exactly the mirrored samples.
+// Border cells read their taps at mirrored frame coordinates, so no cell
+// outside the frame is ever read after the load.
 // ---------------------------------------------------------------------------
 
 constexpr int kPreTile = 64;
@@ -149,42 +149,97 @@ __global__ void __launch_bounds__(kPreThreads, 2) k_precondition(const float* __
   out += plane * blockIdx.z;
   const int tx0 = blockIdx.x * kPreTile, ty0 = blockIdx.y * kPreTile;
   const int gx0 = tx0 - kPreHalo, gy0 = ty0 - kPreHalo;
-  const int lane = threadIdx.x % 32, warp = threadIdx.x / 32;
-  constexpr int kWarps = kPreThreads / 32;
-  for (int ly = warp; ly < kPreS; ly += kWarps) {
-    const int gy = mirror1d(gy0 + ly, h);
-    for (int lx = lane; lx < kPreS; lx += 32) {
-      int gx = mirror1d(gx0 + lx, w);
-      float v = in[(size_t)gy * w + gx];
-      F[ly * kPreS + lx] = v;
-      X0[ly * kPreS + lx] = v;
+  const int t = threadIdx.x;
+  // Load the haloed tile into F (the source) and X0 (step 0's input).  Tiles
+  // inside the frame take 16-byte loads when rows are 16-byte aligned (gx0 is
+  // a multiple of 4); others mirror every coordinate.  Each thread issues
+  // all of its loads before its first shared-memory store.
+  const bool inside = gx0 >= 0 && gy0 >= 0 && gx0 + kPreS <= w && gy0 + kPreS <= h;
+  const bool vec = inside && (w % 4) == 0 && ((reinterpret_cast<uintptr_t>(in) & 15) == 0);
+  if (vec) {
+    constexpr int kV = kPreS / 4;
+    constexpr int kN = kPreS * kV;
+    constexpr int kIt = (kN + kPreThreads - 1) / kPreThreads;
+    float4 v[kIt];
+#pragma unroll
+    for (int j = 0; j < kIt; ++j) {
+      const int i = t + j * kPreThreads;
+      if (i < kN) {
+        const int ly = i / kV, lx = (i - ly * kV) * 4;
+        v[j] = __ldg(reinterpret_cast<const float4*>(in + (size_t)(gy0 + ly) * w + gx0 + lx));
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < kIt; ++j) {
+      const int i = t + j * kPreThreads;
+      if (i < kN) {
+        const int ly = i / kV, lx = (i - ly * kV) * 4;
+        *reinterpret_cast<float4*>(F + ly * kPreS + lx) = v[j];
+        *reinterpret_cast<float4*>(X0 + ly * kPreS + lx) = v[j];
+      }
+    }
+  } else {
+    constexpr int kN = kPreS * kPreS;
+    constexpr int kIt = (kN + kPreThreads - 1) / kPreThreads;
+    float v[kIt];
+#pragma unroll
+    for (int j = 0; j < kIt; ++j) {
+      const int i = t + j * kPreThreads;
+      if (i < kN) {
+        const int ly = i / kPreS, lx = i - ly * kPreS;
+        v[j] = __ldg(in + (size_t)mirror1d(gy0 + ly, h) * w + mirror1d(gx0 + lx, w));
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < kIt; ++j) {
+      const int i = t + j * kPreThreads;
+      if (i < kN) {
+        F[i] = v[j];
+        X0[i] = v[j];
+      }
     }
   }
   __syncthreads();
   const size_t n = plane;
   const size_t bulk = n - n % 4;
-  // flat < bulk  <=>  (gy, gx) < (bulk_row, bulk_col) lexicographically
   const int bulk_row = (int)(bulk / (size_t)w), bulk_col = (int)(bulk % (size_t)w);
   const int groups = (w >= 3 && h >= 3) ? (w - 2) / 4 : 0;
-  // Whether any cell of the tile lies outside the frame (block-uniform).
-  const bool has_halo_out = gx0 < 0 || gy0 < 0 || gx0 + kPreS > w || gy0 + kPreS > h;
-  // Interior tiles: every updated cell (local 1..86 on both axes) is an
-  // interior pixel inside the SIMD groups and below the division tail, and
-  // no cell of the haloed tile lies outside the frame, so each step is one
-  // formula with no per-cell tests.  Other tiles take the general loop.
-  const bool fast = !has_halo_out && gx0 + kPreS - 2 <= 4 * groups &&
-                    (bulk == n || gy0 + kPreS - 2 < bulk_row);
-  // Every step runs the paired loop over the whole update region.  On edge
-  // tiles that loop also writes cells whose reference arithmetic differs
-  // (frame border, columns past the SIMD groups, the division tail) and
-  // cells outside the frame; a second pass recomputes the former with the
-  // scalar rules and a third copies mirrored values into the latter.
   const int simd_end = min(w - 1, 4 * groups + 1);  // frame x in [1, simd_end) is SIMD
   const int row_end = bulk == n ? h - 1 : min(h - 1, bulk_row);  // rows below take the tail rule
+  // Cells whose reference arithmetic is not the interior formula, in frame
+  // coordinates: rows 0 and [rb, h) (frame border, division tail) and, on
+  // the other rows, columns 0 and [cb, w) (frame border, past the SIMD
+  // groups).  Every other in-frame cell reads only in-frame neighbours.
+  const int rb = max(row_end, 1), cb = max(simd_end, 1);
+  // Special cells of the update region [lo, hi)^2 of a step, enumerated as
+  // special rows x in-frame columns, then special columns x ordinary rows.
+  struct Special {
+    int cx0, ncin, nr0, nrin, rB0, cB0, nsr, nsc;
+    bool r0, c0;
+  };
+  auto special = [&](int lo, int hi) {
+    Special sp;
+    sp.cx0 = max(lo, -gx0);
+    sp.ncin = max(0, min(hi, w - gx0) - sp.cx0);
+    const int ry0 = max(lo, -gy0), ry1 = min(hi, h - gy0);
+    const int cx1 = sp.cx0 + sp.ncin;
+    sp.r0 = -gy0 >= ry0 && -gy0 < ry1;
+    sp.rB0 = max(ry0, rb - gy0);
+    sp.nsr = (sp.r0 ? 1 : 0) + max(0, ry1 - sp.rB0);
+    sp.nr0 = max(ry0, 1 - gy0);
+    sp.nrin = max(0, min(ry1, rb - gy0) - sp.nr0);
+    sp.c0 = -gx0 >= sp.cx0 && -gx0 < cx1;
+    sp.cB0 = max(sp.cx0, cb - gx0);
+    sp.nsc = (sp.c0 ? 1 : 0) + max(0, cx1 - sp.cB0);
+    return sp;
+  };
+  // Interior tiles have no special cell in step 0's region (the largest),
+  // so every step is the paired formula alone.
+  const Special sp0 = special(1, kPreS - 1);
+  const bool fast = sp0.nsr * sp0.ncin + sp0.nsc * sp0.nrin == 0;
   const f2 c2 = f2_pack(k.centre, k.centre), e2 = f2_pack(k.edge, k.edge);
   const f2 k2 = f2_pack(k.corner, k.corner), i2 = f2_pack(k.inv_c, k.inv_c);
   const f2 nz = f2_pack(k.neg_zero, k.neg_zero);
-  const int t = threadIdx.x;
   int cur = 0;
   for (int it = 0; it < 12; ++it) {
     const PreStep ps = c_pre_steps[it];
@@ -197,114 +252,115 @@ __global__ void __launch_bounds__(kPreThreads, 2) k_precondition(const float* __
       const int ly0 = lo + band * ps.rows, ly1 = min(ly0 + ps.rows, hi);
       if (band < ps.bands && ly0 < ly1) {
         // A pair straddling the region's edge also writes the column just
-        // outside it; no later step, fixup, mirror copy or output reads that
-        // column of this plane (each step reads only the previous region).
+        // outside it; no later step or output reads that column of this
+        // plane (each step reads only the previous region).  Cells outside
+        // the frame take values no in-frame cell reads.
         int c = ly0 * kPreS + c0;
-        f2 Mn = *reinterpret_cast<const f2*>(X + c - kPreS);
-        f2 Wn = f2_pack(X[c - kPreS - 1], f2_lo(Mn)), En = f2_pack(f2_hi(Mn), X[c - kPreS + 2]);
-        f2 Mm = *reinterpret_cast<const f2*>(X + c);
-        f2 Wm = f2_pack(X[c - 1], f2_lo(Mm)), Em = f2_pack(f2_hi(Mm), X[c + 2]);
+        f2 M0 = *reinterpret_cast<const f2*>(X + c - kPreS);
+        f2 W0 = f2_pack(X[c - kPreS - 1], f2_lo(M0)), E0 = f2_pack(f2_hi(M0), X[c - kPreS + 2]);
+        f2 M1 = *reinterpret_cast<const f2*>(X + c);
+        f2 W1 = f2_pack(X[c - 1], f2_lo(M1)), E1 = f2_pack(f2_hi(M1), X[c + 2]);
+        f2 M2, W2, E2;
         const int end = ly1 * kPreS + c0;
-#pragma unroll 3
-        for (; c < end; c += kPreS) {
-          const f2 Ms = *reinterpret_cast<const f2*>(X + c + kPreS);
-          const f2 Ws = f2_pack(X[c + kPreS - 1], f2_lo(Ms));
-          const f2 Es = f2_pack(f2_hi(Ms), X[c + kPreS + 2]);
-          // mm*c + (nn + ss + ww + ee)*e + (nw + ne + sw + se)*k
-          const f2 s1 = f2_add(f2_add(f2_add(Mn, Ms), Wm), Em);
-          const f2 s2 = f2_add(f2_add(f2_add(Wn, En), Ws), Es);
-          const f2 kx =
-              f2_add(f2_add(f2_mul(Mm, c2, nz), f2_mul(s1, e2, nz)), f2_mul(s2, k2, nz));
-          const f2 u =
-              f2_add(Mm, f2_mul(f2_sub(*reinterpret_cast<const f2*>(F + c), kx), i2, nz));
-          *reinterpret_cast<f2*>(Y + c) = u;
-          Mn = Mm; Wn = Wm; En = Em;
-          Mm = Ms; Wm = Ws; Em = Es;
+        // One row: (Mn, Wn, En) above, (Mm, Wm, Em) the row updated, (Ms, Ws,
+        // Es) loaded below; three rows per loop trip with the roles rotated
+        // by name, so no register moves carry the rows from trip to trip.
+        // mm*c + (nn + ss + ww + ee)*e + (nw + ne + sw + se)*k
+#define JPXLG_PRE_ROW(Mn, Wn, En, Mm, Wm, Em, Ms, Ws, Es)                                   \
+  {                                                                                          \
+    Ms = *reinterpret_cast<const f2*>(X + c + kPreS);                                        \
+    Ws = f2_pack(X[c + kPreS - 1], f2_lo(Ms));                                               \
+    Es = f2_pack(f2_hi(Ms), X[c + kPreS + 2]);                                               \
+    const f2 s1 = f2_add(f2_add(f2_add(Mn, Ms), Wm), Em);                                    \
+    const f2 s2 = f2_add(f2_add(f2_add(Wn, En), Ws), Es);                                    \
+    const f2 kx = f2_add(f2_add(f2_mul(Mm, c2, nz), f2_mul(s1, e2, nz)), f2_mul(s2, k2, nz)); \
+    *reinterpret_cast<f2*>(Y + c) =                                                          \
+        f2_add(Mm, f2_mul(f2_sub(*reinterpret_cast<const f2*>(F + c), kx), i2, nz));          \
+    c += kPreS;                                                                              \
+  }
+#pragma unroll 1
+        while (c + 2 * kPreS < end) {
+          JPXLG_PRE_ROW(M0, W0, E0, M1, W1, E1, M2, W2, E2)
+          JPXLG_PRE_ROW(M1, W1, E1, M2, W2, E2, M0, W0, E0)
+          JPXLG_PRE_ROW(M2, W2, E2, M0, W0, E0, M1, W1, E1)
         }
+        if (c < end) {
+          JPXLG_PRE_ROW(M0, W0, E0, M1, W1, E1, M2, W2, E2)
+          if (c < end) JPXLG_PRE_ROW(M1, W1, E1, M2, W2, E2, M0, W0, E0)
+        }
+#undef JPXLG_PRE_ROW
       }
     }
     __syncthreads();
     if (!fast) {
-      // Cells whose arithmetic is not the interior formula: whole rows at
-      // the frame's top and bottom (and from the tail row down), and on
-      // the other rows column 0 and the columns from simd_end to w - 1.
-      const int left = -gx0;  // local column of frame x = 0
-      const bool has_left = left >= lo && left < hi;
-      const int r0 = max(max(lo, simd_end - gx0), has_left ? left + 1 : lo);
-      const int r1 = min(hi, w - gx0);
-      const int nright = max(0, r1 - r0);
-      for (int ly = lo + warp; ly < hi; ly += kWarps) {
-        const int gy = gy0 + ly;
-        if (gy < 0 || gy >= h) continue;
-        const bool full = gy == 0 || gy >= row_end;
-        const int ncell = full ? hi - lo : (has_left ? 1 : 0) + nright;
-        for (int i = lane; i < ncell; i += 32) {
-          int lx;
-          if (full) lx = lo + i;
-          else if (has_left) lx = i == 0 ? left : r0 + i - 1;
-          else lx = r0 + i;
-          const int gx = gx0 + lx;
-          if (gx < 0 || gx >= w) continue;
-          const float* q = X + ly * kPreS + lx;
-          const float nw = q[-kPreS - 1], nn = q[-kPreS], ne = q[-kPreS + 1];
-          const float ww = q[-1], mm = q[0], ee = q[1];
-          const float sw = q[kPreS - 1], ss = q[kPreS], se = q[kPreS + 1];
-          const bool border = gx == 0 || gx == w - 1 || gy == 0 || gy == h - 1;
-          float kx;
-          if (!border && gx - 1 < 4 * groups) {
-            kx = mm * k.centre + (nn + ss + ww + ee) * k.edge + (nw + ne + sw + se) * k.corner;
-          } else {
-            // nine taps in order: dy = -1, 0, 1 outer, dx inner
-            float acc = 0.0f;
-            acc += k.corner * nw;
-            acc += k.edge * nn;
-            acc += k.corner * ne;
-            acc += k.edge * ww;
-            acc += k.centre * mm;
-            acc += k.edge * ee;
-            acc += k.corner * sw;
-            acc += k.edge * ss;
-            acc += k.corner * se;
-            kx = acc;
-          }
-          const int c = ly * kPreS + lx;
-          const bool in_bulk = gy < bulk_row || (gy == bulk_row && gx < bulk_col);
-          if (in_bulk) Y[c] = mm + (F[c] - kx) * k.inv_c;
-          else Y[c] = precondition_tail(mm, F[c], kx, k.centre);
-        }
-      }
-      __syncthreads();
-    }
-    // Out-of-frame halo cells take their mirror's new value: whole rows
-    // above or below the frame, and the bands left [lo, xl) and right
-    // [xr, hi) of it on the rows inside.
-    if (has_halo_out) {
-      const int xl = min(hi, max(lo, -gx0));
-      const int xr = max(lo, min(hi, w - gx0));
-      const int nl = xl - lo, nr = hi - xr;
-      for (int ly = lo + warp; ly < hi; ly += kWarps) {
-        const int gy = gy0 + ly;
-        const int my = mirror1d(gy, h) - gy0;
-        if (gy < 0 || gy >= h) {
-          for (int cx = lo + lane; cx < hi; cx += 32)
-            Y[ly * kPreS + cx] = Y[my * kPreS + mirror1d(gx0 + cx, w) - gx0];
+      // Recompute the special cells with their own rules, reading the nine
+      // taps at mirrored frame coordinates (always inside the frame and the
+      // previous step's region), so cells outside the frame are never read.
+      const Special sp = special(lo, hi);
+      const int nrow_cells = sp.nsr * sp.ncin;
+      const int total = nrow_cells + sp.nsc * sp.nrin;
+      for (int i = t; i < total; i += kPreThreads) {
+        int ly, lx;
+        if (i < nrow_cells) {
+          const int r = i / sp.ncin;
+          lx = sp.cx0 + (i - r * sp.ncin);
+          ly = sp.r0 ? (r == 0 ? -gy0 : sp.rB0 + r - 1) : sp.rB0 + r;
         } else {
-          for (int i = lane; i < nl + nr; i += 32) {
-            const int cx = i < nl ? lo + i : xr + (i - nl);
-            Y[ly * kPreS + cx] = Y[ly * kPreS + mirror1d(gx0 + cx, w) - gx0];
-          }
+          const int j = i - nrow_cells;
+          const int ci = j / sp.nrin;
+          ly = sp.nr0 + (j - ci * sp.nrin);
+          lx = sp.c0 ? (ci == 0 ? -gx0 : sp.cB0 + ci - 1) : sp.cB0 + ci;
         }
+        const int gx = gx0 + lx, gy = gy0 + ly;
+        const int xm = mirror1d(gx - 1, w) - gx0, xp = mirror1d(gx + 1, w) - gx0;
+        const int ym = (mirror1d(gy - 1, h) - gy0) * kPreS, yp = (mirror1d(gy + 1, h) - gy0) * kPreS;
+        const int y0 = ly * kPreS;
+        const float nw = X[ym + xm], nn = X[ym + lx], ne = X[ym + xp];
+        const float ww = X[y0 + xm], mm = X[y0 + lx], ee = X[y0 + xp];
+        const float sw = X[yp + xm], ss = X[yp + lx], se = X[yp + xp];
+        const bool border = gx == 0 || gx == w - 1 || gy == 0 || gy == h - 1;
+        float kx;
+        if (!border && gx - 1 < 4 * groups) {
+          kx = mm * k.centre + (nn + ss + ww + ee) * k.edge + (nw + ne + sw + se) * k.corner;
+        } else {
+          // nine taps in order: dy = -1, 0, 1 outer, dx inner
+          float acc = 0.0f;
+          acc += k.corner * nw;
+          acc += k.edge * nn;
+          acc += k.corner * ne;
+          acc += k.edge * ww;
+          acc += k.centre * mm;
+          acc += k.edge * ee;
+          acc += k.corner * sw;
+          acc += k.edge * ss;
+          acc += k.corner * se;
+          kx = acc;
+        }
+        const int c = y0 + lx;
+        const bool in_bulk = gy < bulk_row || (gy == bulk_row && gx < bulk_col);
+        if (in_bulk) Y[c] = mm + (F[c] - kx) * k.inv_c;
+        else Y[c] = precondition_tail(mm, F[c], kx, k.centre);
       }
       __syncthreads();
     }
     cur ^= 1;
   }
-  for (int ly = warp; ly < kPreTile; ly += kWarps)
-    for (int lx = lane; lx < kPreTile; lx += 32) {
-      int gx = tx0 + lx, gy = ty0 + ly;
-      if (gx < w && gy < h)
-        out[(size_t)gy * w + gx] = (cur ? X1 : X0)[(ly + kPreHalo) * kPreS + lx + kPreHalo];
+  const float* R = cur ? X1 : X0;
+  if (tx0 + kPreTile <= w && ty0 + kPreTile <= h && (w % 4) == 0 &&
+      (reinterpret_cast<uintptr_t>(out) & 15) == 0) {
+    constexpr int kV = kPreTile / 4;
+    for (int i = t; i < kPreTile * kV; i += kPreThreads) {
+      const int ly = i / kV, lx = (i - ly * kV) * 4;
+      *reinterpret_cast<float4*>(out + (size_t)(ty0 + ly) * w + tx0 + lx) =
+          *reinterpret_cast<const float4*>(R + (ly + kPreHalo) * kPreS + lx + kPreHalo);
     }
+  } else {
+    for (int i = t; i < kPreTile * kPreTile; i += kPreThreads) {
+      const int ly = i / kPreTile, lx = i - ly * kPreTile;
+      const int gx = tx0 + lx, gy = ty0 + ly;
+      if (gx < w && gy < h) out[(size_t)gy * w + gx] = R[(ly + kPreHalo) * kPreS + lx + kPreHalo];
+    }
+  }
 }
 
 void launch_precondition(const float* in, float* out, int w, int h, cudaStream_t s) {
