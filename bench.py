@@ -349,6 +349,44 @@ def run_search(ctx, torch, np, steps):
     }
 
 
+def run_select(ctxs, streams, images, dev_rgb, covers, req, steps, px_total, torch, np):
+    """Block selection over the step's device-resident images, one context
+    per stream; checks that the device maps equal the set-up's host maps."""
+    import jpxl_gb300 as jg
+
+    maps = torch.empty((len(images), (H + 7) // 8, (W + 7) // 8), dtype=torch.uint8,
+                       device="cuda")
+
+    def select_step(contexts):
+        for i in range(len(images)):
+            jg.select_blocks_device(contexts[i % len(contexts)], W, H, dev_rgb[i].data_ptr(),
+                                    BITS, req, maps[i].data_ptr())
+
+    for _ in range(3):
+        select_step(ctxs)
+    torch.cuda.synchronize()
+    s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    s0.record(streams[0])
+    for st in streams[1:]:
+        st.wait_event(s0)
+    for _ in range(steps):
+        select_step(ctxs)
+    for st in streams[1:]:
+        done = torch.cuda.Event()
+        done.record(st)
+        streams[0].wait_event(done)
+    s1.record(streams[0])
+    torch.cuda.synchronize()
+    ms = max_over_ranks(s0.elapsed_time(s1))
+    if not np.array_equal(maps.cpu().numpy(), np.stack(covers)):
+        raise RuntimeError("device and host block selection disagree")
+    return {"value": round(px_total / (ms / 1e3) / 1e6, 2), "unit": "MPix/s",
+            "ms_per_step": round(ms / steps, 3),
+            "what": ("select_blocks (XYB, inverse Gaborish, DCT8/16/32 scoring, "
+                     "quadtree decision) over the step's images, device-resident"),
+            "sequential_fallbacks": sum(c.cover_fallbacks for c in ctxs)}
+
+
 def run_ours(args):
     import numpy as np
     import torch
@@ -437,33 +475,8 @@ def run_ours(args):
 
     # Block selection (the plan build's first stage) over the same images,
     # device-resident, one context per stream as above.
-    maps = torch.empty((len(images), (H + 7) // 8, (W + 7) // 8), dtype=torch.uint8,
-                       device="cuda")
-
-    def select_step(contexts):
-        for i in range(len(images)):
-            jg.select_blocks_device(contexts[i % len(contexts)], W, H, dev_rgb[i].data_ptr(),
-                                    BITS, req, maps[i].data_ptr())
-
-    for _ in range(3):
-        select_step(ctxs)
-    torch.cuda.synchronize()
-    s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    s0.record(streams[0])
-    for st in streams[1:]:
-        st.wait_event(s0)
-    for _ in range(args.steps):
-        select_step(ctxs)
-    for st in streams[1:]:
-        done = torch.cuda.Event()
-        done.record(st)
-        streams[0].wait_event(done)
-    s1.record(streams[0])
-    torch.cuda.synchronize()
-    select_ms = max_over_ranks(s0.elapsed_time(s1))
-    select_value = px_total / (select_ms / 1e3) / 1e6
-    if not np.array_equal(maps.cpu().numpy(), np.stack(covers)):
-        raise RuntimeError("device and host block selection disagree")
+    select = None if args.no_select else run_select(
+        ctxs, streams, images, dev_rgb, covers, req, args.steps, px_total, torch, np)
 
     # Stage breakdown: the same steps on one stream with stage timers.
     ctx.stage_times()  # reset
@@ -566,11 +579,7 @@ def run_ours(args):
                 "d2h_bytes_per_step": 8 * len(images)},
         "parity": parity,
         "search": search,
-        "select": {"value": round(select_value, 2), "unit": "MPix/s",
-                   "ms_per_step": round(select_ms / args.steps, 3),
-                   "what": ("select_blocks (XYB, inverse Gaborish, DCT8/16/32 scoring, "
-                            "quadtree decision) over the step's images, device-resident"),
-                   "sequential_fallbacks": sum(c.cover_fallbacks for c in ctxs)},
+        "select": select,
         "gpu_launches": int(launches),
         "cfl_sequential_fallbacks": sum(c.cfl_fallbacks for c in ctxs),
         "clocks": clocks,
@@ -598,6 +607,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-search", action="store_true",
                     help="skip the batched quality-search leg")
+    ap.add_argument("--no-select", action="store_true",
+                    help="skip the block-selection timing leg (covers are still selected)")
     ap.add_argument("--streams", type=int, default=4,
                     help="contexts (each with its own stream) that images alternate over")
     args = ap.parse_args()

@@ -71,7 +71,7 @@ struct jpxlg_ctx {
   DevBuf rgb, xyb, pre, coeff, dyhf, qcoeff, lfs, dylf, lfq, cflx, cflb;
   DevBuf planes, aux, sigma, out;
   DevBuf lf_part, lf_seed, cfl_tile, cover, cover_map;
-  DevBuf pyr, partial, score, cxyb;
+  DevBuf pyr, partial, score, cxyb, hpl, bcarry;
   // stage timers
   struct Mark {
     int stage;
@@ -412,8 +412,10 @@ int score_device(jpxlg_ctx* ctx, const jpxlg_ref* ref, const float* cand_dev,
   CK(ctx->pyr.ensure(std::max<size_t>(pyr, 1) * sizeof(float)));
   size_t ctas_total = 0;
   for (int s = 0; s < ref->nscales; ++s)
-    ctas_total += (size_t)((ref->scales[s].w + 31) / 32) * ((ref->scales[s].h + 31) / 32);
+    ctas_total += (size_t)blur_partial_rows(ref->scales[s].w, ref->scales[s].h);
   CK(ctx->partial.ensure(ctas_total * 18 * sizeof(DF)));
+  CK(ctx->hpl.ensure(9 * (size_t)w * h * sizeof(float)));
+  CK(ctx->bcarry.ensure(blur_carry_floats(w, h) * sizeof(float)));
   int ctas[6], pixels[6];
   stage_begin(ctx, JPXLG_STAGE_SSIM);
   uint64_t k = 0;
@@ -438,8 +440,9 @@ int score_device(jpxlg_ctx* ctx, const jpxlg_ref* ref, const float* cand_dev,
       cur_xyb = next + 3 * ns;
       next += 6 * ns;
     }
-    ctas[s] = launch_score_scale(cur_xyb, false, rs, part, ctx->num_sms, ctx->stream);
-    ++k;
+    ctas[s] = launch_score_scale(cur_xyb, rs, ctx->hpl.as<float>(), ctx->bcarry.as<float>(), 0,
+                                 3, part, ctx->stream);
+    k += 4;
     pixels[s] = rs.w * rs.h;
     part += (size_t)ctas[s] * 18;
   }
@@ -474,7 +477,7 @@ int jpxlg_ctx_create(int device, uint32_t flags, jpxlg_ctx** out) {
   } while (0)
   CKC(cudaSetDevice(device));
   CKC(configure_encode_kernels());
-  CKC(configure_ssim_kernels());
+  CKC(configure_blur_kernels());
   CKC(cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking));
   c->stream = c->own_stream;
   CKC(cudaMalloc(&c->d_words, 8 * sizeof(uint32_t)));
@@ -488,13 +491,12 @@ int jpxlg_ctx_create(int device, uint32_t flags, jpxlg_ctx** out) {
   build_dequant_tables(dq.data());
   CKC(cudaMalloc(&c->d_dq, dq.size() * sizeof(float)));
   CKC(cudaMemcpy(c->d_dq, dq.data(), dq.size() * sizeof(float), cudaMemcpyHostToDevice));
-  float iv4[16], iv8[64], iv16[256], sf[12], taps[5], om[9], ob[3], oc[3];
+  float iv4[16], iv8[64], iv16[256], sf[12], om[9], ob[3], oc[3];
   build_iv_tables(iv4, iv8, iv16);
   build_scale_f(sf);
-  build_blur_taps(taps);
   build_opsin_inverse(om, ob, oc);
   upload_dct_constants(iv4, iv8, iv16, sf, c->stream);
-  upload_blur_taps(taps, c->stream);
+  upload_blur_consts(c->stream);
   upload_render_constants(om, ob, oc, c->stream);
   CKC(cudaStreamSynchronize(c->stream));
 #undef CKC
@@ -516,7 +518,7 @@ int jpxlg_ctx_destroy(jpxlg_ctx* ctx) {
                     &ctx->cflb,   &ctx->planes, &ctx->aux,    &ctx->sigma,   &ctx->out,
                     &ctx->lf_part, &ctx->lf_seed, &ctx->cfl_tile, &ctx->cover,
                     &ctx->cover_map, &ctx->pyr,  &ctx->partial,
-                    &ctx->score,  &ctx->cxyb};
+                    &ctx->score,  &ctx->cxyb,   &ctx->hpl,   &ctx->bcarry};
   for (DevBuf* b : bufs) b->release();
   for (auto& m : ctx->marks) {
     cudaEventDestroy(m.a);
@@ -813,6 +815,9 @@ int jpxlg_ssim2_ref_create(jpxlg_ctx* ctx, const float* rgb, int w, int h, uint3
   if (!ctx || !rgb || !out) return fail(ctx, JPXLG_ERR_ARGUMENT, "null argument");
   *out = nullptr;
   if (w < 8 || h < 8) return fail(ctx, JPXLG_ERR_TOO_SMALL, "SSIMULACRA2 needs at least 8x8");
+  if (w > kBlurMaxWidth)
+    return fail(ctx, JPXLG_ERR_ARGUMENT, "SSIMULACRA2 frames are limited to %d columns",
+                kBlurMaxWidth);
   cudaSetDevice(ctx->device);
   std::unique_ptr<jpxlg_ref> R(new jpxlg_ref);
   R->ctx = ctx;
@@ -838,7 +843,8 @@ int jpxlg_ssim2_ref_create(jpxlg_ctx* ctx, const float* rgb, int w, int h, uint3
   CK(cudaMalloc(&R->block, total * sizeof(float)));
   float* cursor = (float*)R->block;
   const size_t n0 = (size_t)w * h;
-  CK(ctx->aux.ensure(n0 * sizeof(float)));
+  CK(ctx->hpl.ensure(9 * n0 * sizeof(float)));
+  CK(ctx->bcarry.ensure(blur_carry_floats(w, h) * sizeof(float)));
   CK(ctx->out.ensure(3 * n0 * sizeof(float)));
   const float* src = rgb;
   if (mem == JPXLG_MEM_HOST) {
@@ -866,8 +872,9 @@ int jpxlg_ssim2_ref_create(jpxlg_ctx* ctx, const float* rgb, int w, int h, uint3
     sc.s11 = cursor;
     cursor += 3 * n;
     launch_positive_xyb(level, sc.xyb, n, ctx->num_sms, ctx->stream);
-    launch_ref_moments(sc.xyb, sc.mu, sc.s11, ctx->aux.as<float>(), sc.w, sc.h, ctx->stream);
-    k += 1 + 12;
+    launch_ref_moments(sc.xyb, sc.mu, sc.s11, ctx->hpl.as<float>(), ctx->bcarry.as<float>(), sc.w,
+                       sc.h, ctx->stream);
+    k += 1 + 4;
   }
   int rc = after_launch(ctx, k);
   if (rc) {
@@ -1226,28 +1233,38 @@ extern "C" int jpxlg_batch_probe(jpxlg_ctx* ctx, int n_items, const jpxlg_batch_
 
 // ---------------------------------------------------------------------------
 // Allocation-free scoring.  jpxlg_ssim2_score_static runs the same kernels as
-// jpxlg_ssim2_score but keeps the candidate pyramid and the per-tile partial
-// sums in one file-scope device array instead of the context's workspace, so
-// no call ever reaches cudaMalloc or cudaFree.
+// jpxlg_ssim2_score but keeps its workspace in one file-scope device array
+// instead of the context's buffers, so no call ever reaches cudaMalloc or
+// cudaFree.
 //
-// Capacity: reference frames up to kStaticMaxSide x kStaticMaxSide.  The
-// pyramid of scales 1..5 of a 2048 x 2048 frame holds
-// 3 * (1024^2 + 512^2 + 256^2 + 128^2 + 64^2) = 4,190,208 floats, and its six
-// scales cover 64^2 + 32^2 + 16^2 + 8^2 + 4^2 + 2^2 = 5,460 tiles of 32 x 32,
-// each with 18 double-float sums of 8 bytes: 17.5 MB in all.  Both counts
-// grow with width and height, so any frame within the side limit fits.
+// Capacity: reference frames up to kStaticMaxSide x kStaticMaxSide.  For a
+// 2048 x 2048 frame the workspace holds the linear pyramid of scales 1..5,
+// 3 * (1024^2 + 512^2 + 256^2 + 128^2 + 64^2) = 4,190,208 floats; the
+// current scale's candidate positive XYB, 3 * 2048^2 = 12,582,912 floats;
+// the row pass of one channel (three planes), 12,582,912 floats; the column
+// pass's segment responses and entry states of one channel,
+// 2 x 64 segments x 18 x 2048 = 4,718,592 floats; and the partial sums, one
+// row of 18 double-float sums per 32 x 32 tile of each scale,
+// 4096 + 1024 + 256 + 64 + 16 + 4 = 5,460 rows: 137 MB in all.  Every count grows with width and height, so any frame within the
+// side limit fits.
+// Channels are scored one after another so that the row pass needs one
+// channel's planes.
 //
-// Nothing in the scratch has to start at zero: each call writes every pyramid
-// level and every partial row before reading it.  There is one scratch per
-// device, so calls whose work overlaps on a device (two streams, two
-// contexts, or two host threads) race on it; callers serialise them.
+// Nothing in the scratch has to start at zero: each call writes every level,
+// plane and partial row before reading it.  There is one scratch per device,
+// so calls whose work overlaps on a device (two streams, two contexts, or
+// two host threads) race on it; callers serialise them.
 namespace {
 
 constexpr int kStaticMaxSide = 2048;
 constexpr size_t kStaticPyrFloats = 4190208;
+constexpr size_t kStaticPlaneFloats = (size_t)kStaticMaxSide * kStaticMaxSide;
 constexpr size_t kStaticPartialRows = 5460;
-constexpr size_t kStaticPyrBytes = kStaticPyrFloats * sizeof(float);  // a multiple of 256
-constexpr size_t kStaticScratchBytes = kStaticPyrBytes + kStaticPartialRows * 18 * sizeof(DF);
+constexpr size_t kStaticCarryFloats = 4718592;
+// pyramid, positive XYB, row pass, segment states
+constexpr size_t kStaticFloats = kStaticPyrFloats + 6 * kStaticPlaneFloats + kStaticCarryFloats;
+constexpr size_t kStaticFloatBytes = kStaticFloats * sizeof(float);  // a multiple of 256
+constexpr size_t kStaticScratchBytes = kStaticFloatBytes + kStaticPartialRows * 18 * sizeof(DF);
 constexpr int kStaticMaxDevices = 64;
 
 static __device__ __align__(256) unsigned char g_score_scratch[kStaticScratchBytes];
@@ -1292,13 +1309,16 @@ extern "C" int jpxlg_ssim2_score_static(jpxlg_ctx* ctx, const jpxlg_ref* ref,
   for (int s = 0; s < ref->nscales; ++s) {
     const SsimScale& rs = ref->scales[s];
     if (s > 0) pyr += 3 * (size_t)rs.w * rs.h;
-    rows += (size_t)((rs.w + 31) / 32) * ((rs.h + 31) / 32);
+    rows += (size_t)blur_partial_rows(rs.w, rs.h);
   }
   if (pyr > kStaticPyrFloats || rows > kStaticPartialRows)
     return fail(ctx, JPXLG_ERR_ARGUMENT, "static scoring scratch too small for %dx%d", ref->w,
                 ref->h);
   float* next = (float*)scratch;
-  DF* part0 = (DF*)(scratch + kStaticPyrBytes);
+  float* xyb = next + kStaticPyrFloats;
+  float* hpl = xyb + 3 * kStaticPlaneFloats;
+  float* carry = hpl + 3 * kStaticPlaneFloats;
+  DF* part0 = (DF*)(scratch + kStaticFloatBytes);
   DF* part = part0;
   const float* cur = linear_rgb_dev;
   int ctas[6], pixels[6];
@@ -1306,14 +1326,18 @@ extern "C" int jpxlg_ssim2_score_static(jpxlg_ctx* ctx, const jpxlg_ref* ref,
   for (int s = 0; s < ref->nscales; ++s) {
     const SsimScale& rs = ref->scales[s];
     if (s > 0) {
-      launch_downscale3(cur, ref->scales[s - 1].w, ref->scales[s - 1].h, next, nullptr,
-                        ctx->stream);
+      launch_downscale3(cur, ref->scales[s - 1].w, ref->scales[s - 1].h, next, xyb, ctx->stream);
       ++k;
       cur = next;
       next += 3 * (size_t)rs.w * rs.h;
+    } else {
+      launch_positive_xyb(cur, xyb, (size_t)rs.w * rs.h, ctx->num_sms, ctx->stream);
+      ++k;
     }
-    ctas[s] = launch_score_scale(cur, true, rs, part, ctx->num_sms, ctx->stream);
-    ++k;
+    for (int c = 0; c < 3; ++c) {
+      ctas[s] = launch_score_scale(xyb, rs, hpl, carry, c, 1, part, ctx->stream);
+      k += 4;
+    }
     pixels[s] = rs.w * rs.h;
     part += (size_t)ctas[s] * 18;
   }

@@ -232,6 +232,12 @@ __device__ __forceinline__ f2 f2_mul(f2 a, f2 b, f2 nz) {
   asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(nz));
   return d;
 }
+// a * b + c per lane with one rounding (the paired __fmaf_rn).
+__device__ __forceinline__ f2 f2_fma(f2 a, f2 b, f2 c) {
+  f2 d;
+  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+  return d;
+}
 
 // ---- double-float (f32 pair) sums --------------------------------------------
 // Products of two f32 are split exactly (two_prod); sums keep hi + lo to

@@ -50,7 +50,6 @@ float host_srgb_to_linear(float v);
 float host_linear_to_srgb(float v);
 void build_srgb_lut(int bits, float* out /* 256 or 65536 */);
 int build_depth_thresholds(int bits, float* thresholds, float* levels_linear);
-void build_blur_taps(float* taps /* 5: centre, +-1 .. +-4 */);
 void build_opsin_inverse(float* matrix9, float* bias3, float* bias_cbrt3);
 float host_cbrt_core(float v);
 

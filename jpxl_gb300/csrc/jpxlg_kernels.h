@@ -120,20 +120,32 @@ struct SsimScale {
   float* mu;    // [3][w*h]
   float* s11;   // [3][w*h]
 };
-void upload_blur_taps(const float* taps, cudaStream_t s);
+// The blur's constants (taps, resonators) into constant memory.
+void upload_blur_consts(cudaStream_t s);
+// Widest frame the row pass stages in shared memory (a line plus its output).
+constexpr int kBlurMaxWidth = 8192;
+size_t blur_row_smem(int w);
+cudaError_t configure_blur_kernels();
+// Rows of partial sums one scale writes (one per 32 x 32 tile), and the
+// floats of the column pass's segment-state scratch for three channels.
+int blur_partial_rows(int w, int h);
+size_t blur_carry_floats(int w, int h);
 // 2x2 mean of linear RGB planes; xyb (optional) receives the result's
 // positive XYB planes.
 void launch_downscale3(const float* in, int w, int h, float* out, float* xyb, cudaStream_t s);
 void launch_positive_xyb(const float* rgb, float* xyb, size_t n, int num_sms, cudaStream_t s);
-void launch_ref_moments(const float* xyb, float* mu, float* s11, float* tmp, int w, int h,
-                        cudaStream_t s);
-// Candidate side of one scale: cand is linear RGB [3][w*h]; partial receives
-// per-CTA double-float sums [ctas][18] (8 bytes each).
+// Reference side of one scale: mu = blur(xyb), s11 = blur(xyb * xyb) per
+// channel; hpl (6 w*h planes) and carry (blur_carry_floats) are scratch.
+void launch_ref_moments(const float* xyb, float* mu, float* s11, float* hpl, float* carry, int w,
+                        int h, cudaStream_t s);
+// Candidate side of one scale for channels c0 .. c0+nch-1: cand_xyb is the
+// candidate's positive XYB [3][w*h]; hpl (3 * nch w*h planes) and carry
+// (blur_carry_floats) are scratch; partial receives one row of 18
+// double-float sums (8 bytes each) per 32 x 32 tile, each channel filling
+// its six.  Returns the number of rows (blur_partial_rows).
 struct DF;
-// cand: the scale's candidate as linear RGB (cand_is_linear) or as its
-// positive XYB planes.
-int launch_score_scale(const float* cand, bool cand_is_linear, const SsimScale& ref, DF* partial,
-                       int num_sms, cudaStream_t s);
+int launch_score_scale(const float* cand_xyb, const SsimScale& ref, float* hpl, float* carry,
+                       int c0, int nch, DF* partial, cudaStream_t s);
 void launch_score_finish(const DF* partials, const int* ctas_per_scale, int nscales,
                          const int* pixels_per_scale, double* out /* score, raw, terms[108] */,
                          cudaStream_t s);

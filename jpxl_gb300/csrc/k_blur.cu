@@ -1,0 +1,712 @@
+// k_blur.cu — SSIMULACRA2's Gaussian (jpxl-perceptual blur.rs) evaluated to
+// the reference's f32 outputs, and the candidate side of one scale.
+//
+// blur.rs runs along every row, then along every column of that result,
+// three f64 two-pole resonators (feedback 2 cos(k pi / 10) and -1, k = 1, 3,
+// 5) fed with s_j = f32(x[j-6] + x[j+4]), and rounds their summed output to
+// f32 once per sample (blur.rs:164 step, :414 horizontal_padded, :574
+// vertical_row).  Split s_j = (x[j-6] + x[j+4]) + e_j, with e_j the rounding
+// error of the f32 pair sum (exact in f32).  The resonators fed with the
+// exact pair sums have a finite response: the 9-tap symmetric FIR
+// FIR_j = sum_d tap_d x[j+d], |d| <= 4 (the fifth harmonics cancel).  Fed
+// with the e's they ring without damping for the rest of the line: R_j.  So
+//
+//     output_j = f32(FIR_j + R_j)
+//
+// up to the reference's own f64 noise (~1e-16 relative).  R is a size- and
+// content-dependent ripple of order 1e-7 of the signal; a plain f32 FIR
+// misses it and lands tens of ulps away, which SSIMULACRA2's variance
+// differences (sigma - mu^2 with C2 = 0.0009) amplify into score errors of
+// a tenth of a point on large near-identical pairs.  Here FIR_j is a
+// double-float dot product (exact pair sums, exact products, compensated
+// accumulation; taps as hi + lo from the f64 recursion's impulse response)
+// and R_j comes from f32 resonators (R's own relative error of 1e-6 is far
+// below an output ulp); one final f32 addition rounds FIR_j + R_j.
+//
+// Lines are split into segments.  Each segment runs its resonators from
+// rest; a scan over the segments (after L steps the state is M^L times the
+// entry state plus the segment's own response, M the resonator's 2x2 step
+// matrix) gives each segment its entry state; each segment then walks again
+// from that state recording R_j, and the FIR outputs, independent of one
+// another, are formed in parallel.  Arithmetic is paired (two f32 lanes per
+// instruction, each rounded as the scalar operation): rows two at a time in
+// the row pass, columns two at a time in the column pass.
+//   B1 k_blur_rows<NQ>       one CTA per row pair and channel, one segment per
+//                            thread; NQ quantities x, x*x (and r*x), products
+//                            rounded to f32 as blur.rs:395 forms them
+//   B2 k_blur_col_local<NQ>  every 32-row segment's response from rest, a
+//                            warp per segment and 32-column strip
+//      k_blur_col_scan<NQ>   the entry states, segments in order, a thread
+//                            per column, quantity and resonator
+//   B3 k_blur_col_out<NQ>    one CTA per 32 x 32 tile and channel: the ripple
+//                            walk per column and quantity, then the outputs;
+//                            NQ = 2 writes mu and sigma11 (reference.rs:90),
+//                            NQ = 3 evaluates pool.rs:248's per-pixel terms on
+//                            the blurred mu2, sigma22, sigma12 and writes one
+//                            row of partial sums per tile
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+
+#include "jpxlg_common.cuh"
+#include "jpxlg_internal.h"
+#include "jpxlg_kernels.h"
+
+namespace jpxlg {
+
+struct BlurConsts {
+  float a[3], b[3];    // MUL_IN and MUL_PREV (blur.rs:41/:47) in f32, for the ripple
+  float th[5], tl[5];  // FIR taps (centre, +-1 .. +-4) as hi + lo
+  // U[k][n] = sin((n+1) w_k) / sin(w_k), w_k = (2k+1) pi / 10: M_k^n is
+  // [[U[n], -U[n-1]], [U[n-1], -U[n-2]]] (period 20 in n; U[-1] = 0).
+  float U[3][20];
+};
+__constant__ BlurConsts c_blur;
+
+// The constants as lane pairs for the paired forms, and the pair (+0, +0)
+// for negations.
+struct BlurPairs {
+  f2 a[3], b[3], th[5], tl[5], z;
+};
+__constant__ BlurPairs c_blur2;
+
+// blur.rs:41 / :47.
+static const double kMulIn[3] = {0.05529523572608661, -0.05883668702694998,
+                                 0.012955819110517063};
+static const double kMulPrev[3] = {1.902113032590307, 1.1755705045849463,
+                                   1.2246467991473532e-16};
+
+void upload_blur_consts(cudaStream_t s) {
+  BlurConsts bc;
+  for (int k = 0; k < 3; ++k) {
+    bc.a[k] = (float)kMulIn[k];
+    bc.b[k] = (float)kMulPrev[k];
+  }
+  // Tap d: the f64 recursion's response at output p + d to a unit sample at
+  // p, the sample entering as the right (x[j+4]) and later the left
+  // (x[j-6]) member of the pair sums.
+  for (int d = 0; d <= 4; ++d) {
+    double prev[3] = {0, 0, 0}, prev2[3] = {0, 0, 0}, out = 0.0;
+    const int p = 16;
+    for (int j = 0; j <= p + d; ++j) {
+      const double s = (j + 4 == p ? 1.0 : 0.0) + (j - 6 == p ? 1.0 : 0.0);
+      double o[3];
+      for (int k = 0; k < 3; ++k) o[k] = s * kMulIn[k] + kMulPrev[k] * prev[k] - prev2[k];
+      for (int k = 0; k < 3; ++k) {
+        prev2[k] = prev[k];
+        prev[k] = o[k];
+      }
+      out = (o[0] + o[1]) + o[2];
+    }
+    bc.th[d] = (float)out;
+    bc.tl[d] = (float)(out - (double)bc.th[d]);
+  }
+  for (int k = 0; k < 3; ++k) {
+    const double w = (2 * k + 1) * M_PI / 10.0;
+    for (int m = 0; m < 20; ++m) bc.U[k][m] = (float)(std::sin((m + 1) * w) / std::sin(w));
+  }
+  cudaMemcpyToSymbolAsync(c_blur, &bc, sizeof(bc), 0, cudaMemcpyHostToDevice, s);
+  BlurPairs bp;
+  auto pair = [](float v) {
+    uint32_t u;
+    std::memcpy(&u, &v, 4);
+    return ((unsigned long long)u << 32) | u;
+  };
+  for (int k = 0; k < 3; ++k) {
+    bp.a[k] = pair(bc.a[k]);
+    bp.b[k] = pair(bc.b[k]);
+  }
+  for (int d = 0; d < 5; ++d) {
+    bp.th[d] = pair(bc.th[d]);
+    bp.tl[d] = pair(bc.tl[d]);
+  }
+  bp.z = 0ull;
+  cudaMemcpyToSymbolAsync(c_blur2, &bp, sizeof(bp), 0, cudaMemcpyHostToDevice, s);
+}
+
+// M_k^steps for the three resonators (row-major 2x2 acting on (o[j], o[j-1])),
+// by repeated squaring in f64.
+static void resonator_power(long long steps, float out[3][4]) {
+  for (int k = 0; k < 3; ++k) {
+    double r[4] = {1, 0, 0, 1};
+    double m[4] = {kMulPrev[k], -1.0, 1.0, 0.0};
+    long long e = steps;
+    while (e > 0) {
+      if (e & 1) {
+        const double t[4] = {r[0] * m[0] + r[1] * m[2], r[0] * m[1] + r[1] * m[3],
+                             r[2] * m[0] + r[3] * m[2], r[2] * m[1] + r[3] * m[3]};
+        for (int i = 0; i < 4; ++i) r[i] = t[i];
+      }
+      const double t[4] = {m[0] * m[0] + m[1] * m[2], m[0] * m[1] + m[1] * m[3],
+                           m[2] * m[0] + m[3] * m[2], m[2] * m[1] + m[3] * m[3]};
+      for (int i = 0; i < 4; ++i) m[i] = t[i];
+      e >>= 1;
+    }
+    for (int i = 0; i < 4; ++i) out[k][i] = (float)r[i];
+  }
+}
+
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+  s = a + b;
+  const float bb = s - a;
+  e = (a - (s - bb)) + (b - bb);
+}
+
+// The ripple: three resonators fed with the pair-sum rounding errors.
+struct Ripple {
+  float p[3], q[3];  // o[j], o[j-1]
+};
+
+__device__ __forceinline__ float ripple_step(Ripple& r, float e) {
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    const float o = (e * c_blur.a[k] + c_blur.b[k] * r.p[k]) - r.q[k];
+    r.q[k] = r.p[k];
+    r.p[k] = o;
+  }
+  return (r.p[0] + r.p[1]) + r.p[2];
+}
+
+// The ripple's input at output j: what rounding added to the pair sum,
+// f32(x[j-6] + x[j+4]) - (x[j-6] + x[j+4]) (two_sum's error with its sign
+// turned).
+__device__ __forceinline__ float pair_error(float left, float right) {
+  float s, e;
+  two_sum(left, right, s, e);
+  return -e;
+}
+
+// ---- paired forms --------------------------------------------------------
+
+__device__ __forceinline__ void two_sum2(f2 a, f2 b, f2& s, f2& e) {
+  s = f2_add(a, b);
+  const f2 bb = f2_sub(s, a);
+  e = f2_add(f2_sub(a, f2_sub(s, bb)), f2_sub(b, bb));
+}
+
+// pair_error on two lanes: f32(l + r) - (l + r), i.e. two_sum's error negated
+// term by term (negation commutes with rounding).
+__device__ __forceinline__ f2 pair_error2(f2 l, f2 r) {
+  const f2 s = f2_add(l, r);
+  const f2 bb = f2_sub(s, l);
+  return f2_add(f2_sub(f2_sub(s, bb), l), f2_sub(bb, r));
+}
+
+struct Ripple2 {
+  f2 p[3], q[3];
+};
+
+__device__ __forceinline__ f2 ripple_step2(Ripple2& r, f2 e, f2 nz) {
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    const f2 o = f2_sub(f2_add(f2_mul(e, c_blur2.a[k], nz), f2_mul(c_blur2.b[k], r.p[k], nz)),
+                        r.q[k]);
+    r.q[k] = r.p[k];
+    r.p[k] = o;
+  }
+  return f2_add(f2_add(r.p[0], r.p[1]), r.p[2]);
+}
+
+// fir_exact on two lanes.
+__device__ __forceinline__ f2 fir_exact2(f2 m4, f2 m3, f2 m2, f2 m1, f2 c0, f2 p1, f2 p2, f2 p3,
+                                         f2 p4, f2 rip, f2 nz) {
+  f2 S = f2_mul(c_blur2.th[0], c0, nz);
+  f2 c = f2_fma(c_blur2.th[0], c0, f2_sub(c_blur2.z, S));
+  c = f2_fma(c_blur2.tl[0], c0, c);
+  const f2 lo[4] = {m1, m2, m3, m4}, hi[4] = {p1, p2, p3, p4};
+#pragma unroll
+  for (int d = 1; d <= 4; ++d) {
+    f2 u, ul;
+    two_sum2(lo[d - 1], hi[d - 1], u, ul);
+    const f2 p = f2_mul(c_blur2.th[d], u, nz);
+    const f2 r = f2_fma(c_blur2.th[d], u, f2_sub(c_blur2.z, p));
+    f2 q;
+    two_sum2(S, p, S, q);
+    c = f2_add(c, q);
+    c = f2_add(c, r);
+    c = f2_fma(c_blur2.th[d], ul, c);
+    c = f2_fma(c_blur2.tl[d], u, c);
+  }
+  return f2_add(S, f2_add(c, rip));
+}
+
+// ---------------------------------------------------------------------------
+// B1 — rows, two at a time (the lanes).
+// ---------------------------------------------------------------------------
+
+constexpr int kRowThreads = 128;
+constexpr int kRowLevels = 7;  // log2(kRowThreads): Kogge-Stone levels
+
+struct RowArgs {
+  const float* x;  // [3][h][w]
+  const float* r;  // [3][h][w] (NQ == 3: the reference side of r*x)
+  float* out;      // [nch][NQ][h][w]
+  int w, h, c0, seg;
+  float nz;                    // -0.0f
+  float pw[kRowLevels][3][4];  // M_k^(seg * 2^l)
+};
+
+template <int NQ>
+__global__ void __launch_bounds__(kRowThreads, 6) k_blur_rows(RowArgs a) {
+  extern __shared__ __align__(16) f2 bsm2[];
+  f2* xl = bsm2;                                      // [w + 20]: x at i - 10, both rows
+  f2* rl = NQ == 3 ? bsm2 + a.w + 20 : nullptr;       // [w + 20]: r likewise (NQ == 3)
+  f2* rip = bsm2 + (NQ == 3 ? 2 : 1) * (a.w + 20);    // [w]: R of both rows
+  __shared__ f2 carry[kRowThreads][6];
+  const int y0 = 2 * blockIdx.x, ch = blockIdx.y, c = a.c0 + ch;
+  const bool two = y0 + 1 < a.h;
+  const size_t n = (size_t)a.w * a.h;
+  const float* xr0 = a.x + n * c + (size_t)y0 * a.w;
+  const float* xr1 = two ? xr0 + a.w : xr0;
+  const float* rr0 = NQ == 3 ? a.r + n * c + (size_t)y0 * a.w : nullptr;
+  const float* rr1 = NQ == 3 ? (two ? rr0 + a.w : rr0) : nullptr;
+  const f2 nz = f2_pack(a.nz, a.nz);
+  const int t = threadIdx.x;
+  const int j0 = min(t * a.seg, a.w), j1 = min(j0 + a.seg, a.w);
+  // Both rows of x (and r) once, zero outside the line.
+#pragma unroll 8
+  for (int i = t; i < a.w + 20; i += kRowThreads) {
+    const int gx = i - 10;
+    const bool in = gx >= 0 && gx < a.w;
+    const float x0 = in ? xr0[gx] : 0.0f, x1 = in && two ? xr1[gx] : 0.0f;
+    xl[i] = f2_pack(x0, x1);
+    if (NQ == 3) {
+      const float r0 = in ? rr0[gx] : 0.0f, r1 = in && two ? rr1[gx] : 0.0f;
+      rl[i] = f2_pack(r0, r1);
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int q = 0; q < NQ; ++q) {
+    // The quantity's line sample i: x, x*x or r*x, each product rounded to
+    // f32 (blur.rs:395).
+    auto L = [&](int i) -> f2 {
+      const f2 xv = xl[i];
+      return q == 0 ? xv : (q == 1 ? f2_mul(xv, xv, nz) : f2_mul(rl[i], xv, nz));
+    };
+    // (1) the segment's ripple from rest, recorded.
+    Ripple2 rp;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) rp.p[k] = rp.q[k] = 0ull;
+#pragma unroll 4
+    for (int j = j0; j < j1; ++j) rip[j] = ripple_step2(rp, pair_error2(L(j + 4), L(j + 14)), nz);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      carry[t][2 * k] = rp.p[k];
+      carry[t][2 * k + 1] = rp.q[k];
+    }
+    __syncthreads();
+    // (2) inclusive scan over segments: S_t = sum_{u <= t} A^(t-u) B_u, per lane.
+#pragma unroll 1
+    for (int l = 0; l < kRowLevels; ++l) {
+      const int d = 1 << l;
+      f2 add[6] = {0, 0, 0, 0, 0, 0};
+      if (t >= d) {
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+          const f2 op = carry[t - d][2 * k], oq = carry[t - d][2 * k + 1];
+          const float* m = a.pw[l][k];
+          add[2 * k] = f2_add(f2_mul(f2_pack(m[0], m[0]), op, nz),
+                              f2_mul(f2_pack(m[1], m[1]), oq, nz));
+          add[2 * k + 1] = f2_add(f2_mul(f2_pack(m[2], m[2]), op, nz),
+                                  f2_mul(f2_pack(m[3], m[3]), oq, nz));
+        }
+      }
+      __syncthreads();
+      if (t >= d)
+#pragma unroll
+        for (int i = 0; i < 6; ++i) carry[t][i] = f2_add(carry[t][i], add[i]);
+      __syncthreads();
+    }
+    // (3) add the homogeneous response of the entry state (p, q) = (o[j0-1],
+    // o[j0-2]): o[j0+i] = U[i+1] p - U[i] q per resonator.
+    if (t > 0) {
+      f2 ep[3], eq[3];
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        ep[k] = carry[t - 1][2 * k];
+        eq[k] = carry[t - 1][2 * k + 1];
+      }
+#pragma unroll 4
+      for (int j = j0; j < j1; ++j) {
+        const int i = j - j0;
+        f2 hom = 0ull;
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+          const float u1 = c_blur.U[k][(i + 1) % 20], u0 = c_blur.U[k][i % 20];
+          hom = f2_add(hom, f2_sub(f2_mul(f2_pack(u1, u1), ep[k], nz),
+                                   f2_mul(f2_pack(u0, u0), eq[k], nz)));
+        }
+        rip[j] = f2_add(rip[j], hom);
+      }
+    }
+    __syncthreads();
+    // (4) the outputs, in parallel.
+    float* o0 = a.out + (size_t)(ch * NQ + q) * n + (size_t)y0 * a.w;
+    float* o1 = o0 + a.w;
+#pragma unroll 2
+    for (int j = t; j < a.w; j += kRowThreads) {
+      const int i = j + 10;
+      const f2 r = fir_exact2(L(i - 4), L(i - 3), L(i - 2), L(i - 1), L(i), L(i + 1), L(i + 2),
+                              L(i + 3), L(i + 4), rip[j], nz);
+      o0[j] = f2_lo(r);
+      if (two) o1[j] = f2_hi(r);
+    }
+    __syncthreads();
+  }
+}
+
+// ---------------------------------------------------------------------------
+// B2/B3 — columns (and the candidate's per-pixel terms).
+// ---------------------------------------------------------------------------
+
+constexpr int kColW = 32;      // columns per strip
+constexpr int kColT = 32;      // rows per segment (and per output tile)
+constexpr int kCarryWarps = 8;
+
+struct ColArgs {
+  const float* hpl;  // [nch][NQ][h][w] row-pass planes
+  float* carry;      // [2][nch][nseg][NQ * 6][w]: segment responses, then entry states
+  float* mu;         // NQ == 2: [3][h][w] outputs
+  float* s11;
+  const float* mu1;  // NQ == 3: reference mu, sigma11, positive XYB; candidate XYB
+  const float* s11r;
+  const float* rx;
+  const float* cx;
+  DF* partial;  // NQ == 3: [nseg][strips][18]
+  int w, h, c0, nseg;
+  float nz;
+  float pw[3][4];  // M_k^kColT
+};
+
+// B2a: every segment's response from rest; one warp per segment, a lane per
+// column (grid: strips x segment groups x channels).
+template <int NQ>
+__global__ void __launch_bounds__(kColW * kCarryWarps, 2) k_blur_col_local(ColArgs a) {
+  const int lane = threadIdx.x % kColW, g = threadIdx.x / kColW;
+  const int x = blockIdx.x * kColW + lane;
+  const int sg = blockIdx.y * kCarryWarps + g, ch = blockIdx.z;
+  if (sg >= a.nseg) return;
+  const size_t n = (size_t)a.w * a.h;
+  const bool col_ok = x < a.w;
+  const float* H = a.hpl + (size_t)ch * NQ * n + (col_ok ? x : 0);
+  float* C = a.carry + (size_t)ch * a.nseg * NQ * 6 * a.w + (col_ok ? x : 0);
+  auto hv = [&](int q, int row) -> float {
+    return (col_ok && row >= 0 && row < a.h) ? __ldg(H + (size_t)q * n + (size_t)row * a.w)
+                                             : 0.0f;
+  };
+  const int r0 = sg * kColT, r1 = min(r0 + kColT, a.h);
+  Ripple rp[NQ];
+#pragma unroll
+  for (int q = 0; q < NQ; ++q)
+#pragma unroll
+    for (int k = 0; k < 3; ++k) rp[q].p[k] = rp[q].q[k] = 0.0f;
+#pragma unroll 4
+  for (int j = r0; j < r1; ++j)
+#pragma unroll
+    for (int q = 0; q < NQ; ++q) ripple_step(rp[q], pair_error(hv(q, j - 6), hv(q, j + 4)));
+  if (col_ok)
+#pragma unroll
+    for (int q = 0; q < NQ; ++q)
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        C[((size_t)sg * NQ * 6 + q * 6 + 2 * k) * a.w] = rp[q].p[k];
+        C[((size_t)sg * NQ * 6 + q * 6 + 2 * k + 1) * a.w] = rp[q].q[k];
+      }
+}
+
+// B2b: entry states, segments in order; one thread per column, quantity and
+// resonator (grid: strips x channels, NQ * 3 warps).
+template <int NQ>
+__global__ void __launch_bounds__(kColW * NQ * 3) k_blur_col_scan(ColArgs a) {
+  const int lane = threadIdx.x % kColW, qk = threadIdx.x / kColW;
+  const int x = blockIdx.x * kColW + lane;
+  const int ch = blockIdx.y;
+  if (x >= a.w) return;
+  const int k = qk % 3;
+  const float* m = a.pw[k];
+  const float* C = a.carry + (size_t)ch * a.nseg * NQ * 6 * a.w + x;
+  float* E = a.carry + (size_t)gridDim.y * a.nseg * NQ * 6 * a.w +
+             (size_t)ch * a.nseg * NQ * 6 * a.w + x;
+  const size_t off = ((size_t)(qk / 3) * 6 + 2 * k) * a.w;
+  const size_t step = (size_t)NQ * 6 * a.w;
+  float sp = 0.0f, sq = 0.0f;
+#pragma unroll 8
+  for (int sg = 0; sg < a.nseg; ++sg) {
+    const float bp = __ldg(C + off + sg * step), bq = __ldg(C + off + sg * step + a.w);
+    E[off + sg * step] = sp;
+    E[off + sg * step + a.w] = sq;
+    const float np = (m[0] * sp + m[1] * sq) + bp;
+    const float nq = (m[2] * sp + m[3] * sq) + bq;
+    sp = np;
+    sq = nq;
+  }
+}
+
+constexpr int kOutThreads = 256;
+
+template <int NQ>
+__global__ void __launch_bounds__(kOutThreads, 4) k_blur_col_out(ColArgs a) {
+  __shared__ __align__(16) float tile[NQ][kColT + 10][kColW];  // rows r0-6 .. r0+kColT+3
+  __shared__ __align__(16) float rp[NQ][kColT][kColW];
+  __shared__ DF red[kOutThreads / 32][6];
+  const int sx = blockIdx.x, sg = blockIdx.y, ch = blockIdx.z, c = a.c0 + ch;
+  const int x0 = sx * kColW, r0 = sg * kColT;
+  const size_t n = (size_t)a.w * a.h;
+  const float* H = a.hpl + (size_t)ch * NQ * n;
+  const int t = threadIdx.x;
+  {
+    constexpr int kElems = (kColT + 10) * kColW;
+    constexpr int kIt = (kElems + kOutThreads - 1) / kOutThreads;
+    float v[NQ][kIt];
+#pragma unroll
+    for (int q = 0; q < NQ; ++q)
+#pragma unroll
+      for (int it = 0; it < kIt; ++it) {
+        const int i = t + it * kOutThreads;
+        const int ly = i / kColW, lx = i % kColW;
+        const int gy = r0 - 6 + ly, gx = x0 + lx;
+        v[q][it] = (i < kElems && gx < a.w && gy >= 0 && gy < a.h)
+                       ? __ldg(H + (size_t)q * n + (size_t)gy * a.w + gx)
+                       : 0.0f;
+      }
+#pragma unroll
+    for (int q = 0; q < NQ; ++q)
+#pragma unroll
+      for (int it = 0; it < kIt; ++it) {
+        const int i = t + it * kOutThreads;
+        if (i < kElems) tile[q][i / kColW][i % kColW] = v[q][it];
+      }
+  }
+  __syncthreads();
+  // The ripple in two halves of kColT / 2 rows per column and quantity: each
+  // half walks from rest (R from rest, and the first half's end state), then
+  // adds the homogeneous response of its entry state (the tile's entry for
+  // the first half; M^(kColT/2) times it plus the first half's end state for
+  // the second) through the U table.
+  constexpr int kHalf = kColT / 2;
+  __shared__ float half_end[NQ][6][kColW];
+  const bool walker = t < 2 * NQ * kColW;
+  const int wq = (t / kColW) % NQ, wh = t / (NQ * kColW), wl = t % kColW, wx = x0 + wl;
+  if (walker) {
+    Ripple st = {{0, 0, 0}, {0, 0, 0}};
+#pragma unroll 8
+    for (int r = wh * kHalf; r < (wh + 1) * kHalf; ++r)
+      rp[wq][r][wl] = ripple_step(st, pair_error(tile[wq][r][wl], tile[wq][r + 10][wl]));
+    if (wh == 0)
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        half_end[wq][2 * k][wl] = st.p[k];
+        half_end[wq][2 * k + 1][wl] = st.q[k];
+      }
+  }
+  __syncthreads();
+  if (walker) {
+    const float* C = a.carry + (size_t)gridDim.z * a.nseg * NQ * 6 * a.w +
+                     ((size_t)(ch * a.nseg + sg) * NQ * 6 + wq * 6) * a.w + wx;
+    float ep[3], eq[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      const float p = wx < a.w ? C[(size_t)(2 * k) * a.w] : 0.0f;
+      const float q = wx < a.w ? C[(size_t)(2 * k + 1) * a.w] : 0.0f;
+      if (wh == 0) {
+        ep[k] = p;
+        eq[k] = q;
+      } else {
+        // M^kHalf (p, q) + the first half's end state.
+        const float* U = c_blur.U[k];
+        const float u0 = U[(kHalf) % 20], u1 = U[(kHalf - 1) % 20], u2 = U[(kHalf - 2) % 20];
+        ep[k] = (u0 * p - u1 * q) + half_end[wq][2 * k][wl];
+        eq[k] = (u1 * p - u2 * q) + half_end[wq][2 * k + 1][wl];
+      }
+    }
+#pragma unroll 4
+    for (int i = 0; i < kHalf; ++i) {
+      float hom = 0.0f;
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        const float* U = c_blur.U[k];
+        hom += U[(i + 1) % 20] * ep[k] - U[i % 20] * eq[k];
+      }
+      rp[wq][wh * kHalf + i][wl] += hom;
+    }
+  }
+  __syncthreads();
+  // Outputs: columns 2j, 2j+1 (the lanes) of rows kR*b .. kR*b+kR-1.
+  constexpr int kR = kColT / (kOutThreads / (kColW / 2));
+  const f2 nz = f2_pack(a.nz, a.nz);
+  const int jp = t % (kColW / 2), b = t / (kColW / 2);
+  const int lx = 2 * jp, gx = x0 + lx;
+  float acc[6] = {0, 0, 0, 0, 0, 0};
+#pragma unroll
+  for (int i = 0; i < kR; ++i) {
+    const int r = kR * b + i, gy = r0 + r;
+    f2 val[NQ];
+#pragma unroll
+    for (int q = 0; q < NQ; ++q) {
+      auto tv = [&](int ly) { return *reinterpret_cast<const f2*>(&tile[q][ly][lx]); };
+      val[q] = fir_exact2(tv(r + 2), tv(r + 3), tv(r + 4), tv(r + 5), tv(r + 6), tv(r + 7),
+                          tv(r + 8), tv(r + 9), tv(r + 10),
+                          *reinterpret_cast<const f2*>(&rp[q][r][lx]), nz);
+    }
+    if (gy >= a.h || gx >= a.w) continue;
+    const bool second = gx + 1 < a.w;
+    const size_t p = (size_t)c * n + (size_t)gy * a.w + gx;
+    if (NQ == 2) {
+      a.mu[p] = f2_lo(val[0]);
+      a.s11[p] = f2_lo(val[1]);
+      if (second) {
+        a.mu[p + 1] = f2_hi(val[0]);
+        a.s11[p + 1] = f2_hi(val[1]);
+      }
+    } else {
+      // pool.rs:248 accumulate_scalar, in the reference's operation order.
+#pragma unroll
+      for (int e = 0; e < 2; ++e) {
+        if (e == 1 && !second) break;
+        const float m1 = __ldg(a.mu1 + p + e);
+        const float m2 = e ? f2_hi(val[0]) : f2_lo(val[0]);
+        const float v11 = __ldg(a.s11r + p + e);
+        const float s22 = e ? f2_hi(val[1]) : f2_lo(val[1]);
+        const float s12 = e ? f2_hi(val[NQ - 1]) : f2_lo(val[NQ - 1]);
+        const float mu11 = m1 * m1, mu22 = m2 * m2, mu12 = m1 * m2;
+        const float md = m1 - m2;
+        const float num_m = 1.0f - md * md;
+        const float num_s = 2.0f * (s12 - mu12) + 0.0009f;
+        const float den_s = (v11 - mu11) + (s22 - mu22) + 0.0009f;
+        const float d = fmaxf(1.0f - (num_m * num_s) / den_s, 0.0f);
+        const float d2 = d * d;
+        // (1 + |i2-m2|) / (1 + |i1-m1|) - 1 as a difference over the
+        // denominator (within the 0.01-point contract the fast division, at
+        // most 2 ulp off, serves; identical images give a zero numerator).
+        const float a1 = fabsf(__ldg(a.rx + p + e) - m1), a2 = fabsf(__ldg(a.cx + p + e) - m2);
+        const float d1 = __fdividef(a2 - a1, 1.0f + a1);
+        const float art = fmaxf(d1, 0.0f), lost = fmaxf(-d1, 0.0f);
+        const float art2 = art * art, lost2 = lost * lost;
+        acc[0] += d;
+        acc[1] += d2 * d2;
+        acc[2] += art;
+        acc[3] += art2 * art2;
+        acc[4] += lost;
+        acc[5] += lost2 * lost2;
+      }
+    }
+  }
+  if (NQ == 3) {
+    // threads, then warps in order, in double-float.
+    const int lane = t % 32, wid = t / 32;
+#pragma unroll
+    for (int k = 0; k < 6; ++k) {
+      const DF s = df_warp_sum(DF{acc[k], 0.0f});
+      if (lane == 0) red[wid][k] = s;
+    }
+    __syncthreads();
+    if (t < 6) {
+      DF s = red[0][t];
+      for (int i = 1; i < kOutThreads / 32; ++i) s = df_add(s, red[i][t]);
+      a.partial[((size_t)sg * gridDim.x + sx) * 18 + c * 6 + t] = s;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Launches.
+// ---------------------------------------------------------------------------
+
+namespace {
+
+int row_seg(int w) {
+  int seg = (w + kRowThreads - 1) / kRowThreads;
+  return seg | 1;  // odd: the threads' shared-memory strides fall on distinct banks
+}
+
+void fill_row_args(RowArgs& a, int w, int h) {
+  a.w = w;
+  a.h = h;
+  a.seg = row_seg(w);
+  a.nz = -0.0f;
+  for (int l = 0; l < kRowLevels; ++l) resonator_power((long long)a.seg << l, a.pw[l]);
+}
+
+void fill_col_args(ColArgs& a, int w, int h) {
+  a.w = w;
+  a.h = h;
+  a.nseg = (h + kColT - 1) / kColT;
+  a.nz = -0.0f;
+  resonator_power(kColT, a.pw);
+}
+
+}  // namespace
+
+// x, r and R lines of a row pair.
+size_t blur_row_smem(int w) { return (size_t)(3 * w + 40) * sizeof(f2); }
+
+
+cudaError_t configure_blur_kernels() {
+  const int smem = (int)blur_row_smem(kBlurMaxWidth);
+  cudaError_t e = cudaFuncSetAttribute(k_blur_rows<2>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  if (e != cudaSuccess) return e;
+  return cudaFuncSetAttribute(k_blur_rows<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+}
+
+int blur_partial_rows(int w, int h) {
+  return ((w + kColW - 1) / kColW) * ((h + kColT - 1) / kColT);
+}
+
+size_t blur_carry_floats(int w, int h) {
+  return (size_t)2 * 3 * ((h + kColT - 1) / kColT) * 3 * 6 * w;
+}
+
+void launch_ref_moments(const float* xyb, float* mu, float* s11, float* hpl, float* carry, int w,
+                        int h, cudaStream_t s) {
+  RowArgs ra{};
+  ra.x = xyb;
+  ra.out = hpl;
+  ra.c0 = 0;
+  fill_row_args(ra, w, h);
+  k_blur_rows<2><<<dim3((h + 1) / 2, 3), kRowThreads, blur_row_smem(w), s>>>(ra);
+  ColArgs ca{};
+  ca.hpl = hpl;
+  ca.carry = carry;
+  ca.mu = mu;
+  ca.s11 = s11;
+  ca.c0 = 0;
+  fill_col_args(ca, w, h);
+  const int strips = (w + kColW - 1) / kColW;
+  const int groups = (ca.nseg + kCarryWarps - 1) / kCarryWarps;
+  k_blur_col_local<2><<<dim3(strips, groups, 3), kColW * kCarryWarps, 0, s>>>(ca);
+  k_blur_col_scan<2><<<dim3(strips, 3), kColW * 2 * 3, 0, s>>>(ca);
+  k_blur_col_out<2><<<dim3(strips, ca.nseg, 3), kOutThreads, 0, s>>>(ca);
+}
+
+int launch_score_scale(const float* cand_xyb, const SsimScale& ref, float* hpl, float* carry,
+                       int c0, int nch, DF* partial, cudaStream_t s) {
+  const int w = ref.w, h = ref.h;
+  RowArgs ra{};
+  ra.x = cand_xyb;
+  ra.r = ref.xyb;
+  ra.out = hpl;
+  ra.c0 = c0;
+  fill_row_args(ra, w, h);
+  k_blur_rows<3><<<dim3((h + 1) / 2, nch), kRowThreads, blur_row_smem(w), s>>>(ra);
+  ColArgs ca{};
+  ca.hpl = hpl;
+  ca.carry = carry;
+  ca.mu1 = ref.mu;
+  ca.s11r = ref.s11;
+  ca.rx = ref.xyb;
+  ca.cx = cand_xyb;
+  ca.partial = partial;
+  ca.c0 = c0;
+  fill_col_args(ca, w, h);
+  const int strips = (w + kColW - 1) / kColW;
+  const int groups = (ca.nseg + kCarryWarps - 1) / kCarryWarps;
+  k_blur_col_local<3><<<dim3(strips, groups, nch), kColW * kCarryWarps, 0, s>>>(ca);
+  k_blur_col_scan<3><<<dim3(strips, nch), kColW * 3 * 3, 0, s>>>(ca);
+  k_blur_col_out<3><<<dim3(strips, ca.nseg, nch), kOutThreads, 0, s>>>(ca);
+  return blur_partial_rows(w, h);
+}
+
+}  // namespace jpxlg

@@ -789,7 +789,7 @@ __global__ void __launch_bounds__(kCflThreads) k_cfl_tile_bits(EncArgs a,
     s_rstep[ch][cell] = 1.0f / st;
   }
   __syncthreads();
-  unsigned long long bits[2][4] = {{0, 0, 0, 0}, {0, 0, 0, 0}};
+  uint32_t bits[2][4] = {{0, 0, 0, 0}, {0, 0, 0, 0}};
   float kx[4], kb[4];
 #pragma unroll
   for (int i = 0; i < 4; ++i) {
@@ -832,7 +832,7 @@ __global__ void __launch_bounds__(kCflThreads) k_cfl_tile_bits(EncArgs a,
     uint32_t v[8];
 #pragma unroll
     for (int q = 0; q < 8; ++q) {
-      v[q] = (uint32_t)bits[q / 4][q % 4];
+      v[q] = bits[q / 4][q % 4];
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) v[q] += __shfl_xor_sync(0xffffffffu, v[q], o);
     }

@@ -217,21 +217,6 @@ int build_depth_thresholds(int bits, float* thresholds, float* levels_linear) {
   return levels;
 }
 
-// jpxl-perceptual blur.rs: the three truncated-cosine resonators fed with
-// x[n-N-1] + x[n+N-1] have, in exact arithmetic, a finite impulse response of
-// nine taps (the cosines' fifth harmonics cancel beyond |k| = 4).  Tap k is
-// sum_j MUL_IN[j] * sin((5-k) w_j) / sin(w_j) with 2 cos(w_j) = MUL_PREV[j].
-void build_blur_taps(float* taps) {
-  static const double mul_in[3] = {0.05529523572608661, -0.05883668702694998,
-                                   0.012955819110517063};
-  static const double omega[3] = {M_PI / 10.0, 3.0 * M_PI / 10.0, M_PI / 2.0};
-  for (int k = 0; k <= 4; ++k) {
-    double t = 0.0;
-    for (int j = 0; j < 3; ++j) t += mul_in[j] * std::sin((5 - k) * omega[j]) / std::sin(omega[j]);
-    taps[k] = (float)t;
-  }
-}
-
 // jpxl-core simd.rs:36 on the host (used for the opsin bias cube roots).
 float host_cbrt_core(float value) {
   const uint32_t B1 = 709958130u, B2 = 642849266u;
