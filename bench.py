@@ -530,12 +530,22 @@ def run_ours(args):
     per_launch_s = top_ms / 1e3 / max(top_launches, 1)
     achieved = bytes_per_launch / per_launch_s / 1e9
     peak, peak_kind = measured_peaks()
-    # DRAM bytes per launch of the stage's kernel from the committed ncu capture
-    # of this workload (single-kernel stages only).
-    traffic = None
+    # DRAM bytes per launch from the committed ncu capture of this workload:
+    # a single-kernel stage's kernel, or for the metric's stage the DRAM bytes
+    # of its scale-0 kernels, times 4/3 for the pyramid's smaller scales,
+    # spread over the stage's launches per probe.
+    traffic, traffic_basis = None, None
     tf = ROOT / "profiles" / "traffic_2048x2048_rgb16.json"
-    if tf.exists() and (W, H) == (2048, 2048) and top in STAGE_KERNEL:
-        traffic = json.loads(tf.read_text()).get(STAGE_KERNEL[top])
+    if tf.exists() and (W, H) == (2048, 2048):
+        measured = json.loads(tf.read_text())
+        if top in STAGE_KERNEL and STAGE_KERNEL[top] in measured:
+            traffic = measured[STAGE_KERNEL[top]]
+            traffic_basis = f"{STAGE_KERNEL[top]}, one launch (ncu)"
+        elif top == "ssim" and all(k in measured for k in SSIM_SCALE0_KERNELS):
+            per_probe = sum(measured[k] for k in SSIM_SCALE0_KERNELS) * 4 / 3
+            traffic = int(per_probe * n_img / max(top_launches, 1))
+            traffic_basis = ("ssim stage: " + " + ".join(SSIM_SCALE0_KERNELS) +
+                             " at scale 0 (ncu) x 4/3 for scales 1-5, per launch of the stage")
 
     # CPU baseline: the restatement on a bounded sample, one thread; the same
     # sample through the CUDA path gives the errors reported beside the number.
@@ -569,7 +579,8 @@ def run_ours(args):
         "stages_ms": {k: round(v[0] / args.steps, 4) for k, v in stages.items()},
         "roofline": {"kernel": top, "bound": "hbm", "achieved": round(achieved, 1),
                      "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4),
-                     "peak_kind": peak_kind, "traffic": traffic},
+                     "peak_kind": peak_kind, "traffic": traffic,
+                     "traffic_basis": traffic_basis},
         "cpu_baseline": {"value": cpu_value, "unit": "MPix/s", "cores": 1,
                          "kind": "port",
                          "sample": f"one {CPU_SAMPLE}x{CPU_SAMPLE} RGB16 crop of image 0, full "
@@ -593,6 +604,8 @@ def run_ours(args):
 # Stages that are one kernel launch per image, and that kernel.
 STAGE_KERNEL = {"precondition": "k_precondition", "gaborish": "k_gaborish", "xyb": "k_srgb_to_xyb",
                 "colour": "k_colour_out"}
+# The metric stage's kernels that carry its DRAM traffic (per scale).
+SSIM_SCALE0_KERNELS = ("k_blur_rows<3>", "k_blur_col_local<3>", "k_blur_col_out<3>")
 
 
 def main():

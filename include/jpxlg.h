@@ -183,7 +183,9 @@ int jpxlg_reconstruct(jpxlg_ctx* ctx, const jpxlg_layout* layout, const jpxlg_pl
                       const jpxlg_params* params, int out_kind, int bits, void* out,
                       uint32_t mem);
 
-/* SSIMULACRA2 reference moments of a linear-sRGB image (planes follow mem). */
+/* SSIMULACRA2 reference moments of a linear-sRGB image (planes follow mem).
+ * Frames are limited to 8192 columns (the row pass stages a row pair in
+ * shared memory); wider ones return JPXLG_ERR_ARGUMENT. */
 int jpxlg_ssim2_ref_create(jpxlg_ctx* ctx, const float* linear_rgb, int width, int height,
                            uint32_t mem, jpxlg_ref** out);
 int jpxlg_ssim2_ref_destroy(jpxlg_ref* ref);

@@ -199,18 +199,46 @@ def test_score_identical_is_exactly_one_hundred(ctx, oracle):
     assert jg.score_pair(ctx, a, a) == 100.0
 
 
-@pytest.mark.parametrize("w,h,amp", [(320, 240, 0.002), (320, 240, 0.03), (67, 45, 0.01)])
+# The blur reproduces the reference's f32 outputs (up to its f64 rounding
+# ties), so scores agree far inside the 0.01-point contract; MEASURED_TOL
+# holds that.  Sizes cover the minimum frame, widths and heights that are not
+# multiples of the 32-column strips or 32-row tiles, a single strip, tall and
+# wide frames (many segments along one axis) and the widest row the row pass
+# stages.
+MEASURED_TOL = 1e-4
+
+
+@pytest.mark.parametrize("w,h,amp", [(320, 240, 0.002), (320, 240, 0.03), (67, 45, 0.01),
+                                     (8, 8, 0.02), (33, 1000, 0.005), (1000, 33, 0.005),
+                                     (8192, 24, 0.003), (517, 331, 0.0005)])
 def test_score_matches_the_restatement(ctx, oracle, w, h, amp):
     a, b = oracle.perceptual_pair(w, h, 2, amp, 7)
-    want, _, _ = oracle.ssim2(a, b)
+    want, _, want_terms = oracle.ssim2(a, b)
     got = jg.score_pair(ctx, a, b)
     assert abs(got - want) < SCORE_TOL, (got, want)
+    assert abs(got - want) < MEASURED_TOL, (got, want)
+    ref = jg.PrecomputedReference(ctx, a)
+    try:
+        terms = np.asarray(jg.Ssimulacra2(ctx).score(ref, b).terms)[: len(want_terms)]
+    finally:
+        ref.close()
+    # every pooled norm, not only their weighted sum (norms of near-zero maps
+    # move by ~1e-8 where a blurred value sits on one of the reference's f64
+    # rounding ties)
+    assert np.allclose(terms, want_terms, rtol=1e-3, atol=1e-7), np.max(np.abs(terms - want_terms))
 
 
 def test_score_of_the_recorded_4mp_pair(ctx, oracle):
     a, b = oracle.perceptual_pair(2400, 1800, 9, 0.01, 3)
     got = jg.score_pair(ctx, a, b)
     assert abs(got - 77.38494501660614) < SCORE_TOL
+    assert abs(got - 77.38494501660614) < MEASURED_TOL
+
+
+def test_wider_than_the_row_pass_is_an_error(ctx):
+    a = np.zeros((3, 8, 8193), np.float32)
+    with pytest.raises(jg.JpxlError):
+        jg.PrecomputedReference(ctx, a)
 
 
 def test_probe_equals_encode_render_score(ctx, oracle):
