@@ -67,7 +67,7 @@ __constant__ BlurConsts c_blur;
 // The constants as lane pairs for the paired forms, and the pair (+0, +0)
 // for negations.
 struct BlurPairs {
-  f2 a[3], b[3], th[5], tl[5], z;
+  f2 a[3], b[3], th[5], tl[5], nth[5], ntl[5], z;  // nth, ntl: the taps negated
 };
 __constant__ BlurPairs c_blur2;
 
@@ -120,6 +120,8 @@ void upload_blur_consts(cudaStream_t s) {
   for (int d = 0; d < 5; ++d) {
     bp.th[d] = pair(bc.th[d]);
     bp.tl[d] = pair(bc.tl[d]);
+    bp.nth[d] = pair(-bc.th[d]);
+    bp.ntl[d] = pair(-bc.tl[d]);
   }
   bp.z = 0ull;
   cudaMemcpyToSymbolAsync(c_blur2, &bp, sizeof(bp), 0, cudaMemcpyHostToDevice, s);
@@ -208,27 +210,28 @@ __device__ __forceinline__ f2 ripple_step2(Ripple2& r, f2 e, f2 nz) {
   return f2_add(f2_add(r.p[0], r.p[1]), r.p[2]);
 }
 
-// fir_exact on two lanes.
+// The double-float FIR on two lanes.  The low word is kept negated (cn = -c,
+// exact since rounding is symmetric) so that every product error comes from
+// one FMA with a negated tap: fma(-t, u, t*u rounded) = -(t*u - its rounding).
 __device__ __forceinline__ f2 fir_exact2(f2 m4, f2 m3, f2 m2, f2 m1, f2 c0, f2 p1, f2 p2, f2 p3,
                                          f2 p4, f2 rip, f2 nz) {
   f2 S = f2_mul(c_blur2.th[0], c0, nz);
-  f2 c = f2_fma(c_blur2.th[0], c0, f2_sub(c_blur2.z, S));
-  c = f2_fma(c_blur2.tl[0], c0, c);
+  f2 cn = f2_fma(c_blur2.ntl[0], c0, f2_fma(c_blur2.nth[0], c0, S));
   const f2 lo[4] = {m1, m2, m3, m4}, hi[4] = {p1, p2, p3, p4};
 #pragma unroll
   for (int d = 1; d <= 4; ++d) {
     f2 u, ul;
     two_sum2(lo[d - 1], hi[d - 1], u, ul);
     const f2 p = f2_mul(c_blur2.th[d], u, nz);
-    const f2 r = f2_fma(c_blur2.th[d], u, f2_sub(c_blur2.z, p));
+    const f2 rn = f2_fma(c_blur2.nth[d], u, p);  // -(th*u - p)
     f2 q;
     two_sum2(S, p, S, q);
-    c = f2_add(c, q);
-    c = f2_add(c, r);
-    c = f2_fma(c_blur2.th[d], ul, c);
-    c = f2_fma(c_blur2.tl[d], u, c);
+    cn = f2_sub(cn, q);
+    cn = f2_add(cn, rn);
+    cn = f2_fma(c_blur2.nth[d], ul, cn);
+    cn = f2_fma(c_blur2.ntl[d], u, cn);
   }
-  return f2_add(S, f2_add(c, rip));
+  return f2_add(S, f2_sub(rip, cn));
 }
 
 // ---------------------------------------------------------------------------
