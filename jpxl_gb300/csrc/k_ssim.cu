@@ -113,6 +113,8 @@ __global__ void __launch_bounds__(kFinishThreads) k_score_finish(const DF* __res
   for (int s = 0; s < fa.nscales; ++s) {
     if (g < kFinishGroups) {
       DF acc{0.0f, 0.0f};
+      // Loads run ahead of the (sequential, fixed-order) additions.
+#pragma unroll 8
       for (int i = g; i < fa.ctas[s]; i += kFinishGroups)
         acc = df_add(acc, partials[(base + i) * 18 + k]);
       gsum[g][k] = acc;
