@@ -76,7 +76,8 @@ typedef enum {
   JPXLG_ERR_CUDA = -4,         /* CUDA runtime failure */
   JPXLG_ERR_NO_DEVICE = -5,    /* no usable sm_103 device */
   JPXLG_ERR_TOO_SMALL = -6,    /* SSIMULACRA2 needs 8x8 (MetricError::TooSmall) */
-  JPXLG_ERR_MISMATCH = -7      /* dimensions differ (MetricError::DimensionMismatch) */
+  JPXLG_ERR_MISMATCH = -7,     /* dimensions differ (MetricError::DimensionMismatch) */
+  JPXLG_ERR_STREAM = -8        /* malformed or truncated entropy-coded stream (EntropyError) */
 } jpxlg_status;
 
 enum { JPXLG_MEM_HOST = 0, JPXLG_MEM_DEVICE = 1 };
@@ -254,6 +255,33 @@ int jpxlg_batch_run(jpxlg_ctx* ctx, jpxlg_batch* batch, double* scores, uint32_t
 int jpxlg_batch_destroy(jpxlg_batch* batch);
 int jpxlg_batch_probe(jpxlg_ctx* ctx, int n_items, const jpxlg_batch_item* items,
                       double* scores);
+
+/* Host-side entropy decoding (ISO/IEC 18181-1 Annex C), replacing
+ * jpxl-entropy's SymbolDecoder (crates/jpxl-entropy/src/decoder.rs):
+ *   jpxlg_symbols_open     SymbolDecoder::open: reads the distribution bundle
+ *                          (LZ77 parameters, context map, hybrid-uint
+ *                          configurations, prefix codes or ANS
+ *                          distributions) starting at bit `bit_offset` of
+ *                          data[0..size) (LSB-first, the codestream's bit
+ *                          order) and seeds the ANS state; num_dist is the
+ *                          number of contexts the referencing clause supplies
+ *   jpxlg_symbols_read     SymbolDecoder::read_uint for context `ctx`
+ *   jpxlg_symbols_read_many  read_uint for a sequence of contexts
+ *   jpxlg_symbols_set_dist_multiplier  set_dist_multiplier (LZ77 row stride)
+ *   jpxlg_symbols_finish   SymbolDecoder::finish: JPXLG_OK when an ANS stream
+ *                          ends in its final state (C.3.2)
+ *   jpxlg_symbols_bits_read  the reader position, in bits from data[0]
+ * The stream is copied at open.  Malformed or truncated streams return
+ * JPXLG_ERR_STREAM.  Host code only: no device is needed. */
+typedef struct jpxlg_symbols jpxlg_symbols;
+int jpxlg_symbols_open(const uint8_t* data, size_t size, size_t bit_offset, uint32_t num_dist,
+                       jpxlg_symbols** out);
+int jpxlg_symbols_read(jpxlg_symbols* s, uint32_t ctx, uint32_t* value);
+int jpxlg_symbols_read_many(jpxlg_symbols* s, const uint32_t* ctx, size_t n, uint32_t* values);
+int jpxlg_symbols_set_dist_multiplier(jpxlg_symbols* s, uint32_t multiplier);
+int jpxlg_symbols_finish(const jpxlg_symbols* s);
+size_t jpxlg_symbols_bits_read(const jpxlg_symbols* s);
+int jpxlg_symbols_destroy(jpxlg_symbols* s);
 
 /* Allocation-free variant of jpxlg_ssim2_score; it has no counterpart in the
  * reference.  The candidate (device planes) is scored against `ref` using a

@@ -439,6 +439,63 @@ class BatchProbe:
             pass
 
 
+class SymbolDecoder:
+    """jpxl-entropy decoder.rs SymbolDecoder over the library's host-side
+    Annex C decoder (jpxlg_symbols_*): ``open`` reads the distribution bundle
+    of an entropy-coded stream at bit ``bit_offset`` of ``data`` (LSB-first),
+    ``read_uint`` pulls integers per context, ``finish`` checks the ANS final
+    state.  Host code; no device is needed."""
+
+    def __init__(self, data: bytes, num_dist: int, bit_offset: int = 0):
+        self.lib = _lib.load()
+        buf = np.frombuffer(bytes(data), np.uint8)
+        h = C.c_void_p()
+        rc = self.lib.jpxlg_symbols_open(buf.ctypes.data if buf.size else None, buf.size,
+                                         bit_offset, num_dist, C.byref(h))
+        if rc:
+            raise JpxlError(rc, "jpxlg_symbols_open")
+        self.handle = h
+
+    def set_dist_multiplier(self, multiplier: int) -> None:
+        self.lib.jpxlg_symbols_set_dist_multiplier(self.handle, multiplier)
+
+    def read_uint(self, ctx: int) -> int:
+        v = C.c_uint32()
+        rc = self.lib.jpxlg_symbols_read(self.handle, ctx, C.byref(v))
+        if rc:
+            raise JpxlError(rc, f"jpxlg_symbols_read (context {ctx})")
+        return v.value
+
+    def read_many(self, contexts) -> np.ndarray:
+        ctx = np.ascontiguousarray(contexts, np.uint32)
+        out = np.zeros(ctx.size, np.uint32)
+        rc = self.lib.jpxlg_symbols_read_many(self.handle, ctx.ctypes.data, ctx.size,
+                                              out.ctypes.data)
+        if rc:
+            raise JpxlError(rc, "jpxlg_symbols_read_many")
+        return out
+
+    def finish(self) -> None:
+        rc = self.lib.jpxlg_symbols_finish(self.handle)
+        if rc:
+            raise JpxlError(rc, "ANS stream did not end in its final state")
+
+    @property
+    def bits_read(self) -> int:
+        return int(self.lib.jpxlg_symbols_bits_read(self.handle))
+
+    def close(self):
+        if self.handle:
+            self.lib.jpxlg_symbols_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 def score_pair(ctx: Context, ref_rgb: np.ndarray, cand_rgb: np.ndarray) -> float:
     """jpxl-perceptual lib.rs:195 score_pair on linear [3, H, W] planes."""
     a = np.ascontiguousarray(ref_rgb, dtype=np.float32)

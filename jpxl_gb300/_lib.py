@@ -45,6 +45,13 @@ SIGNATURES: dict[str, tuple] = {
     "jpxlg_batch_run": (_I, [_P, _P, _P, _U32]),
     "jpxlg_batch_destroy": (_I, [_P]),
     "jpxlg_batch_probe": (_I, [_P, _I, _P, _P]),
+    "jpxlg_symbols_open": (_I, [_P, C.c_size_t, C.c_size_t, _U32, C.POINTER(_P)]),
+    "jpxlg_symbols_read": (_I, [_P, _U32, C.POINTER(_U32)]),
+    "jpxlg_symbols_read_many": (_I, [_P, _P, C.c_size_t, _P]),
+    "jpxlg_symbols_set_dist_multiplier": (_I, [_P, _U32]),
+    "jpxlg_symbols_finish": (_I, [_P]),
+    "jpxlg_symbols_bits_read": (C.c_size_t, [_P]),
+    "jpxlg_symbols_destroy": (_I, [_P]),
 }
 
 
