@@ -209,6 +209,10 @@ def gpu_parity(ctx, crop, ccover, oracle_out, np):
         "cfl_mismatches": int(np.count_nonzero(plan.cfl_x != plan_c["cfl_x"]) +
                               np.count_nonzero(plan.cfl_b != plan_c["cfl_b"])),
         "pixel_max_abs": float(np.max(np.abs(lin.astype(np.float64) - lin_c))),
+        "pixel_rmse": float(np.sqrt(np.mean((lin.astype(np.float64) - lin_c) ** 2))),
+        # linear-at-depth values are one per 16-bit level, so unequal values
+        # are unequal output levels
+        "dn_mismatches": int(np.count_nonzero(lin != lin_c)),
         "score_abs_diff": float(abs(score - score_c)),
     }
 

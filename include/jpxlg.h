@@ -283,6 +283,49 @@ int jpxlg_symbols_finish(const jpxlg_symbols* s);
 size_t jpxlg_symbols_bits_read(const jpxlg_symbols* s);
 int jpxlg_symbols_destroy(jpxlg_symbols* s);
 
+/* Host-side codestream reader for the lossy VarDCT path, replacing the front
+ * end of jpxl-decode's decode (crates/jpxl-decode/src/decode.rs:400 decode,
+ * :2513 decode_vardct_frame, vardct/hf_coeff.rs:689 decode_hf_group): the
+ * image headers, frame header and TOC, modular sub-bitstreams (MA trees,
+ * H.3/H.5 predictors) and the VarDCT sections, decoded to the frame's integer
+ * content.  Bare codestreams with one regular frame; ICC profiles, previews,
+ * patches, splines, noise, LF frames, extra channels and modular transforms
+ * are reported as unsupported (JPXLG_ERR_STREAM with a reason in
+ * jpxlg_codestream_last_error).  Host code only: no device is needed.
+ *   jpxlg_codestream_open          parse and decode; *out owns the result
+ *   jpxlg_codestream_info          sizes, frame parameters, per-DctSelect
+ *                                  varblock counts, and how many sections
+ *                                  ended in their TOC entry's last byte
+ *   jpxlg_codestream_blocks        quantized LF (3 planes X, Y, B of
+ *                                  blocks_w x blocks_h), the block map
+ *                                  (DctSelect | 0x80 at varblock origins), HF
+ *                                  multipliers, EPF sharpness, and the CfL
+ *                                  factors of each 64x64 tile; NULL skips one
+ *   jpxlg_codestream_coefficients  quantized HF coefficients as the plan's
+ *                                  coefficient image, 3 x (8*blocks_h) x
+ *                                  (8*blocks_w)
+ *   jpxlg_codestream_channel       a modular frame's channel, width x height */
+typedef struct jpxlg_codestream jpxlg_codestream;
+typedef struct {
+  uint32_t width, height, bits_per_sample, xyb_encoded, colour_space;
+  int32_t transfer;
+  uint32_t encoding, num_passes, gaborish, gaborish_custom, epf_iters, x_qm_scale, b_qm_scale;
+  uint32_t adaptive_lf_smoothing, global_scale, quant_lf, extra_precision, default_matrices;
+  uint32_t default_lf_dequant, default_chroma_correlation;
+  int32_t x_factor_lf, b_factor_lf;
+  uint32_t blocks_w, blocks_h, num_varblocks, num_channels, sections, sections_exact;
+  uint32_t transform_counts[27];
+} jpxlg_codestream_info_t;
+int jpxlg_codestream_open(const uint8_t* data, size_t size, jpxlg_codestream** out);
+const char* jpxlg_codestream_last_error(void);
+int jpxlg_codestream_info(const jpxlg_codestream* cs, jpxlg_codestream_info_t* info);
+int jpxlg_codestream_blocks(const jpxlg_codestream* cs, int32_t* lf, uint8_t* block_map,
+                            uint32_t* hf_mul, uint8_t* sharpness, int8_t* x_from_y,
+                            int8_t* b_from_y);
+int jpxlg_codestream_coefficients(const jpxlg_codestream* cs, int32_t* out);
+int jpxlg_codestream_channel(const jpxlg_codestream* cs, uint32_t index, int32_t* out);
+int jpxlg_codestream_destroy(jpxlg_codestream* cs);
+
 /* Allocation-free variant of jpxlg_ssim2_score; it has no counterpart in the
  * reference.  The candidate (device planes) is scored against `ref` using a
  * fixed device scratch inside the library instead of the context's

@@ -496,6 +496,82 @@ class SymbolDecoder:
             pass
 
 
+class _CodestreamInfo(C.Structure):
+    _fields_ = [(n, C.c_uint32) for n in ("width", "height", "bits_per_sample", "xyb_encoded",
+                                          "colour_space")] + [("transfer", C.c_int32)] + \
+        [(n, C.c_uint32) for n in ("encoding", "num_passes", "gaborish", "gaborish_custom",
+                                   "epf_iters", "x_qm_scale", "b_qm_scale",
+                                   "adaptive_lf_smoothing", "global_scale", "quant_lf",
+                                   "extra_precision", "default_matrices", "default_lf_dequant",
+                                   "default_chroma_correlation")] + \
+        [("x_factor_lf", C.c_int32), ("b_factor_lf", C.c_int32)] + \
+        [(n, C.c_uint32) for n in ("blocks_w", "blocks_h", "num_varblocks", "num_channels",
+                                   "sections", "sections_exact")] + \
+        [("transform_counts", C.c_uint32 * 27)]
+
+
+class Codestream:
+    """jpxl-decode's front end (decode.rs:400 decode up to the VarDCT
+    frame's integer content, decode.rs:2513) over the library's host-side
+    codestream reader (jpxlg_codestream_*).  ``info`` holds the headers'
+    parameters; ``blocks()`` and ``coefficients()`` return the quantized LF,
+    block map, HF multipliers, sharpness, CfL factors and coefficient image
+    in the plan's layout.  Host code; no device is needed."""
+
+    def __init__(self, data: bytes):
+        self.lib = _lib.load()
+        buf = np.frombuffer(bytes(data), np.uint8)
+        h = C.c_void_p()
+        rc = self.lib.jpxlg_codestream_open(buf.ctypes.data if buf.size else None, buf.size,
+                                            C.byref(h))
+        if rc:
+            raise JpxlError(rc, "jpxlg_codestream_open: " +
+                            self.lib.jpxlg_codestream_last_error().decode())
+        self.handle = h
+        raw = _CodestreamInfo()
+        self.lib.jpxlg_codestream_info(self.handle, C.byref(raw))
+        self.info = {n: getattr(raw, n) for n, _ in _CodestreamInfo._fields_}
+        self.info["transform_counts"] = list(raw.transform_counts)
+
+    def blocks(self) -> dict:
+        bw, bh = self.info["blocks_w"], self.info["blocks_h"]
+        tw, th = (self.info["width"] + 63) // 64, (self.info["height"] + 63) // 64
+        out = {"lf": np.zeros((3, bh, bw), np.int32), "block_map": np.zeros((bh, bw), np.uint8),
+               "hf_mul": np.zeros((bh, bw), np.uint32), "sharpness": np.zeros((bh, bw), np.uint8),
+               "cfl_x": np.zeros((th, tw), np.int8), "cfl_b": np.zeros((th, tw), np.int8)}
+        rc = self.lib.jpxlg_codestream_blocks(self.handle, *(out[k].ctypes.data for k in (
+            "lf", "block_map", "hf_mul", "sharpness", "cfl_x", "cfl_b")))
+        if rc:
+            raise JpxlError(rc, "jpxlg_codestream_blocks")
+        return out
+
+    def coefficients(self) -> np.ndarray:
+        bw, bh = self.info["blocks_w"], self.info["blocks_h"]
+        out = np.zeros((3, 8 * bh, 8 * bw), np.int32)
+        rc = self.lib.jpxlg_codestream_coefficients(self.handle, out.ctypes.data)
+        if rc:
+            raise JpxlError(rc, "jpxlg_codestream_coefficients")
+        return out
+
+    def channel(self, index: int) -> np.ndarray:
+        out = np.zeros((self.info["height"], self.info["width"]), np.int32)
+        rc = self.lib.jpxlg_codestream_channel(self.handle, index, out.ctypes.data)
+        if rc:
+            raise JpxlError(rc, "jpxlg_codestream_channel")
+        return out
+
+    def close(self):
+        if getattr(self, "handle", None):
+            self.lib.jpxlg_codestream_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 def score_pair(ctx: Context, ref_rgb: np.ndarray, cand_rgb: np.ndarray) -> float:
     """jpxl-perceptual lib.rs:195 score_pair on linear [3, H, W] planes."""
     a = np.ascontiguousarray(ref_rgb, dtype=np.float32)

@@ -24,7 +24,7 @@ LIB = OUT_DIR / "libjpxlg.so"
 INCLUDE = HERE.parent / "include"
 
 UNITS = ["tables.cu", "k_encode.cu", "k_cover.cu", "k_render.cu", "k_ssim.cu", "k_blur.cu",
-         "jpxlg_api.cu", "entropy.cu"]
+         "jpxlg_api.cu", "entropy.cu", "codestream.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = [
     "-O3",

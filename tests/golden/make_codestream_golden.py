@@ -1,0 +1,40 @@
+"""Copies the reference's cjxl-encoded VarDCT fixtures and their djxl
+decodes into tests/golden/codestream/ (the .jxl codestreams and .npy pixel
+references are test data; nothing of the reference's source is copied).
+
+Run in a checkout that has the reference source at /root/reference (it is
+not present where the tests run; the copied files are the committed fixture):
+
+    python tests/golden/make_codestream_golden.py
+
+Source: JPXL/tests/fixtures/handmade/{50..53,63}_*.jxl with the .npy decodes
+committed beside them (djxl v0.13.0 196a43d9 --output_format npy; provenance
+in each fixture's .jxl.txt sidecar), plus the lossless modular fixture 07.
+"""
+from __future__ import annotations
+
+import shutil
+from pathlib import Path
+
+SRC = Path("/root/reference/JPXL/tests/fixtures/handmade")
+OUT = Path(__file__).resolve().parent / "codestream"
+NAMES = ["07_modular_gray_8x8_lossless",
+         "50_vardct_mixed_gray_128x128_nofilters_d1",
+         "51_vardct_mixed_gray_128x128_nofilters_d4",
+         "52_vardct_mixed_gray_128x128_filters_d1",
+         "53_vardct_mixed_gray_128x128_filters_d4",
+         "63_vardct_outofgamut_rgb_64x64_nofilters_d4"]
+
+
+def main() -> None:
+    OUT.mkdir(exist_ok=True)
+    for name in NAMES:
+        for ext in (".jxl", ".npy"):
+            src = SRC / (name + ext)
+            if src.exists():
+                shutil.copyfile(src, OUT / src.name)
+                print("copied", src.name)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,129 @@
+"""Host codestream reader (jpxlg_codestream_*): headers, TOC, modular
+sub-bitstreams and the VarDCT sections of cjxl-encoded fixtures, decoded to
+the frame's integer content (jpxl-decode decode.rs:2513 decode_vardct_frame,
+vardct/hf_coeff.rs:689).
+
+The fixtures (tests/golden/codestream/, copied by make_codestream_golden.py
+from the reference's tests/fixtures/handmade) are real encoder output, so a
+wrong context model or a misread field shows up as an ANS stream that does
+not end in its final state (an error) or a section whose reader stops short
+of, or past, the size its TOC entry gives.  Host code only.
+"""
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+import jpxl_gb300 as jg
+
+GOLDEN = Path(__file__).resolve().parent / "golden" / "codestream"
+VARDCT = sorted(p.stem for p in GOLDEN.glob("*_vardct_*.jxl"))
+ERR_STREAM = -8
+
+
+def load(name):
+    return jg.Codestream((GOLDEN / (name + ".jxl")).read_bytes())
+
+
+def test_fixtures_present():
+    assert len(VARDCT) == 5, VARDCT
+
+
+@pytest.mark.parametrize("name", VARDCT)
+def test_vardct_fixture_decodes_with_every_section_exact(name):
+    cs = load(name)
+    i = cs.info
+    assert i["encoding"] == 0
+    assert i["sections"] >= 1
+    assert i["sections_exact"] == i["sections"], "a section ended away from its TOC size"
+    side = 64 if name.startswith("63_") else 128
+    assert (i["width"], i["height"]) == (side, side)
+    assert i["colour_space"] == (0 if "_rgb_" in name else 1)
+    assert i["xyb_encoded"] == 1
+    if "nofilters" in name:
+        assert i["gaborish"] == 0 and i["epf_iters"] == 0
+    else:
+        assert i["gaborish"] == 1 and i["epf_iters"] >= 1
+    assert i["blocks_w"] == side // 8 and i["blocks_h"] == side // 8
+    assert i["num_varblocks"] == sum(i["transform_counts"])
+
+
+# Block rows x columns of each DctSelect (Table I.1).
+SHAPES = {0: (1, 1), 1: (1, 1), 2: (1, 1), 3: (1, 1), 4: (2, 2), 5: (4, 4), 6: (2, 1),
+          7: (1, 2), 8: (4, 1), 9: (1, 4), 10: (4, 2), 11: (2, 4), 12: (1, 1), 13: (1, 1),
+          14: (1, 1), 15: (1, 1), 16: (1, 1), 17: (1, 1), 18: (8, 8), 19: (8, 4), 20: (4, 8)}
+
+
+@pytest.mark.parametrize("name", VARDCT)
+def test_block_map_tiles_the_frame(name):
+    cs = load(name)
+    b = cs.blocks()
+    bmap = b["block_map"]
+    bh, bw = bmap.shape
+    cover = np.zeros((bh, bw), np.int32)
+    counts = np.zeros(27, np.int64)
+    for by in range(bh):
+        for bx in range(bw):
+            if bmap[by, bx] & 0x80:
+                sel = int(bmap[by, bx] & 0x7F)
+                counts[sel] += 1
+                r, c = SHAPES[sel]
+                cover[by:by + r, bx:bx + c] += 1
+                assert (bmap[by:by + r, bx:bx + c] & 0x7F == sel).all()
+                assert (b["hf_mul"][by:by + r, bx:bx + c] == b["hf_mul"][by, bx]).all()
+    assert (cover == 1).all()
+    assert counts.tolist() == cs.info["transform_counts"]
+    assert (b["hf_mul"] >= 1).all()
+    assert b["sharpness"].max() <= 7
+
+
+@pytest.mark.parametrize("name", VARDCT)
+def test_coefficients_sit_outside_the_lf_corners(name):
+    """The HF coefficients never fill a varblock's LLF corner (those cells
+    come from the LF image), and the content is non-trivial."""
+    cs = load(name)
+    coeff = cs.coefficients()
+    b = cs.blocks()
+    bmap = b["block_map"]
+    assert np.count_nonzero(coeff) > 0
+    for by, bx in zip(*np.nonzero(bmap & 0x80)):
+        r, c = SHAPES[int(bmap[by, bx] & 0x7F)]
+        cr, cc = min(r, c), max(r, c)
+        for ch in range(3):
+            if r > c:  # portrait: stored transposed
+                corner = coeff[ch, 8 * by:8 * by + cc, 8 * bx:8 * bx + cr][:c, :r]
+            else:
+                corner = coeff[ch, 8 * by:8 * by + cr, 8 * bx:8 * bx + cc][:r, :c]
+            assert not corner.any(), (by, bx, ch)
+
+
+@pytest.mark.parametrize("name", VARDCT)
+def test_truncated_codestream_is_a_stream_error(name):
+    data = (GOLDEN / (name + ".jxl")).read_bytes()
+    for cut in (len(data) // 3, len(data) - 1):
+        with pytest.raises(jg.JpxlError) as e:
+            jg.Codestream(data[:cut])
+        assert e.value.code == ERR_STREAM
+
+
+def test_lf_planes_are_plausible():
+    """Grey fixtures: the X and B LF planes of a grey image are close to
+    constant while Y carries the picture."""
+    cs = load("51_vardct_mixed_gray_128x128_nofilters_d4")
+    lf = cs.blocks()["lf"]
+    assert np.ptp(lf[1]) > 10 * max(1, np.ptp(lf[0]))
+
+
+def test_not_a_codestream():
+    with pytest.raises(jg.JpxlError) as e:
+        jg.Codestream(b"\x00\x00\x00\x0cJXL \r\n\x87\n")
+    assert e.value.code == ERR_STREAM
+
+
+def test_unsupported_feature_is_reported_not_misdecoded():
+    """The lossless modular fixture uses a modular transform, which the
+    reader reports instead of decoding wrongly."""
+    with pytest.raises(jg.JpxlError) as e:
+        load("07_modular_gray_8x8_lossless")
+    assert e.value.code == ERR_STREAM
+    assert "not supported" in str(e.value)
