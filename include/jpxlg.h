@@ -87,7 +87,9 @@ enum {
   JPXLG_OUT_XYB = 0,          /* three float planes after restoration */
   JPXLG_OUT_LINEAR = 1,       /* three float linear-sRGB planes */
   JPXLG_OUT_SRGB8 = 2,        /* interleaved 8-bit sRGB, as the decoder writes it */
-  JPXLG_OUT_LINEAR_DEPTH = 3  /* linear planes after a round trip through `bits` */
+  JPXLG_OUT_LINEAR_DEPTH = 3, /* linear planes after a round trip through `bits` */
+  JPXLG_OUT_SRGB_FLOAT = 4    /* three float planes through the sRGB curve, unclipped,
+                                 as jpxl-decode's float output (decode.rs:3441) */
 };
 
 typedef struct jpxlg_ctx jpxlg_ctx;
@@ -325,6 +327,18 @@ int jpxlg_codestream_blocks(const jpxlg_codestream* cs, int32_t* lf, uint8_t* bl
 int jpxlg_codestream_coefficients(const jpxlg_codestream* cs, int32_t* out);
 int jpxlg_codestream_channel(const jpxlg_codestream* cs, uint32_t index, int32_t* out);
 int jpxlg_codestream_destroy(jpxlg_codestream* cs);
+/* Reconstruction of a decoded VarDCT frame on the GPU (jpxl-decode
+ * decode.rs:2700-3061): LF dequantization with the LF CfL and, unless the
+ * frame skips it, adaptive LF smoothing (vardct/lf.rs:351), then the
+ * varblock render (DCT8..DCT32 and their rectangles, DCT2x2, DCT64x64,
+ * DCT64x32, DCT32x64), Gaborish, EPF and the colour transform, into three
+ * float planes (JPXLG_OUT_XYB, _LINEAR, _SRGB_FLOAT) or interleaved sRGB8.
+ * A grey image's value is the first plane.  Frames that need parameters the
+ * kernels do not carry (custom dequantization matrices, chroma correlation,
+ * Gabor weights or EPF parameters, a custom opsin matrix, other transforms)
+ * return JPXLG_ERR_STREAM. */
+int jpxlg_codestream_render(jpxlg_ctx* ctx, const jpxlg_codestream* cs, int out_kind, void* out,
+                            uint32_t mem);
 
 /* Allocation-free variant of jpxlg_ssim2_score; it has no counterpart in the
  * reference.  The candidate (device planes) is scored against `ref` using a

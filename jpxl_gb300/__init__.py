@@ -553,6 +553,19 @@ class Codestream:
             raise JpxlError(rc, "jpxlg_codestream_coefficients")
         return out
 
+    def render(self, ctx: "Context", out: str = "srgb_float") -> np.ndarray:
+        """The frame reconstructed on the GPU (jpxlg_codestream_render):
+        float planes [3, H, W] for "xyb", "linear" and "srgb_float" (the
+        decoder's unclipped float output), or [H, W, 3] uint8 for "srgb8".
+        A grey image's samples are plane 0."""
+        kinds = {"xyb": 0, "linear": 1, "srgb8": 2, "srgb_float": 4}
+        w, h = self.info["width"], self.info["height"]
+        buf = (np.zeros((h, w, 3), np.uint8) if out == "srgb8"
+               else np.zeros((3, h, w), np.float32))
+        ctx.check(self.lib.jpxlg_codestream_render(ctx.handle, self.handle, kinds[out],
+                                                   buf.ctypes.data, MEM_HOST))
+        return buf
+
     def channel(self, index: int) -> np.ndarray:
         out = np.zeros((self.info["height"], self.info["width"]), np.int32)
         rc = self.lib.jpxlg_codestream_channel(self.handle, index, out.ctypes.data)

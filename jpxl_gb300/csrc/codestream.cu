@@ -1200,10 +1200,6 @@ void decode(const uint8_t* data, size_t size, Decoded* out) {
 
 // ---- C ABI --------------------------------------------------------------------
 
-struct jpxlg_codestream {
-  jpxlg::cs::Decoded d;
-};
-
 namespace {
 thread_local std::string g_codestream_error;
 }

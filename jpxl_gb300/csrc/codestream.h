@@ -121,3 +121,8 @@ void decode(const uint8_t* data, size_t size, Decoded* out);
 
 }  // namespace cs
 }  // namespace jpxlg
+
+// The C ABI's handle (include/jpxlg.h jpxlg_codestream).
+struct jpxlg_codestream {
+  jpxlg::cs::Decoded d;
+};

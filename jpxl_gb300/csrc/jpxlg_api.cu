@@ -12,6 +12,7 @@
 #include <vector>
 
 #include "../../include/jpxlg.h"
+#include "codestream.h"
 #include "jpxlg_common.cuh"
 #include "jpxlg_internal.h"
 #include "jpxlg_kernels.h"
@@ -270,7 +271,8 @@ int encode_device(jpxlg_ctx* ctx, const jpxlg_layout* L, const void* rgb_dev, in
                   int8_t* cflb, int32_t* lf_factors_biased) {
   const Geo& g = L->geo;
   if (!L->all_square)
-    return fail(ctx, JPXLG_ERR_BLOCK_MAP, "the encoder covers frames with square varblocks only");
+    return fail(ctx, JPXLG_ERR_BLOCK_MAP,
+                "the encoder covers frames with DCT8, DCT16 and DCT32 varblocks only");
   const size_t n = (size_t)g.w * g.h, n8 = (size_t)g.W8 * g.H8, nb = (size_t)g.bw * g.bh;
   CK(ctx->xyb.ensure(3 * n * sizeof(float)));
   CK(ctx->coeff.ensure(3 * n8 * sizeof(float)));
@@ -332,7 +334,8 @@ int encode_device(jpxlg_ctx* ctx, const jpxlg_layout* L, const void* rgb_dev, in
 int render_device(jpxlg_ctx* ctx, const jpxlg_layout* L, const int32_t* qcoeff,
                   const int32_t* lfq, const int8_t* cflx, const int8_t* cflb, int fx_biased,
                   int fb_biased, const int* lf_dev_unbiased, const jpxlg_params* p, int out_kind,
-                  int bits, void* out_dev, float* pxyb_dev = nullptr) {
+                  int bits, void* out_dev, float* pxyb_dev = nullptr,
+                  const float* lf_float = nullptr) {
   const Geo& g = L->geo;
   const size_t n = (size_t)g.w * g.h, nb = (size_t)g.bw * g.bh;
   CK(ctx->planes.ensure(3 * n * sizeof(float)));
@@ -354,6 +357,7 @@ int render_device(jpxlg_ctx* ctx, const jpxlg_layout* L, const int32_t* qcoeff,
   a.lf_factors_dev = lf_dev_unbiased;
   a.planes = ctx->planes.as<float>();
   a.sigma = ctx->sigma.as<float>();
+  a.lf_float = lf_float;
   stage_begin(ctx, JPXLG_STAGE_RENDER_VARBLOCKS);
   launch_mul_table(p->global_scale, ctx->d_mul, ctx->stream);
   launch_render_varblocks(a, L->lists, L->counts, ctx->stream);
@@ -388,7 +392,7 @@ int render_device(jpxlg_ctx* ctx, const jpxlg_layout* L, const int32_t* qcoeff,
   }
   int b = out_kind == JPXLG_OUT_SRGB8 ? 8 : bits;
   const DepthTable* dt = nullptr;
-  if (out_kind != JPXLG_OUT_LINEAR) {
+  if (out_kind != JPXLG_OUT_LINEAR && out_kind != JPXLG_OUT_SRGB_FLOAT) {
     dt = get_depth(ctx, b);
     if (!dt) return fail(ctx, JPXLG_ERR_CUDA, "depth table allocation failed");
   }
@@ -491,9 +495,12 @@ int jpxlg_ctx_create(int device, uint32_t flags, jpxlg_ctx** out) {
   build_dequant_tables(dq.data());
   CKC(cudaMalloc(&c->d_dq, dq.size() * sizeof(float)));
   CKC(cudaMemcpy(c->d_dq, dq.data(), dq.size() * sizeof(float), cudaMemcpyHostToDevice));
-  float iv4[16], iv8[64], iv16[256], sf[12], om[9], ob[3], oc[3];
+  float iv4[16], iv8[64], iv16[256], sf[32], om[9], ob[3], oc[3];
   build_iv_tables(iv4, iv8, iv16);
   build_scale_f(sf);
+  std::vector<float> dct64(64 * 64);
+  build_dct64_matrix(dct64.data());
+  upload_dct64(dct64.data(), c->stream);
   build_opsin_inverse(om, ob, oc);
   upload_dct_constants(iv4, iv8, iv16, sf, c->stream);
   upload_blur_consts(c->stream);
@@ -616,7 +623,7 @@ int jpxlg_layout_create(jpxlg_ctx* ctx, int width, int height, const uint8_t* bl
       int sel = e & 0x1f;
       Shape sh;
       if (!shape_of(sel, &sh))
-        return fail(ctx, JPXLG_ERR_BLOCK_MAP, "block (%d,%d): DctSelect %d is not a plain DCT", bx,
+        return fail(ctx, JPXLG_ERR_BLOCK_MAP, "block (%d,%d): DctSelect %d is not carried", bx,
                     by, sel);
       if (bx % sh.bcols || by % sh.brows || bx + sh.bcols > g.bw || by + sh.brows > g.bh)
         return fail(ctx, JPXLG_ERR_BLOCK_MAP, "block (%d,%d): varblock misaligned or outside", bx,
@@ -632,7 +639,8 @@ int jpxlg_layout_create(jpxlg_ctx* ctx, int width, int height, const uint8_t* bl
       int cls = 0;
       while (kShapeSel[cls] != sel) ++cls;
       bucket[cls].push_back(((uint32_t)by << 16) | (uint32_t)bx);
-      if (sh.brows != sh.bcols) L->all_square = false;
+      // the encoder's kernels cover DCT8/16/32 only
+      if (sh.brows != sh.bcols || sh.brows > 4 || sel == 2) L->all_square = false;
       if (hf_mul[(size_t)by * g.bw + bx] == 0)
         return fail(ctx, JPXLG_ERR_ARGUMENT, "block (%d,%d): hf_mul must be positive", bx, by);
     }
@@ -777,7 +785,7 @@ int jpxlg_reconstruct(jpxlg_ctx* ctx, const jpxlg_layout* L, const jpxlg_plan* p
     return fail(ctx, JPXLG_ERR_ARGUMENT, "null plan buffer");
   int rc = check_params(ctx, p);
   if (rc) return rc;
-  if (out_kind < 0 || out_kind > 3) return fail(ctx, JPXLG_ERR_ARGUMENT, "bad out_kind");
+  if (out_kind < 0 || out_kind > 4) return fail(ctx, JPXLG_ERR_ARGUMENT, "bad out_kind");
   if (out_kind == JPXLG_OUT_LINEAR_DEPTH && (bits < 1 || bits > 16))
     return fail(ctx, JPXLG_ERR_ARGUMENT, "depth must be 1..16 bits");
   for (int i = 0; i < 2; ++i)
@@ -1343,4 +1351,102 @@ extern "C" int jpxlg_ssim2_score_static(jpxlg_ctx* ctx, const jpxlg_ref* ref,
   }
   launch_score_finish(part0, ctas, ref->nscales, pixels, out_dev, ctx->stream);
   return after_launch(ctx, k + 1);
+}
+
+// ---------------------------------------------------------------------------
+// Decoded codestreams: the frame's integer content from the host reader,
+// reconstructed by the same kernels as a plan (decode.rs:2700-3061).
+// ---------------------------------------------------------------------------
+
+extern "C" int jpxlg_codestream_render(jpxlg_ctx* ctx, const jpxlg_codestream* cs, int out_kind,
+                                       void* out, uint32_t mem) {
+  if (!ctx || !cs || !out) return fail(ctx, JPXLG_ERR_ARGUMENT, "null argument");
+  if (out_kind < 0 || out_kind > 4 || out_kind == JPXLG_OUT_LINEAR_DEPTH)
+    return fail(ctx, JPXLG_ERR_ARGUMENT, "bad out_kind");
+  const jpxlg::cs::Decoded& d = cs->d;
+  const jpxlg::cs::VarDctFrame& v = d.vardct;
+  const jpxlg::cs::FrameInfo& f = d.frame;
+  if (f.encoding != 0) return fail(ctx, JPXLG_ERR_STREAM, "not a VarDCT frame");
+  if (!v.default_matrices)
+    return fail(ctx, JPXLG_ERR_STREAM, "custom dequantization matrices are not carried");
+  if (v.colour_factor != 84 || v.base_corr_x != 0.0f || v.base_corr_b != 1.0f)
+    return fail(ctx, JPXLG_ERR_STREAM, "custom chroma correlation is not carried");
+  if (f.gab_custom) return fail(ctx, JPXLG_ERR_STREAM, "custom Gabor weights are not carried");
+  static const jpxlg::cs::FrameInfo kDefaults;
+  for (int i = 0; i < 8; ++i)
+    if (f.epf_sharp_lut[i] != kDefaults.epf_sharp_lut[i])
+      return fail(ctx, JPXLG_ERR_STREAM, "a custom EPF sharpness table is not carried");
+  for (int c = 0; c < 3; ++c)
+    if (f.epf_channel_scale[c] != kDefaults.epf_channel_scale[c])
+      return fail(ctx, JPXLG_ERR_STREAM, "custom EPF channel scales are not carried");
+  if (f.epf_quant_mul != kDefaults.epf_quant_mul ||
+      f.epf_pass0_sigma_scale != kDefaults.epf_pass0_sigma_scale ||
+      f.epf_pass2_sigma_scale != kDefaults.epf_pass2_sigma_scale ||
+      f.epf_border_sad_mul != kDefaults.epf_border_sad_mul)
+    return fail(ctx, JPXLG_ERR_STREAM, "custom EPF sigma parameters are not carried");
+  if (!d.image.default_opsin || !d.image.xyb_encoded)
+    return fail(ctx, JPXLG_ERR_STREAM, "only XYB frames with the default opsin matrix");
+  if (out_kind == JPXLG_OUT_SRGB_FLOAT && d.image.transfer != 13)
+    return fail(ctx, JPXLG_ERR_STREAM, "only the sRGB transfer function is carried");
+  cudaSetDevice(ctx->device);
+  const int W = (int)f.width, H = (int)f.height;
+  jpxlg_layout* raw = nullptr;
+  int rc = jpxlg_layout_create(ctx, W, H, v.block_map.data(), v.hf_mul.data(),
+                               v.sharpness.data(), &raw);
+  if (rc) return rc;
+  std::unique_ptr<jpxlg_layout, int (*)(jpxlg_layout*)> L(raw, jpxlg_layout_destroy);
+  const Geo& g = L->geo;
+  if ((uint32_t)g.tw != v.tiles_w || (uint32_t)g.th != v.tiles_h)
+    return fail(ctx, JPXLG_ERR_ARGUMENT, "CfL tile grid mismatch");
+  jpxlg_params p{};
+  p.global_scale = v.global_scale;
+  p.quant_lf = v.quant_lf;
+  p.x_qm_scale = f.x_qm_scale;
+  p.b_qm_scale = f.b_qm_scale;
+  p.gaborish = f.gab ? 1u : 0u;
+  p.epf_iters = f.epf_iters;
+  if ((rc = check_params(ctx, &p))) return rc;
+  const size_t n = (size_t)g.w * g.h, n8 = (size_t)g.W8 * g.H8, nb = (size_t)g.bw * g.bh;
+  const size_t nt = (size_t)g.tw * g.th;
+  std::vector<int32_t> qimg(3 * n8);
+  if ((rc = jpxlg_codestream_coefficients(cs, qimg.data()))) return rc;
+  std::vector<int32_t> lfq(3 * nb);
+  for (int c = 0; c < 3; ++c) std::copy(v.lf[c].begin(), v.lf[c].end(), lfq.begin() + c * nb);
+  CK(ctx->qcoeff.ensure(3 * n8 * sizeof(int32_t)));
+  CK(ctx->lfq.ensure(3 * nb * sizeof(int32_t)));
+  CK(ctx->cflx.ensure(nt));
+  CK(ctx->cflb.ensure(nt));
+  CK(ctx->lfs.ensure(3 * nb * sizeof(float)));
+  CK(ctx->aux.ensure(3 * std::max(n, nb) * sizeof(float)));
+  CK(cudaMemcpyAsync(ctx->qcoeff.p, qimg.data(), 3 * n8 * sizeof(int32_t), cudaMemcpyHostToDevice,
+                     ctx->stream));
+  CK(cudaMemcpyAsync(ctx->lfq.p, lfq.data(), 3 * nb * sizeof(int32_t), cudaMemcpyHostToDevice,
+                     ctx->stream));
+  CK(cudaMemcpyAsync(ctx->cflx.p, v.x_from_y.data(), nt, cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(ctx->cflb.p, v.b_from_y.data(), nt, cudaMemcpyHostToDevice, ctx->stream));
+  // LF multipliers (quantizer.rs:232): 65536 * (m_lf / 128) / (gs * quant_lf) in f64.
+  float m[3];
+  const double denom = (double)v.global_scale * (double)v.quant_lf;
+  for (int c = 0; c < 3; ++c) m[c] = (float)(65536.0 * (double)(v.m_lf[c] / 128.0f) / denom);
+  const float kx = 0.0f + (float)v.x_factor_lf / 84.0f;
+  const float kb = 1.0f + (float)v.b_factor_lf / 84.0f;
+  const bool smooth = (f.flags & 128) == 0;
+  launch_lf_prepare(ctx->lfq.as<int32_t>(), g.bw, g.bh, m, (float)(1u << v.extra_precision), kx,
+                    kb, smooth, ctx->aux.as<float>(), ctx->lfs.as<float>(), ctx->num_sms,
+                    ctx->stream);
+  if ((rc = after_launch(ctx, smooth ? 2 : 1))) return rc;
+  const size_t out_bytes = out_kind == JPXLG_OUT_SRGB8 ? 3 * n : 3 * n * sizeof(float);
+  void* dst = out;
+  if (mem != JPXLG_MEM_DEVICE) {
+    CK(ctx->out.ensure(out_bytes));
+    dst = ctx->out.p;
+  }
+  rc = render_device(ctx, L.get(), ctx->qcoeff.as<int32_t>(), ctx->lfq.as<int32_t>(),
+                     ctx->cflx.as<int8_t>(), ctx->cflb.as<int8_t>(), v.x_factor_lf + 128,
+                     v.b_factor_lf + 128, nullptr, &p, out_kind, 8, dst, nullptr,
+                     ctx->lfs.as<float>());
+  if (rc) return rc;
+  if (mem != JPXLG_MEM_DEVICE)
+    CK(cudaMemcpyAsync(out, ctx->out.p, out_bytes, cudaMemcpyDeviceToHost, ctx->stream));
+  return sync_and_check(ctx);
 }

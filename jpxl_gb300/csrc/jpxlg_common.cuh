@@ -38,8 +38,9 @@ __device__ __forceinline__ int mirror1d(int c, int size) {
 }
 
 // ---- transforms -------------------------------------------------------------
-// The nine plain DCTRxC types (Table I.1): DctSelect, footprint rows/cols in
-// blocks, dequant matrix slot (0..5 in the library's compact table).
+// The varblock types the pixel path carries (Table I.1): the nine plain
+// DCTRxC types up to 32 (the encoder's), DCT2x2, and DCT64x64 / DCT64x32 /
+// DCT32x64 (decoded streams): DctSelect and footprint rows/cols in blocks.
 struct Shape {
   int brows, bcols;
 };
@@ -54,11 +55,16 @@ __host__ __device__ __forceinline__ bool shape_of(int sel, Shape* s) {
     case 9: *s = {1, 4}; return true;
     case 10: *s = {4, 2}; return true;
     case 11: *s = {2, 4}; return true;
+    case 2: *s = {1, 1}; return true;
+    case 18: *s = {8, 8}; return true;
+    case 19: *s = {8, 4}; return true;
+    case 20: *s = {4, 8}; return true;
     default: return false;
   }
 }
 // compact dequant slot: 0 DCT8, 1 DCT16x16, 2 DCT32x32, 3 DCT16x8/8x16,
-// 4 DCT32x8/8x32, 5 DCT32x16/16x32 (Table I.4 indices 0,4,5,6,7,8).
+// 4 DCT32x8/8x32, 5 DCT32x16/16x32, 6 DCT2x2, 7 DCT64x64, 8 DCT64x32/32x64
+// (Table I.4 indices 0,4,5,6,7,8,2,11,12).
 __host__ __device__ __forceinline__ int dq_slot(int sel) {
   switch (sel) {
     case 0: return 0;
@@ -66,16 +72,19 @@ __host__ __device__ __forceinline__ int dq_slot(int sel) {
     case 5: return 2;
     case 6: case 7: return 3;
     case 8: case 9: return 4;
+    case 2: return 6;
+    case 18: return 7;
+    case 19: case 20: return 8;
     default: return 5;
   }
 }
 // Offsets of each slot's landscape matrix in the packed dequant table.
 __host__ __device__ __forceinline__ int dq_offset(int slot) {
-  // sizes: 64, 256, 1024, 128, 256, 512
-  const int off[6] = {0, 64, 320, 1344, 1472, 1728};
+  // sizes: 64, 256, 1024, 128, 256, 512, 64, 4096, 2048
+  const int off[9] = {0, 64, 320, 1344, 1472, 1728, 2240, 2304, 6400};
   return off[slot];
 }
-constexpr int kDequantTableFloats = 2240;  // per channel
+constexpr int kDequantTableFloats = 8448;  // per channel
 
 // ---- exact-parity cube roots -----------------------------------------------
 // The reference has two cube roots, each f64 iteration rounded once to f32:

@@ -35,14 +35,16 @@ struct QuantScalars {
   float qm[3];         // {qm_multiplier(x), 1, qm_multiplier(b)}
 };
 
-// Nine shape classes of the plain DCTRxC types, in this order.
-constexpr int kNumShapes = 9;
-constexpr int kShapeSel[kNumShapes] = {0, 4, 5, 6, 7, 8, 9, 10, 11};
+// Shape classes, in this order: the nine plain DCTRxC types up to 32, then
+// DCT2x2, DCT64x64, DCT64x32 and DCT32x64.
+constexpr int kNumShapes = 13;
+constexpr int kShapeSel[kNumShapes] = {0, 4, 5, 6, 7, 8, 9, 10, 11, 2, 18, 19, 20};
 
 // ---- host tables (tables.cu) -------------------------------------------------
 void build_dequant_tables(float* out /* 3 * kDequantTableFloats */);
 void build_iv_tables(float* iv4, float* iv8, float* iv16);
-void build_scale_f(float* out /* [3][4]: lf counts 1,2,4 x c<4 */);
+void build_scale_f(float* out /* [4][8]: lf counts 1,2,4,8 x c<8 */);
+void build_dct64_matrix(float* out /* [64][64]: DCT-II rows u, columns x */);
 float host_hf_multiplier(uint32_t gs, uint32_t hf_mul);
 float host_qm_multiplier(uint32_t qm_scale);
 void host_lf_multipliers(uint32_t gs, uint32_t quant_lf, float out[3]);

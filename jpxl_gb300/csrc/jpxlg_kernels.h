@@ -49,7 +49,15 @@ struct RenderArgs {
   const int* lf_factors_dev; // when non-null, read the LF factors from here
   float* planes;             // [3][w*h] XYB out
   float* sigma;              // [bw*bh]
+  const float* lf_float = nullptr;  // [3][bw*bh] final LF (decoded frames); else from lfq
 };
+
+// LF of a decoded frame: dequantize, LF CfL and (smooth) adaptive smoothing
+// into out [3][bw*bh]; tmp holds as much when smoothing.
+void launch_lf_prepare(const int32_t* lfq, int bw, int bh, const float m[3], float div, float kx,
+                       float kb, bool smooth, float* tmp, float* out, int num_sms,
+                       cudaStream_t s);
+void upload_dct64(const float* matrix, cudaStream_t s);
 
 // Fills table[h] = hf_multiplier_f64(global_scale, h) for h < kMulTableN.
 void launch_mul_table(uint32_t global_scale, float* table, cudaStream_t s);

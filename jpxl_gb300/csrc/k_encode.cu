@@ -18,7 +18,7 @@ namespace jpxlg {
 __constant__ float c_iv4[16];
 __constant__ float c_iv8[64];
 __constant__ float c_iv16[256];
-__constant__ float c_scale_f[12];  // [lf count 1,2,4][c < 4]
+__constant__ float c_scale_f[32];  // [lf count 1,2,4,8][c < 8]
 
 // ---------------------------------------------------------------------------
 // K1 — jpxl-encode-policy source.rs:226 (RGB8) / :355 (RGB16): code point ->
@@ -400,7 +400,7 @@ __device__ __forceinline__ int32_t lf_quantize(float target, float m, uint32_t* 
 // forward.rs:779 lf_from_llf_into for an n x n (n = 1, 2, 4) LLF corner:
 // divide by scale_f(y)*scale_f(x), then IDCT_2D.
 __device__ __forceinline__ void lf_from_llf(const float* llf, int n, float* lf) {
-  const float* sf = &c_scale_f[(n == 1 ? 0 : (n == 2 ? 1 : 2)) * 4];
+  const float* sf = &c_scale_f[(n == 1 ? 0 : (n == 2 ? 1 : 2)) * 8];
   float work[16];
   for (int y = 0; y < n; ++y)
     for (int x = 0; x < n; ++x) work[y * n + x] = llf[y * n + x] / (sf[y] * sf[x]);
@@ -1191,7 +1191,7 @@ void upload_dct_constants(const float* iv4, const float* iv8, const float* iv16,
   cudaMemcpyToSymbolAsync(c_iv4, iv4, sizeof(float) * 16, 0, cudaMemcpyHostToDevice, s);
   cudaMemcpyToSymbolAsync(c_iv8, iv8, sizeof(float) * 64, 0, cudaMemcpyHostToDevice, s);
   cudaMemcpyToSymbolAsync(c_iv16, iv16, sizeof(float) * 256, 0, cudaMemcpyHostToDevice, s);
-  cudaMemcpyToSymbolAsync(c_scale_f, scale_f, sizeof(float) * 12, 0, cudaMemcpyHostToDevice, s);
+  cudaMemcpyToSymbolAsync(c_scale_f, scale_f, sizeof(float) * 32, 0, cudaMemcpyHostToDevice, s);
   // 0.145f / q in IEEE single precision, as bias_adjust divides on the device.
   static float quot[kBiasQuotN];
   quot[0] = 0.0f;

@@ -15,26 +15,53 @@
 
 namespace jpxlg {
 
-extern __constant__ float c_scale_f[12];
+extern __constant__ float c_scale_f[32];
 extern __constant__ float c_quant_bias[3];
 
 __constant__ float c_opsin_m[9];
 __constant__ float c_opsin_bias[3];
 __constant__ float c_opsin_bias_cbrt[3];
+// dct.rs:631 the 64-point DCT-II matrix (rows u, columns x), f32 entries.
+__device__ float g_dct64[64 * 64];
+
+// dct.rs:678 matrix_pass for N = 64 (the reference's transforms above 32
+// points): each output an f64 dot product of f32 entries, rounded once, then
+// the normative factor sqrt(64) = 8.
+__device__ __forceinline__ void idct_64(float* v) {
+  float out[64];
+#pragma unroll 1
+  for (int k = 0; k < 64; ++k) {
+    double acc = 0.0;
+#pragma unroll 8
+    for (int j = 0; j < 64; ++j) acc += (double)g_dct64[j * 64 + k] * (double)v[j];
+    out[k] = (float)acc;
+  }
+#pragma unroll
+  for (int k = 0; k < 64; ++k) v[k] = out[k] * 8.0f;
+}
 
 template <int N>
 __device__ __forceinline__ void idct_n(float* v) {
-  idct_1d<N>(v);
+  if constexpr (N == 64) idct_64(v);
+  else idct_1d<N>(v);
 }
 
-// dct.rs:956 DCT_2D of an LF rectangle cy x cx (cy <= cx, both <= 4) in place.
+template <int N>
+__device__ __forceinline__ void dct_small(float* v) {
+  if (N == 2) dct_1d<2>(v);
+  else if (N == 4) dct_1d<4>(v);
+  else if (N == 8) dct_1d<8>(v);
+}
+
+// dct.rs:956 DCT_2D of an LF rectangle cy x cx (cy <= cx, both <= 8) in place.
 __device__ __forceinline__ void dct2d_small(float* m, int rows, int cols) {
-  float col[4], s[16];
+  float col[8], s[64];
   // column pass (length rows) on rows x cols
   for (int c = 0; c < cols; ++c) {
     for (int r = 0; r < rows; ++r) col[r] = m[r * cols + c];
-    if (rows == 2) dct_1d<2>(col);
-    else if (rows == 4) dct_1d<4>(col);
+    if (rows == 2) dct_small<2>(col);
+    else if (rows == 4) dct_small<4>(col);
+    else if (rows == 8) dct_small<8>(col);
     for (int r = 0; r < rows; ++r) m[r * cols + c] = col[r];
   }
   // transpose to cols x rows, column pass (length cols)
@@ -42,8 +69,9 @@ __device__ __forceinline__ void dct2d_small(float* m, int rows, int cols) {
     for (int c = 0; c < cols; ++c) s[c * rows + r] = m[r * cols + c];
   for (int r = 0; r < rows; ++r) {
     for (int c = 0; c < cols; ++c) col[c] = s[c * rows + r];
-    if (cols == 2) dct_1d<2>(col);
-    else if (cols == 4) dct_1d<4>(col);
+    if (cols == 2) dct_small<2>(col);
+    else if (cols == 4) dct_small<4>(col);
+    else if (cols == 8) dct_small<8>(col);
     for (int c = 0; c < cols; ++c) s[c * rows + r] = col[c];
   }
   // cols x rows result; landscape => transpose back when cols > rows
@@ -63,7 +91,9 @@ __device__ __forceinline__ void dct2d_small(float* m, int rows, int cols) {
 // the C rows of the result, producing sample column i in thread i.
 // ---------------------------------------------------------------------------
 
-template <int R, int C>
+// KIND 1: DCT2x2 (R = C = 8): the dequantized block goes through the three
+// aux_idct_2x2 stages of jpxl-core varblock.rs:917 instead of IDCT_2D.
+template <int R, int C, int KIND = 0>
 __global__ void __launch_bounds__(128) k_render_vb(RenderArgs a, const uint32_t* __restrict__ list,
                                                    int count) {
   constexpr int T = R > C ? R : C;
@@ -74,7 +104,7 @@ __global__ void __launch_bounds__(128) k_render_vb(RenderArgs a, const uint32_t*
   constexpr int LY = CR / 8, LX = CC / 8;  // LLF corner
   constexpr int VPB = 128 / T;
   __shared__ float L[VPB][CR][CC + 1];
-  __shared__ float LLF[VPB][3][16];
+  __shared__ float LLF[VPB][3][64];
   const int g = threadIdx.x / T, j = threadIdx.x % T;
   const int vi = blockIdx.x * VPB + g;
   const bool active = vi < count;
@@ -103,22 +133,28 @@ __global__ void __launch_bounds__(128) k_render_vb(RenderArgs a, const uint32_t*
         k_x_lf = 0.0f + (float)a.lf_factors_dev[0] / 84.0f;
         k_b_lf = 1.0f + (float)a.lf_factors_dev[1] / 84.0f;
       }
-      float rect[16];
+      float rect[64];
       for (int dy = 0; dy < BR; ++dy)
         for (int dx = 0; dx < BC; ++dx) {
           size_t bi = (size_t)(by + dy) * geo.bw + bx + dx;
-          float dY = a.qs.m_dc[1] * (float)a.lfq[bplane + bi] / 1.0f;
           float v;
-          if (c == 1) v = dY;
-          else {
-            float d = a.qs.m_dc[c] * (float)a.lfq[bplane * c + bi] / 1.0f;
-            v = d + (c == 0 ? k_x_lf : k_b_lf) * dY;
+          if (a.lf_float) {
+            v = a.lf_float[bplane * c + bi];  // dequantized, LF CfL and smoothing applied
+          } else {
+            float dY = a.qs.m_dc[1] * (float)a.lfq[bplane + bi] / 1.0f;
+            if (c == 1) v = dY;
+            else {
+              float d = a.qs.m_dc[c] * (float)a.lfq[bplane * c + bi] / 1.0f;
+              v = d + (c == 0 ? k_x_lf : k_b_lf) * dY;
+            }
           }
           if (portrait) rect[dx * BR + dy] = v; else rect[dy * BC + dx] = v;
         }
       if (LY * LX > 1) dct2d_small(rect, LY, LX);
-      const float* sfy = &c_scale_f[(LY == 1 ? 0 : (LY == 2 ? 1 : 2)) * 4];
-      const float* sfx = &c_scale_f[(LX == 1 ? 0 : (LX == 2 ? 1 : 2)) * 4];
+      constexpr int sfiy = LY == 1 ? 0 : (LY == 2 ? 1 : (LY == 4 ? 2 : 3));
+      constexpr int sfix = LX == 1 ? 0 : (LX == 2 ? 1 : (LX == 4 ? 2 : 3));
+      const float* sfy = &c_scale_f[sfiy * 8];
+      const float* sfx = &c_scale_f[sfix * 8];
       for (int y = 0; y < LY; ++y)
         for (int x = 0; x < LX; ++x) LLF[g][c][y * LX + x] = rect[y * LX + x] * sfy[y] * sfx[x];
     }
@@ -129,8 +165,11 @@ __global__ void __launch_bounds__(128) k_render_vb(RenderArgs a, const uint32_t*
   // lib.rs:913: adjusted * (mul*qm) * matrix, left to right).
   float dY[CR];
   // compact dequant slot of this shape (Table I.4 indices 0,4,5,6,7,8)
-  constexpr int slot = (R == C) ? (R == 8 ? 0 : (R == 16 ? 1 : 2))
-                                : (CC == 16 ? 3 : (CR == 8 ? 4 : 5));
+  constexpr int slot = KIND == 1 ? 6
+                       : (R == 64 && C == 64) ? 7
+                       : (T == 64) ? 8
+                       : (R == C) ? (R == 8 ? 0 : (R == 16 ? 1 : 2))
+                                  : (CC == 16 ? 3 : (CR == 8 ? 4 : 5));
   const int off = dq_offset(slot);
   // The channel loop stays rolled, and for square shapes both IDCT passes
   // run through one copy of the transform: a 32-point transform inlined six
@@ -157,7 +196,49 @@ __global__ void __launch_bounds__(128) k_render_vb(RenderArgs a, const uint32_t*
     }
     __syncthreads();
     float v[T];
-    if constexpr (R == C) {
+    if constexpr (KIND == 1) {
+      // varblock.rs:895 aux_idct_2x2 with s = 2, 4, 8, each stage reading the
+      // previous one; thread 0 of the group runs the cascade, then thread j
+      // writes sample column j.
+      if (active && j == 0) {
+        float b[64], r[64];
+#pragma unroll
+        for (int i = 0; i < 64; ++i) b[i] = L[g][i / 8][i % 8];
+#pragma unroll
+        for (int st = 2; st <= 8; st *= 2) {
+          const int h = st / 2;
+#pragma unroll
+          for (int i = 0; i < 64; ++i) r[i] = b[i];
+#pragma unroll
+          for (int y = 0; y < h; ++y)
+#pragma unroll
+            for (int x = 0; x < h; ++x) {
+              const float c00 = b[y * 8 + x], c01 = b[y * 8 + h + x];
+              const float c10 = b[(y + h) * 8 + x], c11 = b[(y + h) * 8 + h + x];
+              r[(2 * y) * 8 + 2 * x] = ((c00 + c01) + c10) + c11;
+              r[(2 * y) * 8 + 2 * x + 1] = ((c00 + c01) - c10) - c11;
+              r[(2 * y + 1) * 8 + 2 * x] = ((c00 - c01) + c10) - c11;
+              r[(2 * y + 1) * 8 + 2 * x + 1] = ((c00 - c01) - c10) + c11;
+            }
+#pragma unroll
+          for (int i = 0; i < 64; ++i) b[i] = r[i];
+        }
+#pragma unroll
+        for (int i = 0; i < 64; ++i) L[g][i / 8][i % 8] = b[i];
+      }
+      __syncthreads();
+      if (active) {
+        const int fx = x0 + j;
+        if (fx < geo.w) {
+#pragma unroll
+          for (int rr = 0; rr < 8; ++rr) {
+            const int fy = y0 + rr;
+            if (fy < geo.h) a.planes[plane * c + (size_t)fy * geo.w + fx] = L[g][rr][j];
+          }
+        }
+      }
+      __syncthreads();
+    } else if constexpr (R == C) {
       // Step A (st = 0): thread j transforms column j of L in place.
       // Step B (st = 1): thread j transforms row j of the result into sample
       // column j and scatters it inside the frame.
@@ -237,8 +318,13 @@ void launch_render_varblocks(const RenderArgs& a, const uint32_t* const* lists, 
     k_render_vb<R, C><<<(counts[IDX] + (128 / ((R) > (C) ? (R) : (C))) - 1) /            \
                             (128 / ((R) > (C) ? (R) : (C))),                             \
                         128, 0, s>>>(a, lists[IDX], counts[IDX]);
+#define JPXLG_RVK(IDX, R, C, K)                                                          \
+  if (counts[IDX])                                                                       \
+    k_render_vb<R, C, K><<<(counts[IDX] + (128 / ((R) > (C) ? (R) : (C))) - 1) /         \
+                               (128 / ((R) > (C) ? (R) : (C))),                          \
+                           128, 0, s>>>(a, lists[IDX], counts[IDX]);
   // shape classes in kShapeSel order: DCT8, 16x16, 32x32, 16x8, 8x16, 32x8,
-  // 8x32, 32x16, 16x32 (rows x cols of samples)
+  // 8x32, 32x16, 16x32, DCT2x2, 64x64, 64x32, 32x64 (rows x cols of samples)
   JPXLG_RV(0, 8, 8)
   JPXLG_RV(1, 16, 16)
   JPXLG_RV(2, 32, 32)
@@ -248,7 +334,12 @@ void launch_render_varblocks(const RenderArgs& a, const uint32_t* const* lists, 
   JPXLG_RV(6, 8, 32)
   JPXLG_RV(7, 32, 16)
   JPXLG_RV(8, 16, 32)
+  JPXLG_RVK(9, 8, 8, 1)
+  JPXLG_RV(10, 64, 64)
+  JPXLG_RV(11, 64, 32)
+  JPXLG_RV(12, 32, 64)
 #undef JPXLG_RV
+#undef JPXLG_RVK
 }
 
 // ---------------------------------------------------------------------------
@@ -478,6 +569,15 @@ __global__ void __launch_bounds__(256) k_colour_out(const float* __restrict__ xy
       o[i] = rgb[0];
       o[n + i] = rgb[1];
       o[2 * n + i] = rgb[2];
+    } else if (KIND == 4) {
+      // jpxl-core color.rs:490 linear_to_srgb, odd-symmetric, unclipped.
+      float* o = (float*)out;
+#pragma unroll
+      for (int q = 0; q < 3; ++q) {
+        const float v = rgb[q], av = fabsf(v);
+        const float e = av <= 0.0031308f ? 12.92f * av : 1.055f * powf(av, 1.0f / 2.4f) - 0.055f;
+        o[q * n + i] = v < 0.0f ? -e : e;
+      }
     } else if (KIND == 2) {
       uint8_t* o = (uint8_t*)out;
       o[3 * i] = (uint8_t)level_of(rgb[0], T, nlev - 1);
@@ -520,8 +620,70 @@ void launch_colour_out(const float* xyb, int w, int h, int out_kind, const float
     k_colour_out<1><<<blocks, 256, 0, s>>>(xyb, n, thresholds, levels, nlevels, out, nullptr);
   else if (out_kind == 2)
     k_colour_out<2><<<blocks, 256, 0, s>>>(xyb, n, thresholds, levels, nlevels, out, nullptr);
+  else if (out_kind == 4)
+    k_colour_out<4><<<blocks, 256, 0, s>>>(xyb, n, thresholds, levels, nlevels, out, nullptr);
   else
     k_colour_out<3><<<blocks, 256, 0, s>>>(xyb, n, thresholds, levels, nlevels, out, pxyb);
+}
+
+// ---------------------------------------------------------------------------
+// R5 — LF of a decoded frame (jpxl-decode vardct/lf.rs:448 dequantize_lf and
+// :351 adaptive_smoothing, decode.rs:3246 over the whole frame): dequantize
+// (m * q / 2^extra_precision), apply the LF CfL, then smooth interior cells.
+// ---------------------------------------------------------------------------
+
+__global__ void __launch_bounds__(256) k_lf_dequant(const int32_t* __restrict__ lfq, size_t nb,
+                                                    float m0, float m1, float m2, float div,
+                                                    float kx, float kb, float* __restrict__ out) {
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < nb;
+       i += (size_t)gridDim.x * blockDim.x) {
+    const float dx = m0 * (float)lfq[i] / div;
+    const float dy = m1 * (float)lfq[nb + i] / div;
+    const float db = m2 * (float)lfq[2 * nb + i] / div;
+    out[i] = dx + kx * dy;
+    out[nb + i] = dy;
+    out[2 * nb + i] = db + kb * dy;
+  }
+}
+
+__global__ void __launch_bounds__(256) k_lf_smooth(const float* __restrict__ in, int bw, int bh,
+                                                   float m0, float m1, float m2,
+                                                   float* __restrict__ out) {
+  const size_t nb = (size_t)bw * bh;
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < nb;
+       i += (size_t)gridDim.x * blockDim.x) {
+    const int x = (int)(i % bw), y = (int)(i / bw);
+    if (x == 0 || y == 0 || x == bw - 1 || y == bh - 1) {
+      for (int c = 0; c < 3; ++c) out[c * nb + i] = in[c * nb + i];
+      continue;
+    }
+    float wa[3], sv[3];
+    for (int c = 0; c < 3; ++c) {
+      const float* p = in + c * nb;
+      auto g = [&](int dx, int dy) { return p[(size_t)(y + dy) * bw + x + dx]; };
+      sv[c] = g(0, 0);
+      wa[c] = (0.052262735f * sv[c] + 0.2034514f * (((g(-1, 0) + g(1, 0)) + g(0, -1)) + g(0, 1))) +
+              0.03348292f * (((g(-1, -1) + g(1, -1)) + g(-1, 1)) + g(1, 1));
+    }
+    const float m[3] = {m0, m1, m2};
+    float gap = 0.5f;
+    for (int c = 0; c < 3; ++c) gap = fmaxf(gap, fabsf(wa[c] - sv[c]) / m[c]);
+    const float factor = fmaxf(3.0f - 4.0f * gap, 0.0f);
+    for (int c = 0; c < 3; ++c) out[c * nb + i] = (wa[c] - sv[c]) * factor + sv[c];
+  }
+}
+
+void launch_lf_prepare(const int32_t* lfq, int bw, int bh, const float m[3], float div, float kx,
+                       float kb, bool smooth, float* tmp, float* out, int num_sms,
+                       cudaStream_t s) {
+  const size_t nb = (size_t)bw * bh;
+  const int blocks = (int)std::max<size_t>(1, std::min<size_t>((nb + 255) / 256, num_sms * 4));
+  k_lf_dequant<<<blocks, 256, 0, s>>>(lfq, nb, m[0], m[1], m[2], div, kx, kb, smooth ? tmp : out);
+  if (smooth) k_lf_smooth<<<blocks, 256, 0, s>>>(tmp, bw, bh, m[0], m[1], m[2], out);
+}
+
+void upload_dct64(const float* matrix, cudaStream_t s) {
+  cudaMemcpyToSymbolAsync(g_dct64, matrix, sizeof(float) * 64 * 64, 0, cudaMemcpyHostToDevice, s);
 }
 
 void upload_render_constants(const float* opsin_m, const float* opsin_bias,

@@ -51,12 +51,62 @@ const double kP16x32[3][8] = {
      -0.2692727459704829, -0.38272769465388551, -0.22924222653091453, -0.20719098826199578},
     {1807.236946760964614, -1.2, -1.2, -0.7, -0.7, -0.7, -0.4, -0.5}};
 
+// Indices 11 (DCT64x64) and 12 (DCT64x32 / DCT32x64): {base, SeqA | SeqB |
+// SeqC} per channel (jpxl-core dequant.rs:746-790).
+const double kSeqA[7] = {-1.025, -0.78, -0.65012, -0.19041574084286472, -0.20819395464,
+                         -0.421064, -0.32733845535848671};
+const double kSeqB[7] = {-0.3041958212306401, -0.3633036457487539, -0.35660379990111464,
+                         -0.3443074455424403, -0.33699592683512467, -0.30180866526242109,
+                         -0.27321683125358037};
+const double kSeqC[7] = {-1.2, -1.2, -0.8, -0.7, -0.7, -0.4, -0.5};
+const double kLargeBase[2][3] = {{23966.1665298448605, 8380.19148390090414, 4493.02378009847706},
+                                 {15358.89804933239925, 5597.360516150652990,
+                                  2919.961618960011210}};
+double kP64x64[3][8], kP64x32[3][8];
+struct LargeInit {
+  LargeInit() {
+    const double* seq[3] = {kSeqA, kSeqB, kSeqC};
+    for (int c = 0; c < 3; ++c) {
+      kP64x64[c][0] = kLargeBase[0][c];
+      kP64x32[c][0] = kLargeBase[1][c];
+      for (int i = 0; i < 7; ++i) kP64x64[c][i + 1] = kP64x32[c][i + 1] = seq[c][i];
+    }
+  }
+} g_large_init;
+
+// Table I.6 DCT2 params (dequant.rs:986), used as weights directly.
+const double kDct2[3][6] = {{3840.0, 2560.0, 1280.0, 640.0, 480.0, 300.0},
+                            {960.0, 640.0, 320.0, 180.0, 140.0, 120.0},
+                            {640.0, 320.0, 128.0, 64.0, 32.0, 16.0}};
+
 struct Slot {
   const double (*params)[8];
   int np, rows, cols;
 };
-const Slot kSlots[6] = {{kP8x8, 6, 8, 8},    {kP16x16, 7, 16, 16}, {kP32x32, 8, 32, 32},
-                        {kP16x8, 7, 8, 16},  {kP32x8, 8, 8, 32},   {kP16x32, 8, 16, 32}};
+const Slot kSlots[9] = {{kP8x8, 6, 8, 8},    {kP16x16, 7, 16, 16}, {kP32x32, 8, 32, 32},
+                        {kP16x8, 7, 8, 16},  {kP32x8, 8, 8, 32},   {kP16x32, 8, 16, 32},
+                        {nullptr, 0, 8, 8},  {kP64x64, 8, 64, 64}, {kP64x32, 8, 32, 64}};
+
+// I.2.4 mode DCT2 (dequant.rs:1328): six rectangles of the 8x8 weights
+// matrix, (0, 0) set to one; the matrix is the f32 reciprocal.
+void dct2_into(const double* p, float* out) {
+  double w[64] = {};
+  auto fill = [&](int x0, int y0, int x1, int y1, double v) {
+    for (int y = y0; y < y1; ++y)
+      for (int x = x0; x < x1; ++x) w[y * 8 + x] = v;
+  };
+  fill(4, 4, 8, 8, p[5]);
+  fill(4, 0, 8, 4, p[4]);
+  fill(0, 4, 4, 8, p[4]);
+  fill(2, 2, 4, 4, p[3]);
+  fill(2, 0, 4, 2, p[2]);
+  fill(0, 2, 2, 4, p[2]);
+  fill(1, 1, 2, 2, p[1]);
+  fill(0, 1, 1, 2, p[0]);
+  fill(1, 0, 2, 1, p[0]);
+  w[0] = 1.0;
+  for (int i = 0; i < 64; ++i) out[i] = (float)(1.0 / w[i]);
+}
 
 // I.2.4 GetDctQuantWeights: geometric interpolation of the band sequence
 // over the radial distance, then the f32 reciprocal (dequant.rs:321).
@@ -89,9 +139,23 @@ void weights_into(const double* params, int np, int rows, int cols, float* out) 
 
 void build_dequant_tables(float* out) {
   for (int c = 0; c < 3; ++c)
-    for (int s = 0; s < 6; ++s)
-      weights_into(kSlots[s].params[c], kSlots[s].np, kSlots[s].rows, kSlots[s].cols,
-                   out + c * kDequantTableFloats + dq_offset(s));
+    for (int s = 0; s < 9; ++s) {
+      float* dst = out + c * kDequantTableFloats + dq_offset(s);
+      if (s == 6) dct2_into(kDct2[c], dst);
+      else weights_into(kSlots[s].params[c], kSlots[s].np, kSlots[s].rows, kSlots[s].cols, dst);
+    }
+}
+
+// dct.rs:631 build_dct_matrix(64): orthonormal DCT-II rows in f64, narrowed.
+void build_dct64_matrix(float* out) {
+  const int n = 64;
+  for (int u = 0; u < n; ++u) {
+    const double scale = std::sqrt(u == 0 ? 1.0 / n : 2.0 / n);
+    for (int x = 0; x < n; ++x) {
+      const double angle = M_PI * (double)(2 * x + 1) * (double)u / (2.0 * n);
+      out[u * n + x] = (float)(scale * std::cos(angle));
+    }
+  }
 }
 
 // ---- DCT-IV leaves (dct.rs:148-211) ------------------------------------------
@@ -126,15 +190,15 @@ void build_iv_tables(float* iv4, float* iv8, float* iv16) {
   fill(16, m16, iv16);
 }
 
-// varblock.rs:789 ScaleF closed form, for LF counts 1, 2, 4 (b = 8*count).
+// varblock.rs:789 ScaleF closed form, for LF counts 1, 2, 4, 8 (b = 8*count).
 void build_scale_f(float* out) {
-  const int counts[3] = {1, 2, 4};
-  for (int i = 0; i < 3; ++i)
-    for (int c = 0; c < 4; ++c) {
+  const int counts[4] = {1, 2, 4, 8};
+  for (int i = 0; i < 4; ++i)
+    for (int c = 0; c < 8; ++c) {
       double cf = (double)c, bf = (double)(counts[i] * 8);
       double inv = std::cos(cf * M_PI / (2.0 * bf)) * std::cos(cf * M_PI / bf) *
                    std::cos(2.0 * cf * M_PI / bf);
-      out[i * 4 + c] = (float)(1.0 / inv);
+      out[i * 8 + c] = (float)(1.0 / inv);
     }
 }
 

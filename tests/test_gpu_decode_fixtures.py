@@ -1,0 +1,54 @@
+"""Decoded pixels of cjxl-encoded VarDCT fixtures against djxl's own decode
+(the .npy committed beside each fixture), at the reference's conformance
+classes (jpxl-decode tests/e2e_vardct.rs:282-380, ISO/IEC 18181-3 Table
+A.1): no filters, peak 0.004 and per-channel RMSE 1e-5; with Gaborish and
+EPF, peak 0.06 and RMSE 0.02.  The host reader decodes the codestream; the
+GPU reconstructs it (LF dequantization, CfL and smoothing; DCT8..DCT64,
+DCT2x2; Gaborish, EPF; opsin inverse and the sRGB curve).
+"""
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+import jpxl_gb300 as jg
+
+pytestmark = pytest.mark.gpu
+
+GOLDEN = Path(__file__).resolve().parent / "golden" / "codestream"
+CASES = [("50_vardct_mixed_gray_128x128_nofilters_d1", 0.004, 1e-5),
+         ("51_vardct_mixed_gray_128x128_nofilters_d4", 0.004, 1e-5),
+         ("63_vardct_outofgamut_rgb_64x64_nofilters_d4", 0.004, 1e-5),
+         ("52_vardct_mixed_gray_128x128_filters_d1", 0.06, 0.02),
+         ("53_vardct_mixed_gray_128x128_filters_d4", 0.06, 0.02)]
+
+
+def grade(out, ref):
+    chans = ref.shape[2]
+    diff = [out[c].astype(np.float64) - ref[:, :, c] for c in range(chans)]
+    peak = max(float(np.abs(d).max()) for d in diff)
+    rmse = [float(np.sqrt(np.mean(d * d))) for d in diff]
+    return peak, rmse
+
+
+@pytest.mark.parametrize("name,peak,rmse", CASES, ids=[c[0][:2] for c in CASES])
+def test_decoded_fixture_matches_djxl(ctx, name, peak, rmse):
+    cs = jg.Codestream((GOLDEN / (name + ".jxl")).read_bytes())
+    out = cs.render(ctx, "srgb_float")
+    ref = np.load(GOLDEN / (name + ".npy"))[0]
+    assert out.shape[1:] == ref.shape[:2]
+    got_peak, got_rmse = grade(out, ref)
+    assert got_peak <= peak and max(got_rmse) <= rmse, (got_peak, got_rmse, cs.info["transform_counts"])
+
+
+def test_decoded_grey_fixture_is_grey(ctx):
+    cs = jg.Codestream((GOLDEN / "51_vardct_mixed_gray_128x128_nofilters_d4.jxl").read_bytes())
+    out = cs.render(ctx, "srgb_float")
+    assert np.abs(out[0] - out[1]).max() < 1e-3 and np.abs(out[0] - out[2]).max() < 1e-3
+
+
+def test_decode_render_is_deterministic(ctx):
+    cs = jg.Codestream((GOLDEN / "52_vardct_mixed_gray_128x128_filters_d1.jxl").read_bytes())
+    a = cs.render(ctx, "linear")
+    b = cs.render(ctx, "linear")
+    assert np.array_equal(a, b)
