@@ -7,9 +7,10 @@ not present where the tests run; the copied files are the committed fixture):
 
     python tests/golden/make_codestream_golden.py
 
-Source: JPXL/tests/fixtures/handmade/{50..53,63}_*.jxl with the .npy decodes
+Source: JPXL/tests/fixtures/handmade/{50..53,63,64,70,71}_*.jxl with the .npy decodes
 committed beside them (djxl v0.13.0 196a43d9 --output_format npy; provenance
-in each fixture's .jxl.txt sidecar), plus the lossless modular fixture 07.
+in each fixture's .jxl.txt sidecar; 64 has none), plus the lossless modular
+fixture 07.
 """
 from __future__ import annotations
 
@@ -23,7 +24,10 @@ NAMES = ["07_modular_gray_8x8_lossless",
          "51_vardct_mixed_gray_128x128_nofilters_d4",
          "52_vardct_mixed_gray_128x128_filters_d1",
          "53_vardct_mixed_gray_128x128_filters_d4",
-         "63_vardct_outofgamut_rgb_64x64_nofilters_d4"]
+         "63_vardct_outofgamut_rgb_64x64_nofilters_d4",
+         "64_vardct_lfgroupseam_rgb_128x2176_nofilters_d6",
+         "70_progressive_ac_gray_128x128_nofilters",
+         "71_qprogressive_ac_gray_128x128_nofilters"]
 
 
 def main() -> None:

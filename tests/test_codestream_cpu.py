@@ -18,6 +18,7 @@ import jpxl_gb300 as jg
 
 GOLDEN = Path(__file__).resolve().parent / "golden" / "codestream"
 VARDCT = sorted(p.stem for p in GOLDEN.glob("*_vardct_*.jxl"))
+PROGRESSIVE = sorted(p.stem for p in GOLDEN.glob("*progressive*.jxl"))
 ERR_STREAM = -8
 
 
@@ -26,7 +27,31 @@ def load(name):
 
 
 def test_fixtures_present():
-    assert len(VARDCT) == 5, VARDCT
+    assert len(VARDCT) == 6, VARDCT
+    assert len(PROGRESSIVE) == 2, PROGRESSIVE
+
+
+@pytest.mark.parametrize("name", PROGRESSIVE)
+def test_progressive_fixture_decodes_every_pass(name):
+    """Several HF passes (each its own coefficient orders, histograms and
+    group sections, coefficients shifted per pass) in a multi-section TOC."""
+    cs = load(name)
+    i = cs.info
+    assert i["num_passes"] == (3 if name.startswith("70_") else 2)
+    assert i["sections"] == 3 + i["num_passes"]  # LfGlobal, LF group, HfGlobal, a group per pass
+    assert i["sections_exact"] == i["sections"]
+    assert np.count_nonzero(cs.coefficients()) > 0
+
+
+def test_two_lf_groups():
+    """128 x 2176: two LF groups (2048 rows each) and nine groups, thirteen
+    sections; varblocks of both LF groups land in one frame-wide map."""
+    cs = load("64_vardct_lfgroupseam_rgb_128x2176_nofilters_d6")
+    i = cs.info
+    assert (i["width"], i["height"]) == (128, 2176)
+    assert i["sections"] == 13 and i["sections_exact"] == 13
+    b = cs.blocks()
+    assert np.count_nonzero(b["block_map"] & 0x80) == i["num_varblocks"] == 16 * 272
 
 
 @pytest.mark.parametrize("name", VARDCT)
@@ -37,6 +62,9 @@ def test_vardct_fixture_decodes_with_every_section_exact(name):
     assert i["sections"] >= 1
     assert i["sections_exact"] == i["sections"], "a section ended away from its TOC size"
     side = 64 if name.startswith("63_") else 128
+    if name.startswith("64_"):
+        assert (i["width"], i["height"]) == (128, 2176)
+        return
     assert (i["width"], i["height"]) == (side, side)
     assert i["colour_space"] == (0 if "_rgb_" in name else 1)
     assert i["xyb_encoded"] == 1
