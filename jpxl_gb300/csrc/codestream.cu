@@ -1134,6 +1134,9 @@ void decode(const uint8_t* data, size_t size, Decoded* out) {
   r.b.pos = 16;
   ImageInfo& m = out->image;
   size_header(r, &m.width, &m.height);
+  // The reference's default pixel budget (jpxl-core limits.rs:42, 2^30),
+  // which bounds every allocation a hostile header can ask for.
+  need((uint64_t)m.width * m.height <= (1ull << 30), "image larger than 2^30 pixels");
   bool preview = false, animation = false, timecodes = false;
   image_metadata(r, &m, &preview, &animation, &timecodes);
   need(!m.want_icc, "ICC profiles are not supported");

@@ -155,3 +155,32 @@ def test_unsupported_feature_is_reported_not_misdecoded():
         load("07_modular_gray_8x8_lossless")
     assert e.value.code == ERR_STREAM
     assert "not supported" in str(e.value)
+
+
+def test_mutated_codestreams_fail_cleanly():
+    """Seeded bit flips, byte overwrites, truncations and appended garbage over
+    every fixture: each decodes or reports a stream error; nothing crashes or
+    runs away (a few seconds in all)."""
+    rng = np.random.default_rng(20261204)
+    files = sorted(GOLDEN.glob("*.jxl"))
+    decoded = 0
+    for trial in range(2000):
+        data = bytearray(files[trial % len(files)].read_bytes())
+        kind = trial % 4
+        if kind == 0:
+            for _ in range(int(rng.integers(1, 4))):
+                i = int(rng.integers(len(data)))
+                data[i] ^= 1 << int(rng.integers(8))
+        elif kind == 1:
+            for _ in range(int(rng.integers(1, 6))):
+                data[int(rng.integers(min(40, len(data))))] = int(rng.integers(256))
+        elif kind == 2:
+            data = data[:int(rng.integers(2, len(data)))]
+        else:
+            data += bytes(rng.integers(0, 256, int(rng.integers(1, 64))).tolist())
+        try:
+            jg.Codestream(bytes(data))
+            decoded += 1
+        except jg.JpxlError as e:
+            assert e.code == ERR_STREAM
+    assert 0 < decoded < 2000
