@@ -12,6 +12,7 @@
 #include <cmath>
 #include <cstring>
 #include <memory>
+#include <mutex>
 
 #include "entropy.h"
 #include "jpxlg.h"
@@ -772,6 +773,16 @@ std::vector<uint32_t> natural_order(uint32_t bwidth, uint32_t bheight) {
   return out;
 }
 
+// Natural orders are the same for every frame: built once per process.
+const std::vector<uint32_t>& cached_natural_order(int order_id) {
+  static std::vector<uint32_t> cache[13];
+  static std::once_flag once[13];
+  std::call_once(once[order_id], [order_id] {
+    cache[order_id] = natural_order(kOrderDims[order_id][0], kOrderDims[order_id][1]);
+  });
+  return cache[order_id];
+}
+
 // I.2.2 (block_ctx.rs:212).
 struct BlockCtx {
   std::vector<int32_t> lf_thr[3];
@@ -983,10 +994,11 @@ void decode_frame_vardct(std::vector<Section>& sec, bool single, Decoded* out) {
   vd.default_matrices = hg.flag();
   if (!vd.default_matrices) read_dequant_params(hg);
   const uint32_t num_presets = hg.bits(ceil_log2(num_groups)) + 1;
-  std::vector<std::vector<uint32_t>> natural(13);
-  for (int o = 0; o < 13; ++o) natural[o] = natural_order(kOrderDims[o][0], kOrderDims[o][1]);
+  const std::vector<uint32_t>* natural[13];
+  for (int o = 0; o < 13; ++o) natural[o] = &cached_natural_order(o);
   struct Pass {
-    std::vector<std::vector<uint32_t>> orders;  // [order_id * 3 + c]
+    std::vector<std::vector<uint32_t>> orders;  // permuted orders, [order_id * 3 + c]
+    const std::vector<uint32_t>* ordering[39];  // the order in force: natural or permuted
     std::unique_ptr<Stream> hist;
   };
   std::vector<Pass> passes(fr.num_passes);
@@ -995,17 +1007,20 @@ void decode_frame_vardct(std::vector<Section>& sec, bool single, Decoded* out) {
     static const U32Dist kUsed[4] = {{0, 0x5F}, {0, 0x13}, {0, 0}, {13, 0}};
     const uint32_t used = hg.u32(kUsed);
     p.orders.resize(39);
-    for (int o = 0; o < 13; ++o)
-      for (int c = 0; c < 3; ++c) p.orders[o * 3 + c] = natural[o];
+    for (int o = 0; o < 39; ++o) p.ordering[o] = natural[o / 3];
     if (used) {
       Stream s;
       need(s.open(hg.b, 8, 0, false), "coefficient order histograms");
       for (int o = 0; o < 13; ++o) {
         if (!((used >> o) & 1)) continue;
-        const uint32_t size = (uint32_t)natural[o].size();
+        const std::vector<uint32_t>& nat = *natural[o];
+        const uint32_t size = (uint32_t)nat.size();
         for (int c = 0; c < 3; ++c) {
           const std::vector<uint32_t> perm = read_permutation(hg, s, size, size / 64);
-          for (uint32_t k = 0; k < size; ++k) p.orders[o * 3 + c][k] = natural[o][perm[k]];
+          std::vector<uint32_t>& dst = p.orders[o * 3 + c];
+          dst.resize(size);
+          for (uint32_t k = 0; k < size; ++k) dst[k] = nat[perm[k]];
+          p.ordering[o * 3 + c] = &dst;
         }
       }
       need(s.final_state(), "coefficient order final state");
@@ -1067,7 +1082,7 @@ void decode_frame_vardct(std::vector<Section>& sec, bool single, Decoded* out) {
           for (uint32_t j = 0; j < ti.rows; ++j)
             for (uint32_t i = 0; i < ti.cols; ++i) nz[c][(size_t)(ly + j) * gbw + lx + i] = per;
           if (non_zeros == 0) continue;
-          const std::vector<uint32_t>& order = P.orders[ti.order_id * 3 + c];
+          const std::vector<uint32_t>& order = *P.ordering[ti.order_id * 3 + c];
           need(order.size() == size, "coefficient order size");
           int32_t* blk = vd.coeffs[c].data() + vb.coeff_offset;
           uint32_t remaining = non_zeros;

@@ -608,7 +608,7 @@ struct Stream {
       for (auto& a : ans) JPXLG_REQ(a.read(b, log_alpha));
       if (!defer_state) JPXLG_REQ(b.read(32, &state));
     }
-    if (lz_enabled) window.assign(kWindow, 0);
+    window.clear();
     return true;
   }
 
@@ -616,11 +616,9 @@ struct Stream {
   // LZ77 window (jpxl-entropy decoder.rs:255 restart).
   bool restart(Bits& b) {
     if (!use_prefix) JPXLG_REQ(b.read(32, &state));
-    if (lz_enabled) {
-      std::fill(window.begin(), window.end(), 0u);
-      num_decoded = copy_pos = 0;
-      num_to_copy = 0;
-    }
+    window.clear();
+    num_decoded = copy_pos = 0;
+    num_to_copy = 0;
     return true;
   }
 
@@ -683,13 +681,17 @@ struct Stream {
     return ans[cluster].decode(b, &state, out);
   }
 
+  // The window grows with the symbols decoded (up to 2^20 entries, then
+  // wraps); slots not yet written read as zero, as in a zero-filled window.
   void push(uint32_t v) {
-    window[num_decoded & (kWindow - 1)] = v;
+    if (window.size() < kWindow) window.push_back(v);
+    else window[num_decoded & (kWindow - 1)] = v;
     ++num_decoded;
   }
 
   bool copied(uint32_t* out) {
-    const uint32_t v = window[copy_pos & (kWindow - 1)];
+    const uint64_t slot = copy_pos & (kWindow - 1);
+    const uint32_t v = slot < window.size() ? window[slot] : 0u;
     ++copy_pos;
     --num_to_copy;
     push(v);
