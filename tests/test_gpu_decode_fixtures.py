@@ -14,6 +14,10 @@ import pytest
 import jpxl_gb300 as jg
 
 pytestmark = pytest.mark.gpu
+# What the path achieves (sRGB float samples): djxl's own pixels to about
+# 1.5e-6 on the grey fixtures and 4.6e-5 on the out-of-gamut RGB one, held
+# here beside the conformance classes.
+MEASURED_PEAK = 1e-4
 
 GOLDEN = Path(__file__).resolve().parent / "golden" / "codestream"
 CASES = [("50_vardct_mixed_gray_128x128_nofilters_d1", 0.004, 1e-5),
@@ -41,6 +45,7 @@ def test_decoded_fixture_matches_djxl(ctx, name, peak, rmse):
     assert out.shape[1:] == ref.shape[:2]
     got_peak, got_rmse = grade(out, ref)
     assert got_peak <= peak and max(got_rmse) <= rmse, (got_peak, got_rmse, cs.info["transform_counts"])
+    assert got_peak <= MEASURED_PEAK, got_peak
 
 
 def test_decoded_grey_fixture_is_grey(ctx):
