@@ -501,6 +501,7 @@ int jpxlg_ctx_create(int device, uint32_t flags, jpxlg_ctx** out) {
   std::vector<float> dct64(64 * 64);
   build_dct64_matrix(dct64.data());
   upload_dct64(dct64.data(), c->stream);
+  upload_afv(&kAfvBasis[0][0], c->stream);
   build_opsin_inverse(om, ob, oc);
   upload_dct_constants(iv4, iv8, iv16, sf, c->stream);
   upload_blur_consts(c->stream);

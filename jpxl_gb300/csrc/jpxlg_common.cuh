@@ -39,8 +39,9 @@ __device__ __forceinline__ int mirror1d(int c, int size) {
 
 // ---- transforms -------------------------------------------------------------
 // The varblock types the pixel path carries (Table I.1): the nine plain
-// DCTRxC types up to 32 (the encoder's), DCT2x2, and DCT64x64 / DCT64x32 /
-// DCT32x64 (decoded streams): DctSelect and footprint rows/cols in blocks.
+// DCTRxC types up to 32 (the encoder's) and, for decoded streams, the 8x8
+// special transforms (Hornuss, DCT2x2, DCT4x4, DCT4x8/8x4, AFV0-3) and
+// DCT64x64 / DCT64x32 / DCT32x64: DctSelect and footprint rows/cols in blocks.
 struct Shape {
   int brows, bcols;
 };
@@ -55,7 +56,9 @@ __host__ __device__ __forceinline__ bool shape_of(int sel, Shape* s) {
     case 9: *s = {1, 4}; return true;
     case 10: *s = {4, 2}; return true;
     case 11: *s = {2, 4}; return true;
-    case 2: *s = {1, 1}; return true;
+    case 1: case 2: case 3: case 12: case 13: case 14: case 15: case 16: case 17:
+      *s = {1, 1};
+      return true;
     case 18: *s = {8, 8}; return true;
     case 19: *s = {8, 4}; return true;
     case 20: *s = {4, 8}; return true;
@@ -63,8 +66,9 @@ __host__ __device__ __forceinline__ bool shape_of(int sel, Shape* s) {
   }
 }
 // compact dequant slot: 0 DCT8, 1 DCT16x16, 2 DCT32x32, 3 DCT16x8/8x16,
-// 4 DCT32x8/8x32, 5 DCT32x16/16x32, 6 DCT2x2, 7 DCT64x64, 8 DCT64x32/32x64
-// (Table I.4 indices 0,4,5,6,7,8,2,11,12).
+// 4 DCT32x8/8x32, 5 DCT32x16/16x32, 6 DCT2x2, 7 DCT64x64, 8 DCT64x32/32x64,
+// 9 Hornuss, 10 DCT4x4, 11 DCT4x8/8x4, 12 AFV0-3 (Table I.4 indices
+// 0,4,5,6,7,8,2,11,12,1,3,9,10).
 __host__ __device__ __forceinline__ int dq_slot(int sel) {
   switch (sel) {
     case 0: return 0;
@@ -75,16 +79,20 @@ __host__ __device__ __forceinline__ int dq_slot(int sel) {
     case 2: return 6;
     case 18: return 7;
     case 19: case 20: return 8;
+    case 1: return 9;
+    case 3: return 10;
+    case 12: case 13: return 11;
+    case 14: case 15: case 16: case 17: return 12;
     default: return 5;
   }
 }
 // Offsets of each slot's landscape matrix in the packed dequant table.
 __host__ __device__ __forceinline__ int dq_offset(int slot) {
-  // sizes: 64, 256, 1024, 128, 256, 512, 64, 4096, 2048
-  const int off[9] = {0, 64, 320, 1344, 1472, 1728, 2240, 2304, 6400};
+  // sizes: 64, 256, 1024, 128, 256, 512, 64, 4096, 2048, 64, 64, 64, 64
+  const int off[13] = {0, 64, 320, 1344, 1472, 1728, 2240, 2304, 6400, 8448, 8512, 8576, 8640};
   return off[slot];
 }
-constexpr int kDequantTableFloats = 8448;  // per channel
+constexpr int kDequantTableFloats = 8704;  // per channel
 
 // ---- exact-parity cube roots -----------------------------------------------
 // The reference has two cube roots, each f64 iteration rounded once to f32:

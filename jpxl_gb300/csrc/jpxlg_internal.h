@@ -36,15 +36,18 @@ struct QuantScalars {
 };
 
 // Shape classes, in this order: the nine plain DCTRxC types up to 32, then
-// DCT2x2, DCT64x64, DCT64x32 and DCT32x64.
-constexpr int kNumShapes = 13;
-constexpr int kShapeSel[kNumShapes] = {0, 4, 5, 6, 7, 8, 9, 10, 11, 2, 18, 19, 20};
+// DCT2x2, DCT64x64, DCT64x32, DCT32x64, Hornuss, DCT4x4, DCT8x4, DCT4x8 and
+// AFV0-3.
+constexpr int kNumShapes = 21;
+constexpr int kShapeSel[kNumShapes] = {0, 4,  5,  6,  7, 8, 9,  10, 11, 2,  18,
+                                       19, 20, 1, 3, 13, 12, 14, 15, 16, 17};
 
 // ---- host tables (tables.cu) -------------------------------------------------
 void build_dequant_tables(float* out /* 3 * kDequantTableFloats */);
 void build_iv_tables(float* iv4, float* iv8, float* iv16);
 void build_scale_f(float* out /* [4][8]: lf counts 1,2,4,8 x c<8 */);
 void build_dct64_matrix(float* out /* [64][64]: DCT-II rows u, columns x */);
+extern const double kAfvBasis[16][16];  // jpxl-core varblock.rs AFV_BASIS (Table I.11)
 float host_hf_multiplier(uint32_t gs, uint32_t hf_mul);
 float host_qm_multiplier(uint32_t qm_scale);
 void host_lf_multipliers(uint32_t gs, uint32_t quant_lf, float out[3]);

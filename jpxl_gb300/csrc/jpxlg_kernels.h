@@ -58,6 +58,7 @@ void launch_lf_prepare(const int32_t* lfq, int bw, int bh, const float m[3], flo
                        float kb, bool smooth, float* tmp, float* out, int num_sms,
                        cudaStream_t s);
 void upload_dct64(const float* matrix, cudaStream_t s);
+void upload_afv(const double* basis, cudaStream_t s);
 
 // Fills table[h] = hf_multiplier_f64(global_scale, h) for h < kMulTableN.
 void launch_mul_table(uint32_t global_scale, float* table, cudaStream_t s);

@@ -40,6 +40,158 @@ __device__ __forceinline__ void idct_64(float* v) {
   for (int k = 0; k < 64; ++k) v[k] = out[k] * 8.0f;
 }
 
+// jpxl-core dct.rs:982 idct_2d_in_place for the small shapes of the 8x8
+// special transforms: coef is landscape (min x max), out ROWS x COLS samples.
+template <int ROWS, int COLS>
+__device__ __forceinline__ void idct2d_raw(const float* coef, float* out) {
+  float s[ROWS * COLS];
+#pragma unroll
+  for (int r = 0; r < ROWS; ++r)
+#pragma unroll
+    for (int c = 0; c < COLS; ++c)
+      s[c * ROWS + r] = COLS > ROWS ? coef[r * COLS + c] : coef[c * ROWS + r];
+#pragma unroll
+  for (int k = 0; k < ROWS; ++k) {
+    float v[COLS];
+#pragma unroll
+    for (int i = 0; i < COLS; ++i) v[i] = s[i * ROWS + k];
+    idct_1d<COLS>(v);
+#pragma unroll
+    for (int i = 0; i < COLS; ++i) s[i * ROWS + k] = v[i];
+  }
+#pragma unroll
+  for (int r = 0; r < ROWS; ++r)
+#pragma unroll
+    for (int c = 0; c < COLS; ++c) out[r * COLS + c] = s[c * ROWS + r];
+#pragma unroll
+  for (int c = 0; c < COLS; ++c) {
+    float v[ROWS];
+#pragma unroll
+    for (int i = 0; i < ROWS; ++i) v[i] = out[i * COLS + c];
+    idct_1d<ROWS>(v);
+#pragma unroll
+    for (int i = 0; i < ROWS; ++i) out[i * COLS + c] = v[i];
+  }
+}
+
+__device__ double g_afv[256];  // Table I.11, uploaded by the host
+
+// The 8x8 special transforms of jpxl-core varblock.rs:926-1230 on a
+// dequantized block b (row-major, LLF at 0): KIND 2 Hornuss, 3 DCT4x4,
+// 4 DCT8x4, 5 DCT4x8, 6..9 AFV0..AFV3.  Evaluation order follows the
+// reference expression by expression.
+template <int KIND>
+__device__ __forceinline__ void special_block(const float* b, float* o) {
+  auto at = [&](int x, int y) { return b[y * 8 + x]; };
+  auto set = [&](int x, int y, float v) { o[y * 8 + x] = v; };
+  if constexpr (KIND == 2 || KIND == 3) {
+    const float c00 = b[0], c01 = b[1], c10 = b[8], c11 = b[9];
+    const float dcs[4] = {((c00 + c01) + c10) + c11, ((c00 + c01) - c10) - c11,
+                          ((c00 - c01) + c10) - c11, ((c00 - c01) - c10) + c11};
+#pragma unroll
+    for (int y = 0; y < 2; ++y)
+#pragma unroll
+      for (int x = 0; x < 2; ++x) {
+        if constexpr (KIND == 2) {
+          float rs = 0.0f;
+#pragma unroll
+          for (int iy = 0; iy < 4; ++iy)
+#pragma unroll
+            for (int ix = (iy == 0 ? 1 : 0); ix < 4; ++ix) rs += at(x + ix * 2, y + iy * 2);
+          const float centre = dcs[y * 2 + x] - rs / 16.0f;
+          set(4 * x + 1, 4 * y + 1, centre);
+#pragma unroll
+          for (int iy = 0; iy < 4; ++iy)
+#pragma unroll
+            for (int ix = 0; ix < 4; ++ix)
+              if (!(ix == 1 && iy == 1)) set(x * 4 + ix, y * 4 + iy, at(x + ix * 2, y + iy * 2) + centre);
+          set(4 * x, 4 * y, at(x + 2, y + 2) + centre);
+        } else {
+          float blk[16], smp[16];
+#pragma unroll
+          for (int iy = 0; iy < 4; ++iy)
+#pragma unroll
+            for (int ix = 0; ix < 4; ++ix) blk[iy * 4 + ix] = at(x + ix * 2, y + iy * 2);
+          blk[0] = dcs[y * 2 + x];
+          idct2d_raw<4, 4>(blk, smp);
+#pragma unroll
+          for (int l = 0; l < 4; ++l)
+#pragma unroll
+            for (int k = 0; k < 4; ++k) set(4 * x + k, 4 * y + l, smp[l * 4 + k]);
+        }
+      }
+  } else if constexpr (KIND == 4 || KIND == 5) {
+    const float coef0 = at(0, 0), coef1 = at(0, 1);
+    const float dcs[2] = {coef0 + coef1, coef0 - coef1};
+#pragma unroll
+    for (int half = 0; half < 2; ++half) {
+      float g[32], smp[32];
+#pragma unroll
+      for (int iy = 0; iy < 4; ++iy)
+#pragma unroll
+        for (int ix = 0; ix < 8; ++ix) g[iy * 8 + ix] = at(ix, half + iy * 2);
+      g[0] = dcs[half];
+      if constexpr (KIND == 4) {
+        idct2d_raw<8, 4>(g, smp);
+#pragma unroll
+        for (int iy = 0; iy < 8; ++iy)
+#pragma unroll
+          for (int ix = 0; ix < 4; ++ix) set(4 * half + ix, iy, smp[iy * 4 + ix]);
+      } else {
+        idct2d_raw<4, 8>(g, smp);
+#pragma unroll
+        for (int iy = 0; iy < 4; ++iy)
+#pragma unroll
+          for (int ix = 0; ix < 8; ++ix) set(ix, 4 * half + iy, smp[iy * 8 + ix]);
+      }
+    }
+  } else {
+    constexpr int n = KIND - 6, fx = n & 1, fy = n / 2;
+    float ca[16], sa[16];
+    ca[0] = ((at(0, 0) + at(0, 1)) + at(1, 0)) * 4.0f;
+#pragma unroll
+    for (int iy = 0; iy < 4; ++iy)
+#pragma unroll
+      for (int ix = (iy == 0 ? 1 : 0); ix < 4; ++ix) ca[iy * 4 + ix] = at(ix * 2, iy * 2);
+#pragma unroll
+    for (int q = 0; q < 16; ++q) {
+      double acc = 0.0;
+#pragma unroll
+      for (int j = 0; j < 16; ++j) acc += (double)ca[j] * g_afv[j * 16 + q];
+      sa[q] = (float)acc;
+    }
+#pragma unroll
+    for (int iy = 0; iy < 4; ++iy)
+#pragma unroll
+      for (int ix = 0; ix < 4; ++ix) {
+        const int sx = fx ? 3 - ix : ix, sy = fy ? 3 - iy : iy;
+        set(fx * 4 + ix, fy * 4 + iy, sa[sy * 4 + sx]);
+      }
+    float c44[16], s44[16];
+#pragma unroll
+    for (int iy = 0; iy < 4; ++iy)
+#pragma unroll
+      for (int ix = 0; ix < 4; ++ix) c44[iy * 4 + ix] = at(ix * 2 + 1, iy * 2);
+    c44[0] = (at(0, 0) - at(1, 0)) + at(0, 1);
+    idct2d_raw<4, 4>(c44, s44);
+#pragma unroll
+    for (int iy = 0; iy < 4; ++iy)
+#pragma unroll
+      for (int ix = 0; ix < 4; ++ix) set((fx ? 0 : 4) + ix, fy * 4 + iy, s44[iy * 4 + ix]);
+    float c48[32], s48[32];
+#pragma unroll
+    for (int iy = 0; iy < 4; ++iy)
+#pragma unroll
+      for (int ix = 0; ix < 8; ++ix) c48[iy * 8 + ix] = at(ix, 1 + iy * 2);
+    c48[0] = at(0, 0) - at(0, 1);
+    idct2d_raw<4, 8>(c48, s48);
+#pragma unroll
+    for (int iy = 0; iy < 4; ++iy)
+#pragma unroll
+      for (int ix = 0; ix < 8; ++ix) set(ix, (fy ? 0 : 4) + iy, s48[iy * 8 + ix]);
+  }
+}
+
 template <int N>
 __device__ __forceinline__ void idct_n(float* v) {
   if constexpr (N == 64) idct_64(v);
@@ -166,6 +318,10 @@ __global__ void __launch_bounds__(128) k_render_vb(RenderArgs a, const uint32_t*
   float dY[CR];
   // compact dequant slot of this shape (Table I.4 indices 0,4,5,6,7,8)
   constexpr int slot = KIND == 1 ? 6
+                       : KIND == 2 ? 9
+                       : KIND == 3 ? 10
+                       : (KIND == 4 || KIND == 5) ? 11
+                       : KIND >= 6 ? 12
                        : (R == 64 && C == 64) ? 7
                        : (T == 64) ? 8
                        : (R == C) ? (R == 8 ? 0 : (R == 16 ? 1 : 2))
@@ -196,7 +352,30 @@ __global__ void __launch_bounds__(128) k_render_vb(RenderArgs a, const uint32_t*
     }
     __syncthreads();
     float v[T];
-    if constexpr (KIND == 1) {
+    if constexpr (KIND >= 2) {
+      // thread 0 of the group reconstructs the block, then thread j writes
+      // sample column j.
+      if (active && j == 0) {
+        float b[64], o[64];
+#pragma unroll
+        for (int i = 0; i < 64; ++i) b[i] = L[g][i / 8][i % 8];
+        special_block<KIND>(b, o);
+#pragma unroll
+        for (int i = 0; i < 64; ++i) L[g][i / 8][i % 8] = o[i];
+      }
+      __syncthreads();
+      if (active) {
+        const int fx = x0 + j;
+        if (fx < geo.w) {
+#pragma unroll
+          for (int rr = 0; rr < 8; ++rr) {
+            const int fy = y0 + rr;
+            if (fy < geo.h) a.planes[plane * c + (size_t)fy * geo.w + fx] = L[g][rr][j];
+          }
+        }
+      }
+      __syncthreads();
+    } else if constexpr (KIND == 1) {
       // varblock.rs:895 aux_idct_2x2 with s = 2, 4, 8, each stage reading the
       // previous one; thread 0 of the group runs the cascade, then thread j
       // writes sample column j.
@@ -338,6 +517,14 @@ void launch_render_varblocks(const RenderArgs& a, const uint32_t* const* lists, 
   JPXLG_RV(10, 64, 64)
   JPXLG_RV(11, 64, 32)
   JPXLG_RV(12, 32, 64)
+  JPXLG_RVK(13, 8, 8, 2)  // Hornuss
+  JPXLG_RVK(14, 8, 8, 3)  // DCT4x4
+  JPXLG_RVK(15, 8, 8, 4)  // DCT8x4
+  JPXLG_RVK(16, 8, 8, 5)  // DCT4x8
+  JPXLG_RVK(17, 8, 8, 6)  // AFV0..AFV3
+  JPXLG_RVK(18, 8, 8, 7)
+  JPXLG_RVK(19, 8, 8, 8)
+  JPXLG_RVK(20, 8, 8, 9)
 #undef JPXLG_RV
 #undef JPXLG_RVK
 }
@@ -680,6 +867,10 @@ void launch_lf_prepare(const int32_t* lfq, int bw, int bh, const float m[3], flo
   const int blocks = (int)std::max<size_t>(1, std::min<size_t>((nb + 255) / 256, num_sms * 4));
   k_lf_dequant<<<blocks, 256, 0, s>>>(lfq, nb, m[0], m[1], m[2], div, kx, kb, smooth ? tmp : out);
   if (smooth) k_lf_smooth<<<blocks, 256, 0, s>>>(tmp, bw, bh, m[0], m[1], m[2], out);
+}
+
+void upload_afv(const double* basis, cudaStream_t s) {
+  cudaMemcpyToSymbolAsync(g_afv, basis, sizeof(double) * 256, 0, cudaMemcpyHostToDevice, s);
 }
 
 void upload_dct64(const float* matrix, cudaStream_t s) {

@@ -87,6 +87,121 @@ const Slot kSlots[9] = {{kP8x8, 6, 8, 8},    {kP16x16, 7, 16, 16}, {kP32x32, 8, 
                         {kP16x8, 7, 8, 16},  {kP32x8, 8, 8, 32},   {kP16x32, 8, 16, 32},
                         {nullptr, 0, 8, 8},  {kP64x64, 8, 64, 64}, {kP64x32, 8, 32, 64}};
 
+// Table I.6 params of the 8x8 special matrices (dequant.rs:714-1004).
+const double kHornuss[3][3] = {{280.0, 3160.0, 3160.0}, {60.0, 864.0, 864.0},
+                               {18.0, 200.0, 200.0}};
+const double kDct4x4[3][4] = {{2200.0, 0.0, 0.0, 0.0}, {392.0, 0.0, 0.0, 0.0},
+                              {112.0, -0.25, -0.25, -0.5}};
+const double kDct4x8[3][4] = {
+    {2198.050556016380522, -0.96269623020744692, -0.76194253026666783, -0.6551140670773547},
+    {764.3655248643528689, -0.92630200888366945, -0.9675229603596517, -0.27845290869168118},
+    {527.107573587542228, -1.4594385811273854, -1.450082094097871593, -1.5843722511996204}};
+const double kAfv[3][9] = {{3072.0, 3072.0, 256.0, 256.0, 256.0, 414.0, 0.0, 0.0, 0.0},
+                           {1024.0, 1024.0, 50.0, 50.0, 50.0, 58.0, 0.0, 0.0, 0.0},
+                           {384.0, 384.0, 12.0, 12.0, 12.0, 22.0, -0.25, -0.25, -0.25}};
+// AFV's band positions (dequant.rs:512-580): the frequency of each 4x4 cell.
+const double kAfvFreqs[16] = {0.0,
+                              0.0,
+                              0.8517778890324296,
+                              5.37778436506804,
+                              0.0,
+                              0.0,
+                              4.734747904497923,
+                              5.449245381693219,
+                              1.6598270267479331,
+                              4.0,
+                              7.275749096817861,
+                              10.423227632456525,
+                              2.662932286148962,
+                              7.630657783650829,
+                              8.962388608184032,
+                              12.97166202570235};
+
+double band_mult(double v) { return v > 0.0 ? 1.0 + v : 1.0 / (1.0 - v); }
+
+// dequant.rs:416 Interpolate.
+double interpolate(double pos, double max, const double* bands, int n) {
+  const int last = n - 1;
+  if (last == 0) return bands[0];
+  const double scaled = pos * (double)last / max;
+  const double fl = std::floor(scaled);
+  const int idx = (int)fl;
+  const double frac = scaled - fl;
+  const double a = bands[idx], b = bands[idx + 1];
+  return a * std::pow(b / a, frac);
+}
+
+// dequant.rs:461 GetDctQuantWeights as weights (not reciprocals), cols x rows.
+void dct_weights(int cols, int rows, const double* params, int np, double* w) {
+  double bands[8];
+  bands[0] = params[0];
+  for (int i = 1; i < np; ++i) bands[i] = bands[i - 1] * band_mult(params[i]);
+  const double max = M_SQRT2 + 1e-6;
+  for (int y = 0; y < rows; ++y)
+    for (int x = 0; x < cols; ++x) {
+      const double dx = (double)x / (double)(cols - 1), dy = (double)y / (double)(rows - 1);
+      w[y * cols + x] = interpolate(std::sqrt(dx * dx + dy * dy), max, bands, np);
+    }
+}
+
+// I.2.4 modes Hornuss, DCT4, DCT4x8 and AFV (dequant.rs:1300-1450) for
+// slots 9..12, as f32 reciprocals of the 8x8 weights.
+void special_into(int slot, int c, float* out) {
+  double w[64];
+  auto set = [&](int x, int y, double v) { w[y * 8 + x] = v; };
+  auto at = [&](int x, int y) { return w[y * 8 + x]; };
+  if (slot == 9) {
+    for (int i = 0; i < 64; ++i) w[i] = kHornuss[c][0];
+    set(0, 1, kHornuss[c][1]);
+    set(1, 0, kHornuss[c][1]);
+    set(1, 1, kHornuss[c][2]);
+    set(0, 0, 1.0);
+  } else if (slot == 10) {
+    double base[16];
+    dct_weights(4, 4, kDct4x4[c], 4, base);
+    for (int y = 0; y < 8; ++y)
+      for (int x = 0; x < 8; ++x) set(x, y, base[(y / 2) * 4 + x / 2]);
+    // params (1, 1): the divisions leave the matrix as it is
+    set(0, 1, at(0, 1) / 1.0);
+    set(1, 0, at(1, 0) / 1.0);
+    set(1, 1, at(1, 1) / 1.0);
+  } else if (slot == 11) {
+    double base[32];
+    dct_weights(8, 4, kDct4x8[c], 4, base);
+    for (int y = 0; y < 8; ++y)
+      for (int x = 0; x < 8; ++x) set(x, y, base[(y / 2) * 8 + x]);
+    set(0, 1, at(0, 1) / 1.0);
+  } else {
+    double w4x8[32], w4x4[16], bands[4];
+    dct_weights(8, 4, kDct4x8[c], 4, w4x8);
+    dct_weights(4, 4, kDct4x4[c], 4, w4x4);
+    const double* p = kAfv[c];
+    bands[0] = p[5];
+    for (int i = 1; i < 4; ++i) bands[i] = bands[i - 1] * band_mult(p[i + 5]);
+    for (int i = 0; i < 64; ++i) w[i] = 0.0;
+    set(0, 0, 1.0);
+    set(0, 1, p[0]);
+    set(1, 0, p[1]);
+    set(0, 2, p[2]);
+    set(2, 0, p[3]);
+    set(2, 2, p[4]);
+    const double lo = kAfvFreqs[2], hi = kAfvFreqs[15];
+    const double range = hi - lo + 1e-6;
+    for (int y = 0; y < 4; ++y)
+      for (int x = 0; x < 4; ++x) {
+        if (x < 2 && y < 2) continue;
+        set(2 * x, 2 * y, interpolate(kAfvFreqs[y * 4 + x] - lo, range, bands, 4));
+      }
+    for (int y = 0; y < 4; ++y)
+      for (int x = 0; x < 8; ++x)
+        if (x || y) set(x, 2 * y + 1, w4x8[y * 8 + x]);
+    for (int y = 0; y < 4; ++y)
+      for (int x = 0; x < 4; ++x)
+        if (x || y) set(2 * x + 1, 2 * y, w4x4[y * 4 + x]);
+  }
+  for (int i = 0; i < 64; ++i) out[i] = (float)(1.0 / w[i]);
+}
+
 // I.2.4 mode DCT2 (dequant.rs:1328): six rectangles of the 8x8 weights
 // matrix, (0, 0) set to one; the matrix is the f32 reciprocal.
 void dct2_into(const double* p, float* out) {
@@ -139,12 +254,72 @@ void weights_into(const double* params, int np, int rows, int cols, float* out) 
 
 void build_dequant_tables(float* out) {
   for (int c = 0; c < 3; ++c)
-    for (int s = 0; s < 9; ++s) {
+    for (int s = 0; s < 13; ++s) {
       float* dst = out + c * kDequantTableFloats + dq_offset(s);
       if (s == 6) dct2_into(kDct2[c], dst);
+      else if (s >= 9) special_into(s, c, dst);
       else weights_into(kSlots[s].params[c], kSlots[s].np, kSlots[s].rows, kSlots[s].cols, dst);
     }
 }
+
+// Table I.11, the AFV basis (standard data, as jpxl-core varblock.rs prints
+// it): row j is basis function j over the 4x4 samples in raster order.
+const double kAfvBasis[16][16] = {
+    {0.25, 0.25, 0.25, 0.25, 0.25, 0.25, 0.25, 0.25, 0.25, 0.25, 0.25, 0.25, 0.25, 0.25, 0.25,
+     0.25},
+    {0.876902929799142, 0.2206518106944235, -0.10140050393753763, -0.1014005039375375,
+     0.2206518106944236, -0.10140050393753777, -0.10140050393753772, -0.10140050393753763,
+     -0.10140050393753758, -0.10140050393753769, -0.1014005039375375, -0.10140050393753768,
+     -0.10140050393753768, -0.10140050393753759, -0.10140050393753763, -0.10140050393753741},
+    {0.0, 0.0, 0.40670075830260755, 0.44444816619734445, 0.0, 0.0, 0.19574399372042936,
+     0.2929100136981264, -0.40670075830260716, -0.19574399372042872, 0.0, 0.11379074460448091,
+     -0.44444816619734384, -0.29291001369812636, -0.1137907446044814, 0.0},
+    {0.0, 0.0, -0.21255748058288748, 0.3085497062849767, 0.0, 0.4706702258572536,
+     -0.1621205195722993, 0.0, -0.21255748058287047, -0.16212051957228327,
+     -0.47067022585725277, -0.1464291867126764, 0.3085497062849487, 0.0, -0.14642918671266536,
+     0.4251149611657548},
+    {0.0, -0.7071067811865474, 0.0, 0.0, 0.7071067811865476, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0,
+     0.0, 0.0, 0.0, 0.0},
+    {-0.4105377591765233, 0.6235485373547691, -0.06435071657946274, -0.06435071657946266,
+     0.6235485373547694, -0.06435071657946284, -0.0643507165794628, -0.06435071657946274,
+     -0.06435071657946272, -0.06435071657946279, -0.06435071657946266, -0.06435071657946277,
+     -0.06435071657946277, -0.06435071657946273, -0.06435071657946274, -0.0643507165794626},
+    {0.0, 0.0, -0.4517556589999482, 0.15854503551840063, 0.0, -0.04038515160822202,
+     0.0074182263792423875, 0.39351034269210167, -0.45175565899994635, 0.007418226379244351,
+     0.1107416575309343, 0.08298163094882051, 0.15854503551839705, 0.3935103426921022,
+     0.0829816309488214, -0.45175565899994796},
+    {0.0, 0.0, -0.304684750724869, 0.5112616136591823, 0.0, 0.0, -0.290480129728998,
+     -0.06578701549142804, 0.304684750724884, 0.2904801297290076, 0.0, -0.23889773523344604,
+     -0.5112616136592012, 0.06578701549142545, 0.23889773523345467, 0.0},
+    {0.0, 0.0, 0.3017929516615495, 0.25792362796341184, 0.0, 0.16272340142866204,
+     0.09520022653475037, 0.0, 0.3017929516615503, 0.09520022653475055, -0.16272340142866173,
+     -0.35312385449816297, 0.25792362796341295, 0.0, -0.3531238544981624, -0.6035859033230976},
+    {0.0, 0.0, 0.40824829046386274, 0.0, 0.0, 0.0, 0.0, -0.4082482904638628,
+     -0.4082482904638635, 0.0, 0.0, -0.40824829046386296, 0.0, 0.4082482904638634,
+     0.408248290463863, 0.0},
+    {0.0, 0.0, 0.1747866975480809, 0.0812611176717539, 0.0, 0.0, -0.3675398009862027,
+     -0.307882213957909, -0.17478669754808135, 0.3675398009862011, 0.0, 0.4826689115059883,
+     -0.08126111767175039, 0.30788221395790305, -0.48266891150598584, 0.0},
+    {0.0, 0.0, -0.21105601049335784, 0.18567180916109802, 0.0, 0.0, 0.49215859013738733,
+     -0.38525013709251915, 0.21105601049335806, -0.49215859013738905, 0.0, 0.17419412659916217,
+     -0.18567180916109904, 0.3852501370925211, -0.1741941265991621, 0.0},
+    {0.0, 0.0, -0.14266084808807264, -0.3416446842253372, 0.0, 0.7367497537172237,
+     0.24627107722075148, -0.08574019035519306, -0.14266084808807344, 0.24627107722075137,
+     0.14883399227113567, -0.04768680350229251, -0.3416446842253373, -0.08574019035519267,
+     -0.047686803502292804, -0.14266084808807242},
+    {0.0, 0.0, -0.13813540350758585, 0.3302282550303788, 0.0, 0.08755115000587084,
+     -0.07946706605909573, -0.4613374887461511, -0.13813540350758294, -0.07946706605910261,
+     0.49724647109535086, 0.12538059448563663, 0.3302282550303805, -0.4613374887461554,
+     0.12538059448564315, -0.13813540350758452},
+    {0.0, 0.0, -0.17437602599651067, 0.0702790691196284, 0.0, -0.2921026642334881,
+     0.3623817333531167, 0.0, -0.1743760259965108, 0.36238173335311646, 0.29210266423348785,
+     -0.4326608024727445, 0.07027906911962818, 0.0, -0.4326608024727457, 0.34875205199302267},
+    {0.0, 0.0, 0.11354987314994337, -0.07417504595810355, 0.0, 0.19402893032594343,
+     -0.435190496523228, 0.21918684838857466, 0.11354987314994257, -0.4351904965232251,
+     0.5550443808910661, -0.25468277124066463, -0.07417504595810233, 0.2191868483885728,
+     -0.25468277124066413, 0.1135498731499429},
+};
+
 
 // dct.rs:631 build_dct_matrix(64): orthonormal DCT-II rows in f64, narrowed.
 void build_dct64_matrix(float* out) {

@@ -59,3 +59,24 @@ def test_decode_render_is_deterministic(ctx):
     a = cs.render(ctx, "linear")
     b = cs.render(ctx, "linear")
     assert np.array_equal(a, b)
+
+
+def test_hornuss_fixture_against_its_source(ctx):
+    """06_gradient_300x200_lossy (cjxl -d 1 -e 7; Gaborish and EPF; five
+    sections over partial edge groups) carries 47 Hornuss varblocks among
+    eleven transform types and has no djxl decode committed.  Its sidecar
+    records how far djxl's 8-bit decode departs from the generator it states
+    (R = x*255/(w-1), G = y*255/(h-1), B = (x+y) mod 256): a peak of exactly
+    53 / 28 / 94 of 255.  The 8-bit output here departs by the same peaks
+    (ringing at the sawtooth's wrap, clipped), with mean errors of a d = 1
+    encode."""
+    cs = jg.Codestream((GOLDEN / "06_gradient_300x200_lossy.jxl").read_bytes())
+    assert cs.info["transform_counts"][1] == 47
+    out = cs.render(ctx, "srgb8").astype(np.int32)
+    h, w = 200, 300
+    y, x = np.mgrid[0:h, 0:w]
+    src = [x * 255 // (w - 1), y * 255 // (h - 1), (x + y) % 256]
+    peaks = [int(np.abs(out[:, :, c] - src[c]).max()) for c in range(3)]
+    means = [float(np.abs(out[:, :, c] - src[c]).mean()) for c in range(3)]
+    assert peaks == [53, 28, 94], peaks
+    assert max(means) < 1.0, means
