@@ -14,7 +14,8 @@ Prints one JSON line.  `value` is source MPix/s with inputs resident in HBM;
 copy of each image and the D2H read of each score inside the timed region).
 `parity` states the CUDA path's errors against the CPU restatement on the CPU
 sample; `search` times the batched quality search (64 uneven RGB8 frames x 8
-candidate quantizers = 512 probes in one CUDA graph launch).
+candidate quantizers = 512 probes in one CUDA graph launch); `decode` times
+the decode of the committed cjxl streams (host parse, GPU reconstruction).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 """
@@ -391,6 +392,56 @@ def run_select(ctxs, streams, images, dev_rgb, covers, req, steps, px_total, tor
             "sequential_fallbacks": sum(c.cover_fallbacks for c in ctxs)}
 
 
+DECODE_STREAMS = ("06_gradient_300x200_lossy", "64_vardct_lfgroupseam_rgb_128x2176_nofilters_d6")
+
+
+def run_decode(ctx, reps, np):
+    """Decode of the committed cjxl streams (jpxl-decode decode.rs:400 up to
+    the float output): host parse (headers, TOC, entropy-coded sections),
+    GPU reconstruction from the parsed frame, and both end to end with the
+    pixels back on the host.  The streams are small, so the figures carry
+    per-call overheads; they measure the decode path, not a peak rate."""
+    import jpxl_gb300 as jg
+
+    out = {"workload": "cjxl streams " + ", ".join(DECODE_STREAMS) +
+           " (tests/golden/codestream), decoded to float sRGB planes", "unit": "MPix/s",
+           "streams": {}}
+    tot_px = tot_parse = tot_render = tot_e2e = 0.0
+    for name in DECODE_STREAMS:
+        data = (ROOT / "tests" / "golden" / "codestream" / (name + ".jxl")).read_bytes()
+        cs = jg.Codestream(data)
+        px = cs.info["width"] * cs.info["height"]
+        for _ in range(3):
+            cs.render(ctx, "srgb_float")
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            jg.Codestream(data).close()
+        parse = (time.perf_counter() - t0) / reps
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            cs.render(ctx, "srgb_float")
+        render = (time.perf_counter() - t0) / reps
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            c2 = jg.Codestream(data)
+            c2.render(ctx, "srgb_float")
+            c2.close()
+        e2e = (time.perf_counter() - t0) / reps
+        cs.close()
+        out["streams"][name] = {"pixels": px, "bytes": len(data),
+                                "parse_ms": round(parse * 1e3, 3),
+                                "render_ms": round(render * 1e3, 3),
+                                "e2e_ms": round(e2e * 1e3, 3)}
+        tot_px += px
+        tot_parse += parse
+        tot_render += render
+        tot_e2e += e2e
+    out["value"] = round(tot_px / tot_e2e / 1e6, 2)
+    out["parse_mpix_s"] = round(tot_px / tot_parse / 1e6, 2)
+    out["render_mpix_s"] = round(tot_px / tot_render / 1e6, 2)
+    return out
+
+
 def run_ours(args):
     import numpy as np
     import torch
@@ -481,6 +532,9 @@ def run_ours(args):
     # device-resident, one context per stream as above.
     select = None if args.no_select else run_select(
         ctxs, streams, images, dev_rgb, covers, req, args.steps, px_total, torch, np)
+
+    # Decode of cjxl streams (host parse + GPU reconstruction), rank 0.
+    decode = None if args.no_decode or rank != 0 else run_decode(ctx, 20, np)
 
     # Stage breakdown: the same steps on one stream with stage timers.
     ctx.stage_times()  # reset
@@ -595,6 +649,7 @@ def run_ours(args):
         "parity": parity,
         "search": search,
         "select": select,
+        "decode": decode,
         "gpu_launches": int(launches),
         "cfl_sequential_fallbacks": sum(c.cfl_fallbacks for c in ctxs),
         "clocks": clocks,
@@ -626,6 +681,7 @@ def main():
                     help="skip the batched quality-search leg")
     ap.add_argument("--no-select", action="store_true",
                     help="skip the block-selection timing leg (covers are still selected)")
+    ap.add_argument("--no-decode", action="store_true", help="skip the stream-decode leg")
     ap.add_argument("--streams", type=int, default=4,
                     help="contexts (each with its own stream) that images alternate over")
     args = ap.parse_args()
