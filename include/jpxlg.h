@@ -290,7 +290,8 @@ int jpxlg_symbols_destroy(jpxlg_symbols* s);
  * :2513 decode_vardct_frame, vardct/hf_coeff.rs:689 decode_hf_group): the
  * image headers, frame header and TOC, modular sub-bitstreams (MA trees,
  * H.3/H.5 predictors) and the VarDCT sections, decoded to the frame's integer
- * content.  Bare codestreams with one regular frame; ICC profiles, previews,
+ * content.  Bare codestreams or ISO/IEC 18181-2 containers (jxlc, or jxlp
+ * fragments) with one regular frame; ICC profiles, previews,
  * patches, splines, noise, LF frames, extra channels and modular transforms
  * are reported as unsupported (JPXLG_ERR_STREAM with a reason in
  * jpxlg_codestream_last_error).  Host code only: no device is needed.

@@ -1,7 +1,7 @@
 // codestream.cu — the host-side codestream reader declared in codestream.h.
 // Follows ISO/IEC 18181-1 as jpxl-decode reads it; each part cites the
 // reference file it restates (paths under JPXL/crates/jpxl-decode/src unless
-// noted).  Supported: bare codestreams, image headers without ICC profiles or
+// noted).  Supported: bare codestreams and containers, image headers without ICC profiles or
 // previews, one frame; VarDCT frames without patches, splines or noise and
 // modular sub-bitstreams without transforms (what cjxl writes for the VarDCT
 // fixtures); modular frames whose channels all fit the global section.
@@ -1141,8 +1141,61 @@ TransformShape transform_shape(uint8_t dct_select) {
   return TransformShape{t.rows, t.cols};
 }
 
+// ISO/IEC 18181-2 container (jpxl-decode container.rs): the codestream of a
+// boxed file, from its one jxlc box or its jxlp fragments in index order.
+bool unbox(const uint8_t* data, size_t size, std::vector<uint8_t>* cs) {
+  static const uint8_t kSig[12] = {0, 0, 0, 0x0C, 'J', 'X', 'L', ' ', 0x0D, 0x0A, 0x87, 0x0A};
+  if (size < 12 || std::memcmp(data, kSig, 12) != 0) return false;
+  size_t pos = 0;
+  bool jxlc = false, last_seen = false;
+  uint32_t next_index = 0;
+  while (pos < size) {
+    need(size - pos >= 8, "truncated container box");
+    uint64_t len = ((uint64_t)data[pos] << 24) | ((uint64_t)data[pos + 1] << 16) |
+                   ((uint64_t)data[pos + 2] << 8) | data[pos + 3];
+    const uint8_t* type = data + pos + 4;
+    size_t header = 8;
+    if (len == 1) {
+      need(size - pos >= 16, "truncated container box");
+      len = 0;
+      for (int i = 0; i < 8; ++i) len = (len << 8) | data[pos + 8 + i];
+      header = 16;
+    } else if (len == 0) {
+      len = size - pos;
+    }
+    need(len >= header && len <= size - pos, "container box size");
+    const uint8_t* body = data + pos + header;
+    const size_t body_len = (size_t)len - header;
+    if (std::memcmp(type, "jxlc", 4) == 0) {
+      need(!jxlc && next_index == 0, "jxlc with another codestream box");
+      jxlc = true;
+      cs->assign(body, body + body_len);
+    } else if (std::memcmp(type, "jxlp", 4) == 0) {
+      need(!jxlc && !last_seen && body_len >= 4, "jxlp box");
+      const uint32_t idx = ((uint32_t)body[0] << 24) | ((uint32_t)body[1] << 16) |
+                           ((uint32_t)body[2] << 8) | body[3];
+      need((idx & 0x7fffffffu) == next_index, "jxlp fragments out of order");
+      ++next_index;
+      last_seen = (idx >> 31) != 0;
+      cs->insert(cs->end(), body + 4, body + body_len);
+    } else {
+      need(std::memcmp(type, "brob", 4) != 0 || body_len < 4 ||
+               (std::memcmp(body, "jxlc", 4) != 0 && std::memcmp(body, "jxlp", 4) != 0),
+           "a Brotli-compressed codestream box is not supported");
+    }
+    pos += (size_t)len;
+  }
+  need(jxlc || last_seen, "container without a complete codestream");
+  return true;
+}
+
 void decode(const uint8_t* data, size_t size, Decoded* out) {
-  need(data && size >= 2 && data[0] == 0xFF && data[1] == 0x0A, "not a bare JPEG XL codestream");
+  std::vector<uint8_t> boxed;
+  if (data && unbox(data, size, &boxed)) {
+    decode(boxed.data(), boxed.size(), out);
+    return;
+  }
+  need(data && size >= 2 && data[0] == 0xFF && data[1] == 0x0A, "not a JPEG XL codestream");
   Reader r;
   r.b.data = data;
   r.b.size_bits = size * 8;

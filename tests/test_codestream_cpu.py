@@ -144,7 +144,7 @@ def test_lf_planes_are_plausible():
 
 def test_not_a_codestream():
     with pytest.raises(jg.JpxlError) as e:
-        jg.Codestream(b"\x00\x00\x00\x0cJXL \r\n\x87\n")
+        jg.Codestream(b"\x00\x00\x00\x0cJXL \r\n\x87\x0b")
     assert e.value.code == ERR_STREAM
 
 
@@ -184,3 +184,40 @@ def test_mutated_codestreams_fail_cleanly():
         except jg.JpxlError as e:
             assert e.code == ERR_STREAM
     assert 0 < decoded < 2000
+
+
+def _box(kind: bytes, body: bytes) -> bytes:
+    return (8 + len(body)).to_bytes(4, "big") + kind + body
+
+
+SIGNATURE = bytes([0, 0, 0, 0x0C]) + b"JXL " + bytes([0x0D, 0x0A, 0x87, 0x0A])
+
+
+def test_container_jxlc_and_jxlp():
+    """The same stream bare, in one jxlc box, and split over jxlp fragments
+    (18181-2; jpxl-decode container.rs) decodes to the same content; other
+    boxes are skipped."""
+    name = "52_vardct_mixed_gray_128x128_filters_d1"
+    data = (GOLDEN / (name + ".jxl")).read_bytes()
+    ftyp = _box(b"ftyp", b"jxl " + bytes(4) + b"jxl ")
+    boxed = SIGNATURE + ftyp + _box(b"jxlc", data) + _box(b"Exif", bytes(8))
+    cut = len(data) // 3
+    parts = SIGNATURE + ftyp + _box(b"jxlp", (0).to_bytes(4, "big") + data[:cut]) + \
+        _box(b"xml ", b"<x/>") + _box(b"jxlp", (1 | 1 << 31).to_bytes(4, "big") + data[cut:])
+    ref = load(name).coefficients()
+    for blob in (boxed, parts):
+        cs = jg.Codestream(blob)
+        assert cs.info["sections_exact"] == cs.info["sections"]
+        assert np.array_equal(cs.coefficients(), ref)
+
+
+def test_container_errors():
+    data = (GOLDEN / "51_vardct_mixed_gray_128x128_nofilters_d4.jxl").read_bytes()
+    bad = [SIGNATURE + _box(b"jxlp", (1).to_bytes(4, "big") + data),      # wrong first index
+           SIGNATURE + _box(b"jxlp", (0).to_bytes(4, "big") + data),      # no final fragment
+           SIGNATURE + _box(b"jxlc", data)[:-5] + b"\x00" * 2,            # box past the end
+           SIGNATURE]                                                      # no codestream
+    for blob in bad:
+        with pytest.raises(jg.JpxlError) as e:
+            jg.Codestream(blob)
+        assert e.value.code == ERR_STREAM
