@@ -1212,7 +1212,12 @@ void decode(const uint8_t* data, size_t size, Decoded* out) {
   need(!preview, "preview frames are not supported");
   FrameInfo& f = out->frame;
   frame_header(r, m, animation, timecodes, &f);
-  need(f.frame_type == 0, "only regular frames are supported");
+  if (f.frame_type != 0) {
+    static const char* kTypes[4] = {"regular", "LF", "reference-only", "skip-progressive"};
+    throw Malformed{std::string("only regular frames are supported (first frame: ") +
+                    kTypes[f.frame_type & 3] + ", " + (f.encoding ? "modular" : "VarDCT") +
+                    ", flags " + std::to_string(f.flags) + ")"};
+  }
   need(f.upsampling == 1, "upsampled frames are not supported");
   // F.3 TOC (toc.rs:127).
   const uint32_t gdim = f.encoding == 0 ? 256 : (128u << f.group_size_shift);
