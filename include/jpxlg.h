@@ -291,8 +291,9 @@ int jpxlg_symbols_destroy(jpxlg_symbols* s);
  * image headers, frame header and TOC, modular sub-bitstreams (MA trees,
  * H.3/H.5 predictors) and the VarDCT sections, decoded to the frame's integer
  * content.  Bare codestreams or ISO/IEC 18181-2 containers (jxlc, or jxlp
- * fragments) with one regular frame; ICC profiles, previews,
- * patches, splines, noise, LF frames, extra channels and modular transforms
+ * fragments) with one regular frame, optionally after a modular LF frame
+ * (kUseLfFrame); ICC profiles, previews,
+ * patches, splines, noise, extra channels and palette transforms
  * are reported as unsupported (JPXLG_ERR_STREAM with a reason in
  * jpxlg_codestream_last_error).  Host code only: no device is needed.
  *   jpxlg_codestream_open          parse and decode; *out owns the result

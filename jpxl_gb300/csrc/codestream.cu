@@ -324,7 +324,7 @@ void frame_header(Reader& r, const ImageInfo& m, bool animation, bool timecodes,
       for (uint32_t i = 0; i < num_ds; ++i) r.u32(kLast);
     }
   }
-  if (f->frame_type == 1) r.bits(2);  // lf_level
+  if (f->frame_type == 1) f->lf_level = r.bits(2) + 1;
   bool have_crop = false;
   if (f->frame_type != 1) have_crop = r.flag();
   int64_t x0 = 0, y0 = 0;
@@ -614,14 +614,244 @@ struct GlobalTree {
   Stream dists;
 };
 
-// H.2-H.4: one modular sub-bitstream over `ch` (shapes set by the caller).
+// H.6 transforms (modular/transform.rs, squeeze.rs, rct.rs): RCT and
+// squeeze; palettes are reported as unsupported.
+struct SqueezeStep {
+  bool horizontal, in_place;
+  uint32_t begin_c, num_c;
+};
+struct ModTransform {
+  bool squeeze;
+  uint32_t begin_c = 0, rct_type = 0;
+  std::vector<SqueezeStep> steps;
+};
+
+// squeeze.rs default_params: a channel pair split first, then halvings
+// until both dimensions are at most 8.
+std::vector<SqueezeStep> default_squeeze(const std::vector<Channel>& ch) {
+  need(!ch.empty(), "default squeeze without channels");
+  std::vector<SqueezeStep> sp;
+  uint32_t w = ch[0].w, h = ch[0].h;
+  const uint32_t count = (uint32_t)ch.size();
+  if (count > 2 && ch[1].w == w && ch[1].h == h) {
+    sp.push_back({true, false, 1, 2});
+    sp.push_back({false, false, 1, 2});
+  }
+  if (h >= w && h > 8) {
+    sp.push_back({false, true, 0, count});
+    h = (h + 1) / 2;
+  }
+  while (w > 8 || h > 8) {
+    if (w > 8) {
+      sp.push_back({true, true, 0, count});
+      w = (w + 1) / 2;
+    }
+    if (h > 8) {
+      sp.push_back({false, true, 0, count});
+      h = (h + 1) / 2;
+    }
+  }
+  return sp;
+}
+
+ModTransform read_transform(Reader& r) {
+  static const U32Dist kBeginC[4] = {{3, 0}, {6, 8}, {10, 72}, {13, 1096}};
+  ModTransform t;
+  const uint32_t tr = r.bits(2);
+  if (tr == 2) {
+    static const U32Dist kNumSq[4] = {{0, 0}, {4, 1}, {6, 9}, {8, 41}};
+    static const U32Dist kNumC[4] = {{0, 1}, {0, 2}, {0, 3}, {4, 4}};
+    t.squeeze = true;
+    const uint32_t n = r.u32(kNumSq);
+    for (uint32_t i = 0; i < n; ++i) {
+      SqueezeStep st;
+      st.horizontal = r.flag();
+      st.in_place = r.flag();
+      st.begin_c = r.u32(kBeginC);
+      st.num_c = r.u32(kNumC);
+      t.steps.push_back(st);
+    }
+    return t;
+  }
+  need(tr == 0, "palette transforms are not supported");
+  static const U32Dist kRct[4] = {{0, 6}, {2, 0}, {4, 2}, {6, 10}};
+  t.squeeze = false;
+  t.begin_c = r.u32(kBeginC);
+  t.rct_type = r.u32(kRct);
+  need(t.rct_type < 42, "rct_type");
+  return t;
+}
+
+// transform.rs:350 forward_squeeze on the channel shapes.
+void forward_squeeze(std::vector<Channel>& ch, const std::vector<SqueezeStep>& steps) {
+  for (const SqueezeStep& st : steps) {
+    need(st.num_c >= 1, "squeeze num_c");
+    const size_t begin = st.begin_c, end = (size_t)st.begin_c + st.num_c - 1;
+    need(end < ch.size(), "squeeze channel range");
+    const size_t r = st.in_place ? end + 1 : ch.size();
+    for (size_t c = begin; c <= end; ++c) {
+      Channel& sc = ch[c];
+      need(sc.w && sc.h, "squeeze of an empty channel");
+      Channel res;
+      if (st.horizontal) {
+        res.w = sc.w / 2;
+        res.h = sc.h;
+        sc.w = (sc.w + 1) / 2;
+        if (sc.hshift >= 0) ++sc.hshift;
+      } else {
+        res.h = sc.h / 2;
+        res.w = sc.w;
+        sc.h = (sc.h + 1) / 2;
+        if (sc.vshift >= 0) ++sc.vshift;
+      }
+      res.hshift = sc.hshift;
+      res.vshift = sc.vshift;
+      const size_t at = r + (c - begin);
+      need(at <= ch.size(), "squeeze residual index");
+      ch.insert(ch.begin() + (ptrdiff_t)at, res);
+    }
+    need(ch.size() <= (1u << 16), "channel count");
+  }
+}
+
+// squeeze.rs:157 tendency.
+int64_t tendency(int64_t a, int64_t b, int64_t c) {
+  if (a >= b && b >= c) {
+    int64_t x = (4 * a - 3 * c - b + 6) / 12;
+    if (x - (x & 1) > 2 * (a - b)) x = 2 * (a - b) + 1;
+    if (x + (x & 1) > 2 * (b - c)) x = 2 * (b - c);
+    return x;
+  }
+  if (a <= b && b <= c) {
+    int64_t x = (4 * a - 3 * c - b - 6) / 12;
+    if (x + (x & 1) < 2 * (a - b)) x = 2 * (a - b) - 1;
+    if (x - (x & 1) < 2 * (b - c)) x = 2 * (b - c);
+    return x;
+  }
+  return 0;
+}
+
+// squeeze.rs:183/:238 horiz_isqueeze / vert_isqueeze.
+Channel unsqueeze(const Channel& lo, const Channel& res, bool horizontal) {
+  Channel out;
+  out.hshift = lo.hshift;
+  out.vshift = lo.vshift;
+  if (horizontal) {
+    need(res.h == lo.h && (lo.w == res.w || lo.w == res.w + 1), "horizontal unsqueeze shapes");
+    out.w = lo.w + res.w;
+    out.h = lo.h;
+    if (out.hshift > 0) --out.hshift;
+    out.v.assign((size_t)out.w * out.h, 0);
+    for (uint32_t y = 0; y < lo.h; ++y) {
+      for (uint32_t x = 0; x < res.w; ++x) {
+        const int64_t avg = lo.at(x, y), residu = res.at(x, y);
+        const int64_t next = x + 1 < lo.w ? (int64_t)lo.at(x + 1, y) : avg;
+        const int64_t left = x > 0 ? (int64_t)out.at(2 * x - 1, y) : avg;
+        const int64_t diff = residu + tendency(left, avg, next);
+        const int64_t first = avg + diff / 2;
+        out.at(2 * x, y) = (int32_t)first;
+        out.at(2 * x + 1, y) = (int32_t)(first - diff);
+      }
+      if (lo.w > res.w) out.at(2 * res.w, y) = lo.at(res.w, y);
+    }
+  } else {
+    need(res.w == lo.w && (lo.h == res.h || lo.h == res.h + 1), "vertical unsqueeze shapes");
+    out.w = lo.w;
+    out.h = lo.h + res.h;
+    if (out.vshift > 0) --out.vshift;
+    out.v.assign((size_t)out.w * out.h, 0);
+    for (uint32_t y = 0; y < res.h; ++y)
+      for (uint32_t x = 0; x < lo.w; ++x) {
+        const int64_t avg = lo.at(x, y), residu = res.at(x, y);
+        const int64_t next = y + 1 < lo.h ? (int64_t)lo.at(x, y + 1) : avg;
+        const int64_t top = y > 0 ? (int64_t)out.at(x, 2 * y - 1) : avg;
+        const int64_t diff = residu + tendency(top, avg, next);
+        const int64_t first = avg + diff / 2;
+        out.at(x, 2 * y) = (int32_t)first;
+        out.at(x, 2 * y + 1) = (int32_t)(first - diff);
+      }
+    if (lo.h > res.h)
+      for (uint32_t x = 0; x < lo.w; ++x) out.at(x, 2 * res.h) = lo.at(x, res.h);
+  }
+  return out;
+}
+
+// rct.rs:59 inverse_pixel over channels begin_c..begin_c+3.
+void inverse_rct(std::vector<Channel>& ch, uint32_t begin, uint32_t type) {
+  need((size_t)begin + 3 <= ch.size(), "RCT channel range");
+  Channel& c0 = ch[begin];
+  Channel& c1 = ch[begin + 1];
+  Channel& c2 = ch[begin + 2];
+  need(c0.same_shape(c1) && c0.same_shape(c2), "RCT channel shapes");
+  const uint32_t perm = type / 7, kind = type % 7;
+  for (size_t i = 0; i < c0.v.size(); ++i) {
+    const int64_t a = c0.v[i];
+    int64_t b = c1.v[i], c = c2.v[i], d, e, f;
+    if (kind == 6) {
+      const int64_t tmp = a - (c >> 1);
+      e = c + tmp;
+      f = tmp - (b >> 1);
+      d = f + b;
+    } else {
+      if (kind & 1) c += a;
+      if ((kind >> 1) == 1) b += a;
+      if ((kind >> 1) == 2) b += (a + c) >> 1;
+      d = a;
+      e = b;
+      f = c;
+    }
+    int64_t v[3];
+    const uint32_t half = perm / 3;
+    v[perm % 3] = d;
+    v[(perm + 1 + half) % 3] = e;
+    v[(perm + 2 - half) % 3] = f;
+    c0.v[i] = (int32_t)v[0];
+    c1.v[i] = (int32_t)v[1];
+    c2.v[i] = (int32_t)v[2];
+  }
+}
+
+void inverse_transforms(std::vector<Channel>& ch, const std::vector<ModTransform>& tf) {
+  for (size_t k = tf.size(); k-- > 0;) {
+    const ModTransform& t = tf[k];
+    if (!t.squeeze) {
+      inverse_rct(ch, t.begin_c, t.rct_type);
+      continue;
+    }
+    for (size_t s = t.steps.size(); s-- > 0;) {
+      const SqueezeStep& st = t.steps[s];
+      const size_t begin = st.begin_c, end = (size_t)st.begin_c + st.num_c - 1;
+      need(end < ch.size(), "inverse squeeze range");
+      const size_t r = st.in_place ? end + 1 : ch.size() + begin - (end + 1);
+      for (size_t c = begin; c <= end; ++c) {
+        need(r < ch.size() && r != c, "inverse squeeze residual");
+        ch[c] = unsqueeze(ch[c], ch[r], st.horizontal);
+        ch.erase(ch.begin() + (ptrdiff_t)r);
+      }
+    }
+  }
+}
+
+// H.2-H.4: one modular sub-bitstream over `ch` (shapes set by the caller),
+// transforms undone at the end.
 void modular_stream(Reader& r, std::vector<Channel>& ch, uint32_t stream_index,
                     const GlobalTree& gt) {
   if (ch.empty()) return;
   const bool use_global = r.flag();
   const WpHeader wp = read_wp(r);
   static const U32Dist kNbTransforms[4] = {{0, 0}, {0, 1}, {4, 2}, {8, 18}};
-  need(r.u32(kNbTransforms) == 0, "modular transforms are not supported");
+  const uint32_t nbt = r.u32(kNbTransforms);
+  need(nbt <= 512, "transform count");
+  std::vector<ModTransform> transforms;
+  for (uint32_t i = 0; i < nbt; ++i) {
+    transforms.push_back(read_transform(r));
+    ModTransform& t = transforms.back();
+    if (t.squeeze) {
+      if (t.steps.empty()) t.steps = default_squeeze(ch);
+      forward_squeeze(ch, t.steps);
+    }
+  }
+  for (Channel& c : ch) c.v.assign((size_t)c.w * c.h, 0);
   Tree local;
   std::unique_ptr<Stream> owned(new Stream);
   const Tree* tree;
@@ -700,6 +930,7 @@ void modular_stream(Reader& r, std::vector<Channel>& ch, uint32_t stream_index,
     }
   }
   need(s.final_state(), "modular stream final state");
+  inverse_transforms(ch, transforms);
 }
 
 Channel make_channel(uint32_t w, uint32_t h) {
@@ -818,7 +1049,7 @@ BlockCtx read_block_ctx(Reader& r) {
 }
 
 uint32_t block_context(const BlockCtx& m, int c, uint32_t order_id, uint32_t qf,
-                       const int32_t qdc[3]) {
+                       const int32_t qdc[3], bool lf_idx_is_zero) {
   const int cls = c < 2 ? (c ^ 1) : 2;
   size_t idx = (size_t)cls * 13 + order_id;
   idx *= m.qf_thr.size() + 1;
@@ -826,14 +1057,16 @@ uint32_t block_context(const BlockCtx& m, int c, uint32_t order_id, uint32_t qf,
     if (qf > t) ++idx;
   for (int i = 0; i < 3; ++i) idx *= m.lf_thr[i].size() + 1;
   size_t lf = 0;
-  for (int32_t t : m.lf_thr[0])
-    if (qdc[0] > t) ++lf;
-  lf *= m.lf_thr[2].size() + 1;
-  for (int32_t t : m.lf_thr[2])
-    if (qdc[2] > t) ++lf;
-  lf *= m.lf_thr[1].size() + 1;
-  for (int32_t t : m.lf_thr[1])
-    if (qdc[1] > t) ++lf;
+  if (!lf_idx_is_zero) {
+    for (int32_t t : m.lf_thr[0])
+      if (qdc[0] > t) ++lf;
+    lf *= m.lf_thr[2].size() + 1;
+    for (int32_t t : m.lf_thr[2])
+      if (qdc[2] > t) ++lf;
+    lf *= m.lf_thr[1].size() + 1;
+    for (int32_t t : m.lf_thr[1])
+      if (qdc[1] > t) ++lf;
+  }
   need(idx + lf < m.map.size(), "block context index");
   return m.map[idx + lf];
 }
@@ -884,8 +1117,9 @@ void decode_frame_vardct(std::vector<Section>& sec, bool single, Decoded* out) {
   const FrameInfo& fr = out->frame;
   VarDctFrame& vd = out->vardct;
   auto section = [&](uint64_t i) -> Reader& { return single ? sec[0].r : sec[i].r; };
-  need((fr.flags & (1 | 2 | 16 | 32)) == 0,
-       "noise, patches, splines and LF frames are not supported");
+  need((fr.flags & (1 | 2 | 16)) == 0, "noise, patches and splines are not supported");
+  vd.lf_from_frame = (fr.flags & 32) != 0;
+  need(!vd.lf_from_frame || !vd.lf_frame[0].empty(), "kUseLfFrame without an LF frame");
   need(img.num_extra == 0, "extra channels are not supported");
   const uint32_t W = fr.width, H = fr.height;
   const uint32_t gdim = 256, lfdim = 2048;
@@ -932,15 +1166,18 @@ void decode_frame_vardct(std::vector<Section>& sec, bool single, Decoded* out) {
     const uint32_t gw = std::min(lfdim, W - x0), gh = std::min(lfdim, H - y0);
     const uint32_t bw = (gw + 7) / 8, bh = (gh + 7) / 8;
     const uint32_t bx0 = x0 / 8, by0 = y0 / 8;
-    vd.extra_precision = r.bits(2);
-    std::vector<Channel> lfch = {make_channel(bw, bh), make_channel(bw, bh), make_channel(bw, bh)};
-    modular_stream(r, lfch, (uint32_t)(1 + lg), gt);
-    // stream order Y, X, B (lf.rs:80)
-    const int plane_of[3] = {1, 0, 2};
-    for (int k = 0; k < 3; ++k)
-      for (uint32_t y = 0; y < bh; ++y)
-        for (uint32_t x = 0; x < bw; ++x)
-          vd.lf[plane_of[k]][(size_t)(by0 + y) * vd.bw + bx0 + x] = lfch[k].at(x, y);
+    if (!vd.lf_from_frame) {
+      vd.extra_precision = r.bits(2);
+      std::vector<Channel> lfch = {make_channel(bw, bh), make_channel(bw, bh),
+                                   make_channel(bw, bh)};
+      modular_stream(r, lfch, (uint32_t)(1 + lg), gt);
+      // stream order Y, X, B (lf.rs:80)
+      const int plane_of[3] = {1, 0, 2};
+      for (int k = 0; k < 3; ++k)
+        for (uint32_t y = 0; y < bh; ++y)
+          for (uint32_t x = 0; x < bw; ++x)
+            vd.lf[plane_of[k]][(size_t)(by0 + y) * vd.bw + bx0 + x] = lfch[k].at(x, y);
+    }
     // HF metadata (G.2.4; hf_meta.rs:111).
     const uint32_t nb = 1 + r.bits(ceil_log2((uint64_t)bw * bh));
     const uint32_t cw = (gw + 63) / 64, chh = (gh + 63) / 64;
@@ -1067,7 +1304,8 @@ void decode_frame_vardct(std::vector<Section>& sec, bool single, Decoded* out) {
         const size_t lfi = (size_t)vb.by * vd.bw + vb.bx;
         const int32_t qdc[3] = {vd.lf[0][lfi], vd.lf[1][lfi], vd.lf[2][lfi]};
         for (int c : {1, 0, 2}) {
-          const uint32_t bc = block_context(bctx, c, ti.order_id, vb.hf_mul, qdc);
+          const uint32_t bc =
+              block_context(bctx, c, ti.order_id, vb.hf_mul, qdc, vd.lf_from_frame);
           uint32_t pred;
           if (lx == 0 && ly == 0) pred = 32;
           else if (lx == 0) pred = nz_at(c, lx, ly - 1);
@@ -1116,22 +1354,77 @@ void decode_frame_vardct(std::vector<Section>& sec, bool single, Decoded* out) {
   });
 }
 
-void decode_frame_modular(std::vector<Section>& sec, Decoded* out) {
+void decode_frame_modular(std::vector<Section>& sec, Decoded* out, float m_lf[3] = nullptr) {
   const ImageInfo& img = out->image;
   const FrameInfo& fr = out->frame;
   need((fr.flags & (2 | 16 | 32)) == 0, "patches, splines and LF frames are not supported");
   need(img.num_extra == 0, "extra channels are not supported");
   Reader& g = sec[0].r;
-  if (!g.flag())
-    for (int c = 0; c < 3; ++c) g.f16();
+  if (!g.flag()) {
+    for (int c = 0; c < 3; ++c) {
+      const float v = g.f16();
+      if (m_lf) m_lf[c] = v;
+    }
+  }
   const GlobalTree gt = read_global_tree(g);
-  const uint32_t n = img.colour_space == 1 ? 1 : 3;
+  const uint32_t n = (img.xyb_encoded || img.colour_space != 1) ? 3 : 1;
   const uint32_t gdim = 128u << fr.group_size_shift;
   need(fr.width <= gdim && fr.height <= gdim,
        "modular frames larger than one group are not supported");
   out->modular.clear();
   for (uint32_t c = 0; c < n; ++c) out->modular.push_back(make_channel(fr.width, fr.height));
   modular_stream(g, out->modular, 0, gt);
+}
+
+// F.3 TOC (toc.rs:127) of frame f, read at r: the frame's sections, and the
+// byte after the last one.
+void read_toc(Reader& r, const uint8_t* data, size_t size, const FrameInfo& f,
+              std::vector<Section>* sections, uint64_t* end_byte) {
+  const uint32_t gdim = f.encoding == 0 ? 256 : (128u << f.group_size_shift);
+  const uint64_t groups = (uint64_t)((f.width + gdim - 1) / gdim) * ((f.height + gdim - 1) / gdim);
+  const uint64_t lf_groups =
+      (uint64_t)((f.width + 8 * gdim - 1) / (8 * gdim)) * ((f.height + 8 * gdim - 1) / (8 * gdim));
+  const uint64_t nsec = (groups == 1 && f.num_passes == 1) ? 1 : 1 + lf_groups + 1 + f.num_passes * groups;
+  need(nsec <= (1u << 20), "section count");
+  const bool permuted = r.flag();
+  std::vector<uint32_t> perm;
+  if (permuted) {
+    Stream s;
+    need(s.open(r.b, 8, 0, false), "TOC permutation");
+    perm = read_permutation(r, s, (uint32_t)nsec, 0);
+    need(s.final_state(), "TOC permutation final state");
+  }
+  r.pad_to_byte();
+  static const U32Dist kEntry[4] = {{10, 0}, {14, 1024}, {22, 17408}, {30, 4211712}};
+  std::vector<uint64_t> sizes(nsec), offsets(nsec);
+  for (auto& s : sizes) s = r.u32(kEntry);
+  r.pad_to_byte();
+  uint64_t running = 0;
+  for (uint64_t i = 0; i < nsec; ++i) {
+    offsets[i] = running;
+    running += sizes[i];
+  }
+  if (permuted) {
+    std::vector<uint64_t> po(nsec), ps(nsec);
+    for (uint64_t i = 0; i < nsec; ++i) {
+      po[i] = offsets[perm[i]];
+      ps[i] = sizes[perm[i]];
+    }
+    offsets = po;
+    sizes = ps;
+  }
+  const uint64_t base = r.b.pos / 8;
+  need(base + running <= size, "sections past the end of the codestream");
+  std::vector<Section>& sec = *sections;
+  sec.assign(nsec, Section{});
+  for (uint64_t i = 0; i < nsec; ++i) {
+    sec[i].r.b.data = data;
+    sec[i].r.b.pos = (size_t)(base + offsets[i]) * 8;
+    sec[i].r.b.size_bits = (size_t)(base + offsets[i] + sizes[i]) * 8;
+    sec[i].start_bits = sec[i].r.b.pos;
+    sec[i].size_bytes = sizes[i];
+  }
+  *end_byte = base + running;
 }
 
 }  // namespace
@@ -1211,7 +1504,39 @@ void decode(const uint8_t* data, size_t size, Decoded* out) {
   r.pad_to_byte();
   need(!preview, "preview frames are not supported");
   FrameInfo& f = out->frame;
+  for (;;) {
+  f = FrameInfo{};
   frame_header(r, m, animation, timecodes, &f);
+  if (f.frame_type == 1) {
+    // An LF frame (F.1): modular, 1/8^lf_level of the image; its XYB is the
+    // next VarDCT frame's LF (decode.rs:1686 decode_lf_frame, :1747).
+    need(f.encoding == 1 && f.lf_level == 1 && m.xyb_encoded,
+         "only modular LF frames at level 1 of XYB images are supported");
+    f.width = (f.width + 7) / 8;
+    f.height = (f.height + 7) / 8;
+    std::vector<Section> sec;
+    uint64_t end_byte = 0;
+    read_toc(r, data, size, f, &sec, &end_byte);
+    float m_lf[3] = {1.0f / 32.0f, 1.0f / 4.0f, 1.0f / 2.0f};
+    decode_frame_modular(sec, out, m_lf);
+    need(out->modular.size() == 3, "LF frame channels");
+    const size_t cells = (size_t)f.width * f.height;
+    VarDctFrame& vd = out->vardct;
+    for (auto& pl : vd.lf_frame) pl.assign(cells, 0.0f);
+    const float mx = m_lf[0] / 128.0f, my = m_lf[1] / 128.0f, mb = m_lf[2] / 128.0f;
+    for (size_t i = 0; i < cells; ++i) {
+      const float yp = (float)out->modular[0].v[i], xp = (float)out->modular[1].v[i];
+      const float bp = (float)out->modular[2].v[i];
+      vd.lf_frame[0][i] = xp * mx;
+      vd.lf_frame[1][i] = yp * my;
+      vd.lf_frame[2][i] = (bp + yp) * mb;
+    }
+    out->modular.clear();
+    r.b.pos = (size_t)end_byte * 8;
+    continue;
+  }
+  break;
+  }
   if (f.frame_type != 0) {
     static const char* kTypes[4] = {"regular", "LF", "reference-only", "skip-progressive"};
     throw Malformed{std::string("only regular frames are supported (first frame: ") +
@@ -1219,57 +1544,19 @@ void decode(const uint8_t* data, size_t size, Decoded* out) {
                     ", flags " + std::to_string(f.flags) + ")"};
   }
   need(f.upsampling == 1, "upsampled frames are not supported");
-  // F.3 TOC (toc.rs:127).
-  const uint32_t gdim = f.encoding == 0 ? 256 : (128u << f.group_size_shift);
-  const uint64_t groups = (uint64_t)((f.width + gdim - 1) / gdim) * ((f.height + gdim - 1) / gdim);
-  const uint64_t lf_groups =
-      (uint64_t)((f.width + 8 * gdim - 1) / (8 * gdim)) * ((f.height + 8 * gdim - 1) / (8 * gdim));
-  const uint64_t nsec = (groups == 1 && f.num_passes == 1) ? 1 : 1 + lf_groups + 1 + f.num_passes * groups;
-  need(nsec <= (1u << 20), "section count");
-  const bool permuted = r.flag();
-  std::vector<uint32_t> perm;
-  if (permuted) {
-    Stream s;
-    need(s.open(r.b, 8, 0, false), "TOC permutation");
-    perm = read_permutation(r, s, (uint32_t)nsec, 0);
-    need(s.final_state(), "TOC permutation final state");
-  }
-  r.pad_to_byte();
-  static const U32Dist kEntry[4] = {{10, 0}, {14, 1024}, {22, 17408}, {30, 4211712}};
-  std::vector<uint64_t> sizes(nsec), offsets(nsec);
-  for (auto& s : sizes) s = r.u32(kEntry);
-  r.pad_to_byte();
-  uint64_t running = 0;
-  for (uint64_t i = 0; i < nsec; ++i) {
-    offsets[i] = running;
-    running += sizes[i];
-  }
-  if (permuted) {
-    std::vector<uint64_t> po(nsec), ps(nsec);
-    for (uint64_t i = 0; i < nsec; ++i) {
-      po[i] = offsets[perm[i]];
-      ps[i] = sizes[perm[i]];
-    }
-    offsets = po;
-    sizes = ps;
-  }
-  const uint64_t base = r.b.pos / 8;
-  need(base + running <= size, "sections past the end of the codestream");
-  std::vector<Section> sec(nsec);
-  for (uint64_t i = 0; i < nsec; ++i) {
-    sec[i].r.b.data = data;
-    sec[i].r.b.pos = (size_t)(base + offsets[i]) * 8;
-    sec[i].r.b.size_bits = (size_t)(base + offsets[i] + sizes[i]) * 8;
-    sec[i].start_bits = sec[i].r.b.pos;
-    sec[i].size_bytes = sizes[i];
-  }
+  std::vector<Section> sec;
+  uint64_t end_byte = 0;
+  read_toc(r, data, size, f, &sec, &end_byte);
+  const uint64_t nsec = sec.size();
   out->sections = nsec;
-  out->section_sizes = sizes;
+  out->section_sizes.resize(nsec);
+  for (uint64_t i = 0; i < nsec; ++i) out->section_sizes[i] = sec[i].size_bytes;
   if (f.encoding == 0) decode_frame_vardct(sec, nsec == 1, out);
   else decode_frame_modular(sec, out);
   out->section_bits.resize(nsec);
   for (uint64_t i = 0; i < nsec; ++i) out->section_bits[i] = sec[i].r.b.pos - sec[i].start_bits;
 }
+
 
 }  // namespace cs
 }  // namespace jpxlg

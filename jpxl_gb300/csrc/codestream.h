@@ -68,6 +68,7 @@ struct FrameInfo {
   float epf_quant_mul = 0.46f, epf_pass0_sigma_scale = 0.9f, epf_pass2_sigma_scale = 6.5f;
   float epf_border_sad_mul = 2.0f / 3.0f;
   uint32_t width = 0, height = 0;  // frame samples (image / upsampling)
+  uint32_t lf_level = 0;           // LF frames
 };
 
 // A varblock of an LF group: its top-left 8x8 block (frame block coordinates),
@@ -97,6 +98,8 @@ struct VarDctFrame {
   std::vector<Varblock> varblocks;
   std::vector<int32_t> coeffs[3];      // per channel, varblocks back to back, raster
   uint32_t histogram_counts[27] = {};  // varblocks per DctSelect
+  bool lf_from_frame = false;          // LF taken from an LF frame (kUseLfFrame)
+  std::vector<float> lf_frame[3];      // that LF, X, Y, B planes of bw x bh
 };
 
 struct Decoded {

@@ -1431,11 +1431,20 @@ extern "C" int jpxlg_codestream_render(jpxlg_ctx* ctx, const jpxlg_codestream* c
   for (int c = 0; c < 3; ++c) m[c] = (float)(65536.0 * (double)(v.m_lf[c] / 128.0f) / denom);
   const float kx = 0.0f + (float)v.x_factor_lf / 84.0f;
   const float kb = 1.0f + (float)v.b_factor_lf / 84.0f;
-  const bool smooth = (f.flags & 128) == 0;
-  launch_lf_prepare(ctx->lfq.as<int32_t>(), g.bw, g.bh, m, (float)(1u << v.extra_precision), kx,
-                    kb, smooth, ctx->aux.as<float>(), ctx->lfs.as<float>(), ctx->num_sms,
-                    ctx->stream);
-  if ((rc = after_launch(ctx, smooth ? 2 : 1))) return rc;
+  if (v.lf_from_frame) {
+    // The LF frame's XYB is the LF as it stands (no CfL, no smoothing).
+    for (int c = 0; c < 3; ++c) {
+      if (v.lf_frame[c].size() != nb) return fail(ctx, JPXLG_ERR_STREAM, "LF frame size");
+      CK(cudaMemcpyAsync(ctx->lfs.as<float>() + c * nb, v.lf_frame[c].data(), nb * sizeof(float),
+                         cudaMemcpyHostToDevice, ctx->stream));
+    }
+  } else {
+    const bool smooth = (f.flags & 128) == 0;
+    launch_lf_prepare(ctx->lfq.as<int32_t>(), g.bw, g.bh, m, (float)(1u << v.extra_precision),
+                      kx, kb, smooth, ctx->aux.as<float>(), ctx->lfs.as<float>(), ctx->num_sms,
+                      ctx->stream);
+    if ((rc = after_launch(ctx, smooth ? 2 : 1))) return rc;
+  }
   const size_t out_bytes = out_kind == JPXLG_OUT_SRGB8 ? 3 * n : 3 * n * sizeof(float);
   void* dst = out;
   if (mem != JPXLG_MEM_DEVICE) {

@@ -28,7 +28,7 @@ def load(name):
 
 def test_fixtures_present():
     assert len(VARDCT) == 6, VARDCT
-    assert len(PROGRESSIVE) == 2, PROGRESSIVE
+    assert len(PROGRESSIVE) == 3, PROGRESSIVE
 
 
 @pytest.mark.parametrize("name", PROGRESSIVE)
@@ -37,6 +37,8 @@ def test_progressive_fixture_decodes_every_pass(name):
     group sections, coefficients shifted per pass) in a multi-section TOC."""
     cs = load(name)
     i = cs.info
+    if name.startswith("73_"):
+        return  # an LF frame first; see test_lf_frame_streams
     assert i["num_passes"] == (3 if name.startswith("70_") else 2)
     assert i["sections"] == 3 + i["num_passes"]  # LfGlobal, LF group, HfGlobal, a group per pass
     assert i["sections_exact"] == i["sections"]
@@ -149,12 +151,41 @@ def test_not_a_codestream():
 
 
 def test_unsupported_feature_is_reported_not_misdecoded():
-    """The lossless modular fixture uses a modular transform, which the
-    reader reports instead of decoding wrongly."""
+    """The modular fixture 07 uses a palette, which the reader reports
+    instead of decoding wrongly."""
     with pytest.raises(jg.JpxlError) as e:
         load("07_modular_gray_8x8_lossless")
     assert e.value.code == ERR_STREAM
-    assert "not supported" in str(e.value)
+    assert "palette" in str(e.value)
+
+
+@pytest.mark.parametrize("name,w,h,gen", [
+    ("60_sawtooth_32x32_lossless", 32, 32, lambda x, y: [(x * 7 + y * 3) % 256]),
+    ("40_checker_64x64_lossless", 64, 64,
+     lambda x, y: [np.where((x // 8 + y // 8) % 2 == 0, 255, 0)] * 3),
+    ("11_modular_gradient_256x256_lossless", 256, 256, lambda x, y: [x, y, (x + y) % 256]),
+])
+def test_lossless_modular_frames_match_their_generators(name, w, h, gen):
+    """Lossless modular frames (MA trees, the H.5 predictor, RCT and squeeze,
+    cjxl -d 0): every channel equals the generator each sidecar states."""
+    cs = load(name)
+    assert cs.info["encoding"] == 1 and (cs.info["width"], cs.info["height"]) == (w, h)
+    y, x = np.mgrid[0:h, 0:w]
+    want = gen(x, y)
+    assert cs.info["num_channels"] == len(want)
+    for c, plane in enumerate(want):
+        assert np.array_equal(cs.channel(c), plane), c
+
+
+@pytest.mark.parametrize("name", ["72_lfframe_gray_128x128_nofilters",
+                                  "73_progressive_all_gray_128x128_nofilters"])
+def test_lf_frame_streams(name):
+    """cjxl --progressive_dc: a modular LF frame (squeezed, 16x16) ahead of
+    the VarDCT frame, which takes its LF from it (kUseLfFrame)."""
+    cs = load(name)
+    i = cs.info
+    assert i["encoding"] == 0 and i["sections_exact"] == i["sections"]
+    assert i["num_passes"] == (1 if name.startswith("72_") else 2)
 
 
 def test_mutated_codestreams_fail_cleanly():

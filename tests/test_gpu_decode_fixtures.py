@@ -26,7 +26,9 @@ CASES = [("50_vardct_mixed_gray_128x128_nofilters_d1", 0.004, 1e-5),
          ("52_vardct_mixed_gray_128x128_filters_d1", 0.06, 0.02),
          ("53_vardct_mixed_gray_128x128_filters_d4", 0.06, 0.02),
          ("70_progressive_ac_gray_128x128_nofilters", 0.004, 1e-5),
-         ("71_qprogressive_ac_gray_128x128_nofilters", 0.004, 1e-5)]
+         ("71_qprogressive_ac_gray_128x128_nofilters", 0.004, 1e-5),
+         ("72_lfframe_gray_128x128_nofilters", 0.004, 1e-5),
+         ("73_progressive_all_gray_128x128_nofilters", 0.004, 1e-5)]
 
 
 def grade(out, ref):
