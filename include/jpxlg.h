@@ -292,9 +292,10 @@ int jpxlg_symbols_destroy(jpxlg_symbols* s);
  * H.3/H.5 predictors) and the VarDCT sections, decoded to the frame's integer
  * content.  Bare codestreams or ISO/IEC 18181-2 containers (jxlc, or jxlp
  * fragments) with one regular frame, optionally after a modular LF frame
- * (kUseLfFrame); ICC profiles, previews,
- * patches, splines, noise, extra channels and palette transforms
- * are reported as unsupported (JPXLG_ERR_STREAM with a reason in
+ * (kUseLfFrame); modular transforms RCT, squeeze and palette; a VarDCT
+ * frame's extra channels up to one group.  ICC profiles, previews, patches,
+ * splines, noise, upsampling and larger extra channels are reported as
+ * unsupported (JPXLG_ERR_STREAM with a reason in
  * jpxlg_codestream_last_error).  Host code only: no device is needed.
  *   jpxlg_codestream_open          parse and decode; *out owns the result
  *   jpxlg_codestream_info          sizes, frame parameters, per-DctSelect
@@ -328,6 +329,9 @@ int jpxlg_codestream_blocks(const jpxlg_codestream* cs, int32_t* lf, uint8_t* bl
                             int8_t* b_from_y);
 int jpxlg_codestream_coefficients(const jpxlg_codestream* cs, int32_t* out);
 int jpxlg_codestream_channel(const jpxlg_codestream* cs, uint32_t index, int32_t* out);
+/* A VarDCT frame's extra channel (alpha, ...) as sample / (2^bits - 1),
+ * width x height (channels no larger than a 256x256 group). */
+int jpxlg_codestream_extra(const jpxlg_codestream* cs, uint32_t index, float* out);
 int jpxlg_codestream_destroy(jpxlg_codestream* cs);
 /* Reconstruction of a decoded VarDCT frame on the GPU (jpxl-decode
  * decode.rs:2700-3061): LF dequantization with the LF CfL and, unless the

@@ -566,6 +566,15 @@ class Codestream:
                                                    buf.ctypes.data, MEM_HOST))
         return buf
 
+    def extra(self, index: int) -> np.ndarray:
+        """A VarDCT frame's extra channel (alpha, ...) normalised to its bit
+        depth, float32 [H, W]."""
+        out = np.zeros((self.info["height"], self.info["width"]), np.float32)
+        rc = self.lib.jpxlg_codestream_extra(self.handle, index, out.ctypes.data)
+        if rc:
+            raise JpxlError(rc, "jpxlg_codestream_extra")
+        return out
+
     def channel(self, index: int) -> np.ndarray:
         out = np.zeros((self.info["height"], self.info["width"]), np.int32)
         rc = self.lib.jpxlg_codestream_channel(self.handle, index, out.ctypes.data)

@@ -58,6 +58,7 @@ SIGNATURES: dict[str, tuple] = {
     "jpxlg_codestream_blocks": (_I, [_P, _P, _P, _P, _P, _P, _P]),
     "jpxlg_codestream_coefficients": (_I, [_P, _P]),
     "jpxlg_codestream_channel": (_I, [_P, _U32, _P]),
+    "jpxlg_codestream_extra": (_I, [_P, _U32, _P]),
     "jpxlg_codestream_destroy": (_I, [_P]),
     "jpxlg_codestream_render": (_I, [_P, _P, _I, _P, _U32]),
 }

@@ -149,15 +149,19 @@ void extensions(Reader& r) {
 }
 
 // headers/extra_channels.rs:154.
-void extra_channel(Reader& r) {
-  if (r.flag()) return;
+void extra_channel(Reader& r, ImageInfo::Extra* ec) {
+  *ec = ImageInfo::Extra{};
+  if (r.flag()) return;  // all_default: 8-bit alpha
   const uint32_t type = r.enumv();
   uint32_t b, e;
   bool f;
   bit_depth(r, &b, &e, &f);
+  need(!f, "floating-point extra channels are not supported");
   static const U32Dist kShift[4] = {{0, 0}, {0, 3}, {0, 4}, {3, 1}};
   static const U32Dist kName[4] = {{0, 0}, {4, 0}, {5, 16}, {10, 48}};
-  r.u32(kShift);
+  ec->type = type;
+  ec->bits = b;
+  ec->dim_shift = r.u32(kShift);
   r.skip(8ull * r.u32(kName));
   if (type == 0) r.flag();  // alpha_associated
   if (type == 2)
@@ -224,7 +228,8 @@ void image_metadata(Reader& r, ImageInfo* m, bool* preview, bool* animation, boo
     static const U32Dist kExtra[4] = {{0, 0}, {0, 1}, {4, 2}, {12, 1}};
     m->num_extra = r.u32(kExtra);
     need(m->num_extra <= 256, "extra channel count");
-    for (uint32_t i = 0; i < m->num_extra; ++i) extra_channel(r);
+    m->extra.resize(m->num_extra);
+    for (uint32_t i = 0; i < m->num_extra; ++i) extra_channel(r, &m->extra[i]);
     m->xyb_encoded = r.flag();
     colour_encoding(r, m);
     if (extra_fields && !r.flag()) {  // tone mapping
@@ -614,40 +619,59 @@ struct GlobalTree {
   Stream dists;
 };
 
-// H.6 transforms (modular/transform.rs, squeeze.rs, rct.rs): RCT and
-// squeeze; palettes are reported as unsupported.
+// H.6 transforms (modular/transform.rs, squeeze.rs, rct.rs, palette.rs).
 struct SqueezeStep {
   bool horizontal, in_place;
   uint32_t begin_c, num_c;
 };
 struct ModTransform {
-  bool squeeze;
+  int kind = 0;  // 0 RCT, 1 palette, 2 squeeze
   uint32_t begin_c = 0, rct_type = 0;
+  uint32_t num_c = 0, nb_colours = 0, nb_deltas = 0, d_pred = 0;  // palette
   std::vector<SqueezeStep> steps;
 };
 
+// Table H.10, the delta palette (standard data, as jpxl-decode
+// modular/palette.rs prints it).
+const int16_t kDeltaPalette[72][3] = {
+    {0, 0, 0}, {4, 4, 4}, {11, 0, 0}, {0, 0, -13}, {0, -12, 0}, {-10, -10, -10},
+    {-18, -18, -18}, {-27, -27, -27}, {-18, -18, 0}, {0, 0, -32}, {-32, 0, 0}, {-37, -37, -37},
+    {0, -32, -32}, {24, 24, 45}, {50, 50, 50}, {-45, -24, -24}, {-24, -45, -45}, {0, -24, -24},
+    {-34, -34, 0}, {-24, 0, -24}, {-45, -45, -24}, {64, 64, 64}, {-32, 0, -32}, {0, -32, 0},
+    {-32, 0, 32}, {-24, -45, -24}, {45, 24, 45}, {24, -24, -45}, {-45, -24, 24}, {80, 80, 80},
+    {64, 0, 0}, {0, 0, -64}, {0, -64, -64}, {-24, -24, 45}, {96, 96, 96}, {64, 64, 0},
+    {45, -24, -24}, {34, -34, 0}, {112, 112, 112}, {24, -45, -45}, {45, 45, -24}, {0, -32, 32},
+    {24, -24, 45}, {0, 96, 96}, {45, -24, 24}, {24, -45, -24}, {-24, -45, 24}, {0, -64, 0},
+    {96, 0, 0}, {128, 128, 128}, {64, 0, 64}, {144, 144, 144}, {96, 96, 0}, {-36, -36, 36},
+    {45, -24, -45}, {45, -45, -24}, {0, 0, -96}, {0, 128, 128}, {0, 96, 0}, {45, 24, -45},
+    {-128, 0, 0}, {24, -45, 24}, {-45, 24, -45}, {64, 0, -64}, {64, -64, -64}, {96, 0, 96},
+    {45, -45, 24}, {24, 45, -45}, {64, 64, -64}, {128, 128, 0}, {0, 0, -128}, {-24, 45, -45},
+};
+
+
 // squeeze.rs default_params: a channel pair split first, then halvings
 // until both dimensions are at most 8.
-std::vector<SqueezeStep> default_squeeze(const std::vector<Channel>& ch) {
-  need(!ch.empty(), "default squeeze without channels");
+std::vector<SqueezeStep> default_squeeze(const std::vector<Channel>& ch, size_t nb_meta) {
+  need(ch.size() > nb_meta, "default squeeze without channels");
   std::vector<SqueezeStep> sp;
-  uint32_t w = ch[0].w, h = ch[0].h;
-  const uint32_t count = (uint32_t)ch.size();
-  if (count > 2 && ch[1].w == w && ch[1].h == h) {
-    sp.push_back({true, false, 1, 2});
-    sp.push_back({false, false, 1, 2});
+  const uint32_t first = (uint32_t)nb_meta;
+  uint32_t w = ch[first].w, h = ch[first].h;
+  const uint32_t count = (uint32_t)(ch.size() - nb_meta);
+  if (count > 2 && ch[first + 1].w == w && ch[first + 1].h == h) {
+    sp.push_back({true, false, first + 1, 2});
+    sp.push_back({false, false, first + 1, 2});
   }
   if (h >= w && h > 8) {
-    sp.push_back({false, true, 0, count});
+    sp.push_back({false, true, first, count});
     h = (h + 1) / 2;
   }
   while (w > 8 || h > 8) {
     if (w > 8) {
-      sp.push_back({true, true, 0, count});
+      sp.push_back({true, true, first, count});
       w = (w + 1) / 2;
     }
     if (h > 8) {
-      sp.push_back({false, true, 0, count});
+      sp.push_back({false, true, first, count});
       h = (h + 1) / 2;
     }
   }
@@ -661,7 +685,7 @@ ModTransform read_transform(Reader& r) {
   if (tr == 2) {
     static const U32Dist kNumSq[4] = {{0, 0}, {4, 1}, {6, 9}, {8, 41}};
     static const U32Dist kNumC[4] = {{0, 1}, {0, 2}, {0, 3}, {4, 4}};
-    t.squeeze = true;
+    t.kind = 2;
     const uint32_t n = r.u32(kNumSq);
     for (uint32_t i = 0; i < n; ++i) {
       SqueezeStep st;
@@ -673,22 +697,91 @@ ModTransform read_transform(Reader& r) {
     }
     return t;
   }
-  need(tr == 0, "palette transforms are not supported");
-  static const U32Dist kRct[4] = {{0, 6}, {2, 0}, {4, 2}, {6, 10}};
-  t.squeeze = false;
+  need(tr <= 1, "transform id");
   t.begin_c = r.u32(kBeginC);
+  if (tr == 1) {
+    static const U32Dist kNumC[4] = {{0, 1}, {0, 3}, {0, 4}, {13, 1}};
+    static const U32Dist kColours[4] = {{8, 0}, {10, 256}, {12, 1280}, {16, 5376}};
+    static const U32Dist kDeltas[4] = {{0, 0}, {8, 1}, {10, 257}, {16, 1281}};
+    t.kind = 1;
+    t.num_c = r.u32(kNumC);
+    t.nb_colours = r.u32(kColours);
+    t.nb_deltas = r.u32(kDeltas);
+    t.d_pred = r.bits(4);
+    need(t.d_pred <= 13, "palette predictor");
+    return t;
+  }
+  static const U32Dist kRct[4] = {{0, 6}, {2, 0}, {4, 2}, {6, 10}};
+  t.kind = 0;
   t.rct_type = r.u32(kRct);
   need(t.rct_type < 42, "rct_type");
   return t;
 }
 
+// transform.rs:291 forward_palette on the channel shapes: the index channel
+// stays, the others go, and the palette (nb_colours x num_c) becomes the
+// first (meta) channel.
+void forward_palette(std::vector<Channel>& ch, const ModTransform& t, size_t* nb_meta) {
+  need(t.num_c >= 1 && (size_t)t.begin_c + t.num_c <= ch.size(), "palette channel range");
+  const size_t begin = t.begin_c, end = begin + t.num_c;
+  for (size_t c = begin + 1; c < end; ++c) need(ch[c].same_shape(ch[begin]), "palette shapes");
+  if (begin < *nb_meta) {
+    need(end <= *nb_meta && (int64_t)*nb_meta + 2 - (int64_t)t.num_c >= 0, "palette meta range");
+    *nb_meta = *nb_meta + 2 - t.num_c;
+  } else {
+    *nb_meta += 1;
+  }
+  ch.erase(ch.begin() + (ptrdiff_t)begin + 1, ch.begin() + (ptrdiff_t)end);
+  Channel meta;
+  meta.w = t.nb_colours;
+  meta.h = t.num_c;
+  meta.hshift = meta.vshift = -1;
+  ch.insert(ch.begin(), meta);
+}
+
+// palette.rs:130 lookup: an explicit colour, an implicit one past
+// nb_colours, or (negative index) a delta-palette entry.
+int64_t palette_lookup(const Channel& pal, const ModTransform& t, uint32_t bits, uint32_t c,
+                       int32_t index32) {
+  need(bits >= 1 && bits <= 32, "palette bit depth");
+  const int64_t bitdepth = bits, full = ((int64_t)1 << bitdepth) - 1;
+  const int64_t index = index32, nbc = t.nb_colours;
+  if (index >= 0 && index < nbc) return pal.at((uint32_t)index, c);
+  if (index >= nbc) {
+    int64_t i = index - nbc;
+    if (i < 64) {
+      const uint32_t shift = 2 * c;
+      const int64_t bucket = shift >= 63 ? 0 : (i >> shift) & 3;
+      const int64_t bias = (int64_t)1 << std::max<int64_t>(bitdepth - 3, 0);
+      return bucket * full / 4 + bias;
+    }
+    i -= 64;
+    for (uint32_t k = 0; k < c; ++k) {
+      if (i == 0) break;
+      i /= 5;
+    }
+    return (i % 5) * full / 4;
+  }
+  if (c >= 3) return 0;
+  const int64_t folded = ((-index - 1) % 143 + 143) % 143;
+  int64_t value = kDeltaPalette[(folded + 1) >> 1][c];
+  if ((folded & 1) == 0) value = -value;
+  if (bitdepth > 8) value <<= std::min<int64_t>(bitdepth, 24) - 8;
+  return value;
+}
+
 // transform.rs:350 forward_squeeze on the channel shapes.
-void forward_squeeze(std::vector<Channel>& ch, const std::vector<SqueezeStep>& steps) {
+void forward_squeeze(std::vector<Channel>& ch, const std::vector<SqueezeStep>& steps,
+                     size_t* nb_meta) {
   for (const SqueezeStep& st : steps) {
     need(st.num_c >= 1, "squeeze num_c");
     const size_t begin = st.begin_c, end = (size_t)st.begin_c + st.num_c - 1;
     need(end < ch.size(), "squeeze channel range");
     const size_t r = st.in_place ? end + 1 : ch.size();
+    if (begin < *nb_meta) {
+      need(st.in_place && end < *nb_meta, "squeeze inside the meta channels");
+      *nb_meta += st.num_c;
+    }
     for (size_t c = begin; c <= end; ++c) {
       Channel& sc = ch[c];
       need(sc.w && sc.h, "squeeze of an empty channel");
@@ -811,11 +904,50 @@ void inverse_rct(std::vector<Channel>& ch, uint32_t begin, uint32_t type) {
   }
 }
 
-void inverse_transforms(std::vector<Channel>& ch, const std::vector<ModTransform>& tf) {
+// palette.rs:238 apply_inverse.
+void inverse_palette(std::vector<Channel>& ch, const ModTransform& t, uint32_t bits,
+                     const WpHeader& wp) {
+  need(!ch.empty(), "palette without its meta channel");
+  const Channel pal = ch[0];
+  ch.erase(ch.begin());
+  need(pal.h >= t.num_c, "palette height");
+  const size_t first = t.begin_c;
+  need(first < ch.size(), "palette index channel");
+  const Channel idx = ch[first];
+  for (uint32_t k = 1; k < t.num_c; ++k) {
+    need(first + k <= ch.size(), "palette channel insert");
+    ch.insert(ch.begin() + (ptrdiff_t)(first + k), idx);
+  }
+  for (uint32_t c = 0; c < t.num_c; ++c) {
+    Channel& tg = ch[first + c];
+    Weighted wpred(tg.w);
+    const bool weighted = t.d_pred == 6;
+    for (uint32_t y = 0; y < tg.h; ++y) {
+      for (uint32_t x = 0; x < tg.w; ++x) {
+        const int32_t index = tg.at(x, y);
+        int64_t value = palette_lookup(pal, t, bits, c, index);
+        const Neighbours nb = gather(tg, x, y);
+        if (weighted) wpred.run(wp, nb, x);
+        if ((int64_t)index < (int64_t)t.nb_deltas)
+          value += predict(nb, t.d_pred, weighted ? wpred.prediction : 0);
+        tg.at(x, y) = (int32_t)value;
+        if (weighted) wpred.update(x, (int32_t)value);
+      }
+      if (weighted) wpred.next_row();
+    }
+  }
+}
+
+void inverse_transforms(std::vector<Channel>& ch, const std::vector<ModTransform>& tf,
+                        uint32_t bits, const WpHeader& wp) {
   for (size_t k = tf.size(); k-- > 0;) {
     const ModTransform& t = tf[k];
-    if (!t.squeeze) {
+    if (t.kind == 0) {
       inverse_rct(ch, t.begin_c, t.rct_type);
+      continue;
+    }
+    if (t.kind == 1) {
+      inverse_palette(ch, t, bits, wp);
       continue;
     }
     for (size_t s = t.steps.size(); s-- > 0;) {
@@ -835,7 +967,7 @@ void inverse_transforms(std::vector<Channel>& ch, const std::vector<ModTransform
 // H.2-H.4: one modular sub-bitstream over `ch` (shapes set by the caller),
 // transforms undone at the end.
 void modular_stream(Reader& r, std::vector<Channel>& ch, uint32_t stream_index,
-                    const GlobalTree& gt) {
+                    const GlobalTree& gt, uint32_t bits = 8) {
   if (ch.empty()) return;
   const bool use_global = r.flag();
   const WpHeader wp = read_wp(r);
@@ -843,12 +975,17 @@ void modular_stream(Reader& r, std::vector<Channel>& ch, uint32_t stream_index,
   const uint32_t nbt = r.u32(kNbTransforms);
   need(nbt <= 512, "transform count");
   std::vector<ModTransform> transforms;
+  size_t nb_meta = 0;
   for (uint32_t i = 0; i < nbt; ++i) {
     transforms.push_back(read_transform(r));
     ModTransform& t = transforms.back();
-    if (t.squeeze) {
-      if (t.steps.empty()) t.steps = default_squeeze(ch);
-      forward_squeeze(ch, t.steps);
+    if (t.kind == 2) {
+      if (t.steps.empty()) t.steps = default_squeeze(ch, nb_meta);
+      forward_squeeze(ch, t.steps, &nb_meta);
+    } else if (t.kind == 1) {
+      forward_palette(ch, t, &nb_meta);
+    } else {
+      need((size_t)t.begin_c + 3 <= ch.size(), "RCT channel range");
     }
   }
   for (Channel& c : ch) c.v.assign((size_t)c.w * c.h, 0);
@@ -930,7 +1067,7 @@ void modular_stream(Reader& r, std::vector<Channel>& ch, uint32_t stream_index,
     }
   }
   need(s.final_state(), "modular stream final state");
-  inverse_transforms(ch, transforms);
+  inverse_transforms(ch, transforms, bits, wp);
 }
 
 Channel make_channel(uint32_t w, uint32_t h) {
@@ -1120,7 +1257,6 @@ void decode_frame_vardct(std::vector<Section>& sec, bool single, Decoded* out) {
   need((fr.flags & (1 | 2 | 16)) == 0, "noise, patches and splines are not supported");
   vd.lf_from_frame = (fr.flags & 32) != 0;
   need(!vd.lf_from_frame || !vd.lf_frame[0].empty(), "kUseLfFrame without an LF frame");
-  need(img.num_extra == 0, "extra channels are not supported");
   const uint32_t W = fr.width, H = fr.height;
   const uint32_t gdim = 256, lfdim = 2048;
   const uint32_t gx = (W + gdim - 1) / gdim, gy = (H + gdim - 1) / gdim;
@@ -1157,6 +1293,16 @@ void decode_frame_vardct(std::vector<Section>& sec, bool single, Decoded* out) {
     vd.b_factor_lf = (int)g.bits(8) - 128;
   }
   const GlobalTree gt = read_global_tree(g);
+  // GlobalModular (G.1.3): a VarDCT frame's channels are its extra channels;
+  // those no larger than a group are decoded here (decode.rs:2589).
+  out->extra.clear();
+  for (const ImageInfo::Extra& e : img.extra) {
+    const uint32_t sh = e.dim_shift;
+    out->extra.push_back(make_channel((W + (1u << sh) - 1) >> sh, (H + (1u << sh) - 1) >> sh));
+    need(out->extra.back().w <= gdim && out->extra.back().h <= gdim,
+         "extra channels larger than a group are not supported");
+  }
+  modular_stream(g, out->extra, 0, gt, img.bits_per_sample);
 
   // LF groups (G.2; decode.rs:2625-2700).
   std::vector<std::vector<Varblock>> placements(num_lf);
@@ -1373,7 +1519,7 @@ void decode_frame_modular(std::vector<Section>& sec, Decoded* out, float m_lf[3]
        "modular frames larger than one group are not supported");
   out->modular.clear();
   for (uint32_t c = 0; c < n; ++c) out->modular.push_back(make_channel(fr.width, fr.height));
-  modular_stream(g, out->modular, 0, gt);
+  modular_stream(g, out->modular, 0, gt, img.bits_per_sample);
 }
 
 // F.3 TOC (toc.rs:127) of frame f, read at r: the frame's sections, and the
@@ -1619,7 +1765,7 @@ extern "C" int jpxlg_codestream_info(const jpxlg_codestream* cs, jpxlg_codestrea
   info->blocks_w = d.vardct.bw;
   info->blocks_h = d.vardct.bh;
   info->num_varblocks = (uint32_t)d.vardct.varblocks.size();
-  info->num_channels = (uint32_t)d.modular.size();
+  info->num_channels = (uint32_t)(d.modular.size() + d.extra.size());
   info->sections = (uint32_t)d.sections;
   uint32_t exact = 0;
   for (uint64_t i = 0; i < d.sections && i < d.section_bits.size(); ++i)
@@ -1672,6 +1818,18 @@ extern "C" int jpxlg_codestream_channel(const jpxlg_codestream* cs, uint32_t ind
   if (!cs || !out || index >= cs->d.modular.size()) return JPXLG_ERR_ARGUMENT;
   const jpxlg::cs::Channel& c = cs->d.modular[index];
   std::memcpy(out, c.v.data(), c.v.size() * sizeof(int32_t));
+  return JPXLG_OK;
+}
+
+// A VarDCT frame's extra channel as floats (sample / (2^bits - 1)), its
+// width x height.
+extern "C" int jpxlg_codestream_extra(const jpxlg_codestream* cs, uint32_t index, float* out) {
+  if (!cs || !out || index >= cs->d.extra.size() || index >= cs->d.image.extra.size())
+    return JPXLG_ERR_ARGUMENT;
+  const jpxlg::cs::Channel& c = cs->d.extra[index];
+  const uint32_t bits = cs->d.image.extra[index].bits;
+  const float maxv = bits >= 32 ? 4294967295.0f : (float)((1ull << bits) - 1);
+  for (size_t i = 0; i < c.v.size(); ++i) out[i] = (float)c.v[i] / maxv;
   return JPXLG_OK;
 }
 

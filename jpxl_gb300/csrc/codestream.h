@@ -44,6 +44,10 @@ struct ImageInfo {
   uint32_t num_extra = 0;
   uint32_t orientation = 1;
   float intensity_target = 255.0f;
+  struct Extra {
+    uint32_t type = 0, bits = 8, dim_shift = 0;
+  };
+  std::vector<Extra> extra;  // extra channels (alpha, depth, ...)
   bool default_opsin = true;
   float opsin_inv[9], opsin_bias[3], quant_bias[4], quant_bias_numerator = 0.145f;
 };
@@ -107,6 +111,7 @@ struct Decoded {
   FrameInfo frame;
   VarDctFrame vardct;
   std::vector<Channel> modular;        // a modular frame's channels
+  std::vector<Channel> extra;          // a VarDCT frame's extra channels
   uint64_t sections = 0;
   std::vector<uint64_t> section_bits;  // bits each section's reader consumed
   std::vector<uint64_t> section_sizes; // TOC entries, bytes

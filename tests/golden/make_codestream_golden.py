@@ -7,10 +7,10 @@ not present where the tests run; the copied files are the committed fixture):
 
     python tests/golden/make_codestream_golden.py
 
-Source: JPXL/tests/fixtures/handmade/{04,06,11,40,50..53,60,63,64,70..73}_*.jxl with the .npy decodes
+Source: JPXL/tests/fixtures/handmade/{03,04,06,07,09,11,40,50..53,60,63,64,70..73,82,110}_*.jxl with the .npy decodes
 committed beside them (djxl v0.13.0 196a43d9 --output_format npy; provenance
-in each fixture's .jxl.txt sidecar; 64 has none), plus the lossless modular
-fixture 07.
+in each fixture's .jxl.txt sidecar; 64 and the lossless fixtures have none).
+110 (photon noise) is the stream the reader reports as unsupported.
 """
 from __future__ import annotations
 
@@ -19,14 +19,18 @@ from pathlib import Path
 
 SRC = Path("/root/reference/JPXL/tests/fixtures/handmade")
 OUT = Path(__file__).resolve().parent / "codestream"
-NAMES = ["04_gradient_8x8_lossy",
+NAMES = ["03_gradient_8x8_lossless",
+         "04_gradient_8x8_lossy",
          "11_modular_gradient_256x256_lossless",
          "40_checker_64x64_lossless",
          "60_sawtooth_32x32_lossless",
          "72_lfframe_gray_128x128_nofilters",
          "73_progressive_all_gray_128x128_nofilters",
+         "82_alpha_vardct_rgba_64x64_nofilters",
+         "110_noise_rgb_32x32",
          "06_gradient_300x200_lossy",
          "07_modular_gray_8x8_lossless",
+         "09_modular_rgb_64x64_lossless",
          "50_vardct_mixed_gray_128x128_nofilters_d1",
          "51_vardct_mixed_gray_128x128_nofilters_d4",
          "52_vardct_mixed_gray_128x128_filters_d1",
