@@ -292,9 +292,10 @@ int jpxlg_symbols_destroy(jpxlg_symbols* s);
  * H.3/H.5 predictors) and the VarDCT sections, decoded to the frame's integer
  * content.  Bare codestreams or ISO/IEC 18181-2 containers (jxlc, or jxlp
  * fragments) with one regular frame, optionally after a modular LF frame
- * (kUseLfFrame); modular transforms RCT, squeeze and palette; a VarDCT
- * frame's extra channels up to one group.  ICC profiles, previews, patches,
- * splines, noise, upsampling and larger extra channels are reported as
+ * (kUseLfFrame); modular transforms RCT, squeeze and palette; modular
+ * frames of several groups (one pass) with extra channels; a VarDCT frame's
+ * extra channels up to one group.  ICC profiles, previews, patches, splines,
+ * noise, upsampling and larger VarDCT extra channels are reported as
  * unsupported (JPXLG_ERR_STREAM with a reason in
  * jpxlg_codestream_last_error).  Host code only: no device is needed.
  *   jpxlg_codestream_open          parse and decode; *out owns the result
@@ -309,7 +310,9 @@ int jpxlg_symbols_destroy(jpxlg_symbols* s);
  *   jpxlg_codestream_coefficients  quantized HF coefficients as the plan's
  *                                  coefficient image, 3 x (8*blocks_h) x
  *                                  (8*blocks_w)
- *   jpxlg_codestream_channel       a modular frame's channel, width x height */
+ *   jpxlg_codestream_channel       a modular frame's channel, width x height
+ *                                  (its colour channels, then its extra
+ *                                  channels) */
 typedef struct jpxlg_codestream jpxlg_codestream;
 typedef struct {
   uint32_t width, height, bits_per_sample, xyb_encoded, colour_space;
@@ -320,6 +323,7 @@ typedef struct {
   int32_t x_factor_lf, b_factor_lf;
   uint32_t blocks_w, blocks_h, num_varblocks, num_channels, sections, sections_exact;
   uint32_t transform_counts[27];
+  uint32_t orientation, num_extra; /* Exif orientation 1-8 (not applied); extra channels */
 } jpxlg_codestream_info_t;
 int jpxlg_codestream_open(const uint8_t* data, size_t size, jpxlg_codestream** out);
 const char* jpxlg_codestream_last_error(void);

@@ -507,7 +507,8 @@ class _CodestreamInfo(C.Structure):
         [("x_factor_lf", C.c_int32), ("b_factor_lf", C.c_int32)] + \
         [(n, C.c_uint32) for n in ("blocks_w", "blocks_h", "num_varblocks", "num_channels",
                                    "sections", "sections_exact")] + \
-        [("transform_counts", C.c_uint32 * 27)]
+        [("transform_counts", C.c_uint32 * 27)] + \
+        [(n, C.c_uint32) for n in ("orientation", "num_extra")]
 
 
 class Codestream:
@@ -567,8 +568,8 @@ class Codestream:
         return buf
 
     def extra(self, index: int) -> np.ndarray:
-        """A VarDCT frame's extra channel (alpha, ...) normalised to its bit
-        depth, float32 [H, W]."""
+        """A frame's extra channel (alpha, ...) normalised to its bit depth,
+        float32 [H, W]."""
         out = np.zeros((self.info["height"], self.info["width"]), np.float32)
         rc = self.lib.jpxlg_codestream_extra(self.handle, index, out.ctypes.data)
         if rc:

@@ -964,11 +964,26 @@ void inverse_transforms(std::vector<Channel>& ch, const std::vector<ModTransform
   }
 }
 
+// What a GlobalModular stream that stopped at a channel larger than a group
+// leaves for the group sections: its transforms (undone once every group is
+// in), the weighted-predictor header they use, and the channel indices.
+struct Deferred {
+  std::vector<ModTransform> transforms;
+  WpHeader wp;
+  size_t nb_meta = 0, first_undecoded = 0;
+};
+
 // H.2-H.4: one modular sub-bitstream over `ch` (shapes set by the caller),
-// transforms undone at the end.
+// transforms undone at the end.  With `defer`, decoding stops at the first
+// non-meta channel wider or taller than group_dim (G.1.3; modular/mod.rs:649)
+// and the transforms are handed back instead of undone.
 void modular_stream(Reader& r, std::vector<Channel>& ch, uint32_t stream_index,
-                    const GlobalTree& gt, uint32_t bits = 8) {
-  if (ch.empty()) return;
+                    const GlobalTree& gt, uint32_t bits = 8, uint32_t group_dim = 0,
+                    Deferred* defer = nullptr) {
+  if (ch.empty()) {
+    if (defer) *defer = Deferred{};
+    return;
+  }
   const bool use_global = r.flag();
   const WpHeader wp = read_wp(r);
   static const U32Dist kNbTransforms[4] = {{0, 0}, {0, 1}, {4, 2}, {8, 18}};
@@ -989,6 +1004,11 @@ void modular_stream(Reader& r, std::vector<Channel>& ch, uint32_t stream_index,
     }
   }
   for (Channel& c : ch) c.v.assign((size_t)c.w * c.h, 0);
+  size_t end = ch.size();
+  if (defer) {
+    end = std::min(nb_meta, ch.size());
+    while (end < ch.size() && ch[end].w <= group_dim && ch[end].h <= group_dim) ++end;
+  }
   Tree local;
   std::unique_ptr<Stream> owned(new Stream);
   const Tree* tree;
@@ -1004,10 +1024,10 @@ void modular_stream(Reader& r, std::vector<Channel>& ch, uint32_t stream_index,
   }
   Stream& s = *owned;
   uint32_t dist_mult = 0;
-  for (const Channel& c : ch)
-    if (c.w && c.h) dist_mult = std::max(dist_mult, c.w);
+  for (size_t i = 0; i < end; ++i)
+    if (ch[i].w && ch[i].h) dist_mult = std::max(dist_mult, ch[i].w);
   s.dist_multiplier = dist_mult;
-  for (size_t i = 0; i < ch.size(); ++i) {
+  for (size_t i = 0; i < end; ++i) {
     Channel& cur = ch[i];
     if (!cur.w || !cur.h) continue;
     std::vector<size_t> prev;
@@ -1067,6 +1087,13 @@ void modular_stream(Reader& r, std::vector<Channel>& ch, uint32_t stream_index,
     }
   }
   need(s.final_state(), "modular stream final state");
+  if (defer) {
+    defer->transforms = std::move(transforms);
+    defer->wp = wp;
+    defer->nb_meta = nb_meta;
+    defer->first_undecoded = end;
+    return;
+  }
   inverse_transforms(ch, transforms, bits, wp);
 }
 
@@ -1500,11 +1527,85 @@ void decode_frame_vardct(std::vector<Section>& sec, bool single, Decoded* out) {
   });
 }
 
+// The channel pieces of one LF group (G.2.3) or pass group (G.4.2), rect in
+// frame samples: one sub-bitstream over the selected channels' pieces, the
+// origin shifted exactly and the extent rounded up (decode.rs:2159), then
+// copied back into the frame's channels.
+void decode_group_channels(Reader& r, std::vector<Channel>& ch, const std::vector<size_t>& sel,
+                           uint32_t x0, uint32_t y0, uint32_t w, uint32_t h,
+                           uint32_t stream_index, const GlobalTree& gt) {
+  if (sel.empty()) return;
+  std::vector<Channel> piece;
+  std::vector<std::pair<uint32_t, uint32_t>> origin;
+  for (size_t i : sel) {
+    const Channel& c = ch[i];
+    const uint32_t hs = (uint32_t)std::max(c.hshift, 0), vs = (uint32_t)std::max(c.vshift, 0);
+    const uint32_t px = x0 >> hs, py = y0 >> vs;
+    const uint32_t ex = (uint32_t)(((uint64_t)x0 + w + (1ull << hs) - 1) >> hs);
+    const uint32_t ey = (uint32_t)(((uint64_t)y0 + h + (1ull << vs) - 1) >> vs);
+    Channel p;
+    p.w = std::min(ex > px ? ex - px : 0u, c.w > px ? c.w - px : 0u);
+    p.h = std::min(ey > py ? ey - py : 0u, c.h > py ? c.h - py : 0u);
+    p.hshift = c.hshift;
+    p.vshift = c.vshift;
+    piece.push_back(std::move(p));
+    origin.emplace_back(px, py);
+  }
+  modular_stream(r, piece, stream_index, gt);
+  for (size_t k = 0; k < sel.size(); ++k) {
+    Channel& dst = ch[sel[k]];
+    const Channel& src = piece[k];
+    need(src.w == 0 || (origin[k].first + src.w <= dst.w && origin[k].second + src.h <= dst.h),
+         "group piece outside its channel");
+    for (uint32_t y = 0; y < src.h; ++y)
+      for (uint32_t x = 0; x < src.w; ++x)
+        dst.at(origin[k].first + x, origin[k].second + y) = src.at(x, y);
+  }
+}
+
+// G.2.3 and G.4.2 for the channels GlobalModular left undecoded, then the
+// deferred transforms.  lf_section(lg) and group_section(g) give the readers
+// positioned at each section's modular data; one pass, frame of W x H.
+template <class LfSec, class GroupSec>
+void decode_modular_groups(std::vector<Channel>& ch, Deferred& d, uint32_t W, uint32_t H,
+                           uint32_t gdim, const GlobalTree& gt, uint32_t bits,
+                           LfSec lf_section, GroupSec group_section) {
+  if (d.first_undecoded < ch.size()) {
+    const uint32_t lfdim = 8 * gdim;
+    const uint32_t gx = (W + gdim - 1) / gdim, gy = (H + gdim - 1) / gdim;
+    const uint32_t lgx = (W + lfdim - 1) / lfdim, lgy = (H + lfdim - 1) / lfdim;
+    const uint64_t num_lf = (uint64_t)lgx * lgy, num_groups = (uint64_t)gx * gy;
+    std::vector<size_t> lf_sel, pass_sel;
+    for (size_t i = d.first_undecoded; i < ch.size(); ++i) {
+      const Channel& c = ch[i];
+      if (c.hshift >= 3 && c.vshift >= 3) {
+        lf_sel.push_back(i);
+        continue;
+      }
+      if (i < d.nb_meta) continue;
+      const uint32_t hs = (uint32_t)std::min(std::max(c.hshift, 0), 31);
+      const uint32_t vs = (uint32_t)std::min(std::max(c.vshift, 0), 31);
+      if (c.w <= (gdim >> hs) && c.h <= (gdim >> vs)) continue;  // decode.rs:352
+      if (std::min(c.hshift, c.vshift) < 3) pass_sel.push_back(i);
+    }
+    for (uint64_t lg = 0; lg < num_lf; ++lg) {
+      const uint32_t x0 = (uint32_t)(lg % lgx) * lfdim, y0 = (uint32_t)(lg / lgx) * lfdim;
+      decode_group_channels(lf_section(lg), ch, lf_sel, x0, y0, std::min(lfdim, W - x0),
+                            std::min(lfdim, H - y0), (uint32_t)(1 + num_lf + lg), gt);
+    }
+    for (uint64_t g = 0; g < num_groups; ++g) {
+      const uint32_t x0 = (uint32_t)(g % gx) * gdim, y0 = (uint32_t)(g / gx) * gdim;
+      decode_group_channels(group_section(g), ch, pass_sel, x0, y0, std::min(gdim, W - x0),
+                            std::min(gdim, H - y0), (uint32_t)(1 + 3 * num_lf + 17 + g), gt);
+    }
+  }
+  inverse_transforms(ch, d.transforms, bits, d.wp);
+}
+
 void decode_frame_modular(std::vector<Section>& sec, Decoded* out, float m_lf[3] = nullptr) {
   const ImageInfo& img = out->image;
   const FrameInfo& fr = out->frame;
   need((fr.flags & (2 | 16 | 32)) == 0, "patches, splines and LF frames are not supported");
-  need(img.num_extra == 0, "extra channels are not supported");
   Reader& g = sec[0].r;
   if (!g.flag()) {
     for (int c = 0; c < 3; ++c) {
@@ -1515,11 +1616,28 @@ void decode_frame_modular(std::vector<Section>& sec, Decoded* out, float m_lf[3]
   const GlobalTree gt = read_global_tree(g);
   const uint32_t n = (img.xyb_encoded || img.colour_space != 1) ? 3 : 1;
   const uint32_t gdim = 128u << fr.group_size_shift;
-  need(fr.width <= gdim && fr.height <= gdim,
-       "modular frames larger than one group are not supported");
+  need(fr.num_passes == 1 || (fr.width <= gdim && fr.height <= gdim),
+       "modular frames of several passes and groups are not supported");
   out->modular.clear();
   for (uint32_t c = 0; c < n; ++c) out->modular.push_back(make_channel(fr.width, fr.height));
-  modular_stream(g, out->modular, 0, gt, img.bits_per_sample);
+  // The extra channels follow the colour channels in the one channel list
+  // of GlobalModular (G.1.3; decode.rs:1226 initial_channels); they are handed out apart.
+  for (const ImageInfo::Extra& e : img.extra) {
+    const uint32_t sh = e.dim_shift;
+    need(sh == 0, "extra channels with a dim_shift are not supported");
+    out->modular.push_back(make_channel(fr.width, fr.height));
+  }
+  Deferred d;
+  modular_stream(g, out->modular, 0, gt, img.bits_per_sample, gdim, &d);
+  const bool single = sec.size() == 1;
+  const uint64_t num_lf = (uint64_t)((fr.width + 8 * gdim - 1) / (8 * gdim)) *
+                          ((fr.height + 8 * gdim - 1) / (8 * gdim));
+  decode_modular_groups(
+      out->modular, d, fr.width, fr.height, gdim, gt, img.bits_per_sample,
+      [&](uint64_t lg) -> Reader& { return single ? sec[0].r : sec[1 + lg].r; },
+      [&](uint64_t gi) -> Reader& { return single ? sec[0].r : sec[2 + num_lf + gi].r; });
+  out->extra.assign(out->modular.begin() + n, out->modular.end());
+  out->modular.resize(n);
 }
 
 // F.3 TOC (toc.rs:127) of frame f, read at r: the frame's sections, and the
@@ -1772,6 +1890,8 @@ extern "C" int jpxlg_codestream_info(const jpxlg_codestream* cs, jpxlg_codestrea
     if ((d.section_bits[i] + 7) / 8 == d.section_sizes[i]) ++exact;
   info->sections_exact = exact;
   for (int i = 0; i < 27; ++i) info->transform_counts[i] = d.vardct.histogram_counts[i];
+  info->orientation = d.image.orientation;
+  info->num_extra = (uint32_t)d.image.extra.size();
   return JPXLG_OK;
 }
 
@@ -1815,14 +1935,16 @@ extern "C" int jpxlg_codestream_coefficients(const jpxlg_codestream* cs, int32_t
 }
 
 extern "C" int jpxlg_codestream_channel(const jpxlg_codestream* cs, uint32_t index, int32_t* out) {
-  if (!cs || !out || index >= cs->d.modular.size()) return JPXLG_ERR_ARGUMENT;
-  const jpxlg::cs::Channel& c = cs->d.modular[index];
+  const size_t nm = cs ? cs->d.modular.size() : 0;
+  if (!cs || !out || index >= nm + (cs->d.frame.encoding == 1 ? cs->d.extra.size() : 0))
+    return JPXLG_ERR_ARGUMENT;
+  const jpxlg::cs::Channel& c = index < nm ? cs->d.modular[index] : cs->d.extra[index - nm];
   std::memcpy(out, c.v.data(), c.v.size() * sizeof(int32_t));
   return JPXLG_OK;
 }
 
-// A VarDCT frame's extra channel as floats (sample / (2^bits - 1)), its
-// width x height.
+// A frame's extra channel as floats (sample / (2^bits - 1)), its width x
+// height.
 extern "C" int jpxlg_codestream_extra(const jpxlg_codestream* cs, uint32_t index, float* out) {
   if (!cs || !out || index >= cs->d.extra.size() || index >= cs->d.image.extra.size())
     return JPXLG_ERR_ARGUMENT;

@@ -7,7 +7,7 @@ not present where the tests run; the copied files are the committed fixture):
 
     python tests/golden/make_codestream_golden.py
 
-Source: JPXL/tests/fixtures/handmade/{03,04,06,07,09,11,40,50..53,60,63,64,70..73,82,110}_*.jxl with the .npy decodes
+Source: JPXL/tests/fixtures/handmade/{03..07,09,11,12,14..16,21,40,50..53,60,63,64,70..73,80..82,100..107,109,110}_*.jxl with the .npy decodes
 committed beside them (djxl v0.13.0 196a43d9 --output_format npy; provenance
 in each fixture's .jxl.txt sidecar; 64 and the lossless fixtures have none).
 110 (photon noise) is the stream the reader reports as unsupported.
@@ -28,6 +28,23 @@ NAMES = ["03_gradient_8x8_lossless",
          "73_progressive_all_gray_128x128_nofilters",
          "82_alpha_vardct_rgba_64x64_nofilters",
          "110_noise_rgb_32x32",
+         "80_alpha_rgba_8x8_lossless",
+         "81_alpha_rgba_600x520_lossless",
+         "05_gradient_300x200_lossless",
+         "12_modular_gray_300x200_lossless",
+         "21_gradient_260x10_lossless",
+         "14_modular_gray_600x520_multisection_lossless",
+         "15_modular_rgb_600x520_multisection_lossless",
+         "16_modular_gray_511x8_multisection_lossless",
+         "100_orientation_identity_rgba_24x16",
+         "101_orientation_flip_h_rgba_24x16",
+         "102_orientation_rot180_rgba_24x16",
+         "103_orientation_flip_v_rgba_24x16",
+         "104_orientation_transpose_rgba_24x16",
+         "105_orientation_rot90cw_rgba_24x16",
+         "106_orientation_antitranspose_rgba_24x16",
+         "107_orientation_rot90ccw_rgba_24x16",
+         "109_orientation_transpose_vardct_rgba_64x64",
          "06_gradient_300x200_lossy",
          "07_modular_gray_8x8_lossless",
          "09_modular_rgb_64x64_lossless",

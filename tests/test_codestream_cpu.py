@@ -27,7 +27,7 @@ def load(name):
 
 
 def test_fixtures_present():
-    assert len(VARDCT) == 7, VARDCT
+    assert len(VARDCT) == 8, VARDCT
     assert len(PROGRESSIVE) == 3, PROGRESSIVE
 
 
@@ -63,7 +63,7 @@ def test_vardct_fixture_decodes_with_every_section_exact(name):
     assert i["encoding"] == 0
     assert i["sections"] >= 1
     assert i["sections_exact"] == i["sections"], "a section ended away from its TOC size"
-    side = 64 if name.startswith(("63_", "82_")) else 128
+    side = 64 if name.startswith(("63_", "82_", "109_")) else 128
     if name.startswith("64_"):
         assert (i["width"], i["height"]) == (128, 2176)
         return
@@ -168,6 +168,17 @@ def test_unsupported_feature_is_reported_not_misdecoded():
     ("03_gradient_8x8_lossless", 8, 8, lambda x, y: [x * 255 // 7, y * 255 // 7, (x + y) % 256]),
     ("09_modular_rgb_64x64_lossless", 64, 64,
      lambda x, y: [x * 255 // 63, y * 255 // 63, (x + y) % 256]),
+    ("05_gradient_300x200_lossless", 300, 200,
+     lambda x, y: [x * 255 // 299, y * 255 // 199, (x + y) % 256]),
+    ("12_modular_gray_300x200_lossless", 300, 200, lambda x, y: [(x + y) * 255 // 498]),
+    ("21_gradient_260x10_lossless", 260, 10,
+     lambda x, y: [x * 255 // 259, y * 255 // 9, (x + y) % 256]),
+    # several groups: G.2.3 / G.4.2 channel pieces in their own sections
+    ("14_modular_gray_600x520_multisection_lossless", 600, 520,
+     lambda x, y: [(x + y) * 255 // 1118]),
+    ("15_modular_rgb_600x520_multisection_lossless", 600, 520,
+     lambda x, y: [x * 255 // 599, y * 255 // 519, (x + y) % 256]),
+    ("16_modular_gray_511x8_multisection_lossless", 511, 8, lambda x, y: [(x + y) * 255 // 517]),
 ])
 def test_lossless_modular_frames_match_their_generators(name, w, h, gen):
     """Lossless modular frames (MA trees, the H.5 predictor, RCT, squeeze and
@@ -175,6 +186,7 @@ def test_lossless_modular_frames_match_their_generators(name, w, h, gen):
     states."""
     cs = load(name)
     assert cs.info["encoding"] == 1 and (cs.info["width"], cs.info["height"]) == (w, h)
+    assert cs.info["sections_exact"] == cs.info["sections"]
     y, x = np.mgrid[0:h, 0:w]
     want = gen(x, y)
     assert cs.info["num_channels"] == len(want)
@@ -266,3 +278,46 @@ def test_alpha_of_a_vardct_frame():
     cs = load(name)
     ref = np.load(GOLDEN / (name + ".npy"))[0, :, :, 3]
     assert np.abs(cs.extra(0) - ref).max() < 1e-6
+
+
+# Exif orientations 1-8 as the display transform of an [H, W, C] image
+# (Table A.6 of 18181-1; djxl applies it, the reader reports it).
+ORIENT = {1: lambda a: a, 2: lambda a: a[:, ::-1], 3: lambda a: a[::-1, ::-1],
+          4: lambda a: a[::-1], 5: lambda a: a.transpose(1, 0, 2),
+          6: lambda a: np.rot90(a, -1), 7: lambda a: a[::-1, ::-1].transpose(1, 0, 2),
+          8: lambda a: np.rot90(a, 1)}
+MODULAR_RGBA = ["80_alpha_rgba_8x8_lossless"] + sorted(
+    p.stem for p in GOLDEN.glob("10[0-7]_orientation_*.jxl"))
+
+
+@pytest.mark.parametrize("name", MODULAR_RGBA)
+def test_modular_rgba_matches_djxl(name):
+    """Lossless modular RGBA frames: the alpha channel follows the colour
+    channels in the frame's channel list; after the stream's orientation the
+    integers equal djxl's decode (f32 round trip only)."""
+    cs = load(name)
+    i = cs.info
+    assert i["num_extra"] == 1 and i["num_channels"] == 4
+    rgba = np.stack([cs.channel(k) for k in range(4)], -1).astype(np.float32) / 255.0
+    assert np.array_equal(cs.extra(0), rgba[:, :, 3])
+    assert rgba[:, :, 3].min() < rgba[:, :, 3].max()
+    ref = np.load(GOLDEN / (name + ".npy"))[0]
+    got = ORIENT[i["orientation"]](rgba)
+    assert got.shape == ref.shape
+    assert np.abs(got - ref).max() < 1e-6
+
+
+def test_orientation_fixtures_cover_all_eight():
+    assert sorted(load(n).info["orientation"] for n in MODULAR_RGBA[1:]) == list(range(1, 9))
+
+
+def test_multigroup_rgba_decodes_every_section_exactly():
+    """81_alpha_rgba_600x520_lossless: 3x3 groups of 256 with an alpha channel
+    among the group pieces; twelve sections, each read to its TOC size, and
+    an alpha plane that is not constant."""
+    cs = load("81_alpha_rgba_600x520_lossless")
+    i = cs.info
+    assert (i["sections"], i["sections_exact"], i["num_channels"]) == (12, 12, 4)
+    a = cs.channel(3)
+    assert a.shape == (520, 600) and a.min() < a.max()
+    assert np.array_equal(cs.extra(0), a.astype(np.float32) / 255.0)
