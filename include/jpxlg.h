@@ -294,9 +294,8 @@ int jpxlg_symbols_destroy(jpxlg_symbols* s);
  * fragments) with one regular frame, optionally after a modular LF frame
  * (kUseLfFrame); modular transforms RCT, squeeze and palette; modular
  * frames of several groups (one pass) with extra channels; a VarDCT frame's
- * extra channels up to one group.  ICC profiles, previews, patches, splines,
- * noise, upsampling and larger VarDCT extra channels are reported as
- * unsupported (JPXLG_ERR_STREAM with a reason in
+ * extra channels.  ICC profiles, previews, patches, splines, noise and
+ * upsampling are reported as unsupported (JPXLG_ERR_STREAM with a reason in
  * jpxlg_codestream_last_error).  Host code only: no device is needed.
  *   jpxlg_codestream_open          parse and decode; *out owns the result
  *   jpxlg_codestream_info          sizes, frame parameters, per-DctSelect

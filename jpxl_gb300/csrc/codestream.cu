@@ -1269,6 +1269,86 @@ const uint8_t kCoeffNzCtx[64] = {0,   0,   31,  62,  62,  93,  93,  93,  93,  12
                                  206, 206, 206, 206, 206, 206, 206, 206, 206, 206, 206, 206};
 constexpr uint32_t kNonZeroCtx = 37, kCoeffCtx = 458, kCtxPerBlock = kNonZeroCtx + kCoeffCtx;
 
+// The channel pieces of one LF group (G.2.3) or pass group (G.4.2), rect in
+// frame samples: one sub-bitstream over the selected channels' pieces, the
+// origin shifted exactly and the extent rounded up (decode.rs:2159), then
+// copied back into the frame's channels.
+void decode_group_channels(Reader& r, std::vector<Channel>& ch, const std::vector<size_t>& sel,
+                           uint32_t x0, uint32_t y0, uint32_t w, uint32_t h,
+                           uint32_t stream_index, const GlobalTree& gt) {
+  if (sel.empty()) return;
+  std::vector<Channel> piece;
+  std::vector<std::pair<uint32_t, uint32_t>> origin;
+  for (size_t i : sel) {
+    const Channel& c = ch[i];
+    const uint32_t hs = (uint32_t)std::max(c.hshift, 0), vs = (uint32_t)std::max(c.vshift, 0);
+    const uint32_t px = x0 >> hs, py = y0 >> vs;
+    const uint32_t ex = (uint32_t)(((uint64_t)x0 + w + (1ull << hs) - 1) >> hs);
+    const uint32_t ey = (uint32_t)(((uint64_t)y0 + h + (1ull << vs) - 1) >> vs);
+    Channel p;
+    p.w = std::min(ex > px ? ex - px : 0u, c.w > px ? c.w - px : 0u);
+    p.h = std::min(ey > py ? ey - py : 0u, c.h > py ? c.h - py : 0u);
+    p.hshift = c.hshift;
+    p.vshift = c.vshift;
+    piece.push_back(std::move(p));
+    origin.emplace_back(px, py);
+  }
+  modular_stream(r, piece, stream_index, gt);
+  for (size_t k = 0; k < sel.size(); ++k) {
+    Channel& dst = ch[sel[k]];
+    const Channel& src = piece[k];
+    need(src.w == 0 || (origin[k].first + src.w <= dst.w && origin[k].second + src.h <= dst.h),
+         "group piece outside its channel");
+    for (uint32_t y = 0; y < src.h; ++y)
+      for (uint32_t x = 0; x < src.w; ++x)
+        dst.at(origin[k].first + x, origin[k].second + y) = src.at(x, y);
+  }
+}
+
+// G.2.3 and G.4.2 for the channels GlobalModular left undecoded: the
+// selections once, then each LF group's and pass group's pieces as their
+// sections reach the modular data, then the deferred transforms.  One pass.
+struct ModularGroups {
+  std::vector<Channel>& ch;
+  Deferred& d;
+  const GlobalTree& gt;
+  uint32_t W, H, gdim, lfdim, gx, lgx;
+  uint64_t num_lf;
+  std::vector<size_t> lf_sel, pass_sel;
+
+  ModularGroups(std::vector<Channel>& ch_, Deferred& d_, const GlobalTree& gt_, uint32_t W_,
+                uint32_t H_, uint32_t gdim_)
+      : ch(ch_), d(d_), gt(gt_), W(W_), H(H_), gdim(gdim_), lfdim(8 * gdim_) {
+    gx = (W + gdim - 1) / gdim;
+    lgx = (W + lfdim - 1) / lfdim;
+    num_lf = (uint64_t)lgx * ((H + lfdim - 1) / lfdim);
+    for (size_t i = d.first_undecoded; i < ch.size(); ++i) {
+      const Channel& c = ch[i];
+      if (c.hshift >= 3 && c.vshift >= 3) {
+        lf_sel.push_back(i);
+        continue;
+      }
+      if (i < d.nb_meta) continue;
+      const uint32_t hs = (uint32_t)std::min(std::max(c.hshift, 0), 31);
+      const uint32_t vs = (uint32_t)std::min(std::max(c.vshift, 0), 31);
+      if (c.w <= (gdim >> hs) && c.h <= (gdim >> vs)) continue;  // decode.rs:352
+      if (std::min(c.hshift, c.vshift) < 3) pass_sel.push_back(i);
+    }
+  }
+  bool any() const { return !lf_sel.empty() || !pass_sel.empty(); }
+  void lf_group(uint64_t lg, Reader& r) {
+    const uint32_t x0 = (uint32_t)(lg % lgx) * lfdim, y0 = (uint32_t)(lg / lgx) * lfdim;
+    decode_group_channels(r, ch, lf_sel, x0, y0, std::min(lfdim, W - x0),
+                          std::min(lfdim, H - y0), (uint32_t)(1 + num_lf + lg), gt);
+  }
+  void pass_group(uint64_t g, Reader& r) {
+    const uint32_t x0 = (uint32_t)(g % gx) * gdim, y0 = (uint32_t)(g / gx) * gdim;
+    decode_group_channels(r, ch, pass_sel, x0, y0, std::min(gdim, W - x0),
+                          std::min(gdim, H - y0), (uint32_t)(1 + 3 * num_lf + 17 + g), gt);
+  }
+  void finish(uint32_t bits) { inverse_transforms(ch, d.transforms, bits, d.wp); }
+};
+
 struct Section {
   Reader r;
   uint64_t start_bits, size_bytes;
@@ -1324,12 +1404,16 @@ void decode_frame_vardct(std::vector<Section>& sec, bool single, Decoded* out) {
   // those no larger than a group are decoded here (decode.rs:2589).
   out->extra.clear();
   for (const ImageInfo::Extra& e : img.extra) {
-    const uint32_t sh = e.dim_shift;
-    out->extra.push_back(make_channel((W + (1u << sh) - 1) >> sh, (H + (1u << sh) - 1) >> sh));
-    need(out->extra.back().w <= gdim && out->extra.back().h <= gdim,
-         "extra channels larger than a group are not supported");
+    need(e.dim_shift == 0, "extra channels with a dim_shift are not supported");
+    out->extra.push_back(make_channel(W, H));
   }
-  modular_stream(g, out->extra, 0, gt, img.bits_per_sample);
+  // Channels larger than a group continue in the LF groups (after the LF
+  // coefficients) and the pass groups (after the HF coefficients).
+  Deferred ed;
+  modular_stream(g, out->extra, 0, gt, img.bits_per_sample, gdim, &ed);
+  ModularGroups mg(out->extra, ed, gt, W, H, gdim);
+  need(!mg.any() || fr.num_passes == 1,
+       "extra channels larger than a group in several passes are not supported");
 
   // LF groups (G.2; decode.rs:2625-2700).
   std::vector<std::vector<Varblock>> placements(num_lf);
@@ -1351,6 +1435,7 @@ void decode_frame_vardct(std::vector<Section>& sec, bool single, Decoded* out) {
           for (uint32_t x = 0; x < bw; ++x)
             vd.lf[plane_of[k]][(size_t)(by0 + y) * vd.bw + bx0 + x] = lfch[k].at(x, y);
     }
+    mg.lf_group(lg, r);  // ModularLfGroup (G.2.3)
     // HF metadata (G.2.4; hf_meta.rs:111).
     const uint32_t nb = 1 + r.bits(ceil_log2((uint64_t)bw * bh));
     const uint32_t cw = (gw + 63) / 64, chh = (gh + 63) / 64;
@@ -1517,89 +1602,16 @@ void decode_frame_vardct(std::vector<Section>& sec, bool single, Decoded* out) {
         }
       }
       need(s.final_state(), "HF final state");
+      mg.pass_group(grp, r);  // ModularGroup (G.4.2)
     }
   }
+  mg.finish(img.bits_per_sample);
   // Varblocks in raster order of their origins.
   for (auto& lgp : placements)
     for (const Varblock& v : lgp) vd.varblocks.push_back(v);
   std::sort(vd.varblocks.begin(), vd.varblocks.end(), [](const Varblock& a, const Varblock& b) {
     return a.by != b.by ? a.by < b.by : a.bx < b.bx;
   });
-}
-
-// The channel pieces of one LF group (G.2.3) or pass group (G.4.2), rect in
-// frame samples: one sub-bitstream over the selected channels' pieces, the
-// origin shifted exactly and the extent rounded up (decode.rs:2159), then
-// copied back into the frame's channels.
-void decode_group_channels(Reader& r, std::vector<Channel>& ch, const std::vector<size_t>& sel,
-                           uint32_t x0, uint32_t y0, uint32_t w, uint32_t h,
-                           uint32_t stream_index, const GlobalTree& gt) {
-  if (sel.empty()) return;
-  std::vector<Channel> piece;
-  std::vector<std::pair<uint32_t, uint32_t>> origin;
-  for (size_t i : sel) {
-    const Channel& c = ch[i];
-    const uint32_t hs = (uint32_t)std::max(c.hshift, 0), vs = (uint32_t)std::max(c.vshift, 0);
-    const uint32_t px = x0 >> hs, py = y0 >> vs;
-    const uint32_t ex = (uint32_t)(((uint64_t)x0 + w + (1ull << hs) - 1) >> hs);
-    const uint32_t ey = (uint32_t)(((uint64_t)y0 + h + (1ull << vs) - 1) >> vs);
-    Channel p;
-    p.w = std::min(ex > px ? ex - px : 0u, c.w > px ? c.w - px : 0u);
-    p.h = std::min(ey > py ? ey - py : 0u, c.h > py ? c.h - py : 0u);
-    p.hshift = c.hshift;
-    p.vshift = c.vshift;
-    piece.push_back(std::move(p));
-    origin.emplace_back(px, py);
-  }
-  modular_stream(r, piece, stream_index, gt);
-  for (size_t k = 0; k < sel.size(); ++k) {
-    Channel& dst = ch[sel[k]];
-    const Channel& src = piece[k];
-    need(src.w == 0 || (origin[k].first + src.w <= dst.w && origin[k].second + src.h <= dst.h),
-         "group piece outside its channel");
-    for (uint32_t y = 0; y < src.h; ++y)
-      for (uint32_t x = 0; x < src.w; ++x)
-        dst.at(origin[k].first + x, origin[k].second + y) = src.at(x, y);
-  }
-}
-
-// G.2.3 and G.4.2 for the channels GlobalModular left undecoded, then the
-// deferred transforms.  lf_section(lg) and group_section(g) give the readers
-// positioned at each section's modular data; one pass, frame of W x H.
-template <class LfSec, class GroupSec>
-void decode_modular_groups(std::vector<Channel>& ch, Deferred& d, uint32_t W, uint32_t H,
-                           uint32_t gdim, const GlobalTree& gt, uint32_t bits,
-                           LfSec lf_section, GroupSec group_section) {
-  if (d.first_undecoded < ch.size()) {
-    const uint32_t lfdim = 8 * gdim;
-    const uint32_t gx = (W + gdim - 1) / gdim, gy = (H + gdim - 1) / gdim;
-    const uint32_t lgx = (W + lfdim - 1) / lfdim, lgy = (H + lfdim - 1) / lfdim;
-    const uint64_t num_lf = (uint64_t)lgx * lgy, num_groups = (uint64_t)gx * gy;
-    std::vector<size_t> lf_sel, pass_sel;
-    for (size_t i = d.first_undecoded; i < ch.size(); ++i) {
-      const Channel& c = ch[i];
-      if (c.hshift >= 3 && c.vshift >= 3) {
-        lf_sel.push_back(i);
-        continue;
-      }
-      if (i < d.nb_meta) continue;
-      const uint32_t hs = (uint32_t)std::min(std::max(c.hshift, 0), 31);
-      const uint32_t vs = (uint32_t)std::min(std::max(c.vshift, 0), 31);
-      if (c.w <= (gdim >> hs) && c.h <= (gdim >> vs)) continue;  // decode.rs:352
-      if (std::min(c.hshift, c.vshift) < 3) pass_sel.push_back(i);
-    }
-    for (uint64_t lg = 0; lg < num_lf; ++lg) {
-      const uint32_t x0 = (uint32_t)(lg % lgx) * lfdim, y0 = (uint32_t)(lg / lgx) * lfdim;
-      decode_group_channels(lf_section(lg), ch, lf_sel, x0, y0, std::min(lfdim, W - x0),
-                            std::min(lfdim, H - y0), (uint32_t)(1 + num_lf + lg), gt);
-    }
-    for (uint64_t g = 0; g < num_groups; ++g) {
-      const uint32_t x0 = (uint32_t)(g % gx) * gdim, y0 = (uint32_t)(g / gx) * gdim;
-      decode_group_channels(group_section(g), ch, pass_sel, x0, y0, std::min(gdim, W - x0),
-                            std::min(gdim, H - y0), (uint32_t)(1 + 3 * num_lf + 17 + g), gt);
-    }
-  }
-  inverse_transforms(ch, d.transforms, bits, d.wp);
 }
 
 void decode_frame_modular(std::vector<Section>& sec, Decoded* out, float m_lf[3] = nullptr) {
@@ -1630,12 +1642,14 @@ void decode_frame_modular(std::vector<Section>& sec, Decoded* out, float m_lf[3]
   Deferred d;
   modular_stream(g, out->modular, 0, gt, img.bits_per_sample, gdim, &d);
   const bool single = sec.size() == 1;
-  const uint64_t num_lf = (uint64_t)((fr.width + 8 * gdim - 1) / (8 * gdim)) *
-                          ((fr.height + 8 * gdim - 1) / (8 * gdim));
-  decode_modular_groups(
-      out->modular, d, fr.width, fr.height, gdim, gt, img.bits_per_sample,
-      [&](uint64_t lg) -> Reader& { return single ? sec[0].r : sec[1 + lg].r; },
-      [&](uint64_t gi) -> Reader& { return single ? sec[0].r : sec[2 + num_lf + gi].r; });
+  ModularGroups mg(out->modular, d, gt, fr.width, fr.height, gdim);
+  if (mg.any()) {
+    const uint64_t num_groups = (uint64_t)mg.gx * ((fr.height + gdim - 1) / gdim);
+    for (uint64_t lg = 0; lg < mg.num_lf; ++lg) mg.lf_group(lg, single ? sec[0].r : sec[1 + lg].r);
+    for (uint64_t gi = 0; gi < num_groups; ++gi)
+      mg.pass_group(gi, single ? sec[0].r : sec[2 + mg.num_lf + gi].r);
+  }
+  mg.finish(img.bits_per_sample);
   out->extra.assign(out->modular.begin() + n, out->modular.end());
   out->modular.resize(n);
 }

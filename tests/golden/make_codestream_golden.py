@@ -7,7 +7,7 @@ not present where the tests run; the copied files are the committed fixture):
 
     python tests/golden/make_codestream_golden.py
 
-Source: JPXL/tests/fixtures/handmade/{03..07,09,11,12,14..16,21,40,50..53,60,63,64,70..73,80..82,100..107,109,110}_*.jxl with the .npy decodes
+Source: JPXL/tests/fixtures/handmade/{03..07,09,11,12,14..16,21,40,50..53,60,63,64,70..73,80..84,100..107,109,110}_*.jxl with the .npy decodes
 committed beside them (djxl v0.13.0 196a43d9 --output_format npy; provenance
 in each fixture's .jxl.txt sidecar; 64 and the lossless fixtures have none).
 110 (photon noise) is the stream the reader reports as unsupported.
@@ -27,6 +27,8 @@ NAMES = ["03_gradient_8x8_lossless",
          "72_lfframe_gray_128x128_nofilters",
          "73_progressive_all_gray_128x128_nofilters",
          "82_alpha_vardct_rgba_64x64_nofilters",
+         "83_alpha_vardct_rgba_384x320_nofilters",
+         "84_alpha_vardct_ga_128x128_nofilters",
          "110_noise_rgb_32x32",
          "80_alpha_rgba_8x8_lossless",
          "81_alpha_rgba_600x520_lossless",

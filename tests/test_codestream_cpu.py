@@ -27,7 +27,7 @@ def load(name):
 
 
 def test_fixtures_present():
-    assert len(VARDCT) == 8, VARDCT
+    assert len(VARDCT) == 10, VARDCT
     assert len(PROGRESSIVE) == 3, PROGRESSIVE
 
 
@@ -66,6 +66,9 @@ def test_vardct_fixture_decodes_with_every_section_exact(name):
     side = 64 if name.startswith(("63_", "82_", "109_")) else 128
     if name.startswith("64_"):
         assert (i["width"], i["height"]) == (128, 2176)
+        return
+    if name.startswith("83_"):
+        assert (i["width"], i["height"]) == (384, 320)
         return
     assert (i["width"], i["height"]) == (side, side)
     assert i["colour_space"] == (0 if ("_rgb_" in name or "_rgba_" in name) else 1)
@@ -321,3 +324,18 @@ def test_multigroup_rgba_decodes_every_section_exactly():
     a = cs.channel(3)
     assert a.shape == (520, 600) and a.min() < a.max()
     assert np.array_equal(cs.extra(0), a.astype(np.float32) / 255.0)
+
+
+def test_vardct_alpha_over_several_groups():
+    """83_alpha_vardct_rgba_384x320_nofilters: an alpha channel larger than a
+    group, decoded in the pass groups after each group's HF coefficients
+    (G.4.2), so a wrong split desynchronises the colour, not just the alpha:
+    all seven sections end at their TOC sizes, and the alpha (a radial ramp
+    with a transparent notch) is continuous across the group seams."""
+    cs = load("83_alpha_vardct_rgba_384x320_nofilters")
+    i = cs.info
+    assert (i["sections"], i["sections_exact"], i["num_extra"]) == (7, 7, 1)
+    a = np.round(cs.extra(0) * 255).astype(np.int32)
+    assert a.min() == 0 and a.max() > 250
+    dx, dy = np.abs(np.diff(a, axis=1)), np.abs(np.diff(a, axis=0))
+    assert dx[:, 255].max() <= 4 and dy[255].max() <= 4
