@@ -50,7 +50,8 @@
  *               bits 0..4 the Table I.1 DctSelect (0 DCT8, 4 DCT16,
  *               5 DCT32, 6 DCT16x8, 7 DCT8x16, 8 DCT32x8, 9 DCT8x32,
  *               10 DCT32x16, 11 DCT16x32), bit 7 set on the top-left block of
- *               each varblock.  Varblocks are naturally aligned.
+ *               each varblock.  A varblock may start at any block inside
+ *               the frame; encoding needs naturally aligned DCT8/16/32.
  *   coeff image int32, three planes of (8*bh) x (8*bw): a varblock at block
  *               (bx,by) of R x C blocks stores its landscape coefficient
  *               matrix (min(R,C)*8 rows, max(R,C)*8 cols, row-major as the

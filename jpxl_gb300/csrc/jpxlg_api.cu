@@ -613,8 +613,8 @@ int jpxlg_layout_create(jpxlg_ctx* ctx, int width, int height, const uint8_t* bl
   L->geo = make_geo(width, height);
   const Geo& g = L->geo;
   const size_t nb = (size_t)g.bw * g.bh;
-  // Validate the cover (every block covered exactly once by naturally
-  // aligned varblocks of the nine plain DCT shapes) and bucket origins.
+  // Validate the cover (every block covered exactly once by varblocks of
+  // the carried shapes, inside the frame) and bucket origins.
   std::vector<uint8_t> covered(nb, 0);
   std::vector<uint32_t> bucket[kNumShapes];
   for (int by = 0; by < g.bh; ++by)
@@ -626,8 +626,8 @@ int jpxlg_layout_create(jpxlg_ctx* ctx, int width, int height, const uint8_t* bl
       if (!shape_of(sel, &sh))
         return fail(ctx, JPXLG_ERR_BLOCK_MAP, "block (%d,%d): DctSelect %d is not carried", bx,
                     by, sel);
-      if (bx % sh.bcols || by % sh.brows || bx + sh.bcols > g.bw || by + sh.brows > g.bh)
-        return fail(ctx, JPXLG_ERR_BLOCK_MAP, "block (%d,%d): varblock misaligned or outside", bx,
+      if (bx + sh.bcols > g.bw || by + sh.brows > g.bh)
+        return fail(ctx, JPXLG_ERR_BLOCK_MAP, "block (%d,%d): varblock outside the frame", bx,
                     by);
       for (int dy = 0; dy < sh.brows; ++dy)
         for (int dx = 0; dx < sh.bcols; ++dx) {
@@ -640,8 +640,10 @@ int jpxlg_layout_create(jpxlg_ctx* ctx, int width, int height, const uint8_t* bl
       int cls = 0;
       while (kShapeSel[cls] != sel) ++cls;
       bucket[cls].push_back(((uint32_t)by << 16) | (uint32_t)bx);
-      // the encoder's kernels cover DCT8/16/32 only
-      if (sh.brows != sh.bcols || sh.brows > 4 || sel == 2) L->all_square = false;
+      // the encoder's kernels cover naturally aligned DCT8/16/32 only; the
+      // format (and the render) place a varblock at any block
+      if (sh.brows != sh.bcols || sh.brows > 4 || sel == 2 || bx % sh.bcols || by % sh.brows)
+        L->all_square = false;
       if (hf_mul[(size_t)by * g.bw + bx] == 0)
         return fail(ctx, JPXLG_ERR_ARGUMENT, "block (%d,%d): hf_mul must be positive", bx, by);
     }
