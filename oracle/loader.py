@@ -71,6 +71,16 @@ def load() -> C.CDLL:
         lib.orc_ssim2.argtypes = [p, p, i, i, p, p, p]
         lib.orc_perceptual_add_noise.argtypes = [p, p, p, i, f, C.c_uint32]
         lib.orc_perceptual_synthetic.argtypes = [i, i, C.c_uint32, p, p, p]
+        for name in ("orc_dct_2d", "orc_idct_2d"):
+            getattr(lib, name).argtypes = [p, i, i]
+        for name in ("orc64_dct_2d", "orc64_idct_2d"):
+            getattr(lib, name).argtypes = [p, i, i, p]
+        lib.orc64_encode_transform.restype = i
+        lib.orc64_encode_transform.argtypes = [p, i, i, i, p, i, p, p, p]
+        lib.orc64_reconstruct.restype = i
+        lib.orc64_reconstruct.argtypes = [i, i, p, p, p, p, p, p, p, p, i, p]
+        lib.orc64_ssim2.restype = i
+        lib.orc64_ssim2.argtypes = [p, p, p, p, i, i, p, p]
         _lib = lib
     return _lib
 
@@ -170,3 +180,93 @@ def perceptual_pair(w: int, h: int, seed: int, amp: float, noise_seed: int):
     lib.orc_perceptual_add_noise(b[0].ctypes.data, b[1].ctypes.data, b[2].ctypes.data, w * h,
                                  C.c_float(amp), noise_seed)
     return a, b
+
+
+# ---- FP64 truth (oracle_fp64.cpp): the same algorithm in f64 throughout ----
+
+def dct_2d(block: np.ndarray, f64: bool = False) -> np.ndarray:
+    """DCT_2D of a rows x cols block into the landscape layout (f32 butterflies
+    of the restatement, or the f64 truth with `f64`)."""
+    lib = load()
+    rows, cols = block.shape
+    shape = (rows, cols) if cols > rows else (cols, rows)
+    if f64:
+        src = np.ascontiguousarray(block, np.float64)
+        out = np.zeros(shape, np.float64)
+        lib.orc64_dct_2d(src.ctypes.data, rows, cols, out.ctypes.data)
+        return out
+    work = np.ascontiguousarray(block, np.float32).copy()
+    lib.orc_dct_2d(work.ctypes.data, rows, cols)
+    return work.reshape(shape)
+
+
+def idct_2d(coef: np.ndarray, rows: int, cols: int, f64: bool = False) -> np.ndarray:
+    """IDCT_2D of landscape coefficients into rows x cols samples."""
+    lib = load()
+    if f64:
+        src = np.ascontiguousarray(coef, np.float64)
+        out = np.zeros((rows, cols), np.float64)
+        lib.orc64_idct_2d(src.ctypes.data, rows, cols, out.ctypes.data)
+        return out
+    work = np.ascontiguousarray(coef, np.float32).copy()
+    lib.orc_idct_2d(work.ctypes.data, rows, cols)
+    return work.reshape(rows, cols)
+
+
+def fp64_encode_transform(rgb: np.ndarray, block_map: np.ndarray, *, gaborish: bool,
+                          bits: int | None = None):
+    """orc64_encode_transform: (rc, xyb, preconditioned planes, coefficient image), f64."""
+    lib = load()
+    h, w = rgb.shape[:2]
+    bw, bh = (w + 7) // 8, (h + 7) // 8
+    if bits is None:
+        bits = 8 if rgb.dtype == np.uint8 else 16
+    rgb = np.ascontiguousarray(rgb)
+    xyb = np.zeros((3, h, w), np.float64)
+    pre = np.zeros((3, h, w), np.float64)
+    coeff = np.zeros((3, bh * 8, bw * 8), np.float64)
+    bm = np.ascontiguousarray(block_map, np.uint8)
+    rc = lib.orc64_encode_transform(rgb.ctypes.data, w, h, bits, bm.ctypes.data, int(gaborish),
+                                    xyb.ctypes.data, pre.ctypes.data, coeff.ctypes.data)
+    return rc, xyb, pre, coeff
+
+
+def fp64_reconstruct(w: int, h: int, block_map, hf_mul, sharpness, plan: dict, *,
+                     global_scale: int, quant_lf: int = 16, x_qm_scale: int = 2,
+                     b_qm_scale: int = 2, gaborish: bool = False, epf_iters: int = 0,
+                     out_kind: int = 1):
+    """orc64_reconstruct: (rc, [3, h, w] f64): out_kind 1 linear sRGB, 0 XYB
+    after restoration, 4 XYB before restoration."""
+    lib = load()
+    p = RenderParams(global_scale, quant_lf, x_qm_scale, b_qm_scale, int(gaborish), epf_iters,
+                     int(plan["lf_factors"][0]), int(plan["lf_factors"][1]))
+    out = np.zeros((3, h, w), np.float64)
+    arrs = [np.ascontiguousarray(block_map, np.uint8), np.ascontiguousarray(hf_mul, np.uint32),
+            np.ascontiguousarray(sharpness, np.uint8),
+            np.ascontiguousarray(plan["qcoeff"], np.int32),
+            np.ascontiguousarray(plan["lf"], np.int32),
+            np.ascontiguousarray(plan["cfl_x"], np.int8),
+            np.ascontiguousarray(plan["cfl_b"], np.int8)]
+    rc = lib.orc64_reconstruct(w, h, *[a.ctypes.data for a in arrs], C.byref(p), out_kind,
+                               out.ctypes.data)
+    return rc, out
+
+
+def fp64_ssim2(ref: np.ndarray, cand: np.ndarray):
+    """orc64_ssim2 on linear [3, H, W] planes (f32 or f64): (score, terms)."""
+    lib = load()
+    _, h, w = ref.shape
+
+    def planes(a):
+        if a.dtype == np.float64:
+            a = np.ascontiguousarray(a)
+            return None, (C.c_void_p * 3)(*[a[c].ctypes.data for c in range(3)]), a
+        a = np.ascontiguousarray(a, np.float32)
+        return (C.c_void_p * 3)(*[a[c].ctypes.data for c in range(3)]), None, a
+
+    r32, r64, _ra = planes(ref)
+    c32, c64, _ca = planes(cand)
+    sc = C.c_double()
+    terms = np.zeros(6 * 18, np.float64)
+    n = lib.orc64_ssim2(r32, c32, r64, c64, w, h, C.byref(sc), terms.ctypes.data)
+    return sc.value, terms[: max(n, 0) * 18]

@@ -145,6 +145,23 @@ float orc_dct_iv_entry(int M, int u, int n);
 void orc_perceptual_synthetic(int w, int h, uint32_t seed, float* r, float* g, float* b);
 void orc_perceptual_add_noise(float* r, float* g, float* b, int n, float amp, uint32_t seed);
 
+/* ---- FP64 truth (oracle_fp64.cpp) ----
+ * The same algorithm with every operation in f64 and the transforms as exact
+ * cosine sums; tables and constants at the values the f32 path holds. */
+void orc64_dct_2d(const double* in, int rows, int cols, double* out);
+void orc64_idct_2d(const double* coef, int rows, int cols, double* out);
+int orc64_encode_transform(const void* rgb, int w, int h, int bits, const uint8_t* block_map,
+                           int gaborish, double* xyb_out, double* pre_out, double* coeff_out);
+/* out_kind: 0 = XYB after restoration, 1 = linear sRGB, 4 = XYB before
+ * restoration; out holds 3*w*h doubles. */
+int orc64_reconstruct(int w, int h, const uint8_t* block_map, const uint32_t* hf_mul_blocks,
+                      const uint8_t* sharpness, const int32_t* qcoeff, const int32_t* lf,
+                      const int8_t* cfl_x, const int8_t* cfl_b, const orc_render_params* p,
+                      int out_kind, double* out);
+/* Inputs as f32 planes (ref/cand) or f64 planes (ref64/cand64, used when
+ * non-NULL). Returns the number of scales. */
+int orc64_ssim2(const float* const* ref, const float* const* cand, const double* const* ref64,
+                const double* const* cand64, int w, int h, double* score, double* terms);
 
 #ifdef __cplusplus
 }

@@ -556,6 +556,17 @@ int mirror1d(int64_t c, int size) {
   }
 }
 
+// A plane extended by r samples on every side with mirror1d's values.
+std::vector<float> pad_mirror(const float* in, int w, int h, int r) {
+  const int pw = w + 2 * r, ph = h + 2 * r;
+  std::vector<float> out((size_t)pw * ph);
+  for (int y = 0; y < ph; ++y) {
+    const float* row = in + (size_t)mirror1d(y - r, h) * w;
+    for (int x = 0; x < pw; ++x) out[(size_t)y * pw + x] = row[mirror1d(x - r, w)];
+  }
+  return out;
+}
+
 // ---------------------------------------------------------------------------
 // Encoder inverse Gaborish (jpxl-encode/src/vardct/gaborish.rs)
 // ---------------------------------------------------------------------------
@@ -651,13 +662,15 @@ void gaborish_w(const float* in, int w, int h, float w1, float w2, float* out) {
   float unnorm = std::fma(4.0f, w2, std::fma(4.0f, w1, 1.0f));
   float scale = 1.0f / unnorm;
   float centre = scale, edge = w1 * scale, corner = w2 * scale;
+  const std::vector<float> pad = pad_mirror(in, w, h, 1);
+  const int pw = w + 2;
   for (int y = 0; y < h; ++y) {
     for (int x = 0; x < w; ++x) {
       float acc = 0.0f;
       for (int dy = -1; dy <= 1; ++dy)
         for (int dx = -1; dx <= 1; ++dx) {
           float wt = (dx == 0 && dy == 0) ? centre : ((dx == 0 || dy == 0) ? edge : corner);
-          float s = in[(size_t)mirror1d(y + dy, h) * w + mirror1d(x + dx, w)];
+          float s = pad[(size_t)(y + 1 + dy) * pw + (x + 1 + dx)];
           acc = std::fma(wt, s, acc);
         }
       out[(size_t)y * w + x] = acc;
@@ -693,9 +706,12 @@ void epf_step(int step, const float* const* in, int w, int h, const float* sigma
   int ncross = step == 2 ? 1 : 5;
   const float scale[3] = {40.0f, 5.0f, 3.5f};
   int bw = (w + 7) / 8;
-  auto at = [&](int c, int x, int y) -> float {
-    return in[c][(size_t)mirror1d(y, h) * w + mirror1d(x, w)];
-  };
+  // The taps reach 3 samples out (offset 2 plus the cross's 1): each plane
+  // mirrored by 3 once, so that a sample is one lookup.
+  const std::vector<float> pad[3] = {pad_mirror(in[0], w, h, 3), pad_mirror(in[1], w, h, 3),
+                                     pad_mirror(in[2], w, h, 3)};
+  const int pw = w + 6;
+  auto at = [&](int c, int x, int y) -> float { return pad[c][(size_t)(y + 3) * pw + (x + 3)]; };
   for (int y = 0; y < h; ++y) {
     int ry = y % 8;
     bool border_row = ry == 0 || ry == 7;

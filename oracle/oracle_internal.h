@@ -39,6 +39,23 @@ struct TransformInfo {
   int ccols;     // landscape coefficient cols = max*8
 };
 bool transform_info(int sel, TransformInfo* t);
+
+// A varblock decoded from the block map.
+struct Varblock {
+  int bx, by;
+  TransformInfo t;
+};
+// Parses the per-block map into varblocks (raster order of their origins);
+// kErrBlockMap unless the footprints tile the block grid exactly.
+int parse_block_map(const uint8_t* map, int bw, int bh, std::vector<Varblock>* out);
+// Coefficient image addressing (see oracle.h): landscape cell (y, x) of a
+// varblock at (bx, by).
+inline size_t coeff_index(const Varblock& vb, int y, int x, int W8) {
+  bool portrait = vb.t.brows > vb.t.bcols;
+  int row = vb.by * 8 + (portrait ? x : y);
+  int col = vb.bx * 8 + (portrait ? y : x);
+  return (size_t)row * W8 + col;
+}
 float scale_f(int c, int lf_count);
 void dequant_matrix(int dq, int channel, float* out, int* rows, int* cols);
 const float* dequant_matrix_cached(int dq, int channel);
@@ -69,6 +86,7 @@ struct HfQuant {
 };
 
 int mirror1d(int64_t c, int size);
+std::vector<float> pad_mirror(const float* in, int w, int h, int r);
 void gab_precondition(const float* f, int w, int h, float* x);
 void gaborish(const float* in, int w, int h, float* out);
 void gaborish_w(const float* in, int w, int h, float w1, float w2, float* out);

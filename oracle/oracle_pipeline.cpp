@@ -14,15 +14,9 @@
 
 namespace orc {
 
-// A varblock decoded from the block map.
-struct Varblock {
-  int bx, by;
-  TransformInfo t;
-};
-
 // Parses the per-block map into varblocks (raster order of their origins)
 // and checks that the footprints tile the block grid exactly.
-static int parse_block_map(const uint8_t* map, int bw, int bh, std::vector<Varblock>* out) {
+int parse_block_map(const uint8_t* map, int bw, int bh, std::vector<Varblock>* out) {
   std::vector<uint8_t> covered((size_t)bw * bh, 0);
   for (int by = 0; by < bh; ++by) {
     for (int bx = 0; bx < bw; ++bx) {
@@ -48,14 +42,6 @@ static int parse_block_map(const uint8_t* map, int bw, int bh, std::vector<Varbl
   return kOk;
 }
 
-// Coefficient image addressing (see oracle.h): landscape cell (y, x) of a
-// varblock at (bx, by).
-static inline size_t coeff_index(const Varblock& vb, int y, int x, int W8) {
-  bool portrait = vb.t.brows > vb.t.bcols;
-  int row = vb.by * 8 + (portrait ? x : y);
-  int col = vb.bx * 8 + (portrait ? y : x);
-  return (size_t)row * W8 + col;
-}
 
 // ---------------------------------------------------------------------------
 // Source (jpxl-encode-policy/src/source.rs:226 / :355)

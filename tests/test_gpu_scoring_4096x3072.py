@@ -1,10 +1,12 @@
-"""SSIMULACRA2 scoring at 4096 x 3072 RGB8: an original from the synthetic
+"""SSIMULACRA2 scoring at 4096 x 3072 RGB8 (four of the configuration's 32
+pairs, seeds 3100-3103): an original from the synthetic
 generator against its VarDCT reconstruction (cover from select_blocks, CfL,
 Gaborish, 3-step EPF, 8-bit sRGB output) at a seeded global scale in
 [20000, 80000].  The GPU score must equal the restatement's within 0.01
 points (the contract); the blur reproduces the reference's f32 outputs, so
 the measured difference is about 1e-6 and the test also holds it under
-1e-4.  The metric's two GPU routes (score_pair, and a precomputed reference
+1e-4.  Against the FP64 truth of the metric each score stays within 0.01
+points.  The metric's two GPU routes (score_pair, and a precomputed reference
 scored twice) must agree exactly.
 
 A plain f32 9-tap FIR in place of the reference's recursion scored this pair
@@ -37,13 +39,19 @@ def _pair(ctx, seed):
     return jg.srgb_to_linear_planes(rgb, 8), jg.srgb_to_linear_planes(dec, 8), gs
 
 
-def test_reconstruction_pair_matches_the_restatement(ctx, oracle):
-    src, dec, gs = _pair(ctx, 3100)
+@pytest.mark.parametrize("seed", [3100, 3101, 3102, 3103])
+def test_reconstruction_pair_matches_the_restatement(ctx, oracle, seed):
+    src, dec, gs = _pair(ctx, seed)
     got = jg.score_pair(ctx, src, dec)
     want = oracle.ssim2(src, dec)[0]
     assert abs(got - want) < SCORE_TOL, (gs, got, want)
     assert abs(got - want) < MEASURED_TOL, (gs, got, want)
     assert 0.0 < got < 100.0
+    # error against the FP64 truth of the metric on the same pair
+    truth = oracle.fp64_ssim2(src, dec)[0]
+    assert abs(got - truth) < SCORE_TOL, (gs, got, truth)
+    if seed != 3100:
+        return
     ref = jg.PrecomputedReference(ctx, src)
     try:
         metric = jg.Ssimulacra2(ctx)
