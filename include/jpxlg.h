@@ -107,7 +107,28 @@ typedef struct {
   uint32_t gaborish;      /* RestorationDecision::gaborish */
   uint32_t epf_iters;     /* RestorationDecision::epf_iters, 0..3 */
   uint32_t cfl;           /* chroma-from-luma estimation on */
+  uint32_t precision;     /* JPXLG_PRECISION_*: how the DCTs are evaluated (no
+                           * reference field; 0 = the reference's arithmetic) */
 } jpxlg_params;
+
+/* Precision of the DCTs of the encode transform and the render (the other
+ * stages are the same in every mode).
+ *   FP32    the reference's butterflies in FP32 on the CUDA cores, bit-exact
+ *           with jpxl-core dct.rs (quantized coefficients, pixels).
+ *   BF16X3  batched dense contractions on the tcgen05 tensor cores, each f32
+ *           operand split into two bf16 terms and the three leading products
+ *           accumulated in FP32 (about 2^-16 relative error per product).
+ *   BF16X6  the same with three bf16 terms and six products (FP32-level
+ *           error).
+ * The split forms cover the square DCT8/16/32 varblocks (every shape the
+ * encoder produces); other shapes render through the FP32 kernels. Their
+ * coefficients differ from the reference's in the last bits, so quantized
+ * integers can differ where a coefficient sits at a decision boundary. */
+enum {
+  JPXLG_PRECISION_FP32 = 0,
+  JPXLG_PRECISION_BF16X3 = 1,
+  JPXLG_PRECISION_BF16X6 = 2
+};
 
 /* The quantized half of a plan (jpxl-encode vardct/plan.rs:434 LfQuantPlanes,
  * :519 VarblockCoefficients, :251 CflGrid, LfCorrelationDecision). */

@@ -60,6 +60,10 @@ STAGES = ("xyb", "precondition", "fdct_luma", "cfl", "quant_chroma", "render_var
           "gaborish", "epf", "colour", "ssim")
 
 
+# jpxlg_params.precision (include/jpxlg.h JPXLG_PRECISION_*)
+PRECISIONS = {"fp32": 0, "bf16x3": 1, "bf16x6": 2}
+
+
 class JpxlError(RuntimeError):
     """A non-zero jpxlg_status; ``code`` is the status."""
 
@@ -79,6 +83,9 @@ class EncodeRequest:
     gaborish: bool = False
     epf_iters: int = 0
     cfl: bool = True
+    # How the DCTs run: "fp32" (the reference's arithmetic, bit-exact),
+    # "bf16x3" or "bf16x6" (split-precision contractions on the tensor cores).
+    precision: str = "fp32"
 
     @classmethod
     def with_global_scale(cls, gs: int, **kw) -> "EncodeRequest":
@@ -87,7 +94,8 @@ class EncodeRequest:
 
     def _struct(self) -> Params:
         return Params(self.global_scale, self.quant_lf, self.x_qm_scale, self.b_qm_scale,
-                      int(bool(self.gaborish)), self.epf_iters, int(bool(self.cfl)))
+                      int(bool(self.gaborish)), self.epf_iters, int(bool(self.cfl)),
+                      PRECISIONS[self.precision])
 
 
 @dataclass

@@ -75,6 +75,7 @@ class Params(C.Structure):
         ("gaborish", C.c_uint32),
         ("epf_iters", C.c_uint32),
         ("cfl", C.c_uint32),
+        ("precision", C.c_uint32),
     ]
 
 

@@ -2,7 +2,8 @@
 
 Every translation unit is compiled by nvcc with one ``-gencode`` for
 compute_103a/sm_103a, relocatable device code (the DCT constant tables are
-shared across units), ``-fmad=false`` (the reference never contracts a*b+c)
+shared across units; the tensor-core unit is whole-program code, see
+WHOLE_PROGRAM_UNITS), ``-fmad=false`` (the reference never contracts a*b+c)
 and ``-ffp-contract=off`` for the host table code.  Units compile in
 parallel; a unit is rebuilt only when a source or header is newer than its
 object.
@@ -24,7 +25,7 @@ LIB = OUT_DIR / "libjpxlg.so"
 INCLUDE = HERE.parent / "include"
 
 UNITS = ["tables.cu", "k_encode.cu", "k_cover.cu", "k_render.cu", "k_ssim.cu", "k_blur.cu",
-         "jpxlg_api.cu", "entropy.cu", "codestream.cu"]
+         "jpxlg_api.cu", "entropy.cu", "codestream.cu", "k_tc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = [
     "-O3",
@@ -53,12 +54,19 @@ def _newest_header() -> float:
     return max(p.stat().st_mtime for p in heads)
 
 
+# Units compiled as whole-program device code: the tensor-core unit, whose
+# tcgen05 sequence gave wrong accumulators when built as relocatable device
+# code (it refers to no device symbol of another unit).
+WHOLE_PROGRAM_UNITS = {"k_tc.cu"}
+
+
 def _compile(unit: str, extra: list[str]) -> Path:
     src = CSRC / unit
     obj = OBJ_DIR / (unit + ".o")
     if obj.exists() and obj.stat().st_mtime >= max(src.stat().st_mtime, _newest_header()):
         return obj
-    cmd = [nvcc(), *ARCH, *FLAGS, *extra, "-I", str(CSRC), "-I", str(INCLUDE), "-c", str(src),
+    flags = [f for f in FLAGS if not (unit in WHOLE_PROGRAM_UNITS and f == "-rdc=true")]
+    cmd = [nvcc(), *ARCH, *flags, *extra, "-I", str(CSRC), "-I", str(INCLUDE), "-c", str(src),
            "-o", str(obj)]
     res = subprocess.run(cmd, capture_output=True, text=True)
     if res.returncode != 0:

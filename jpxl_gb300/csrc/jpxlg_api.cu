@@ -70,7 +70,7 @@ struct jpxlg_ctx {
   double* h_score = nullptr;    // pinned score out (2 + 108)
   // workspace
   DevBuf rgb, xyb, pre, coeff, dyhf, qcoeff, lfs, dylf, lfq, cflx, cflb;
-  DevBuf planes, aux, sigma, out;
+  DevBuf planes, aux, sigma, out, llf;
   DevBuf lf_part, lf_seed, cfl_tile, cover, cover_map;
   DevBuf pyr, partial, score, cxyb, hpl, bcarry;
   // stage timers
@@ -180,6 +180,8 @@ int sync_and_check(jpxlg_ctx* ctx) {
     if (err & kDevQuantRange)
       return fail(ctx, JPXLG_ERR_QUANT, "a quantization target outside the working range");
     if (err & kDevBadStep) return fail(ctx, JPXLG_ERR_QUANT, "a degenerate quantization step");
+    if (err & kDevTcTimeout)
+      return fail(ctx, JPXLG_ERR_CUDA, "a tensor-core transform timed out waiting for its MMA");
     return fail(ctx, JPXLG_ERR_BLOCK_MAP, "a block-map entry the kernels cannot place");
   }
   return JPXLG_OK;
@@ -231,6 +233,8 @@ int check_params(jpxlg_ctx* ctx, const jpxlg_params* p) {
   if (p->x_qm_scale > 7 || p->b_qm_scale > 7)
     return fail(ctx, JPXLG_ERR_ARGUMENT, "qm scales are u(3)");
   if (p->epf_iters > 3) return fail(ctx, JPXLG_ERR_ARGUMENT, "epf_iters outside 0..=3");
+  if (p->precision > JPXLG_PRECISION_BF16X6)
+    return fail(ctx, JPXLG_ERR_ARGUMENT, "precision must be a JPXLG_PRECISION_* value");
   return JPXLG_OK;
 }
 
@@ -310,7 +314,15 @@ int encode_device(jpxlg_ctx* ctx, const jpxlg_layout* L, const void* rgb_dev, in
   // square classes only: DCT8, DCT16, DCT32 are shape classes 0..2
   stage_begin(ctx, JPXLG_STAGE_FDCT_LUMA);
   launch_mul_table(p->global_scale, ctx->d_mul, ctx->stream);
-  rc = after_launch(ctx, 1 + launch_fdct_luma(a, L->lists, L->counts, ctx->stream));
+  if (p->precision == JPXLG_PRECISION_FP32) {
+    rc = after_launch(ctx, 1 + launch_fdct_luma(a, L->lists, L->counts, ctx->stream));
+  } else {
+    // split-precision forward transform of all three channels on the tensor
+    // cores, then the luma quantization from the coefficient image
+    const int terms = p->precision == JPXLG_PRECISION_BF16X3 ? 2 : 3;
+    int k = 1 + launch_fdct_tc(a, L->lists, L->counts, terms, ctx->num_sms, ctx->stream);
+    rc = after_launch(ctx, k + launch_luma_from_image(a, L->lists, L->counts, ctx->stream));
+  }
   stage_end(ctx);
   if (rc) return rc;
   stage_begin(ctx, JPXLG_STAGE_CFL);
@@ -338,6 +350,9 @@ int render_device(jpxlg_ctx* ctx, const jpxlg_layout* L, const int32_t* qcoeff,
                   const float* lf_float = nullptr) {
   const Geo& g = L->geo;
   const size_t n = (size_t)g.w * g.h, nb = (size_t)g.bw * g.bh;
+  if (p->precision != JPXLG_PRECISION_FP32 && (uintptr_t)qcoeff % 16 != 0)
+    return fail(ctx, JPXLG_ERR_ARGUMENT,
+                "the split-precision render reads 16-byte aligned coefficient planes");
   CK(ctx->planes.ensure(3 * n * sizeof(float)));
   CK(ctx->aux.ensure(3 * n * sizeof(float)));
   CK(ctx->sigma.ensure(nb * sizeof(float)));
@@ -358,11 +373,29 @@ int render_device(jpxlg_ctx* ctx, const jpxlg_layout* L, const int32_t* qcoeff,
   a.planes = ctx->planes.as<float>();
   a.sigma = ctx->sigma.as<float>();
   a.lf_float = lf_float;
+  a.err = ctx->d_words;
   stage_begin(ctx, JPXLG_STAGE_RENDER_VARBLOCKS);
   launch_mul_table(p->global_scale, ctx->d_mul, ctx->stream);
-  launch_render_varblocks(a, L->lists, L->counts, ctx->stream);
   uint64_t k = 1;
-  for (int i = 0; i < kNumShapes; ++i) k += L->counts[i] ? 1 : 0;
+  if (p->precision == JPXLG_PRECISION_FP32) {
+    launch_render_varblocks(a, L->lists, L->counts, ctx->stream);
+    for (int i = 0; i < kNumShapes; ++i) k += L->counts[i] ? 1 : 0;
+  } else {
+    // square classes on the tensor cores; any other shape through the FP32
+    // kernels (a decoded stream's cover)
+    const int terms = p->precision == JPXLG_PRECISION_BF16X3 ? 2 : 3;
+    CK(ctx->llf.ensure(48 * sizeof(float) *
+                       (size_t)std::max(1, L->counts[0] + L->counts[1] + L->counts[2])));
+    float* llf[3] = {ctx->llf.as<float>(), ctx->llf.as<float>() + 48 * (size_t)L->counts[0],
+                     ctx->llf.as<float>() + 48 * (size_t)(L->counts[0] + L->counts[1])};
+    k += launch_llf_sigma(a, L->lists, L->counts, llf, ctx->stream);
+    const float* cllf[3] = {llf[0], llf[1], llf[2]};
+    k += launch_render_tc(a, L->lists, L->counts, cllf, terms, ctx->num_sms, ctx->stream);
+    int rest[kNumShapes];
+    for (int i = 0; i < kNumShapes; ++i) rest[i] = i < 3 ? 0 : L->counts[i];
+    launch_render_varblocks(a, L->lists, rest, ctx->stream);
+    for (int i = 3; i < kNumShapes; ++i) k += rest[i] ? 1 : 0;
+  }
   int rc = after_launch(ctx, k);
   stage_end(ctx);
   if (rc) return rc;
@@ -482,6 +515,7 @@ int jpxlg_ctx_create(int device, uint32_t flags, jpxlg_ctx** out) {
   CKC(cudaSetDevice(device));
   CKC(configure_encode_kernels());
   CKC(configure_blur_kernels());
+  CKC(configure_tc_kernels());
   CKC(cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking));
   c->stream = c->own_stream;
   CKC(cudaMalloc(&c->d_words, 8 * sizeof(uint32_t)));
@@ -506,6 +540,7 @@ int jpxlg_ctx_create(int device, uint32_t flags, jpxlg_ctx** out) {
   upload_dct_constants(iv4, iv8, iv16, sf, c->stream);
   upload_blur_consts(c->stream);
   upload_render_constants(om, ob, oc, c->stream);
+  upload_tc_basis(c->stream);
   CKC(cudaStreamSynchronize(c->stream));
 #undef CKC
   *out = ctx.release();
@@ -526,7 +561,7 @@ int jpxlg_ctx_destroy(jpxlg_ctx* ctx) {
                     &ctx->cflb,   &ctx->planes, &ctx->aux,    &ctx->sigma,   &ctx->out,
                     &ctx->lf_part, &ctx->lf_seed, &ctx->cfl_tile, &ctx->cover,
                     &ctx->cover_map, &ctx->pyr,  &ctx->partial,
-                    &ctx->score,  &ctx->cxyb,   &ctx->hpl,   &ctx->bcarry};
+                    &ctx->score,  &ctx->cxyb,   &ctx->hpl,   &ctx->bcarry, &ctx->llf};
   for (DevBuf* b : bufs) b->release();
   for (auto& m : ctx->marks) {
     cudaEventDestroy(m.a);

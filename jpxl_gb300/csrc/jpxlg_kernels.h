@@ -8,6 +8,8 @@
 
 namespace jpxlg {
 
+struct DF;  // double-float partial sums (jpxlg_common.cuh)
+
 // Everything the encoder kernels read and write (device pointers).
 struct EncArgs {
   Geo geo;
@@ -50,6 +52,7 @@ struct RenderArgs {
   float* planes;             // [3][w*h] XYB out
   float* sigma;              // [bw*bh]
   const float* lf_float = nullptr;  // [3][bw*bh] final LF (decoded frames); else from lfq
+  uint32_t* err = nullptr;   // device error word
 };
 
 // LF of a decoded frame: dequantize, LF CfL and (smooth) adaptive smoothing
@@ -88,6 +91,26 @@ int launch_quant_chroma(const EncArgs& a, const uint32_t* const* lists, const in
 
 void launch_render_varblocks(const RenderArgs& a, const uint32_t* const* lists,
                              const int* counts, cudaStream_t s);
+
+// Split-precision transforms on the tensor cores (k_tc.cu), square shape
+// classes 0..2 (DCT8, DCT16, DCT32); terms = 2 (BF16x3) or 3 (BF16x6).
+// Each returns the number of kernels it launched.  The render form needs
+// 16-byte aligned coefficient planes.
+cudaError_t configure_tc_kernels();
+void upload_tc_basis(cudaStream_t s);
+int launch_fdct_tc(const EncArgs& a, const uint32_t* const* lists, const int* counts, int terms,
+                   int num_sms, cudaStream_t s);
+int launch_render_tc(const RenderArgs& a, const uint32_t* const* lists, const int* counts,
+                     const float* const* llf, int terms, int num_sms, cudaStream_t s);
+// The LLF rectangles (48 floats per varblock: 3 channels x 16) and the EPF
+// sigma of square classes 0..2, for launch_render_tc (k_render.cu).
+int launch_llf_sigma(const RenderArgs& a, const uint32_t* const* lists, const int* counts,
+                     float* const* llf, cudaStream_t s);
+// Luma LF and HF quantization of the square varblocks from a coefficient
+// image the split-precision forward transform wrote (k_fdct_luma without its
+// own transform).
+int launch_luma_from_image(const EncArgs& a, const uint32_t* const* lists, const int* counts,
+                           cudaStream_t s);
 void launch_gaborish(const float* in, float* out, int w, int h, cudaStream_t s);
 void launch_epf_step(int step, const float* in, float* out, const float* sigma, int w, int h,
                      cudaStream_t s);

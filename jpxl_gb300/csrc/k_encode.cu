@@ -438,7 +438,7 @@ __device__ __forceinline__ void lf_from_llf(const float* llf, int n, float* lf) 
 // which it writes to column bx*8+j of the coefficient image (coalesced).
 // ---------------------------------------------------------------------------
 
-template <int N>
+template <int N, bool FROM_IMAGE = false>
 __global__ void __launch_bounds__(128) k_fdct_luma(EncArgs a, const uint32_t* __restrict__ list,
                                                    int count) {
   constexpr int VPB = 128 / N;  // varblocks per CTA
@@ -459,8 +459,24 @@ __global__ void __launch_bounds__(128) k_fdct_luma(EncArgs a, const uint32_t* __
   // not inlined six times past the instruction cache.  Luma runs last, so
   // its coefficients are in v when the loop ends.
   float v[N];
+  if constexpr (FROM_IMAGE) {
+    // The split-precision forward transform has written all three channels'
+    // coefficients: column j of the luma matrix, and the LLF corners.
+    if (active) {
+#pragma unroll
+      for (int k = 0; k < N; ++k) v[k] = a.coeff[cplane + (size_t)(y0 + k) * geo.W8 + x0 + j];
+      if (j < n) {
+#pragma unroll
+        for (int c = 0; c < 3; ++c)
+#pragma unroll
+          for (int k = 0; k < n; ++k)
+            LL[g][c][k * n + j] = a.coeff[cplane * c + (size_t)(y0 + k) * geo.W8 + x0 + j];
+      }
+    }
+    __syncthreads();
+  }
 #pragma unroll 1
-  for (int pass = 0; pass < 6; ++pass) {
+  for (int pass = 0; pass < (FROM_IMAGE ? 0 : 6); ++pass) {
     const int c = pass < 2 ? 0 : (pass < 4 ? 2 : 1);
     if (active) {
       if ((pass & 1) == 0) {
@@ -1142,6 +1158,15 @@ int launch_fdct_luma(const EncArgs& a, const uint32_t* const* lists, const int* 
   if (counts[0]) { k_fdct_luma<8><<<(counts[0] + 15) / 16, 128, 0, s>>>(a, lists[0], counts[0]); ++k; }
   if (counts[1]) { k_fdct_luma<16><<<(counts[1] + 7) / 8, 128, 0, s>>>(a, lists[1], counts[1]); ++k; }
   if (counts[2]) { k_fdct_luma<32><<<(counts[2] + 3) / 4, 128, 0, s>>>(a, lists[2], counts[2]); ++k; }
+  return k;
+}
+
+int launch_luma_from_image(const EncArgs& a, const uint32_t* const* lists, const int* counts,
+                           cudaStream_t s) {
+  int k = 0;
+  if (counts[0]) { k_fdct_luma<8, true><<<(counts[0] + 15) / 16, 128, 0, s>>>(a, lists[0], counts[0]); ++k; }
+  if (counts[1]) { k_fdct_luma<16, true><<<(counts[1] + 7) / 8, 128, 0, s>>>(a, lists[1], counts[1]); ++k; }
+  if (counts[2]) { k_fdct_luma<32, true><<<(counts[2] + 3) / 4, 128, 0, s>>>(a, lists[2], counts[2]); ++k; }
   return k;
 }
 

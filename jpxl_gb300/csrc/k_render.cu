@@ -198,43 +198,6 @@ __device__ __forceinline__ void idct_n(float* v) {
   else idct_1d<N>(v);
 }
 
-template <int N>
-__device__ __forceinline__ void dct_small(float* v) {
-  if (N == 2) dct_1d<2>(v);
-  else if (N == 4) dct_1d<4>(v);
-  else if (N == 8) dct_1d<8>(v);
-}
-
-// dct.rs:956 DCT_2D of an LF rectangle cy x cx (cy <= cx, both <= 8) in place.
-__device__ __forceinline__ void dct2d_small(float* m, int rows, int cols) {
-  float col[8], s[64];
-  // column pass (length rows) on rows x cols
-  for (int c = 0; c < cols; ++c) {
-    for (int r = 0; r < rows; ++r) col[r] = m[r * cols + c];
-    if (rows == 2) dct_small<2>(col);
-    else if (rows == 4) dct_small<4>(col);
-    else if (rows == 8) dct_small<8>(col);
-    for (int r = 0; r < rows; ++r) m[r * cols + c] = col[r];
-  }
-  // transpose to cols x rows, column pass (length cols)
-  for (int r = 0; r < rows; ++r)
-    for (int c = 0; c < cols; ++c) s[c * rows + r] = m[r * cols + c];
-  for (int r = 0; r < rows; ++r) {
-    for (int c = 0; c < cols; ++c) col[c] = s[c * rows + r];
-    if (cols == 2) dct_small<2>(col);
-    else if (cols == 4) dct_small<4>(col);
-    else if (cols == 8) dct_small<8>(col);
-    for (int c = 0; c < cols; ++c) s[c * rows + r] = col[c];
-  }
-  // cols x rows result; landscape => transpose back when cols > rows
-  if (cols <= rows) {
-    for (int i = 0; i < rows * cols; ++i) m[i] = s[i];
-  } else {
-    for (int c = 0; c < cols; ++c)
-      for (int r = 0; r < rows; ++r) m[r * cols + c] = s[c * rows + r];
-  }
-}
-
 // ---------------------------------------------------------------------------
 // R1 — one varblock of R x C samples per group of T = max(R, C) threads.
 // Landscape coefficients are crows = min x ccols = max.  IDCT_2D
@@ -488,6 +451,74 @@ __global__ void __launch_bounds__(128) k_render_vb(RenderArgs a, const uint32_t*
     const float lut = s == 7 ? 1.0f : (float)s / 7.0f;
     a.sigma[bi] = mul * 0.46f * lut;
   }
+}
+
+// The LLF rectangles and EPF sigma of the square varblocks of size N that
+// the split-precision render (k_tc.cu) transforms: varblock.rs:817
+// llf_from_lf (LF dequantized by reconstruct.rs:84 with the LF CfL of
+// plan-render lib.rs:1314, DCT_2D, times scale_f) and restoration.rs:338
+// vardct_sigma, exactly as k_render_vb forms them.  One thread per
+// (varblock, channel); llf receives 16 floats per channel per varblock.
+template <int N>
+__global__ void __launch_bounds__(128) k_llf_sigma(RenderArgs a, const uint32_t* __restrict__ list,
+                                                   int count, float* __restrict__ llf) {
+  constexpr int n = N / 8;
+  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= count * 3) return;
+  const int vi = idx / 3, c = idx % 3;
+  const uint32_t packed = list[vi];
+  const int bx = packed & 0xffff, by = packed >> 16;
+  const Geo& geo = a.geo;
+  const size_t bplane = (size_t)geo.bw * geo.bh;
+  float k_x_lf = a.k_x_lf, k_b_lf = a.k_b_lf;
+  if (a.lf_factors_dev) {
+    k_x_lf = 0.0f + (float)a.lf_factors_dev[0] / 84.0f;
+    k_b_lf = 1.0f + (float)a.lf_factors_dev[1] / 84.0f;
+  }
+  if (c == 0) {
+    const float mul = hf_multiplier(a.mul_table, a.qs.global_scale,
+                                    a.hf_mul[(size_t)by * geo.bw + bx]);
+    for (int i = 0; i < n * n; ++i) {
+      const size_t bi = (size_t)(by + i / n) * geo.bw + bx + i % n;
+      int sh = a.sharpness[bi];
+      sh = sh > 7 ? 7 : sh;
+      const float lut = sh == 7 ? 1.0f : (float)sh / 7.0f;
+      a.sigma[bi] = mul * 0.46f * lut;
+    }
+  }
+  float rect[64];
+  for (int dy = 0; dy < n; ++dy)
+    for (int dx = 0; dx < n; ++dx) {
+      const size_t bi = (size_t)(by + dy) * geo.bw + bx + dx;
+      float v;
+      if (a.lf_float) {
+        v = a.lf_float[bplane * c + bi];
+      } else {
+        const float dY = a.qs.m_dc[1] * (float)a.lfq[bplane + bi] / 1.0f;
+        if (c == 1) {
+          v = dY;
+        } else {
+          const float d = a.qs.m_dc[c] * (float)a.lfq[bplane * c + bi] / 1.0f;
+          v = d + (c == 0 ? k_x_lf : k_b_lf) * dY;
+        }
+      }
+      rect[dy * n + dx] = v;
+    }
+  if (n > 1) dct2d_small(rect, n, n);
+  constexpr int sfi = n == 1 ? 0 : (n == 2 ? 1 : (n == 4 ? 2 : 3));
+  const float* sf = &c_scale_f[sfi * 8];
+  float* o = llf + (size_t)vi * 48 + c * 16;
+  for (int y = 0; y < n; ++y)
+    for (int x = 0; x < n; ++x) o[y * n + x] = rect[y * n + x] * sf[y] * sf[x];
+}
+
+int launch_llf_sigma(const RenderArgs& a, const uint32_t* const* lists, const int* counts,
+                     float* const* llf, cudaStream_t s) {
+  int k = 0;
+  if (counts[0]) { k_llf_sigma<8><<<(3 * counts[0] + 127) / 128, 128, 0, s>>>(a, lists[0], counts[0], llf[0]); ++k; }
+  if (counts[1]) { k_llf_sigma<16><<<(3 * counts[1] + 127) / 128, 128, 0, s>>>(a, lists[1], counts[1], llf[1]); ++k; }
+  if (counts[2]) { k_llf_sigma<32><<<(3 * counts[2] + 127) / 128, 128, 0, s>>>(a, lists[2], counts[2], llf[2]); ++k; }
+  return k;
 }
 
 void launch_render_varblocks(const RenderArgs& a, const uint32_t* const* lists, const int* counts,
