@@ -2,20 +2,28 @@
 """Benchmark of the lossy VarDCT pixel path + SSIMULACRA2 on GB300.
 
 Workload (one "step"): the quality controller's probe — encode transform,
-reconstruct (dequantize, IDCT, Gaborish, 3-step EPF, colour, 8/16-bit depth
+reconstruct (dequantize, IDCT, Gaborish, 3-step EPF, colour, 16-bit depth
 round trip) and SSIMULACRA2 against the precomputed source — over a batch of
-8 distinct 2048x2048 RGB16 synthetic images (seeded; mixed DCT8/16/32 cover;
-CfL; Gaborish; uniform sharpness 7; global_scale 40000).  Source moments for
-the metric are precomputed once per image, outside the timed region, as the
-reference's evaluator does (evaluator.rs:88 -> reference.rs:90).
+8 distinct 2048x2048 RGB16 synthetic images (seeded; mixed DCT8/16/32 cover
+from select_blocks; CfL; Gaborish; uniform sharpness 7; global_scale 40000).
+Source moments for the metric are precomputed once per image, outside the
+timed region, as the reference's evaluator does (evaluator.rs:88 ->
+reference.rs:90).
+
+The DCTs run in the precision named by --precision (the headline): "fp32"
+(the reference's butterflies, bit-exact), "bf16x3" or "bf16x6"
+(split-precision contractions on the tcgen05 tensor cores).  Every mode is
+timed on the same inputs and reported under `precision_modes`.
 
 Prints one JSON line.  `value` is source MPix/s with inputs resident in HBM;
 `e2e` is the same metric through the C ABI with pinned host buffers (the H2D
 copy of each image and the D2H read of each score inside the timed region).
-`parity` states the CUDA path's errors against the CPU restatement on the CPU
-sample; `search` times the batched quality search (64 uneven RGB8 frames x 8
-candidate quantizers = 512 probes in one CUDA graph launch); `decode` times
-the decode of the committed cjxl streams (host parse, GPU reconstruction).
+`parity` states each mode's errors on image 0 of the step (full size)
+against the CPU restatement of the reference and against the FP64 truth;
+`scoring` times SSIMULACRA2 on 32 pairs of 4096x3072 RGB8 (source against
+reconstruction); `search` times the batched quality search (64 uneven RGB8
+frames x 8 candidate quantizers = 512 probes in one CUDA graph launch);
+`decode` times the decode of the committed cjxl streams.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 """
@@ -42,20 +50,18 @@ WORKLOAD = ("2048x2048 RGB16 quality probe: encode transform (XYB, inverse Gabor
             "CfL, quantize) + reconstruct (Gaborish, 3-step EPF, 16-bit depth) + SSIMULACRA2 "
             "(6 scales)")
 
-# Algorithmic HBM bytes per source pixel of each stage for this workload
-# (f32 planes, int32 coefficients, RGB16 input).
-STAGE_BYTES_PER_PX = {
-    "xyb": 6 + 12,              # RGB16 in, 3 f32 planes out
-    "precondition": 12 + 12,    # 3 planes in, 3 out
-    "fdct_luma": 12 + 12 + 4 + 4 + 0.5,  # planes in; coeffs, dY, qY out; LF
-    "cfl": 12 + 4,              # coeffs + dY read
-    "quant_chroma": 8 + 4 + 8,  # cX, cB, dY in; qX, qB out
-    "render_varblocks": 12 + 12,  # q in, XYB planes out
-    "gaborish": 12 + 12,
-    "epf": 3 * (12 + 12),       # three steps
-    "colour": 12 + 12,
-    "ssim": (12 + 36) * 4 / 3 + 15,  # candidate + reference moments over the pyramid
-}
+PRECISIONS = ("fp32", "bf16x3", "bf16x6")
+
+# Algorithmic HBM bytes per source pixel of the path's three parts (the
+# minimum each must move: RGB16 in + int32 coefficients out for the encode
+# transform; coefficients in + f32 planes out for the reconstruction;
+# candidate planes + the reference's nine moment planes over the pyramid for
+# SSIMULACRA2).
+GROUP_BYTES_PER_PX = {"encode": 18.2, "reconstruct": 24.2, "ssim": 60.0}
+STAGE_GROUP = {"xyb": "encode", "precondition": "encode", "fdct_luma": "encode", "cfl": "encode",
+               "quant_chroma": "encode", "render_varblocks": "reconstruct",
+               "gaborish": "reconstruct", "epf": "reconstruct", "colour": "reconstruct",
+               "ssim": "ssim"}
 
 
 def shard_units(units: list, rank: int, world: int) -> list:
@@ -150,19 +156,20 @@ def measured_peaks() -> tuple[float, str]:
     return 6800.0, "fallback"
 
 
+def step_seeds(rank: int, world: int) -> list:
+    return shard_units(list(range(IMAGES_PER_STEP * world)), rank, world)
+
+
 def make_workload(rank: int, world: int):
     """This rank's share of the step's images (RGB only; covers are chosen
     by select_blocks at the probe's quantizer)."""
-    import numpy as np
-
     from jpxl_gb300 import synth
 
-    seeds = shard_units(list(range(IMAGES_PER_STEP * world)), rank, world)
-    return [synth.synthetic_rgb(W, H, seed=1000 + s, bits=BITS) for s in seeds], np
+    return [synth.synthetic_rgb(W, H, seed=1000 + s, bits=BITS) for s in step_seeds(rank, world)]
 
 
 def oracle_cover(rgb, gs):
-    """The restatement's select_blocks (CPU arm and parity sample)."""
+    """The restatement's select_blocks (the reference arm's cover)."""
     from oracle import loader
 
     rc, cover, _ = loader.select_blocks(rgb, global_scale=gs, gaborish=True)
@@ -189,45 +196,94 @@ def cpu_probe(rgb, cover, np, full=False):
     return (plan, lin, score) if full else score
 
 
-def gpu_parity(ctx, crop, ccover, oracle_out, np):
-    """Errors of the CUDA path against the CPU restatement on the timed CPU sample."""
-    import jpxl_gb300 as jg
+def at_depth_f64(lin, np, bits=BITS):
+    """The f64 truth of the output depth round trip: round(linear_to_srgb(x)
+    * max) clamped, back through srgb_to_linear, all in f64."""
+    mx = float((1 << bits) - 1)
+    a = np.abs(lin)
+    e = np.where(a <= 0.0031308, 12.92 * a, 1.055 * np.power(a, 1 / 2.4) - 0.055)
+    e = np.where(lin < 0, -e, e)
+    lvl = np.clip(np.round(e * mx), 0, mx) / mx
+    return np.where(lvl <= 0.04045, lvl / 12.92, np.power((lvl + 0.055) / 1.055, 2.4))
 
-    plan_c, lin_c, score_c = oracle_out
-    h, w = crop.shape[:2]
-    req = jg.EncodeRequest.with_global_scale(GLOBAL_SCALE, gaborish=True, epf_iters=3)
-    layout = jg.Layout(ctx, w, h, ccover, 1, 7)
-    plan = ctx.encode_transform(layout, crop, req)
-    lin = jg.PlanRenderer(ctx).render(layout, plan, req, out="linear_at_depth", bits=BITS)
-    ref = jg.PrecomputedReference(ctx, jg.srgb_to_linear_planes(crop, BITS))
-    score = ctx.probe(layout, ref, crop, req, BITS)
+
+def _mismatches(a, b, np):
+    d = a.astype(np.int64) - b.astype(np.int64)
+    return {"adjacent": int(np.count_nonzero(np.abs(d) == 1)),
+            "other": int(np.count_nonzero(np.abs(d) > 1))}
+
+
+def gpu_parity(ctx, rgb, cover, np):
+    """Every mode's errors on one full-size image: against the CPU restatement
+    of the reference (plan, pixels at depth, score) and against the FP64
+    truth (linear pixels, score).  Also times the restatement's probe on that
+    image as the single-thread CPU baseline."""
+    import jpxl_gb300 as jg
+    from oracle import loader
+
+    h, w = rgb.shape[:2]
+    hf = np.ones(cover.shape, np.uint32)
+    sh = np.full(cover.shape, 7, np.uint8)
+    t0 = time.perf_counter()
+    plan_c, lin_c, score_c = cpu_probe(rgb, cover, np, full=True)
+    cpu_s = time.perf_counter() - t0
+    kw = dict(global_scale=GLOBAL_SCALE, gaborish=True, epf_iters=3)
+    rc, truth_lin = loader.fp64_reconstruct(w, h, cover, hf, sh, plan_c, out_kind=1, **kw)
+    assert rc == 0
+    src = jg.srgb_to_linear_planes(rgb, BITS)
+    truth_score = loader.fp64_ssim2(src, at_depth_f64(truth_lin, np))[0]
+    layout = jg.Layout(ctx, w, h, cover, 1, 7)
+    ref = jg.PrecomputedReference(ctx, src)
+    out = {"sample": (f"image 0 of the step ({w}x{h}); 'oracle' = the CPU restatement of the "
+                      "reference's arithmetic, 'fp64' = the same algorithm in f64 throughout "
+                      "(render of the reference's plan; its score at 16-bit depth)"),
+           "fp64_truth_score": truth_score,
+           "oracle_score": score_c,
+           "oracle_score_vs_fp64": abs(score_c - truth_score)}
+    ref_plan = layout.empty_plan()
+    ref_plan.qcoeff[...] = plan_c["qcoeff"]
+    ref_plan.lf[...] = plan_c["lf"]
+    ref_plan.cfl_x[...] = plan_c["cfl_x"]
+    ref_plan.cfl_b[...] = plan_c["cfl_b"]
+    ref_plan.lf_factors = plan_c["lf_factors"]
+    plan32 = None
+    for prec in PRECISIONS:
+        req = jg.EncodeRequest.with_global_scale(GLOBAL_SCALE, gaborish=True, epf_iters=3,
+                                                 precision=prec)
+        plan = ctx.encode_transform(layout, rgb, req)
+        if prec == "fp32":
+            plan32 = plan
+        # pixels: this mode's render of the reference's plan
+        renderer = jg.PlanRenderer(ctx)
+        lin = renderer.render(layout, ref_plan, req, out="linear_at_depth", bits=BITS)
+        linear = renderer.render(layout, ref_plan, req, out="linear").astype(np.float64)
+        score = ctx.probe(layout, ref, rgb, req)
+        err = np.abs(linear - truth_lin)
+        o = {
+            "qcoeff_mismatches": _mismatches(plan.qcoeff, plan_c["qcoeff"], np),
+            "lf_mismatches": _mismatches(plan.lf, plan_c["lf"], np),
+            "cfl_mismatches": int(np.count_nonzero(plan.cfl_x != plan_c["cfl_x"]) +
+                                  np.count_nonzero(plan.cfl_b != plan_c["cfl_b"])),
+            "pixel_max_abs": float(np.max(np.abs(lin.astype(np.float64) - lin_c))),
+            # linear-at-depth values are one per 16-bit level
+            "dn_mismatches": int(np.count_nonzero(lin != lin_c)),
+            "score": score,
+            "score_abs_diff": float(abs(score - score_c)),
+            "vs_fp64": {"pixel_max_abs": float(err.max()),
+                        "pixel_rmse": float(np.sqrt(np.mean(err ** 2))),
+                        "score_abs_diff": float(abs(score - truth_score))},
+        }
+        if prec != "fp32":
+            o["qcoeff_mismatches_vs_fp32"] = _mismatches(plan.qcoeff, plan32.qcoeff, np)
+        out[prec] = o
     ref.close()
     layout.close()
-    return {
-        "sample": f"the CPU sample ({w}x{h} crop); restatement of the reference's arithmetic",
-        "qcoeff_mismatches": int(np.count_nonzero(plan.qcoeff != plan_c["qcoeff"])),
-        "lf_mismatches": int(np.count_nonzero(plan.lf != plan_c["lf"])),
-        "cfl_mismatches": int(np.count_nonzero(plan.cfl_x != plan_c["cfl_x"]) +
-                              np.count_nonzero(plan.cfl_b != plan_c["cfl_b"])),
-        "pixel_max_abs": float(np.max(np.abs(lin.astype(np.float64) - lin_c))),
-        "pixel_rmse": float(np.sqrt(np.mean((lin.astype(np.float64) - lin_c) ** 2))),
-        # linear-at-depth values are one per 16-bit level, so unequal values
-        # are unequal output levels
-        "dn_mismatches": int(np.count_nonzero(lin != lin_c)),
-        "score_abs_diff": float(abs(score - score_c)),
-    }
-
-
-CPU_SAMPLE = 512  # crop side of the bounded CPU sample
-
-
-def cpu_sample(images, np):
-    crop = np.ascontiguousarray(images[0][:CPU_SAMPLE, :CPU_SAMPLE])
-    return crop, oracle_cover(crop, GLOBAL_SCALE)
+    return out, w * h / cpu_s / 1e6
 
 
 def run_reference(args):
-    """The CPU arm: the restatement of the reference on all host threads."""
+    """The CPU arm: the restatement of the reference on all host threads, one
+    full-size image of the workload per thread per step."""
     import concurrent.futures
 
     import numpy as np
@@ -237,15 +293,18 @@ def run_reference(args):
         return
     from oracle import loader
 
-    loader.build()
-    threads = os.cpu_count() or 1
-    images = []
     from jpxl_gb300 import synth
 
-    for i in range(threads):
-        rgb = synth.synthetic_rgb(CPU_SAMPLE, CPU_SAMPLE, seed=5000 + i, bits=BITS)
-        images.append((rgb, oracle_cover(rgb, GLOBAL_SCALE)))
+    loader.build()
+    threads = os.cpu_count() or 1
     pool = concurrent.futures.ThreadPoolExecutor(max_workers=threads)
+    # The step's images (the GPU arm's seeds, cycled), with the restatement's
+    # own covers chosen before the timed region.
+    seeds = [1000 + (i % IMAGES_PER_STEP) for i in range(threads)]
+    uniq = sorted(set(seeds))
+    base = dict(zip(uniq, pool.map(lambda s: synth.synthetic_rgb(W, H, seed=s, bits=BITS), uniq)))
+    covers = dict(zip(uniq, pool.map(lambda s: oracle_cover(base[s], GLOBAL_SCALE), uniq)))
+    images = [(base[s], covers[s]) for s in seeds]
 
     def step():
         list(pool.map(lambda t: cpu_probe(t[0], t[1], np), images))
@@ -256,17 +315,18 @@ def run_reference(args):
     for _ in range(args.steps):
         step()
     dt = time.perf_counter() - t0
-    mpix = CPU_SAMPLE * CPU_SAMPLE * threads * args.steps / 1e6
+    mpix = W * H * threads * args.steps / 1e6
     value = mpix / dt
-    sample = (f"{threads} concurrent {CPU_SAMPLE}x{CPU_SAMPLE} RGB16 crops per step, one per "
-              f"host thread, same probe arithmetic as the GPU arm")
+    sample = (f"{threads} concurrent {W}x{H} RGB16 probes per step (the GPU arm's images, "
+              f"cycled), one per host thread; the C++ restatement of the reference, -O3")
     print(json.dumps({
         "impl": "reference", "metric": "probe MPix/s (encode+reconstruct+SSIMULACRA2)",
         "value": round(value, 4), "unit": "MPix/s", "n_gpus": args.gpus, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(dt / args.steps * 1e3, 3),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic", "config": {"workload": WORKLOAD, "images_per_step": threads,
-                                         "image": f"{CPU_SAMPLE}x{CPU_SAMPLE} crops"},
+                                         "width": W, "height": H, "bits": BITS,
+                                         "global_scale": GLOBAL_SCALE},
         "cpu_baseline": {"value": round(value, 4), "unit": "MPix/s", "cores": threads,
                          "kind": "port", "sample": sample},
         "e2e": {"value": round(value, 4), "unit": "MPix/s", "h2d_bytes_per_step": 0,
@@ -295,14 +355,14 @@ def search_workload(np):
     return frames
 
 
-def run_search(ctx, torch, np, steps):
+def run_search(ctx, torch, np, steps, precisions):
     """The batched quality search: every frame x every candidate quantizer as
     one graph launch of 512 probes; the chosen quantizer per frame is the
-    coarsest whose score reaches the threshold."""
+    coarsest whose score reaches the threshold.  Timed per precision."""
     import jpxl_gb300 as jg
 
     frames = search_workload(np)
-    items, keep = [], []
+    keep, slots = [], []
     for rgb in frames:
         h, w = rgb.shape[:2]
         ref = jg.PrecomputedReference(ctx, jg.srgb_to_linear_planes(rgb, 8))
@@ -314,44 +374,127 @@ def run_search(ctx, torch, np, steps):
             req = jg.EncodeRequest.with_global_scale(gs, gaborish=True, epf_iters=3)
             layout = jg.Layout(ctx, w, h, jg.select_blocks(ctx, rgb, req), 1, 7)
             keep.append((layout, None, None))
-            items.append(jg.BatchItem(layout, ref, dev.data_ptr(), 8, req))
+            slots.append((layout, ref, dev, gs))
     torch.cuda.synchronize()
-    batch = jg.BatchProbe(ctx, items, lanes=4)
-    scores = torch.zeros(len(items), dtype=torch.float64, device="cuda")
-    stream = torch.cuda.current_stream()
-    for _ in range(2):
-        batch.run_device(scores.data_ptr())
-    ctx.synchronize()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    for _ in range(steps):
-        batch.run_device(scores.data_ptr())
-    e1.record(stream)
-    torch.cuda.synchronize()
-    ms = e0.elapsed_time(e1) / steps
     px = sum(rgb.shape[0] * rgb.shape[1] for rgb in frames) * len(SEARCH_CANDIDATES)
-    sc = scores.cpu().numpy().reshape(len(frames), len(SEARCH_CANDIDATES))
-    chosen = []
-    for row in sc:
-        ok = [gs for gs, v in zip(SEARCH_CANDIDATES, row) if v >= SEARCH_THRESHOLD]
-        chosen.append(min(ok) if ok else None)
-    batch.close()
+    result = {
+        "workload": (f"{len(frames)} RGB8 frames of uneven sizes (w 256-3840, h 256-2160) x "
+                     f"{len(SEARCH_CANDIDATES)} candidate global scales = {len(slots)} probes "
+                     "(encode, render at depth, SSIMULACRA2) as one CUDA graph launch; each "
+                     "probe's cover from select_blocks at its quantizer"),
+        "unit": "MPix/s (rendered+scored)", "steps": steps, "lanes": 4,
+        "threshold": SEARCH_THRESHOLD}
+    stream = torch.cuda.current_stream()
+    for prec in precisions:
+        items = [jg.BatchItem(layout, ref, dev.data_ptr(), 8,
+                              jg.EncodeRequest.with_global_scale(gs, gaborish=True, epf_iters=3,
+                                                                 precision=prec))
+                 for layout, ref, dev, gs in slots]
+        batch = jg.BatchProbe(ctx, items, lanes=4)
+        scores = torch.zeros(len(items), dtype=torch.float64, device="cuda")
+        for _ in range(2):
+            batch.run_device(scores.data_ptr())
+        ctx.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(steps):
+            batch.run_device(scores.data_ptr())
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / steps
+        sc = scores.cpu().numpy().reshape(len(frames), len(SEARCH_CANDIDATES))
+        chosen = []
+        for row in sc:
+            ok = [gs for gs, v in zip(SEARCH_CANDIDATES, row) if v >= SEARCH_THRESHOLD]
+            chosen.append(min(ok) if ok else None)
+        batch.close()
+        result[prec] = {
+            "value": round(px / (ms / 1e3) / 1e6, 2), "ms_per_batch": round(ms, 2),
+            "frames_meeting_threshold": sum(c is not None for c in chosen),
+            "chosen_global_scale": {str(gs): chosen.count(gs) for gs in SEARCH_CANDIDATES}}
+    result["value"] = result[precisions[0]]["value"]
     for layout, ref, _ in keep:
         if ref is not None:
             ref.close()
         if layout is not None:
             layout.close()
-    return {
-        "workload": (f"{len(frames)} RGB8 frames of uneven sizes (w 256-3840, h 256-2160) x "
-                     f"{len(SEARCH_CANDIDATES)} candidate global scales = {len(items)} probes "
-                     "(encode, render at depth, SSIMULACRA2) as one CUDA graph launch; each "
-                     "probe's cover from select_blocks at its quantizer"),
-        "value": round(px / (ms / 1e3) / 1e6, 2), "unit": "MPix/s (rendered+scored)",
-        "ms_per_batch": round(ms, 2), "steps": steps, "lanes": 4,
-        "threshold": SEARCH_THRESHOLD,
-        "frames_meeting_threshold": sum(c is not None for c in chosen),
-        "chosen_global_scale": {str(gs): chosen.count(gs) for gs in SEARCH_CANDIDATES},
-    }
+    return result
+
+
+SCORING_ORIGINALS = 2
+SCORING_SCALES_PER_ORIGINAL = 16
+SW, SH = 4096, 3072
+
+
+def run_scoring(ctx, torch, np, steps):
+    """SSIMULACRA2 on 32 pairs of 4096x3072 RGB8: an original from the
+    generator against its VarDCT reconstruction (select_blocks cover, CfL,
+    Gaborish, 3-step EPF, 8-bit sRGB) at a seeded global scale in
+    [20000, 80000].  Two figures: candidate side against precomputed
+    references (the evaluator's pattern; device-resident, CUDA events), and
+    score_pair end to end (both sides, host-resident linear planes in, score
+    out, wall clock)."""
+    import ctypes as C
+
+    import jpxl_gb300 as jg
+    from jpxl_gb300 import synth
+
+    rng = np.random.default_rng(3100)
+    pairs, refs, host = [], [], []
+    for o in range(SCORING_ORIGINALS):
+        rgb = synth.synthetic_rgb(SW, SH, seed=3100 + o, bits=8)
+        src = jg.srgb_to_linear_planes(rgb, 8)
+        ref = jg.PrecomputedReference(ctx, src)
+        refs.append(ref)
+        for _ in range(SCORING_SCALES_PER_ORIGINAL):
+            gs = int(rng.integers(20000, 80001))
+            req = jg.EncodeRequest.with_global_scale(gs, gaborish=True, epf_iters=3)
+            layout = jg.Layout(ctx, SW, SH, jg.select_blocks(ctx, rgb, req), 1, 7)
+            plan = ctx.encode_transform(layout, rgb, req)
+            dec = jg.PlanRenderer(ctx).render(layout, plan, req, out="srgb8")
+            layout.close()
+            lin = jg.srgb_to_linear_planes(dec, 8)
+            pairs.append((ref, torch.from_numpy(lin).cuda()))
+            if len(host) < 4:
+                host.append((src, lin))
+    torch.cuda.synchronize()
+    out = torch.zeros(len(pairs), dtype=torch.float64, device="cuda")
+    stream = torch.cuda.current_stream()
+    ctx.set_stream(stream.cuda_stream)
+
+    def device_round():
+        for k, (ref, cand) in enumerate(pairs):
+            ctx.check(ctx.lib.jpxlg_ssim2_score(ctx.handle, ref.handle,
+                                                C.c_void_p(cand.data_ptr()), jg.MEM_DEVICE,
+                                                C.c_void_p(out.data_ptr() + 8 * k), None, None))
+
+    device_round()
+    ctx.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(steps):
+        device_round()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / steps
+    scores = out.cpu().numpy()
+    # score_pair end to end on a few host pairs (reference side included)
+    jg.score_pair(ctx, *host[0])
+    t0 = time.perf_counter()
+    for src, lin in host:
+        jg.score_pair(ctx, src, lin)
+    pair_s = (time.perf_counter() - t0) / len(host)
+    for ref in refs:
+        ref.close()
+    px = SW * SH
+    return {"workload": (f"{len(pairs)} pairs of {SW}x{SH} RGB8 ({SCORING_ORIGINALS} generator "
+                         f"originals x {SCORING_SCALES_PER_ORIGINAL} seeded global scales in "
+                         "[20000, 80000]); source against its reconstruction"),
+            "unit": "MPix/s", "value": round(px * len(pairs) / (ms / 1e3) / 1e6, 2),
+            "ms_per_pair": round(ms / len(pairs), 3),
+            "score_pair_e2e_mpix_s": round(px / pair_s / 1e6, 2),
+            "score_pair_e2e_ms": round(pair_s * 1e3, 2),
+            "scores_range": [round(float(scores.min()), 4), round(float(scores.max()), 4)]}
 
 
 def run_select(ctxs, streams, images, dev_rgb, covers, req, steps, px_total, torch, np):
@@ -442,6 +585,42 @@ def run_decode(ctx, reps, np):
     return out
 
 
+def roofline_of(stages: dict, n_img: int) -> dict:
+    """Achieved HBM bandwidth of each part of the path (algorithmic bytes per
+    source pixel x pixels, over the part's CUDA-event time on one stream),
+    the dominant part's fraction of the measured copy bandwidth, and the DRAM
+    traffic per probe from the committed ncu capture."""
+    peak, peak_kind = measured_peaks()
+    px = W * H * n_img
+    groups = {}
+    for stage, (ms, launches) in stages.items():
+        g = STAGE_GROUP[stage]
+        t = groups.setdefault(g, [0.0, 0])
+        t[0] += ms
+        t[1] += launches
+    parts = {}
+    for g, (ms, launches) in groups.items():
+        achieved = GROUP_BYTES_PER_PX[g] * px / (ms / 1e3) / 1e9
+        parts[g] = {"bytes_per_px": GROUP_BYTES_PER_PX[g], "ms_per_probe": round(ms / n_img, 4),
+                    "achieved": round(achieved, 1), "frac": round(achieved / peak, 4),
+                    "launches_per_probe": launches // max(n_img, 1)}
+    top = max(parts, key=lambda g: parts[g]["ms_per_probe"])
+    traffic, basis = None, None
+    tf = ROOT / "profiles" / "traffic_probe_2048x2048_rgb16.json"
+    if tf.exists() and (W, H) == (2048, 2048):
+        t = json.loads(tf.read_text())
+        traffic = t["groups"].get(top)
+        basis = t["source"]
+        for g in parts:
+            parts[g]["traffic_per_probe"] = t["groups"].get(g)
+    return {"kernel": f"{top} stage ({parts[top]['launches_per_probe']} launches per probe)",
+            "bound": "hbm", "achieved": parts[top]["achieved"], "peak": peak, "unit": "GB/s",
+            "frac": parts[top]["frac"], "peak_kind": peak_kind,
+            "algorithmic_bytes_per_probe": int(GROUP_BYTES_PER_PX[top] * W * H),
+            "traffic": traffic, "traffic_unit": "bytes per probe (DRAM read + write, ncu)",
+            "traffic_basis": basis, "parts": parts}
+
+
 def run_ours(args):
     import numpy as np
     import torch
@@ -458,7 +637,7 @@ def run_ours(args):
     from jpxl_gb300 import build
 
     build.build()
-    images, _ = make_workload(rank, world)
+    images = make_workload(rank, world)
     # One context per stream: images alternate over the streams so that the
     # small launches of one probe overlap the work of another.  Dedicated
     # torch streams carry both the library's work and the timing events (the
@@ -475,11 +654,13 @@ def run_ours(args):
         streams.append(st)
     ctx = ctxs[0]
     torch.cuda.set_stream(streams[0])
-    req = jg.EncodeRequest.with_global_scale(GLOBAL_SCALE, gaborish=True, epf_iters=3)
+    reqs = {p: jg.EncodeRequest.with_global_scale(GLOBAL_SCALE, gaborish=True, epf_iters=3,
+                                                  precision=p) for p in PRECISIONS}
+    req = reqs[args.precision]
     layouts, refs, dev_rgb, host_rgb, covers = [], [], [], [], []
     for rgb in images:
         # The probe's cover is the encoder's own choice at this quantizer.
-        covers.append(jg.select_blocks(ctx, rgb, req, BITS))
+        covers.append(jg.select_blocks(ctx, rgb, reqs["fp32"], BITS))
         layouts.append(jg.Layout(ctx, W, H, covers[-1], 1, 7))
         src = torch.from_numpy(jg.srgb_to_linear_planes(rgb, BITS)).cuda()
         refs.append(jg.PrecomputedReference(ctx, device_ptr=src.data_ptr(), width=W, height=H))
@@ -495,55 +676,80 @@ def run_ours(args):
     for c in ctxs:
         c.synchronize()
 
-    def device_step(contexts):
+    def device_step(contexts, r):
         for i in range(len(images)):
             contexts[i % len(contexts)].probe_device(layouts[i], refs[i], dev_rgb[i].data_ptr(),
-                                                     BITS, req, scores.data_ptr() + 8 * i)
+                                                     BITS, r, scores.data_ptr() + 8 * i)
 
-    for _ in range(max(args.warmup, 3)):
-        device_step(ctxs)
-    torch.cuda.synchronize()
+    def timed(r, steps, sampler=None):
+        for _ in range(max(args.warmup, 3)):
+            device_step(ctxs, r)
+        torch.cuda.synchronize()
+        if sampler:
+            sampler.start()
+        launches0 = sum(c.launches for c in ctxs)
+        barrier()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(streams[0])
+        for st in streams[1:]:
+            st.wait_event(e0)
+        for _ in range(steps):
+            device_step(ctxs, r)
+        for st in streams[1:]:
+            done = torch.cuda.Event()
+            done.record(st)
+            streams[0].wait_event(done)
+        e1.record(streams[0])
+        torch.cuda.synchronize()
+        barrier()
+        ms = e0.elapsed_time(e1)
+        launches = sum(c.launches for c in ctxs) - launches0
+        return max_over_ranks(ms), launches
+
+    def stage_breakdown(r, steps):
+        ctx.stage_times()  # reset
+        ctx.stage_timing(True)
+        for _ in range(steps):
+            device_step([ctx], r)
+        ctx.synchronize()
+        st = ctx.stage_times()
+        ctx.stage_timing(False)
+        return st
+
+    px_per_step = W * H * len(images) * world
+    # The headline mode, timed with the clock sampler running.
     sampler = ClockSampler(local)
-    sampler.start()
-    launches0 = sum(c.launches for c in ctxs)
-    barrier()
-    torch.cuda.synchronize()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(streams[0])
-    for st in streams[1:]:
-        st.wait_event(e0)
-    for _ in range(args.steps):
-        device_step(ctxs)
-    for st in streams[1:]:
-        done = torch.cuda.Event()
-        done.record(st)
-        streams[0].wait_event(done)
-    e1.record(streams[0])
-    torch.cuda.synchronize()
-    barrier()
-    ms = e0.elapsed_time(e1)
-    launches = sum(c.launches for c in ctxs) - launches0
+    ms_max, launches = timed(req, args.steps, sampler)
     clocks = sampler.stop()
-    ms_max = max_over_ranks(ms)
-    px_total = W * H * len(images) * args.steps * world
+    px_total = px_per_step * args.steps
     value = px_total / (ms_max / 1e3) / 1e6
+    head_scores = scores.cpu().numpy().copy()
+    # Every precision mode on the same inputs, and each one's stage times.
+    modes, stage_sets = {}, {}
+    for p in PRECISIONS:
+        if p == args.precision:
+            ms_p = ms_max
+        else:
+            ms_p, _ = timed(reqs[p], args.steps)
+        p_scores = scores.cpu().numpy().copy()
+        stage_sets[p] = stage_breakdown(reqs[p], args.steps)
+        dct_ms = (stage_sets[p]["fdct_luma"][0] + stage_sets[p]["render_varblocks"][0]) / \
+            (args.steps * len(images))
+        modes[p] = {"value": round(px_total / (ms_p / 1e3) / 1e6, 2),
+                    "ms_per_step": round(ms_p / args.steps, 3),
+                    "dct_stages_ms_per_image": round(dct_ms, 4),
+                    "scores": [round(float(x), 6) for x in p_scores]}
+    for p in PRECISIONS:
+        modes[p]["vs_fp32"] = round(modes[p]["value"] / modes["fp32"]["value"], 4)
+        modes[p]["dct_stages_vs_fp32"] = round(
+            modes["fp32"]["dct_stages_ms_per_image"] / modes[p]["dct_stages_ms_per_image"], 3)
+    stages = stage_sets[args.precision]
 
     # Block selection (the plan build's first stage) over the same images,
     # device-resident, one context per stream as above.
     select = None if args.no_select else run_select(
-        ctxs, streams, images, dev_rgb, covers, req, args.steps, px_total, torch, np)
-
-    # Decode of cjxl streams (host parse + GPU reconstruction), rank 0.
-    decode = None if args.no_decode or rank != 0 else run_decode(ctx, 20, np)
-
-    # Stage breakdown: the same steps on one stream with stage timers.
-    ctx.stage_times()  # reset
-    ctx.stage_timing(True)
-    for _ in range(args.steps):
-        device_step([ctx])
-    ctx.synchronize()
-    stages = ctx.stage_times()
-    ctx.stage_timing(False)
+        ctxs, streams, images, dev_rgb, covers, reqs["fp32"], args.steps, px_total, torch, np)
 
     # e2e through the C ABI with pinned host buffers: one host thread per
     # context, each probing its share of the images (host mode copies the
@@ -572,71 +778,31 @@ def run_ours(args):
     torch.cuda.synchronize()
     e2e_s = max_over_ranks(time.perf_counter() - t0)
     e2e = px_total / e2e_s / 1e6
-    dev_scores = scores.cpu().numpy()
-    if not np.allclose(dev_scores, host_scores):
-        raise RuntimeError(f"device and host probes disagree: {dev_scores} {host_scores}")
+    if not np.allclose(head_scores, host_scores):
+        raise RuntimeError(f"device and host probes disagree: {head_scores} {host_scores}")
 
     if rank != 0:
         if world > 1:
             dist.destroy_process_group()
         return
-    # Roofline of the dominant stage.
-    top = max(stages, key=lambda k: stages[k][0])
-    top_ms, top_launches = stages[top]
-    n_img = len(images) * args.steps
-    bytes_per_launch = STAGE_BYTES_PER_PX[top] * W * H * n_img / max(top_launches, 1)
-    per_launch_s = top_ms / 1e3 / max(top_launches, 1)
-    achieved = bytes_per_launch / per_launch_s / 1e9
-    peak, peak_kind = measured_peaks()
-    # DRAM bytes per launch from the committed ncu capture of this workload:
-    # a single-kernel stage's kernel, or for the metric's stage the DRAM bytes
-    # of its scale-0 kernels, times 4/3 for the pyramid's smaller scales,
-    # spread over the stage's launches per probe.
-    traffic, traffic_basis = None, None
-    tf = ROOT / "profiles" / "traffic_2048x2048_rgb16.json"
-    if tf.exists() and (W, H) == (2048, 2048):
-        measured = json.loads(tf.read_text())
-        if top in STAGE_KERNEL and STAGE_KERNEL[top] in measured:
-            traffic = measured[STAGE_KERNEL[top]]
-            traffic_basis = f"{STAGE_KERNEL[top]}, one launch (ncu)"
-        elif top == "ssim" and all(k in measured for k in SSIM_SCALE0_KERNELS):
-            per_probe = sum(measured[k] for k in SSIM_SCALE0_KERNELS) * 4 / 3
-            traffic = int(per_probe * n_img / max(top_launches, 1))
-            traffic_basis = ("ssim stage: " + " + ".join(SSIM_SCALE0_KERNELS) +
-                             " at scale 0 (ncu) x 4/3 for scales 1-5, per launch of the stage")
-
-    # What bounds the dominant stage's kernels instead of HBM: their FP32 (FMA)
-    # pipe and issue figures from the committed captures.
-    limiter = None
-    pf = ROOT / "profiles" / "pipes_2048x2048_rgb16.json"
-    if pf.exists() and (W, H) == (2048, 2048):
-        pipes = json.loads(pf.read_text())
-        names = SSIM_SCALE0_KERNELS if top == "ssim" else (STAGE_KERNEL.get(top),)
-        found = {k: pipes[k] for k in names if k in pipes}
-        if found:
-            limiter = {"pipe": "fma", "kernels": found, "source": pipes["source"]}
-
-    # CPU baseline: the restatement on a bounded sample, one thread; the same
-    # sample through the CUDA path gives the errors reported beside the number.
-    cpu_value = None
-    parity = None
+    roofline = roofline_of(stages, len(images) * args.steps)
+    decode = None if args.no_decode else run_decode(ctx, 20, np)
+    # Parity of every mode on image 0 at full size (the oracle's probe on it
+    # is also the single-thread CPU baseline).
+    cpu_value, parity = None, None
     if not args.no_cpu:
-        crop, ccover = cpu_sample(images, np)
-        t0 = time.perf_counter()
-        oracle_out = cpu_probe(crop, ccover, np, full=True)
-        cpu_s = time.perf_counter() - t0
-        cpu_value = round(CPU_SAMPLE * CPU_SAMPLE / cpu_s / 1e6, 4)
-        parity = gpu_parity(ctx, crop, ccover, oracle_out, np)
-        req_c = jg.EncodeRequest.with_global_scale(GLOBAL_SCALE, gaborish=True, epf_iters=3)
-        parity["cover_mismatches"] = int(np.count_nonzero(
-            jg.select_blocks(ctx, crop, req_c, BITS) != ccover))
-    search = None if args.no_search else run_search(ctx, torch, np, 3)
+        parity, cpu_value = gpu_parity(ctx, images[0], covers[0], np)
+    scoring = None if args.no_scoring else run_scoring(ctx, torch, np, 3)
+    search = None if args.no_search else run_search(
+        ctx, torch, np, 3, (args.precision,) + tuple(p for p in ("fp32",) if p != args.precision))
 
     line = {
         "metric": "probe MPix/s (encode+reconstruct+SSIMULACRA2)",
         "value": round(value, 2), "unit": "MPix/s", "n_gpus": world, "steps": args.steps,
         "warmup": max(args.warmup, 3), "ms_per_step": round(ms_max / args.steps, 3),
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32" if args.precision == "fp32" else f"f32 ({args.precision} DCTs)",
+        "precision": args.precision,
         "data": "synthetic",
         "config": {"workload": WORKLOAD, "images_per_step": IMAGES_PER_STEP, "width": W,
                    "height": H, "bits": BITS, "global_scale": GLOBAL_SCALE,
@@ -645,51 +811,48 @@ def run_ours(args):
                    "l2": (f"inputs larger than L2: {IMAGES_PER_STEP} distinct images, "
                           f"{W * H * 6 * IMAGES_PER_STEP / 1e6:.0f} MB of RGB16 per step"),
                    "parallelism": f"replicas x{world}", "streams": nstreams},
+        "precision_modes": modes,
         "stages_ms": {k: round(v[0] / args.steps, 4) for k, v in stages.items()},
-        "roofline": {"kernel": top, "bound": "hbm", "achieved": round(achieved, 1),
-                     "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4),
-                     "peak_kind": peak_kind, "traffic": traffic,
-                     "traffic_basis": traffic_basis, "limiter": limiter},
-        "cpu_baseline": {"value": cpu_value, "unit": "MPix/s", "cores": 1,
-                         "kind": "port",
-                         "sample": f"one {CPU_SAMPLE}x{CPU_SAMPLE} RGB16 crop of image 0, full "
-                                   "probe, single thread"},
+        "roofline": roofline,
+        "cpu_baseline": {"value": None if cpu_value is None else round(cpu_value, 4),
+                         "unit": "MPix/s", "cores": 1, "kind": "port",
+                         "sample": (f"image 0 of the step ({W}x{H} RGB16), the full probe "
+                                    "(encode, render at depth, score) on one thread; the C++ "
+                                    "restatement of the reference, -O3")},
         "e2e": {"value": round(e2e, 2), "unit": "MPix/s",
                 "h2d_bytes_per_step": int(sum(r.nbytes for r in images)),
                 "d2h_bytes_per_step": 8 * len(images)},
         "parity": parity,
+        "scoring": scoring,
         "search": search,
         "select": select,
         "decode": decode,
         "gpu_launches": int(launches),
         "cfl_sequential_fallbacks": sum(c.cfl_fallbacks for c in ctxs),
         "clocks": clocks,
-        "scores": [round(float(s), 6) for s in dev_scores],
+        "scores": [round(float(s), 6) for s in head_scores],
     }
     print(json.dumps(line), flush=True)
     if world > 1:
         dist.destroy_process_group()
 
 
-# Stages that are one kernel launch per image, and that kernel.
-STAGE_KERNEL = {"precondition": "k_precondition", "gaborish": "k_gaborish", "xyb": "k_srgb_to_xyb",
-                "colour": "k_colour_out"}
-# The metric stage's kernels that carry its DRAM traffic (per scale).
-SSIM_SCALE0_KERNELS = ("k_blur_rows<3>", "k_blur_col_local<3>", "k_blur_col_out<3>")
-
-
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=40)
+    ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--precision", default="bf16x6", choices=list(PRECISIONS),
+                    help="DCT precision of the headline figure")
     # Smaller cases for profiler captures (the headline workload is the default).
     ap.add_argument("--size", type=int, default=None, help="square image side (profiling)")
     ap.add_argument("--images", type=int, default=None, help="images per step (profiling)")
-    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the parity / CPU baseline leg")
     ap.add_argument("--no-search", action="store_true",
                     help="skip the batched quality-search leg")
+    ap.add_argument("--no-scoring", action="store_true",
+                    help="skip the 4096x3072 scoring leg")
     ap.add_argument("--no-select", action="store_true",
                     help="skip the block-selection timing leg (covers are still selected)")
     ap.add_argument("--no-decode", action="store_true", help="skip the stream-decode leg")
