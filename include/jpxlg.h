@@ -347,6 +347,17 @@ typedef struct {
   uint32_t orientation, num_extra; /* Exif orientation 1-8 (not applied); extra channels */
 } jpxlg_codestream_info_t;
 int jpxlg_codestream_open(const uint8_t* data, size_t size, jpxlg_codestream** out);
+/* jpxl-core limits.rs Limits: the largest image (width x height) and the
+ * cumulative bytes of channels and planes one stream may make the reader
+ * allocate; each allocation is charged before it is made, and a stream past
+ * either limit returns JPXLG_ERR_STREAM.  jpxlg_codestream_open uses the
+ * reference's defaults (Limits::new, limits.rs:38): 2^30 pixels, 4 GiB. */
+typedef struct {
+  uint64_t max_pixels;
+  uint64_t max_alloc_bytes;
+} jpxlg_codestream_limits;
+int jpxlg_codestream_open_limits(const uint8_t* data, size_t size,
+                                 const jpxlg_codestream_limits* limits, jpxlg_codestream** out);
 const char* jpxlg_codestream_last_error(void);
 int jpxlg_codestream_info(const jpxlg_codestream* cs, jpxlg_codestream_info_t* info);
 int jpxlg_codestream_blocks(const jpxlg_codestream* cs, int32_t* lf, uint8_t* block_map,

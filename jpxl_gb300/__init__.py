@@ -519,6 +519,12 @@ class _CodestreamInfo(C.Structure):
         [(n, C.c_uint32) for n in ("orientation", "num_extra")]
 
 
+class CodestreamLimits(C.Structure):
+    """jpxlg_codestream_limits (jpxl-core limits.rs Limits)."""
+
+    _fields_ = [("max_pixels", C.c_uint64), ("max_alloc_bytes", C.c_uint64)]
+
+
 class Codestream:
     """jpxl-decode's front end (decode.rs:400 decode up to the VarDCT
     frame's integer content, decode.rs:2513) over the library's host-side
@@ -527,12 +533,18 @@ class Codestream:
     block map, HF multipliers, sharpness, CfL factors and coefficient image
     in the plan's layout.  Host code; no device is needed."""
 
-    def __init__(self, data: bytes):
+    def __init__(self, data: bytes, max_pixels: int | None = None,
+                 max_alloc_bytes: int | None = None):
         self.lib = _lib.load()
         buf = np.frombuffer(bytes(data), np.uint8)
         h = C.c_void_p()
-        rc = self.lib.jpxlg_codestream_open(buf.ctypes.data if buf.size else None, buf.size,
-                                            C.byref(h))
+        limits = None
+        if max_pixels is not None or max_alloc_bytes is not None:
+            # limits.rs Limits::new() defaults for the field not given
+            limits = C.byref(CodestreamLimits(max_pixels or (1 << 30),
+                                              max_alloc_bytes or (4 << 30)))
+        rc = self.lib.jpxlg_codestream_open_limits(buf.ctypes.data if buf.size else None,
+                                                   buf.size, limits, C.byref(h))
         if rc:
             raise JpxlError(rc, "jpxlg_codestream_open: " +
                             self.lib.jpxlg_codestream_last_error().decode())

@@ -53,6 +53,7 @@ SIGNATURES: dict[str, tuple] = {
     "jpxlg_symbols_bits_read": (C.c_size_t, [_P]),
     "jpxlg_symbols_destroy": (_I, [_P]),
     "jpxlg_codestream_open": (_I, [_P, C.c_size_t, C.POINTER(_P)]),
+    "jpxlg_codestream_open_limits": (_I, [_P, C.c_size_t, _P, C.POINTER(_P)]),
     "jpxlg_codestream_last_error": (C.c_char_p, []),
     "jpxlg_codestream_info": (_I, [_P, _P]),
     "jpxlg_codestream_blocks": (_I, [_P, _P, _P, _P, _P, _P, _P]),

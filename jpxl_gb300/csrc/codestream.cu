@@ -30,6 +30,25 @@ void need(bool c, const char* what) {
   if (!c) fail(what);
 }
 
+// jpxl-core limits.rs max_alloc_bytes: every channel and plane the reader
+// allocates for one stream is charged to a running total (as
+// modular/channel.rs:106 charges each channel to the reference's meter), and
+// the stream is rejected as malformed once the total would pass 4 GiB,
+// before the allocation is made.  A header of a few bytes can otherwise
+// declare planes whose zero-fill alone exhausts the host.
+// The limits default to the reference's Limits::new() (limits.rs:38):
+// 2^30 pixels, 4 GiB; jpxlg_codestream_open_limits sets them per stream.
+thread_local uint64_t t_alloc_bytes = 0;
+thread_local uint64_t t_max_alloc_bytes = 4ull << 30;
+thread_local uint64_t t_max_pixels = 1ull << 30;
+void charge(uint64_t count, uint64_t elem_bytes) {
+  const uint64_t bytes = count * elem_bytes;
+  need(count == 0 || bytes / count == elem_bytes, "allocation size");
+  t_alloc_bytes += bytes;
+  need(t_alloc_bytes >= bytes && t_alloc_bytes <= t_max_alloc_bytes,
+       "the stream's planes exceed the allocation limit");
+}
+
 int32_t unpack_signed(uint32_t u) {
   return (u & 1) ? (int32_t)(-(int64_t)(u >> 1) - 1) : (int32_t)(u >> 1);
 }
@@ -834,6 +853,7 @@ Channel unsqueeze(const Channel& lo, const Channel& res, bool horizontal) {
     out.w = lo.w + res.w;
     out.h = lo.h;
     if (out.hshift > 0) --out.hshift;
+    charge((uint64_t)out.w * out.h, sizeof(int32_t));
     out.v.assign((size_t)out.w * out.h, 0);
     for (uint32_t y = 0; y < lo.h; ++y) {
       for (uint32_t x = 0; x < res.w; ++x) {
@@ -852,6 +872,7 @@ Channel unsqueeze(const Channel& lo, const Channel& res, bool horizontal) {
     out.w = lo.w;
     out.h = lo.h + res.h;
     if (out.vshift > 0) --out.vshift;
+    charge((uint64_t)out.w * out.h, sizeof(int32_t));
     out.v.assign((size_t)out.w * out.h, 0);
     for (uint32_t y = 0; y < res.h; ++y)
       for (uint32_t x = 0; x < lo.w; ++x) {
@@ -1003,7 +1024,10 @@ void modular_stream(Reader& r, std::vector<Channel>& ch, uint32_t stream_index,
       need((size_t)t.begin_c + 3 <= ch.size(), "RCT channel range");
     }
   }
-  for (Channel& c : ch) c.v.assign((size_t)c.w * c.h, 0);
+  for (Channel& c : ch) {
+    charge((uint64_t)c.w * c.h, sizeof(int32_t));
+    c.v.assign((size_t)c.w * c.h, 0);
+  }
   size_t end = ch.size();
   if (defer) {
     end = std::min(nb_meta, ch.size());
@@ -1101,7 +1125,8 @@ Channel make_channel(uint32_t w, uint32_t h) {
   Channel c;
   c.w = w;
   c.h = h;
-  need((uint64_t)w * h <= (1ull << 30), "channel size");
+  need((uint64_t)w * h <= t_max_pixels, "channel size");
+  charge((uint64_t)w * h, sizeof(int32_t));
   c.v.assign((size_t)w * h, 0);
   return c;
 }
@@ -1372,6 +1397,7 @@ void decode_frame_vardct(std::vector<Section>& sec, bool single, Decoded* out) {
   vd.bw = (W + 7) / 8;
   vd.bh = (H + 7) / 8;
   const size_t nblocks = (size_t)vd.bw * vd.bh;
+  charge(nblocks, 3 * sizeof(int32_t) + 3 + sizeof(uint32_t));
   for (auto& p : vd.lf) p.assign(nblocks, 0);
   vd.block_map.assign(nblocks, 0);
   vd.hf_mul.assign(nblocks, 0);
@@ -1532,6 +1558,7 @@ void decode_frame_vardct(std::vector<Section>& sec, bool single, Decoded* out) {
       const TransformInfo& ti = kTransforms[v.transform];
       offset += 64u * ti.rows * ti.cols;
     }
+  charge(offset, 3 * sizeof(int32_t));
   for (auto& c : vd.coeffs) c.assign(offset, 0);
 
   // Pass groups (G.4; hf_coeff.rs:689).
@@ -1775,7 +1802,7 @@ void decode(const uint8_t* data, size_t size, Decoded* out) {
   size_header(r, &m.width, &m.height);
   // The reference's default pixel budget (jpxl-core limits.rs:42, 2^30),
   // which bounds every allocation a hostile header can ask for.
-  need((uint64_t)m.width * m.height <= (1ull << 30), "image larger than 2^30 pixels");
+  need((uint64_t)m.width * m.height <= t_max_pixels, "image larger than the pixel limit");
   bool preview = false, animation = false, timecodes = false;
   image_metadata(r, &m, &preview, &animation, &timecodes);
   need(!m.want_icc, "ICC profiles are not supported");
@@ -1800,6 +1827,7 @@ void decode(const uint8_t* data, size_t size, Decoded* out) {
     need(out->modular.size() == 3, "LF frame channels");
     const size_t cells = (size_t)f.width * f.height;
     VarDctFrame& vd = out->vardct;
+    charge(cells, 3 * sizeof(float));
     for (auto& pl : vd.lf_frame) pl.assign(cells, 0.0f);
     const float mx = m_lf[0] / 128.0f, my = m_lf[1] / 128.0f, mb = m_lf[2] / 128.0f;
     for (size_t i = 0; i < cells; ++i) {
@@ -1848,11 +1876,22 @@ thread_local std::string g_codestream_error;
 extern "C" const char* jpxlg_codestream_last_error(void) { return g_codestream_error.c_str(); }
 
 extern "C" int jpxlg_codestream_open(const uint8_t* data, size_t size, jpxlg_codestream** out) {
+  return jpxlg_codestream_open_limits(data, size, nullptr, out);
+}
+
+extern "C" int jpxlg_codestream_open_limits(const uint8_t* data, size_t size,
+                                            const jpxlg_codestream_limits* limits,
+                                            jpxlg_codestream** out) {
   if (!out || (!data && size)) return JPXLG_ERR_ARGUMENT;
+  if (limits && (limits->max_pixels == 0 || limits->max_alloc_bytes == 0))
+    return JPXLG_ERR_ARGUMENT;
+  jpxlg::cs::t_max_pixels = limits ? limits->max_pixels : (1ull << 30);
+  jpxlg::cs::t_max_alloc_bytes = limits ? limits->max_alloc_bytes : (4ull << 30);
   *out = nullptr;
   std::unique_ptr<jpxlg_codestream> cs(new (std::nothrow) jpxlg_codestream);
   if (!cs) return JPXLG_ERR_ARGUMENT;
   try {
+    jpxlg::cs::t_alloc_bytes = 0;
     jpxlg::cs::decode(data, size, &cs->d);
   } catch (const jpxlg::cs::Malformed& e) {
     g_codestream_error = e.what;

@@ -339,3 +339,23 @@ def test_vardct_alpha_over_several_groups():
     assert a.min() == 0 and a.max() > 250
     dx, dy = np.abs(np.diff(a, axis=1)), np.abs(np.diff(a, axis=0))
     assert dx[:, 255].max() <= 4 and dy[255].max() <= 4
+
+
+def test_allocation_and_pixel_limits_reject_before_allocating():
+    """jpxl-core limits.rs: every plane the reader allocates for a stream is
+    charged to a cumulative meter before it is made; a stream past the limit
+    (or an image past the pixel limit) is a stream error, not an allocation.
+    Fixture 53 (128x128 VarDCT) needs a few hundred kB of planes: it opens
+    under the defaults and under a 16 MB meter, and fails cleanly under a
+    64 kB one or a 100-pixel limit."""
+    data = (GOLDEN / "53_vardct_mixed_gray_128x128_filters_d4.jxl").read_bytes()
+    jg.Codestream(data).close()
+    jg.Codestream(data, max_alloc_bytes=16 << 20).close()
+    with pytest.raises(jg.JpxlError) as e:
+        jg.Codestream(data, max_alloc_bytes=64 << 10)
+    assert e.value.code == -8 and "allocation limit" in str(e.value)
+    with pytest.raises(jg.JpxlError) as e:
+        jg.Codestream(data, max_pixels=100)
+    assert e.value.code == -8 and "pixel limit" in str(e.value)
+    # the limits are per stream: the next default open succeeds again
+    jg.Codestream(data).close()
