@@ -125,11 +125,17 @@ int fail(jpxlg_ctx* ctx, int code, const char* fmt, ...) {
   return code;
 }
 
+// A failed runtime call returns JPXLG_ERR_CUDA.  A non-sticky error (a
+// failed allocation) also stays in the runtime's last-error slot, where the
+// next launch check would find it: it is read off here, so that the context
+// stays usable.
 #define CK(call)                                                                     \
   do {                                                                               \
     cudaError_t e_ = (call);                                                         \
-    if (e_ != cudaSuccess)                                                           \
+    if (e_ != cudaSuccess) {                                                         \
+      cudaGetLastError();                                                            \
       return fail(ctx, JPXLG_ERR_CUDA, "%s: %s", #call, cudaGetErrorString(e_));     \
+    }                                                                                \
   } while (0)
 
 cudaEvent_t pool_event(jpxlg_ctx* ctx) {
@@ -664,6 +670,11 @@ int jpxlg_layout_create(jpxlg_ctx* ctx, int width, int height, const uint8_t* bl
       if (bx + sh.bcols > g.bw || by + sh.brows > g.bh)
         return fail(ctx, JPXLG_ERR_BLOCK_MAP, "block (%d,%d): varblock outside the frame", bx,
                     by);
+      // jpxl-decode vardct/hf_meta.rs:222: a varblock lies inside one LF
+      // group (256 x 256 pixels = 32 x 32 blocks), as every stream carries.
+      if (bx / 32 != (bx + sh.bcols - 1) / 32 || by / 32 != (by + sh.brows - 1) / 32)
+        return fail(ctx, JPXLG_ERR_BLOCK_MAP,
+                    "block (%d,%d): varblock crosses the LF-group boundary", bx, by);
       for (int dy = 0; dy < sh.brows; ++dy)
         for (int dx = 0; dx < sh.bcols; ++dx) {
           size_t i = (size_t)(by + dy) * g.bw + bx + dx;

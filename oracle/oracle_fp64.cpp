@@ -577,12 +577,12 @@ extern "C" int orc64_ssim2(const float* const* ref, const float* const* cand,
         const double num_m = 1.0 - md * md;
         const double num_s = 2.0 * (s12[i] - m1 * m2) + C2;
         const double den_s = (s11[i] - m1 * m1) + (s22[i] - m2 * m2) + C2;
-        const double d = std::max(1.0 - (num_m * num_s) / den_s, 0.0);
+        const double d = std::fmax(1.0 - (num_m * num_s) / den_s, 0.0);
         sums[0] += d;
         sums[1] += d * d * d * d;
         const double d1 =
             (1.0 + std::fabs(cx[k][i] - m2)) / (1.0 + std::fabs(rx[k][i] - m1)) - 1.0;
-        const double art = std::max(d1, 0.0), lost = std::max(-d1, 0.0);
+        const double art = std::fmax(d1, 0.0), lost = std::fmax(-d1, 0.0);
         sums[2] += art;
         sums[3] += art * art * art * art;
         sums[4] += lost;

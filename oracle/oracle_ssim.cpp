@@ -160,15 +160,16 @@ extern "C" int orc_ssim2(const float* const* ref, const float* const* cand, int 
         float num_m = 1.0f - md * md;
         float num_s = 2.0f * (s12[i] - mu12) + C2;
         float den_s = (s11[i] - mu11) + (s22[i] - mu22) + C2;
-        double d = std::max(1.0 - (double)((num_m * num_s) / den_s), 0.0);
+        // Rust's f64::max returns the other operand of a NaN: fmax
+        double d = std::fmax(1.0 - (double)((num_m * num_s) / den_s), 0.0);
         sums[0] += d;
         sums[1] += d * d * d * d;
         double d1 = (1.0 + (double)std::fabs(cx[k][i] - m2)) /
                         (1.0 + (double)std::fabs(rx[k][i] - m1)) - 1.0;
-        double art = std::max(d1, 0.0);
+        double art = std::fmax(d1, 0.0);
         sums[2] += art;
         sums[3] += art * art * art * art;
-        double lost = std::max(-d1, 0.0);
+        double lost = std::fmax(-d1, 0.0);
         sums[4] += lost;
         sums[5] += lost * lost * lost * lost;
       }
