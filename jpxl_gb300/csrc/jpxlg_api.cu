@@ -1362,13 +1362,20 @@ extern "C" int jpxlg_ssim2_score_static(jpxlg_ctx* ctx, const jpxlg_ref* ref,
   unsigned char* scratch = nullptr;
   int rc = static_scratch(ctx, &scratch);
   if (rc) return rc;
+  // Every region checked against its capacity at run time, not only through
+  // the side limit: the pyramid, the partial-sum rows, and per scale the
+  // candidate's positive XYB and one channel's row-pass planes (three planes
+  // each) and its column-pass carry (a third of the three channels').
   size_t pyr = 0, rows = 0;
+  bool fits = true;
   for (int s = 0; s < ref->nscales; ++s) {
     const SsimScale& rs = ref->scales[s];
     if (s > 0) pyr += 3 * (size_t)rs.w * rs.h;
     rows += (size_t)blur_partial_rows(rs.w, rs.h);
+    fits = fits && (size_t)rs.w * rs.h <= kStaticPlaneFloats &&
+           blur_carry_floats(rs.w, rs.h) / 3 <= kStaticCarryFloats;
   }
-  if (pyr > kStaticPyrFloats || rows > kStaticPartialRows)
+  if (!fits || pyr > kStaticPyrFloats || rows > kStaticPartialRows)
     return fail(ctx, JPXLG_ERR_ARGUMENT, "static scoring scratch too small for %dx%d", ref->w,
                 ref->h);
   float* next = (float*)scratch;

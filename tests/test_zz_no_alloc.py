@@ -50,6 +50,26 @@ def test_static_scratch_score_matches_allocating_score(ctx):
     ref.close()
 
 
+@pytest.mark.parametrize("w,h", [(2048, 2048), (2048, 9), (9, 2048)])
+def test_static_scratch_at_its_capacity_edge(ctx, w, h):
+    """Frames at the side limit fill the scratch regions to their sizes:
+    the result must still equal the allocating entry point's."""
+    torch = pytest.importorskip("torch")
+    ref_planes = _planes(w, h, 21, 0.0)
+    cand = _planes(w, h, 21, 0.03)
+    ref = jg.PrecomputedReference(ctx, ref_planes)
+    metric = jg.Ssimulacra2(ctx)
+    want = metric.score(ref, cand)
+    out = torch.full((110,), float("nan"), dtype=torch.float64, device="cuda")
+    cand_dev = torch.from_numpy(cand).cuda()
+    torch.cuda.synchronize()
+    metric.score_static_device(ref, cand_dev.data_ptr(), out.data_ptr())
+    ctx.synchronize()
+    got = out.cpu().numpy()
+    assert abs(got[0] - want.score) <= TOL, (got[0], want.score)
+    ref.close()
+
+
 def test_static_scratch_rejects_frames_beyond_its_limit(ctx):
     torch = pytest.importorskip("torch")
     w, h = 2056, 8
