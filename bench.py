@@ -729,10 +729,10 @@ def run_ours(args):
     modes, stage_sets = {}, {}
     for p in PRECISIONS:
         if p == args.precision:
-            ms_p = ms_max
+            ms_p, p_scores = ms_max, head_scores
         else:
             ms_p, _ = timed(reqs[p], args.steps)
-        p_scores = scores.cpu().numpy().copy()
+            p_scores = scores.cpu().numpy().copy()
         stage_sets[p] = stage_breakdown(reqs[p], args.steps)
         dct_ms = (stage_sets[p]["fdct_luma"][0] + stage_sets[p]["render_varblocks"][0]) / \
             (args.steps * len(images))
