@@ -316,7 +316,8 @@ int jpxlg_symbols_destroy(jpxlg_symbols* s);
  * fragments) with one regular frame, optionally after a modular LF frame
  * (kUseLfFrame); modular transforms RCT, squeeze and palette; modular
  * frames of several groups (one pass) with extra channels; a VarDCT frame's
- * extra channels.  ICC profiles, previews, patches, splines, noise and
+ * extra channels, except those with a dim_shift and, in a frame of several
+ * passes, those larger than a group (both return JPXLG_ERR_STREAM).  ICC profiles, previews, patches, splines, noise and
  * upsampling are reported as unsupported (JPXLG_ERR_STREAM with a reason in
  * jpxlg_codestream_last_error).  Host code only: no device is needed.
  *   jpxlg_codestream_open          parse and decode; *out owns the result
@@ -394,7 +395,9 @@ int jpxlg_codestream_render(jpxlg_ctx* ctx, const jpxlg_codestream* cs, int out_
  * Limits: reference frames up to 2048 x 2048 (larger ones return
  * JPXLG_ERR_ARGUMENT); the first call on a device resolves the scratch
  * address and should come before any stream capture; there is one scratch
- * per device, so calls in flight at the same time on one device race. */
+ * per device, so calls in flight at the same time on one device race.  The
+ * scratch is a 137 MB __device__ array, resident on every device where the
+ * library's module loads, whether or not this entry point is called. */
 int jpxlg_ssim2_score_static(jpxlg_ctx* ctx, const jpxlg_ref* ref,
                              const float* linear_rgb_dev, double* out_dev);
 
