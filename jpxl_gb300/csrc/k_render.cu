@@ -26,15 +26,45 @@ __device__ float g_dct64[64 * 64];
 
 // dct.rs:678 matrix_pass for N = 64 (the reference's transforms above 32
 // points): each output an f64 dot product of f32 entries, rounded once, then
-// the normative factor sqrt(64) = 8.
+// the normative factor sqrt(64) = 8.  The dot product runs in double-float on
+// the FP32 pipe (GB300's FP64 rate is a small fraction of its FP32 rate):
+// each product is exact as p + e (e from one FMA), four independent
+// compensated partial sums carry the rest, and one rounding to f32 ends it.
+// Both that sum and the reference's sequential f64 sum lie within ~1e-15
+// (relative) of the exact dot product, so they round to the same f32 unless
+// the exact value lies that close to a rounding midpoint.
+__device__ __forceinline__ void df_acc(float& hi, float& lo, float a, float b) {
+  const float p = a * b;
+  const float e = __fmaf_rn(a, b, -p);  // a*b = p + e exactly
+  const float s = hi + p;
+  const float bb = s - hi;
+  const float err = (hi - (s - bb)) + (p - bb);  // hi + p = s + err exactly
+  hi = s;
+  lo = lo + (err + e);
+}
+
 __device__ __forceinline__ void idct_64(float* v) {
   float out[64];
 #pragma unroll 1
   for (int k = 0; k < 64; ++k) {
-    double acc = 0.0;
-#pragma unroll 8
-    for (int j = 0; j < 64; ++j) acc += (double)g_dct64[j * 64 + k] * (double)v[j];
-    out[k] = (float)acc;
+    float h[4] = {0.0f, 0.0f, 0.0f, 0.0f}, l[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+#pragma unroll
+    for (int j = 0; j < 64; j += 4)
+#pragma unroll
+      for (int i = 0; i < 4; ++i) df_acc(h[i], l[i], g_dct64[(j + i) * 64 + k], v[j + i]);
+    // combine the four partial sums (double-float additions)
+    float hi = h[0], lo = l[0];
+#pragma unroll
+    for (int i = 1; i < 4; ++i) {
+      const float s = hi + h[i];
+      const float bb = s - hi;
+      const float err = (hi - (s - bb)) + (h[i] - bb);
+      hi = s;
+      lo = lo + (err + l[i]);
+    }
+    const float r = hi + lo;
+    // one correct rounding of hi + lo: r is f32(hi + lo) (round to nearest)
+    out[k] = r;
   }
 #pragma unroll
   for (int k = 0; k < 64; ++k) v[k] = out[k] * 8.0f;
