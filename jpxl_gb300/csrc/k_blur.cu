@@ -17,14 +17,11 @@
 // content-dependent ripple of order 1e-7 of the signal; a plain f32 FIR
 // misses it and lands tens of ulps away, which SSIMULACRA2's variance
 // differences (sigma - mu^2 with C2 = 0.0009) amplify into score errors of
-// a tenth of a point on large near-identical pairs.  Here FIR_j is formed on
-// a common grid (fir_grid2: each sample split once into a high part on a
-// power-of-two grid fixed per line or tile and an exact rest, so that the
-// high parts' pair sums, their products with 12-bit tap pieces and the
-// five-term sum are exact in f32 and only small cross terms round; taps from
-// the f64 recursion's impulse response) and R_j comes from f32 resonators
-// (R's own relative error of 1e-6 is far below an output ulp); one final f32
-// addition rounds FIR_j + R_j.
+// a tenth of a point on large near-identical pairs.  Here FIR_j is a
+// double-float dot product (exact pair sums, exact products, compensated
+// accumulation; taps as hi + lo from the f64 recursion's impulse response)
+// and R_j comes from f32 resonators (R's own relative error of 1e-6 is far
+// below an output ulp); one final f32 addition rounds FIR_j + R_j.
 //
 // Lines are split into segments.  Each segment runs its resonators from
 // rest; a scan over the segments (after L steps the state is M^L times the
@@ -60,7 +57,7 @@ namespace jpxlg {
 
 struct BlurConsts {
   float a[3], b[3];    // MUL_IN and MUL_PREV (blur.rs:41/:47) in f32, for the ripple
-  float gh[5], gl[5];  // FIR taps (centre, +-1 .. +-4): a 12-bit piece on the 2^-13 grid + the rest
+  float th[5], tl[5];  // FIR taps (centre, +-1 .. +-4) as hi + lo
   // U[k][n] = sin((n+1) w_k) / sin(w_k), w_k = (2k+1) pi / 10: M_k^n is
   // [[U[n], -U[n-1]], [U[n-1], -U[n-2]]] (period 20 in n; U[-1] = 0).
   float U[3][20];
@@ -70,7 +67,7 @@ __constant__ BlurConsts c_blur;
 // The constants as lane pairs for the paired forms, and the pair (+0, +0)
 // for negations.
 struct BlurPairs {
-  f2 a[3], b[3], gh[5], gl[5], z;
+  f2 a[3], b[3], th[5], tl[5], nth[5], ntl[5], z;  // nth, ntl: the taps negated
 };
 __constant__ BlurPairs c_blur2;
 
@@ -102,8 +99,8 @@ void upload_blur_consts(cudaStream_t s) {
       }
       out = (o[0] + o[1]) + o[2];
     }
-    bc.gh[d] = (float)(std::nearbyint(out * 8192.0) / 8192.0);
-    bc.gl[d] = (float)(out - (double)bc.gh[d]);
+    bc.th[d] = (float)out;
+    bc.tl[d] = (float)(out - (double)bc.th[d]);
   }
   for (int k = 0; k < 3; ++k) {
     const double w = (2 * k + 1) * M_PI / 10.0;
@@ -121,8 +118,10 @@ void upload_blur_consts(cudaStream_t s) {
     bp.b[k] = pair(bc.b[k]);
   }
   for (int d = 0; d < 5; ++d) {
-    bp.gh[d] = pair(bc.gh[d]);
-    bp.gl[d] = pair(bc.gl[d]);
+    bp.th[d] = pair(bc.th[d]);
+    bp.tl[d] = pair(bc.tl[d]);
+    bp.nth[d] = pair(-bc.th[d]);
+    bp.ntl[d] = pair(-bc.tl[d]);
   }
   bp.z = 0ull;
   cudaMemcpyToSymbolAsync(c_blur2, &bp, sizeof(bp), 0, cudaMemcpyHostToDevice, s);
@@ -182,6 +181,12 @@ __device__ __forceinline__ float pair_error(float left, float right) {
 
 // ---- paired forms --------------------------------------------------------
 
+__device__ __forceinline__ void two_sum2(f2 a, f2 b, f2& s, f2& e) {
+  s = f2_add(a, b);
+  const f2 bb = f2_sub(s, a);
+  e = f2_add(f2_sub(a, f2_sub(s, bb)), f2_sub(b, bb));
+}
+
 // pair_error on two lanes: f32(l + r) - (l + r), i.e. two_sum's error negated
 // term by term (negation commutes with rounding).
 __device__ __forceinline__ f2 pair_error2(f2 l, f2 r) {
@@ -205,48 +210,28 @@ __device__ __forceinline__ f2 ripple_step2(Ripple2& r, f2 e, f2 nz) {
   return f2_add(f2_add(r.p[0], r.p[1]), r.p[2]);
 }
 
-// The FIR on a common grid (two lanes).  Every sample x of the window is
-// split once as x = h + l, h the nearest multiple of G = 2^(E-11) (the
-// grid of the line or tile, |x| < 2^(E-1)), l the exact rest; each tap as
-// gh + gl, gh a multiple of 2^-13 below 2^12 units.  Then h's pair sums are
-// exact multiples of G below 2^11 G, their products with gh exact multiples
-// of G 2^-13 below 2^23 units, and the five-term sum below 2^23 units (the
-// taps' pieces sum to 8192 units): the FMA chain S is exact.  The cross
-// terms (gh l, gl h, gl l: at most 2^-11 of the output) round in f32, and the
-// sum S + (L + rip) rounds once.  The result is the reference's f32 blur
-// output except where the exact value lies within about 2^-35 relative of a
-// rounding midpoint (measured: 3 in 10^4 samples, 1 ulp).
-__device__ __forceinline__ f2 fir_grid2(const f2* h, const f2* l, f2 rip, f2 z) {
-  f2 S = f2_fma(c_blur2.gh[0], h[4], z);
-  const f2 c = f2_add(h[4], l[4]);
-  f2 L = f2_fma(c_blur2.gh[0], l[4], z);
-  L = f2_fma(c_blur2.gl[0], c, L);
+// The double-float FIR on two lanes.  The low word is kept negated (cn = -c,
+// exact since rounding is symmetric) so that every product error comes from
+// one FMA with a negated tap: fma(-t, u, t*u rounded) = -(t*u - its rounding).
+__device__ __forceinline__ f2 fir_exact2(f2 m4, f2 m3, f2 m2, f2 m1, f2 c0, f2 p1, f2 p2, f2 p3,
+                                         f2 p4, f2 rip, f2 nz) {
+  f2 S = f2_mul(c_blur2.th[0], c0, nz);
+  f2 cn = f2_fma(c_blur2.ntl[0], c0, f2_fma(c_blur2.nth[0], c0, S));
+  const f2 lo[4] = {m1, m2, m3, m4}, hi[4] = {p1, p2, p3, p4};
 #pragma unroll
   for (int d = 1; d <= 4; ++d) {
-    const f2 uh = f2_add(h[4 - d], h[4 + d]);
-    const f2 ul = f2_add(l[4 - d], l[4 + d]);
-    S = f2_fma(c_blur2.gh[d], uh, S);
-    L = f2_fma(c_blur2.gh[d], ul, L);
-    L = f2_fma(c_blur2.gl[d], uh, L);
-    L = f2_fma(c_blur2.gl[d], ul, L);
+    f2 u, ul;
+    two_sum2(lo[d - 1], hi[d - 1], u, ul);
+    const f2 p = f2_mul(c_blur2.th[d], u, nz);
+    const f2 rn = f2_fma(c_blur2.nth[d], u, p);  // -(th*u - p)
+    f2 q;
+    two_sum2(S, p, S, q);
+    cn = f2_sub(cn, q);
+    cn = f2_add(cn, rn);
+    cn = f2_fma(c_blur2.nth[d], ul, cn);
+    cn = f2_fma(c_blur2.ntl[d], u, cn);
   }
-  return f2_add(S, f2_add(L, rip));
-}
-
-// The grid constant 1.5 * 2^(E+12) of values bounded by m (|x| <= m <
-// 2^(E-1)): x + C rounds x to a multiple of 2^(E-11).  A line of zeros, or
-// one with a non-finite sample (whose outputs are not finite either way),
-// takes the grid of 1.
-__device__ __forceinline__ float grid_const(float m) {
-  if (!(m > 0.0f) || !(m < 3.0e38f)) m = 1.0f;
-  int e;
-  frexpf(m, &e);  // m < 2^e
-  return ldexpf(1.5f, e + 13);
-}
-
-__device__ __forceinline__ void grid_split2(f2 v, f2 C, f2& h, f2& l) {
-  h = f2_sub(f2_add(v, C), C);
-  l = f2_sub(v, h);
+  return f2_add(S, f2_sub(rip, cn));
 }
 
 // ---------------------------------------------------------------------------
@@ -272,7 +257,6 @@ __global__ void __launch_bounds__(kRowThreads, 6) k_blur_rows(RowArgs a) {
   f2* rl = NQ == 3 ? bsm2 + a.w + 20 : nullptr;       // [w + 20]: r likewise (NQ == 3)
   f2* rip = bsm2 + (NQ == 3 ? 2 : 1) * (a.w + 20);    // [w]: R of both rows
   __shared__ f2 carry[kRowThreads][6];
-  __shared__ float lmax[kRowThreads / 32][4];  // per warp: max |x|, |r| of each row
   const int y0 = 2 * blockIdx.x, ch = blockIdx.y, c = a.c0 + ch;
   const bool two = y0 + 1 < a.h;
   const size_t n = (size_t)a.w * a.h;
@@ -283,46 +267,19 @@ __global__ void __launch_bounds__(kRowThreads, 6) k_blur_rows(RowArgs a) {
   const f2 nz = f2_pack(a.nz, a.nz);
   const int t = threadIdx.x;
   const int j0 = min(t * a.seg, a.w), j1 = min(j0 + a.seg, a.w);
-  // Both rows of x (and r) once, zero outside the line, and each row's
-  // largest |x| and |r| (for the grid of the outputs' FIR).
-  float mx0 = 0.0f, mx1 = 0.0f, mr0 = 0.0f, mr1 = 0.0f;
+  // Both rows of x (and r) once, zero outside the line.
 #pragma unroll 8
   for (int i = t; i < a.w + 20; i += kRowThreads) {
     const int gx = i - 10;
     const bool in = gx >= 0 && gx < a.w;
     const float x0 = in ? xr0[gx] : 0.0f, x1 = in && two ? xr1[gx] : 0.0f;
     xl[i] = f2_pack(x0, x1);
-    mx0 = fmaxf(mx0, fabsf(x0));
-    mx1 = fmaxf(mx1, fabsf(x1));
     if (NQ == 3) {
       const float r0 = in ? rr0[gx] : 0.0f, r1 = in && two ? rr1[gx] : 0.0f;
       rl[i] = f2_pack(r0, r1);
-      mr0 = fmaxf(mr0, fabsf(r0));
-      mr1 = fmaxf(mr1, fabsf(r1));
     }
   }
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) {
-    mx0 = fmaxf(mx0, __shfl_xor_sync(0xffffffffu, mx0, o));
-    mx1 = fmaxf(mx1, __shfl_xor_sync(0xffffffffu, mx1, o));
-    mr0 = fmaxf(mr0, __shfl_xor_sync(0xffffffffu, mr0, o));
-    mr1 = fmaxf(mr1, __shfl_xor_sync(0xffffffffu, mr1, o));
-  }
-  if ((t & 31) == 0) {
-    lmax[t >> 5][0] = mx0;
-    lmax[t >> 5][1] = mx1;
-    lmax[t >> 5][2] = mr0;
-    lmax[t >> 5][3] = mr1;
-  }
   __syncthreads();
-  mx0 = mx1 = mr0 = mr1 = 0.0f;
-#pragma unroll
-  for (int wi = 0; wi < kRowThreads / 32; ++wi) {
-    mx0 = fmaxf(mx0, lmax[wi][0]);
-    mx1 = fmaxf(mx1, lmax[wi][1]);
-    mr0 = fmaxf(mr0, lmax[wi][2]);
-    mr1 = fmaxf(mr1, lmax[wi][3]);
-  }
 #pragma unroll
   for (int q = 0; q < NQ; ++q) {
     // The quantity's line sample i: x, x*x or r*x, each product rounded to
@@ -388,42 +345,14 @@ __global__ void __launch_bounds__(kRowThreads, 6) k_blur_rows(RowArgs a) {
       }
     }
     __syncthreads();
-    // (4) the outputs: each thread walks its own segment with a 9-sample
-    // window of split samples in registers (each sample split once) and
-    // leaves each output in rip[j]; a coalesced copy follows.  The quantity's
-    // bound per row: its largest |x|, |x|^2 or |r||x| (rounding is monotone,
-    // so every rounded product stays within the rounded bound).
-    {
-      const f2 C2 = f2_pack(
-          grid_const(q == 0 ? mx0 : (q == 1 ? mx0 * mx0 : mr0 * mx0)),
-          grid_const(q == 0 ? mx1 : (q == 1 ? mx1 * mx1 : mr1 * mx1)));
-      f2 H[9], Lo[9];
-#pragma unroll
-      for (int k = 0; k < 8; ++k) grid_split2(L(j0 + 6 + k), C2, H[k], Lo[k]);
-#pragma unroll 1
-      for (int jj = j0; jj < j1; jj += 9) {
-#pragma unroll
-        for (int s = 0; s < 9; ++s) {
-          const int j = jj + s;
-          if (j < j1) {
-            grid_split2(L(j + 14), C2, H[(s + 8) % 9], Lo[(s + 8) % 9]);
-            f2 hh[9], ll[9];
-#pragma unroll
-            for (int k = 0; k < 9; ++k) {
-              hh[k] = H[(s + k) % 9];
-              ll[k] = Lo[(s + k) % 9];
-            }
-            rip[j] = fir_grid2(hh, ll, rip[j], nz);
-          }
-        }
-      }
-    }
-    __syncthreads();
+    // (4) the outputs, in parallel.
     float* o0 = a.out + (size_t)(ch * NQ + q) * n + (size_t)y0 * a.w;
     float* o1 = o0 + a.w;
-#pragma unroll 4
+#pragma unroll 2
     for (int j = t; j < a.w; j += kRowThreads) {
-      const f2 r = rip[j];
+      const int i = j + 10;
+      const f2 r = fir_exact2(L(i - 4), L(i - 3), L(i - 2), L(i - 1), L(i), L(i + 1), L(i + 2),
+                              L(i + 3), L(i + 4), rip[j], nz);
       o0[j] = f2_lo(r);
       if (two) o1[j] = f2_hi(r);
     }
@@ -524,9 +453,7 @@ template <int NQ>
 __global__ void __launch_bounds__(kOutThreads, 4) k_blur_col_out(ColArgs a) {
   __shared__ __align__(16) float tile[NQ][kColT + 10][kColW];  // rows r0-6 .. r0+kColT+3
   __shared__ __align__(16) float rp[NQ][kColT][kColW];
-  __shared__ __align__(16) float tlo[NQ][kColT + 10][kColW];  // the split's rest
   __shared__ DF red[kOutThreads / 32][6];
-  __shared__ float tmax[kOutThreads / 32][NQ];
   const int sx = blockIdx.x, sg = blockIdx.y, ch = blockIdx.z, c = a.c0 + ch;
   const int x0 = sx * kColW, r0 = sg * kColT;
   const size_t n = (size_t)a.w * a.h;
@@ -548,18 +475,12 @@ __global__ void __launch_bounds__(kOutThreads, 4) k_blur_col_out(ColArgs a) {
                        : 0.0f;
       }
 #pragma unroll
-    for (int q = 0; q < NQ; ++q) {
-      float m = 0.0f;
+    for (int q = 0; q < NQ; ++q)
 #pragma unroll
       for (int it = 0; it < kIt; ++it) {
         const int i = t + it * kOutThreads;
         if (i < kElems) tile[q][i / kColW][i % kColW] = v[q][it];
-        m = fmaxf(m, fabsf(v[q][it]));
       }
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
-      if ((t & 31) == 0) tmax[t >> 5][q] = m;
-    }
   }
   __syncthreads();
   // The ripple in two halves of kColT / 2 rows per column and quantity: each
@@ -615,28 +536,6 @@ __global__ void __launch_bounds__(kOutThreads, 4) k_blur_col_out(ColArgs a) {
     }
   }
   __syncthreads();
-  // The tile's samples split on the tile's grid per quantity (fir_grid2):
-  // the high part in place, the rest in tlo.
-  {
-    float C[NQ];
-#pragma unroll
-    for (int q = 0; q < NQ; ++q) {
-      float m = 0.0f;
-#pragma unroll
-      for (int wi = 0; wi < kOutThreads / 32; ++wi) m = fmaxf(m, tmax[wi][q]);
-      C[q] = grid_const(m);
-    }
-    constexpr int kElems = (kColT + 10) * kColW;
-#pragma unroll
-    for (int q = 0; q < NQ; ++q)
-      for (int i = t; i < kElems; i += kOutThreads) {
-        float& v = tile[q][i / kColW][i % kColW];
-        const float h = (v + C[q]) - C[q];
-        tlo[q][i / kColW][i % kColW] = v - h;
-        v = h;
-      }
-  }
-  __syncthreads();
   // Outputs: columns 2j, 2j+1 (the lanes) of rows kR*b .. kR*b+kR-1.
   constexpr int kR = kColT / (kOutThreads / (kColW / 2));
   const f2 nz = f2_pack(a.nz, a.nz);
@@ -649,13 +548,10 @@ __global__ void __launch_bounds__(kOutThreads, 4) k_blur_col_out(ColArgs a) {
     f2 val[NQ];
 #pragma unroll
     for (int q = 0; q < NQ; ++q) {
-      f2 hh[9], ll[9];
-#pragma unroll
-      for (int k = 0; k < 9; ++k) {
-        hh[k] = *reinterpret_cast<const f2*>(&tile[q][r + 2 + k][lx]);
-        ll[k] = *reinterpret_cast<const f2*>(&tlo[q][r + 2 + k][lx]);
-      }
-      val[q] = fir_grid2(hh, ll, *reinterpret_cast<const f2*>(&rp[q][r][lx]), nz);
+      auto tv = [&](int ly) { return *reinterpret_cast<const f2*>(&tile[q][ly][lx]); };
+      val[q] = fir_exact2(tv(r + 2), tv(r + 3), tv(r + 4), tv(r + 5), tv(r + 6), tv(r + 7),
+                          tv(r + 8), tv(r + 9), tv(r + 10),
+                          *reinterpret_cast<const f2*>(&rp[q][r][lx]), nz);
     }
     if (gy >= a.h || gx >= a.w) continue;
     const bool second = gx + 1 < a.w;
