@@ -727,7 +727,8 @@ def run_ours(args):
     head_scores = scores.cpu().numpy().copy()
     # Every precision mode on the same inputs, and each one's stage times.
     modes, stage_sets = {}, {}
-    for p in PRECISIONS:
+    mode_list = [p for p in PRECISIONS if p in args.modes.split(",") or p == args.precision]
+    for p in mode_list:
         if p == args.precision:
             ms_p, p_scores = ms_max, head_scores
         else:
@@ -740,7 +741,9 @@ def run_ours(args):
                     "ms_per_step": round(ms_p / args.steps, 3),
                     "dct_stages_ms_per_image": round(dct_ms, 4),
                     "scores": [round(float(x), 6) for x in p_scores]}
-    for p in PRECISIONS:
+    for p in mode_list:
+        if "fp32" not in modes:
+            break
         modes[p]["vs_fp32"] = round(modes[p]["value"] / modes["fp32"]["value"], 4)
         modes[p]["dct_stages_vs_fp32"] = round(
             modes["fp32"]["dct_stages_ms_per_image"] / modes[p]["dct_stages_ms_per_image"], 3)
@@ -845,6 +848,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--precision", default="bf16x6", choices=list(PRECISIONS),
                     help="DCT precision of the headline figure")
+    ap.add_argument("--modes", default=",".join(PRECISIONS),
+                    help="precision modes timed besides the headline (comma-separated)")
     # Smaller cases for profiler captures (the headline workload is the default).
     ap.add_argument("--size", type=int, default=None, help="square image side (profiling)")
     ap.add_argument("--images", type=int, default=None, help="images per step (profiling)")
