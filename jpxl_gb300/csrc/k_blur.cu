@@ -292,6 +292,12 @@ __global__ void __launch_bounds__(kRowThreads, 6) k_blur_rows(RowArgs a) {
     Ripple2 rp;
 #pragma unroll
     for (int k = 0; k < 3; ++k) rp.p[k] = rp.q[k] = 0ull;
+    // blur.rs:414 starts the recursion four samples before the line, fed
+    // with 0 + x[0..3]: no rounding, so no ripple, for finite samples, and
+    // NaN through the whole line for a non-finite one.
+    if (t == 0)
+#pragma unroll
+      for (int j = -4; j < 0; ++j) ripple_step2(rp, pair_error2(L(j + 4), L(j + 14)), nz);
 #pragma unroll 4
     for (int j = j0; j < j1; ++j) rip[j] = ripple_step2(rp, pair_error2(L(j + 4), L(j + 14)), nz);
 #pragma unroll
@@ -434,7 +440,20 @@ __global__ void __launch_bounds__(kColW * NQ * 3) k_blur_col_scan(ColArgs a) {
              (size_t)ch * a.nseg * NQ * 6 * a.w + x;
   const size_t off = ((size_t)(qk / 3) * 6 + 2 * k) * a.w;
   const size_t step = (size_t)NQ * 6 * a.w;
+  // The first segment's entry: blur.rs:574 runs the recursion from four rows
+  // before the plane, fed with 0 + rows 0..3 (zero ripple for finite samples,
+  // NaN for the rest of the column from a non-finite one).
   float sp = 0.0f, sq = 0.0f;
+  {
+    const size_t n = (size_t)a.w * a.h;
+    const float* H = a.hpl + ((size_t)ch * NQ + qk / 3) * n + x;
+    for (int i = 0; i < 4 && i < a.h; ++i) {
+      const float e = pair_error(0.0f, __ldg(H + (size_t)i * a.w));
+      const float o = (e * c_blur.a[k] + c_blur.b[k] * sp) - sq;
+      sq = sp;
+      sp = o;
+    }
+  }
 #pragma unroll 8
   for (int sg = 0; sg < a.nseg; ++sg) {
     const float bp = __ldg(C + off + sg * step), bq = __ldg(C + off + sg * step + a.w);
