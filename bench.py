@@ -23,7 +23,8 @@ against the CPU restatement of the reference and against the FP64 truth;
 `scoring` times SSIMULACRA2 on 32 pairs of 4096x3072 RGB8 (source against
 reconstruction); `search` times the batched quality search (64 uneven RGB8
 frames x 8 candidate quantizers = 512 probes in one CUDA graph launch);
-`decode` times the decode of the committed cjxl streams.
+`decode` times 256 cjxl streams decoded to 8-bit sRGB by one graph launch
+and counts the samples 1 DN off djxl's decodes.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 """
@@ -535,54 +536,76 @@ def run_select(ctxs, streams, images, dev_rgb, covers, req, steps, px_total, tor
             "sequential_fallbacks": sum(c.cover_fallbacks for c in ctxs)}
 
 
-DECODE_STREAMS = ("06_gradient_300x200_lossy", "64_vardct_lfgroupseam_rgb_128x2176_nofilters_d6")
+DECODE_WITH_DJXL = ("50_vardct_mixed_gray_128x128_nofilters_d1", "51_vardct_mixed_gray_128x128_nofilters_d4",
+                    "52_vardct_mixed_gray_128x128_filters_d1", "53_vardct_mixed_gray_128x128_filters_d4",
+                    "63_vardct_outofgamut_rgb_64x64_nofilters_d4",
+                    "70_progressive_ac_gray_128x128_nofilters",
+                    "71_qprogressive_ac_gray_128x128_nofilters", "72_lfframe_gray_128x128_nofilters",
+                    "73_progressive_all_gray_128x128_nofilters",
+                    "82_alpha_vardct_rgba_64x64_nofilters",
+                    "109_orientation_transpose_vardct_rgba_64x64")
+DECODE_OTHERS = ("06_gradient_300x200_lossy", "64_vardct_lfgroupseam_rgb_128x2176_nofilters_d6")
+DECODE_N = 256
+
+
+def _quantize_8(np, v):
+    """jpxl-decode decode.rs:3498 quantize_sample at max 255."""
+    s = v.astype(np.float32) * np.float32(255.0)
+    r = np.where(s >= 0, np.floor(s + np.float32(0.5)), np.ceil(s - np.float32(0.5)))
+    return np.where(np.isfinite(r), np.clip(r, 0, 255), 0).astype(np.int32)
 
 
 def run_decode(ctx, reps, np):
-    """Decode of the committed cjxl streams (jpxl-decode decode.rs:400 up to
-    the float output): host parse (headers, TOC, entropy-coded sections),
-    GPU reconstruction from the parsed frame, and both end to end with the
-    pixels back on the host.  The streams are small, so the figures carry
-    per-call overheads; they measure the decode path, not a peak rate."""
+    """Batched decode: the committed cjxl VarDCT streams repeated to 256,
+    rendered to 8-bit sRGB by one graph launch (jpxlg_decode_batch_*).  The
+    host parses every stream (headers, TOC, entropy-coded sections) at open;
+    each graph launch copies the staged coefficients in, renders all 256
+    frames over four lanes and copies the 8-bit pixels back to pinned host
+    memory.  `value` is end to end: parse of all streams plus one graph run,
+    per second.  Against djxl's decodes (the .npy beside 11 of the 13
+    fixtures, quantized as quantize_sample does) the samples 1 DN off are
+    counted."""
     import jpxl_gb300 as jg
 
-    out = {"workload": "cjxl streams " + ", ".join(DECODE_STREAMS) +
-           " (tests/golden/codestream), decoded to float sRGB planes", "unit": "MPix/s",
-           "streams": {}}
-    tot_px = tot_parse = tot_render = tot_e2e = 0.0
-    for name in DECODE_STREAMS:
-        data = (ROOT / "tests" / "golden" / "codestream" / (name + ".jxl")).read_bytes()
-        cs = jg.Codestream(data)
-        px = cs.info["width"] * cs.info["height"]
+    names = DECODE_WITH_DJXL + DECODE_OTHERS
+    order = [names[i % len(names)] for i in range(DECODE_N)]
+    gdir = ROOT / "tests" / "golden" / "codestream"
+    data = {n: (gdir / (n + ".jxl")).read_bytes() for n in names}
+    t0 = time.perf_counter()
+    streams = [jg.Codestream(data[n]) for n in order]
+    parse = time.perf_counter() - t0
+    px = sum(s.info["width"] * s.info["height"] for s in streams)
+    batch = jg.DecodeBatch(ctx, streams, "srgb8")
+    try:
         for _ in range(3):
-            cs.render(ctx, "srgb_float")
+            outs = batch.run()
         t0 = time.perf_counter()
         for _ in range(reps):
-            jg.Codestream(data).close()
-        parse = (time.perf_counter() - t0) / reps
-        t0 = time.perf_counter()
-        for _ in range(reps):
-            cs.render(ctx, "srgb_float")
-        render = (time.perf_counter() - t0) / reps
-        t0 = time.perf_counter()
-        for _ in range(reps):
-            c2 = jg.Codestream(data)
-            c2.render(ctx, "srgb_float")
-            c2.close()
-        e2e = (time.perf_counter() - t0) / reps
-        cs.close()
-        out["streams"][name] = {"pixels": px, "bytes": len(data),
-                                "parse_ms": round(parse * 1e3, 3),
-                                "render_ms": round(render * 1e3, 3),
-                                "e2e_ms": round(e2e * 1e3, 3)}
-        tot_px += px
-        tot_parse += parse
-        tot_render += render
-        tot_e2e += e2e
-    out["value"] = round(tot_px / tot_e2e / 1e6, 2)
-    out["parse_mpix_s"] = round(tot_px / tot_parse / 1e6, 2)
-    out["render_mpix_s"] = round(tot_px / tot_render / 1e6, 2)
-    return out
+            batch.run()
+        graph = (time.perf_counter() - t0) / reps
+        off = samples = worst = 0
+        for n, s, out in zip(order, streams, outs):
+            if n not in DECODE_WITH_DJXL:
+                continue
+            ref = np.load(gdir / (n + ".npy"))[0][:, :, :3]
+            got = out.transpose(1, 0, 2) if s.info["orientation"] == 5 else out
+            got = got[:, :, :ref.shape[2]]  # a grey image's value is plane 0
+            d = np.abs(got.astype(np.int32) - _quantize_8(np, ref))
+            off += int((d > 0).sum())
+            worst = max(worst, int(d.max()))
+            samples += d.size
+    finally:
+        batch.close()
+        for s in streams:
+            s.close()
+    return {"workload": f"{DECODE_N} cjxl VarDCT streams ({len(names)} committed fixtures, "
+                        "tests/golden/codestream, repeated), one graph launch to 8-bit sRGB",
+            "unit": "MPix/s", "streams": DECODE_N, "pixels": px,
+            "value": round(px / (parse + graph) / 1e6, 2),
+            "parse_ms": round(parse * 1e3, 3), "graph_ms": round(graph * 1e3, 3),
+            "parse_mpix_s": round(px / parse / 1e6, 2),
+            "graph_mpix_s": round(px / graph / 1e6, 2),
+            "vs_djxl_8bit": {"samples": samples, "samples_1dn_off": off, "max_dn": worst}}
 
 
 def roofline_of(stages: dict, n_img: int) -> dict:

@@ -383,6 +383,29 @@ int jpxlg_codestream_destroy(jpxlg_codestream* cs);
 int jpxlg_codestream_render(jpxlg_ctx* ctx, const jpxlg_codestream* cs, int out_kind, void* out,
                             uint32_t mem);
 
+/* Batched decode: replaces a loop of jpxl-decode decode() calls
+ * (crates/jpxl-decode/src/decode.rs:400, through decode_vardct_frame :2513
+ * and quantize_sample :3498 for 8-bit output) over many streams with one
+ * graph launch.  jpxlg_decode_batch_create stages every opened stream
+ * (the host's entropy decoding is done at open; here the coefficient image,
+ * LF planes and CfL tiles go into pinned host memory), spreads the streams
+ * over `lanes` internal contexts (0 picks min(n, 4)), renders each once to
+ * size the workspaces, and captures one CUDA graph on ctx's stream: per
+ * stream, the staged planes to the device, LF preparation, the render into
+ * `out_kind` (as jpxlg_codestream_render) and the pixels back to a pinned
+ * host buffer.  The streams must stay open while the batch lives.
+ * jpxlg_decode_batch_run launches the graph; with JPXLG_MEM_HOST it waits
+ * and copies stream i's pixels to outs[i] (host; NULL entries, or outs
+ * NULL, skip the copy); with JPXLG_MEM_DEVICE it queues device-to-device
+ * copies to outs[i] and returns without waiting.  Streams the renderer does
+ * not carry fail creation with JPXLG_ERR_STREAM, naming the stream. */
+typedef struct jpxlg_decode_batch jpxlg_decode_batch;
+int jpxlg_decode_batch_create(jpxlg_ctx* ctx, int n, const jpxlg_codestream* const* streams,
+                              int out_kind, int lanes, jpxlg_decode_batch** out);
+int jpxlg_decode_batch_run(jpxlg_ctx* ctx, jpxlg_decode_batch* batch, void* const* outs,
+                           uint32_t mem);
+int jpxlg_decode_batch_destroy(jpxlg_decode_batch* batch);
+
 /* Allocation-free variant of jpxlg_ssim2_score; it has no counterpart in the
  * reference.  The candidate (device planes) is scored against `ref` using a
  * fixed device scratch inside the library instead of the context's

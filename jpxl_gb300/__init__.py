@@ -615,6 +615,46 @@ class Codestream:
             pass
 
 
+class DecodeBatch:
+    """Many opened streams rendered by one graph launch (jpxlg_decode_batch_*):
+    a loop of decode.rs:400 decode calls as one CUDA graph.  The streams must
+    stay open while the batch lives."""
+
+    KINDS = {"xyb": 0, "linear": 1, "srgb8": 2, "srgb_float": 4}
+
+    def __init__(self, ctx: Context, streams: list, out: str = "srgb8", lanes: int = 0):
+        self.ctx, self.streams, self.out = ctx, list(streams), out
+        arr = (C.c_void_p * len(self.streams))(*[s.handle.value for s in self.streams])
+        h = C.c_void_p()
+        ctx.check(ctx.lib.jpxlg_decode_batch_create(ctx.handle, len(self.streams), arr,
+                                                    self.KINDS[out], lanes, C.byref(h)))
+        self.handle = h
+        self.buffers = []
+        for s in self.streams:
+            w, hh = s.info["width"], s.info["height"]
+            self.buffers.append(np.zeros((hh, w, 3), np.uint8) if out == "srgb8"
+                                else np.zeros((3, hh, w), np.float32))
+        self._outs = (C.c_void_p * len(self.buffers))(*[b.ctypes.data for b in self.buffers])
+
+    def run(self, copy: bool = True) -> list:
+        """Launches the graph and waits; returns every stream's pixels (the
+        same arrays each run) unless copy is False."""
+        self.ctx.check(self.ctx.lib.jpxlg_decode_batch_run(
+            self.ctx.handle, self.handle, self._outs if copy else None, MEM_HOST))
+        return self.buffers
+
+    def close(self):
+        if getattr(self, "handle", None):
+            self.ctx.lib.jpxlg_decode_batch_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 def score_pair(ctx: Context, ref_rgb: np.ndarray, cand_rgb: np.ndarray) -> float:
     """jpxl-perceptual lib.rs:195 score_pair on linear [3, H, W] planes."""
     a = np.ascontiguousarray(ref_rgb, dtype=np.float32)

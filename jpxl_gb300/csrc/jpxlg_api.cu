@@ -4,6 +4,7 @@
 #include <algorithm>
 #include <cstdarg>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <memory>
@@ -1414,9 +1415,40 @@ extern "C" int jpxlg_ssim2_score_static(jpxlg_ctx* ctx, const jpxlg_ref* ref,
 // reconstructed by the same kernels as a plan (decode.rs:2700-3061).
 // ---------------------------------------------------------------------------
 
-extern "C" int jpxlg_codestream_render(jpxlg_ctx* ctx, const jpxlg_codestream* cs, int out_kind,
-                                       void* out, uint32_t mem) {
-  if (!ctx || !cs || !out) return fail(ctx, JPXLG_ERR_ARGUMENT, "null argument");
+namespace {
+
+// A parsed VarDCT frame staged for the GPU render: its layout and
+// parameters, and in one host block (pinned for batches) the coefficient
+// image, the LF planes, the CfL tiles and (an LF frame) the LF XYB planes.
+struct DecodeStage {
+  jpxlg_layout* L = nullptr;
+  jpxlg_params p{};
+  size_t n = 0, n8 = 0, nb = 0, nt = 0;
+  void* host = nullptr;
+  bool pinned = false;
+  int32_t* q = nullptr;
+  int32_t* lfq = nullptr;
+  int8_t* cflx = nullptr;
+  int8_t* cflb = nullptr;
+  float* lf_frame = nullptr;  // 3 * nb, or null
+  float m[3] = {0, 0, 0};
+  float kx = 0, kb = 1, div = 1;
+  bool smooth = false;
+  int fx = 128, fb = 128;
+  DecodeStage() = default;
+  DecodeStage(const DecodeStage&) = delete;
+  DecodeStage& operator=(const DecodeStage&) = delete;
+  ~DecodeStage() {
+    if (L) jpxlg_layout_destroy(L);
+    if (pinned) cudaFreeHost(host);
+    else std::free(host);
+  }
+};
+
+// Checks that the renderer carries everything the frame uses, and stages
+// it (host work only: the coefficient image from the parsed groups).
+int decode_stage(jpxlg_ctx* ctx, const jpxlg_codestream* cs, int out_kind, bool pinned,
+                 DecodeStage& st) {
   if (out_kind < 0 || out_kind > 4 || out_kind == JPXLG_OUT_LINEAR_DEPTH)
     return fail(ctx, JPXLG_ERR_ARGUMENT, "bad out_kind");
   const jpxlg::cs::Decoded& d = cs->d;
@@ -1444,74 +1476,260 @@ extern "C" int jpxlg_codestream_render(jpxlg_ctx* ctx, const jpxlg_codestream* c
     return fail(ctx, JPXLG_ERR_STREAM, "only XYB frames with the default opsin matrix");
   if (out_kind == JPXLG_OUT_SRGB_FLOAT && d.image.transfer != 13)
     return fail(ctx, JPXLG_ERR_STREAM, "only the sRGB transfer function is carried");
-  cudaSetDevice(ctx->device);
+  CK(cudaSetDevice(ctx->device));
   const int W = (int)f.width, H = (int)f.height;
-  jpxlg_layout* raw = nullptr;
   int rc = jpxlg_layout_create(ctx, W, H, v.block_map.data(), v.hf_mul.data(),
-                               v.sharpness.data(), &raw);
+                               v.sharpness.data(), &st.L);
   if (rc) return rc;
-  std::unique_ptr<jpxlg_layout, int (*)(jpxlg_layout*)> L(raw, jpxlg_layout_destroy);
-  const Geo& g = L->geo;
+  const Geo& g = st.L->geo;
   if ((uint32_t)g.tw != v.tiles_w || (uint32_t)g.th != v.tiles_h)
     return fail(ctx, JPXLG_ERR_ARGUMENT, "CfL tile grid mismatch");
-  jpxlg_params p{};
-  p.global_scale = v.global_scale;
-  p.quant_lf = v.quant_lf;
-  p.x_qm_scale = f.x_qm_scale;
-  p.b_qm_scale = f.b_qm_scale;
-  p.gaborish = f.gab ? 1u : 0u;
-  p.epf_iters = f.epf_iters;
-  if ((rc = check_params(ctx, &p))) return rc;
-  const size_t n = (size_t)g.w * g.h, n8 = (size_t)g.W8 * g.H8, nb = (size_t)g.bw * g.bh;
-  const size_t nt = (size_t)g.tw * g.th;
-  std::vector<int32_t> qimg(3 * n8);
-  if ((rc = jpxlg_codestream_coefficients(cs, qimg.data()))) return rc;
-  std::vector<int32_t> lfq(3 * nb);
-  for (int c = 0; c < 3; ++c) std::copy(v.lf[c].begin(), v.lf[c].end(), lfq.begin() + c * nb);
-  CK(ctx->qcoeff.ensure(3 * n8 * sizeof(int32_t)));
-  CK(ctx->lfq.ensure(3 * nb * sizeof(int32_t)));
-  CK(ctx->cflx.ensure(nt));
-  CK(ctx->cflb.ensure(nt));
-  CK(ctx->lfs.ensure(3 * nb * sizeof(float)));
-  CK(ctx->aux.ensure(3 * std::max(n, nb) * sizeof(float)));
-  CK(cudaMemcpyAsync(ctx->qcoeff.p, qimg.data(), 3 * n8 * sizeof(int32_t), cudaMemcpyHostToDevice,
-                     ctx->stream));
-  CK(cudaMemcpyAsync(ctx->lfq.p, lfq.data(), 3 * nb * sizeof(int32_t), cudaMemcpyHostToDevice,
-                     ctx->stream));
-  CK(cudaMemcpyAsync(ctx->cflx.p, v.x_from_y.data(), nt, cudaMemcpyHostToDevice, ctx->stream));
-  CK(cudaMemcpyAsync(ctx->cflb.p, v.b_from_y.data(), nt, cudaMemcpyHostToDevice, ctx->stream));
-  // LF multipliers (quantizer.rs:232): 65536 * (m_lf / 128) / (gs * quant_lf) in f64.
-  float m[3];
-  const double denom = (double)v.global_scale * (double)v.quant_lf;
-  for (int c = 0; c < 3; ++c) m[c] = (float)(65536.0 * (double)(v.m_lf[c] / 128.0f) / denom);
-  const float kx = 0.0f + (float)v.x_factor_lf / 84.0f;
-  const float kb = 1.0f + (float)v.b_factor_lf / 84.0f;
-  if (v.lf_from_frame) {
-    // The LF frame's XYB is the LF as it stands (no CfL, no smoothing).
-    for (int c = 0; c < 3; ++c) {
-      if (v.lf_frame[c].size() != nb) return fail(ctx, JPXLG_ERR_STREAM, "LF frame size");
-      CK(cudaMemcpyAsync(ctx->lfs.as<float>() + c * nb, v.lf_frame[c].data(), nb * sizeof(float),
-                         cudaMemcpyHostToDevice, ctx->stream));
-    }
-  } else {
-    const bool smooth = (f.flags & 128) == 0;
-    launch_lf_prepare(ctx->lfq.as<int32_t>(), g.bw, g.bh, m, (float)(1u << v.extra_precision),
-                      kx, kb, smooth, ctx->aux.as<float>(), ctx->lfs.as<float>(), ctx->num_sms,
-                      ctx->stream);
-    if ((rc = after_launch(ctx, smooth ? 2 : 1))) return rc;
+  st.p.global_scale = v.global_scale;
+  st.p.quant_lf = v.quant_lf;
+  st.p.x_qm_scale = f.x_qm_scale;
+  st.p.b_qm_scale = f.b_qm_scale;
+  st.p.gaborish = f.gab ? 1u : 0u;
+  st.p.epf_iters = f.epf_iters;
+  if ((rc = check_params(ctx, &st.p))) return rc;
+  st.n = (size_t)g.w * g.h;
+  st.n8 = (size_t)g.W8 * g.H8;
+  st.nb = (size_t)g.bw * g.bh;
+  st.nt = (size_t)g.tw * g.th;
+  if (v.lf_from_frame)
+    for (int c = 0; c < 3; ++c)
+      if (v.lf_frame[c].size() != st.nb) return fail(ctx, JPXLG_ERR_STREAM, "LF frame size");
+  const size_t qb = 3 * st.n8 * sizeof(int32_t), lb = 3 * st.nb * sizeof(int32_t);
+  const size_t fb = v.lf_from_frame ? 3 * st.nb * sizeof(float) : 0;
+  const size_t bytes = qb + lb + fb + 2 * st.nt;
+  st.pinned = pinned;
+  if (pinned) CK(cudaMallocHost(&st.host, bytes));
+  else if (!(st.host = std::malloc(bytes)))
+    return fail(ctx, JPXLG_ERR_CUDA, "host staging of %zu bytes", bytes);
+  char* h = (char*)st.host;
+  st.q = (int32_t*)h;
+  st.lfq = (int32_t*)(h + qb);
+  st.lf_frame = fb ? (float*)(h + qb + lb) : nullptr;
+  st.cflx = (int8_t*)(h + qb + lb + fb);
+  st.cflb = st.cflx + st.nt;
+  if ((rc = jpxlg_codestream_coefficients(cs, st.q))) return rc;
+  for (int c = 0; c < 3; ++c) {
+    std::copy(v.lf[c].begin(), v.lf[c].end(), st.lfq + c * st.nb);
+    if (st.lf_frame) std::copy(v.lf_frame[c].begin(), v.lf_frame[c].end(), st.lf_frame + c * st.nb);
   }
-  const size_t out_bytes = out_kind == JPXLG_OUT_SRGB8 ? 3 * n : 3 * n * sizeof(float);
+  std::copy(v.x_from_y.begin(), v.x_from_y.begin() + st.nt, st.cflx);
+  std::copy(v.b_from_y.begin(), v.b_from_y.begin() + st.nt, st.cflb);
+  // LF multipliers (quantizer.rs:232): 65536 * (m_lf / 128) / (gs * quant_lf) in f64.
+  const double denom = (double)v.global_scale * (double)v.quant_lf;
+  for (int c = 0; c < 3; ++c) st.m[c] = (float)(65536.0 * (double)(v.m_lf[c] / 128.0f) / denom);
+  st.kx = 0.0f + (float)v.x_factor_lf / 84.0f;
+  st.kb = 1.0f + (float)v.b_factor_lf / 84.0f;
+  st.div = (float)(1u << v.extra_precision);
+  st.smooth = (f.flags & 128) == 0;
+  st.fx = v.x_factor_lf + 128;
+  st.fb = v.b_factor_lf + 128;
+  return JPXLG_OK;
+}
+
+// Queues a staged frame's render on ctx's stream: the staged planes to the
+// device, the LF image (dequantized, CfL'd and smoothed, or the LF frame's
+// XYB as it stands), then the render into out_dev.  No allocation once the
+// context's buffers have grown to the frame.
+int decode_enqueue(jpxlg_ctx* ctx, const DecodeStage& st, int out_kind, void* out_dev) {
+  const Geo& g = st.L->geo;
+  CK(ctx->qcoeff.ensure(3 * st.n8 * sizeof(int32_t)));
+  CK(ctx->lfq.ensure(3 * st.nb * sizeof(int32_t)));
+  CK(ctx->cflx.ensure(st.nt));
+  CK(ctx->cflb.ensure(st.nt));
+  CK(ctx->lfs.ensure(3 * st.nb * sizeof(float)));
+  CK(ctx->aux.ensure(3 * std::max(st.n, st.nb) * sizeof(float)));
+  CK(cudaMemcpyAsync(ctx->qcoeff.p, st.q, 3 * st.n8 * sizeof(int32_t), cudaMemcpyHostToDevice,
+                     ctx->stream));
+  CK(cudaMemcpyAsync(ctx->lfq.p, st.lfq, 3 * st.nb * sizeof(int32_t), cudaMemcpyHostToDevice,
+                     ctx->stream));
+  CK(cudaMemcpyAsync(ctx->cflx.p, st.cflx, st.nt, cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(ctx->cflb.p, st.cflb, st.nt, cudaMemcpyHostToDevice, ctx->stream));
+  int rc;
+  if (st.lf_frame) {
+    CK(cudaMemcpyAsync(ctx->lfs.p, st.lf_frame, 3 * st.nb * sizeof(float),
+                       cudaMemcpyHostToDevice, ctx->stream));
+  } else {
+    launch_lf_prepare(ctx->lfq.as<int32_t>(), g.bw, g.bh, st.m, st.div, st.kx, st.kb, st.smooth,
+                      ctx->aux.as<float>(), ctx->lfs.as<float>(), ctx->num_sms, ctx->stream);
+    if ((rc = after_launch(ctx, st.smooth ? 2 : 1))) return rc;
+  }
+  return render_device(ctx, st.L, ctx->qcoeff.as<int32_t>(), ctx->lfq.as<int32_t>(),
+                       ctx->cflx.as<int8_t>(), ctx->cflb.as<int8_t>(), st.fx, st.fb, nullptr,
+                       &st.p, out_kind, 8, out_dev, nullptr, ctx->lfs.as<float>());
+}
+
+size_t decode_out_bytes(const DecodeStage& st, int out_kind) {
+  return out_kind == JPXLG_OUT_SRGB8 ? 3 * st.n : 3 * st.n * sizeof(float);
+}
+
+}  // namespace
+
+extern "C" int jpxlg_codestream_render(jpxlg_ctx* ctx, const jpxlg_codestream* cs, int out_kind,
+                                       void* out, uint32_t mem) {
+  if (!ctx || !cs || !out) return fail(ctx, JPXLG_ERR_ARGUMENT, "null argument");
+  DecodeStage st;
+  int rc = decode_stage(ctx, cs, out_kind, false, st);
+  if (rc) return rc;
+  const size_t out_bytes = decode_out_bytes(st, out_kind);
   void* dst = out;
   if (mem != JPXLG_MEM_DEVICE) {
     CK(ctx->out.ensure(out_bytes));
     dst = ctx->out.p;
   }
-  rc = render_device(ctx, L.get(), ctx->qcoeff.as<int32_t>(), ctx->lfq.as<int32_t>(),
-                     ctx->cflx.as<int8_t>(), ctx->cflb.as<int8_t>(), v.x_factor_lf + 128,
-                     v.b_factor_lf + 128, nullptr, &p, out_kind, 8, dst, nullptr,
-                     ctx->lfs.as<float>());
-  if (rc) return rc;
+  if ((rc = decode_enqueue(ctx, st, out_kind, dst))) return rc;
   if (mem != JPXLG_MEM_DEVICE)
     CK(cudaMemcpyAsync(out, ctx->out.p, out_bytes, cudaMemcpyDeviceToHost, ctx->stream));
   return sync_and_check(ctx);
+}
+
+// ---------------------------------------------------------------------------
+// Batched decode: many parsed streams rendered by one graph launch.
+// ---------------------------------------------------------------------------
+
+struct jpxlg_decode_batch {
+  jpxlg_ctx* owner = nullptr;
+  int device = 0;
+  int out_kind = 0;
+  std::vector<jpxlg_ctx*> lanes;
+  std::vector<std::unique_ptr<DecodeStage>> items;
+  std::vector<size_t> out_bytes, out_off;
+  uint8_t* d_out = nullptr;  // every item's pixels, back to back
+  uint8_t* h_out = nullptr;  // pinned mirror, filled inside the graph
+  cudaEvent_t fork = nullptr;
+  std::vector<cudaEvent_t> joins;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+};
+
+namespace {
+
+void decode_batch_free(jpxlg_decode_batch* b) {
+  if (!b) return;
+  if (b->exec) cudaGraphExecDestroy(b->exec);
+  if (b->graph) cudaGraphDestroy(b->graph);
+  if (b->fork) cudaEventDestroy(b->fork);
+  for (cudaEvent_t e : b->joins) cudaEventDestroy(e);
+  b->items.clear();
+  for (jpxlg_ctx* l : b->lanes) jpxlg_ctx_destroy(l);
+  cudaFree(b->d_out);
+  cudaFreeHost(b->h_out);
+  delete b;
+}
+
+// Item i on lane i % lanes: its render, then its pixels to the pinned mirror.
+int decode_batch_enqueue(jpxlg_ctx* ctx, jpxlg_decode_batch* b) {
+  const size_t L = b->lanes.size();
+  for (size_t i = 0; i < b->items.size(); ++i) {
+    jpxlg_ctx* lane = b->lanes[i % L];
+    int rc = decode_enqueue(lane, *b->items[i], b->out_kind, b->d_out + b->out_off[i]);
+    if (rc) return fail(ctx, rc, "decode batch item %zu: %s", i, lane->last_error.c_str());
+    CK(cudaMemcpyAsync(b->h_out + b->out_off[i], b->d_out + b->out_off[i], b->out_bytes[i],
+                       cudaMemcpyDeviceToHost, lane->stream));
+  }
+  return JPXLG_OK;
+}
+
+int decode_batch_check(jpxlg_ctx* ctx, jpxlg_decode_batch* b) {
+  for (jpxlg_ctx* lane : b->lanes) {
+    int rc = sync_and_check(lane);
+    if (rc) return fail(ctx, rc, "decode batch lane: %s", lane->last_error.c_str());
+  }
+  return JPXLG_OK;
+}
+
+}  // namespace
+
+extern "C" int jpxlg_decode_batch_create(jpxlg_ctx* ctx, int n, const jpxlg_codestream* const* streams,
+                                         int out_kind, int lanes, jpxlg_decode_batch** out) {
+  if (!ctx || !streams || !out || n <= 0) return fail(ctx, JPXLG_ERR_ARGUMENT, "null argument");
+  *out = nullptr;
+  if (out_kind < 0 || out_kind > 4 || out_kind == JPXLG_OUT_LINEAR_DEPTH)
+    return fail(ctx, JPXLG_ERR_ARGUMENT, "bad out_kind");
+  for (int i = 0; i < n; ++i)
+    if (!streams[i]) return fail(ctx, JPXLG_ERR_ARGUMENT, "stream %d: null", i);
+  if (lanes <= 0) lanes = std::min(n, 4);
+  lanes = std::min(lanes, n);
+  CK(cudaSetDevice(ctx->device));
+  std::unique_ptr<jpxlg_decode_batch, void (*)(jpxlg_decode_batch*)> b(new jpxlg_decode_batch,
+                                                                       decode_batch_free);
+  b->owner = ctx;
+  b->device = ctx->device;
+  b->out_kind = out_kind;
+  size_t total = 0;
+  for (int i = 0; i < n; ++i) {
+    b->items.emplace_back(new DecodeStage);
+    int rc = decode_stage(ctx, streams[i], out_kind, true, *b->items.back());
+    if (rc) return fail(ctx, rc, "decode batch stream %d: %s", i, ctx->last_error.c_str());
+    const size_t bytes = decode_out_bytes(*b->items.back(), out_kind);
+    total = (total + 255) & ~(size_t)255;
+    b->out_off.push_back(total);
+    b->out_bytes.push_back(bytes);
+    total += bytes;
+  }
+  for (int l = 0; l < lanes; ++l) {
+    jpxlg_ctx* lane = nullptr;
+    int rc = jpxlg_ctx_create(ctx->device, 0, &lane);
+    if (rc) return fail(ctx, rc, "decode batch lane %d: context creation failed", l);
+    b->lanes.push_back(lane);
+    cudaEvent_t e = nullptr;
+    CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    b->joins.push_back(e);
+  }
+  CK(cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming));
+  CK(cudaMalloc(&b->d_out, total));
+  CK(cudaMallocHost(&b->h_out, total));
+  // Warm-up: the lanes' buffers grow to their largest frame here.
+  int rc = decode_batch_enqueue(ctx, b.get());
+  if (rc) return rc;
+  if ((rc = decode_batch_check(ctx, b.get()))) return rc;
+  CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+  cudaEventRecord(b->fork, ctx->stream);
+  for (jpxlg_ctx* lane : b->lanes) cudaStreamWaitEvent(lane->stream, b->fork, 0);
+  rc = decode_batch_enqueue(ctx, b.get());
+  for (size_t l = 0; l < b->lanes.size(); ++l) {
+    cudaEventRecord(b->joins[l], b->lanes[l]->stream);
+    cudaStreamWaitEvent(ctx->stream, b->joins[l], 0);
+  }
+  cudaError_t ce = cudaStreamEndCapture(ctx->stream, &b->graph);
+  if (rc) return rc;
+  if (ce != cudaSuccess)
+    return fail(ctx, JPXLG_ERR_CUDA, "decode batch capture: %s", cudaGetErrorString(ce));
+  CK(cudaGraphInstantiate(&b->exec, b->graph, 0));
+  *out = b.release();
+  return JPXLG_OK;
+}
+
+extern "C" int jpxlg_decode_batch_run(jpxlg_ctx* ctx, jpxlg_decode_batch* b, void* const* outs,
+                                      uint32_t mem) {
+  if (!ctx || !b) return fail(ctx, JPXLG_ERR_ARGUMENT, "null argument");
+  if (b->owner != ctx) return fail(ctx, JPXLG_ERR_ARGUMENT, "batch belongs to another context");
+  CK(cudaSetDevice(ctx->device));
+  CK(cudaGraphLaunch(b->exec, ctx->stream));
+  if (mem == JPXLG_MEM_DEVICE) {
+    if (outs)
+      for (size_t i = 0; i < b->items.size(); ++i)
+        if (outs[i])
+          CK(cudaMemcpyAsync(outs[i], b->d_out + b->out_off[i], b->out_bytes[i],
+                             cudaMemcpyDeviceToDevice, ctx->stream));
+    return JPXLG_OK;
+  }
+  CK(cudaStreamSynchronize(ctx->stream));
+  int rc = decode_batch_check(ctx, b);
+  if (rc) return rc;
+  if (outs)
+    for (size_t i = 0; i < b->items.size(); ++i)
+      if (outs[i]) std::memcpy(outs[i], b->h_out + b->out_off[i], b->out_bytes[i]);
+  return JPXLG_OK;
+}
+
+extern "C" int jpxlg_decode_batch_destroy(jpxlg_decode_batch* b) {
+  if (!b) return JPXLG_ERR_ARGUMENT;
+  cudaSetDevice(b->device);
+  cudaDeviceSynchronize();
+  decode_batch_free(b);
+  return JPXLG_OK;
 }
