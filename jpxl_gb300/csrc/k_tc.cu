@@ -557,7 +557,7 @@ __global__ void __launch_bounds__(kThreads) k_render_tc(RenderArgs a,
   end(st, &mbar, a.err);
 }
 
-int g_tc_ctas_per_sm = 3;
+int g_tc_ctas_per_sm = 4;  // four 128-column TMEM allocations fill an SM's 512
 
 template <typename K>
 cudaError_t set_smem(K kernel, int bytes) {
