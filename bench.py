@@ -22,7 +22,8 @@ copy of each image and the D2H read of each score inside the timed region).
 against the CPU restatement of the reference and against the FP64 truth;
 `scoring` times SSIMULACRA2 on 32 pairs of 4096x3072 RGB8 (source against
 reconstruction); `search` times the batched quality search (64 uneven RGB8
-frames x 8 candidate quantizers = 512 probes in one CUDA graph launch);
+frames x 8 candidate quantizers = 512 probes in one CUDA graph launch) and,
+under `navigate`, the quality controller's own search over the same frames;
 `decode` times 256 cjxl streams decoded to 8-bit sRGB by one graph launch
 and counts the samples 1 DN off djxl's decodes.
 
@@ -62,7 +63,27 @@ GROUP_BYTES_PER_PX = {"encode": 18.2, "reconstruct": 24.2, "ssim": 60.0}
 STAGE_GROUP = {"xyb": "encode", "precondition": "encode", "fdct_luma": "encode", "cfl": "encode",
                "quant_chroma": "encode", "render_varblocks": "reconstruct",
                "gaborish": "reconstruct", "epf": "reconstruct", "colour": "reconstruct",
-               "ssim": "ssim"}
+               "ssim": "ssim", "ssim_rows": "ssim", "ssim_col_ripple": "ssim",
+               "ssim_col_out": "ssim"}
+# The metric's blur kernels, each timed under its own stage: algorithmic bytes
+# per pixel of every pyramid scale (f32 planes read and written once):
+# k_blur_rows<3> reads the candidate's and the reference's positive XYB and
+# writes the nine row-pass planes (15 planes); k_blur_col_local<3> and
+# k_blur_col_scan<3> read the nine (9); k_blur_col_out<3> reads the nine and
+# the reference's mu, sigma11 and XYB and the candidate's XYB (21).
+KERNEL_STAGES = {"ssim_rows": ("k_blur_rows<3>", 60.0),
+                 "ssim_col_ripple": ("k_blur_col_local<3> + k_blur_col_scan<3>", 36.0),
+                 "ssim_col_out": ("k_blur_col_out<3>", 84.0)}
+
+
+def pyramid_pixels(w: int, h: int) -> int:
+    """Pixels over SSIMULACRA2's scales (halving, rounded up, while 8x8 fits;
+    at most six)."""
+    total, s = 0, 0
+    while s < 6 and w >= 8 and h >= 8:
+        total += w * h
+        w, h, s = (w + 1) // 2, (h + 1) // 2, s + 1
+    return total
 
 
 def shard_units(units: list, rank: int, world: int) -> list:
@@ -414,12 +435,46 @@ def run_search(ctx, torch, np, steps, precisions):
             "frames_meeting_threshold": sum(c is not None for c in chosen),
             "chosen_global_scale": {str(gs): chosen.count(gs) for gs in SEARCH_CANDIDATES}}
     result["value"] = result[precisions[0]]["value"]
+    result["navigate"] = run_navigate(ctx, frames, [(ref, dev) for _, ref, dev in keep
+                                                    if ref is not None], np)
     for layout, ref, _ in keep:
         if ref is not None:
             ref.close()
         if layout is not None:
             layout.close()
     return result
+
+
+def run_navigate(ctx, frames, refs_devs, np):
+    """The quality controller's own search (jpxl_gb300.quality: the baseline
+    solve of search_frame_perceptual, Balanced budget) over the same frames
+    toward the same threshold, every frame starting at global scale 40000:
+    the frames navigate in lockstep, one jpxlg batch per round.  Timed on
+    the host clock (cover selection, batch creation and every round)."""
+    from jpxl_gb300 import quality as q
+
+    sframes = [q.SearchFrame(rgb, dev.data_ptr(), ref, 8)
+               for rgb, (ref, dev) in zip(frames, refs_devs)]
+    starts = [q.rung_for_global_scale(40000)] * len(frames)
+    t0 = time.perf_counter()
+    prober = q.BatchedProber(ctx, sframes)
+    outs = q.search(prober, starts, SEARCH_THRESHOLD, "balanced",
+                    quant_lf=prober.request.quant_lf)
+    sec = time.perf_counter() - t0
+    px = sum(rgb.shape[0] * rgb.shape[1] * len(o.probes) for rgb, o in zip(frames, outs))
+    statuses = {}
+    for o in outs:
+        statuses[o.status] = statuses.get(o.status, 0) + 1
+    gs = sorted(o.quantizer.global_scale for o in outs)
+    return {"workload": f"{len(frames)} frames, target {SEARCH_THRESHOLD}, Balanced budget, "
+                        "start at global scale 40000",
+            "ms": round(sec * 1e3, 1), "rounds": prober.batches, "probes": prober.probes,
+            "probes_per_frame": round(prober.probes / len(frames), 2),
+            "frames_per_s": round(len(frames) / sec, 2),
+            "probed_mpix_s": round(px / sec / 1e6, 2),
+            "frames_meeting_target": sum(o.score >= SEARCH_THRESHOLD for o in outs),
+            "statuses": statuses,
+            "chosen_global_scale": {"min": gs[0], "median": gs[len(gs) // 2], "max": gs[-1]}}
 
 
 SCORING_ORIGINALS = 2
@@ -609,10 +664,11 @@ def run_decode(ctx, reps, np):
 
 
 def roofline_of(stages: dict, n_img: int) -> dict:
-    """Achieved HBM bandwidth of each part of the path (algorithmic bytes per
-    source pixel x pixels, over the part's CUDA-event time on one stream),
-    the dominant part's fraction of the measured copy bandwidth, and the DRAM
-    traffic per probe from the committed ncu capture."""
+    """The dominant kernel's achieved HBM bandwidth (its algorithmic bytes
+    per launch over its CUDA-event time on one stream) as a fraction of the
+    measured copy bandwidth, with its DRAM traffic per probe from the
+    committed ncu capture; `parts` gives the same for the path's three parts
+    (SURVEY's bytes per source pixel)."""
     peak, peak_kind = measured_peaks()
     px = W * H * n_img
     groups = {}
@@ -627,21 +683,44 @@ def roofline_of(stages: dict, n_img: int) -> dict:
         parts[g] = {"bytes_per_px": GROUP_BYTES_PER_PX[g], "ms_per_probe": round(ms / n_img, 4),
                     "achieved": round(achieved, 1), "frac": round(achieved / peak, 4),
                     "launches_per_probe": launches // max(n_img, 1)}
-    top = max(parts, key=lambda g: parts[g]["ms_per_probe"])
-    traffic, basis = None, None
     tf = ROOT / "profiles" / "traffic_probe_2048x2048_rgb16.json"
-    if tf.exists() and (W, H) == (2048, 2048):
-        t = json.loads(tf.read_text())
-        traffic = t["groups"].get(top)
-        basis = t["source"]
+    cap = json.loads(tf.read_text()) if tf.exists() and (W, H) == (2048, 2048) else None
+    if cap:
         for g in parts:
-            parts[g]["traffic_per_probe"] = t["groups"].get(g)
-    return {"kernel": f"{top} stage ({parts[top]['launches_per_probe']} launches per probe)",
-            "bound": "hbm", "achieved": parts[top]["achieved"], "peak": peak, "unit": "GB/s",
-            "frac": parts[top]["frac"], "peak_kind": peak_kind,
-            "algorithmic_bytes_per_probe": int(GROUP_BYTES_PER_PX[top] * W * H),
-            "traffic": traffic, "traffic_unit": "bytes per probe (DRAM read + write, ncu)",
-            "traffic_basis": basis, "parts": parts}
+            parts[g]["traffic_per_probe"] = cap["groups"].get(g)
+    ppx = pyramid_pixels(W, H)
+    kernels = {}
+    for st, (name, bpp) in KERNEL_STAGES.items():
+        ms, launches = stages.get(st, (0.0, 0))
+        if ms <= 0 or launches <= 0:
+            continue
+        per_launch_bytes = bpp * ppx * n_img / launches
+        achieved = bpp * ppx * n_img / (ms / 1e3) / 1e9
+        kernels[st] = {"kernel": name, "bytes_per_px": bpp,
+                       "launches_per_probe": launches // max(n_img, 1),
+                       "us_per_launch": round(ms * 1e3 / launches, 2),
+                       "algorithmic_bytes_per_launch": int(per_launch_bytes),
+                       "achieved": round(achieved, 1), "frac": round(achieved / peak, 4),
+                       "traffic_per_probe": (cap or {}).get("kernels", {}).get(st)}
+    if not kernels:
+        top = max(parts, key=lambda g: parts[g]["ms_per_probe"])
+        return {"kernel": f"{top} stage", "bound": "hbm", "achieved": parts[top]["achieved"],
+                "peak": peak, "unit": "GB/s", "frac": parts[top]["frac"],
+                "peak_kind": peak_kind, "traffic": None, "parts": parts}
+    top = max(kernels, key=lambda k: stages[k][0])
+    kt = kernels[top]
+    return {"kernel": f"{kt['kernel']} ({kt['launches_per_probe']} launches per probe, every "
+                      "pyramid scale)",
+            "bound": "hbm", "achieved": kt["achieved"], "peak": peak, "unit": "GB/s",
+            "frac": kt["frac"], "peak_kind": peak_kind,
+            "algorithmic_bytes_per_launch": kt["algorithmic_bytes_per_launch"],
+            "traffic": (int(kt["traffic_per_probe"] / kt["launches_per_probe"])
+                        if kt["traffic_per_probe"] and kt["launches_per_probe"] else None),
+            "traffic_unit": "bytes per launch, the mean over one probe's launches (DRAM read + "
+                            "write, ncu)",
+            "traffic_basis": (cap or {}).get("source"),
+            "limiter": "FP32 pipe (double-float FIR), see profiles/",
+            "kernels": kernels, "parts": parts}
 
 
 def run_ours(args):

@@ -174,7 +174,10 @@ enum {
   JPXLG_STAGE_GABORISH,         /* R2 */
   JPXLG_STAGE_EPF,              /* R3, all steps */
   JPXLG_STAGE_COLOUR,           /* R4 */
-  JPXLG_STAGE_SSIM,             /* S1-S5 candidate side */
+  JPXLG_STAGE_SSIM,             /* S1-S5 candidate side, but for the three below */
+  JPXLG_STAGE_SSIM_ROWS,        /* S3 blur row pass (every scale) */
+  JPXLG_STAGE_SSIM_COL_RIPPLE,  /* S3 blur column ripple: segment responses, entry states */
+  JPXLG_STAGE_SSIM_COL_OUT,     /* S3/S4 blur column outputs with the per-pixel terms */
   JPXLG_STAGE_COUNT
 };
 int jpxlg_stage_timing(jpxlg_ctx* ctx, int enable);

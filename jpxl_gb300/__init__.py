@@ -23,6 +23,10 @@ this package                   reference (JPXL, crates/...)
 ``BatchProbe``                 the candidate sweep of search_frame_perceptual
                                (quality.rs:2405) over evaluate (evaluator.rs:295),
                                as one CUDA graph
+``quality.search``             search_frame_perceptual's baseline solve
+                               (quality.rs:1775) over BatchProbe rounds
+``Codestream``                 jpxl-decode decode.rs:400 up to the frame content
+``DecodeBatch``                a loop of decode.rs:400 decode calls as one graph
 =============================  ==================================================
 
 Arrays are numpy (host memory) unless stated; the ``*_device`` variants take
@@ -57,7 +61,7 @@ ORIGIN = 0x80
 
 # JPXLG_STAGE_* order (include/jpxlg.h).
 STAGES = ("xyb", "precondition", "fdct_luma", "cfl", "quant_chroma", "render_varblocks",
-          "gaborish", "epf", "colour", "ssim")
+          "gaborish", "epf", "colour", "ssim", "ssim_rows", "ssim_col_ripple", "ssim_col_out")
 
 
 # jpxlg_params.precision (include/jpxlg.h JPXLG_PRECISION_*)

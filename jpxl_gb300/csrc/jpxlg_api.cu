@@ -168,6 +168,19 @@ void stage_end(jpxlg_ctx* ctx) {
   ctx->open_stage = -1;
 }
 
+// The blur kernels of one SSIMULACRA2 scale, each under its own stage: the
+// row pass, the column ripple, the column outputs; the rest of the metric
+// (positive XYB, downscaling, the final sums) stays under JPXLG_STAGE_SSIM.
+void ssim_stage_hook(void* user, int part) {
+  jpxlg_ctx* ctx = static_cast<jpxlg_ctx*>(user);
+  static const int kNext[4] = {JPXLG_STAGE_SSIM_ROWS, JPXLG_STAGE_SSIM_COL_RIPPLE,
+                               JPXLG_STAGE_SSIM_COL_OUT, JPXLG_STAGE_SSIM};
+  static const int kLaunched[4] = {0, 1, 2, 1};  // the kernels since the previous part
+  ctx->launches += kLaunched[part];
+  stage_end(ctx);
+  stage_begin(ctx, kNext[part]);
+}
+
 int after_launch(jpxlg_ctx* ctx, uint64_t n) {
   ctx->launches += n;
   cudaError_t e = cudaGetLastError();
@@ -485,8 +498,7 @@ int score_device(jpxlg_ctx* ctx, const jpxlg_ref* ref, const float* cand_dev,
       next += 6 * ns;
     }
     ctas[s] = launch_score_scale(cur_xyb, rs, ctx->hpl.as<float>(), ctx->bcarry.as<float>(), 0,
-                                 3, part, ctx->stream);
-    k += 4;
+                                 3, part, ctx->stream, ssim_stage_hook, ctx);  // counts its 4
     pixels[s] = rs.w * rs.h;
     part += (size_t)ctas[s] * 18;
   }

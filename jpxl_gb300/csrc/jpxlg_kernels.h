@@ -176,8 +176,13 @@ void launch_ref_moments(const float* xyb, float* mu, float* s11, float* hpl, flo
 // double-float sums (8 bytes each) per 32 x 32 tile, each channel filling
 // its six.  Returns the number of rows (blur_partial_rows).
 struct DF;
+// Called between a scale's kernels when the caller times them: part 0
+// before the row pass, 1 before the column ripple, 2 before the column
+// outputs, 3 after them.
+using ScaleHook = void (*)(void* user, int part);
 int launch_score_scale(const float* cand_xyb, const SsimScale& ref, float* hpl, float* carry,
-                       int c0, int nch, DF* partial, cudaStream_t s);
+                       int c0, int nch, DF* partial, cudaStream_t s, ScaleHook hook = nullptr,
+                       void* user = nullptr);
 void launch_score_finish(const DF* partials, const int* ctas_per_scale, int nscales,
                          const int* pixels_per_scale, double* out /* score, raw, terms[108] */,
                          cudaStream_t s);

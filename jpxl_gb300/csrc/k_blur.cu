@@ -280,14 +280,20 @@ __global__ void __launch_bounds__(kRowThreads, 6) k_blur_rows(RowArgs a) {
     }
   }
   __syncthreads();
+  // Quantities in the order x, r*x, x*x, each product line formed once in
+  // place (r*x over r, then x*x over x) and rounded to f32 (blur.rs:395).
 #pragma unroll
-  for (int q = 0; q < NQ; ++q) {
-    // The quantity's line sample i: x, x*x or r*x, each product rounded to
-    // f32 (blur.rs:395).
-    auto L = [&](int i) -> f2 {
-      const f2 xv = xl[i];
-      return q == 0 ? xv : (q == 1 ? f2_mul(xv, xv, nz) : f2_mul(rl[i], xv, nz));
-    };
+  for (int qi = 0; qi < NQ; ++qi) {
+    const int q = NQ == 3 ? (qi == 0 ? 0 : (qi == 1 ? 2 : 1)) : qi;
+    if (q != 0) {
+      for (int i = t; i < a.w + 20; i += kRowThreads) {
+        if (q == 2) rl[i] = f2_mul(rl[i], xl[i], nz);
+        else xl[i] = f2_mul(xl[i], xl[i], nz);
+      }
+      __syncthreads();
+    }
+    const f2* line = q == 2 ? rl : xl;
+    auto L = [&](int i) -> f2 { return line[i]; };
     // (1) the segment's ripple from rest, recorded.
     Ripple2 rp;
 #pragma unroll
@@ -564,6 +570,20 @@ __global__ void __launch_bounds__(kOutThreads, 4) k_blur_col_out(ColArgs a) {
 #pragma unroll
   for (int i = 0; i < kR; ++i) {
     const int r = kR * b + i, gy = r0 + r;
+    // The reference side's mu, sigma11 and XYB and the candidate's XYB at
+    // this row's two outputs, loaded before the FIRs so that their latency
+    // overlaps the arithmetic.
+    float pf[2][4];
+    if (NQ == 3)
+#pragma unroll
+      for (int e = 0; e < 2; ++e) {
+        const bool in = gy < a.h && gx + e < a.w;
+        const size_t p = (size_t)c * n + (size_t)(in ? gy : 0) * a.w + (in ? gx + e : 0);
+        pf[e][0] = in ? __ldg(a.mu1 + p) : 0.0f;
+        pf[e][1] = in ? __ldg(a.s11r + p) : 0.0f;
+        pf[e][2] = in ? __ldg(a.rx + p) : 0.0f;
+        pf[e][3] = in ? __ldg(a.cx + p) : 0.0f;
+      }
     f2 val[NQ];
 #pragma unroll
     for (int q = 0; q < NQ; ++q) {
@@ -587,9 +607,9 @@ __global__ void __launch_bounds__(kOutThreads, 4) k_blur_col_out(ColArgs a) {
 #pragma unroll
       for (int e = 0; e < 2; ++e) {
         if (e == 1 && !second) break;
-        const float m1 = __ldg(a.mu1 + p + e);
+        const float m1 = pf[e][0];
         const float m2 = e ? f2_hi(val[0]) : f2_lo(val[0]);
-        const float v11 = __ldg(a.s11r + p + e);
+        const float v11 = pf[e][1];
         const float s22 = e ? f2_hi(val[1]) : f2_lo(val[1]);
         const float s12 = e ? f2_hi(val[NQ - 1]) : f2_lo(val[NQ - 1]);
         const float mu11 = m1 * m1, mu22 = m2 * m2, mu12 = m1 * m2;
@@ -602,7 +622,7 @@ __global__ void __launch_bounds__(kOutThreads, 4) k_blur_col_out(ColArgs a) {
         // (1 + |i2-m2|) / (1 + |i1-m1|) - 1 as a difference over the
         // denominator (within the 0.01-point contract the fast division, at
         // most 2 ulp off, serves; identical images give a zero numerator).
-        const float a1 = fabsf(__ldg(a.rx + p + e) - m1), a2 = fabsf(__ldg(a.cx + p + e) - m2);
+        const float a1 = fabsf(pf[e][2] - m1), a2 = fabsf(pf[e][3] - m2);
         const float d1 = __fdividef(a2 - a1, 1.0f + a1);
         const float art = fmaxf(d1, 0.0f), lost = fmaxf(-d1, 0.0f);
         const float art2 = art * art, lost2 = lost * lost;
@@ -704,8 +724,10 @@ void launch_ref_moments(const float* xyb, float* mu, float* s11, float* hpl, flo
 }
 
 int launch_score_scale(const float* cand_xyb, const SsimScale& ref, float* hpl, float* carry,
-                       int c0, int nch, DF* partial, cudaStream_t s) {
+                       int c0, int nch, DF* partial, cudaStream_t s, ScaleHook hook,
+                       void* user) {
   const int w = ref.w, h = ref.h;
+  if (hook) hook(user, 0);
   RowArgs ra{};
   ra.x = cand_xyb;
   ra.r = ref.xyb;
@@ -713,6 +735,7 @@ int launch_score_scale(const float* cand_xyb, const SsimScale& ref, float* hpl, 
   ra.c0 = c0;
   fill_row_args(ra, w, h);
   k_blur_rows<3><<<dim3((h + 1) / 2, nch), kRowThreads, blur_row_smem(w), s>>>(ra);
+  if (hook) hook(user, 1);
   ColArgs ca{};
   ca.hpl = hpl;
   ca.carry = carry;
@@ -727,7 +750,9 @@ int launch_score_scale(const float* cand_xyb, const SsimScale& ref, float* hpl, 
   const int groups = (ca.nseg + kCarryWarps - 1) / kCarryWarps;
   k_blur_col_local<3><<<dim3(strips, groups, nch), kColW * kCarryWarps, 0, s>>>(ca);
   k_blur_col_scan<3><<<dim3(strips, nch), kColW * 3 * 3, 0, s>>>(ca);
+  if (hook) hook(user, 2);
   k_blur_col_out<3><<<dim3(strips, ca.nseg, nch), kOutThreads, 0, s>>>(ca);
+  if (hook) hook(user, 3);
   return blur_partial_rows(w, h);
 }
 
