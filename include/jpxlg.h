@@ -205,6 +205,15 @@ int jpxlg_encode_transform(jpxlg_ctx* ctx, const jpxlg_layout* layout, const voi
 int jpxlg_encode_stages(jpxlg_ctx* ctx, const jpxlg_layout* layout, const void* rgb, int bits,
                         const jpxlg_params* params, float* xyb, float* pre, float* coeff);
 
+/* Diagnostic: the decoder's 8x8 special transforms (jpxl-core varblock.rs:
+ * 1218 samples_from_coefficients for DCT2x2, Hornuss, DCT4x4, DCT8x4,
+ * DCT4x8 and AFV0-3, I.9.3-I.9.8) on n dequantized coefficient blocks
+ * (64 floats each, row-major, the LLF at 0) into n blocks of 64 samples, the
+ * kernels jpxlg_codestream_render runs for those transforms.  kind: 1 DCT2x2,
+ * 2 Hornuss, 3 DCT4x4, 4 DCT8x4, 5 DCT4x8, 6..9 AFV0..AFV3. */
+int jpxlg_diag_special_blocks(jpxlg_ctx* ctx, int kind, const float* coef, int n, float* out,
+                              uint32_t mem);
+
 /* Quantized plan -> pixels.  `out` sizes: JPXLG_OUT_SRGB8 w*h*3 bytes, other
  * kinds 3*w*h floats.  `bits` is the depth of JPXLG_OUT_LINEAR_DEPTH. */
 int jpxlg_reconstruct(jpxlg_ctx* ctx, const jpxlg_layout* layout, const jpxlg_plan* plan,

@@ -659,6 +659,21 @@ class DecodeBatch:
             pass
 
 
+SPECIAL_KINDS = {"dct2x2": 1, "hornuss": 2, "dct4x4": 3, "dct8x4": 4, "dct4x8": 5,
+                 "afv0": 6, "afv1": 7, "afv2": 8, "afv3": 9}
+
+
+def special_blocks(ctx: Context, kind: int, coef: np.ndarray) -> np.ndarray:
+    """The decoder's 8x8 special transforms (varblock.rs:1218) on dequantized
+    coefficient blocks, float32 [n, 8, 8] (LLF at [0, 0]) -> samples
+    [n, 8, 8], through the kernels the stream render uses."""
+    c = np.ascontiguousarray(coef, np.float32).reshape(-1, 64)
+    out = np.zeros_like(c)
+    ctx.check(ctx.lib.jpxlg_diag_special_blocks(ctx.handle, kind, c.ctypes.data, c.shape[0],
+                                                out.ctypes.data, MEM_HOST))
+    return out.reshape(-1, 8, 8)
+
+
 def score_pair(ctx: Context, ref_rgb: np.ndarray, cand_rgb: np.ndarray) -> float:
     """jpxl-perceptual lib.rs:195 score_pair on linear [3, H, W] planes."""
     a = np.ascontiguousarray(ref_rgb, dtype=np.float32)

@@ -808,6 +808,30 @@ int jpxlg_encode_transform(jpxlg_ctx* ctx, const jpxlg_layout* L, const void* rg
   return JPXLG_OK;
 }
 
+int jpxlg_diag_special_blocks(jpxlg_ctx* ctx, int kind, const float* coef, int n, float* out,
+                              uint32_t mem) {
+  if (!ctx || !coef || !out || n <= 0) return fail(ctx, JPXLG_ERR_ARGUMENT, "null argument");
+  if (kind < 1 || kind > 9) return fail(ctx, JPXLG_ERR_ARGUMENT, "kind must be 1..9");
+  CK(cudaSetDevice(ctx->device));
+  const size_t bytes = (size_t)n * 64 * sizeof(float);
+  const float* din = coef;
+  float* dout = out;
+  if (mem != JPXLG_MEM_DEVICE) {
+    CK(ctx->coeff.ensure(bytes));
+    CK(ctx->out.ensure(bytes));
+    CK(cudaMemcpyAsync(ctx->coeff.p, coef, bytes, cudaMemcpyHostToDevice, ctx->stream));
+    din = ctx->coeff.as<float>();
+    dout = ctx->out.as<float>();
+  }
+  launch_special_diag(kind, din, n, dout, ctx->stream);
+  int rc = after_launch(ctx, 1);
+  if (rc) return rc;
+  if (mem == JPXLG_MEM_DEVICE) return JPXLG_OK;
+  CK(cudaMemcpyAsync(out, dout, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  return JPXLG_OK;
+}
+
 int jpxlg_encode_stages(jpxlg_ctx* ctx, const jpxlg_layout* L, const void* rgb, int bits,
                         const jpxlg_params* p, float* xyb, float* pre, float* coeff) {
   if (!ctx || !L || !rgb) return fail(ctx, JPXLG_ERR_ARGUMENT, "null argument");

@@ -62,6 +62,7 @@ void launch_lf_prepare(const int32_t* lfq, int bw, int bh, const float m[3], flo
                        cudaStream_t s);
 void upload_dct64(const float* matrix, cudaStream_t s);
 void upload_afv(const double* basis, cudaStream_t s);
+bool launch_special_diag(int kind, const float* coef, int n, float* out, cudaStream_t s);
 
 // Fills table[h] = hf_multiplier_f64(global_scale, h) for h < kMulTableN.
 void launch_mul_table(uint32_t global_scale, float* table, cudaStream_t s);

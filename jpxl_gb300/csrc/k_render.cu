@@ -106,6 +106,32 @@ __device__ __forceinline__ void idct2d_raw(const float* coef, float* out) {
 
 __device__ double g_afv[256];  // Table I.11, uploaded by the host
 
+// varblock.rs:917 DCT2x2: aux_idct_2x2 (:898) with s = 2, 4, 8, each stage
+// reading the previous one; b (row-major, LLF at 0) becomes the samples.
+__device__ __forceinline__ void dct2x2_block(float* b) {
+  float r[64];
+#pragma unroll
+  for (int st = 2; st <= 8; st *= 2) {
+    const int h = st / 2;
+#pragma unroll
+    for (int i = 0; i < 64; ++i) r[i] = b[i];
+#pragma unroll
+    for (int y = 0; y < h; ++y)
+#pragma unroll
+      for (int x = 0; x < h; ++x) {
+        const float c00 = b[y * 8 + x], c01 = b[y * 8 + h + x];
+        const float c10 = b[(y + h) * 8 + x], c11 = b[(y + h) * 8 + h + x];
+        r[(2 * y) * 8 + 2 * x] = ((c00 + c01) + c10) + c11;
+        r[(2 * y) * 8 + 2 * x + 1] = ((c00 + c01) - c10) - c11;
+        r[(2 * y + 1) * 8 + 2 * x] = ((c00 - c01) + c10) - c11;
+        r[(2 * y + 1) * 8 + 2 * x + 1] = ((c00 - c01) - c10) + c11;
+      }
+#pragma unroll
+    for (int i = 0; i < 64; ++i) b[i] = r[i];
+  }
+}
+
+
 // The 8x8 special transforms of jpxl-core varblock.rs:926-1230 on a
 // dequantized block b (row-major, LLF at 0): KIND 2 Hornuss, 3 DCT4x4,
 // 4 DCT8x4, 5 DCT4x8, 6..9 AFV0..AFV3.  Evaluation order follows the
@@ -373,28 +399,10 @@ __global__ void __launch_bounds__(128) k_render_vb(RenderArgs a, const uint32_t*
       // previous one; thread 0 of the group runs the cascade, then thread j
       // writes sample column j.
       if (active && j == 0) {
-        float b[64], r[64];
+        float b[64];
 #pragma unroll
         for (int i = 0; i < 64; ++i) b[i] = L[g][i / 8][i % 8];
-#pragma unroll
-        for (int st = 2; st <= 8; st *= 2) {
-          const int h = st / 2;
-#pragma unroll
-          for (int i = 0; i < 64; ++i) r[i] = b[i];
-#pragma unroll
-          for (int y = 0; y < h; ++y)
-#pragma unroll
-            for (int x = 0; x < h; ++x) {
-              const float c00 = b[y * 8 + x], c01 = b[y * 8 + h + x];
-              const float c10 = b[(y + h) * 8 + x], c11 = b[(y + h) * 8 + h + x];
-              r[(2 * y) * 8 + 2 * x] = ((c00 + c01) + c10) + c11;
-              r[(2 * y) * 8 + 2 * x + 1] = ((c00 + c01) - c10) - c11;
-              r[(2 * y + 1) * 8 + 2 * x] = ((c00 - c01) + c10) - c11;
-              r[(2 * y + 1) * 8 + 2 * x + 1] = ((c00 - c01) - c10) + c11;
-            }
-#pragma unroll
-          for (int i = 0; i < 64; ++i) b[i] = r[i];
-        }
+        dct2x2_block(b);
 #pragma unroll
         for (int i = 0; i < 64; ++i) L[g][i / 8][i % 8] = b[i];
       }
@@ -928,6 +936,44 @@ void launch_lf_prepare(const int32_t* lfq, int bw, int bh, const float m[3], flo
   const int blocks = (int)std::max<size_t>(1, std::min<size_t>((nb + 255) / 256, num_sms * 4));
   k_lf_dequant<<<blocks, 256, 0, s>>>(lfq, nb, m[0], m[1], m[2], div, kx, kb, smooth ? tmp : out);
   if (smooth) k_lf_smooth<<<blocks, 256, 0, s>>>(tmp, bw, bh, m[0], m[1], m[2], out);
+}
+
+// The special transforms on given blocks, one thread per block (a
+// diagnostic of jpxlg_diag_special_blocks): kind 1 DCT2x2, 2..9 as
+// special_block.
+template <int KIND>
+__global__ void __launch_bounds__(64) k_special_diag(const float* __restrict__ coef, int n,
+                                                     float* __restrict__ out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  float b[64], o[64];
+#pragma unroll
+  for (int k = 0; k < 64; ++k) b[k] = coef[(size_t)i * 64 + k];
+  if constexpr (KIND == 1) {
+    dct2x2_block(b);
+#pragma unroll
+    for (int k = 0; k < 64; ++k) o[k] = b[k];
+  } else {
+    special_block<KIND>(b, o);
+  }
+#pragma unroll
+  for (int k = 0; k < 64; ++k) out[(size_t)i * 64 + k] = o[k];
+}
+
+bool launch_special_diag(int kind, const float* coef, int n, float* out, cudaStream_t s) {
+  const int blocks = (n + 63) / 64;
+  switch (kind) {
+    case 1: k_special_diag<1><<<blocks, 64, 0, s>>>(coef, n, out); return true;
+    case 2: k_special_diag<2><<<blocks, 64, 0, s>>>(coef, n, out); return true;
+    case 3: k_special_diag<3><<<blocks, 64, 0, s>>>(coef, n, out); return true;
+    case 4: k_special_diag<4><<<blocks, 64, 0, s>>>(coef, n, out); return true;
+    case 5: k_special_diag<5><<<blocks, 64, 0, s>>>(coef, n, out); return true;
+    case 6: k_special_diag<6><<<blocks, 64, 0, s>>>(coef, n, out); return true;
+    case 7: k_special_diag<7><<<blocks, 64, 0, s>>>(coef, n, out); return true;
+    case 8: k_special_diag<8><<<blocks, 64, 0, s>>>(coef, n, out); return true;
+    case 9: k_special_diag<9><<<blocks, 64, 0, s>>>(coef, n, out); return true;
+    default: return false;
+  }
 }
 
 void upload_afv(const double* basis, cudaStream_t s) {

@@ -81,6 +81,8 @@ def load() -> C.CDLL:
         lib.orc64_reconstruct.argtypes = [i, i, p, p, p, p, p, p, p, p, i, p]
         lib.orc64_ssim2.restype = i
         lib.orc64_ssim2.argtypes = [p, p, p, p, i, i, p, p]
+        lib.orc_special_block.restype = i
+        lib.orc_special_block.argtypes = [i, p, p, p]
         _lib = lib
     return _lib
 
@@ -270,3 +272,21 @@ def fp64_ssim2(ref: np.ndarray, cand: np.ndarray):
     terms = np.zeros(6 * 18, np.float64)
     n = lib.orc64_ssim2(r32, c32, r64, c64, w, h, C.byref(sc), terms.ctypes.data)
     return sc.value, terms[: max(n, 0) * 18]
+
+
+SPECIAL_KINDS = {"dct2x2": 1, "hornuss": 2, "dct4x4": 3, "dct8x4": 4, "dct4x8": 5,
+                 "afv0": 6, "afv1": 7, "afv2": 8, "afv3": 9}
+
+
+def special_block(kind: int, coef: np.ndarray, afv_basis=None) -> np.ndarray:
+    """orc_special_block: a dequantized 8x8 coefficient block (float32 [8, 8],
+    row-major, LLF at [0, 0]) to its 8x8 samples; afv_basis is Table I.11
+    ([16, 16] f64), needed for the AFV kinds 6..9."""
+    lib = load()
+    c = np.ascontiguousarray(coef, np.float32).reshape(8, 8)
+    out = np.zeros((8, 8), np.float32)
+    basis = None if afv_basis is None else np.ascontiguousarray(afv_basis, np.float64)
+    rc = lib.orc_special_block(kind, c.ctypes.data, _ptr(basis), out.ctypes.data)
+    if rc:
+        raise ValueError(f"orc_special_block kind {kind}: {rc}")
+    return out

@@ -137,6 +137,11 @@ int orc_ssim2(const float* const* ref, const float* const* cand, int w, int h,
 /* ssimulacra2.rs:391 WEIGHTS[i]; the f64 recursive blur of one plane. */
 double orc_ssim2_weight(int i);
 void orc_blur_plane(const float* in, int w, int h, float* out);
+/* The decoder's 8x8 special transforms (varblock.rs:898-1230): a dequantized
+ * coefficient block (row-major, LLF at 0) to its 8x8 samples.  kind: 1 DCT2x2,
+ * 2 Hornuss, 3 DCT4x4, 4 DCT8x4, 5 DCT4x8, 6..9 AFV0..AFV3; afv_basis is
+ * Table I.11 (16 x 16 f64), needed for AFV.  Returns 0, or -1 for a bad kind. */
+int orc_special_block(int kind, const float* coef, const double* afv_basis, float* out);
 /* entry (u, n) of the orthonormal DCT-IV leaf of size M (dct.rs:148-211) */
 float orc_dct_iv_entry(int M, int u, int n);
 

@@ -11,6 +11,7 @@ Sources (JPXL/crates/...):
   jpxl-perceptual/src/ssimulacra2.rs:391 WEIGHTS
   jpxl-core/src/dequant.rs:712-1020      Table I.6 DCT parameter rows
   jpxl-perceptual/src/blur.rs:41/:47     MUL_IN / MUL_PREV
+  jpxl-core/src/varblock.rs AFV_BASIS    Table I.11, the AFV basis
   .akr/records/jpegxl-rs/evidence.akr:6424  recorded score bits of the 4.3 MP pair
 """
 from __future__ import annotations
@@ -52,6 +53,11 @@ def main() -> None:
         vals = numbers(block(dq, name))
         n = len(vals) // 3
         out[name] = [vals[i * n:(i + 1) * n] for i in range(3)]
+    vb = (REF / "jpxl-core/src/varblock.rs").read_text()
+    afv = numbers(block(vb, "AFV_BASIS"))
+    if len(afv) != 256:
+        raise ValueError(f"AFV_BASIS: {len(afv)} entries")
+    out["AFV_BASIS"] = [afv[i * 16:(i + 1) * 16] for i in range(16)]
     ev = Path("/root/reference/.akr/records/jpegxl-rs/evidence.akr").read_text()
     m = re.search(r"Raw score bits ([0-9a-f]{16})", ev)
     out["SCORE_BITS_4MP_PAIR"] = m.group(1) if m else None
