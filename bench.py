@@ -612,14 +612,15 @@ def _quantize_8(np, v):
 
 def run_decode(ctx, reps, np):
     """Batched decode: the committed cjxl VarDCT streams repeated to 256,
-    rendered to 8-bit sRGB by one graph launch (jpxlg_decode_batch_*).  The
-    host parses every stream (headers, TOC, entropy-coded sections) at open;
-    each graph launch copies the staged coefficients in, renders all 256
-    frames over four lanes and copies the 8-bit pixels back to pinned host
-    memory.  `value` is end to end: parse of all streams plus one graph run,
-    per second.  Against djxl's decodes (the .npy beside 11 of the 13
-    fixtures, quantized as quantize_sample does) the samples 1 DN off are
-    counted."""
+    rendered to 8-bit sRGB by one graph launch (jpxlg_decode_batch_*), with
+    the FP32 IDCTs and with the split-precision ones (square varblocks on the
+    tensor cores).  The host parses every stream (headers, TOC,
+    entropy-coded sections) at open; each graph launch copies the staged
+    coefficients in, renders all 256 frames over four lanes and copies the
+    8-bit pixels back to pinned host memory.  `value` is end to end: parse
+    of all streams plus one FP32 graph run, per second.  Against djxl's
+    decodes (the .npy beside 11 of the 13 fixtures, quantized as
+    quantize_sample does) the samples 1 DN off are counted per mode."""
     import jpxl_gb300 as jg
 
     names = DECODE_WITH_DJXL + DECODE_OTHERS
@@ -630,37 +631,47 @@ def run_decode(ctx, reps, np):
     streams = [jg.Codestream(data[n]) for n in order]
     parse = time.perf_counter() - t0
     px = sum(s.info["width"] * s.info["height"] for s in streams)
-    batch = jg.DecodeBatch(ctx, streams, "srgb8")
+    refs = {n: _quantize_8(np, np.load(gdir / (n + ".npy"))[0][:, :, :3])
+            for n in DECODE_WITH_DJXL}
+    modes = {}
     try:
-        for _ in range(3):
-            outs = batch.run()
-        t0 = time.perf_counter()
-        for _ in range(reps):
-            batch.run()
-        graph = (time.perf_counter() - t0) / reps
-        off = samples = worst = 0
-        for n, s, out in zip(order, streams, outs):
-            if n not in DECODE_WITH_DJXL:
-                continue
-            ref = np.load(gdir / (n + ".npy"))[0][:, :, :3]
-            got = out.transpose(1, 0, 2) if s.info["orientation"] == 5 else out
-            got = got[:, :, :ref.shape[2]]  # a grey image's value is plane 0
-            d = np.abs(got.astype(np.int32) - _quantize_8(np, ref))
-            off += int((d > 0).sum())
-            worst = max(worst, int(d.max()))
-            samples += d.size
+        for prec in ("fp32", "bf16x6", "bf16x3"):
+            batch = jg.DecodeBatch(ctx, streams, "srgb8", precision=prec)
+            try:
+                for _ in range(3):
+                    outs = batch.run()
+                t0 = time.perf_counter()
+                for _ in range(reps):
+                    batch.run()
+                graph = (time.perf_counter() - t0) / reps
+                off = samples = worst = 0
+                for n, s, out in zip(order, streams, outs):
+                    if n not in refs:
+                        continue
+                    ref = refs[n]
+                    got = out.transpose(1, 0, 2) if s.info["orientation"] == 5 else out
+                    got = got[:, :, :ref.shape[2]]  # a grey image's value is plane 0
+                    d = np.abs(got.astype(np.int32) - ref)
+                    off += int((d > 0).sum())
+                    worst = max(worst, int(d.max()))
+                    samples += d.size
+            finally:
+                batch.close()
+            modes[prec] = {"graph_ms": round(graph * 1e3, 3),
+                           "graph_mpix_s": round(px / graph / 1e6, 2),
+                           "vs_djxl_8bit": {"samples": samples, "samples_1dn_off": off,
+                                            "max_dn": worst}}
     finally:
-        batch.close()
         for s in streams:
             s.close()
+    fp = modes["fp32"]
     return {"workload": f"{DECODE_N} cjxl VarDCT streams ({len(names)} committed fixtures, "
                         "tests/golden/codestream, repeated), one graph launch to 8-bit sRGB",
             "unit": "MPix/s", "streams": DECODE_N, "pixels": px,
-            "value": round(px / (parse + graph) / 1e6, 2),
-            "parse_ms": round(parse * 1e3, 3), "graph_ms": round(graph * 1e3, 3),
-            "parse_mpix_s": round(px / parse / 1e6, 2),
-            "graph_mpix_s": round(px / graph / 1e6, 2),
-            "vs_djxl_8bit": {"samples": samples, "samples_1dn_off": off, "max_dn": worst}}
+            "value": round(px / (parse + fp["graph_ms"] / 1e3) / 1e6, 2),
+            "parse_ms": round(parse * 1e3, 3), "parse_mpix_s": round(px / parse / 1e6, 2),
+            "graph_ms": fp["graph_ms"], "graph_mpix_s": fp["graph_mpix_s"],
+            "vs_djxl_8bit": fp["vs_djxl_8bit"], "precision_modes": modes}
 
 
 def roofline_of(stages: dict, n_img: int) -> dict:

@@ -405,7 +405,9 @@ int jpxlg_codestream_render(jpxlg_ctx* ctx, const jpxlg_codestream* cs, int out_
  * size the workspaces, and captures one CUDA graph on ctx's stream: per
  * stream, the staged planes to the device, LF preparation, the render into
  * `out_kind` (as jpxlg_codestream_render) and the pixels back to a pinned
- * host buffer.  The streams must stay open while the batch lives.
+ * host buffer.  `precision` (JPXLG_PRECISION_*) picks how the square
+ * DCT8/16/32 varblocks' IDCTs run; every other transform renders through
+ * the FP32 kernels.  The streams must stay open while the batch lives.
  * jpxlg_decode_batch_run launches the graph; with JPXLG_MEM_HOST it waits
  * and copies stream i's pixels to outs[i] (host; NULL entries, or outs
  * NULL, skip the copy); with JPXLG_MEM_DEVICE it queues device-to-device
@@ -413,7 +415,8 @@ int jpxlg_codestream_render(jpxlg_ctx* ctx, const jpxlg_codestream* cs, int out_
  * not carry fail creation with JPXLG_ERR_STREAM, naming the stream. */
 typedef struct jpxlg_decode_batch jpxlg_decode_batch;
 int jpxlg_decode_batch_create(jpxlg_ctx* ctx, int n, const jpxlg_codestream* const* streams,
-                              int out_kind, int lanes, jpxlg_decode_batch** out);
+                              int out_kind, uint32_t precision, int lanes,
+                              jpxlg_decode_batch** out);
 int jpxlg_decode_batch_run(jpxlg_ctx* ctx, jpxlg_decode_batch* batch, void* const* outs,
                            uint32_t mem);
 int jpxlg_decode_batch_destroy(jpxlg_decode_batch* batch);

@@ -626,12 +626,14 @@ class DecodeBatch:
 
     KINDS = {"xyb": 0, "linear": 1, "srgb8": 2, "srgb_float": 4}
 
-    def __init__(self, ctx: Context, streams: list, out: str = "srgb8", lanes: int = 0):
+    def __init__(self, ctx: Context, streams: list, out: str = "srgb8", lanes: int = 0,
+                 precision: str = "fp32"):
         self.ctx, self.streams, self.out = ctx, list(streams), out
         arr = (C.c_void_p * len(self.streams))(*[s.handle.value for s in self.streams])
         h = C.c_void_p()
         ctx.check(ctx.lib.jpxlg_decode_batch_create(ctx.handle, len(self.streams), arr,
-                                                    self.KINDS[out], lanes, C.byref(h)))
+                                                    self.KINDS[out], PRECISIONS[precision],
+                                                    lanes, C.byref(h)))
         self.handle = h
         self.buffers = []
         for s in self.streams:

@@ -63,7 +63,7 @@ SIGNATURES: dict[str, tuple] = {
     "jpxlg_codestream_extra": (_I, [_P, _U32, _P]),
     "jpxlg_codestream_destroy": (_I, [_P]),
     "jpxlg_codestream_render": (_I, [_P, _P, _I, _P, _U32]),
-    "jpxlg_decode_batch_create": (_I, [_P, _I, _P, _I, _I, C.POINTER(_P)]),
+    "jpxlg_decode_batch_create": (_I, [_P, _I, _P, _I, _U32, _I, C.POINTER(_P)]),
     "jpxlg_decode_batch_run": (_I, [_P, _P, _P, _U32]),
     "jpxlg_decode_batch_destroy": (_I, [_P]),
 }

@@ -1484,7 +1484,7 @@ struct DecodeStage {
 // Checks that the renderer carries everything the frame uses, and stages
 // it (host work only: the coefficient image from the parsed groups).
 int decode_stage(jpxlg_ctx* ctx, const jpxlg_codestream* cs, int out_kind, bool pinned,
-                 DecodeStage& st) {
+                 DecodeStage& st, uint32_t precision = JPXLG_PRECISION_FP32) {
   if (out_kind < 0 || out_kind > 4 || out_kind == JPXLG_OUT_LINEAR_DEPTH)
     return fail(ctx, JPXLG_ERR_ARGUMENT, "bad out_kind");
   const jpxlg::cs::Decoded& d = cs->d;
@@ -1526,6 +1526,7 @@ int decode_stage(jpxlg_ctx* ctx, const jpxlg_codestream* cs, int out_kind, bool 
   st.p.b_qm_scale = f.b_qm_scale;
   st.p.gaborish = f.gab ? 1u : 0u;
   st.p.epf_iters = f.epf_iters;
+  st.p.precision = precision;
   if ((rc = check_params(ctx, &st.p))) return rc;
   st.n = (size_t)g.w * g.h;
   st.n8 = (size_t)g.W8 * g.H8;
@@ -1680,7 +1681,8 @@ int decode_batch_check(jpxlg_ctx* ctx, jpxlg_decode_batch* b) {
 }  // namespace
 
 extern "C" int jpxlg_decode_batch_create(jpxlg_ctx* ctx, int n, const jpxlg_codestream* const* streams,
-                                         int out_kind, int lanes, jpxlg_decode_batch** out) {
+                                         int out_kind, uint32_t precision, int lanes,
+                                         jpxlg_decode_batch** out) {
   if (!ctx || !streams || !out || n <= 0) return fail(ctx, JPXLG_ERR_ARGUMENT, "null argument");
   *out = nullptr;
   if (out_kind < 0 || out_kind > 4 || out_kind == JPXLG_OUT_LINEAR_DEPTH)
@@ -1698,7 +1700,7 @@ extern "C" int jpxlg_decode_batch_create(jpxlg_ctx* ctx, int n, const jpxlg_code
   size_t total = 0;
   for (int i = 0; i < n; ++i) {
     b->items.emplace_back(new DecodeStage);
-    int rc = decode_stage(ctx, streams[i], out_kind, true, *b->items.back());
+    int rc = decode_stage(ctx, streams[i], out_kind, true, *b->items.back(), precision);
     if (rc) return fail(ctx, rc, "decode batch stream %d: %s", i, ctx->last_error.c_str());
     const size_t bytes = decode_out_bytes(*b->items.back(), out_kind);
     total = (total + 255) & ~(size_t)255;
