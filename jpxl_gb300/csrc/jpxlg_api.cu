@@ -57,6 +57,11 @@ struct jpxlg_ctx {
   int num_sms = 0;
   cudaStream_t own_stream = nullptr;
   cudaStream_t stream = nullptr;
+  // Side streams for the shape classes of a launch (ClassStreams below),
+  // forked from and joined back into `stream` with events.
+  cudaStream_t side[2] = {nullptr, nullptr};
+  cudaEvent_t fork_ev = nullptr;
+  cudaEvent_t join_ev[2] = {nullptr, nullptr};
   std::string last_error;
   uint64_t launches = 0;
   // tables
@@ -186,6 +191,47 @@ int after_launch(jpxlg_ctx* ctx, uint64_t n) {
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return fail(ctx, JPXLG_ERR_CUDA, "kernel launch: %s", cudaGetErrorString(e));
   return JPXLG_OK;
+}
+
+// A stream per shape class for one launch of independent per-class kernels:
+// the class with the most varblocks stays on the context's stream, the
+// others alternate over the two side streams, forked from the context's
+// stream here and joined back by class_join.  A small class (a handful of
+// DCT32 varblocks is one CTA that runs for tens of microseconds on its
+// latency chains) then overlaps the large one instead of following it.
+struct ClassStreams {
+  cudaStream_t s[kNumShapes];
+  bool used[2] = {false, false};
+};
+
+ClassStreams class_fork(jpxlg_ctx* ctx, const int* counts, int n) {
+  ClassStreams cs;
+  int biggest = -1;
+  for (int i = 0; i < n; ++i)
+    if (counts[i] && (biggest < 0 || counts[i] > counts[biggest])) biggest = i;
+  int side = 0;
+  for (int i = 0; i < kNumShapes; ++i) {
+    cs.s[i] = ctx->stream;
+    if (i < n && counts[i] && i != biggest && ctx->side[0]) {
+      cs.s[i] = ctx->side[side];
+      cs.used[side] = true;
+      side ^= 1;
+    }
+  }
+  if (cs.used[0] || cs.used[1]) {
+    cudaEventRecord(ctx->fork_ev, ctx->stream);
+    for (int k = 0; k < 2; ++k)
+      if (cs.used[k]) cudaStreamWaitEvent(ctx->side[k], ctx->fork_ev, 0);
+  }
+  return cs;
+}
+
+void class_join(jpxlg_ctx* ctx, const ClassStreams& cs) {
+  for (int k = 0; k < 2; ++k)
+    if (cs.used[k]) {
+      cudaEventRecord(ctx->join_ev[k], ctx->side[k]);
+      cudaStreamWaitEvent(ctx->stream, ctx->join_ev[k], 0);
+    }
 }
 
 // Reads and clears the device error word after the stream drains.
@@ -334,24 +380,37 @@ int encode_device(jpxlg_ctx* ctx, const jpxlg_layout* L, const void* rgb_dev, in
   // square classes only: DCT8, DCT16, DCT32 are shape classes 0..2
   stage_begin(ctx, JPXLG_STAGE_FDCT_LUMA);
   launch_mul_table(p->global_scale, ctx->d_mul, ctx->stream);
-  if (p->precision == JPXLG_PRECISION_FP32) {
-    rc = after_launch(ctx, 1 + launch_fdct_luma(a, L->lists, L->counts, ctx->stream));
-  } else {
-    // split-precision forward transform of all three channels on the tensor
-    // cores, then the luma quantization from the coefficient image
-    const int terms = p->precision == JPXLG_PRECISION_BF16X3 ? 2 : 3;
-    int k = 1 + launch_fdct_tc(a, L->lists, L->counts, terms, ctx->num_sms, ctx->stream);
-    rc = after_launch(ctx, k + launch_luma_from_image(a, L->lists, L->counts, ctx->stream));
+  {
+    const ClassStreams cs = class_fork(ctx, L->counts, 3);
+    if (p->precision == JPXLG_PRECISION_FP32) {
+      rc = after_launch(ctx, 1 + launch_fdct_luma(a, L->lists, L->counts, cs.s));
+    } else {
+      // split-precision forward transform of all three channels on the
+      // tensor cores, then the luma quantization from the coefficient image
+      const int terms = p->precision == JPXLG_PRECISION_BF16X3 ? 2 : 3;
+      int k = 1 + launch_fdct_tc(a, L->lists, L->counts, terms, ctx->num_sms, cs.s);
+      rc = after_launch(ctx, k + launch_luma_from_image(a, L->lists, L->counts, cs.s));
+    }
+    class_join(ctx, cs);
   }
   stage_end(ctx);
   if (rc) return rc;
   stage_begin(ctx, JPXLG_STAGE_CFL);
-  rc = after_launch(ctx, launch_cfl(a, ctx->lf_seed.as<int>(), ctx->lf_part.p, ctx->cfl_tile.p,
-                                    ctx->stream));
+  {
+    const int chains[2] = {2, 1};  // the tile chain on the context's stream, the LF one beside
+    const ClassStreams cs = class_fork(ctx, chains, 2);
+    rc = after_launch(ctx, launch_cfl(a, ctx->lf_seed.as<int>(), ctx->lf_part.p,
+                                      ctx->cfl_tile.p, cs.s[0], cs.s[1]));
+    class_join(ctx, cs);
+  }
   stage_end(ctx);
   if (rc) return rc;
   stage_begin(ctx, JPXLG_STAGE_QUANT_CHROMA);
-  rc = after_launch(ctx, launch_quant_chroma(a, L->lists, L->counts, ctx->stream));
+  {
+    const ClassStreams cs = class_fork(ctx, L->counts, 3);
+    rc = after_launch(ctx, launch_quant_chroma(a, L->lists, L->counts, cs.s));
+    class_join(ctx, cs);
+  }
   stage_end(ctx);
   if (rc) return rc;
   // biased copy of the LF factors for the plan
@@ -397,8 +456,9 @@ int render_device(jpxlg_ctx* ctx, const jpxlg_layout* L, const int32_t* qcoeff,
   stage_begin(ctx, JPXLG_STAGE_RENDER_VARBLOCKS);
   launch_mul_table(p->global_scale, ctx->d_mul, ctx->stream);
   uint64_t k = 1;
+  const ClassStreams cs = class_fork(ctx, L->counts, kNumShapes);
   if (p->precision == JPXLG_PRECISION_FP32) {
-    launch_render_varblocks(a, L->lists, L->counts, ctx->stream);
+    launch_render_varblocks(a, L->lists, L->counts, cs.s);
     for (int i = 0; i < kNumShapes; ++i) k += L->counts[i] ? 1 : 0;
   } else {
     // square classes on the tensor cores; any other shape through the FP32
@@ -408,14 +468,15 @@ int render_device(jpxlg_ctx* ctx, const jpxlg_layout* L, const int32_t* qcoeff,
                        (size_t)std::max(1, L->counts[0] + L->counts[1] + L->counts[2])));
     float* llf[3] = {ctx->llf.as<float>(), ctx->llf.as<float>() + 48 * (size_t)L->counts[0],
                      ctx->llf.as<float>() + 48 * (size_t)(L->counts[0] + L->counts[1])};
-    k += launch_llf_sigma(a, L->lists, L->counts, llf, ctx->stream);
+    k += launch_llf_sigma(a, L->lists, L->counts, llf, cs.s);
     const float* cllf[3] = {llf[0], llf[1], llf[2]};
-    k += launch_render_tc(a, L->lists, L->counts, cllf, terms, ctx->num_sms, ctx->stream);
+    k += launch_render_tc(a, L->lists, L->counts, cllf, terms, ctx->num_sms, cs.s);
     int rest[kNumShapes];
     for (int i = 0; i < kNumShapes; ++i) rest[i] = i < 3 ? 0 : L->counts[i];
-    launch_render_varblocks(a, L->lists, rest, ctx->stream);
+    launch_render_varblocks(a, L->lists, rest, cs.s);
     for (int i = 3; i < kNumShapes; ++i) k += rest[i] ? 1 : 0;
   }
+  class_join(ctx, cs);
   int rc = after_launch(ctx, k);
   stage_end(ctx);
   if (rc) return rc;
@@ -502,8 +563,9 @@ int score_device(jpxlg_ctx* ctx, const jpxlg_ref* ref, const float* cand_dev,
     pixels[s] = rs.w * rs.h;
     part += (size_t)ctas[s] * 18;
   }
-  launch_score_finish(ctx->partial.as<DF>(), ctas, ref->nscales, pixels, out_dev, ctx->stream);
-  int rc = after_launch(ctx, k + 1);
+  k += launch_score_finish(ctx->partial.as<DF>(), ctas, ref->nscales, pixels, out_dev,
+                           ctx->stream);
+  int rc = after_launch(ctx, k);
   stage_end(ctx);
   return rc;
 }
@@ -537,6 +599,11 @@ int jpxlg_ctx_create(int device, uint32_t flags, jpxlg_ctx** out) {
   CKC(configure_tc_kernels());
   CKC(cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking));
   c->stream = c->own_stream;
+  for (int k = 0; k < 2; ++k) {
+    CKC(cudaStreamCreateWithFlags(&c->side[k], cudaStreamNonBlocking));
+    CKC(cudaEventCreateWithFlags(&c->join_ev[k], cudaEventDisableTiming));
+  }
+  CKC(cudaEventCreateWithFlags(&c->fork_ev, cudaEventDisableTiming));
   CKC(cudaMalloc(&c->d_words, 8 * sizeof(uint32_t)));
   CKC(cudaMemset(c->d_words, 0, 8 * sizeof(uint32_t)));
   CKC(cudaMalloc(&c->d_lf, 4 * sizeof(int)));
@@ -593,6 +660,14 @@ int jpxlg_ctx_destroy(jpxlg_ctx* ctx) {
   cudaFree(ctx->d_mul);
   cudaFreeHost(ctx->h_words);
   cudaFreeHost(ctx->h_score);
+  for (int k = 0; k < 2; ++k) {
+    if (ctx->side[k]) {
+      cudaStreamSynchronize(ctx->side[k]);
+      cudaStreamDestroy(ctx->side[k]);
+    }
+    if (ctx->join_ev[k]) cudaEventDestroy(ctx->join_ev[k]);
+  }
+  if (ctx->fork_ev) cudaEventDestroy(ctx->fork_ev);
   cudaStreamDestroy(ctx->own_stream);
   delete ctx;
   return JPXLG_OK;
@@ -1442,8 +1517,8 @@ extern "C" int jpxlg_ssim2_score_static(jpxlg_ctx* ctx, const jpxlg_ref* ref,
     pixels[s] = rs.w * rs.h;
     part += (size_t)ctas[s] * 18;
   }
-  launch_score_finish(part0, ctas, ref->nscales, pixels, out_dev, ctx->stream);
-  return after_launch(ctx, k + 1);
+  k += launch_score_finish(part0, ctas, ref->nscales, pixels, out_dev, ctx->stream);
+  return after_launch(ctx, k);
 }
 
 // ---------------------------------------------------------------------------

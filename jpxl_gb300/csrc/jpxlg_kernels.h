@@ -77,21 +77,26 @@ void upload_dct_constants(const float* iv4, const float* iv8, const float* iv16,
 void launch_srgb_to_xyb(const void* rgb, int bits, size_t n, const float* lut, float* x, float* y,
                         float* b, uint32_t* not_gray, int num_sms, cudaStream_t s);
 void launch_precondition(const float* in, float* out, int w, int h, cudaStream_t s);
-// Each returns the number of kernels it launched.
+// The per-shape-class launchers take one stream per class (s[i] for class
+// i), so that independent classes can run side by side.  Each returns the
+// number of kernels it launched.
 int launch_fdct_luma(const EncArgs& a, const uint32_t* const* lists, const int* counts,
-                     cudaStream_t s);
+                     const cudaStream_t* s);
 // LF CfL partials: kLfCtas CTAs, each 7 double-float sums and 8 bit counts.
 constexpr int kLfCtas = 128;
 constexpr size_t kCflScratchBytes = (size_t)kLfCtas * (7 * 8 + 8 * 4);
 // Per-tile CfL scratch: 8 double-float sums and 2 seeds per 64x64 tile.
 inline size_t cfl_tile_scratch_bytes(int ntiles) { return (size_t)ntiles * (8 * 8 + 2 * 4); }
+// The per-tile chain runs on s, the LF factors' chain on lf_s (it reads
+// only the LF planes); the caller joins lf_s back before the factors are
+// read.
 int launch_cfl(const EncArgs& a, int* lf_seeds, void* lf_scratch, void* tile_scratch,
-               cudaStream_t s);
+               cudaStream_t s, cudaStream_t lf_s);
 int launch_quant_chroma(const EncArgs& a, const uint32_t* const* lists, const int* counts,
-                        cudaStream_t s);
+                        const cudaStream_t* s);
 
 void launch_render_varblocks(const RenderArgs& a, const uint32_t* const* lists,
-                             const int* counts, cudaStream_t s);
+                             const int* counts, const cudaStream_t* s);
 
 // Split-precision transforms on the tensor cores (k_tc.cu), square shape
 // classes 0..2 (DCT8, DCT16, DCT32); terms = 2 (BF16x3) or 3 (BF16x6).
@@ -100,18 +105,18 @@ void launch_render_varblocks(const RenderArgs& a, const uint32_t* const* lists,
 cudaError_t configure_tc_kernels();
 void upload_tc_basis(cudaStream_t s);
 int launch_fdct_tc(const EncArgs& a, const uint32_t* const* lists, const int* counts, int terms,
-                   int num_sms, cudaStream_t s);
+                   int num_sms, const cudaStream_t* s);
 int launch_render_tc(const RenderArgs& a, const uint32_t* const* lists, const int* counts,
-                     const float* const* llf, int terms, int num_sms, cudaStream_t s);
+                     const float* const* llf, int terms, int num_sms, const cudaStream_t* s);
 // The LLF rectangles (48 floats per varblock: 3 channels x 16) and the EPF
 // sigma of square classes 0..2, for launch_render_tc (k_render.cu).
 int launch_llf_sigma(const RenderArgs& a, const uint32_t* const* lists, const int* counts,
-                     float* const* llf, cudaStream_t s);
+                     float* const* llf, const cudaStream_t* s);
 // Luma LF and HF quantization of the square varblocks from a coefficient
 // image the split-precision forward transform wrote (k_fdct_luma without its
 // own transform).
 int launch_luma_from_image(const EncArgs& a, const uint32_t* const* lists, const int* counts,
-                           cudaStream_t s);
+                           const cudaStream_t* s);
 void launch_gaborish(const float* in, float* out, int w, int h, cudaStream_t s);
 void launch_epf_step(int step, const float* in, float* out, const float* sigma, int w, int h,
                      cudaStream_t s);
@@ -184,8 +189,9 @@ using ScaleHook = void (*)(void* user, int part);
 int launch_score_scale(const float* cand_xyb, const SsimScale& ref, float* hpl, float* carry,
                        int c0, int nch, DF* partial, cudaStream_t s, ScaleHook hook = nullptr,
                        void* user = nullptr);
-void launch_score_finish(const DF* partials, const int* ctas_per_scale, int nscales,
-                         const int* pixels_per_scale, double* out /* score, raw, terms[108] */,
-                         cudaStream_t s);
+// Two launches (the per-scale sums, then the score); returns 2.  The sums
+// overwrite row 0 of each scale's partial rows.
+int launch_score_finish(DF* partials, const int* ctas_per_scale, int nscales,
+                        const int* pixels_per_scale, double* out, cudaStream_t s);
 
 }  // namespace jpxlg

@@ -1152,26 +1152,26 @@ __global__ void __launch_bounds__(128) k_quant_chroma(EncArgs a, const uint32_t*
 }
 
 int launch_fdct_luma(const EncArgs& a, const uint32_t* const* lists, const int* counts,
-                     cudaStream_t s) {
-  // square classes: 0 -> DCT8, 1 -> DCT16, 2 -> DCT32
+                     const cudaStream_t* s) {
+  // square classes: 0 -> DCT8, 1 -> DCT16, 2 -> DCT32, each on its stream
   int k = 0;
-  if (counts[0]) { k_fdct_luma<8><<<(counts[0] + 15) / 16, 128, 0, s>>>(a, lists[0], counts[0]); ++k; }
-  if (counts[1]) { k_fdct_luma<16><<<(counts[1] + 7) / 8, 128, 0, s>>>(a, lists[1], counts[1]); ++k; }
-  if (counts[2]) { k_fdct_luma<32><<<(counts[2] + 3) / 4, 128, 0, s>>>(a, lists[2], counts[2]); ++k; }
+  if (counts[0]) { k_fdct_luma<8><<<(counts[0] + 15) / 16, 128, 0, s[0]>>>(a, lists[0], counts[0]); ++k; }
+  if (counts[1]) { k_fdct_luma<16><<<(counts[1] + 7) / 8, 128, 0, s[1]>>>(a, lists[1], counts[1]); ++k; }
+  if (counts[2]) { k_fdct_luma<32><<<(counts[2] + 3) / 4, 128, 0, s[2]>>>(a, lists[2], counts[2]); ++k; }
   return k;
 }
 
 int launch_luma_from_image(const EncArgs& a, const uint32_t* const* lists, const int* counts,
-                           cudaStream_t s) {
+                           const cudaStream_t* s) {
   int k = 0;
-  if (counts[0]) { k_fdct_luma<8, true><<<(counts[0] + 15) / 16, 128, 0, s>>>(a, lists[0], counts[0]); ++k; }
-  if (counts[1]) { k_fdct_luma<16, true><<<(counts[1] + 7) / 8, 128, 0, s>>>(a, lists[1], counts[1]); ++k; }
-  if (counts[2]) { k_fdct_luma<32, true><<<(counts[2] + 3) / 4, 128, 0, s>>>(a, lists[2], counts[2]); ++k; }
+  if (counts[0]) { k_fdct_luma<8, true><<<(counts[0] + 15) / 16, 128, 0, s[0]>>>(a, lists[0], counts[0]); ++k; }
+  if (counts[1]) { k_fdct_luma<16, true><<<(counts[1] + 7) / 8, 128, 0, s[1]>>>(a, lists[1], counts[1]); ++k; }
+  if (counts[2]) { k_fdct_luma<32, true><<<(counts[2] + 3) / 4, 128, 0, s[2]>>>(a, lists[2], counts[2]); ++k; }
   return k;
 }
 
 int launch_cfl(const EncArgs& a, int* lf_seeds, void* lf_scratch, void* tile_scratch,
-               cudaStream_t s) {
+               cudaStream_t s, cudaStream_t lf_s) {
   dim3 tiles(a.geo.tw, a.geo.th);
   const int ntiles = a.geo.tw * a.geo.th;
   DF* tile_sums = (DF*)tile_scratch;
@@ -1181,19 +1181,20 @@ int launch_cfl(const EncArgs& a, int* lf_seeds, void* lf_scratch, void* tile_scr
   k_cfl_tile_bits<<<tiles, kCflThreads, 0, s>>>(a, tile_seeds);
   DF* sums = (DF*)lf_scratch;
   uint32_t* bits = (uint32_t*)((char*)lf_scratch + kLfCtas * 7 * sizeof(DF));
-  k_cfl_lf_sums<<<kLfCtas, kLfThreads, 0, s>>>(a, sums);
-  k_cfl_lf_seed<<<1, 64, 0, s>>>(a, sums, lf_seeds);
-  k_cfl_lf_bits<<<kLfCtas, kLfThreads, 0, s>>>(a, lf_seeds, bits);
-  k_cfl_lf_pick<<<1, 32, 0, s>>>(a, lf_seeds, bits);
+  // The LF factors' chain reads only the LF planes: on its own stream.
+  k_cfl_lf_sums<<<kLfCtas, kLfThreads, 0, lf_s>>>(a, sums);
+  k_cfl_lf_seed<<<1, 64, 0, lf_s>>>(a, sums, lf_seeds);
+  k_cfl_lf_bits<<<kLfCtas, kLfThreads, 0, lf_s>>>(a, lf_seeds, bits);
+  k_cfl_lf_pick<<<1, 32, 0, lf_s>>>(a, lf_seeds, bits);
   return 7;
 }
 
 int launch_quant_chroma(const EncArgs& a, const uint32_t* const* lists, const int* counts,
-                        cudaStream_t s) {
+                        const cudaStream_t* s) {
   int k = 0;
-  if (counts[0]) { k_quant_chroma<8><<<(counts[0] + 15) / 16, 128, 0, s>>>(a, lists[0], counts[0]); ++k; }
-  if (counts[1]) { k_quant_chroma<16><<<(counts[1] + 7) / 8, 128, 0, s>>>(a, lists[1], counts[1]); ++k; }
-  if (counts[2]) { k_quant_chroma<32><<<(counts[2] + 3) / 4, 128, 0, s>>>(a, lists[2], counts[2]); ++k; }
+  if (counts[0]) { k_quant_chroma<8><<<(counts[0] + 15) / 16, 128, 0, s[0]>>>(a, lists[0], counts[0]); ++k; }
+  if (counts[1]) { k_quant_chroma<16><<<(counts[1] + 7) / 8, 128, 0, s[1]>>>(a, lists[1], counts[1]); ++k; }
+  if (counts[2]) { k_quant_chroma<32><<<(counts[2] + 3) / 4, 128, 0, s[2]>>>(a, lists[2], counts[2]); ++k; }
   return k;
 }
 

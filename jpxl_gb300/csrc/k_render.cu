@@ -551,26 +551,26 @@ __global__ void __launch_bounds__(128) k_llf_sigma(RenderArgs a, const uint32_t*
 }
 
 int launch_llf_sigma(const RenderArgs& a, const uint32_t* const* lists, const int* counts,
-                     float* const* llf, cudaStream_t s) {
+                     float* const* llf, const cudaStream_t* s) {
   int k = 0;
-  if (counts[0]) { k_llf_sigma<8><<<(3 * counts[0] + 127) / 128, 128, 0, s>>>(a, lists[0], counts[0], llf[0]); ++k; }
-  if (counts[1]) { k_llf_sigma<16><<<(3 * counts[1] + 127) / 128, 128, 0, s>>>(a, lists[1], counts[1], llf[1]); ++k; }
-  if (counts[2]) { k_llf_sigma<32><<<(3 * counts[2] + 127) / 128, 128, 0, s>>>(a, lists[2], counts[2], llf[2]); ++k; }
+  if (counts[0]) { k_llf_sigma<8><<<(3 * counts[0] + 127) / 128, 128, 0, s[0]>>>(a, lists[0], counts[0], llf[0]); ++k; }
+  if (counts[1]) { k_llf_sigma<16><<<(3 * counts[1] + 127) / 128, 128, 0, s[1]>>>(a, lists[1], counts[1], llf[1]); ++k; }
+  if (counts[2]) { k_llf_sigma<32><<<(3 * counts[2] + 127) / 128, 128, 0, s[2]>>>(a, lists[2], counts[2], llf[2]); ++k; }
   return k;
 }
 
 void launch_render_varblocks(const RenderArgs& a, const uint32_t* const* lists, const int* counts,
-                             cudaStream_t s) {
+                             const cudaStream_t* s) {
 #define JPXLG_RV(IDX, R, C)                                                              \
   if (counts[IDX])                                                                       \
     k_render_vb<R, C><<<(counts[IDX] + (128 / ((R) > (C) ? (R) : (C))) - 1) /            \
                             (128 / ((R) > (C) ? (R) : (C))),                             \
-                        128, 0, s>>>(a, lists[IDX], counts[IDX]);
+                        128, 0, s[IDX]>>>(a, lists[IDX], counts[IDX]);
 #define JPXLG_RVK(IDX, R, C, K)                                                          \
   if (counts[IDX])                                                                       \
     k_render_vb<R, C, K><<<(counts[IDX] + (128 / ((R) > (C) ? (R) : (C))) - 1) /         \
                                (128 / ((R) > (C) ? (R) : (C))),                          \
-                           128, 0, s>>>(a, lists[IDX], counts[IDX]);
+                           128, 0, s[IDX]>>>(a, lists[IDX], counts[IDX]);
   // shape classes in kShapeSel order: DCT8, 16x16, 32x32, 16x8, 8x16, 32x8,
   // 8x32, 32x16, 16x32, DCT2x2, 64x64, 64x32, 32x64 (rows x cols of samples)
   JPXLG_RV(0, 8, 8)

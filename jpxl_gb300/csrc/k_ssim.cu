@@ -2,7 +2,8 @@
 // blur (k_blur.cu):
 //   S1 k_downscale3        pyramid.rs:19 2x2 mean, edge replicated
 //   S2 k_positive_xyb      color.rs:66 positive XYB (reproducible cube root)
-//   S5 k_score_finish      norms, 108 weights, remap (ssimulacra2.rs:509/:531)
+//   S5 k_score_reduce      the partial rows' sums per scale and quantity
+//      k_score_finish      norms, 108 weights, remap (ssimulacra2.rs:509/:531)
 //
 // The per-strip partial sums that S5 folds come from k_blur_cols (f32 per
 // 32 rows of a column, double-float above that, fixed order).
@@ -95,39 +96,50 @@ struct FinishArgs {
   long long pixels[6];
 };
 
-constexpr int kFinishThreads = 1024;
-constexpr int kFinishGroups = kFinishThreads / 18;  // 56 groups of 18 threads
+constexpr int kReduceThreads = 256;
+constexpr int kFinishThreads = 128;
 
+// S5a: one CTA per (quantity, scale): thread t sums the quantity's tile rows
+// t, t + 256, ... of the scale in order in double-float, then the threads'
+// sums meet in a fixed tree (warps, then warps in order).  The total goes to
+// row 0 of the scale's partial rows, column k (only this CTA reads that
+// column).  Deterministic for a given frame size; every load of a scale is
+// in flight at once instead of behind one CTA's sequential chains.
+__global__ void __launch_bounds__(kReduceThreads) k_score_reduce(DF* __restrict__ partials,
+                                                                 FinishArgs fa) {
+  __shared__ DF wsum[kReduceThreads / 32];
+  const int k = blockIdx.x, s = blockIdx.y, t = threadIdx.x;
+  size_t base = 0;
+  for (int i = 0; i < s; ++i) base += fa.ctas[i];
+  DF acc{0.0f, 0.0f};
+#pragma unroll 4
+  for (int i = t; i < fa.ctas[s]; i += kReduceThreads)
+    acc = df_add(acc, partials[(base + i) * 18 + k]);
+  const DF w = df_warp_sum(acc);
+  if ((t & 31) == 0) wsum[t >> 5] = w;
+  __syncthreads();
+  if (t == 0) {
+    DF tot = wsum[0];
+    for (int i = 1; i < kReduceThreads / 32; ++i) tot = df_add(tot, wsum[i]);
+    partials[base * 18 + k] = tot;
+  }
+}
+
+// S5b: the norms, weights and remap from the 6 x 18 sums.
 __global__ void __launch_bounds__(kFinishThreads) k_score_finish(const DF* __restrict__ partials,
                                                                  FinishArgs fa,
                                                                  double* __restrict__ out) {
-  // Per scale: thread (g, k) sums quantity k of tile rows g, g + 56, ... in
-  // order in double-float; the 56 group sums of each quantity are added in
-  // group order.  Deterministic for a given frame size, f32 issue rates.
-  __shared__ DF gsum[kFinishGroups][18];
   __shared__ double scale_sums[6][18];
   __shared__ double terms[6][3][6];
   __shared__ double wterm[108];
-  const int g = threadIdx.x / 18, k = threadIdx.x % 18;
-  size_t base = 0;
-  for (int s = 0; s < fa.nscales; ++s) {
-    if (g < kFinishGroups) {
-      DF acc{0.0f, 0.0f};
-      // Loads run ahead of the (sequential, fixed-order) additions.
-#pragma unroll 8
-      for (int i = g; i < fa.ctas[s]; i += kFinishGroups)
-        acc = df_add(acc, partials[(base + i) * 18 + k]);
-      gsum[g][k] = acc;
+  if (threadIdx.x < 18) {
+    size_t base = 0;
+    for (int s = 0; s < fa.nscales; ++s) {
+      scale_sums[s][threadIdx.x] = df_value(partials[base * 18 + threadIdx.x]);
+      base += fa.ctas[s];
     }
-    __syncthreads();
-    if (threadIdx.x < 18) {
-      DF t = gsum[0][threadIdx.x];
-      for (int i = 1; i < kFinishGroups; ++i) t = df_add(t, gsum[i][threadIdx.x]);
-      scale_sums[s][threadIdx.x] = df_value(t);
-    }
-    __syncthreads();
-    base += fa.ctas[s];
   }
+  __syncthreads();
   // pool.rs:60 norms, one (scale, channel) per thread.
   if (threadIdx.x < fa.nscales * 3) {
     const int s = threadIdx.x / 3, c = threadIdx.x % 3;
@@ -167,15 +179,17 @@ __global__ void __launch_bounds__(kFinishThreads) k_score_finish(const DF* __res
       for (int m = 0; m < 6; ++m) out[2 + (s * 3 + c) * 6 + m] = terms[s][c][m];
 }
 
-void launch_score_finish(const DF* partials, const int* ctas_per_scale, int nscales,
-                         const int* pixels_per_scale, double* out, cudaStream_t s) {
+int launch_score_finish(DF* partials, const int* ctas_per_scale, int nscales,
+                        const int* pixels_per_scale, double* out, cudaStream_t s) {
   FinishArgs fa;
   fa.nscales = nscales;
   for (int i = 0; i < 6; ++i) {
     fa.ctas[i] = i < nscales ? ctas_per_scale[i] : 0;
     fa.pixels[i] = i < nscales ? pixels_per_scale[i] : 0;
   }
+  k_score_reduce<<<dim3(18, nscales), kReduceThreads, 0, s>>>(partials, fa);
   k_score_finish<<<1, kFinishThreads, 0, s>>>(partials, fa, out);
+  return 2;
 }
 
 

@@ -620,32 +620,32 @@ void upload_tc_basis(cudaStream_t s) {
 }
 
 int launch_fdct_tc(const EncArgs& a, const uint32_t* const* lists, const int* counts, int terms,
-                   int num_sms, cudaStream_t s) {
+                   int num_sms, const cudaStream_t* s) {
   int k = 0;
-  // shape classes 0, 1, 2 are DCT8, DCT16, DCT32
+  // shape classes 0, 1, 2 are DCT8, DCT16, DCT32, each on its stream
   if (terms == 2) {
-    if (counts[0]) k += launch_fdct_one<8, 2>(a, lists[0], counts[0], num_sms, s);
-    if (counts[1]) k += launch_fdct_one<16, 2>(a, lists[1], counts[1], num_sms, s);
-    if (counts[2]) k += launch_fdct_one<32, 2>(a, lists[2], counts[2], num_sms, s);
+    if (counts[0]) k += launch_fdct_one<8, 2>(a, lists[0], counts[0], num_sms, s[0]);
+    if (counts[1]) k += launch_fdct_one<16, 2>(a, lists[1], counts[1], num_sms, s[1]);
+    if (counts[2]) k += launch_fdct_one<32, 2>(a, lists[2], counts[2], num_sms, s[2]);
   } else {
-    if (counts[0]) k += launch_fdct_one<8, 3>(a, lists[0], counts[0], num_sms, s);
-    if (counts[1]) k += launch_fdct_one<16, 3>(a, lists[1], counts[1], num_sms, s);
-    if (counts[2]) k += launch_fdct_one<32, 3>(a, lists[2], counts[2], num_sms, s);
+    if (counts[0]) k += launch_fdct_one<8, 3>(a, lists[0], counts[0], num_sms, s[0]);
+    if (counts[1]) k += launch_fdct_one<16, 3>(a, lists[1], counts[1], num_sms, s[1]);
+    if (counts[2]) k += launch_fdct_one<32, 3>(a, lists[2], counts[2], num_sms, s[2]);
   }
   return k;
 }
 
 int launch_render_tc(const RenderArgs& a, const uint32_t* const* lists, const int* counts,
-                     const float* const* llf, int terms, int num_sms, cudaStream_t s) {
+                     const float* const* llf, int terms, int num_sms, const cudaStream_t* s) {
   int k = 0;
   if (terms == 2) {
-    if (counts[0]) k += launch_render_one<8, 2>(a, lists[0], counts[0], llf[0], num_sms, s);
-    if (counts[1]) k += launch_render_one<16, 2>(a, lists[1], counts[1], llf[1], num_sms, s);
-    if (counts[2]) k += launch_render_one<32, 2>(a, lists[2], counts[2], llf[2], num_sms, s);
+    if (counts[0]) k += launch_render_one<8, 2>(a, lists[0], counts[0], llf[0], num_sms, s[0]);
+    if (counts[1]) k += launch_render_one<16, 2>(a, lists[1], counts[1], llf[1], num_sms, s[1]);
+    if (counts[2]) k += launch_render_one<32, 2>(a, lists[2], counts[2], llf[2], num_sms, s[2]);
   } else {
-    if (counts[0]) k += launch_render_one<8, 3>(a, lists[0], counts[0], llf[0], num_sms, s);
-    if (counts[1]) k += launch_render_one<16, 3>(a, lists[1], counts[1], llf[1], num_sms, s);
-    if (counts[2]) k += launch_render_one<32, 3>(a, lists[2], counts[2], llf[2], num_sms, s);
+    if (counts[0]) k += launch_render_one<8, 3>(a, lists[0], counts[0], llf[0], num_sms, s[0]);
+    if (counts[1]) k += launch_render_one<16, 3>(a, lists[1], counts[1], llf[1], num_sms, s[1]);
+    if (counts[2]) k += launch_render_one<32, 3>(a, lists[2], counts[2], llf[2], num_sms, s[2]);
   }
   return k;
 }
