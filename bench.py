@@ -380,7 +380,9 @@ def search_workload(np):
 def run_search(ctx, torch, np, steps, precisions):
     """The batched quality search: every frame x every candidate quantizer as
     one graph launch of 512 probes; the chosen quantizer per frame is the
-    coarsest whose score reaches the threshold.  Timed per precision."""
+    coarsest whose score reaches the threshold.  The launch shape comes from
+    the autotuner (jpxl_gb300.tune, on the headline precision's batch);
+    timed per precision."""
     import jpxl_gb300 as jg
 
     frames = search_workload(np)
@@ -404,15 +406,32 @@ def run_search(ctx, torch, np, steps, precisions):
                      f"{len(SEARCH_CANDIDATES)} candidate global scales = {len(slots)} probes "
                      "(encode, render at depth, SSIMULACRA2) as one CUDA graph launch; each "
                      "probe's cover from select_blocks at its quantizer"),
-        "unit": "MPix/s (rendered+scored)", "steps": steps, "lanes": 4,
+        "unit": "MPix/s (rendered+scored)", "steps": steps,
         "threshold": SEARCH_THRESHOLD}
     stream = torch.cuda.current_stream()
+
+    def items_for(prec):
+        return [jg.BatchItem(layout, ref, dev.data_ptr(), 8,
+                             jg.EncodeRequest.with_global_scale(gs, gaborish=True, epf_iters=3,
+                                                                precision=prec))
+                for layout, ref, dev, gs in slots]
+
+    # The batch's launch shape (lanes, and the tensor-core kernels' CTAs per
+    # SM) from the autotuner, tuned on the headline precision's batch; the
+    # cache goes to a scratch file, each run tunes afresh.
+    from jpxl_gb300 import tune
+    import tempfile
+    with tempfile.TemporaryDirectory() as td:
+        tuned = tune.tune_batch(ctx, items_for(precisions[0]), precision=precisions[0],
+                                device=torch.cuda.get_device_name(), lanes=(2, 4, 8),
+                                tc_ctas=None if precisions[0] == "fp32" else (2, 4),
+                                reps=2, warmup=1, path=Path(td) / "tune.json")
+    result["tuned"] = tuned
+    result["lanes"] = tuned["lanes"]
+    previous_ctas = tune.set_tc_ctas_per_sm(ctx.lib, tuned["tc_ctas_per_sm"])
     for prec in precisions:
-        items = [jg.BatchItem(layout, ref, dev.data_ptr(), 8,
-                              jg.EncodeRequest.with_global_scale(gs, gaborish=True, epf_iters=3,
-                                                                 precision=prec))
-                 for layout, ref, dev, gs in slots]
-        batch = jg.BatchProbe(ctx, items, lanes=4)
+        items = items_for(prec)
+        batch = jg.BatchProbe(ctx, items, lanes=tuned["lanes"])
         scores = torch.zeros(len(items), dtype=torch.float64, device="cuda")
         for _ in range(2):
             batch.run_device(scores.data_ptr())
@@ -434,6 +453,7 @@ def run_search(ctx, torch, np, steps, precisions):
             "value": round(px / (ms / 1e3) / 1e6, 2), "ms_per_batch": round(ms, 2),
             "frames_meeting_threshold": sum(c is not None for c in chosen),
             "chosen_global_scale": {str(gs): chosen.count(gs) for gs in SEARCH_CANDIDATES}}
+    tune.set_tc_ctas_per_sm(ctx.lib, previous_ctas)
     result["value"] = result[precisions[0]]["value"]
     result["navigate"] = run_navigate(ctx, frames, [(ref, dev) for _, ref, dev in keep
                                                     if ref is not None], np)

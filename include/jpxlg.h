@@ -205,6 +205,18 @@ int jpxlg_encode_transform(jpxlg_ctx* ctx, const jpxlg_layout* layout, const voi
 int jpxlg_encode_stages(jpxlg_ctx* ctx, const jpxlg_layout* layout, const void* rgb, int bits,
                         const jpxlg_params* params, float* xyb, float* pre, float* coeff);
 
+/* Launch tunables (no reference counterpart), process-wide, for the
+ * autotuner (jpxl_gb300/tune.py):
+ *   JPXLG_TUNE_TC_CTAS_PER_SM  persistent CTAs per SM of the split-precision
+ *                              tensor-core kernels, 1..4 (default 4: four
+ *                              128-column TMEM allocations fill an SM).
+ * jpxlg_tune_set returns the previous value (JPXLG_ERR_ARGUMENT for an
+ * unknown knob or a value out of range); launches queued afterwards use the
+ * new value (a batch captures it when it is created). */
+enum { JPXLG_TUNE_TC_CTAS_PER_SM = 0 };
+int jpxlg_tune_set(int knob, int value);
+int jpxlg_tune_get(int knob);
+
 /* Diagnostic: the decoder's 8x8 special transforms (jpxl-core varblock.rs:
  * 1218 samples_from_coefficients for DCT2x2, Hornuss, DCT4x4, DCT8x4,
  * DCT4x8 and AFV0-3, I.9.3-I.9.8) on n dequantized coefficient blocks

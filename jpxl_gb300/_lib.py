@@ -33,6 +33,8 @@ SIGNATURES: dict[str, tuple] = {
     "jpxlg_encode_transform": (_I, [_P, _P, _P, _I, _P, _P, _U32]),
     "jpxlg_encode_stages": (_I, [_P, _P, _P, _I, _P, _P, _P, _P]),
     "jpxlg_diag_special_blocks": (_I, [_P, _I, _P, _I, _P, _U32]),
+    "jpxlg_tune_set": (_I, [_I, _I]),
+    "jpxlg_tune_get": (_I, [_I]),
     "jpxlg_reconstruct": (_I, [_P, _P, _P, _P, _I, _I, _P, _U32]),
     "jpxlg_ssim2_ref_create": (_I, [_P, _P, _I, _I, _U32, C.POINTER(_P)]),
     "jpxlg_ssim2_ref_destroy": (_I, [_P]),

@@ -883,6 +883,16 @@ int jpxlg_encode_transform(jpxlg_ctx* ctx, const jpxlg_layout* L, const void* rg
   return JPXLG_OK;
 }
 
+int jpxlg_tune_set(int knob, int value) {
+  if (knob != JPXLG_TUNE_TC_CTAS_PER_SM || value < 1 || value > 4) return JPXLG_ERR_ARGUMENT;
+  return tc_ctas_per_sm(value);
+}
+
+int jpxlg_tune_get(int knob) {
+  if (knob != JPXLG_TUNE_TC_CTAS_PER_SM) return JPXLG_ERR_ARGUMENT;
+  return tc_ctas_per_sm(0);
+}
+
 int jpxlg_diag_special_blocks(jpxlg_ctx* ctx, int kind, const float* coef, int n, float* out,
                               uint32_t mem) {
   if (!ctx || !coef || !out || n <= 0) return fail(ctx, JPXLG_ERR_ARGUMENT, "null argument");

@@ -103,6 +103,9 @@ void launch_render_varblocks(const RenderArgs& a, const uint32_t* const* lists,
 // Each returns the number of kernels it launched.  The render form needs
 // 16-byte aligned coefficient planes.
 cudaError_t configure_tc_kernels();
+// Sets the tensor-core kernels' persistent CTAs per SM (1..4; other values
+// leave it) and returns the previous value.
+int tc_ctas_per_sm(int value);
 void upload_tc_basis(cudaStream_t s);
 int launch_fdct_tc(const EncArgs& a, const uint32_t* const* lists, const int* counts, int terms,
                    int num_sms, const cudaStream_t* s);

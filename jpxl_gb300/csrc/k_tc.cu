@@ -60,6 +60,7 @@
 #include <cuda_bf16.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdint>
 
@@ -557,7 +558,9 @@ __global__ void __launch_bounds__(kThreads) k_render_tc(RenderArgs a,
   end(st, &mbar, a.err);
 }
 
-int g_tc_ctas_per_sm = 4;  // four 128-column TMEM allocations fill an SM's 512
+// Persistent CTAs per SM of the tensor-core kernels: at most four, whose
+// 128-column TMEM allocations fill an SM's 512; a tunable (tc_ctas_per_sm).
+std::atomic<int> g_tc_ctas_per_sm{4};
 
 template <typename K>
 cudaError_t set_smem(K kernel, int bytes) {
@@ -568,7 +571,7 @@ template <int N, int TERMS>
 int launch_fdct_one(const EncArgs& a, const uint32_t* list, int count, int num_sms,
                     cudaStream_t s) {
   const int ntiles = (count + Tile<N, TERMS>::kVpt - 1) / Tile<N, TERMS>::kVpt;
-  const int grid = std::min(ntiles, num_sms * g_tc_ctas_per_sm);
+  const int grid = std::min(ntiles, num_sms * g_tc_ctas_per_sm.load());
   k_fdct_tc<N, TERMS><<<grid, kThreads, Tile<N, TERMS>::kBytes, s>>>(a, list, count, ntiles);
   return 1;
 }
@@ -577,13 +580,19 @@ template <int N, int TERMS>
 int launch_render_one(const RenderArgs& a, const uint32_t* list, int count, const float* llf,
                       int num_sms, cudaStream_t s) {
   const int ntiles = (count + Tile<N, TERMS>::kVpt - 1) / Tile<N, TERMS>::kVpt;
-  const int grid = std::min(ntiles, num_sms * g_tc_ctas_per_sm);
+  const int grid = std::min(ntiles, num_sms * g_tc_ctas_per_sm.load());
   k_render_tc<N, TERMS><<<grid, kThreads, Tile<N, TERMS>::kBytes, s>>>(a, list, count, ntiles,
                                                                          llf);
   return 1;
 }
 
 }  // namespace
+
+int tc_ctas_per_sm(int value) {
+  const int old = g_tc_ctas_per_sm.load();
+  if (value >= 1 && value <= 4) g_tc_ctas_per_sm.store(value);
+  return old;
+}
 
 cudaError_t configure_tc_kernels() {
   cudaError_t e = cudaSuccess;
