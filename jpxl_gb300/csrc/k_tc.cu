@@ -420,34 +420,55 @@ __global__ void __launch_bounds__(kThreads) k_fdct_tc(EncArgs a, const uint32_t*
   const Geo& geo = a.geo;
   const size_t plane = (size_t)geo.w * geo.h;
   const size_t cplane = (size_t)geo.W8 * geo.H8;
-  for (int tile = blockIdx.x; tile < ntiles && st.ok; tile += gridDim.x) {
+  // The varblock of this thread's row in a tile, and its sample row r of one
+  // channel, edges replicated (lib.rs:3008); zeros past the list's end.
+  struct Src {
+    bool active;
+    int x0, y0;
+  };
+  auto locate = [&](int tile) {
     const int vi = tile * T::kVpt + b;
     const bool active = vi < count;
     const uint32_t packed = active ? __ldg(&list[vi]) : 0u;
-    const int x0 = (int)(packed & 0xffff) * 8, y0 = (int)(packed >> 16) * 8;
-    const int yy = min(y0 + r, geo.h - 1);
-#pragma unroll 1
-    for (int c = 0; c < 3 && st.ok; ++c) {
-      float row[N];
-      if (active) {
-        // sample row r of the varblock, edges replicated (lib.rs:3008)
-        const float* p = a.pre + plane * c + (size_t)yy * geo.w;
+    return Src{active, (int)(packed & 0xffff) * 8, (int)(packed >> 16) * 8};
+  };
+  auto load_row = [&](const Src& src, int c, float* row) {
+    if (src.active) {
+      const int yy = min(src.y0 + r, geo.h - 1);
+      const float* p = a.pre + plane * c + (size_t)yy * geo.w;
 #pragma unroll
-        for (int x = 0; x < N; ++x) row[x] = __ldg(&p[min(x0 + x, geo.w - 1)]);
-      } else {
+      for (int x = 0; x < N; ++x) row[x] = __ldg(&p[min(src.x0 + x, geo.w - 1)]);
+    } else {
 #pragma unroll
-        for (int x = 0; x < N; ++x) row[x] = 0.0f;
-      }
-      transform_rows<N, TERMS>(smem, &mbar, st, row);
-      if (!st.ok) break;
-      if (active) {
-        // landscape coefficient row r of the varblock
-        float* o = a.coeff + cplane * c + (size_t)(y0 + r) * geo.W8 + x0;
+      for (int x = 0; x < N; ++x) row[x] = 0.0f;
+    }
+  };
+  // (tile, channel) steps in order; the next step's row is loaded before
+  // this step's transform, so that its latency overlaps the MMAs.
+  int tile = blockIdx.x, c = 0;
+  Src cur = tile < ntiles ? locate(tile) : Src{false, 0, 0};
+  float nxt[N];
+  if (tile < ntiles) load_row(cur, 0, nxt);
+  while (tile < ntiles && st.ok) {
+    float row[N];
 #pragma unroll
-        for (int u = 0; u < N; u += 4)
-          *reinterpret_cast<float4*>(o + u) =
-              make_float4(row[u], row[u + 1], row[u + 2], row[u + 3]);
-      }
+    for (int x = 0; x < N; ++x) row[x] = nxt[x];
+    const Src here = cur;
+    const int ch = c;
+    if (++c == 3) {
+      c = 0;
+      tile += gridDim.x;
+      if (tile < ntiles) cur = locate(tile);
+    }
+    if (tile < ntiles) load_row(cur, c, nxt);
+    transform_rows<N, TERMS>(smem, &mbar, st, row);
+    if (!st.ok) break;
+    if (here.active) {
+      // landscape coefficient row r of the varblock
+      float* o = a.coeff + cplane * ch + (size_t)(here.y0 + r) * geo.W8 + here.x0;
+#pragma unroll
+      for (int u = 0; u < N; u += 4)
+        *reinterpret_cast<float4*>(o + u) = make_float4(row[u], row[u + 1], row[u + 2], row[u + 3]);
     }
   }
   end(st, &mbar, a.err);
@@ -481,79 +502,130 @@ __global__ void __launch_bounds__(kThreads) k_render_tc(RenderArgs a,
   const size_t plane = (size_t)geo.w * geo.h;
   constexpr int slot = N == 8 ? 0 : (N == 16 ? 1 : 2);  // compact dequant slots 0..2
   const int dq_off = dq_offset(slot);
-  for (int tile = blockIdx.x; tile < ntiles && st.ok; tile += gridDim.x) {
-    if (t < T::kVpt) {
-      const int vi = tile * T::kVpt + t;
-      if (vi < count) {
-        const uint32_t packed = __ldg(&list[vi]);
-        const int bx = packed & 0xffff, by = packed >> 16;
-        s_mul[t] = hf_multiplier(a.mul_table, a.qs.global_scale,
-                                 a.hf_mul[(size_t)by * geo.bw + bx]);  // reconstruct.rs:27
-        const int tile64 = (by / 8) * geo.tw + bx / 8;
-        s_kx[t] = 0.0f + (float)a.cfl_x[tile64] / 84.0f;  // reconstruct.rs:96
-        s_kb[t] = 1.0f + (float)a.cfl_b[tile64] / 84.0f;
-      }
+  // Per-tile scalars (HF multiplier, CfL factors) of the tile's varblocks,
+  // loaded by thread t < kVpt for varblock t.
+  auto tile_scalars = [&](int tile, float& mul, float& kx, float& kb) {
+    const int vi = tile * T::kVpt + t;
+    if (t < T::kVpt && vi < count) {
+      const uint32_t packed = __ldg(&list[vi]);
+      const int bx = packed & 0xffff, by = packed >> 16;
+      mul = hf_multiplier(a.mul_table, a.qs.global_scale,
+                          a.hf_mul[(size_t)by * geo.bw + bx]);  // reconstruct.rs:27
+      const int tile64 = (by / 8) * geo.tw + bx / 8;
+      kx = 0.0f + (float)a.cfl_x[tile64] / 84.0f;  // reconstruct.rs:96
+      kb = 1.0f + (float)a.cfl_b[tile64] / 84.0f;
     }
-    __syncthreads();
+  };
+  // This thread's quantized row r of channel c of its varblock in a tile,
+  // and in the LLF rows the channel's LLF values.
+  struct QRow {
+    int q[N];
+    float l[n];
+    bool active;
+    int x0, y0;
+  };
+  auto load_q = [&](int tile, int c, QRow& qr) {
     const int vi = tile * T::kVpt + b;
-    const bool active = vi < count;
-    const uint32_t packed = active ? __ldg(&list[vi]) : 0u;
-    const int x0 = (int)(packed & 0xffff) * 8, y0 = (int)(packed >> 16) * 8;
-    float dY[N];
-#pragma unroll 1
-    for (int ci = 0; ci < 3 && st.ok; ++ci) {
-      const int c = ci == 0 ? 1 : (ci == 1 ? 0 : 2);  // luma first: CfL needs it
-      float row[N];
-      if (active) {
-        // landscape row r (plan-render lib.rs:913: adjusted * (mul*qm) *
-        // matrix, left to right), the HF CfL (lib.rs:1344), the LLF corner.
-        const float scale = s_mul[b] * a.qs.qm[c];
-        const float bias = c_tc_bias[c];
-        const float kc = c == 0 ? s_kx[b] : s_kb[b];
-        const float* m = a.dq + c * kDequantTableFloats + dq_off + r * N;
-        const float* lc = llf + (size_t)vi * 48 + c * 16 + r * n;
-        const int4* q4 =
-            reinterpret_cast<const int4*>(a.qcoeff + cplane * c + (size_t)(y0 + r) * geo.W8 + x0);
+    qr.active = vi < count;
+    const uint32_t packed = qr.active ? __ldg(&list[vi]) : 0u;
+    qr.x0 = (int)(packed & 0xffff) * 8;
+    qr.y0 = (int)(packed >> 16) * 8;
+    if (!qr.active) return;
+    const int4* q4 =
+        reinterpret_cast<const int4*>(a.qcoeff + cplane * c + (size_t)(qr.y0 + r) * geo.W8 + qr.x0);
 #pragma unroll
-        for (int u4 = 0; u4 < N / 4; ++u4) {
-          const int4 q = __ldg(&q4[u4]);
-          const float4 mm = __ldg(reinterpret_cast<const float4*>(m) + u4);
-          const int qs[4] = {q.x, q.y, q.z, q.w};
-          const float ms[4] = {mm.x, mm.y, mm.z, mm.w};
+    for (int u4 = 0; u4 < N / 4; ++u4) {
+      const int4 v = __ldg(&q4[u4]);
+      qr.q[4 * u4] = v.x;
+      qr.q[4 * u4 + 1] = v.y;
+      qr.q[4 * u4 + 2] = v.z;
+      qr.q[4 * u4 + 3] = v.w;
+    }
+    if (r < n) {
+      const float* lc = llf + (size_t)vi * 48 + c * 16 + r * n;
 #pragma unroll
-          for (int i = 0; i < 4; ++i) {
-            const int u = u4 * 4 + i;
-            float d = bias_adjust(qs[i], bias) * scale * ms[i];
-            if (c == 1) dY[u] = d;
-            else d = d + kc * dY[u];
-            if (r < n && u < n) d = __ldg(&lc[u]);
-            row[u] = d;
-          }
-        }
-      } else {
-#pragma unroll
-        for (int u = 0; u < N; ++u) row[u] = 0.0f;
+      for (int u = 0; u < n; ++u) qr.l[u] = __ldg(&lc[u]);
+    }
+  };
+  auto channel_of = [](int ci) { return ci == 0 ? 1 : (ci == 1 ? 0 : 2); };  // luma first: CfL needs it
+  // (tile, channel) steps in order; the next step's quantized row (and, at
+  // a tile's last channel, the next tile's scalars) is loaded before this
+  // step's transform, so that its latency overlaps the MMAs.
+  int tile = blockIdx.x, ci = 0;
+  float pm = 0.0f, pkx = 0.0f, pkb = 0.0f;
+  QRow nq;
+  if (tile < ntiles) {
+    tile_scalars(tile, pm, pkx, pkb);
+    load_q(tile, channel_of(0), nq);
+  }
+  float dY[N];
+  while (tile < ntiles && st.ok) {
+    if (ci == 0) {
+      if (t < T::kVpt) {
+        s_mul[t] = pm;
+        s_kx[t] = pkx;
+        s_kb[t] = pkb;
       }
-      transform_rows<N, TERMS>(smem, &mbar, st, row);
-      if (!st.ok) break;
-      if (active) {
-        const int fy = y0 + r;
-        if (fy < geo.h) {
-          float* o = a.planes + plane * c + (size_t)fy * geo.w + x0;
-          if (x0 + N <= geo.w && (geo.w & 3) == 0) {
+      __syncthreads();
+    }
+    const QRow q = nq;
+    const int c = channel_of(ci);
+    int ntile = tile, nci = ci + 1;
+    if (nci == 3) {
+      nci = 0;
+      ntile += gridDim.x;
+    }
+    if (ntile < ntiles) {
+      load_q(ntile, channel_of(nci), nq);
+      if (nci == 0) tile_scalars(ntile, pm, pkx, pkb);
+    }
+    float row[N];
+    if (q.active) {
+      // landscape row r (plan-render lib.rs:913: adjusted * (mul*qm) *
+      // matrix, left to right), the HF CfL (lib.rs:1344), the LLF corner.
+      const float scale = s_mul[b] * a.qs.qm[c];
+      const float bias = c_tc_bias[c];
+      const float kc = c == 0 ? s_kx[b] : s_kb[b];
+      const float* m = a.dq + c * kDequantTableFloats + dq_off + r * N;
 #pragma unroll
-            for (int x = 0; x < N; x += 4)
-              *reinterpret_cast<float4*>(o + x) =
-                  make_float4(row[x], row[x + 1], row[x + 2], row[x + 3]);
-          } else {
+      for (int u4 = 0; u4 < N / 4; ++u4) {
+        const float4 mm = __ldg(reinterpret_cast<const float4*>(m) + u4);
+        const float ms[4] = {mm.x, mm.y, mm.z, mm.w};
 #pragma unroll
-            for (int x = 0; x < N; ++x)
-              if (x0 + x < geo.w) o[x] = row[x];
-          }
+        for (int i = 0; i < 4; ++i) {
+          const int u = u4 * 4 + i;
+          float d = bias_adjust(q.q[u], bias) * scale * ms[i];
+          if (c == 1) dY[u] = d;
+          else d = d + kc * dY[u];
+          if (r < n && u < n) d = q.l[u < n ? u : 0];
+          row[u] = d;
+        }
+      }
+    } else {
+#pragma unroll
+      for (int u = 0; u < N; ++u) row[u] = 0.0f;
+    }
+    transform_rows<N, TERMS>(smem, &mbar, st, row);
+    if (!st.ok) break;
+    if (q.active) {
+      const int fy = q.y0 + r;
+      if (fy < geo.h) {
+        float* o = a.planes + plane * c + (size_t)fy * geo.w + q.x0;
+        if (q.x0 + N <= geo.w && (geo.w & 3) == 0) {
+#pragma unroll
+          for (int x = 0; x < N; x += 4)
+            *reinterpret_cast<float4*>(o + x) =
+                make_float4(row[x], row[x + 1], row[x + 2], row[x + 3]);
+        } else {
+#pragma unroll
+          for (int x = 0; x < N; ++x)
+            if (q.x0 + x < geo.w) o[x] = row[x];
         }
       }
     }
-    __syncthreads();  // s_* are rewritten by the next tile
+    if (nci == 0) __syncthreads();  // s_* are rewritten at the next tile's start
+    tile = ntile;
+    ci = nci;
   }
   end(st, &mbar, a.err);
 }
