@@ -761,7 +761,7 @@ __global__ void __launch_bounds__(128) k_cfl_tile_seeds(EncArgs a, const DF* __r
 
 // (3) Residual bits of every candidate through the DCT8x8 baseline quantizer
 // (cells folded onto the 8x8 grid, lib.rs:3585), then the choice.
-__global__ void __launch_bounds__(kCflThreads) k_cfl_tile_bits(EncArgs a,
+__global__ void __launch_bounds__(kCflThreads, 4) k_cfl_tile_bits(EncArgs a,
                                                                const int* __restrict__ seeds) {
   __shared__ uint32_t s_bits[kCflThreads / 32][8];
   __shared__ float s_step[2][64], s_rstep[2][64];
