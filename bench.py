@@ -68,11 +68,11 @@ STAGE_GROUP = {"xyb": "encode", "precondition": "encode", "fdct_luma": "encode",
 # The metric's blur kernels, each timed under its own stage: algorithmic bytes
 # per pixel of every pyramid scale (f32 planes read and written once):
 # k_blur_rows<3> reads the candidate's and the reference's positive XYB and
-# writes the nine row-pass planes (15 planes); k_blur_col_local<3> and
-# k_blur_col_scan<3> read the nine (9); k_blur_col_out<3> reads the nine and
-# the reference's mu, sigma11 and XYB and the candidate's XYB (21).
+# writes the nine row-pass planes (15 planes); k_blur_col_out<3> (the column
+# pass with the ripple's segment scan inside) reads the nine and the
+# reference's mu, sigma11 and XYB and the candidate's XYB (21).  The column
+# ripple's stage now holds only the reset of the scan's flags.
 KERNEL_STAGES = {"ssim_rows": ("k_blur_rows<3>", 60.0),
-                 "ssim_col_ripple": ("k_blur_col_local<3> + k_blur_col_scan<3>", 36.0),
                  "ssim_col_out": ("k_blur_col_out<3>", 84.0)}
 
 

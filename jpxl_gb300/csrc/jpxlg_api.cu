@@ -180,7 +180,7 @@ void ssim_stage_hook(void* user, int part) {
   jpxlg_ctx* ctx = static_cast<jpxlg_ctx*>(user);
   static const int kNext[4] = {JPXLG_STAGE_SSIM_ROWS, JPXLG_STAGE_SSIM_COL_RIPPLE,
                                JPXLG_STAGE_SSIM_COL_OUT, JPXLG_STAGE_SSIM};
-  static const int kLaunched[4] = {0, 1, 2, 1};  // the kernels since the previous part
+  static const int kLaunched[4] = {0, 1, 0, 1};  // the kernels since the previous part
   ctx->launches += kLaunched[part];
   stage_end(ctx);
   stage_begin(ctx, kNext[part]);
@@ -248,6 +248,8 @@ int sync_and_check(jpxlg_ctx* ctx) {
     if (err & kDevBadStep) return fail(ctx, JPXLG_ERR_QUANT, "a degenerate quantization step");
     if (err & kDevTcTimeout)
       return fail(ctx, JPXLG_ERR_CUDA, "a tensor-core transform timed out waiting for its MMA");
+    if (err & kDevBlurTimeout)
+      return fail(ctx, JPXLG_ERR_CUDA, "the blur's column scan timed out waiting for a segment");
     return fail(ctx, JPXLG_ERR_BLOCK_MAP, "a block-map entry the kernels cannot place");
   }
   return JPXLG_OK;
@@ -559,7 +561,8 @@ int score_device(jpxlg_ctx* ctx, const jpxlg_ref* ref, const float* cand_dev,
       next += 6 * ns;
     }
     ctas[s] = launch_score_scale(cur_xyb, rs, ctx->hpl.as<float>(), ctx->bcarry.as<float>(), 0,
-                                 3, part, ctx->stream, ssim_stage_hook, ctx);  // counts its 4
+                                 3, part, ctx->d_words, ctx->stream, ssim_stage_hook,
+                                 ctx);  // the hook counts its kernels
     pixels[s] = rs.w * rs.h;
     part += (size_t)ctas[s] * 18;
   }
@@ -1052,8 +1055,8 @@ int jpxlg_ssim2_ref_create(jpxlg_ctx* ctx, const float* rgb, int w, int h, uint3
     cursor += 3 * n;
     launch_positive_xyb(level, sc.xyb, n, ctx->num_sms, ctx->stream);
     launch_ref_moments(sc.xyb, sc.mu, sc.s11, ctx->hpl.as<float>(), ctx->bcarry.as<float>(), sc.w,
-                       sc.h, ctx->stream);
-    k += 1 + 4;
+                       sc.h, ctx->d_words, ctx->stream);
+    k += 1 + 2;
   }
   int rc = after_launch(ctx, k);
   if (rc) {
@@ -1521,8 +1524,8 @@ extern "C" int jpxlg_ssim2_score_static(jpxlg_ctx* ctx, const jpxlg_ref* ref,
       ++k;
     }
     for (int c = 0; c < 3; ++c) {
-      ctas[s] = launch_score_scale(xyb, rs, hpl, carry, c, 1, part, ctx->stream);
-      k += 4;
+      ctas[s] = launch_score_scale(xyb, rs, hpl, carry, c, 1, part, ctx->d_words, ctx->stream);
+      k += kScoreScaleKernels;
     }
     pixels[s] = rs.w * rs.h;
     part += (size_t)ctas[s] * 18;

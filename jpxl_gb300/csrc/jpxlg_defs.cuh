@@ -17,6 +17,7 @@ enum DevError : uint32_t {
   kDevBadStep = 1u << 1,      // degenerate quantization step
   kDevBlockMap = 1u << 2,     // a block-map entry the kernel cannot place
   kDevTcTimeout = 1u << 3,    // a bounded wait on a tensor-core MMA ran out
+  kDevBlurTimeout = 1u << 4,  // a bounded wait on a previous column segment ran out
 };
 
 __device__ __forceinline__ void raise_error(uint32_t* err, uint32_t bit) {

@@ -176,22 +176,26 @@ size_t blur_carry_floats(int w, int h);
 void launch_downscale3(const float* in, int w, int h, float* out, float* xyb, cudaStream_t s);
 void launch_positive_xyb(const float* rgb, float* xyb, size_t n, int num_sms, cudaStream_t s);
 // Reference side of one scale: mu = blur(xyb), s11 = blur(xyb * xyb) per
-// channel; hpl (6 w*h planes) and carry (blur_carry_floats) are scratch.
+// channel; hpl (6 w*h planes) and carry (blur_carry_floats) are scratch; a
+// column-scan wait that runs out raises kDevBlurTimeout in err.  Three
+// launches: the row pass, the column flags' reset, the column pass.
 void launch_ref_moments(const float* xyb, float* mu, float* s11, float* hpl, float* carry, int w,
-                        int h, cudaStream_t s);
+                        int h, uint32_t* err, cudaStream_t s);
 // Candidate side of one scale for channels c0 .. c0+nch-1: cand_xyb is the
 // candidate's positive XYB [3][w*h]; hpl (3 * nch w*h planes) and carry
 // (blur_carry_floats) are scratch; partial receives one row of 18
 // double-float sums (8 bytes each) per 32 x 32 tile, each channel filling
 // its six.  Returns the number of rows (blur_partial_rows).
 struct DF;
-// Called between a scale's kernels when the caller times them: part 0
-// before the row pass, 1 before the column ripple, 2 before the column
-// outputs, 3 after them.
+// Called between a scale's launches when the caller times them: part 0
+// before the row pass, 1 after it, 2 before the column pass (its flags'
+// reset and its kernel, which runs the ripple's segment scan inside), 3
+// after it.  Two kernels per scale (kScoreScaleKernels).
 using ScaleHook = void (*)(void* user, int part);
+constexpr int kScoreScaleKernels = 2;
 int launch_score_scale(const float* cand_xyb, const SsimScale& ref, float* hpl, float* carry,
-                       int c0, int nch, DF* partial, cudaStream_t s, ScaleHook hook = nullptr,
-                       void* user = nullptr);
+                       int c0, int nch, DF* partial, uint32_t* err, cudaStream_t s,
+                       ScaleHook hook = nullptr, void* user = nullptr);
 // Two launches (the per-scale sums, then the score); returns 2.  The sums
 // overwrite row 0 of each scale's partial rows.
 int launch_score_finish(DF* partials, const int* ctas_per_scale, int nscales,

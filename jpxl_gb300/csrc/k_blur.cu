@@ -26,24 +26,27 @@
 // Lines are split into segments.  Each segment runs its resonators from
 // rest; a scan over the segments (after L steps the state is M^L times the
 // entry state plus the segment's own response, M the resonator's 2x2 step
-// matrix) gives each segment its entry state; each segment then walks again
-// from that state recording R_j, and the FIR outputs, independent of one
-// another, are formed in parallel.  Arithmetic is paired (two f32 lanes per
-// instruction, each rounded as the scalar operation): rows two at a time in
-// the row pass, columns two at a time in the column pass.
-//   B1 k_blur_rows<NQ>       one CTA per row pair and channel, one segment per
-//                            thread; NQ quantities x, x*x (and r*x), products
-//                            rounded to f32 as blur.rs:395 forms them
-//   B2 k_blur_col_local<NQ>  every 32-row segment's response from rest, a
-//                            warp per segment and 32-column strip
-//      k_blur_col_scan<NQ>   the entry states, segments in order, a thread
-//                            per column, quantity and resonator
-//   B3 k_blur_col_out<NQ>    one CTA per 32 x 32 tile and channel: the ripple
-//                            walk per column and quantity, then the outputs;
-//                            NQ = 2 writes mu and sigma11 (reference.rs:90),
-//                            NQ = 3 evaluates pool.rs:248's per-pixel terms on
-//                            the blurred mu2, sigma22, sigma12 and writes one
-//                            row of partial sums per tile
+// matrix) gives each segment its entry state; each segment adds the
+// homogeneous response of that state to its R from rest, and the FIR
+// outputs, independent of one another, are formed in parallel.  Arithmetic
+// is paired (two f32 lanes per instruction, each rounded as the scalar
+// operation): rows two at a time in the row pass, columns two at a time in
+// the column pass.
+//   B1 k_blur_rows<NQ>     one CTA per row pair and channel, one segment per
+//                          thread, the scan across the CTA's threads; NQ
+//                          quantities x, x*x (and r*x), products rounded to
+//                          f32 as blur.rs:395 forms them
+//   B2 k_blur_col_out<NQ>  one CTA per 32-row segment of a 32-column strip
+//                          and channel: the ripple from rest per column and
+//                          quantity, the chained scan over the strip's
+//                          segments (each CTA waits, boundedly, for the
+//                          previous segment's published state; CTAs take
+//                          their segments in the order they start), then the
+//                          outputs; NQ = 2 writes mu and sigma11
+//                          (reference.rs:90), NQ = 3 evaluates pool.rs:248's
+//                          per-pixel terms on the blurred mu2, sigma22,
+//                          sigma12 and writes one row of partial sums per
+//                          tile
 #include <algorithm>
 #include <cmath>
 #include <cstdint>
@@ -378,7 +381,6 @@ __global__ void __launch_bounds__(kRowThreads, 6) k_blur_rows(RowArgs a) {
 
 constexpr int kColW = 32;      // columns per strip
 constexpr int kColT = 32;      // rows per segment (and per output tile)
-constexpr int kCarryWarps = 8;
 
 struct ColArgs {
   const float* hpl;  // [nch][NQ][h][w] row-pass planes
@@ -390,87 +392,20 @@ struct ColArgs {
   const float* rx;
   const float* cx;
   DF* partial;  // NQ == 3: [nseg][strips][18]
-  int w, h, c0, nseg;
+  uint32_t* err;  // the context's device error word
+  int w, h, c0, nseg, nch, strips;
   float nz;
   float pw[3][4];  // M_k^kColT
 };
 
-// B2a: every segment's response from rest; one warp per segment, a lane per
-// column (grid: strips x segment groups x channels).
-template <int NQ>
-__global__ void __launch_bounds__(kColW * kCarryWarps, 2) k_blur_col_local(ColArgs a) {
-  const int lane = threadIdx.x % kColW, g = threadIdx.x / kColW;
-  const int x = blockIdx.x * kColW + lane;
-  const int sg = blockIdx.y * kCarryWarps + g, ch = blockIdx.z;
-  if (sg >= a.nseg) return;
-  const size_t n = (size_t)a.w * a.h;
-  const bool col_ok = x < a.w;
-  const float* H = a.hpl + (size_t)ch * NQ * n + (col_ok ? x : 0);
-  float* C = a.carry + (size_t)ch * a.nseg * NQ * 6 * a.w + (col_ok ? x : 0);
-  auto hv = [&](int q, int row) -> float {
-    return (col_ok && row >= 0 && row < a.h) ? __ldg(H + (size_t)q * n + (size_t)row * a.w)
-                                             : 0.0f;
-  };
-  const int r0 = sg * kColT, r1 = min(r0 + kColT, a.h);
-  Ripple rp[NQ];
-#pragma unroll
-  for (int q = 0; q < NQ; ++q)
-#pragma unroll
-    for (int k = 0; k < 3; ++k) rp[q].p[k] = rp[q].q[k] = 0.0f;
-#pragma unroll 4
-  for (int j = r0; j < r1; ++j)
-#pragma unroll
-    for (int q = 0; q < NQ; ++q) ripple_step(rp[q], pair_error(hv(q, j - 6), hv(q, j + 4)));
-  if (col_ok)
-#pragma unroll
-    for (int q = 0; q < NQ; ++q)
-#pragma unroll
-      for (int k = 0; k < 3; ++k) {
-        C[((size_t)sg * NQ * 6 + q * 6 + 2 * k) * a.w] = rp[q].p[k];
-        C[((size_t)sg * NQ * 6 + q * 6 + 2 * k + 1) * a.w] = rp[q].q[k];
-      }
+// The column pass's cross-segment state lives in the carry buffer:
+// [nch][nseg][NQ * 6][w] inclusive states (the ripple's state after each
+// segment, from the top of the plane), then the publication flags
+// [nch][strips][nseg] and the work counter, zeroed before each launch.
+__host__ __device__ inline size_t col_state_floats(int nch, int nseg, int w) {
+  return (size_t)nch * nseg * 3 * 6 * w;
 }
-
-// B2b: entry states, segments in order; one thread per column, quantity and
-// resonator (grid: strips x channels, NQ * 3 warps).
-template <int NQ>
-__global__ void __launch_bounds__(kColW * NQ * 3) k_blur_col_scan(ColArgs a) {
-  const int lane = threadIdx.x % kColW, qk = threadIdx.x / kColW;
-  const int x = blockIdx.x * kColW + lane;
-  const int ch = blockIdx.y;
-  if (x >= a.w) return;
-  const int k = qk % 3;
-  const float* m = a.pw[k];
-  const float* C = a.carry + (size_t)ch * a.nseg * NQ * 6 * a.w + x;
-  float* E = a.carry + (size_t)gridDim.y * a.nseg * NQ * 6 * a.w +
-             (size_t)ch * a.nseg * NQ * 6 * a.w + x;
-  const size_t off = ((size_t)(qk / 3) * 6 + 2 * k) * a.w;
-  const size_t step = (size_t)NQ * 6 * a.w;
-  // The first segment's entry: blur.rs:574 runs the recursion from four rows
-  // before the plane, fed with 0 + rows 0..3 (zero ripple for finite samples,
-  // NaN for the rest of the column from a non-finite one).
-  float sp = 0.0f, sq = 0.0f;
-  {
-    const size_t n = (size_t)a.w * a.h;
-    const float* H = a.hpl + ((size_t)ch * NQ + qk / 3) * n + x;
-    for (int i = 0; i < 4 && i < a.h; ++i) {
-      const float e = pair_error(0.0f, __ldg(H + (size_t)i * a.w));
-      const float o = (e * c_blur.a[k] + c_blur.b[k] * sp) - sq;
-      sq = sp;
-      sp = o;
-    }
-  }
-#pragma unroll 8
-  for (int sg = 0; sg < a.nseg; ++sg) {
-    const float bp = __ldg(C + off + sg * step), bq = __ldg(C + off + sg * step + a.w);
-    E[off + sg * step] = sp;
-    E[off + sg * step + a.w] = sq;
-    const float np = (m[0] * sp + m[1] * sq) + bp;
-    const float nq = (m[2] * sp + m[3] * sq) + bq;
-    sp = np;
-    sq = nq;
-  }
-}
+constexpr uint32_t kColWaitLimit = 1u << 20;  // polls of a predecessor's flag (about a second)
 
 constexpr int kOutThreads = 256;
 
@@ -479,11 +414,26 @@ __global__ void __launch_bounds__(kOutThreads, 4) k_blur_col_out(ColArgs a) {
   __shared__ __align__(16) float tile[NQ][kColT + 10][kColW];  // rows r0-6 .. r0+kColT+3
   __shared__ __align__(16) float rp[NQ][kColT][kColW];
   __shared__ DF red[kOutThreads / 32][6];
-  const int sx = blockIdx.x, sg = blockIdx.y, ch = blockIdx.z, c = a.c0 + ch;
+  __shared__ float half_end[2][NQ][6][kColW];  // each half's end state from rest
+  __shared__ float entry[NQ][6][kColW];        // the segment's entry state
+  __shared__ int s_item, s_late;
+  const int t = threadIdx.x;
+  float* const incl = a.carry;  // inclusive states
+  int* const flags = reinterpret_cast<int*>(a.carry + col_state_floats(a.nch, a.nseg, a.w));
+  int* const counter = flags + (size_t)a.nch * a.strips * a.nseg;
+  // Items in the order CTAs start (segments slowest), so that the segment a
+  // CTA waits for belongs to a CTA that has already started.
+  if (t == 0) {
+    s_item = atomicAdd(counter, 1);
+    s_late = 0;
+  }
+  __syncthreads();
+  const int per_sg = a.strips * a.nch;
+  const int sg = s_item / per_sg, ch = (s_item % per_sg) / a.strips, sx = s_item % a.strips;
+  const int c = a.c0 + ch;
   const int x0 = sx * kColW, r0 = sg * kColT;
   const size_t n = (size_t)a.w * a.h;
   const float* H = a.hpl + (size_t)ch * NQ * n;
-  const int t = threadIdx.x;
   {
     constexpr int kElems = (kColT + 10) * kColW;
     constexpr int kIt = (kElems + kOutThreads - 1) / kOutThreads;
@@ -509,44 +459,103 @@ __global__ void __launch_bounds__(kOutThreads, 4) k_blur_col_out(ColArgs a) {
   }
   __syncthreads();
   // The ripple in two halves of kColT / 2 rows per column and quantity: each
-  // half walks from rest (R from rest, and the first half's end state), then
-  // adds the homogeneous response of its entry state (the tile's entry for
-  // the first half; M^(kColT/2) times it plus the first half's end state for
-  // the second) through the U table.
+  // half walks from rest, recording R from rest and its end state.
   constexpr int kHalf = kColT / 2;
-  __shared__ float half_end[NQ][6][kColW];
   const bool walker = t < 2 * NQ * kColW;
-  const int wq = (t / kColW) % NQ, wh = t / (NQ * kColW), wl = t % kColW, wx = x0 + wl;
+  const int wq = (t / kColW) % NQ, wh = t / (NQ * kColW), wl = t % kColW;
   if (walker) {
     Ripple st = {{0, 0, 0}, {0, 0, 0}};
 #pragma unroll 8
     for (int r = wh * kHalf; r < (wh + 1) * kHalf; ++r)
       rp[wq][r][wl] = ripple_step(st, pair_error(tile[wq][r][wl], tile[wq][r + 10][wl]));
-    if (wh == 0)
 #pragma unroll
-      for (int k = 0; k < 3; ++k) {
-        half_end[wq][2 * k][wl] = st.p[k];
-        half_end[wq][2 * k + 1][wl] = st.q[k];
-      }
+    for (int k = 0; k < 3; ++k) {
+      half_end[wh][wq][2 * k][wl] = st.p[k];
+      half_end[wh][wq][2 * k + 1][wl] = st.q[k];
+    }
   }
   __syncthreads();
+  // The chained scan over the column's segments: the entry state is the
+  // previous segment's inclusive state (for the first segment, the state
+  // blur.rs:574 reaches over its four warm-up rows, fed with 0 + rows 0..3:
+  // zero ripple for finite samples); this segment's inclusive state is
+  // M^kColT times the entry plus its own response from rest, M^kHalf times
+  // the first half's end state plus the second's.  Published with a flag;
+  // every wait is bounded and a wait that runs out raises kDevBlurTimeout.
+  const bool scanner = t < NQ * kColW;
+  const int sq = t / kColW, sl = t % kColW, sxc = x0 + sl;
+  float* const my_incl = incl + ((size_t)(ch * a.nseg + sg) * NQ * 6 + sq * 6) * a.w + sxc;
+  if (sg == 0) {
+    if (scanner)
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        float sp = 0.0f, sqq = 0.0f;
+        for (int i = 0; i < 4 && i < a.h; ++i) {
+          const float e = pair_error(0.0f, tile[sq][6 + i][sl]);
+          const float o = (e * c_blur.a[k] + c_blur.b[k] * sp) - sqq;
+          sqq = sp;
+          sp = o;
+        }
+        entry[sq][2 * k][sl] = sp;
+        entry[sq][2 * k + 1][sl] = sqq;
+      }
+  } else {
+    int* const prev_flag = flags + ((size_t)ch * a.strips + sx) * a.nseg + (sg - 1);
+    if (t == 0) {
+      uint32_t it = 0;
+      while (atomicAdd(prev_flag, 0) == 0 && it < kColWaitLimit) {
+        __nanosleep(64);
+        ++it;
+      }
+      if (it == kColWaitLimit) s_late = 1;
+      __threadfence();
+    }
+    __syncthreads();
+    if (scanner && sxc < a.w) {
+      const float* pv = my_incl - (size_t)NQ * 6 * a.w;
+#pragma unroll
+      for (int k = 0; k < 6; ++k) entry[sq][k][sl] = __ldcg(pv + (size_t)k * a.w);
+    } else if (scanner) {
+#pragma unroll
+      for (int k = 0; k < 6; ++k) entry[sq][k][sl] = 0.0f;
+    }
+  }
+  if (scanner && sxc < a.w) {
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      const float* U = c_blur.U[k];
+      const float u0 = U[kHalf % 20], u1 = U[(kHalf - 1) % 20], u2 = U[(kHalf - 2) % 20];
+      const float p1 = half_end[0][sq][2 * k][sl], q1 = half_end[0][sq][2 * k + 1][sl];
+      const float bp = (u0 * p1 - u1 * q1) + half_end[1][sq][2 * k][sl];
+      const float bq = (u1 * p1 - u2 * q1) + half_end[1][sq][2 * k + 1][sl];
+      const float* m = a.pw[k];
+      const float sp = entry[sq][2 * k][sl], sqq = entry[sq][2 * k + 1][sl];
+      my_incl[(size_t)(2 * k) * a.w] = (m[0] * sp + m[1] * sqq) + bp;
+      my_incl[(size_t)(2 * k + 1) * a.w] = (m[2] * sp + m[3] * sqq) + bq;
+    }
+    __threadfence();
+  }
+  __syncthreads();
+  if (t == 0) {
+    atomicExch(flags + ((size_t)ch * a.strips + sx) * a.nseg + sg, 1);
+    if (s_late) raise_error(a.err, kDevBlurTimeout);
+  }
+  // Each half adds the homogeneous response of its entry state through the
+  // U table: the segment's entry for the first half, M^kHalf times it plus
+  // the first half's end state for the second.
   if (walker) {
-    const float* C = a.carry + (size_t)gridDim.z * a.nseg * NQ * 6 * a.w +
-                     ((size_t)(ch * a.nseg + sg) * NQ * 6 + wq * 6) * a.w + wx;
     float ep[3], eq[3];
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
-      const float p = wx < a.w ? C[(size_t)(2 * k) * a.w] : 0.0f;
-      const float q = wx < a.w ? C[(size_t)(2 * k + 1) * a.w] : 0.0f;
+      const float p = entry[wq][2 * k][wl], q = entry[wq][2 * k + 1][wl];
       if (wh == 0) {
         ep[k] = p;
         eq[k] = q;
       } else {
-        // M^kHalf (p, q) + the first half's end state.
         const float* U = c_blur.U[k];
         const float u0 = U[(kHalf) % 20], u1 = U[(kHalf - 1) % 20], u2 = U[(kHalf - 2) % 20];
-        ep[k] = (u0 * p - u1 * q) + half_end[wq][2 * k][wl];
-        eq[k] = (u1 * p - u2 * q) + half_end[wq][2 * k + 1][wl];
+        ep[k] = (u0 * p - u1 * q) + half_end[0][wq][2 * k][wl];
+        eq[k] = (u1 * p - u2 * q) + half_end[0][wq][2 * k + 1][wl];
       }
     }
 #pragma unroll 4
@@ -647,7 +656,7 @@ __global__ void __launch_bounds__(kOutThreads, 4) k_blur_col_out(ColArgs a) {
     if (t < 6) {
       DF s = red[0][t];
       for (int i = 1; i < kOutThreads / 32; ++i) s = df_add(s, red[i][t]);
-      a.partial[((size_t)sg * gridDim.x + sx) * 18 + c * 6 + t] = s;
+      a.partial[((size_t)sg * a.strips + sx) * 18 + c * 6 + t] = s;
     }
   }
 }
@@ -671,12 +680,24 @@ void fill_row_args(RowArgs& a, int w, int h) {
   for (int l = 0; l < kRowLevels; ++l) resonator_power((long long)a.seg << l, a.pw[l]);
 }
 
-void fill_col_args(ColArgs& a, int w, int h) {
+void fill_col_args(ColArgs& a, int w, int h, int nch, uint32_t* err) {
   a.w = w;
   a.h = h;
   a.nseg = (h + kColT - 1) / kColT;
+  a.nch = nch;
+  a.strips = (w + kColW - 1) / kColW;
+  a.err = err;
   a.nz = -0.0f;
   resonator_power(kColT, a.pw);
+}
+
+// The column pass: the flags and work counter zeroed, then one CTA per
+// 32 x 32 tile and channel.
+template <int NQ>
+void launch_columns(const ColArgs& ca, cudaStream_t s) {
+  int* flags = reinterpret_cast<int*>(ca.carry + col_state_floats(ca.nch, ca.nseg, ca.w));
+  cudaMemsetAsync(flags, 0, ((size_t)ca.nch * ca.strips * ca.nseg + 1) * sizeof(int), s);
+  k_blur_col_out<NQ><<<ca.strips * ca.nseg * ca.nch, kOutThreads, 0, s>>>(ca);
 }
 
 }  // namespace
@@ -698,11 +719,13 @@ int blur_partial_rows(int w, int h) {
 }
 
 size_t blur_carry_floats(int w, int h) {
+  // the inclusive states of three channels, then the flags and the counter
+  // (which the same count of floats again covers many times over)
   return (size_t)2 * 3 * ((h + kColT - 1) / kColT) * 3 * 6 * w;
 }
 
 void launch_ref_moments(const float* xyb, float* mu, float* s11, float* hpl, float* carry, int w,
-                        int h, cudaStream_t s) {
+                        int h, uint32_t* err, cudaStream_t s) {
   RowArgs ra{};
   ra.x = xyb;
   ra.out = hpl;
@@ -715,17 +738,13 @@ void launch_ref_moments(const float* xyb, float* mu, float* s11, float* hpl, flo
   ca.mu = mu;
   ca.s11 = s11;
   ca.c0 = 0;
-  fill_col_args(ca, w, h);
-  const int strips = (w + kColW - 1) / kColW;
-  const int groups = (ca.nseg + kCarryWarps - 1) / kCarryWarps;
-  k_blur_col_local<2><<<dim3(strips, groups, 3), kColW * kCarryWarps, 0, s>>>(ca);
-  k_blur_col_scan<2><<<dim3(strips, 3), kColW * 2 * 3, 0, s>>>(ca);
-  k_blur_col_out<2><<<dim3(strips, ca.nseg, 3), kOutThreads, 0, s>>>(ca);
+  fill_col_args(ca, w, h, 3, err);
+  launch_columns<2>(ca, s);
 }
 
 int launch_score_scale(const float* cand_xyb, const SsimScale& ref, float* hpl, float* carry,
-                       int c0, int nch, DF* partial, cudaStream_t s, ScaleHook hook,
-                       void* user) {
+                       int c0, int nch, DF* partial, uint32_t* err, cudaStream_t s,
+                       ScaleHook hook, void* user) {
   const int w = ref.w, h = ref.h;
   if (hook) hook(user, 0);
   RowArgs ra{};
@@ -745,13 +764,9 @@ int launch_score_scale(const float* cand_xyb, const SsimScale& ref, float* hpl, 
   ca.cx = cand_xyb;
   ca.partial = partial;
   ca.c0 = c0;
-  fill_col_args(ca, w, h);
-  const int strips = (w + kColW - 1) / kColW;
-  const int groups = (ca.nseg + kCarryWarps - 1) / kCarryWarps;
-  k_blur_col_local<3><<<dim3(strips, groups, nch), kColW * kCarryWarps, 0, s>>>(ca);
-  k_blur_col_scan<3><<<dim3(strips, nch), kColW * 3 * 3, 0, s>>>(ca);
+  fill_col_args(ca, w, h, nch, err);
   if (hook) hook(user, 2);
-  k_blur_col_out<3><<<dim3(strips, ca.nseg, nch), kOutThreads, 0, s>>>(ca);
+  launch_columns<3>(ca, s);
   if (hook) hook(user, 3);
   return blur_partial_rows(w, h);
 }
