@@ -176,8 +176,9 @@ enum {
   JPXLG_STAGE_COLOUR,           /* R4 */
   JPXLG_STAGE_SSIM,             /* S1-S5 candidate side, but for the three below */
   JPXLG_STAGE_SSIM_ROWS,        /* S3 blur row pass (every scale) */
-  JPXLG_STAGE_SSIM_COL_RIPPLE,  /* S3 blur column ripple: segment responses, entry states */
-  JPXLG_STAGE_SSIM_COL_OUT,     /* S3/S4 blur column outputs with the per-pixel terms */
+  JPXLG_STAGE_SSIM_COL_RIPPLE,  /* S3 the reset of the column scan's flags (the ripple's
+                                   segment scan runs inside the column pass) */
+  JPXLG_STAGE_SSIM_COL_OUT,     /* S3/S4 blur column pass with the per-pixel terms */
   JPXLG_STAGE_COUNT
 };
 int jpxlg_stage_timing(jpxlg_ctx* ctx, int enable);
