@@ -327,8 +327,7 @@ int transform_frame(jpxlg_ctx* ctx, const Geo& g, const void* rgb_dev, int bits,
   if (p->gaborish) {
     CK(ctx->pre.ensure(3 * n * sizeof(float)));
     stage_begin(ctx, JPXLG_STAGE_PRECONDITION);
-    launch_precondition(xyb, ctx->pre.as<float>(), g.w, g.h, ctx->stream);
-    rc = after_launch(ctx, 1);
+    rc = after_launch(ctx, launch_precondition(xyb, ctx->pre.as<float>(), g.w, g.h, ctx->stream));
     stage_end(ctx);
     if (rc) return rc;
     pre = ctx->pre.as<float>();

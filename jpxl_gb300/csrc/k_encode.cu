@@ -6,6 +6,7 @@
 //   K5 k_quant_chroma<N>   X/B quantization against reconstructed luma
 // Each kernel restates the reference arithmetic it replaces (cited per
 // kernel) in the reference's operation order; the build uses -fmad=false.
+#include <algorithm>
 #include <cstdint>
 
 #include "jpxlg_common.cuh"
@@ -74,7 +75,7 @@ void launch_srgb_to_xyb(const void* rgb, int bits, size_t n, const float* lut, f
 // ---------------------------------------------------------------------------
 // K2 — jpxl-encode vardct/gaborish.rs:218 precondition_xyb_planes: twelve
 // Jacobi steps x <- x + (f - Kx) * (1/centre) (tail: / centre) against the
-// encoder's non-FMA J.1 kernel.  All twelve steps run on one shared-memory
+// encoder's non-FMA J.1 kernel.  All twelve steps run on one register-resident
 // tile with a 12-sample halo, so the plane is read once and written once.
 //
 // Bit parity with the reference's position-dependent arithmetic:
@@ -89,45 +90,45 @@ void launch_srgb_to_xyb(const void* rgb, int bits, size_t n, const float* lut, f
 // outside the frame is ever read after the load.
 // ---------------------------------------------------------------------------
 
-constexpr int kPreTile = 64;
+// Tiling.  A CTA owns a 128 x 128 tile of one plane with a 12-sample halo
+// (104 x 104 outputs).  Lane l of warp v holds columns 4l .. 4l+3 of tile
+// rows 4v .. 4v+3 in registers for all twelve steps: west and east
+// neighbours come from the adjacent lanes by shuffle, the rows above and
+// below the warp's four from the neighbouring warps through a shared-memory
+// copy of the step's input (double-buffered, one barrier per step), and the
+// source plane F from shared memory.  Every step updates the whole tile; a
+// cell k samples from the tile's edge is exact for k steps, so after twelve
+// the inner 104 x 104 are, and no cell of the edge ring is ever read by one
+// nearer the centre than itself.
+//
+// Two kernels cover a frame: the tiles whose haloed extent has no cell of
+// another rule (kEdge false), and the ring of tiles around them (kEdge
+// true).  There each step keeps the whole tile's input in shared memory;
+// after the paired update the CTA's threads share out the cells of another
+// rule (frame border, columns past the groups of four, the division tail)
+// and recompute them from their nine taps at mirrored frame coordinates
+// (always among the cell's own 3 x 3 neighbourhood), as the reference does,
+// into the next step's input, which the owning threads read back.
+constexpr int kPreOut = 104;
 constexpr int kPreHalo = 12;
-constexpr int kPreS = kPreTile + 2 * kPreHalo;  // 88
-constexpr int kPreThreads = 512;
-// Three planes (source F and the ping-pong pair) with a 4-float pad on both
-// sides, so that the paired loop's edge lanes may read one column past the
-// region; the base stays 16-byte aligned.
-constexpr int kPrePad = 4;
-constexpr size_t kPreSmem = (3 * kPreS * kPreS + 2 * kPrePad) * sizeof(float);
-
-// Interior-tile mapping of step `it`: lane t updates the column pair
-// p_lo + t % np (columns 2p, 2p+1) over the rows of band t / np; the band
-// is (t * mg) >> 16, exact for t < kPreThreads (checked below).
-struct PreStep {
-  int p_lo, np, mg, bands, rows;
-};
-constexpr PreStep pre_step(int it) {
-  const int lo = 1 + it, hi = kPreS - 1 - it, wd = hi - lo;
-  const int p_lo = lo >> 1, p_hi = (hi - 1) >> 1, np = p_hi - p_lo + 1;
-  const int bands = kPreThreads / np;
-  return {p_lo, np, (65536 + np - 1) / np, bands, (wd + bands - 1) / bands};
-}
-constexpr bool pre_steps_exact() {
-  for (int it = 0; it < 12; ++it) {
-    const PreStep s = pre_step(it);
-    for (int t = 0; t < kPreThreads; ++t)
-      if (((t * s.mg) >> 16) != t / s.np) return false;
-    if (s.bands * s.rows < (kPreS - 2 - 2 * it)) return false;
-  }
-  return true;
-}
-static_assert(pre_steps_exact(), "interior mapping of the inverse Gaborish");
-__constant__ PreStep c_pre_steps[12] = {pre_step(0), pre_step(1), pre_step(2),  pre_step(3),
-                                        pre_step(4), pre_step(5), pre_step(6),  pre_step(7),
-                                        pre_step(8), pre_step(9), pre_step(10), pre_step(11)};
+constexpr int kPreW = kPreOut + 2 * kPreHalo;  // 128: 32 lanes x 4 columns
+constexpr int kPreWarps = kPreW / 4;            // 32 warps of four rows
+constexpr int kPreThreads = 32 * kPreWarps;
+static_assert(kPreW == 128 && kPreHalo >= 12, "tile of the inverse Gaborish");
+// F (the source tile), then the step inputs [2 parities][kPreW][kPreW].
+constexpr size_t kPreSmem = (size_t)3 * kPreW * kPreW * sizeof(float);
 
 struct EncKernel {
   float centre, edge, corner, inv_c;
   float neg_zero;  // -0.0f, the run-time addend of the paired products
+};
+
+// The tiles of a frame: a rectangle [fx0, fx1) x [fy0, fy1) of tiles with no
+// cell of another rule (kEdge false) and the ring around it (kEdge true, one
+// CTA per ring tile in blockIdx.x).
+struct PreTiles {
+  int tx, ty;  // tiles across and down
+  int fx0, fx1, fy0, fy1;
 };
 
 // The update of the last n % 4 samples of the plane divides by the centre
@@ -136,241 +137,290 @@ static __device__ __noinline__ float precondition_tail(float mm, float fv, float
   return mm + (fv - kx) / centre;
 }
 
-__global__ void __launch_bounds__(kPreThreads, 2) k_precondition(const float* __restrict__ in,
+// Four cells of one row, as two lane pairs: rows n (above), m, s (below)
+// with their west and east neighbour samples, f the source samples.
+// mm*c + (((N + S) + W) + E)*e + (((NW + NE) + SW) + SE)*k, then
+// mm + (f - kx) * (1/c), each operation rounded as the reference's.
+__device__ __forceinline__ float4 pre_row4(const float4& n, float nW, float nE, const float4& m,
+                                           float mW, float mE, const float4& s, float sW, float sE,
+                                           const float4& f, f2 c2, f2 e2, f2 k2, f2 i2, f2 nz) {
+  const f2 Mn0 = f2_pack(n.x, n.y), Mn1 = f2_pack(n.z, n.w);
+  const f2 Ms0 = f2_pack(s.x, s.y), Ms1 = f2_pack(s.z, s.w);
+  const f2 Mm0 = f2_pack(m.x, m.y), Mm1 = f2_pack(m.z, m.w);
+  // Offset pairs: (west of pair 0), (east of pair 0 = west of pair 1), (east of pair 1).
+  const f2 Wn = f2_pack(nW, n.x), Cn = f2_pack(n.y, n.z), En = f2_pack(n.w, nE);
+  const f2 Wm = f2_pack(mW, m.x), Cm = f2_pack(m.y, m.z), Em = f2_pack(m.w, mE);
+  const f2 Ws = f2_pack(sW, s.x), Cs = f2_pack(s.y, s.z), Es = f2_pack(s.w, sE);
+  const f2 s1a = f2_add(f2_add(f2_add(Mn0, Ms0), Wm), Cm);
+  const f2 s2a = f2_add(f2_add(f2_add(Wn, Cn), Ws), Cs);
+  const f2 s1b = f2_add(f2_add(f2_add(Mn1, Ms1), Cm), Em);
+  const f2 s2b = f2_add(f2_add(f2_add(Cn, En), Cs), Es);
+  const f2 kxa = f2_add(f2_add(f2_mul(Mm0, c2, nz), f2_mul(s1a, e2, nz)), f2_mul(s2a, k2, nz));
+  const f2 kxb = f2_add(f2_add(f2_mul(Mm1, c2, nz), f2_mul(s1b, e2, nz)), f2_mul(s2b, k2, nz));
+  const f2 ya = f2_add(Mm0, f2_mul(f2_sub(f2_pack(f.x, f.y), kxa), i2, nz));
+  const f2 yb = f2_add(Mm1, f2_mul(f2_sub(f2_pack(f.z, f.w), kxb), i2, nz));
+  return make_float4(f2_lo(ya), f2_hi(ya), f2_lo(yb), f2_hi(yb));
+}
+
+// One cell (tile row ty, column tx; frame cx, cy) by the rules of its
+// position, from the step's input tile S: the nine taps at mirrored frame
+// coordinates (clamped to the tile, which only the edge ring's inexact
+// cells need), summed sequentially when seq, divided when div.
+__device__ float pre_cell(const float* S, const float* F, int ty, int tx, int cx, int cy, int gx0,
+                          int gy0, int w, int h, bool seq, bool div, const EncKernel& k) {
+  auto col = [&](int c) { return min(max(mirror1d(c, w) - gx0, 0), kPreW - 1); };
+  auto row = [&](int c) { return min(max(mirror1d(c, h) - gy0, 0), kPreW - 1) * kPreW; };
+  const int xm = col(cx - 1), xp = col(cx + 1), ym = row(cy - 1), yp = row(cy + 1);
+  const int y0 = ty * kPreW;
+  const float nw = S[ym + xm], nn = S[ym + tx], ne = S[ym + xp];
+  const float ww = S[y0 + xm], mm = S[y0 + tx], ee = S[y0 + xp];
+  const float sw = S[yp + xm], ss = S[yp + tx], se = S[yp + xp];
+  float kx;
+  if (!seq) {
+    kx = mm * k.centre + (nn + ss + ww + ee) * k.edge + (nw + ne + sw + se) * k.corner;
+  } else {
+    // nine taps in order: dy = -1, 0, 1 outer, dx inner
+    float acc = 0.0f;
+    acc += k.corner * nw;
+    acc += k.edge * nn;
+    acc += k.corner * ne;
+    acc += k.edge * ww;
+    acc += k.centre * mm;
+    acc += k.edge * ee;
+    acc += k.corner * sw;
+    acc += k.edge * ss;
+    acc += k.corner * se;
+    kx = acc;
+  }
+  const float fv = F[y0 + tx];
+  return div ? precondition_tail(mm, fv, kx, k.centre) : mm + (fv - kx) * k.inv_c;
+}
+
+__device__ __forceinline__ int pre_clamp(int c, int size) { return min(max(c, 0), size - 1); }
+
+template <bool kEdge>
+__global__ void __launch_bounds__(kPreThreads, 1) k_precondition(const float* __restrict__ in,
                                                               float* __restrict__ out, int w,
-                                                              int h, EncKernel k) {
+                                                              int h, EncKernel k, PreTiles pt) {
   extern __shared__ __align__(16) float pre_smem[];
-  float* const base = pre_smem + kPrePad;
-  float* F = base;
-  float* const X0 = base + kPreS * kPreS;
-  float* const X1 = base + 2 * kPreS * kPreS;
+  float* const F = pre_smem;                  // [kPreW][kPreW]
+  float* const S2 = pre_smem + kPreW * kPreW;  // [2][kPreW][kPreW]
   const size_t plane = (size_t)w * h;
   in += plane * blockIdx.z;
   out += plane * blockIdx.z;
-  const int tx0 = blockIdx.x * kPreTile, ty0 = blockIdx.y * kPreTile;
-  const int gx0 = tx0 - kPreHalo, gy0 = ty0 - kPreHalo;
-  const int t = threadIdx.x;
-  // Load the haloed tile into F (the source) and X0 (step 0's input).  Tiles
-  // inside the frame take 16-byte loads when rows are 16-byte aligned (gx0 is
-  // a multiple of 4); others mirror every coordinate.  Each thread issues
-  // all of its loads before its first shared-memory store.
-  const bool inside = gx0 >= 0 && gy0 >= 0 && gx0 + kPreS <= w && gy0 + kPreS <= h;
-  const bool vec = inside && (w % 4) == 0 && ((reinterpret_cast<uintptr_t>(in) & 15) == 0);
-  if (vec) {
-    constexpr int kV = kPreS / 4;
-    constexpr int kN = kPreS * kV;
-    constexpr int kIt = (kN + kPreThreads - 1) / kPreThreads;
-    float4 v[kIt];
-#pragma unroll
-    for (int j = 0; j < kIt; ++j) {
-      const int i = t + j * kPreThreads;
-      if (i < kN) {
-        const int ly = i / kV, lx = (i - ly * kV) * 4;
-        v[j] = __ldg(reinterpret_cast<const float4*>(in + (size_t)(gy0 + ly) * w + gx0 + lx));
-      }
-    }
-#pragma unroll
-    for (int j = 0; j < kIt; ++j) {
-      const int i = t + j * kPreThreads;
-      if (i < kN) {
-        const int ly = i / kV, lx = (i - ly * kV) * 4;
-        *reinterpret_cast<float4*>(F + ly * kPreS + lx) = v[j];
-        *reinterpret_cast<float4*>(X0 + ly * kPreS + lx) = v[j];
-      }
-    }
+  int tile_x, tile_y;
+  if (!kEdge) {
+    tile_x = pt.fx0 + (int)blockIdx.x;
+    tile_y = pt.fy0 + (int)blockIdx.y;
   } else {
-    constexpr int kN = kPreS * kPreS;
-    constexpr int kIt = (kN + kPreThreads - 1) / kPreThreads;
-    float v[kIt];
-#pragma unroll
-    for (int j = 0; j < kIt; ++j) {
-      const int i = t + j * kPreThreads;
-      if (i < kN) {
-        const int ly = i / kPreS, lx = i - ly * kPreS;
-        v[j] = __ldg(in + (size_t)mirror1d(gy0 + ly, h) * w + mirror1d(gx0 + lx, w));
-      }
-    }
-#pragma unroll
-    for (int j = 0; j < kIt; ++j) {
-      const int i = t + j * kPreThreads;
-      if (i < kN) {
-        F[i] = v[j];
-        X0[i] = v[j];
-      }
+    // Ring tiles: the rows above the rectangle, the rows below it, then the
+    // tiles left and right of it on its rows.
+    int i = (int)blockIdx.x;
+    const int top = pt.fy0 * pt.tx, bottom = (pt.ty - pt.fy1) * pt.tx;
+    if (i < top) {
+      tile_y = i / pt.tx;
+      tile_x = i - tile_y * pt.tx;
+    } else if (i < top + bottom) {
+      i -= top;
+      tile_y = pt.fy1 + i / pt.tx;
+      tile_x = i - (tile_y - pt.fy1) * pt.tx;
+    } else {
+      i -= top + bottom;
+      const int side = pt.fx0 + (pt.tx - pt.fx1);
+      tile_y = pt.fy0 + i / side;
+      const int c = i - (tile_y - pt.fy0) * side;
+      tile_x = c < pt.fx0 ? c : pt.fx1 + (c - pt.fx0);
     }
   }
-  __syncthreads();
-  const size_t n = plane;
-  const size_t bulk = n - n % 4;
-  const int bulk_row = (int)(bulk / (size_t)w), bulk_col = (int)(bulk % (size_t)w);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int tx0 = tile_x * kPreOut, ty0 = tile_y * kPreOut;
+  const int gx0 = tx0 - kPreHalo, gy0 = ty0 - kPreHalo;
+  const int lx = 4 * lane, ly = 4 * warp;  // the thread's first column and row in the tile
+  const int gx = gx0 + lx, gy = gy0 + ly;  // ... in the frame
+  // Load: tiles inside the frame with 16-byte aligned rows take 16-byte
+  // loads; others clamp each coordinate (cells outside the frame are never
+  // read by a cell inside it, so their values do not matter).
+  const bool vec = gx0 >= 0 && gy0 >= 0 && gx0 + kPreW <= w && gy0 + kPreW <= h && (w % 4) == 0 &&
+                   ((reinterpret_cast<uintptr_t>(in) & 15) == 0);
+  float4 X[4];
+  if (vec) {
+#pragma unroll
+    for (int r = 0; r < 4; ++r)
+      X[r] = __ldg(reinterpret_cast<const float4*>(in + (size_t)(gy + r) * w + gx));
+  } else {
+    const int c0 = pre_clamp(gx, w), c1 = pre_clamp(gx + 1, w), c2 = pre_clamp(gx + 2, w),
+              c3 = pre_clamp(gx + 3, w);
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+      const float* row = in + (size_t)pre_clamp(gy + r, h) * w;
+      X[r] = make_float4(__ldg(row + c0), __ldg(row + c1), __ldg(row + c2), __ldg(row + c3));
+    }
+  }
+#pragma unroll
+  for (int r = 0; r < 4; ++r) *reinterpret_cast<float4*>(F + (ly + r) * kPreW + lx) = X[r];
+  // Ring tiles: the cells of another rule are the special rows (frame row
+  // 0 and rows [rb, h)) across the tile's in-frame columns, and the special
+  // columns (0 and [cb, w)) down its other in-frame rows.
   const int groups = (w >= 3 && h >= 3) ? (w - 2) / 4 : 0;
-  const int simd_end = min(w - 1, 4 * groups + 1);  // frame x in [1, simd_end) is SIMD
-  const int row_end = bulk == n ? h - 1 : min(h - 1, bulk_row);  // rows below take the tail rule
-  // Cells whose reference arithmetic is not the interior formula, in frame
-  // coordinates: rows 0 and [rb, h) (frame border, division tail) and, on
-  // the other rows, columns 0 and [cb, w) (frame border, past the SIMD
-  // groups).  Every other in-frame cell reads only in-frame neighbours.
-  const int rb = max(row_end, 1), cb = max(simd_end, 1);
-  // Special cells of the update region [lo, hi)^2 of a step, enumerated as
-  // special rows x in-frame columns, then special columns x ordinary rows.
-  struct Special {
-    int cx0, ncin, nr0, nrin, rB0, cB0, nsr, nsc;
-    bool r0, c0;
-  };
-  auto special = [&](int lo, int hi) {
-    Special sp;
-    sp.cx0 = max(lo, -gx0);
-    sp.ncin = max(0, min(hi, w - gx0) - sp.cx0);
-    const int ry0 = max(lo, -gy0), ry1 = min(hi, h - gy0);
-    const int cx1 = sp.cx0 + sp.ncin;
-    sp.r0 = -gy0 >= ry0 && -gy0 < ry1;
-    sp.rB0 = max(ry0, rb - gy0);
-    sp.nsr = (sp.r0 ? 1 : 0) + max(0, ry1 - sp.rB0);
-    sp.nr0 = max(ry0, 1 - gy0);
-    sp.nrin = max(0, min(ry1, rb - gy0) - sp.nr0);
-    sp.c0 = -gx0 >= sp.cx0 && -gx0 < cx1;
-    sp.cB0 = max(sp.cx0, cb - gx0);
-    sp.nsc = (sp.c0 ? 1 : 0) + max(0, cx1 - sp.cB0);
-    return sp;
-  };
-  // Interior tiles have no special cell in step 0's region (the largest),
-  // so every step is the paired formula alone.
-  const Special sp0 = special(1, kPreS - 1);
-  const bool fast = sp0.nsr * sp0.ncin + sp0.nsc * sp0.nrin == 0;
+  const size_t bulk = plane - plane % 4;
+  int cx0 = 0, ncin = 0, nr0 = 0, nrin = 0, rB0 = 0, cB0 = 0, nsr = 0, nsc = 0;
+  bool r0 = false, c0 = false;
+  bool mine = false;  // the thread owns a cell of another rule
+  if (kEdge) {
+    const int bulk_row = (int)(bulk / (size_t)w), row_end = bulk == plane ? h - 1 : min(h - 1, bulk_row);
+    const int rb = max(row_end, 1), cb = max(min(w - 1, 4 * groups + 1), 1);
+    cx0 = max(0, -gx0);
+    ncin = max(0, min(kPreW, w - gx0) - cx0);
+    const int ry0 = max(0, -gy0), ry1 = min(kPreW, h - gy0), cx1 = cx0 + ncin;
+    r0 = -gy0 >= ry0 && -gy0 < ry1;
+    rB0 = max(ry0, rb - gy0);
+    nsr = (r0 ? 1 : 0) + max(0, ry1 - rB0);
+    nr0 = max(ry0, 1 - gy0);
+    nrin = max(0, min(ry1, rb - gy0) - nr0);
+    c0 = -gx0 >= cx0 && -gx0 < cx1;
+    cB0 = max(cx0, cb - gx0);
+    nsc = (c0 ? 1 : 0) + max(0, cx1 - cB0);
+#pragma unroll
+    for (int r = 0; r < 4; ++r)
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const int cx = gx + j, cy = gy + r;
+        if (cx >= 0 && cx < w && cy >= 0 && cy < h &&
+            (cx == 0 || cx >= cb || cy == 0 || cy >= rb))
+          mine = true;
+      }
+  }
   const f2 c2 = f2_pack(k.centre, k.centre), e2 = f2_pack(k.edge, k.edge);
   const f2 k2 = f2_pack(k.corner, k.corner), i2 = f2_pack(k.inv_c, k.inv_c);
   const f2 nz = f2_pack(k.neg_zero, k.neg_zero);
-  int cur = 0;
-  for (int it = 0; it < 12; ++it) {
-    const PreStep ps = c_pre_steps[it];
-    const int lo = 1 + it, hi = kPreS - 1 - it;
-    const float* X = cur ? X1 : X0;
-    float* Y = cur ? X0 : X1;
-    {
-      const int band = (int)(((unsigned)t * (unsigned)ps.mg) >> 16);
-      const int c0 = 2 * (ps.p_lo + t - band * ps.np);
-      const int ly0 = lo + band * ps.rows, ly1 = min(ly0 + ps.rows, hi);
-      if (band < ps.bands && ly0 < ly1) {
-        // A pair straddling the region's edge also writes the column just
-        // outside it; no later step or output reads that column of this
-        // plane (each step reads only the previous region).  Cells outside
-        // the frame take values no in-frame cell reads.
-        int c = ly0 * kPreS + c0;
-        f2 M0 = *reinterpret_cast<const f2*>(X + c - kPreS);
-        f2 W0 = f2_pack(X[c - kPreS - 1], f2_lo(M0)), E0 = f2_pack(f2_hi(M0), X[c - kPreS + 2]);
-        f2 M1 = *reinterpret_cast<const f2*>(X + c);
-        f2 W1 = f2_pack(X[c - 1], f2_lo(M1)), E1 = f2_pack(f2_hi(M1), X[c + 2]);
-        f2 M2, W2, E2;
-        const int end = ly1 * kPreS + c0;
-        // One row: (Mn, Wn, En) above, (Mm, Wm, Em) the row updated, (Ms, Ws,
-        // Es) loaded below; three rows per loop trip with the roles rotated
-        // by name, so no register moves carry the rows from trip to trip.
-        // mm*c + (nn + ss + ww + ee)*e + (nw + ne + sw + se)*k
-#define JPXLG_PRE_ROW(Mn, Wn, En, Mm, Wm, Em, Ms, Ws, Es)                                   \
-  {                                                                                          \
-    Ms = *reinterpret_cast<const f2*>(X + c + kPreS);                                        \
-    Ws = f2_pack(X[c + kPreS - 1], f2_lo(Ms));                                               \
-    Es = f2_pack(f2_hi(Ms), X[c + kPreS + 2]);                                               \
-    const f2 s1 = f2_add(f2_add(f2_add(Mn, Ms), Wm), Em);                                    \
-    const f2 s2 = f2_add(f2_add(f2_add(Wn, En), Ws), Es);                                    \
-    const f2 kx = f2_add(f2_add(f2_mul(Mm, c2, nz), f2_mul(s1, e2, nz)), f2_mul(s2, k2, nz)); \
-    *reinterpret_cast<f2*>(Y + c) =                                                          \
-        f2_add(Mm, f2_mul(f2_sub(*reinterpret_cast<const f2*>(F + c), kx), i2, nz));          \
-    c += kPreS;                                                                              \
+  const unsigned full = 0xffffffffu;
+  // The rows just above and below the warp's (clamped to the tile: the
+  // tile's edge rows, never read by an exact cell).
+  const int row_up = max(ly - 1, 0) * kPreW + lx, row_down = min(ly + 4, kPreW - 1) * kPreW + lx;
+  if (kEdge) {
+#pragma unroll
+    for (int r = 0; r < 4; ++r) *reinterpret_cast<float4*>(S2 + (ly + r) * kPreW + lx) = X[r];
   }
 #pragma unroll 1
-        while (c + 2 * kPreS < end) {
-          JPXLG_PRE_ROW(M0, W0, E0, M1, W1, E1, M2, W2, E2)
-          JPXLG_PRE_ROW(M1, W1, E1, M2, W2, E2, M0, W0, E0)
-          JPXLG_PRE_ROW(M2, W2, E2, M0, W0, E0, M1, W1, E1)
-        }
-        if (c < end) {
-          JPXLG_PRE_ROW(M0, W0, E0, M1, W1, E1, M2, W2, E2)
-          if (c < end) JPXLG_PRE_ROW(M1, W1, E1, M2, W2, E2, M0, W0, E0)
-        }
-#undef JPXLG_PRE_ROW
-      }
+  for (int it = 0; it < 12; ++it) {
+    float* const S = S2 + (it & 1) * (kPreW * kPreW);
+    // Publish the step's input: the warp's first and last rows (ring tiles
+    // hold the whole tile there already).
+    if (!kEdge) {
+      *reinterpret_cast<float4*>(S + ly * kPreW + lx) = X[0];
+      *reinterpret_cast<float4*>(S + (ly + 3) * kPreW + lx) = X[3];
     }
     __syncthreads();
-    if (!fast) {
-      // Recompute the special cells with their own rules, reading the nine
-      // taps at mirrored frame coordinates (always inside the frame and the
-      // previous step's region), so cells outside the frame are never read.
-      const Special sp = special(lo, hi);
-      const int nrow_cells = sp.nsr * sp.ncin;
-      const int total = nrow_cells + sp.nsc * sp.nrin;
-      for (int i = t; i < total; i += kPreThreads) {
-        int ly, lx;
+    float4 prev = *reinterpret_cast<const float4*>(S + row_up);
+    float pW = __shfl_up_sync(full, prev.w, 1), pE = __shfl_down_sync(full, prev.x, 1);
+    float mW = __shfl_up_sync(full, X[0].w, 1), mE = __shfl_down_sync(full, X[0].x, 1);
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+      const float4 nxt = r < 3 ? X[r + 1 < 4 ? r + 1 : 3] : *reinterpret_cast<const float4*>(S + row_down);
+      const float sW = __shfl_up_sync(full, nxt.w, 1), sE = __shfl_down_sync(full, nxt.x, 1);
+      const float4 f = *reinterpret_cast<const float4*>(F + (ly + r) * kPreW + lx);
+      const float4 y = pre_row4(prev, pW, pE, X[r], mW, mE, nxt, sW, sE, f, c2, e2, k2, i2, nz);
+      prev = X[r];
+      pW = mW;
+      pE = mE;
+      X[r] = y;
+      mW = sW;
+      mE = sE;
+    }
+    if (kEdge) {
+      // The paired results into the next step's input, then the cells of
+      // another rule recomputed there from this step's, shared out over the
+      // CTA; the owners read their cells back.
+      float* const Sn = S2 + ((it + 1) & 1) * (kPreW * kPreW);
+#pragma unroll
+      for (int r = 0; r < 4; ++r) *reinterpret_cast<float4*>(Sn + (ly + r) * kPreW + lx) = X[r];
+      __syncthreads();
+      const int nrow_cells = nsr * ncin;
+      const int total = nrow_cells + nsc * nrin;
+      for (int i = threadIdx.x; i < total; i += kPreThreads) {
+        int ty, tx;
         if (i < nrow_cells) {
-          const int r = i / sp.ncin;
-          lx = sp.cx0 + (i - r * sp.ncin);
-          ly = sp.r0 ? (r == 0 ? -gy0 : sp.rB0 + r - 1) : sp.rB0 + r;
+          const int r = i / ncin;
+          tx = cx0 + (i - r * ncin);
+          ty = r0 ? (r == 0 ? -gy0 : rB0 + r - 1) : rB0 + r;
         } else {
           const int j = i - nrow_cells;
-          const int ci = j / sp.nrin;
-          ly = sp.nr0 + (j - ci * sp.nrin);
-          lx = sp.c0 ? (ci == 0 ? -gx0 : sp.cB0 + ci - 1) : sp.cB0 + ci;
+          const int ci = j / nrin;
+          ty = nr0 + (j - ci * nrin);
+          tx = c0 ? (ci == 0 ? -gx0 : cB0 + ci - 1) : cB0 + ci;
         }
-        const int gx = gx0 + lx, gy = gy0 + ly;
-        const int xm = mirror1d(gx - 1, w) - gx0, xp = mirror1d(gx + 1, w) - gx0;
-        const int ym = (mirror1d(gy - 1, h) - gy0) * kPreS, yp = (mirror1d(gy + 1, h) - gy0) * kPreS;
-        const int y0 = ly * kPreS;
-        const float nw = X[ym + xm], nn = X[ym + lx], ne = X[ym + xp];
-        const float ww = X[y0 + xm], mm = X[y0 + lx], ee = X[y0 + xp];
-        const float sw = X[yp + xm], ss = X[yp + lx], se = X[yp + xp];
-        const bool border = gx == 0 || gx == w - 1 || gy == 0 || gy == h - 1;
-        float kx;
-        if (!border && gx - 1 < 4 * groups) {
-          kx = mm * k.centre + (nn + ss + ww + ee) * k.edge + (nw + ne + sw + se) * k.corner;
-        } else {
-          // nine taps in order: dy = -1, 0, 1 outer, dx inner
-          float acc = 0.0f;
-          acc += k.corner * nw;
-          acc += k.edge * nn;
-          acc += k.corner * ne;
-          acc += k.edge * ww;
-          acc += k.centre * mm;
-          acc += k.edge * ee;
-          acc += k.corner * sw;
-          acc += k.edge * ss;
-          acc += k.corner * se;
-          kx = acc;
-        }
-        const int c = y0 + lx;
-        const bool in_bulk = gy < bulk_row || (gy == bulk_row && gx < bulk_col);
-        if (in_bulk) Y[c] = mm + (F[c] - kx) * k.inv_c;
-        else Y[c] = precondition_tail(mm, F[c], kx, k.centre);
+        const int cx = gx0 + tx, cy = gy0 + ty;
+        const bool border = cx == 0 || cx == w - 1 || cy == 0 || cy == h - 1;
+        const bool seq = border || cx - 1 >= 4 * groups;
+        const bool div = (size_t)cy * w + cx >= bulk;
+        Sn[ty * kPreW + tx] = pre_cell(S, F, ty, tx, cx, cy, gx0, gy0, w, h, seq, div, k);
       }
       __syncthreads();
+      if (mine) {
+#pragma unroll
+        for (int r = 0; r < 4; ++r) X[r] = *reinterpret_cast<const float4*>(Sn + (ly + r) * kPreW + lx);
+      }
     }
-    cur ^= 1;
   }
-  const float* R = cur ? X1 : X0;
-  if (tx0 + kPreTile <= w && ty0 + kPreTile <= h && (w % 4) == 0 &&
-      (reinterpret_cast<uintptr_t>(out) & 15) == 0) {
-    constexpr int kV = kPreTile / 4;
-    for (int i = t; i < kPreTile * kV; i += kPreThreads) {
-      const int ly = i / kV, lx = (i - ly * kV) * 4;
-      *reinterpret_cast<float4*>(out + (size_t)(ty0 + ly) * w + tx0 + lx) =
-          *reinterpret_cast<const float4*>(R + (ly + kPreHalo) * kPreS + lx + kPreHalo);
-    }
-  } else {
-    for (int i = t; i < kPreTile * kPreTile; i += kPreThreads) {
-      const int ly = i / kPreTile, lx = i - ly * kPreTile;
-      const int gx = tx0 + lx, gy = ty0 + ly;
-      if (gx < w && gy < h) out[(size_t)gy * w + gx] = R[(ly + kPreHalo) * kPreS + lx + kPreHalo];
+  // The inner 104 x 104: lanes 3 .. 28 of warps 3 .. 28.
+  const int oh = kPreHalo / 4;
+  if (lane >= oh && lane < 32 - oh && warp >= oh && warp < kPreWarps - oh) {
+    const bool vec_out =
+        gx + 3 < w && (w % 4) == 0 && ((reinterpret_cast<uintptr_t>(out) & 15) == 0);
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+      if (gy + r >= h) break;
+      float* row = out + (size_t)(gy + r) * w;
+      if (vec_out) {
+        *reinterpret_cast<float4*>(row + gx) = X[r];
+      } else {
+        if (gx < w) row[gx] = X[r].x;
+        if (gx + 1 < w) row[gx + 1] = X[r].y;
+        if (gx + 2 < w) row[gx + 2] = X[r].z;
+        if (gx + 3 < w) row[gx + 3] = X[r].w;
+      }
     }
   }
 }
 
-void launch_precondition(const float* in, float* out, int w, int h, cudaStream_t s) {
+int launch_precondition(const float* in, float* out, int w, int h, cudaStream_t s) {
   const float w1 = 0.115169525f, w2 = 0.061248592f;
   // gaborish.rs:31 GaborKernel::new, normalised without FMA.
   float unnorm = 1.0f + 4.0f * w1 + 4.0f * w2;
   float scale = 1.0f / unnorm;
   EncKernel k{scale, w1 * scale, w2 * scale, 1.0f / scale, -0.0f};
-  dim3 grid((w + kPreTile - 1) / kPreTile, (h + kPreTile - 1) / kPreTile, 3);
-  k_precondition<<<grid, kPreThreads, kPreSmem, s>>>(in, out, w, h, k);
+  PreTiles pt{(w + kPreOut - 1) / kPreOut, (h + kPreOut - 1) / kPreOut, 0, 0, 0, 0};
+  // Columns and rows of cells with another rule: 0, [cb, w) and 0, [rb, h)
+  // (the frame border, the columns past the groups of four, the rows of
+  // the division tail).  A tile is in the rectangle when its haloed extent
+  // [t*104 - 12, t*104 + 116) lies inside [1, cb) and [1, rb).
+  const long long n = (long long)w * h;
+  const int groups = (w >= 3 && h >= 3) ? (w - 2) / 4 : 0;
+  const int cb = std::max(std::min(w - 1, 4 * groups + 1), 1);
+  const int row_end = n % 4 == 0 ? h - 1 : (int)std::min<long long>(h - 1, (n - n % 4) / w);
+  const int rb = std::max(row_end, 1);
+  const int reach = kPreW - kPreHalo;  // 116
+  const int fx1 = cb >= reach ? std::min((cb - reach) / kPreOut + 1, pt.tx) : 0;
+  const int fy1 = rb >= reach ? std::min((rb - reach) / kPreOut + 1, pt.ty) : 0;
+  if (fx1 > 1 && fy1 > 1) {
+    pt.fx0 = 1;
+    pt.fx1 = fx1;
+    pt.fy0 = 1;
+    pt.fy1 = fy1;
+  }
+  int launches = 0;
+  const int nfast = (pt.fx1 - pt.fx0) * (pt.fy1 - pt.fy0);
+  if (nfast > 0) {
+    k_precondition<false><<<dim3(pt.fx1 - pt.fx0, pt.fy1 - pt.fy0, 3), kPreThreads, kPreSmem, s>>>(
+        in, out, w, h, k, pt);
+    ++launches;
+  }
+  const int nedge = pt.tx * pt.ty - nfast;
+  if (nedge > 0) {
+    k_precondition<true><<<dim3(nedge, 1, 3), kPreThreads, kPreSmem, s>>>(in, out, w, h, k, pt);
+    ++launches;
+  }
+  return launches;
 }
 
 // ---------------------------------------------------------------------------
@@ -1208,7 +1258,10 @@ void launch_mul_table(uint32_t global_scale, float* table, cudaStream_t s) {
 }
 
 cudaError_t configure_encode_kernels() {
-  return cudaFuncSetAttribute(k_precondition, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  cudaError_t e = cudaFuncSetAttribute(k_precondition<false>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kPreSmem);
+  if (e != cudaSuccess) return e;
+  return cudaFuncSetAttribute(k_precondition<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                               (int)kPreSmem);
 }
 

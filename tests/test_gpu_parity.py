@@ -56,11 +56,13 @@ def test_stages_are_bit_identical(ctx, oracle):
     assert np.array_equal(st["coeff"].view(np.uint32), ref["coeff"].view(np.uint32))
 
 
-@pytest.mark.parametrize("w,h", [(520, 330), (517, 331)])
+@pytest.mark.parametrize("w,h", [(520, 330), (517, 331), (1001, 421), (250, 213), (130, 7),
+                                 (7, 130), (9, 4), (5, 2), (3, 3), (2, 5), (1, 1)])
 def test_precondition_interior_and_edge_tiles(ctx, oracle, w, h):
-    """Frames with many interior 64x64 tiles (the paired-lane loop) around
-    edge tiles (mirrored halo, border taps); 517 x 331 also has the n % 4
-    division tail on its last row."""
+    """Frames with interior 104x104 tiles (the register-resident paired
+    update) inside a ring of edge tiles (border taps, the columns past the
+    groups of four, the n % 4 division tail: 517 x 331 and 1001 x 421), and
+    frames smaller than one tile, down to a single sample."""
     rgb = synth.synthetic_rgb(w, h, seed=w + h, bits=16)
     bmap = synth.fixed_dct8_map(w, h)
     req = jg.EncodeRequest(global_scale=30000, gaborish=True)
