@@ -94,29 +94,37 @@ void launch_srgb_to_xyb(const void* rgb, int bits, size_t n, const float* lut, f
 // (104 x 104 outputs).  Lane l of warp v holds columns 4l .. 4l+3 of tile
 // rows 4v .. 4v+3 in registers for all twelve steps: west and east
 // neighbours come from the adjacent lanes by shuffle, the rows above and
-// below the warp's four from the neighbouring warps through a shared-memory
-// copy of the step's input (double-buffered, one barrier per step), and the
-// source plane F from shared memory.  Every step updates the whole tile; a
-// cell k samples from the tile's edge is exact for k steps, so after twelve
-// the inner 104 x 104 are, and no cell of the edge ring is ever read by one
-// nearer the centre than itself.
+// below the warp's four from the neighbouring warps through shared memory
+// (double-buffered, one barrier per step), and the source plane F from
+// shared memory.  Every step updates the whole tile; a cell k samples from
+// the tile's edge is exact for k steps, so after twelve the inner 104 x 104
+// are, and no cell of the edge ring is ever read by one nearer the centre
+// than itself.
 //
 // Two kernels cover a frame: the tiles whose haloed extent has no cell of
 // another rule (kEdge false), and the ring of tiles around them (kEdge
-// true).  There each step keeps the whole tile's input in shared memory;
-// after the paired update the CTA's threads share out the cells of another
-// rule (frame border, columns past the groups of four, the division tail)
-// and recompute them from their nine taps at mirrored frame coordinates
-// (always among the cell's own 3 x 3 neighbourhood), as the reference does,
-// into the next step's input, which the owning threads read back.
+// true).  A ring tile keeps each step's input in shared memory and, after
+// the paired update of every cell, the CTA's threads share out the cells of
+// another rule (frame border and columns past the groups of four: the
+// sequential nine-tap sum; the last n % 4 cells of the plane: the division
+// by the centre weight) and recompute them from their nine taps at mirrored
+// frame coordinates (always among the cell's own 3 x 3 neighbourhood).
 constexpr int kPreOut = 104;
 constexpr int kPreHalo = 12;
 constexpr int kPreW = kPreOut + 2 * kPreHalo;  // 128: 32 lanes x 4 columns
 constexpr int kPreWarps = kPreW / 4;            // 32 warps of four rows
 constexpr int kPreThreads = 32 * kPreWarps;
 static_assert(kPreW == 128 && kPreHalo >= 12, "tile of the inverse Gaborish");
-// F (the source tile), then the step inputs [2 parities][kPreW][kPreW].
-constexpr size_t kPreSmem = (size_t)3 * kPreW * kPreW * sizeof(float);
+// Tile rows in shared memory are kPreP floats apart: 16-byte aligned for the
+// rows' float4 accesses, and a column's 32 consecutive rows spread over 8
+// banks for the ring's per-cell accesses (a pitch of 128 puts them all in
+// one).
+constexpr int kPreP = kPreW + 4;
+// F (the source tile, [kPreW][kPreP]), then the interior kernel's published
+// rows [2 parities][kPreWarps][first, last][kPreW], or the ring kernel's
+// step inputs [2 parities][kPreW][kPreP].
+constexpr size_t kPreSmem = (size_t)(kPreW * kPreP + 2 * kPreWarps * 2 * kPreW) * sizeof(float);
+constexpr size_t kPreRingSmem = (size_t)3 * kPreW * kPreP * sizeof(float);
 
 struct EncKernel {
   float centre, edge, corner, inv_c;
@@ -137,46 +145,78 @@ static __device__ __noinline__ float precondition_tail(float mm, float fv, float
   return mm + (fv - kx) / centre;
 }
 
-// Four cells of one row, as two lane pairs: rows n (above), m, s (below)
-// with their west and east neighbour samples, f the source samples.
-// mm*c + (((N + S) + W) + E)*e + (((NW + NE) + SW) + SE)*k, then
-// mm + (f - kx) * (1/c), each operation rounded as the reference's.
-__device__ __forceinline__ float4 pre_row4(const float4& n, float nW, float nE, const float4& m,
-                                           float mW, float mE, const float4& s, float sW, float sE,
-                                           const float4& f, f2 c2, f2 e2, f2 k2, f2 i2, f2 nz) {
-  const f2 Mn0 = f2_pack(n.x, n.y), Mn1 = f2_pack(n.z, n.w);
-  const f2 Ms0 = f2_pack(s.x, s.y), Ms1 = f2_pack(s.z, s.w);
-  const f2 Mm0 = f2_pack(m.x, m.y), Mm1 = f2_pack(m.z, m.w);
-  // Offset pairs: (west of pair 0), (east of pair 0 = west of pair 1), (east of pair 1).
-  const f2 Wn = f2_pack(nW, n.x), Cn = f2_pack(n.y, n.z), En = f2_pack(n.w, nE);
-  const f2 Wm = f2_pack(mW, m.x), Cm = f2_pack(m.y, m.z), Em = f2_pack(m.w, mE);
-  const f2 Ws = f2_pack(sW, s.x), Cs = f2_pack(s.y, s.z), Es = f2_pack(s.w, sE);
-  const f2 s1a = f2_add(f2_add(f2_add(Mn0, Ms0), Wm), Cm);
-  const f2 s2a = f2_add(f2_add(f2_add(Wn, Cn), Ws), Cs);
-  const f2 s1b = f2_add(f2_add(f2_add(Mn1, Ms1), Cm), Em);
-  const f2 s2b = f2_add(f2_add(f2_add(Cn, En), Cs), Es);
-  const f2 kxa = f2_add(f2_add(f2_mul(Mm0, c2, nz), f2_mul(s1a, e2, nz)), f2_mul(s2a, k2, nz));
-  const f2 kxb = f2_add(f2_add(f2_mul(Mm1, c2, nz), f2_mul(s1b, e2, nz)), f2_mul(s2b, k2, nz));
-  const f2 ya = f2_add(Mm0, f2_mul(f2_sub(f2_pack(f.x, f.y), kxa), i2, nz));
-  const f2 yb = f2_add(Mm1, f2_mul(f2_sub(f2_pack(f.z, f.w), kxb), i2, nz));
+// The three rows around a row of four cells, as lane pairs.  Columns are
+// paired (0, 1) and (2, 3); W*, C*, E* are the pairs one column to the
+// left of pair 0, between the pairs, and one column to the right of pair 1.
+struct PreRows {
+  f2 Mn0, Mn1, Mm0, Mm1, Ms0, Ms1;
+  f2 Wn, Cn, En, Wm, Cm, Em, Ws, Cs, Es;
+};
+__device__ __forceinline__ PreRows pre_rows(const float4& n, float nW, float nE, const float4& m,
+                                            float mW, float mE, const float4& s, float sW,
+                                            float sE) {
+  PreRows q;
+  q.Mn0 = f2_pack(n.x, n.y);
+  q.Mn1 = f2_pack(n.z, n.w);
+  q.Mm0 = f2_pack(m.x, m.y);
+  q.Mm1 = f2_pack(m.z, m.w);
+  q.Ms0 = f2_pack(s.x, s.y);
+  q.Ms1 = f2_pack(s.z, s.w);
+  q.Wn = f2_pack(nW, n.x);
+  q.Cn = f2_pack(n.y, n.z);
+  q.En = f2_pack(n.w, nE);
+  q.Wm = f2_pack(mW, m.x);
+  q.Cm = f2_pack(m.y, m.z);
+  q.Em = f2_pack(m.w, mE);
+  q.Ws = f2_pack(sW, s.x);
+  q.Cs = f2_pack(s.y, s.z);
+  q.Es = f2_pack(s.w, sE);
+  return q;
+}
+
+// Interior rule: mm*c + (((N + S) + W) + E)*e + (((NW + NE) + SW) + SE)*k.
+__device__ __forceinline__ void pre_kx_interior(const PreRows& q, f2 c2, f2 e2, f2 k2, f2 nz,
+                                                f2& kxa, f2& kxb) {
+  const f2 s1a = f2_add(f2_add(f2_add(q.Mn0, q.Ms0), q.Wm), q.Cm);
+  const f2 s2a = f2_add(f2_add(f2_add(q.Wn, q.Cn), q.Ws), q.Cs);
+  const f2 s1b = f2_add(f2_add(f2_add(q.Mn1, q.Ms1), q.Cm), q.Em);
+  const f2 s2b = f2_add(f2_add(f2_add(q.Cn, q.En), q.Cs), q.Es);
+  kxa = f2_add(f2_add(f2_mul(q.Mm0, c2, nz), f2_mul(s1a, e2, nz)), f2_mul(s2a, k2, nz));
+  kxb = f2_add(f2_add(f2_mul(q.Mm1, c2, nz), f2_mul(s1b, e2, nz)), f2_mul(s2b, k2, nz));
+}
+
+// mm + (f - kx) * (1/c).
+__device__ __forceinline__ float4 pre_update(const PreRows& q, const float4& f, f2 kxa, f2 kxb,
+                                             f2 i2, f2 nz) {
+  const f2 ya = f2_add(q.Mm0, f2_mul(f2_sub(f2_pack(f.x, f.y), kxa), i2, nz));
+  const f2 yb = f2_add(q.Mm1, f2_mul(f2_sub(f2_pack(f.z, f.w), kxb), i2, nz));
   return make_float4(f2_lo(ya), f2_hi(ya), f2_lo(yb), f2_hi(yb));
 }
 
-// One cell (tile row ty, column tx; frame cx, cy) by the rules of its
-// position, from the step's input tile S: the nine taps at mirrored frame
-// coordinates (clamped to the tile, which only the edge ring's inexact
-// cells need), summed sequentially when seq, divided when div.
-__device__ float pre_cell(const float* S, const float* F, int ty, int tx, int cx, int cy, int gx0,
-                          int gy0, int w, int h, bool seq, bool div, const EncKernel& k) {
-  auto col = [&](int c) { return min(max(mirror1d(c, w) - gx0, 0), kPreW - 1); };
-  auto row = [&](int c) { return min(max(mirror1d(c, h) - gy0, 0), kPreW - 1) * kPreW; };
-  const int xm = col(cx - 1), xp = col(cx + 1), ym = row(cy - 1), yp = row(cy + 1);
-  const int y0 = ty * kPreW;
+// A ring tile's cell of another rule, found once: its tile position and the
+// tile rows and columns of its mirrored taps (7 bits each) and its rule.
+struct PreSpecial {
+  uint32_t a;  // tx | xm << 7 | xp << 14 | ty << 21
+  uint32_t b;  // ym | yp << 7 | seq << 14 | div << 15 | valid << 16
+};
+__device__ __forceinline__ PreSpecial pre_special(int ty, int tx, int cx, int cy, int gx0, int gy0,
+                                                  int w, int h, bool seq, bool div) {
+  auto clampt = [](int v) { return min(max(v, 0), kPreW - 1); };
+  const int xm = clampt(mirror1d(cx - 1, w) - gx0), xp = clampt(mirror1d(cx + 1, w) - gx0);
+  const int ym = clampt(mirror1d(cy - 1, h) - gy0), yp = clampt(mirror1d(cy + 1, h) - gy0);
+  return {(uint32_t)tx | (uint32_t)xm << 7 | (uint32_t)xp << 14 | (uint32_t)ty << 21,
+          (uint32_t)ym | (uint32_t)yp << 7 | (uint32_t)seq << 14 | (uint32_t)div << 15 | 1u << 16};
+}
+// Its update from the step's input S into Sn.
+__device__ __forceinline__ void pre_special_step(const PreSpecial& c, const float* S, const float* F,
+                                                 float* Sn, const EncKernel& k) {
+  const int tx = c.a & 127, xm = (c.a >> 7) & 127, xp = (c.a >> 14) & 127, y0 = (c.a >> 21) * kPreP;
+  const int ym = (c.b & 127) * kPreP, yp = ((c.b >> 7) & 127) * kPreP;
   const float nw = S[ym + xm], nn = S[ym + tx], ne = S[ym + xp];
   const float ww = S[y0 + xm], mm = S[y0 + tx], ee = S[y0 + xp];
   const float sw = S[yp + xm], ss = S[yp + tx], se = S[yp + xp];
   float kx;
-  if (!seq) {
+  if (!((c.b >> 14) & 1u)) {
     kx = mm * k.centre + (nn + ss + ww + ee) * k.edge + (nw + ne + sw + se) * k.corner;
   } else {
     // nine taps in order: dy = -1, 0, 1 outer, dx inner
@@ -193,7 +233,59 @@ __device__ float pre_cell(const float* S, const float* F, int ty, int tx, int cx
     kx = acc;
   }
   const float fv = F[y0 + tx];
-  return div ? precondition_tail(mm, fv, kx, k.centre) : mm + (fv - kx) * k.inv_c;
+  Sn[y0 + tx] = ((c.b >> 15) & 1u) ? precondition_tail(mm, fv, kx, k.centre)
+                                    : mm + (fv - kx) * k.inv_c;
+}
+
+// The cells of another rule in a ring tile with frame origin (gx0, gy0):
+// the special rows (frame row 0 and rows [rb, h)) across the tile's
+// in-frame columns, then the special columns (0 and [cb, w)) down its other
+// in-frame rows; rb and cb as the reference's groups of four and division
+// tail place them.
+struct PreRingCells {
+  int cx0, ncin, rB0, nr0, nrin, cB0, nrow_cells, count, groups;
+  bool r0, c0;
+  size_t bulk;
+  __device__ __forceinline__ PreSpecial special(int i, int w, int h, int gx0, int gy0) const {
+    int ty, tx;
+    if (i < nrow_cells) {
+      const int rr = i / ncin;
+      tx = cx0 + (i - rr * ncin);
+      ty = r0 ? (rr == 0 ? -gy0 : rB0 + rr - 1) : rB0 + rr;
+    } else {
+      const int j = i - nrow_cells;
+      const int ci = j / nrin;
+      ty = nr0 + (j - ci * nrin);
+      tx = c0 ? (ci == 0 ? -gx0 : cB0 + ci - 1) : cB0 + ci;
+    }
+    const int cx = gx0 + tx, cy = gy0 + ty;
+    const bool border = cx == 0 || cx == w - 1 || cy == 0 || cy == h - 1;
+    return pre_special(ty, tx, cx, cy, gx0, gy0, w, h, border || cx - 1 >= 4 * groups,
+                       (size_t)cy * w + cx >= bulk);
+  }
+};
+__device__ __forceinline__ PreRingCells pre_ring_cells(int w, int h, int gx0, int gy0) {
+  PreRingCells g;
+  const size_t plane = (size_t)w * h;
+  g.groups = (w >= 3 && h >= 3) ? (w - 2) / 4 : 0;
+  g.bulk = plane - plane % 4;
+  const int bulk_row = (int)(g.bulk / (size_t)w);
+  const int rb = max(g.bulk == plane ? h - 1 : min(h - 1, bulk_row), 1);
+  const int cb = max(min(w - 1, 4 * g.groups + 1), 1);
+  g.cx0 = max(0, -gx0);
+  g.ncin = max(0, min(kPreW, w - gx0) - g.cx0);
+  const int ry0 = max(0, -gy0), ry1 = min(kPreW, h - gy0), cx1 = g.cx0 + g.ncin;
+  g.r0 = -gy0 >= ry0 && -gy0 < ry1;
+  g.rB0 = max(ry0, rb - gy0);
+  const int nsr = (g.r0 ? 1 : 0) + max(0, ry1 - g.rB0);
+  g.nr0 = max(ry0, 1 - gy0);
+  g.nrin = max(0, min(ry1, rb - gy0) - g.nr0);
+  g.c0 = -gx0 >= g.cx0 && -gx0 < cx1;
+  g.cB0 = max(g.cx0, cb - gx0);
+  const int nsc = (g.c0 ? 1 : 0) + max(0, cx1 - g.cB0);
+  g.nrow_cells = nsr * g.ncin;
+  g.count = g.nrow_cells + nsc * g.nrin;
+  return g;
 }
 
 __device__ __forceinline__ int pre_clamp(int c, int size) { return min(max(c, 0), size - 1); }
@@ -203,8 +295,8 @@ __global__ void __launch_bounds__(kPreThreads, 1) k_precondition(const float* __
                                                               float* __restrict__ out, int w,
                                                               int h, EncKernel k, PreTiles pt) {
   extern __shared__ __align__(16) float pre_smem[];
-  float* const F = pre_smem;                  // [kPreW][kPreW]
-  float* const S2 = pre_smem + kPreW * kPreW;  // [2][kPreW][kPreW]
+  float* const F = pre_smem;                   // [kPreW][kPreP]
+  float* const xb = pre_smem + kPreW * kPreP;  // published rows, or the ring's step inputs
   const size_t plane = (size_t)w * h;
   in += plane * blockIdx.z;
   out += plane * blockIdx.z;
@@ -257,110 +349,98 @@ __global__ void __launch_bounds__(kPreThreads, 1) k_precondition(const float* __
     }
   }
 #pragma unroll
-  for (int r = 0; r < 4; ++r) *reinterpret_cast<float4*>(F + (ly + r) * kPreW + lx) = X[r];
-  // Ring tiles: the cells of another rule are the special rows (frame row
-  // 0 and rows [rb, h)) across the tile's in-frame columns, and the special
-  // columns (0 and [cb, w)) down its other in-frame rows.
-  const int groups = (w >= 3 && h >= 3) ? (w - 2) / 4 : 0;
-  const size_t bulk = plane - plane % 4;
-  int cx0 = 0, ncin = 0, nr0 = 0, nrin = 0, rB0 = 0, cB0 = 0, nsr = 0, nsc = 0;
-  bool r0 = false, c0 = false;
-  bool mine = false;  // the thread owns a cell of another rule
-  if (kEdge) {
-    const int bulk_row = (int)(bulk / (size_t)w), row_end = bulk == plane ? h - 1 : min(h - 1, bulk_row);
-    const int rb = max(row_end, 1), cb = max(min(w - 1, 4 * groups + 1), 1);
-    cx0 = max(0, -gx0);
-    ncin = max(0, min(kPreW, w - gx0) - cx0);
-    const int ry0 = max(0, -gy0), ry1 = min(kPreW, h - gy0), cx1 = cx0 + ncin;
-    r0 = -gy0 >= ry0 && -gy0 < ry1;
-    rB0 = max(ry0, rb - gy0);
-    nsr = (r0 ? 1 : 0) + max(0, ry1 - rB0);
-    nr0 = max(ry0, 1 - gy0);
-    nrin = max(0, min(ry1, rb - gy0) - nr0);
-    c0 = -gx0 >= cx0 && -gx0 < cx1;
-    cB0 = max(cx0, cb - gx0);
-    nsc = (c0 ? 1 : 0) + max(0, cx1 - cB0);
-#pragma unroll
-    for (int r = 0; r < 4; ++r)
-#pragma unroll
-      for (int j = 0; j < 4; ++j) {
-        const int cx = gx + j, cy = gy + r;
-        if (cx >= 0 && cx < w && cy >= 0 && cy < h &&
-            (cx == 0 || cx >= cb || cy == 0 || cy >= rb))
-          mine = true;
-      }
-  }
+  for (int r = 0; r < 4; ++r) *reinterpret_cast<float4*>(F + (ly + r) * kPreP + lx) = X[r];
   const f2 c2 = f2_pack(k.centre, k.centre), e2 = f2_pack(k.edge, k.edge);
   const f2 k2 = f2_pack(k.corner, k.corner), i2 = f2_pack(k.inv_c, k.inv_c);
   const f2 nz = f2_pack(k.neg_zero, k.neg_zero);
   const unsigned full = 0xffffffffu;
-  // The rows just above and below the warp's (clamped to the tile: the
-  // tile's edge rows, never read by an exact cell).
-  const int row_up = max(ly - 1, 0) * kPreW + lx, row_down = min(ly + 4, kPreW - 1) * kPreW + lx;
-  if (kEdge) {
-#pragma unroll
-    for (int r = 0; r < 4; ++r) *reinterpret_cast<float4*>(S2 + (ly + r) * kPreW + lx) = X[r];
-  }
+  if (!kEdge) {
+    // The rows just above and below the warp's: the last row of the warp
+    // above and the first of the warp below (the tile's edge rows for the
+    // first and last warps, never read by an exact cell).
+    const int row_up = (2 * max(warp - 1, 0) + 1) * kPreW + lx;
+    const int row_down = (2 * min(warp + 1, kPreWarps - 1)) * kPreW + lx;
 #pragma unroll 1
-  for (int it = 0; it < 12; ++it) {
-    float* const S = S2 + (it & 1) * (kPreW * kPreW);
-    // Publish the step's input: the warp's first and last rows (ring tiles
-    // hold the whole tile there already).
-    if (!kEdge) {
-      *reinterpret_cast<float4*>(S + ly * kPreW + lx) = X[0];
-      *reinterpret_cast<float4*>(S + (ly + 3) * kPreW + lx) = X[3];
+    for (int it = 0; it < 12; ++it) {
+      float* const S = xb + (it & 1) * (kPreWarps * 2 * kPreW);
+      *reinterpret_cast<float4*>(S + (2 * warp) * kPreW + lx) = X[0];
+      *reinterpret_cast<float4*>(S + (2 * warp + 1) * kPreW + lx) = X[3];
+      __syncthreads();
+      float4 prev = *reinterpret_cast<const float4*>(S + row_up);
+      float pW = __shfl_up_sync(full, prev.w, 1), pE = __shfl_down_sync(full, prev.x, 1);
+      float mW = __shfl_up_sync(full, X[0].w, 1), mE = __shfl_down_sync(full, X[0].x, 1);
+#pragma unroll
+      for (int r = 0; r < 4; ++r) {
+        const float4 nxt =
+            r < 3 ? X[r + 1 < 4 ? r + 1 : 3] : *reinterpret_cast<const float4*>(S + row_down);
+        const float sW = __shfl_up_sync(full, nxt.w, 1), sE = __shfl_down_sync(full, nxt.x, 1);
+        const float4 f = *reinterpret_cast<const float4*>(F + (ly + r) * kPreP + lx);
+        f2 kxa, kxb;
+        const PreRows q = pre_rows(prev, pW, pE, X[r], mW, mE, nxt, sW, sE);
+        pre_kx_interior(q, c2, e2, k2, nz, kxa, kxb);
+        const float4 y = pre_update(q, f, kxa, kxb, i2, nz);
+        prev = X[r];
+        pW = mW;
+        pE = mE;
+        X[r] = y;
+        mW = sW;
+        mE = sE;
+      }
+    }
+  } else {
+    // Ring tiles keep the step's input in shared memory and write the
+    // step's output to the other buffer; each thread first finds its cell
+    // of another rule, if it has one.
+    const PreRingCells rc = pre_ring_cells(w, h, gx0, gy0);
+    PreSpecial mine{0u, 0u};
+    if ((int)threadIdx.x < rc.count) mine = rc.special(threadIdx.x, w, h, gx0, gy0);
+#pragma unroll
+    for (int r = 0; r < 4; ++r) *reinterpret_cast<float4*>(xb + (ly + r) * kPreP + lx) = X[r];
+    const int row_up = max(ly - 1, 0) * kPreP + lx;
+#pragma unroll 1
+    for (int it = 0; it < 12; ++it) {
+      const float* const S = xb + (it & 1) * (kPreW * kPreP);
+      float* const Sn = xb + ((it + 1) & 1) * (kPreW * kPreP);
+      __syncthreads();
+      // A warp whose four rows have all left the exact region [1 + it,
+      // 127 - it) rests; its rows in the step buffers are read only by
+      // cells that are no longer exact either.
+      if (!(4 * warp + 3 < 1 + it || 4 * warp >= kPreW - 1 - it)) {
+        float4 prev = *reinterpret_cast<const float4*>(S + row_up);
+        float4 cur = *reinterpret_cast<const float4*>(S + ly * kPreP + lx);
+        float pW = __shfl_up_sync(full, prev.w, 1), pE = __shfl_down_sync(full, prev.x, 1);
+        float mW = __shfl_up_sync(full, cur.w, 1), mE = __shfl_down_sync(full, cur.x, 1);
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+          const float4 nxt =
+              *reinterpret_cast<const float4*>(S + min(ly + r + 1, kPreW - 1) * kPreP + lx);
+          const float sW = __shfl_up_sync(full, nxt.w, 1), sE = __shfl_down_sync(full, nxt.x, 1);
+          const float4 f = *reinterpret_cast<const float4*>(F + (ly + r) * kPreP + lx);
+          f2 kxa, kxb;
+          const PreRows q = pre_rows(prev, pW, pE, cur, mW, mE, nxt, sW, sE);
+          pre_kx_interior(q, c2, e2, k2, nz, kxa, kxb);
+          *reinterpret_cast<float4*>(Sn + (ly + r) * kPreP + lx) = pre_update(q, f, kxa, kxb, i2, nz);
+          prev = cur;
+          pW = mW;
+          pE = mE;
+          cur = nxt;
+          mW = sW;
+          mE = sE;
+        }
+      }
+      __syncthreads();
+      if (mine.b) pre_special_step(mine, S, F, Sn, k);
+      // More cells than threads (none for frames at least 4 samples wide).
+      if (rc.count > kPreThreads) {
+        const PreRingCells more = pre_ring_cells(w, h, gx0, gy0);
+        for (int i = threadIdx.x + kPreThreads; i < more.count; i += kPreThreads)
+          pre_special_step(more.special(i, w, h, gx0, gy0), S, F, Sn, k);
+      }
     }
     __syncthreads();
-    float4 prev = *reinterpret_cast<const float4*>(S + row_up);
-    float pW = __shfl_up_sync(full, prev.w, 1), pE = __shfl_down_sync(full, prev.x, 1);
-    float mW = __shfl_up_sync(full, X[0].w, 1), mE = __shfl_down_sync(full, X[0].x, 1);
+    // Twelve steps end in buffer 0; each thread reads back its own rows.
 #pragma unroll
-    for (int r = 0; r < 4; ++r) {
-      const float4 nxt = r < 3 ? X[r + 1 < 4 ? r + 1 : 3] : *reinterpret_cast<const float4*>(S + row_down);
-      const float sW = __shfl_up_sync(full, nxt.w, 1), sE = __shfl_down_sync(full, nxt.x, 1);
-      const float4 f = *reinterpret_cast<const float4*>(F + (ly + r) * kPreW + lx);
-      const float4 y = pre_row4(prev, pW, pE, X[r], mW, mE, nxt, sW, sE, f, c2, e2, k2, i2, nz);
-      prev = X[r];
-      pW = mW;
-      pE = mE;
-      X[r] = y;
-      mW = sW;
-      mE = sE;
-    }
-    if (kEdge) {
-      // The paired results into the next step's input, then the cells of
-      // another rule recomputed there from this step's, shared out over the
-      // CTA; the owners read their cells back.
-      float* const Sn = S2 + ((it + 1) & 1) * (kPreW * kPreW);
-#pragma unroll
-      for (int r = 0; r < 4; ++r) *reinterpret_cast<float4*>(Sn + (ly + r) * kPreW + lx) = X[r];
-      __syncthreads();
-      const int nrow_cells = nsr * ncin;
-      const int total = nrow_cells + nsc * nrin;
-      for (int i = threadIdx.x; i < total; i += kPreThreads) {
-        int ty, tx;
-        if (i < nrow_cells) {
-          const int r = i / ncin;
-          tx = cx0 + (i - r * ncin);
-          ty = r0 ? (r == 0 ? -gy0 : rB0 + r - 1) : rB0 + r;
-        } else {
-          const int j = i - nrow_cells;
-          const int ci = j / nrin;
-          ty = nr0 + (j - ci * nrin);
-          tx = c0 ? (ci == 0 ? -gx0 : cB0 + ci - 1) : cB0 + ci;
-        }
-        const int cx = gx0 + tx, cy = gy0 + ty;
-        const bool border = cx == 0 || cx == w - 1 || cy == 0 || cy == h - 1;
-        const bool seq = border || cx - 1 >= 4 * groups;
-        const bool div = (size_t)cy * w + cx >= bulk;
-        Sn[ty * kPreW + tx] = pre_cell(S, F, ty, tx, cx, cy, gx0, gy0, w, h, seq, div, k);
-      }
-      __syncthreads();
-      if (mine) {
-#pragma unroll
-        for (int r = 0; r < 4; ++r) X[r] = *reinterpret_cast<const float4*>(Sn + (ly + r) * kPreW + lx);
-      }
-    }
+    for (int r = 0; r < 4; ++r) X[r] = *reinterpret_cast<const float4*>(xb + (ly + r) * kPreP + lx);
   }
   // The inner 104 x 104: lanes 3 .. 28 of warps 3 .. 28.
   const int oh = kPreHalo / 4;
@@ -383,7 +463,8 @@ __global__ void __launch_bounds__(kPreThreads, 1) k_precondition(const float* __
   }
 }
 
-int launch_precondition(const float* in, float* out, int w, int h, cudaStream_t s) {
+int launch_precondition(const float* in, float* out, int w, int h, cudaStream_t s,
+                        cudaStream_t ring_s) {
   const float w1 = 0.115169525f, w2 = 0.061248592f;
   // gaborish.rs:31 GaborKernel::new, normalised without FMA.
   float unnorm = 1.0f + 4.0f * w1 + 4.0f * w2;
@@ -410,14 +491,17 @@ int launch_precondition(const float* in, float* out, int w, int h, cudaStream_t 
   }
   int launches = 0;
   const int nfast = (pt.fx1 - pt.fx0) * (pt.fy1 - pt.fy0);
+  const int nedge = pt.tx * pt.ty - nfast;
+  // The ring first: its tiles take longer, and the interior tiles fill the
+  // SMs around them.
+  if (nedge > 0) {
+    k_precondition<true><<<dim3(nedge, 1, 3), kPreThreads, kPreRingSmem, ring_s>>>(in, out, w, h,
+                                                                                 k, pt);
+    ++launches;
+  }
   if (nfast > 0) {
     k_precondition<false><<<dim3(pt.fx1 - pt.fx0, pt.fy1 - pt.fy0, 3), kPreThreads, kPreSmem, s>>>(
         in, out, w, h, k, pt);
-    ++launches;
-  }
-  const int nedge = pt.tx * pt.ty - nfast;
-  if (nedge > 0) {
-    k_precondition<true><<<dim3(nedge, 1, 3), kPreThreads, kPreSmem, s>>>(in, out, w, h, k, pt);
     ++launches;
   }
   return launches;
@@ -1262,7 +1346,7 @@ cudaError_t configure_encode_kernels() {
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kPreSmem);
   if (e != cudaSuccess) return e;
   return cudaFuncSetAttribute(k_precondition<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              (int)kPreSmem);
+                              (int)kPreRingSmem);
 }
 
 void upload_dct_constants(const float* iv4, const float* iv8, const float* iv16,
