@@ -873,6 +873,8 @@ def run_ours(args):
         modes[p] = {"value": round(px_total / (ms_p / 1e3) / 1e6, 2),
                     "ms_per_step": round(ms_p / args.steps, 3),
                     "dct_stages_ms_per_image": round(dct_ms, 4),
+                    "stages_ms": {k: round(v[0] / args.steps, 4)
+                                  for k, v in stage_sets[p].items()},
                     "scores": [round(float(x), 6) for x in p_scores]}
     for p in mode_list:
         if "fp32" not in modes:

@@ -327,13 +327,7 @@ int transform_frame(jpxlg_ctx* ctx, const Geo& g, const void* rgb_dev, int bits,
   if (p->gaborish) {
     CK(ctx->pre.ensure(3 * n * sizeof(float)));
     stage_begin(ctx, JPXLG_STAGE_PRECONDITION);
-    {
-      const int chains[2] = {2, 1};  // the interior tiles here, the ring of tiles beside
-      const ClassStreams cs = class_fork(ctx, chains, 2);
-      rc = after_launch(ctx, launch_precondition(xyb, ctx->pre.as<float>(), g.w, g.h, cs.s[0],
-                                                 cs.s[1]));
-      class_join(ctx, cs);
-    }
+    rc = after_launch(ctx, launch_precondition(xyb, ctx->pre.as<float>(), g.w, g.h, ctx->stream));
     stage_end(ctx);
     if (rc) return rc;
     pre = ctx->pre.as<float>();

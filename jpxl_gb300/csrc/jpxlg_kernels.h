@@ -76,11 +76,9 @@ void upload_dct_constants(const float* iv4, const float* iv8, const float* iv16,
                           const float* scale_f, cudaStream_t s);
 void launch_srgb_to_xyb(const void* rgb, int bits, size_t n, const float* lut, float* x, float* y,
                         float* b, uint32_t* not_gray, int num_sms, cudaStream_t s);
-// Two launches at most: the tiles inside the frame's rows and columns of
-// other rules on s, the ring of tiles around them on ring_s (which may be
-// s; they write disjoint outputs); returns how many ran.
-int launch_precondition(const float* in, float* out, int w, int h, cudaStream_t s,
-                        cudaStream_t ring_s);
+// One launch (the ring of tiles along the frame's rows and columns of other
+// rules, then the tiles inside it); returns 1.
+int launch_precondition(const float* in, float* out, int w, int h, cudaStream_t s);
 // The per-shape-class launchers take one stream per class (s[i] for class
 // i), so that independent classes can run side by side.  Each returns the
 // number of kernels it launched.

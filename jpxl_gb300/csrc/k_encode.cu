@@ -101,14 +101,16 @@ void launch_srgb_to_xyb(const void* rgb, int bits, size_t n, const float* lut, f
 // are, and no cell of the edge ring is ever read by one nearer the centre
 // than itself.
 //
-// Two kernels cover a frame: the tiles whose haloed extent has no cell of
+// Two kinds of tile cover a frame: those whose haloed extent has no cell of
 // another rule (kEdge false), and the ring of tiles around them (kEdge
 // true).  A ring tile keeps each step's input in shared memory and, after
 // the paired update of every cell, the CTA's threads share out the cells of
 // another rule (frame border and columns past the groups of four: the
 // sequential nine-tap sum; the last n % 4 cells of the plane: the division
 // by the centre weight) and recompute them from their nine taps at mirrored
-// frame coordinates (always among the cell's own 3 x 3 neighbourhood).
+// frame coordinates (always among the cell's own 3 x 3 neighbourhood).  One
+// launch holds both: the ring's CTAs first (they take longer), then the
+// interior's, which fill the SMs around them.
 constexpr int kPreOut = 104;
 constexpr int kPreHalo = 12;
 constexpr int kPreW = kPreOut + 2 * kPreHalo;  // 128: 32 lanes x 4 columns
@@ -132,8 +134,7 @@ struct EncKernel {
 };
 
 // The tiles of a frame: a rectangle [fx0, fx1) x [fy0, fy1) of tiles with no
-// cell of another rule (kEdge false) and the ring around it (kEdge true, one
-// CTA per ring tile in blockIdx.x).
+// cell of another rule (kEdge false) and the ring around it (kEdge true).
 struct PreTiles {
   int tx, ty;  // tiles across and down
   int fx0, fx1, fy0, fy1;
@@ -290,10 +291,13 @@ __device__ __forceinline__ PreRingCells pre_ring_cells(int w, int h, int gx0, in
 
 __device__ __forceinline__ int pre_clamp(int c, int size) { return min(max(c, 0), size - 1); }
 
+// One tile: item is the tile's index among the interior tiles (row-major
+// over the rectangle) or among the ring tiles.
 template <bool kEdge>
-__global__ void __launch_bounds__(kPreThreads, 1) k_precondition(const float* __restrict__ in,
-                                                              float* __restrict__ out, int w,
-                                                              int h, EncKernel k, PreTiles pt) {
+__device__ __forceinline__ void precondition_tile(const float* __restrict__ in,
+                                                  float* __restrict__ out, int w, int h,
+                                                  const EncKernel& k, const PreTiles& pt,
+                                                  int item) {
   extern __shared__ __align__(16) float pre_smem[];
   float* const F = pre_smem;                   // [kPreW][kPreP]
   float* const xb = pre_smem + kPreW * kPreP;  // published rows, or the ring's step inputs
@@ -302,12 +306,13 @@ __global__ void __launch_bounds__(kPreThreads, 1) k_precondition(const float* __
   out += plane * blockIdx.z;
   int tile_x, tile_y;
   if (!kEdge) {
-    tile_x = pt.fx0 + (int)blockIdx.x;
-    tile_y = pt.fy0 + (int)blockIdx.y;
+    const int nfx = pt.fx1 - pt.fx0;
+    tile_y = pt.fy0 + item / nfx;
+    tile_x = pt.fx0 + item % nfx;
   } else {
     // Ring tiles: the rows above the rectangle, the rows below it, then the
     // tiles left and right of it on its rows.
-    int i = (int)blockIdx.x;
+    int i = item;
     const int top = pt.fy0 * pt.tx, bottom = (pt.ty - pt.fy1) * pt.tx;
     if (i < top) {
       tile_y = i / pt.tx;
@@ -463,8 +468,18 @@ __global__ void __launch_bounds__(kPreThreads, 1) k_precondition(const float* __
   }
 }
 
-int launch_precondition(const float* in, float* out, int w, int h, cudaStream_t s,
-                        cudaStream_t ring_s) {
+// Both kinds of tile in one launch: the ring tiles at blockIdx.x < nedge,
+// then the interior tiles.
+__global__ void __launch_bounds__(kPreThreads, 1) k_precondition(const float* __restrict__ in,
+                                                              float* __restrict__ out, int w,
+                                                              int h, EncKernel k, PreTiles pt,
+                                                              int nedge) {
+  const int i = (int)blockIdx.x;
+  if (i < nedge) precondition_tile<true>(in, out, w, h, k, pt, i);
+  else precondition_tile<false>(in, out, w, h, k, pt, i - nedge);
+}
+
+int launch_precondition(const float* in, float* out, int w, int h, cudaStream_t s) {
   const float w1 = 0.115169525f, w2 = 0.061248592f;
   // gaborish.rs:31 GaborKernel::new, normalised without FMA.
   float unnorm = 1.0f + 4.0f * w1 + 4.0f * w2;
@@ -489,22 +504,11 @@ int launch_precondition(const float* in, float* out, int w, int h, cudaStream_t 
     pt.fy0 = 1;
     pt.fy1 = fy1;
   }
-  int launches = 0;
   const int nfast = (pt.fx1 - pt.fx0) * (pt.fy1 - pt.fy0);
   const int nedge = pt.tx * pt.ty - nfast;
-  // The ring first: its tiles take longer, and the interior tiles fill the
-  // SMs around them.
-  if (nedge > 0) {
-    k_precondition<true><<<dim3(nedge, 1, 3), kPreThreads, kPreRingSmem, ring_s>>>(in, out, w, h,
-                                                                                 k, pt);
-    ++launches;
-  }
-  if (nfast > 0) {
-    k_precondition<false><<<dim3(pt.fx1 - pt.fx0, pt.fy1 - pt.fy0, 3), kPreThreads, kPreSmem, s>>>(
-        in, out, w, h, k, pt);
-    ++launches;
-  }
-  return launches;
+  k_precondition<<<dim3(nedge + nfast, 1, 3), kPreThreads, kPreRingSmem, s>>>(in, out, w, h, k,
+                                                                             pt, nedge);
+  return 1;
 }
 
 // ---------------------------------------------------------------------------
@@ -1342,10 +1346,7 @@ void launch_mul_table(uint32_t global_scale, float* table, cudaStream_t s) {
 }
 
 cudaError_t configure_encode_kernels() {
-  cudaError_t e = cudaFuncSetAttribute(k_precondition<false>,
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kPreSmem);
-  if (e != cudaSuccess) return e;
-  return cudaFuncSetAttribute(k_precondition<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  return cudaFuncSetAttribute(k_precondition, cudaFuncAttributeMaxDynamicSharedMemorySize,
                               (int)kPreRingSmem);
 }
 
