@@ -432,21 +432,39 @@ __global__ void __launch_bounds__(kThreads) k_fdct_tc(EncArgs a, const uint32_t*
     const uint32_t packed = active ? __ldg(&list[vi]) : 0u;
     return Src{active, (int)(packed & 0xffff) * 8, (int)(packed >> 16) * 8};
   };
+  // Rows inside the frame of a plane with 16-byte aligned rows take 16-byte
+  // loads.
+  const bool rows16 = (geo.w & 3) == 0 && (reinterpret_cast<uintptr_t>(a.pre) & 15) == 0;
   auto load_row = [&](const Src& src, int c, float* row) {
     if (src.active) {
       const int yy = min(src.y0 + r, geo.h - 1);
       const float* p = a.pre + plane * c + (size_t)yy * geo.w;
+      if (rows16 && src.x0 + N <= geo.w) {
+        const float4* p4 = reinterpret_cast<const float4*>(p + src.x0);
 #pragma unroll
-      for (int x = 0; x < N; ++x) row[x] = __ldg(&p[min(src.x0 + x, geo.w - 1)]);
+        for (int x = 0; x < N; x += 4) {
+          const float4 v = __ldg(p4 + x / 4);
+          row[x] = v.x;
+          row[x + 1] = v.y;
+          row[x + 2] = v.z;
+          row[x + 3] = v.w;
+        }
+      } else {
+#pragma unroll
+        for (int x = 0; x < N; ++x) row[x] = __ldg(&p[min(src.x0 + x, geo.w - 1)]);
+      }
     } else {
 #pragma unroll
       for (int x = 0; x < N; ++x) row[x] = 0.0f;
     }
   };
   // (tile, channel) steps in order; the next step's row is loaded before
-  // this step's transform, so that its latency overlaps the MMAs.
+  // this step's transform, so that its latency overlaps the MMAs, and the
+  // next tile's varblock a tile ahead, so that those loads never wait on it.
+  const Src none{false, 0, 0};
   int tile = blockIdx.x, c = 0;
-  Src cur = tile < ntiles ? locate(tile) : Src{false, 0, 0};
+  Src cur = tile < ntiles ? locate(tile) : none;
+  Src after = tile + (int)gridDim.x < ntiles ? locate(tile + gridDim.x) : none;
   float nxt[N];
   if (tile < ntiles) load_row(cur, 0, nxt);
   while (tile < ntiles && st.ok) {
@@ -458,7 +476,8 @@ __global__ void __launch_bounds__(kThreads) k_fdct_tc(EncArgs a, const uint32_t*
     if (++c == 3) {
       c = 0;
       tile += gridDim.x;
-      if (tile < ntiles) cur = locate(tile);
+      cur = after;
+      if (tile + (int)gridDim.x < ntiles) after = locate(tile + gridDim.x);
     }
     if (tile < ntiles) load_row(cur, c, nxt);
     transform_rows<N, TERMS>(smem, &mbar, st, row);
@@ -524,10 +543,15 @@ __global__ void __launch_bounds__(kThreads) k_render_tc(RenderArgs a,
     bool active;
     int x0, y0;
   };
-  auto load_q = [&](int tile, int c, QRow& qr) {
+  // The list entry of this thread's varblock in a tile (0 past the end),
+  // fetched a tile ahead of its rows.
+  auto entry = [&](int tile) {
+    const int vi = tile * T::kVpt + b;
+    return vi < count ? __ldg(&list[vi]) : 0u;
+  };
+  auto load_q = [&](int tile, int c, uint32_t packed, QRow& qr) {
     const int vi = tile * T::kVpt + b;
     qr.active = vi < count;
-    const uint32_t packed = qr.active ? __ldg(&list[vi]) : 0u;
     qr.x0 = (int)(packed & 0xffff) * 8;
     qr.y0 = (int)(packed >> 16) * 8;
     if (!qr.active) return;
@@ -554,9 +578,12 @@ __global__ void __launch_bounds__(kThreads) k_render_tc(RenderArgs a,
   int tile = blockIdx.x, ci = 0;
   float pm = 0.0f, pkx = 0.0f, pkb = 0.0f;
   QRow nq;
+  uint32_t ent = 0u, ent_after = 0u;  // list entries of this tile and the next
   if (tile < ntiles) {
+    ent = entry(tile);
+    if (tile + (int)gridDim.x < ntiles) ent_after = entry(tile + gridDim.x);
     tile_scalars(tile, pm, pkx, pkb);
-    load_q(tile, channel_of(0), nq);
+    load_q(tile, channel_of(0), ent, nq);
   }
   float dY[N];
   while (tile < ntiles && st.ok) {
@@ -575,8 +602,12 @@ __global__ void __launch_bounds__(kThreads) k_render_tc(RenderArgs a,
       nci = 0;
       ntile += gridDim.x;
     }
+    if (nci == 0) {
+      ent = ent_after;
+      if (ntile + (int)gridDim.x < ntiles) ent_after = entry(ntile + gridDim.x);
+    }
     if (ntile < ntiles) {
-      load_q(ntile, channel_of(nci), nq);
+      load_q(ntile, channel_of(nci), ent, nq);
       if (nci == 0) tile_scalars(ntile, pm, pkx, pkb);
     }
     float row[N];
