@@ -1,6 +1,7 @@
 // jpxlg_api.cu — the C ABI (include/jpxlg.h): contexts, layouts, workspace
 // and the host orchestration of the sm_103a kernels.  Host code only; the
 // kernels live in k_encode.cu, k_render.cu and k_ssim.cu.
+#include <limits>
 #include <algorithm>
 #include <cstdarg>
 #include <cstdio>
@@ -47,6 +48,9 @@ struct DevBuf {
 struct DepthTable {
   float* thr = nullptr;
   float* lev = nullptr;
+  // Entry i: (threshold i-1 or -inf, threshold i or +inf, level i's value,
+  // 0): a level estimate is confirmed and resolved by one 16-byte load.
+  float4* bracket = nullptr;
   int levels = 0;
 };
 
@@ -280,6 +284,13 @@ const DepthTable* get_depth(jpxlg_ctx* ctx, int bits) {
   if (cudaMalloc(&t.lev, levels * sizeof(float)) != cudaSuccess) return nullptr;
   cudaMemcpy(t.thr, thr.data(), levels * sizeof(float), cudaMemcpyHostToDevice);
   cudaMemcpy(t.lev, lev.data(), levels * sizeof(float), cudaMemcpyHostToDevice);
+  // levels - 1 thresholds bracket the levels 0 .. levels - 1.
+  std::vector<float4> br(levels);
+  const float inf = std::numeric_limits<float>::infinity();
+  for (int i = 0; i < levels; ++i)
+    br[i] = make_float4(i == 0 ? -inf : thr[i - 1], i == levels - 1 ? inf : thr[i], lev[i], 0.0f);
+  if (cudaMalloc(&t.bracket, levels * sizeof(float4)) != cudaSuccess) return nullptr;
+  cudaMemcpy(t.bracket, br.data(), levels * sizeof(float4), cudaMemcpyHostToDevice);
   ctx->depth[bits] = t;
   return &ctx->depth[bits];
 }
@@ -513,7 +524,8 @@ int render_device(jpxlg_ctx* ctx, const jpxlg_layout* L, const int32_t* qcoeff,
   }
   stage_begin(ctx, JPXLG_STAGE_COLOUR);
   launch_colour_out(cur, g.w, g.h, out_kind, dt ? dt->thr : nullptr, dt ? dt->lev : nullptr,
-                    dt ? dt->levels : 0, out_dev, pxyb_dev, ctx->num_sms, ctx->stream);
+                    dt ? dt->bracket : nullptr, dt ? dt->levels : 0, out_dev, pxyb_dev,
+                    ctx->num_sms, ctx->stream);
   rc = after_launch(ctx, 1);
   stage_end(ctx);
   return rc;
@@ -643,6 +655,7 @@ int jpxlg_ctx_destroy(jpxlg_ctx* ctx) {
   for (auto& kv : ctx->depth) {
     cudaFree(kv.second.thr);
     cudaFree(kv.second.lev);
+    cudaFree(kv.second.bracket);
   }
   DevBuf* bufs[] = {&ctx->rgb,    &ctx->xyb,   &ctx->pre,     &ctx->coeff,   &ctx->dyhf,
                     &ctx->qcoeff, &ctx->lfs,   &ctx->dylf,    &ctx->lfq,     &ctx->cflx,

@@ -128,9 +128,11 @@ void launch_epf_step(int step, const float* in, float* out, const float* sigma, 
 // out_kind: 1 linear f32 planes, 2 sRGB8 interleaved, 3 linear at depth
 // pxyb (optional, out_kind 3 only): also the SSIMULACRA2 positive XYB planes
 // of the output pixels.
+// bracket (out_kind 3, more than 256 levels): per level (the threshold
+// below, the threshold above, the level's value).
 void launch_colour_out(const float* xyb, int w, int h, int out_kind, const float* thresholds,
-                       const float* levels, int nlevels, void* out, float* pxyb, int num_sms,
-                       cudaStream_t s);
+                       const float* levels, const float4* bracket, int nlevels, void* out,
+                       float* pxyb, int num_sms, cudaStream_t s);
 void upload_render_constants(const float* opsin_m, const float* opsin_bias,
                              const float* opsin_bias_cbrt, cudaStream_t s);
 

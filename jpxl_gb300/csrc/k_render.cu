@@ -764,33 +764,38 @@ __device__ __forceinline__ int level_of(float x, const float* thr, int n) {
   return lo;
 }
 
-// For deep outputs (65535 thresholds in global memory) the level is first
-// estimated from the transfer curve with the fast powf (its error, a few
-// ulp, moves the estimate by well under one level) and then confirmed
-// against the exact thresholds (two loads), stepping by one where the
-// estimate sits on the wrong side; the binary search remains the fallback.
-// The thresholds decide, so the result is exactly the bisected level.
-__device__ __forceinline__ int level_guided(float x, const float* __restrict__ thr, int n,
-                                            float maxv) {
-  if (!isfinite(x)) return 0;
+// The linear value of x's level among n + 1 levels, for deep outputs
+// (65536 levels): the level is first estimated from the transfer curve with
+// the fast powf (its error, a few ulp, moves the estimate by well under one
+// level), then confirmed against the exact thresholds around it, stepping by
+// one where the estimate sits on the wrong side; one 16-byte load of the
+// bracket table per try gives both thresholds and the level's value.  The
+// binary search remains the fallback.  The thresholds decide, so the result
+// is exactly the bisected level's.
+__device__ __forceinline__ float level_value_bracketed(float x, const float4* __restrict__ br,
+                                                       const float* __restrict__ thr,
+                                                       const float* __restrict__ levels, int n,
+                                                       float maxv) {
+  if (!isfinite(x)) return __ldg(&levels[0]);
   float a = fabsf(x);
   float e = a <= 0.0031308f ? 12.92f * a : 1.055f * __powf(a, 1.0f / 2.4f) - 0.055f;
   float s = rintf((x < 0.0f ? -e : e) * maxv);
   int est = (int)fminf(fmaxf(s, 0.0f), maxv);
 #pragma unroll 1
   for (int it = 0; it < 4; ++it) {
-    bool lo_ok = est == 0 || __ldg(&thr[est - 1]) <= x;
-    bool hi_ok = est == n || x < __ldg(&thr[est]);
-    if (lo_ok && hi_ok) return est;
+    const float4 v = __ldg(&br[est]);
+    const bool lo_ok = v.x <= x, hi_ok = x < v.y;
+    if (lo_ok && hi_ok) return v.z;
     est += lo_ok ? 1 : -1;
   }
-  return level_of(x, thr, n);
+  return __ldg(&levels[level_of(x, thr, n)]);
 }
 
 template <int KIND>
 __global__ void __launch_bounds__(256) k_colour_out(const float* __restrict__ xyb, size_t n,
                                                     const float* __restrict__ thr,
-                                                    const float* __restrict__ levels, int nlev,
+                                                    const float* __restrict__ levels,
+                                                    const float4* __restrict__ bracket, int nlev,
                                                     void* __restrict__ out,
                                                     float* __restrict__ pxyb) {
   __shared__ float s_thr[255];
@@ -847,7 +852,8 @@ __global__ void __launch_bounds__(256) k_colour_out(const float* __restrict__ xy
       } else {
         const float maxv = (float)(nlev - 1);
 #pragma unroll
-        for (int q = 0; q < 3; ++q) lin[q] = __ldg(&LV[level_guided(rgb[q], T, nlev - 1, maxv)]);
+        for (int q = 0; q < 3; ++q)
+          lin[q] = level_value_bracketed(rgb[q], bracket, T, LV, nlev - 1, maxv);
       }
       float* o = (float*)out;
       o[i] = lin[0];
@@ -867,19 +873,23 @@ __global__ void __launch_bounds__(256) k_colour_out(const float* __restrict__ xy
 }
 
 void launch_colour_out(const float* xyb, int w, int h, int out_kind, const float* thresholds,
-                       const float* levels, int nlevels, void* out, float* pxyb, int num_sms,
-                       cudaStream_t s) {
+                       const float* levels, const float4* bracket, int nlevels, void* out,
+                       float* pxyb, int num_sms, cudaStream_t s) {
   size_t n = (size_t)w * h;
   int blocks = (int)std::min<size_t>((n + 255) / 256, (size_t)num_sms * 8);
   if (blocks < 1) blocks = 1;
   if (out_kind == 1)
-    k_colour_out<1><<<blocks, 256, 0, s>>>(xyb, n, thresholds, levels, nlevels, out, nullptr);
+    k_colour_out<1><<<blocks, 256, 0, s>>>(xyb, n, thresholds, levels, bracket, nlevels, out,
+                                           nullptr);
   else if (out_kind == 2)
-    k_colour_out<2><<<blocks, 256, 0, s>>>(xyb, n, thresholds, levels, nlevels, out, nullptr);
+    k_colour_out<2><<<blocks, 256, 0, s>>>(xyb, n, thresholds, levels, bracket, nlevels, out,
+                                           nullptr);
   else if (out_kind == 4)
-    k_colour_out<4><<<blocks, 256, 0, s>>>(xyb, n, thresholds, levels, nlevels, out, nullptr);
+    k_colour_out<4><<<blocks, 256, 0, s>>>(xyb, n, thresholds, levels, bracket, nlevels, out,
+                                           nullptr);
   else
-    k_colour_out<3><<<blocks, 256, 0, s>>>(xyb, n, thresholds, levels, nlevels, out, pxyb);
+    k_colour_out<3><<<blocks, 256, 0, s>>>(xyb, n, thresholds, levels, bracket, nlevels, out,
+                                           pxyb);
 }
 
 // ---------------------------------------------------------------------------
