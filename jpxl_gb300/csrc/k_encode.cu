@@ -956,15 +956,31 @@ __global__ void __launch_bounds__(kCflThreads, 4) k_cfl_tile_bits(EncArgs a,
     const int col = threadIdx.x % 64;
     if (col < pw) {
       const int px = px0 + col;
-      for (int row = threadIdx.x / 64; row < ph; row += kCflThreads / 64) {
+      // Each row's block-map entry and three samples are loaded a row ahead
+      // of its quantizer evaluations, so that their latency overlaps them.
+      struct Cell {
+        uint8_t sel;
+        float dy, x, b;
+      };
+      auto fetch = [&](int row) {
         const int py = py0 + row;
-        int lg;
-        if (cell_is_llf(a.block_map, geo.bw, px, py, &lg)) continue;
+        const size_t ci = (size_t)py * geo.W8 + px;
+        return Cell{a.block_map[(size_t)(py >> 3) * geo.bw + (px >> 3)], a.dyhf[ci], a.coeff[ci],
+                    a.coeff[2 * cplane + ci]};
+      };
+      int row = threadIdx.x / 64;
+      Cell nxt = row < ph ? fetch(row) : Cell{0, 0.0f, 0.0f, 0.0f};
+      for (; row < ph; row += kCflThreads / 64) {
+        const int py = py0 + row;
+        const Cell cur = nxt;
+        if (row + kCflThreads / 64 < ph) nxt = fetch(row + kCflThreads / 64);
+        // cell_is_llf on the prefetched block-map entry.
+        const int sel = cur.sel & 0x1f;
+        const int lg = sel == 0 ? 0 : (sel == 4 ? 1 : 2);
         const int mask = (8 << lg) - 1;
+        if ((px & mask) < (1 << lg) && (py & mask) < (1 << lg)) continue;
         const int cell8 = ((py & mask) >> lg) * 8 + ((px & mask) >> lg);
-        size_t ci = (size_t)py * geo.W8 + px;
-        float dy = a.dyhf[ci];
-        float x = a.coeff[ci], b = a.coeff[2 * cplane + ci];
+        const float dy = cur.dy, x = cur.x, b = cur.b;
         const float step_x = s_step[0][cell8], rstep_x = s_rstep[0][cell8];
         const float step_b = s_step[1][cell8], rstep_b = s_rstep[1][cell8];
         float rc;
