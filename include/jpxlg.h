@@ -345,6 +345,8 @@ int jpxlg_symbols_destroy(jpxlg_symbols* s);
  * passes, those larger than a group (both return JPXLG_ERR_STREAM).  ICC profiles, previews, patches, splines, noise and
  * upsampling are reported as unsupported (JPXLG_ERR_STREAM with a reason in
  * jpxlg_codestream_last_error).  Host code only: no device is needed.
+ * Streams may be opened from several host threads at once: the allocation
+ * meter and the last error are per thread, and handles share no state.
  *   jpxlg_codestream_open          parse and decode; *out owns the result
  *   jpxlg_codestream_info          sizes, frame parameters, per-DctSelect
  *                                  varblock counts, and how many sections

@@ -26,6 +26,7 @@ this package                   reference (JPXL, crates/...)
 ``quality.search``             search_frame_perceptual's baseline solve
                                (quality.rs:1775) over BatchProbe rounds
 ``Codestream``                 jpxl-decode decode.rs:400 up to the frame content
+``open_codestreams``           many Codestreams parsed on host threads at once
 ``DecodeBatch``                a loop of decode.rs:400 decode calls as one graph
 =============================  ==================================================
 
@@ -617,6 +618,48 @@ class Codestream:
             self.close()
         except Exception:
             pass
+
+
+def open_codestreams(datas, workers: int | None = None, max_pixels: int | None = None,
+                     max_alloc_bytes: int | None = None) -> list:
+    """Codestream(d) for every d in datas, in order, parsed on up to
+    `workers` host threads (default: one per core).  The reader keeps its
+    allocation meter and last error per thread and ctypes releases the GIL
+    around it, so independent streams parse in parallel.  If any stream is
+    rejected, the others are closed and its JpxlError is raised."""
+    import os
+    from concurrent.futures import ThreadPoolExecutor
+
+    datas = list(datas)
+    n = workers if workers is not None else (os.cpu_count() or 1)
+    n = max(1, min(n, len(datas)))
+
+    def open_one(d):
+        return Codestream(d, max_pixels=max_pixels, max_alloc_bytes=max_alloc_bytes)
+
+    if n == 1:
+        opened = []
+        try:
+            for d in datas:
+                opened.append(open_one(d))
+        except Exception:
+            for s in opened:
+                s.close()
+            raise
+        return opened
+    with ThreadPoolExecutor(n) as ex:
+        futures = [ex.submit(open_one, d) for d in datas]
+    opened, error = [], None
+    for f in futures:
+        try:
+            opened.append(f.result())
+        except Exception as e:  # noqa: BLE001 - re-raised below
+            error = error or e
+    if error is not None:
+        for s in opened:
+            s.close()
+        raise error
+    return opened
 
 
 class DecodeBatch:

@@ -359,3 +359,34 @@ def test_allocation_and_pixel_limits_reject_before_allocating():
     assert e.value.code == -8 and "pixel limit" in str(e.value)
     # the limits are per stream: the next default open succeeds again
     jg.Codestream(data).close()
+
+
+def test_parallel_open_matches_serial():
+    """open_codestreams parses on host threads; every stream's headers,
+    block data and coefficients equal a serial open's, in order."""
+    datas = [(GOLDEN / (n + ".jxl")).read_bytes() for n in VARDCT] * 3
+    par = jg.open_codestreams(datas, workers=8)
+    try:
+        assert len(par) == len(datas)
+        for d, p in zip(datas, par):
+            s = jg.Codestream(d)
+            try:
+                assert p.info == s.info
+                pb, sb = p.blocks(), s.blocks()
+                for k in sb:
+                    assert np.array_equal(pb[k], sb[k]), k
+                assert np.array_equal(p.coefficients(), s.coefficients())
+            finally:
+                s.close()
+    finally:
+        for p in par:
+            p.close()
+
+
+def test_parallel_open_reports_a_bad_stream():
+    """A rejected stream among good ones raises its stream error; the
+    others are closed."""
+    good = (GOLDEN / (VARDCT[0] + ".jxl")).read_bytes()
+    with pytest.raises(jg.JpxlError) as e:
+        jg.open_codestreams([good, good[: len(good) // 3], good], workers=3)
+    assert e.value.code == ERR_STREAM
