@@ -692,12 +692,10 @@ __global__ void __launch_bounds__(256, 3) k_epf(const float* __restrict__ in, fl
     const float pos_mul = at_border ? 2.0f / 3.0f : 1.0f;
     float sum_w = 0.0f, acc0 = 0.0f, acc1 = 0.0f, acc2 = 0.0f;
     constexpr int NT = STEP == 0 ? 13 : 5;
-#pragma unroll
-    for (int tp = 0; tp < NT; ++tp) {
-      // J.4.4 kernels: the 5-pixel cross, plus the diagonals and +-2 for step 0.
-      const int tkx[13] = {0, -1, 1, 0, 0, 1, 1, -1, -1, -2, 2, 0, 0};
-      const int tky[13] = {0, 0, 0, -1, 1, -1, 1, 1, -1, 0, 0, 2, -2};
-      const int kx = tkx[tp], ky = tky[tp];
+    // J.4.4 kernels: the 5-pixel cross, plus the diagonals and +-2 for step 0.
+    constexpr int tkx[13] = {0, -1, 1, 0, 0, 1, 1, -1, -1, -2, 2, 0, 0};
+    constexpr int tky[13] = {0, 0, 0, -1, 1, -1, 1, 1, -1, 0, 0, 2, -2};
+    auto dist = [&](int kx, int ky) {
       float d = 0.0f;
 #pragma unroll
       for (int c = 0; c < 3; ++c) {
@@ -713,14 +711,27 @@ __global__ void __launch_bounds__(256, 3) k_epf(const float* __restrict__ in, fl
           }
         }
       }
+      return d;
+    };
+    auto weight = [&](float d) {
       float sd = pos_mul * d;
-      float wt;
-      if (sd == 0.0f) {
-        wt = 1.0f;
-      } else {
-        float v = __fmaf_rn(sd, -inv_sigma, 1.0f);
-        wt = v > 0.0f ? v : 0.0f;
-      }
+      if (sd == 0.0f) return 1.0f;
+      float v = __fmaf_rn(sd, -inv_sigma, 1.0f);
+      return v > 0.0f ? v : 0.0f;
+    };
+    // The centre tap's distance sums |s - s| over the centre's own patch:
+    // exactly 0 (weight 1) when every sample there is finite, not a number
+    // otherwise.  The next tap's distance takes |s - s'| of the same samples
+    // with positive scales, so it is finite only if they all are; then the
+    // centre's terms are skipped, else evaluated as written.
+    const float d1 = dist(tkx[1], tky[1]);
+    float wts[NT];
+    wts[0] = isfinite(d1) ? 1.0f : weight(dist(0, 0));
+    wts[1] = weight(d1);
+#pragma unroll
+    for (int tp = 0; tp < NT; ++tp) {
+      const int kx = tkx[tp], ky = tky[tp];
+      const float wt = tp < 2 ? wts[tp] : weight(dist(kx, ky));
       sum_w += wt;
       acc0 = __fmaf_rn(t[0][cy + ky][cx + kx], wt, acc0);
       acc1 = __fmaf_rn(t[1][cy + ky][cx + kx], wt, acc1);
