@@ -414,7 +414,9 @@ __global__ void __launch_bounds__(kOutThreads, 4) k_blur_col_out(ColArgs a) {
   __shared__ __align__(16) float tile[NQ][kColT + 10][kColW];  // rows r0-6 .. r0+kColT+3
   __shared__ __align__(16) float rp[NQ][kColT][kColW];
   __shared__ DF red[kOutThreads / 32][6];
-  __shared__ float half_end[2][NQ][6][kColW];  // each half's end state from rest
+  // Each half's end state from rest; once the segment's entry is known,
+  // each half's entry state (read by the outputs as lane pairs).
+  __shared__ __align__(16) float half_end[2][NQ][6][kColW];
   __shared__ float entry[NQ][6][kColW];        // the segment's entry state
   __shared__ int s_item, s_late;
   const int t = threadIdx.x;
@@ -532,6 +534,12 @@ __global__ void __launch_bounds__(kOutThreads, 4) k_blur_col_out(ColArgs a) {
       const float sp = entry[sq][2 * k][sl], sqq = entry[sq][2 * k + 1][sl];
       my_incl[(size_t)(2 * k) * a.w] = (m[0] * sp + m[1] * sqq) + bp;
       my_incl[(size_t)(2 * k + 1) * a.w] = (m[2] * sp + m[3] * sqq) + bq;
+      // Each half's entry state: the segment's entry for the first half,
+      // M^kHalf times it plus the first half's end state for the second.
+      half_end[1][sq][2 * k][sl] = (u0 * sp - u1 * sqq) + p1;
+      half_end[1][sq][2 * k + 1][sl] = (u1 * sp - u2 * sqq) + q1;
+      half_end[0][sq][2 * k][sl] = sp;
+      half_end[0][sq][2 * k + 1][sl] = sqq;
     }
     __threadfence();
   }
@@ -540,36 +548,6 @@ __global__ void __launch_bounds__(kOutThreads, 4) k_blur_col_out(ColArgs a) {
     atomicExch(flags + ((size_t)ch * a.strips + sx) * a.nseg + sg, 1);
     if (s_late) raise_error(a.err, kDevBlurTimeout);
   }
-  // Each half adds the homogeneous response of its entry state through the
-  // U table: the segment's entry for the first half, M^kHalf times it plus
-  // the first half's end state for the second.
-  if (walker) {
-    float ep[3], eq[3];
-#pragma unroll
-    for (int k = 0; k < 3; ++k) {
-      const float p = entry[wq][2 * k][wl], q = entry[wq][2 * k + 1][wl];
-      if (wh == 0) {
-        ep[k] = p;
-        eq[k] = q;
-      } else {
-        const float* U = c_blur.U[k];
-        const float u0 = U[(kHalf) % 20], u1 = U[(kHalf - 1) % 20], u2 = U[(kHalf - 2) % 20];
-        ep[k] = (u0 * p - u1 * q) + half_end[0][wq][2 * k][wl];
-        eq[k] = (u1 * p - u2 * q) + half_end[0][wq][2 * k + 1][wl];
-      }
-    }
-#pragma unroll 4
-    for (int i = 0; i < kHalf; ++i) {
-      float hom = 0.0f;
-#pragma unroll
-      for (int k = 0; k < 3; ++k) {
-        const float* U = c_blur.U[k];
-        hom += U[(i + 1) % 20] * ep[k] - U[i % 20] * eq[k];
-      }
-      rp[wq][wh * kHalf + i][wl] += hom;
-    }
-  }
-  __syncthreads();
   // Outputs: columns 2j, 2j+1 (the lanes) of rows kR*b .. kR*b+kR-1.
   constexpr int kR = kColT / (kOutThreads / (kColW / 2));
   const f2 nz = f2_pack(a.nz, a.nz);
@@ -594,12 +572,24 @@ __global__ void __launch_bounds__(kOutThreads, 4) k_blur_col_out(ColArgs a) {
         pf[e][3] = in ? __ldg(a.cx + p) : 0.0f;
       }
     f2 val[NQ];
+    const int wh = r / kHalf, ir = r % kHalf;
 #pragma unroll
     for (int q = 0; q < NQ; ++q) {
+      // The ripple: its response from rest plus the homogeneous response of
+      // its half's entry state through the U table, hom = sum over the
+      // resonators of U[ir + 1] p - U[ir] q (accumulated from 0).
+      f2 hom = 0ull;
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        const float u1 = c_blur.U[k][(ir + 1) % 20], u0 = c_blur.U[k][ir % 20];
+        const f2 ep = *reinterpret_cast<const f2*>(&half_end[wh][q][2 * k][lx]);
+        const f2 eq = *reinterpret_cast<const f2*>(&half_end[wh][q][2 * k + 1][lx]);
+        hom = f2_add(hom, f2_sub(f2_mul(f2_pack(u1, u1), ep, nz), f2_mul(f2_pack(u0, u0), eq, nz)));
+      }
+      const f2 rip = f2_add(*reinterpret_cast<const f2*>(&rp[q][r][lx]), hom);
       auto tv = [&](int ly) { return *reinterpret_cast<const f2*>(&tile[q][ly][lx]); };
       val[q] = fir_exact2(tv(r + 2), tv(r + 3), tv(r + 4), tv(r + 5), tv(r + 6), tv(r + 7),
-                          tv(r + 8), tv(r + 9), tv(r + 10),
-                          *reinterpret_cast<const f2*>(&rp[q][r][lx]), nz);
+                          tv(r + 8), tv(r + 9), tv(r + 10), rip, nz);
     }
     if (gy >= a.h || gx >= a.w) continue;
     const bool second = gx + 1 < a.w;
