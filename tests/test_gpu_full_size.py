@@ -6,7 +6,7 @@ at global scale 40000 (DCT8/16/32), CfL, Gaborish, 3-step EPF.  The
 reconstruction at 16-bit depth must equal the restatement's bit for bit, the
 probe's score must equal the restatement's within 1e-4 points (the blur
 reproduces the reference's f32 outputs; the contract is 0.01).  Against the
-FP64 truth the linear pixels must stay within 1e-5 (the north star's bound);
+FP64 truth the linear pixels must stay within 1e-5 (the path's pixel bound);
 the score's distance from the FP64 truth is stated, and must be the
 reference arithmetic's own (0.042 points on this image, measured).
 

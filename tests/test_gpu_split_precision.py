@@ -1,7 +1,7 @@
 """The split-precision form of the DCTs (tcgen05 tensor cores, f32 operands
 as bf16 terms, FP32 accumulation) against the FP64 truth and the FP32 form.
 
-Spec bounds for the split form: decoded pixels within 1e-5 max-abs
+The bounds for the split form: decoded pixels within 1e-5 max-abs
 (linear, [0, 1]) of the FP64 truth, SSIMULACRA2 within 0.01 points.  BF16x6
 (three bf16 terms) meets them (measured 3.3e-6 at 2048x2048, the FP32
 kernels' own error is 2.9e-6); BF16x3 (two terms) does not (1.1e-4).  The
