@@ -1,9 +1,9 @@
 """ctypes binding of ``libjpxlg.so`` (the C ABI declared in include/jpxlg.h).
 
 The library is the product: there is no CPU fallback.  ``load()`` raises if
-the shared object is missing or fails to load, so a caller on a GPU machine that
-forgot ``__graft_entry__.build()`` fails loudly instead of silently running
-something else.
+the shared object is missing or fails to load, so a caller on a machine with a
+GPU that has not built the library (``__graft_entry__.build()``) fails loudly
+instead of silently running something else.
 """
 from __future__ import annotations
 

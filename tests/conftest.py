@@ -1,5 +1,5 @@
-"""Shared fixtures: the CPU restatement (the checker) and, on a GPU machine, one
-library context per session."""
+"""Shared fixtures: the CPU restatement (the checker) and, where a GPU is
+present, one library context per session."""
 import sys
 from pathlib import Path
 
