@@ -83,6 +83,7 @@ struct jpxlg_ctx {
   DevBuf planes, aux, sigma, out, llf;
   DevBuf lf_part, lf_seed, cfl_tile, cover, cover_map;
   DevBuf pyr, partial, score, cxyb, hpl, bcarry;
+  DevBuf pair_ref;  // the reference side of jpxlg_score_pair, kept across calls
   // stage timers
   struct Mark {
     int stage;
@@ -661,7 +662,7 @@ int jpxlg_ctx_destroy(jpxlg_ctx* ctx) {
                     &ctx->qcoeff, &ctx->lfs,   &ctx->dylf,    &ctx->lfq,     &ctx->cflx,
                     &ctx->cflb,   &ctx->planes, &ctx->aux,    &ctx->sigma,   &ctx->out,
                     &ctx->lf_part, &ctx->lf_seed, &ctx->cfl_tile, &ctx->cover,
-                    &ctx->cover_map, &ctx->pyr,  &ctx->partial,
+                    &ctx->cover_map, &ctx->pyr,  &ctx->pair_ref, &ctx->partial,
                     &ctx->score,  &ctx->cxyb,   &ctx->hpl,   &ctx->bcarry, &ctx->llf};
   for (DevBuf* b : bufs) b->release();
   for (auto& m : ctx->marks) {
@@ -1004,24 +1005,14 @@ int jpxlg_reconstruct(jpxlg_ctx* ctx, const jpxlg_layout* L, const jpxlg_plan* p
   return sync_and_check(ctx);
 }
 
-int jpxlg_ssim2_ref_create(jpxlg_ctx* ctx, const float* rgb, int w, int h, uint32_t mem,
-                           jpxlg_ref** out) {
-  if (!ctx || !rgb || !out) return fail(ctx, JPXLG_ERR_ARGUMENT, "null argument");
-  *out = nullptr;
-  if (w < 8 || h < 8) return fail(ctx, JPXLG_ERR_TOO_SMALL, "SSIMULACRA2 needs at least 8x8");
-  if (w > kBlurMaxWidth)
-    return fail(ctx, JPXLG_ERR_ARGUMENT, "SSIMULACRA2 frames are limited to %d columns",
-                kBlurMaxWidth);
-  cudaSetDevice(ctx->device);
-  std::unique_ptr<jpxlg_ref> R(new jpxlg_ref);
-  R->ctx = ctx;
-  R->device = ctx->device;
-  R->w = w;
-  R->h = h;
-  // reference.rs:90 — keep halving while the current scale is at least 8x8.
+namespace {
+
+// reference.rs:90: the scales (keep halving while the current one is at
+// least 8x8) and the floats of a reference's planes (per scale: the RGB
+// level, XYB, mu and sigma11, 3 planes each).
+int ref_layout(int w, int h, int dims[6][2], size_t* total) {
   int cw = w, ch = h, ns = 0;
-  size_t total = 0;
-  int dims[6][2];
+  *total = 0;
   for (int s = 0; s < 6; ++s) {
     if (s > 0) {
       if (cw < 8 || ch < 8) break;
@@ -1030,12 +1021,30 @@ int jpxlg_ssim2_ref_create(jpxlg_ctx* ctx, const float* rgb, int w, int h, uint3
     }
     dims[s][0] = cw;
     dims[s][1] = ch;
-    total += 9 * (size_t)cw * ch + 3 * (size_t)cw * ch;  // xyb, mu, s11 + rgb level
+    *total += 9 * (size_t)cw * ch + 3 * (size_t)cw * ch;
     ++ns;
   }
+  return ns;
+}
+
+int ref_check(jpxlg_ctx* ctx, int w, int h) {
+  if (w < 8 || h < 8) return fail(ctx, JPXLG_ERR_TOO_SMALL, "SSIMULACRA2 needs at least 8x8");
+  if (w > kBlurMaxWidth)
+    return fail(ctx, JPXLG_ERR_ARGUMENT, "SSIMULACRA2 frames are limited to %d columns",
+                kBlurMaxWidth);
+  return JPXLG_OK;
+}
+
+// Fills R (w, h, device set) in `block` (ref_layout's floats): the pyramid,
+// positive XYB and the blurred moments of every scale.
+int ref_fill(jpxlg_ctx* ctx, jpxlg_ref* R, void* block, const float* rgb, uint32_t mem) {
+  int dims[6][2];
+  size_t total;
+  const int w = R->w, h = R->h;
+  const int ns = ref_layout(w, h, dims, &total);
   R->nscales = ns;
-  CK(cudaMalloc(&R->block, total * sizeof(float)));
-  float* cursor = (float*)R->block;
+  R->block = block;
+  float* cursor = (float*)block;
   const size_t n0 = (size_t)w * h;
   CK(ctx->hpl.ensure(9 * n0 * sizeof(float)));
   CK(ctx->bcarry.ensure(blur_carry_floats(w, h) * sizeof(float)));
@@ -1070,17 +1079,33 @@ int jpxlg_ssim2_ref_create(jpxlg_ctx* ctx, const float* rgb, int w, int h, uint3
                        sc.h, ctx->d_words, ctx->stream);
     k += 1 + 2;
   }
-  int rc = after_launch(ctx, k);
+  return after_launch(ctx, k);
+}
+
+}  // namespace
+
+int jpxlg_ssim2_ref_create(jpxlg_ctx* ctx, const float* rgb, int w, int h, uint32_t mem,
+                           jpxlg_ref** out) {
+  if (!ctx || !rgb || !out) return fail(ctx, JPXLG_ERR_ARGUMENT, "null argument");
+  *out = nullptr;
+  int rc = ref_check(ctx, w, h);
+  if (rc) return rc;
+  cudaSetDevice(ctx->device);
+  std::unique_ptr<jpxlg_ref> R(new jpxlg_ref);
+  R->ctx = ctx;
+  R->device = ctx->device;
+  R->w = w;
+  R->h = h;
+  int dims[6][2];
+  size_t total;
+  ref_layout(w, h, dims, &total);
+  void* block = nullptr;
+  CK(cudaMalloc(&block, total * sizeof(float)));
+  rc = ref_fill(ctx, R.get(), block, rgb, mem);
+  if (rc == JPXLG_OK && mem == JPXLG_MEM_HOST) rc = sync_and_check(ctx);
   if (rc) {
-    cudaFree(R->block);
+    cudaFree(block);
     return rc;
-  }
-  if (mem == JPXLG_MEM_HOST) {
-    rc = sync_and_check(ctx);
-    if (rc) {
-      cudaFree(R->block);
-      return rc;
-    }
   }
   *out = R.release();
   return JPXLG_OK;
@@ -1136,12 +1161,26 @@ int jpxlg_ssim2_score(jpxlg_ctx* ctx, const jpxlg_ref* R, const float* rgb, uint
 
 int jpxlg_score_pair(jpxlg_ctx* ctx, const float* ref_rgb, const float* cand_rgb, int w, int h,
                      uint32_t mem, double* score) {
-  jpxlg_ref* R = nullptr;
-  int rc = jpxlg_ssim2_ref_create(ctx, ref_rgb, w, h, mem, &R);
+  if (!ctx || !ref_rgb || !cand_rgb || !score)
+    return fail(ctx, JPXLG_ERR_ARGUMENT, "null argument");
+  int rc = ref_check(ctx, w, h);
   if (rc) return rc;
-  rc = jpxlg_ssim2_score(ctx, R, cand_rgb, mem, score, nullptr, nullptr);
+  cudaSetDevice(ctx->device);
+  // The reference side in the context's own buffer, kept for the next call
+  // (no allocation or free per pair).
+  jpxlg_ref R;
+  R.ctx = ctx;
+  R.device = ctx->device;
+  R.w = w;
+  R.h = h;
+  int dims[6][2];
+  size_t total;
+  ref_layout(w, h, dims, &total);
+  CK(ctx->pair_ref.ensure(total * sizeof(float)));
+  rc = ref_fill(ctx, &R, ctx->pair_ref.p, ref_rgb, mem);
+  if (rc) return rc;
+  rc = jpxlg_ssim2_score(ctx, &R, cand_rgb, mem, score, nullptr, nullptr);
   if (mem == JPXLG_MEM_DEVICE && rc == JPXLG_OK) rc = sync_and_check(ctx);
-  jpxlg_ssim2_ref_destroy(R);
   return rc;
 }
 
