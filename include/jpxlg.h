@@ -244,7 +244,9 @@ int jpxlg_ssim2_ref_destroy(jpxlg_ref* ref);
  * follow mem like the planes (device pointers with JPXLG_MEM_DEVICE). */
 int jpxlg_ssim2_score(jpxlg_ctx* ctx, const jpxlg_ref* ref, const float* linear_rgb,
                       uint32_t mem, double* score, double* raw_error, double* terms);
-/* One-shot pair score (reference moments are built and dropped). */
+/* One-shot pair score.  The reference side is built in a device buffer the
+ * context keeps for the next call (its pyramid: about 16 bytes per source
+ * pixel), freed with the context. */
 int jpxlg_score_pair(jpxlg_ctx* ctx, const float* ref_rgb, const float* cand_rgb, int width,
                      int height, uint32_t mem, double* score);
 
