@@ -245,7 +245,7 @@ int jpxlg_ssim2_ref_destroy(jpxlg_ref* ref);
 int jpxlg_ssim2_score(jpxlg_ctx* ctx, const jpxlg_ref* ref, const float* linear_rgb,
                       uint32_t mem, double* score, double* raw_error, double* terms);
 /* One-shot pair score.  The reference side is built in a device buffer the
- * context keeps for the next call (its pyramid: about 16 bytes per source
+ * context keeps for the next call (its pyramid: about 64 bytes per source
  * pixel), freed with the context. */
 int jpxlg_score_pair(jpxlg_ctx* ctx, const float* ref_rgb, const float* cand_rgb, int width,
                      int height, uint32_t mem, double* score);
