@@ -418,7 +418,9 @@ int jpxlg_codestream_render(jpxlg_ctx* ctx, const jpxlg_codestream* cs, int out_
  * graph launch.  jpxlg_decode_batch_create stages every opened stream
  * (the host's entropy decoding is done at open; here the coefficient image,
  * LF planes and CfL tiles go into pinned host memory), spreads the streams
- * over `lanes` internal contexts (0 picks min(n, 4)), renders each once to
+ * over `lanes` internal contexts (0 picks up to 32, fewer when the frames
+ * are large: each lane keeps a workspace of about 64 bytes per pixel of its
+ * largest frame, held to 16 GiB in all), renders each once to
  * size the workspaces, and captures one CUDA graph on ctx's stream: per
  * stream, the staged planes to the device, LF preparation, the render into
  * `out_kind` (as jpxlg_codestream_render) and the pixels back to a pinned
