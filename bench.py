@@ -640,8 +640,8 @@ def run_decode(ctx, reps, np):
     the FP32 IDCTs and with the split-precision ones (square varblocks on the
     tensor cores).  The host parses every stream (headers, TOC,
     entropy-coded sections) at open; each graph launch copies the staged
-    coefficients in, renders all 256 frames over four lanes and copies the
-    8-bit pixels back to pinned host memory.  `value` is end to end: parse
+    coefficients in, renders all 256 frames over the default lanes (up to
+    32) and copies the 8-bit pixels back to pinned host memory.  `value` is end to end: parse
     of all streams plus one FP32 graph run, per second.  Against djxl's
     decodes (the .npy beside 11 of the 13 fixtures, quantized as
     quantize_sample does) the samples 1 DN off are counted per mode.  The
